@@ -1,0 +1,979 @@
+/*
+ * fvc_capi.cu - host side of the renderer behind the C ABI of include/fvc.h.
+ *
+ * Owns the model (nerfacc export loader, src/loader.cu:232-300), the
+ * renderers (PerformanceRenderer / CachePerformanceRenderer, their
+ * resizeRenderbuffers and render), the frustum caches (Cache, CacheRenderer::
+ * resizeCache / initCacheBlockwise / swapCache) and their device memory.
+ * No exception crosses the ABI: every entry point returns a status and
+ * records a thread-local message.
+ */
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstddef>
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/fvc.h"
+#include "fvc_kernels.h"
+
+using namespace fvc;
+
+/* The ABI structs have the byte layout of the reference's structs
+ * (include/common.h, include/renderer_common.h), measured from those headers. */
+static_assert(sizeof(fvc_scene_info) == 76 && offsetof(fvc_scene_info, aabb_from) == 16 &&
+              offsetof(fvc_scene_info, contraction_aabb_from) == 40 && offsetof(fvc_scene_info, contraction_type) == 64 &&
+              offsetof(fvc_scene_info, is_open_gl) == 68 && offsetof(fvc_scene_info, alpha_thre) == 72, "SceneInfo layout");
+static_assert(sizeof(fvc_stepsize_info) == 48, "StepsizeInfo layout");
+static_assert(sizeof(fvc_camera_info) == 144 && offsetof(fvc_camera_info, is_open_gl) == 8 && offsetof(fvc_camera_info, focal) == 16 &&
+              offsetof(fvc_camera_info, principal) == 24 && offsetof(fvc_camera_info, cam2world) == 32 &&
+              offsetof(fvc_camera_info, world2cam) == 80 && offsetof(fvc_camera_info, aperature) == 128 &&
+              offsetof(fvc_camera_info, focus_z) == 132, "CameraInfo layout");
+static_assert(sizeof(fvc_raymarch_info) == 352 && offsetof(fvc_raymarch_info, next_cam_info) == 144 &&
+              offsetof(fvc_raymarch_info, stepsize_info) == 288 && offsetof(fvc_raymarch_info, sample_index) == 336 &&
+              offsetof(fvc_raymarch_info, motion_blur) == 340 && offsetof(fvc_raymarch_info, deterministic) == 341, "RaymarchInfo layout");
+static_assert(sizeof(fvc_ray_result) == 16 && sizeof(fvc_camera_matrix) == 48, "BaseRayResult / CameraMatrix layout");
+
+/* ------------------------------------------------------------------------ */
+/* errors                                                                    */
+/* ------------------------------------------------------------------------ */
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? FVC_ERR_OOM : FVC_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    } while (0)
+
+#define CHECK_ARG(cond, msg) \
+    do {                     \
+        if (!(cond)) return fail(FVC_ERR_ARG, msg); \
+    } while (0)
+
+extern "C" const char *fvc_last_error(void) { return g_err.c_str(); }
+extern "C" const char *fvc_version(void) { return "fvc-gb300 0.1 (sm_103a)"; }
+
+/* ------------------------------------------------------------------------ */
+/* minimal JSON reader (objects, arrays, numbers, strings, bools, null)      */
+/* ------------------------------------------------------------------------ */
+namespace {
+struct JVal {
+    enum Kind { NUL, BOOL, NUM, STR, ARR, OBJ } kind = NUL;
+    double num = 0;
+    bool b = false;
+    std::string str;
+    std::vector<JVal> arr;
+    std::map<std::string, JVal> obj;
+    bool has(const std::string &k) const { return kind == OBJ && obj.count(k); }
+    const JVal &operator[](const std::string &k) const
+    {
+        static JVal none;
+        auto it = obj.find(k);
+        return it == obj.end() ? none : it->second;
+    }
+    double num_or(const std::string &k, double d) const { return has(k) && (*this)[k].kind == NUM ? (*this)[k].num : d; }
+    bool bool_or(const std::string &k, bool d) const { return has(k) && (*this)[k].kind == BOOL ? (*this)[k].b : d; }
+};
+
+struct JParser {
+    const char *p, *e;
+    bool ok = true;
+    void ws() { while (p < e && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p; }
+    JVal parse()
+    {
+        ws();
+        JVal v;
+        if (p >= e) { ok = false; return v; }
+        if (*p == '{') {
+            ++p; v.kind = JVal::OBJ; ws();
+            if (p < e && *p == '}') { ++p; return v; }
+            while (ok) {
+                ws();
+                JVal k = parse();
+                if (k.kind != JVal::STR) { ok = false; break; }
+                ws();
+                if (p >= e || *p != ':') { ok = false; break; }
+                ++p;
+                v.obj[k.str] = parse();
+                ws();
+                if (p < e && *p == ',') { ++p; continue; }
+                if (p < e && *p == '}') { ++p; break; }
+                ok = false;
+            }
+        } else if (*p == '[') {
+            ++p; v.kind = JVal::ARR; ws();
+            if (p < e && *p == ']') { ++p; return v; }
+            while (ok) {
+                v.arr.push_back(parse());
+                ws();
+                if (p < e && *p == ',') { ++p; continue; }
+                if (p < e && *p == ']') { ++p; break; }
+                ok = false;
+            }
+        } else if (*p == '"') {
+            ++p; v.kind = JVal::STR;
+            while (p < e && *p != '"') {
+                if (*p == '\\' && p + 1 < e) { ++p; v.str.push_back(*p == 'n' ? '\n' : *p); ++p; }
+                else v.str.push_back(*p++);
+            }
+            if (p < e) ++p; else ok = false;
+        } else if (!strncmp(p, "true", 4)) { p += 4; v.kind = JVal::BOOL; v.b = true; }
+        else if (!strncmp(p, "false", 5)) { p += 5; v.kind = JVal::BOOL; v.b = false; }
+        else if (!strncmp(p, "null", 4)) { p += 4; }
+        else {
+            char *end = nullptr;
+            v.num = strtod(p, &end);
+            if (end == p) { ok = false; return v; }
+            v.kind = JVal::NUM; p = end;
+        }
+        return v;
+    }
+};
+
+bool read_file(const std::string &path, std::vector<char> &out)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    f.seekg(0, std::ios::end);
+    out.resize((size_t)f.tellg());
+    f.seekg(0);
+    f.read(out.data(), (std::streamsize)out.size());
+    return (bool)f;
+}
+
+/* fp16 bits -> float (exact) */
+float h2f(uint16_t h)
+{
+    const int s = h >> 15, ex = (h >> 10) & 31, m = h & 1023;
+    float v;
+    if (ex == 0) v = std::ldexp((float)m, -24);
+    else if (ex == 31) v = m ? NAN : INFINITY;
+    else v = std::ldexp((float)(m | 1024), ex - 25);
+    return s ? -v : v;
+}
+
+/* Pack a row-major [N x K] fp16 matrix into mma.m16n8k16 B fragments:
+ * for n-tile j, k-step s, lane (g = lane/4, t = lane%4):
+ * b0 = (W[8j+g][16s+2t], W[8j+g][16s+2t+1]), b1 = (.. 16s+2t+8, +9). */
+void frag_pack(const std::vector<uint16_t> &W, int N, int K, uint2 *out)
+{
+    const int KS = K / 16;
+    for (int j = 0; j < N / 8; ++j)
+        for (int s = 0; s < KS; ++s)
+            for (int lane = 0; lane < 32; ++lane) {
+                const int g = lane >> 2, t = lane & 3, n = 8 * j + g, k = 16 * s + 2 * t;
+                uint2 b;
+                b.x = (uint32_t)W[(size_t)n * K + k] | ((uint32_t)W[(size_t)n * K + k + 1] << 16);
+                b.y = (uint32_t)W[(size_t)n * K + k + 8] | ((uint32_t)W[(size_t)n * K + k + 9] << 16);
+                out[(j * KS + s) * 32 + lane] = b;
+            }
+}
+
+/* StepsizeInfo::setAdditionalInfo, include/common.h:109-131 (host double),
+ * plus the low part of log(1+cone) for fvc_pow_1pc. */
+void setup_steps(const fvc_scene_info &sc, fvc_stepsize_info &s)
+{
+    const float R = 128.0f;
+    s.dt_min = s.stepsize;
+    s.dt_max = fmaxf(fmaxf((sc.aabb_to.x - sc.aabb_from.x) / R * 1.732f, (sc.aabb_to.y - sc.aabb_from.y) / R * 1.732f),
+                     (sc.aabb_to.z - sc.aabb_from.z) / R * 1.732f);
+    s.t_min = ((double)s.dt_min) / s.cone_angle;
+    const double d_i_min = 1.0 / s.cone_angle;
+    s.i_min = d_i_min;
+    const double d_log1p_c = std::log(1.0 + s.cone_angle);
+    s.log1p_c = d_log1p_c;
+    const double d_i_max = std::log(s.dt_max / (double)s.dt_min) / d_log1p_c + d_i_min;
+    s.i_max = d_i_max;
+    s.t_max = s.t_min * std::pow(1.0 + s.cone_angle, d_i_max - d_i_min);
+    /* near_i = step_from_t(near) */
+    const float t = s.near_;
+    if (s.cone_angle <= 0.0f) s.near_i = t / s.dt_min;
+    else if (t >= s.t_max) s.near_i = (t - s.t_max) / s.dt_max + s.i_max;
+    else if (t < s.t_min) s.near_i = t / s.dt_min;
+    else s.near_i = fvc_logf(t / s.t_min) / s.log1p_c + s.i_min;
+}
+
+DevSteps dev_steps(const fvc_stepsize_info &s)
+{
+    DevSteps d;
+    d.cone = s.cone_angle; d.log1p_c = s.log1p_c;
+    const double L = std::log(1.0 + (double)s.cone_angle);
+    d.log1p_c_lo = (float)(L - (double)s.log1p_c);
+    d.near_ = s.near_; d.near_i = s.near_i; d.far_ = s.far_;
+    d.dt_min = s.dt_min; d.dt_max = s.dt_max; d.t_min = s.t_min; d.t_max = s.t_max; d.i_min = s.i_min; d.i_max = s.i_max;
+    return d;
+}
+
+DevCam dev_cam(const fvc_camera_info &c)
+{
+    DevCam d;
+    d.W = c.resolution.x; d.H = c.resolution.y; d.gl = c.is_open_gl ? 1 : 0;
+    d.fx = c.focal.x; d.fy = c.focal.y; d.px = c.principal.x; d.py = c.principal.y;
+    const fvc_float4 *m = &c.cam2world.m0, *w = &c.world2cam.m0;
+    for (int r = 0; r < 3; ++r) {
+        d.c2w[4 * r] = m[r].x; d.c2w[4 * r + 1] = m[r].y; d.c2w[4 * r + 2] = m[r].z; d.c2w[4 * r + 3] = m[r].w;
+        d.w2c[4 * r] = w[r].x; d.w2c[4 * r + 1] = w[r].y; d.w2c[4 * r + 2] = w[r].z; d.w2c[4 * r + 3] = w[r].w;
+    }
+    return d;
+}
+
+template <class T>
+int dalloc(T **p, size_t n, const char *what)
+{
+    *p = nullptr;
+    if (n == 0) return FVC_OK;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(FVC_ERR_OOM, std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    }
+    return FVC_OK;
+}
+template <class T>
+void dfree(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+}  // namespace
+
+/* ------------------------------------------------------------------------ */
+/* handles                                                                   */
+/* ------------------------------------------------------------------------ */
+struct fvc_model {
+    int device = 0, n_sms = 0;
+    fvc_scene_info scene{};
+    fvc_stepsize_info steps{};
+    DevScene dscene{};
+    DevGrid grid{};
+    int latent_offset = 1, n_latents = 8, head_hidden = 2;
+    uint8_t *d_bits = nullptr;
+    __half2 *d_table = nullptr;
+    uint2 *d_weights = nullptr;
+    float *d_bias3 = nullptr;
+    size_t table_entries = 0;
+    ~fvc_model()
+    {
+        dfree(d_bits); dfree(d_table); dfree(d_weights); dfree(d_bias3);
+    }
+};
+
+struct fvc_cache {
+    bool initialized = false;
+    int fW = 0, fH = 0, fD = 0, bX = 0, bY = 0, bZ = 0, dX = 0, dY = 0, dZ = 0;
+    int32_t *d_packed = nullptr;
+    float *d_known = nullptr;
+    void *d_voxels = nullptr;
+    fvc_raymarch_info rm_info{};
+    bool built = false;
+    fvc_cache_stats_t stats{};
+    ~fvc_cache()
+    {
+        dfree(d_packed); dfree(d_known);
+        if (d_voxels) cudaFree(d_voxels);
+    }
+    int capacity() const { return dX * dY * dZ; }
+    CacheView view() const
+    {
+        CacheView v;
+        v.packed_index = d_packed; v.known_ranges = d_known; v.voxels = d_voxels;
+        v.fW = fW; v.fH = fH; v.fD = fD; v.bX = bX; v.bY = bY; v.bZ = bZ; v.dX = dX; v.dY = dY; v.dZ = dZ;
+        v.n_valid_slots = std::min(stats.n_bricks_demanded, capacity());
+        return v;
+    }
+};
+
+struct BuildScratch {
+    int n_tiles = 0;
+    CacheRay *rays = nullptr;
+    int *block_step = nullptr;
+    uint8_t *tile_alive = nullptr;
+    int *alive_a = nullptr, *alive_b = nullptr;
+    int *counters = nullptr;  /* n_alive_a, n_alive_b, slot_counter, n_jobs, guard */
+    int *tile_n_samples = nullptr;
+    uint8_t *tile_processed = nullptr, *tile_need = nullptr;
+    int *tile_n_alive = nullptr;
+    void *staging = nullptr;
+    int *jobs = nullptr;
+    void release()
+    {
+        dfree(rays); dfree(block_step); dfree(tile_alive); dfree(alive_a); dfree(alive_b); dfree(counters);
+        dfree(tile_n_samples); dfree(tile_processed); dfree(tile_need); dfree(tile_n_alive); dfree(jobs);
+        if (staging) cudaFree(staging);
+        staging = nullptr;
+        n_tiles = 0;
+    }
+};
+
+struct fvc_renderer {
+    fvc_model *m = nullptr;
+    int kind = FVC_RENDERER_PERFORMANCE;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t low_prio = nullptr;
+    int W = 0, H = 0;
+    int *d_ctl = nullptr;             /* [0] ray counter, [1] guard */
+    RenderStatsDev *d_stats = nullptr;
+    float4 *d_results = nullptr;
+    uchar4 *d_image = nullptr;
+    int4 *d_counts = nullptr;
+    int *h_pinned = nullptr;          /* readback of build counters */
+    fvc_cache *cache = nullptr, *next = nullptr;
+    fvc_cache_settings settings{0, 0, 1, 1, 1, 1};
+    int render_mode = 0;
+    int max_samples = 0;
+    BuildScratch bs;
+    std::mutex read_mutex, write_mutex;
+    ~fvc_renderer()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        dfree(d_ctl); dfree(d_stats); dfree(d_results); dfree(d_image); dfree(d_counts);
+        bs.release();
+        if (h_pinned) cudaFreeHost(h_pinned);
+        if (own_stream) cudaStreamDestroy(own_stream);
+        if (low_prio) cudaStreamDestroy(low_prio);
+    }
+};
+
+/* ------------------------------------------------------------------------ */
+/* model loading                                                             */
+/* ------------------------------------------------------------------------ */
+static int load_model(const std::string &dir, fvc_model &m)
+{
+    std::vector<char> txt;
+    if (!read_file(dir + "/config.json", txt)) return fail(FVC_ERR_IO, "Could not load config file: " + dir + "/config.json");
+    JParser jp{txt.data(), txt.data() + txt.size()};
+    JVal cfg = jp.parse();
+    if (!jp.ok || cfg.kind != JVal::OBJ) return fail(FVC_ERR_CONFIG, "config.json: parse error");
+    const JVal &sc = cfg["scene"];
+    if (sc.kind != JVal::OBJ) return fail(FVC_ERR_CONFIG, "config.json: missing scene");
+    /* parse(SceneInfo&), include/parse_helper.h:25-54 */
+    fvc_scene_info &s = m.scene;
+    s.grid_resolution = (int)sc.num_or("grid_resolution", 0);
+    s.grid_nlvl = (int)sc.num_or("grid_nlvl", 0);
+    s.vals_per_lvl = s.grid_resolution * s.grid_resolution * s.grid_resolution;
+    s.normalized = 0;
+    if (s.grid_resolution != 128) return fail(FVC_ERR_CONFIG, "Performance Renderer only supports fixed grid resolution!");
+    if (s.grid_nlvl < 1 || s.grid_nlvl > 8) return fail(FVC_ERR_CONFIG, "grid_nlvl out of range");
+    const JVal &ab = sc["aabb"];
+    if (ab.kind != JVal::ARR || ab.arr.size() != 6) return fail(FVC_ERR_CONFIG, "scene.aabb needs 6 values");
+    s.aabb_from = {(float)ab.arr[0].num, (float)ab.arr[1].num, (float)ab.arr[2].num};
+    s.aabb_to = {(float)ab.arr[3].num, (float)ab.arr[4].num, (float)ab.arr[5].num};
+    if (sc.has("contraction") && sc["contraction"].has("aabb")) {
+        const JVal &ca = sc["contraction"]["aabb"];
+        if (ca.kind != JVal::ARR || ca.arr.size() != 6) return fail(FVC_ERR_CONFIG, "contraction.aabb needs 6 values");
+        s.contraction_type = FVC_CONTRACTION_WARP_AABB_LINF;
+        s.contraction_aabb_from = {(float)ca.arr[0].num, (float)ca.arr[1].num, (float)ca.arr[2].num};
+        s.contraction_aabb_to = {(float)ca.arr[3].num, (float)ca.arr[4].num, (float)ca.arr[5].num};
+    } else {
+        s.contraction_type = FVC_CONTRACTION_AABB;
+    }
+    s.is_open_gl = sc.bool_or("is_open_gl", false);
+    s.alpha_thre = (float)sc.num_or("alpha_thre", 0.0);
+    /* parse(StepsizeInfo&), :57-63 */
+    fvc_stepsize_info &st = m.steps;
+    st.cone_angle = (float)sc.num_or("cone_angle", 0.0);
+    st.stepsize = (float)sc.num_or("stepsize", 0.0);
+    st.near_ = (float)sc.num_or("near", 0.0);
+    st.far_ = (float)sc.num_or("far", 1e10);
+    if (!(st.stepsize > 0.0f)) return fail(FVC_ERR_CONFIG, "scene.stepsize must be > 0");
+    setup_steps(s, st);
+
+    /* network */
+    const JVal &base = cfg["mlp_base"], &head = cfg["mlp_head"];
+    const JVal &enc = base["encoding"];
+    const int n_levels = (int)enc.num_or("n_levels", 16), F = (int)enc.num_or("n_features_per_level", 2);
+    const int log2T = (int)enc.num_or("log2_hashmap_size", 19), N0 = (int)enc.num_or("base_resolution", 16);
+    const float b = (float)enc.num_or("per_level_scale", 2.0);
+    if (n_levels != 16 || F != 2) return fail(FVC_ERR_CONFIG, "only the 16-level, 2-feature hash grid is built");
+    if (log2T < 4 || log2T > 24) return fail(FVC_ERR_CONFIG, "log2_hashmap_size out of range");
+    const int width = (int)base["network"].num_or("n_neurons", 64);
+    if (width != 64 || (int)base["network"].num_or("n_hidden_layers", 1) != 1)
+        return fail(FVC_ERR_CONFIG, "density network must be 32 -> 64 -> out (1 hidden layer of 64)");
+    const int n_out = (int)base.num_or("n_output", 16);
+    if (n_out < 1 || n_out > 16) return fail(FVC_ERR_CONFIG, "mlp_base.n_output must be 1..16");
+    const bool first_lat_dens = head.bool_or("first_latent_is_density", true);
+    m.latent_offset = first_lat_dens ? 0 : 1;
+    m.n_latents = (int)head.num_or("n_latents", n_out);
+    const int head_in = (int)head.num_or("n_input", 16 + m.n_latents);
+    const int head_in_pad = (head_in + 15) / 16 * 16;
+    m.head_hidden = (int)head["network"].num_or("n_hidden_layers", 2);
+    if ((int)head["network"].num_or("n_neurons", 64) != 64) return fail(FVC_ERR_CONFIG, "head width must be 64");
+    if (m.head_hidden < 1 || m.head_hidden > 2) return fail(FVC_ERR_CONFIG, "head must have 1 or 2 hidden layers");
+    if (m.latent_offset + m.n_latents > 16 || head_in != m.n_latents + 16 || head_in_pad != 32)
+        return fail(FVC_ERR_CONFIG, "head input must be n_latents + 16 SH values padded to 32");
+    const JVal &nested = head["encoding"]["nested"];
+    if (nested.kind == JVal::ARR && nested.arr.size() && (int)nested.arr[0].num_or("degree", 4) != 4)
+        return fail(FVC_ERR_CONFIG, "only SH degree 4 direction encoding is built");
+
+    /* hash-grid levels: scale = N0 * b^l - 1 (float), res = ceil(scale)+1,
+     * size = min(round_up(res^3, 8), 2^log2T); explicit fvc_level_scales wins */
+    DevGrid &g = m.grid;
+    g.n_levels = n_levels;
+    g.dense_mask = 0;
+    const JVal &ls = enc["fvc_level_scales"];
+    const float log2b = std::log2(b);
+    uint32_t off = 0;
+    for (int l = 0; l < n_levels; ++l) {
+        float scale = std::exp2((float)l * log2b) * (float)N0 - 1.0f;
+        if (ls.kind == JVal::ARR && (int)ls.arr.size() == n_levels) scale = (float)ls.arr[l].num;
+        const uint32_t res = (uint32_t)std::ceil(scale) + 1u;
+        uint64_t n = (uint64_t)res * res * res;
+        n = (n + 7) / 8 * 8;
+        const uint32_t size = (uint32_t)std::min<uint64_t>(n, 1ull << log2T);
+        g.scale[l] = scale; g.res[l] = res; g.res2[l] = res * res; g.size[l] = size; g.offset[l] = off;
+        if ((uint64_t)res * res * res <= size) g.dense_mask |= 1u << l;
+        off += size;
+    }
+    m.table_entries = off;
+    std::vector<char> tab, wb, wh, occ;
+    if (!read_file(dir + "/pos_enc.dat", tab)) return fail(FVC_ERR_IO, "missing pos_enc.dat");
+    if (tab.size() != (size_t)off * F * 2)
+        return fail(FVC_ERR_IO, "pos_enc.dat: " + std::to_string(tab.size()) + " bytes, hash grid needs " + std::to_string((size_t)off * F * 2));
+    if (!read_file(dir + "/mlp_base.dat", wb)) return fail(FVC_ERR_IO, "missing mlp_base.dat");
+    const int base_out_pad = (n_out + 15) / 16 * 16;
+    if (wb.size() != (size_t)(64 * 32 + base_out_pad * 64) * 2) return fail(FVC_ERR_IO, "mlp_base.dat has the wrong size");
+    if (!read_file(dir + "/mlp_head.dat", wh)) return fail(FVC_ERR_IO, "missing mlp_head.dat");
+    if (wh.size() != (size_t)(64 * 32 + (m.head_hidden - 1) * 64 * 64 + 16 * 64) * 2) return fail(FVC_ERR_IO, "mlp_head.dat has the wrong size");
+    if (!read_file(dir + "/occupancy_grid.dat", occ)) return fail(FVC_ERR_IO, "missing occupancy_grid.dat");
+    const size_t vals = (size_t)128 * 128 * 128;
+    if (occ.size() != vals * s.grid_nlvl) return fail(FVC_ERR_IO, "occupancy_grid.dat has the wrong size");
+
+    /* Morton bitfield: occupancy_grid_to_morton_kernel + uchar_to_bitfield
+     * (src/loader.cu:20-55) on the host */
+    std::vector<uint8_t> bits(vals * s.grid_nlvl / 8, 0);
+    auto compact = [](uint32_t x) {
+        x &= 0x49249249u; x = (x | (x >> 2)) & 0xc30c30c3u; x = (x | (x >> 4)) & 0x0f00f00fu;
+        x = (x | (x >> 8)) & 0xff0000ffu; x = (x | (x >> 16)) & 0x0000ffffu; return x;
+    };
+    for (size_t i = 0; i < vals * s.grid_nlvl; ++i) {
+        const size_t lvl = i / vals;
+        const uint32_t j = (uint32_t)(i % vals);
+        const uint32_t x = compact(j), y = compact(j >> 1), z = compact(j >> 2);
+        if (occ[lvl * vals + (size_t)x * 16384 + y * 128 + z]) bits[i / 8] |= (uint8_t)(1u << (i % 8));
+    }
+
+    /* weights -> fragment order */
+    auto u16 = [](const std::vector<char> &v, size_t off_h, size_t n) {
+        std::vector<uint16_t> o(n);
+        memcpy(o.data(), v.data() + off_h * 2, n * 2);
+        return o;
+    };
+    std::vector<uint2> W(W_TOTAL, make_uint2(0, 0));
+    frag_pack(u16(wb, 0, 64 * 32), 64, 32, &W[W_L1]);
+    {
+        std::vector<uint16_t> w2 = u16(wb, 64 * 32, (size_t)base_out_pad * 64);
+        w2.resize(16 * 64, 0);
+        frag_pack(w2, 16, 64, &W[W_L2]);
+    }
+    std::vector<uint16_t> h0 = u16(wh, 0, 64 * 32);
+    std::vector<uint16_t> l3(64 * 32, 0);
+    std::vector<float> bias3(64, 0.f);
+    for (int n = 0; n < 64; ++n) {
+        for (int k = 0; k < 16; ++k) {
+            const int src = k - m.latent_offset;
+            if (src >= 0 && src < m.n_latents) l3[n * 32 + k] = h0[n * 32 + src];
+        }
+        for (int j = 0; j < 16; ++j) l3[n * 32 + 16 + j] = h0[n * 32 + m.n_latents + j];
+        double acc = 0.0;  /* inputs padded with 1.0 (include/nerf_network.h:248-253) */
+        for (int k = head_in; k < head_in_pad; ++k) acc += h2f(h0[n * 32 + k]);
+        bias3[n] = (float)acc;
+    }
+    frag_pack(l3, 64, 32, &W[W_L3]);
+    size_t ho = 64 * 32;
+    if (m.head_hidden == 2) {
+        frag_pack(u16(wh, ho, 64 * 64), 64, 64, &W[W_L4]);
+        ho += 64 * 64;
+    }
+    frag_pack(u16(wh, ho, 16 * 64), 16, 64, &W[W_L5]);
+
+    /* device scene block */
+    DevScene &d = m.dscene;
+    d.aabb_from = make_float3(s.aabb_from.x, s.aabb_from.y, s.aabb_from.z);
+    d.aabb_to = make_float3(s.aabb_to.x, s.aabb_to.y, s.aabb_to.z);
+    const float sc2 = (float)(1 << (s.grid_nlvl - 1));
+    d.unit_off = make_float3(s.aabb_from.x / sc2, s.aabb_from.y / sc2, s.aabb_from.z / sc2);
+    d.unit_den = make_float3((s.aabb_to.x - s.aabb_from.x) / sc2, (s.aabb_to.y - s.aabb_from.y) / sc2, (s.aabb_to.z - s.aabb_from.z) / sc2);
+    d.aabb_den = make_float3(s.aabb_to.x - s.aabb_from.x, s.aabb_to.y - s.aabb_from.y, s.aabb_to.z - s.aabb_from.z);
+    d.c_from = make_float3(s.contraction_aabb_from.x, s.contraction_aabb_from.y, s.contraction_aabb_from.z);
+    d.c_den = make_float3(s.contraction_aabb_to.x - s.contraction_aabb_from.x, s.contraction_aabb_to.y - s.contraction_aabb_from.y,
+                          s.contraction_aabb_to.z - s.contraction_aabb_from.z);
+    d.nlvl = s.grid_nlvl; d.normalized = s.normalized; d.contraction = s.contraction_type; d.is_open_gl = s.is_open_gl;
+    d.alpha_thre = s.alpha_thre;
+
+    CU(cudaGetDevice(&m.device));
+    CU(cudaDeviceGetAttribute(&m.n_sms, cudaDevAttrMultiProcessorCount, m.device));
+    int rc;
+    if ((rc = dalloc(&m.d_bits, bits.size(), "occupancy bits"))) return rc;
+    if ((rc = dalloc(&m.d_table, (size_t)off, "hash tables"))) return rc;
+    if ((rc = dalloc(&m.d_weights, (size_t)W_TOTAL, "weights"))) return rc;
+    if ((rc = dalloc(&m.d_bias3, (size_t)64, "bias"))) return rc;
+    CU(cudaMemcpy(m.d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(m.d_table, tab.data(), tab.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(m.d_weights, W.data(), W.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(m.d_bias3, bias3.data(), 64 * sizeof(float), cudaMemcpyHostToDevice));
+    return FVC_OK;
+}
+
+extern "C" int fvc_model_load(const char *data_dir, fvc_model **out)
+{
+    CHECK_ARG(data_dir && out, "fvc_model_load: null argument");
+    *out = nullptr;
+    auto m = std::make_unique<fvc_model>();
+    const int rc = load_model(data_dir, *m);
+    if (rc) return rc;
+    *out = m.release();
+    return FVC_OK;
+}
+
+extern "C" void fvc_model_destroy(fvc_model *m) { delete m; }
+
+extern "C" int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_stepsize_info *steps)
+{
+    CHECK_ARG(m, "fvc_model_info: null model");
+    if (scene) *scene = m->scene;
+    if (steps) *steps = m->steps;
+    return FVC_OK;
+}
+
+static int run_inference(fvc_model *m, const float *pos, const float *dir, int n, float *out4, float *base_out, float *features)
+{
+    CHECK_ARG(m && pos && n >= 0, "inference: bad arguments");
+    if (n == 0) return FVC_OK;
+    float *dp = nullptr, *dd = nullptr, *d4 = nullptr, *db = nullptr, *df = nullptr;
+    int rc = FVC_OK;
+    struct Guard {
+        float **p[5];
+        ~Guard() { for (auto q : p) dfree(*q); }
+    } guard{{&dp, &dd, &d4, &db, &df}};
+    if ((rc = dalloc(&dp, (size_t)3 * n, "inference input"))) return rc;
+    if (dir && (rc = dalloc(&dd, (size_t)3 * n, "inference dir"))) return rc;
+    if (out4 && (rc = dalloc(&d4, (size_t)4 * n, "inference out"))) return rc;
+    if (base_out && (rc = dalloc(&db, (size_t)16 * n, "inference base"))) return rc;
+    if (features && (rc = dalloc(&df, (size_t)32 * n, "inference features"))) return rc;
+    CU(cudaMemcpy(dp, pos, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    if (dir) CU(cudaMemcpy(dd, dir, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    InferenceParams p;
+    p.grid = m->grid; p.table = m->d_table; p.weights = m->d_weights; p.bias3 = m->d_bias3;
+    p.pos = dp; p.dir = dd; p.n = n; p.out4 = d4; p.base_out = db; p.features = df;
+    CU(launch_inference(p, m->head_hidden, m->n_sms, 0));
+    CU(cudaDeviceSynchronize());
+    if (out4) CU(cudaMemcpy(out4, d4, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost));
+    if (base_out) CU(cudaMemcpy(base_out, db, sizeof(float) * 16 * n, cudaMemcpyDeviceToHost));
+    if (features) CU(cudaMemcpy(features, df, sizeof(float) * 32 * n, cudaMemcpyDeviceToHost));
+    return FVC_OK;
+}
+
+extern "C" int fvc_model_density(fvc_model *m, const float *pos, int n, float *log_density_out)
+{
+    std::vector<float> o4((size_t)4 * n);
+    const int rc = run_inference(m, pos, nullptr, n, o4.data(), nullptr, nullptr);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) log_density_out[i] = o4[(size_t)4 * i + 3];
+    return FVC_OK;
+}
+
+extern "C" int fvc_model_inference(fvc_model *m, const float *pos, const float *dir01, int n, float *out)
+{
+    CHECK_ARG(dir01 && out, "fvc_model_inference: null argument");
+    return run_inference(m, pos, dir01, n, out, nullptr, nullptr);
+}
+
+/* test hook: hash features and density-network outputs at given positions */
+extern "C" int fvc_model_debug_encode(fvc_model *m, const float *pos, int n, float *features32, float *base_out16)
+{
+    return run_inference(m, pos, nullptr, n, nullptr, base_out16, features32);
+}
+
+/* ------------------------------------------------------------------------ */
+/* renderers                                                                 */
+/* ------------------------------------------------------------------------ */
+extern "C" int fvc_renderer_create(fvc_model *m, int kind, fvc_renderer **out)
+{
+    CHECK_ARG(m && out, "fvc_renderer_create: null argument");
+    CHECK_ARG(kind >= FVC_RENDERER_BASIC && kind <= FVC_RENDERER_CACHE_PERFORMANCE, "fvc_renderer_create: unknown kind");
+    *out = nullptr;
+    auto r = std::make_unique<fvc_renderer>();
+    r->m = m;
+    r->kind = kind;
+    CU(cudaStreamCreateWithFlags(&r->own_stream, cudaStreamNonBlocking));
+    r->stream = r->own_stream;
+    int lo = 0, hi = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CU(cudaStreamCreateWithPriority(&r->low_prio, cudaStreamNonBlocking, lo)); /* src/cache_renderer.cu:822-825 */
+    int rc;
+    if ((rc = dalloc(&r->d_ctl, (size_t)4, "control words"))) return rc;
+    if ((rc = dalloc(&r->d_stats, (size_t)1, "stats"))) return rc;
+    CU(cudaMallocHost((void **)&r->h_pinned, 16 * sizeof(int)));
+    CU(cudaMemset(r->d_stats, 0, sizeof(RenderStatsDev)));
+    CU(cudaMemset(r->d_ctl, 0, 4 * sizeof(int)));
+    *out = r.release();
+    return FVC_OK;
+}
+
+extern "C" void fvc_renderer_destroy(fvc_renderer *r) { delete r; }
+
+extern "C" int fvc_renderer_set_stream(fvc_renderer *r, void *s)
+{
+    CHECK_ARG(r, "fvc_renderer_set_stream: null renderer");
+    r->stream = s ? (cudaStream_t)s : r->own_stream;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_resize(fvc_renderer *r, int width, int height)
+{
+    CHECK_ARG(r && width > 0 && height > 0, "fvc_renderer_resize: bad arguments");
+    if (width == r->W && height == r->H) return FVC_OK;
+    CU(cudaStreamSynchronize(r->stream));
+    dfree(r->d_results); dfree(r->d_image); dfree(r->d_counts);
+    const size_t n = (size_t)width * height;
+    int rc;
+    if ((rc = dalloc(&r->d_results, n, "results"))) return rc;
+    if ((rc = dalloc(&r->d_image, n, "image"))) return rc;
+    if ((rc = dalloc(&r->d_counts, n, "ray counts"))) return rc;
+    CU(cudaMemset(r->d_image, 0, n * sizeof(uchar4)));
+    r->W = width; r->H = height;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int n)
+{
+    CHECK_ARG(r && n >= 0, "fvc_renderer_set_max_samples_per_ray: bad arguments");
+    r->max_samples = n;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_render_mode(fvc_renderer *r, int mode)
+{
+    CHECK_ARG(r && mode >= 0 && mode <= 2, "fvc_renderer_set_render_mode: bad mode");
+    r->render_mode = mode;
+    return FVC_OK;
+}
+
+static int check_info(const fvc_raymarch_info *info)
+{
+    if (!info->deterministic)
+        return fail(FVC_ERR_CONFIG, "only deterministic rendering (RaymarchInfo::deterministic = true) is built");
+    const fvc_int2 res = info->cam_info.resolution;
+    if (res.x <= 0 || res.y <= 0 || (long long)res.x * res.y > (1ll << 30)) return fail(FVC_ERR_ARG, "bad resolution");
+    return FVC_OK;
+}
+
+static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts)
+{
+    fvc_model *m = r->m;
+    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    RenderParams p;
+    memset(&p, 0, sizeof(p));
+    p.scene = m->dscene;
+    p.steps = dev_steps(info->stepsize_info);
+    p.cam = dev_cam(info->cam_info);
+    p.grid = m->grid;
+    p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.bias3 = m->d_bias3;
+    p.latent_offset = m->latent_offset;
+    p.ray_counter = r->d_ctl; p.guard = r->d_ctl + 1; p.stats = r->d_stats;
+    p.results = results; p.image = image; p.ray_counts = counts;
+    p.sample_index = info->sample_index;
+    p.max_rounds = 1 << 26;
+    p.max_samples_per_ray = r->max_samples;
+    if (cached) {
+        fvc_cache *c = r->cache;
+        if (!c || !c->initialized || !c->built) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
+        if (m->latent_offset != 1)
+            return fail(FVC_ERR_CONFIG, "the Density cache variant needs a model whose first latent is not the density");
+        p.ccam = dev_cam(c->rm_info.cam_info);
+        p.csteps = dev_steps(c->rm_info.stepsize_info);
+        p.cache = c->view();
+        p.render_mode = r->render_mode;
+    }
+    CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
+    CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
+    CU(launch_render(p, cached, m->head_hidden, m->n_sms, r->stream));
+    return FVC_OK;
+}
+
+extern "C" int fvc_render_device(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out)
+{
+    CHECK_ARG(r && info, "fvc_render_device: null argument");
+    int rc;
+    if ((rc = check_info(info))) return rc;
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    return enqueue_render(r, info, out ? (float4 *)out->results : nullptr, out ? (uchar4 *)out->image_rgba8 : nullptr,
+                          out ? (int4 *)out->ray_counts : nullptr);
+}
+
+extern "C" int fvc_render(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out)
+{
+    CHECK_ARG(r && info, "fvc_render: null argument");
+    int rc;
+    if ((rc = check_info(info))) return rc;
+    if ((rc = fvc_renderer_resize(r, info->cam_info.resolution.x, info->cam_info.resolution.y))) return rc;
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    const size_t n = (size_t)r->W * r->H;
+    if (out && out->image_rgba8 && info->sample_index > 0)
+        CU(cudaMemcpyAsync(r->d_image, out->image_rgba8, n * 4, cudaMemcpyHostToDevice, r->stream));
+    if ((rc = enqueue_render(r, info, r->d_results, r->d_image, r->d_counts))) return rc;
+    if (out && out->results) CU(cudaMemcpyAsync(out->results, r->d_results, n * 16, cudaMemcpyDeviceToHost, r->stream));
+    if (out && out->image_rgba8) CU(cudaMemcpyAsync(out->image_rgba8, r->d_image, n * 4, cudaMemcpyDeviceToHost, r->stream));
+    if (out && out->ray_counts) CU(cudaMemcpyAsync(out->ray_counts, r->d_counts, n * 16, cudaMemcpyDeviceToHost, r->stream));
+    CU(cudaStreamSynchronize(r->stream));
+    return FVC_OK;
+}
+
+extern "C" int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *o)
+{
+    CHECK_ARG(r && o, "fvc_render_stats: null argument");
+    RenderStatsDev s;
+    int ctl[4];
+    CU(cudaStreamSynchronize(r->stream));
+    CU(cudaMemcpy(&s, r->d_stats, sizeof(s), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(ctl, r->d_ctl, sizeof(ctl), cudaMemcpyDeviceToHost));
+    const double n_rays = (double)std::max(1, r->W * r->H);
+    o->n_samples = (long long)s.n_samples;
+    o->n_resamples = (long long)s.n_resamples;
+    o->n_cache_hits = (long long)s.n_cache_hits;
+    o->n_dropped = (long long)s.n_dropped;
+    o->n_steps = (long long)s.n_steps;
+    o->n_rounds = s.n_rounds;
+    o->samples_ppx = (double)s.n_samples / n_rays;
+    o->guard_flags = ctl[1];
+    return FVC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* cache                                                                     */
+/* ------------------------------------------------------------------------ */
+extern "C" int fvc_cache_create(fvc_cache **out)
+{
+    CHECK_ARG(out, "fvc_cache_create: null argument");
+    *out = new fvc_cache();
+    return FVC_OK;
+}
+
+extern "C" void fvc_cache_destroy(fvc_cache *c) { delete c; }
+
+extern "C" int fvc_renderer_set_caches(fvc_renderer *r, fvc_cache *cache, fvc_cache *next)
+{
+    CHECK_ARG(r && cache && next, "fvc_renderer_set_caches: null argument");
+    std::scoped_lock lk(r->read_mutex, r->write_mutex);
+    r->cache = cache;
+    r->next = next;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_settings *s)
+{
+    CHECK_ARG(r && s, "fvc_renderer_set_cache_settings: null argument");
+    if (s->interpol_variant != 0 || s->interpol_function != 0 || !s->use_inter_brick_interpolation)
+        return fail(FVC_ERR_CONFIG, "only the default cache settings (Density, Linear, inter-brick) are built");
+    r->settings = *s;
+    return FVC_OK;
+}
+
+/* Cache::resize (src/cache.cu:44-84) with the sizing of
+ * CacheRenderer::resizeCache (src/cache_renderer.cu:832-846). */
+static int cache_resize(fvc_renderer *r, fvc_cache *c, int W, int H, const fvc_stepsize_info &st)
+{
+    const int n_rays = W * H;
+    const int est_samples = n_rays * 32;                         /* INIT_ESTIMATED_N_SAMPLES_PER_RAY */
+    const int est_per_brick = (int)(0.5f * std::pow(8.0f, 3.0f)); /* INIT_ESTIMATED_BRICK_SPARSITY * 8^3 */
+    const int est_bricks = est_samples / est_per_brick;
+    const fvc_scene_info &s = r->m->scene;
+    const float dx = s.aabb_to.x - s.aabb_from.x, dy = s.aabb_to.y - s.aabb_from.y, dz = s.aabb_to.z - s.aabb_from.z;
+    const float diag = sqrtf(dx * dx + dy * dy + dz * dz);       /* max_step_in_scene */
+    const float tq = diag + st.near_;
+    float msteps;
+    if (st.cone_angle <= 0.0f) msteps = tq / st.dt_min;
+    else if (tq >= st.t_max) msteps = (tq - st.t_max) / st.dt_max + st.i_max;
+    else if (tq < st.t_min) msteps = tq / st.dt_min;
+    else msteps = fvc_logf(tq / st.t_min) / st.log1p_c + st.i_min;
+    const int max_n_steps = (int)std::ceil(msteps);
+    const int depth = (max_n_steps + 3) / 4 * 4;
+    const int bX = (W + 7) / 8, bY = (H + 7) / 8, bZ = (depth + 7) / 8;
+    const int dX = 128, dY = 128, dZ = (est_bricks + dX * dY - 1) / (dX * dY);
+    if (c->initialized && c->fW == W && c->fH == H && c->fD == depth && c->dZ == dZ) return FVC_OK;
+    dfree(c->d_packed); dfree(c->d_known);
+    if (c->d_voxels) cudaFree(c->d_voxels);
+    c->d_voxels = nullptr;
+    c->initialized = false;
+    c->built = false;
+    int rc;
+    if ((rc = dalloc(&c->d_packed, (size_t)bX * bY * bZ, "brick index"))) return rc;
+    if ((rc = dalloc(&c->d_known, (size_t)W * H, "known ranges"))) return rc;
+    cudaError_t e = cudaMalloc(&c->d_voxels, (size_t)dX * dY * dZ * 512 * 32);
+    if (e != cudaSuccess) { cudaGetLastError(); c->d_voxels = nullptr; return fail(FVC_ERR_OOM, "cudaMalloc cache data array"); }
+    c->fW = W; c->fH = H; c->fD = depth; c->bX = bX; c->bY = bY; c->bZ = bZ; c->dX = dX; c->dY = dY; c->dZ = dZ;
+    c->initialized = true;
+    return FVC_OK;
+}
+
+extern "C" int fvc_cache_resize(fvc_renderer *r, int width, int height, const fvc_stepsize_info *steps)
+{
+    CHECK_ARG(r && r->next && steps && width > 0 && height > 0, "fvc_cache_resize: bad arguments (caches attached?)");
+    std::lock_guard<std::mutex> lk(r->write_mutex);
+    return cache_resize(r, r->next, width, height, *steps);
+}
+
+extern "C" int fvc_cache_swap(fvc_renderer *r)
+{
+    CHECK_ARG(r && r->cache && r->next, "fvc_cache_swap: caches not attached");
+    std::scoped_lock lk(r->read_mutex, r->write_mutex);
+    std::swap(r->cache, r->next);
+    return FVC_OK;
+}
+
+static int ensure_build_scratch(fvc_renderer *r, int n_tiles)
+{
+    BuildScratch &b = r->bs;
+    if (b.n_tiles == n_tiles) return FVC_OK;
+    b.release();
+    int rc;
+    if ((rc = dalloc(&b.rays, (size_t)n_tiles * 64, "build rays"))) return rc;
+    if ((rc = dalloc(&b.block_step, (size_t)n_tiles, "block steps"))) return rc;
+    if ((rc = dalloc(&b.tile_alive, (size_t)n_tiles, "tile alive"))) return rc;
+    if ((rc = dalloc(&b.alive_a, (size_t)n_tiles, "alive list"))) return rc;
+    if ((rc = dalloc(&b.alive_b, (size_t)n_tiles, "alive list"))) return rc;
+    if ((rc = dalloc(&b.counters, (size_t)8, "build counters"))) return rc;
+    if ((rc = dalloc(&b.tile_n_samples, (size_t)n_tiles, "tile samples"))) return rc;
+    if ((rc = dalloc(&b.tile_processed, (size_t)n_tiles, "tile flags"))) return rc;
+    if ((rc = dalloc(&b.tile_need, (size_t)n_tiles, "tile flags"))) return rc;
+    if ((rc = dalloc(&b.tile_n_alive, (size_t)n_tiles, "tile alive counts"))) return rc;
+    if ((rc = dalloc(&b.jobs, (size_t)2 * n_tiles, "copy jobs"))) return rc;
+    cudaError_t e = cudaMalloc(&b.staging, (size_t)n_tiles * 512 * 32);
+    if (e != cudaSuccess) { cudaGetLastError(); b.staging = nullptr; return fail(FVC_ERR_OOM, "cudaMalloc build staging"); }
+    b.n_tiles = n_tiles;
+    return FVC_OK;
+}
+
+/* CacheRenderer::initCacheBlockwise, src/cache_renderer.cu:931-1051 */
+extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
+{
+    CHECK_ARG(r && info, "fvc_cache_build: null argument");
+    CHECK_ARG(r->next, "fvc_cache_build: caches not attached (fvc_renderer_set_caches)");
+    int rc;
+    if ((rc = check_info(info))) return rc;
+    fvc_model *m = r->m;
+    if (m->latent_offset != 1)
+        return fail(FVC_ERR_CONFIG, "the Density cache variant needs a model whose first latent is not the density");
+    std::lock_guard<std::mutex> lk(r->write_mutex);
+    fvc_cache *c = r->next;
+    const int W = info->cam_info.resolution.x, H = info->cam_info.resolution.y;
+    if ((rc = cache_resize(r, c, W, H, info->stepsize_info))) return rc;
+    c->rm_info = *info;
+    c->built = false;
+    const int n_tiles = c->bX * c->bY;
+    if ((rc = ensure_build_scratch(r, n_tiles))) return rc;
+    BuildScratch &b = r->bs;
+    cudaStream_t s = r->stream;
+
+    CacheBuildParams p;
+    memset(&p, 0, sizeof(p));
+    p.scene = m->dscene; p.steps = dev_steps(info->stepsize_info); p.cam = dev_cam(info->cam_info); p.grid = m->grid;
+    p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.latent_offset = m->latent_offset;
+    p.bX = c->bX; p.bY = c->bY; p.bZ = c->bZ; p.fW = c->fW; p.fH = c->fH; p.fD = c->fD;
+    p.dX = c->dX; p.dY = c->dY; p.dZ = c->dZ; p.capacity = c->capacity();
+    p.rays = b.rays; p.block_step = b.block_step; p.tile_alive = b.tile_alive;
+    p.alive_list = b.alive_a; p.alive_list_next = b.alive_b;
+    p.n_alive_tiles = b.counters + 0; p.n_alive_next = b.counters + 1;
+    p.slot_counter = b.counters + 2; p.n_jobs = b.counters + 3; p.guard = b.counters + 4;
+    p.tile_n_samples = b.tile_n_samples; p.tile_processed = b.tile_processed; p.tile_need = b.tile_need;
+    p.tile_n_alive = b.tile_n_alive; p.staging = b.staging; p.voxels = c->d_voxels;
+    p.packed_index = c->d_packed; p.known_ranges = c->d_known; p.jobs = b.jobs;
+    p.max_search = c->bZ + 4;
+
+    CU(cudaMemsetAsync(b.counters, 0, 8 * sizeof(int), s));
+    CU(cudaMemsetAsync(c->d_packed, 0xff, (size_t)c->bX * c->bY * c->bZ * sizeof(int32_t), s));
+    cache_init_kernel<<<n_tiles, 64, 0, s>>>(p);
+    CU(cudaGetLastError());
+    cache_compact_kernel<<<1, 1024, 0, s>>>(p, n_tiles);
+    CU(cudaGetLastError());
+    const size_t smem = build_smem_bytes();
+    CU(cudaFuncSetAttribute(cache_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CU(cudaMemcpyAsync(r->h_pinned, b.counters, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    int n_alive = r->h_pinned[0];
+    long long n_samples = 0;
+    int iter = 0;
+    const int max_iter = c->bZ + 8;
+    std::vector<int> dummy;
+    for (; iter < max_iter && n_alive > 0; ++iter) {
+        cache_tile_kernel<<<std::min(n_alive, 1 << 16), 64, smem, s>>>(p);
+        CU(cudaGetLastError());
+        cache_assign_kernel<<<1, 1024, 0, s>>>(p);
+        CU(cudaGetLastError());
+        cache_copy_kernel<<<std::min(n_alive, 4 * m->n_sms), 256, 0, s>>>(p);
+        CU(cudaGetLastError());
+        std::swap(p.alive_list, p.alive_list_next);
+        std::swap(p.n_alive_tiles, p.n_alive_next);
+        CU(cudaMemcpyAsync(r->h_pinned, p.n_alive_tiles, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        n_alive = r->h_pinned[0];
+    }
+    cache_known_ranges_kernel<<<n_tiles, 64, 0, s>>>(p);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(r->h_pinned, b.counters, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    const int demanded = r->h_pinned[2], guard = r->h_pinned[4];
+    c->stats.n_bricks_demanded = demanded;
+    c->stats.n_bricks_reserved = c->capacity();
+    c->stats.n_bricks_set = std::min(demanded, c->capacity());
+    c->stats.overflow = demanded > c->capacity();
+    c->stats.n_iterations = iter;
+    c->stats.n_samples = n_samples;
+    c->built = true;
+    if (guard) return fail(FVC_ERR_GUARD, "cache build guard fired: flags " + std::to_string(guard));
+    if (n_alive > 0) return fail(FVC_ERR_GUARD, "cache build did not converge within the frustum depth");
+    return FVC_OK;
+}
+
+extern "C" int fvc_cache_stats(fvc_renderer *r, fvc_cache_stats_t *o)
+{
+    CHECK_ARG(r && o && r->next, "fvc_cache_stats: bad arguments");
+    *o = r->next->built ? r->next->stats : (r->cache ? r->cache->stats : r->next->stats);
+    return FVC_OK;
+}
+
+extern "C" int fvc_cache_dims(fvc_cache *c, fvc_int3 *fd, fvc_int3 *bd, fvc_int3 *dd)
+{
+    CHECK_ARG(c, "fvc_cache_dims: null cache");
+    if (!c->initialized) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
+    if (fd) *fd = {c->fW, c->fH, c->fD};
+    if (bd) *bd = {c->bX, c->bY, c->bZ};
+    if (dd) *dd = {c->dX, c->dY, c->dZ};
+    return FVC_OK;
+}
+
+extern "C" int fvc_cache_read(fvc_cache *c, int32_t *packed, size_t *packed_n, float *known, size_t *known_n, uint32_t *vox,
+                              size_t *vox_n)
+{
+    CHECK_ARG(c, "fvc_cache_read: null cache");
+    if (!c->initialized) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
+    const size_t nb = (size_t)c->bX * c->bY * c->bZ, nk = (size_t)c->fW * c->fH, nv = (size_t)c->capacity() * 512 * 8;
+    if (packed_n) *packed_n = nb;
+    if (known_n) *known_n = nk;
+    if (vox_n) *vox_n = nv;
+    CU(cudaDeviceSynchronize());
+    if (packed) CU(cudaMemcpy(packed, c->d_packed, nb * 4, cudaMemcpyDeviceToHost));
+    if (known) CU(cudaMemcpy(known, c->d_known, nk * 4, cudaMemcpyDeviceToHost));
+    if (vox) CU(cudaMemcpy(vox, c->d_voxels, nv * 4, cudaMemcpyDeviceToHost));
+    return FVC_OK;
+}

@@ -1,0 +1,465 @@
+/*
+ * fvc_device.cuh - device-side marcher math, hash-grid encoding and the
+ * warp-level fused MLP of the GB300 renderer.
+ *
+ * Marcher index math uses the F_* single-rounding intrinsics of
+ * fvc_detmath.h in the reference's operation order
+ * (include/raymarch_common.h, include/common.h) so per-ray step sequences,
+ * occupancy lookups and froxel coordinates are bit-identical to the CPU
+ * oracle.  The network runs on the tensor cores (mma.sync m16n8k16, fp16
+ * inputs, fp32 accumulation); layer outputs are rounded to fp16 between
+ * layers as the reference's fp16 network stores them.
+ */
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "fvc_detmath.h"
+
+namespace fvc {
+
+/* --------------------------------------------------------------------- */
+/* parameter blocks (filled on the host from the C-ABI structs)           */
+/* --------------------------------------------------------------------- */
+struct DevScene {
+    float3 aabb_from, aabb_to;
+    float3 unit_off;  /* aabb_from / 2^(nlvl-1)             (world_to_aabb_unit) */
+    float3 unit_den;  /* (aabb_to - aabb_from) / 2^(nlvl-1) */
+    float3 aabb_den;  /* aabb_to - aabb_from                 (contract_aabb)      */
+    float3 c_from, c_den; /* contraction aabb and its extent */
+    int nlvl, normalized, contraction, is_open_gl;
+    float alpha_thre;
+};
+
+struct DevSteps {
+    float cone, log1p_c, log1p_c_lo, near_, near_i, far_;
+    float dt_min, dt_max, t_min, t_max, i_min, i_max;
+};
+
+struct DevCam {
+    int W, H, gl;
+    float fx, fy, px, py;
+    float c2w[12];
+    float w2c[12];
+};
+
+constexpr int MAX_LEVELS = 16;
+struct DevGrid {
+    int n_levels;
+    uint32_t dense_mask;
+    float scale[MAX_LEVELS];
+    uint32_t res[MAX_LEVELS], res2[MAX_LEVELS], size[MAX_LEVELS], offset[MAX_LEVELS];
+};
+
+/* fragment-ordered weights (uint2 per lane per (n-tile, k-step)) */
+constexpr int W_L1 = 0;                  /* 64 x 32  : 8 ntiles * 2 ksteps * 32 lanes */
+constexpr int W_L2 = W_L1 + 8 * 2 * 32;  /* 16 x 64  : 2 * 4 * 32 */
+constexpr int W_L3 = W_L2 + 2 * 4 * 32;  /* 64 x 32  (head input: base16 | sh16) */
+constexpr int W_L4 = W_L3 + 8 * 2 * 32;  /* 64 x 64 */
+constexpr int W_L5 = W_L4 + 8 * 4 * 32;  /* 16 x 64 */
+constexpr int W_TOTAL = W_L5 + 2 * 4 * 32; /* uint2 entries = 2560 -> 20 KiB */
+
+/* --------------------------------------------------------------------- */
+/* step grid (StepsizeInfo, include/common.h:133-163)                     */
+/* --------------------------------------------------------------------- */
+__device__ __forceinline__ float t_from_step(const DevSteps &s, float step)
+{
+    if (s.cone <= 0.0f) return F_MUL(step, s.dt_min);
+    if (step >= s.i_max) return F_ADD(s.t_max, F_MUL(F_SUB(step, s.i_max), s.dt_max));
+    if (step < s.i_min) return F_MUL(step, s.dt_min);
+    return F_MUL(s.t_min, fvc_pow_1pc(F_SUB(step, s.i_min), s.log1p_c, s.log1p_c_lo));
+}
+
+__device__ __forceinline__ float step_from_t(const DevSteps &s, float t)
+{
+    if (s.cone <= 0.0f) return F_DIV(t, s.dt_min);
+    if (t >= s.t_max) return F_ADD(F_DIV(F_SUB(t, s.t_max), s.dt_max), s.i_max);
+    if (t < s.t_min) return F_DIV(t, s.dt_min);
+    return F_ADD(F_DIV(fvc_logf(F_DIV(t, s.t_min)), s.log1p_c), s.i_min);
+}
+
+/* calculate_stepsize, include/raymarch_common.h:274-284 */
+__device__ __forceinline__ float calc_step(const DevSteps &s, float t)
+{
+    return fmaxf(s.dt_min, fminf(F_MUL(t, s.cone), s.dt_max));
+}
+
+/* valid_t_from_t, include/raymarch_common.h:286-296 */
+__device__ __forceinline__ float valid_t_from_t(const DevSteps &s, float t)
+{
+    return t_from_step(s, F_ADD(roundf(F_SUB(step_from_t(s, fmaxf(t, s.near_)), s.near_i)), s.near_i));
+}
+
+/* --------------------------------------------------------------------- */
+/* rays                                                                   */
+/* --------------------------------------------------------------------- */
+__device__ __forceinline__ float dot4(float ax, float ay, float az, float aw, const float *m)
+{
+    return F_ADD(F_ADD(F_ADD(F_MUL(ax, m[0]), F_MUL(ay, m[1])), F_MUL(az, m[2])), F_MUL(aw, m[3]));
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b)
+{
+    return F_ADD(F_ADD(F_MUL(a.x, b.x), F_MUL(a.y, b.y)), F_MUL(a.z, b.z));
+}
+__device__ __forceinline__ float3 at(float3 o, float3 d, float t)
+{
+    return make_float3(F_ADD(o.x, F_MUL(t, d.x)), F_ADD(o.y, F_MUL(t, d.y)), F_ADD(o.z, F_MUL(t, d.z)));
+}
+
+/* generateRay for the pixel centre (deterministic), include/raymarch_common.h:190-251;
+ * normalize() uses the correctly rounded 1/sqrt (double, rounded once). */
+__device__ __forceinline__ void generate_ray(const DevCam &c, int x, int y, float3 &o, float3 &d)
+{
+    const float sx = F_ADD((float)x, 0.5f), sy = F_ADD((float)y, 0.5f);
+    const float sgn = c.gl ? -1.f : 1.f;
+    const float dx = F_DIV(F_SUB(sx, c.px), c.fx);
+    const float dy = F_MUL(F_DIV(F_SUB(sy, c.py), c.fy), sgn);
+    const float dz = sgn;
+    float3 v = make_float3(dot4(dx, dy, dz, 0.f, c.c2w), dot4(dx, dy, dz, 0.f, c.c2w + 4), dot4(dx, dy, dz, 0.f, c.c2w + 8));
+    const float inv = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn((double)dot3(v, v))));
+    d = make_float3(F_MUL(v.x, inv), F_MUL(v.y, inv), F_MUL(v.z, inv));
+    o = make_float3(c.c2w[3], c.c2w[7], c.c2w[11]);
+}
+
+/* ray_aabb_intersect, include/raymarch_common.h:482-532 */
+__device__ __forceinline__ bool ray_aabb(float3 o, float3 d, float3 from, float3 to, float &tn, float &tf)
+{
+    float tmin = F_DIV(F_SUB(from.x, o.x), d.x), tmax = F_DIV(F_SUB(to.x, o.x), d.x);
+    if (tmin > tmax) { float c = tmin; tmin = tmax; tmax = c; }
+    float tymin = F_DIV(F_SUB(from.y, o.y), d.y), tymax = F_DIV(F_SUB(to.y, o.y), d.y);
+    if (tymin > tymax) { float c = tymin; tymin = tymax; tymax = c; }
+    if (tmin > tymax || tymin > tmax) { tn = 1e10f; tf = 1e10f; return false; }
+    if (tymin > tmin) tmin = tymin;
+    if (tymax < tmax) tmax = tymax;
+    float tzmin = F_DIV(F_SUB(from.z, o.z), d.z), tzmax = F_DIV(F_SUB(to.z, o.z), d.z);
+    if (tzmin > tzmax) { float c = tzmin; tzmin = tzmax; tzmax = c; }
+    if (tmin > tzmax || tzmin > tmax) { tn = 1e10f; tf = 1e10f; return false; }
+    if (tzmin > tmin) tmin = tzmin;
+    if (tzmax < tmax) tmax = tzmax;
+    tn = tmin; tf = tmax;
+    return true;
+}
+
+/* transformRay, include/raymarch_common.h:253-262 */
+__device__ __forceinline__ void transform_ray(const float *m, float3 o, float3 d, float3 &oc, float3 &dc)
+{
+    oc = make_float3(dot4(o.x, o.y, o.z, 1.0f, m), dot4(o.x, o.y, o.z, 1.0f, m + 4), dot4(o.x, o.y, o.z, 1.0f, m + 8));
+    dc = make_float3(dot4(d.x, d.y, d.z, 0.0f, m), dot4(d.x, d.y, d.z, 0.0f, m + 4), dot4(d.x, d.y, d.z, 0.0f, m + 8));
+}
+
+/* --------------------------------------------------------------------- */
+/* occupancy grid (grid_occupied_at<128, true>, include/raymarch_common.h:660-710) */
+/* --------------------------------------------------------------------- */
+__device__ __forceinline__ uint32_t expand_bits3(uint32_t v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ __forceinline__ int frexp_exponent(float m)
+{
+    const uint32_t b = __float_as_uint(m);
+    const int be = (int)((b >> 23) & 0xffu);
+    if (be != 0 && be != 0xff) return be - 126;  /* normal: m = f*2^e, f in [0.5,1) */
+    int e;
+    frexpf(m, &e);
+    return e;
+}
+
+__device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__restrict__ bits, float3 p)
+{
+    float3 u = p;
+    if (!sc.normalized)
+        u = make_float3(F_DIV(F_SUB(p.x, sc.unit_off.x), sc.unit_den.x), F_DIV(F_SUB(p.y, sc.unit_off.y), sc.unit_den.y),
+                        F_DIV(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z));
+    const float ax = F_SUB(u.x, 0.5f), ay = F_SUB(u.y, 0.5f), az = F_SUB(u.z, 0.5f);
+    const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
+    const int mip = max(0, frexp_exponent(mx) + 1);
+    if (mip >= sc.nlvl) return false;
+    const float sm = __int_as_float((127 - mip) << 23); /* scalbnf(1, -mip) */
+    const int ix = (int)F_MUL(F_ADD(F_MUL(ax, sm), 0.5f), 128.0f);
+    const int iy = (int)F_MUL(F_ADD(F_MUL(ay, sm), 0.5f), 128.0f);
+    const int iz = (int)F_MUL(F_ADD(F_MUL(az, sm), 0.5f), 128.0f);
+    const uint32_t idx = expand_bits3((uint32_t)ix) | (expand_bits3((uint32_t)iy) << 1) | (expand_bits3((uint32_t)iz) << 2);
+    const uint32_t bidx = idx / 8u + (uint32_t)((128 * 128 * 128 / 8) * mip);
+    return (__ldg(bits + bidx) >> (idx & 7u)) & 1u;
+}
+
+/* apply_contraction, include/raymarch_common.h:610-653 */
+__device__ __forceinline__ float3 contract(const DevScene &sc, float3 p)
+{
+    if (sc.contraction == 1)
+        return make_float3(F_DIV(F_SUB(p.x, sc.aabb_from.x), sc.aabb_den.x), F_DIV(F_SUB(p.y, sc.aabb_from.y), sc.aabb_den.y),
+                           F_DIV(F_SUB(p.z, sc.aabb_from.z), sc.aabb_den.z));
+    if (sc.contraction == 2 || sc.contraction == 3) {
+        const float ux = F_SUB(F_MUL(F_DIV(F_SUB(p.x, sc.c_from.x), sc.c_den.x), 2.0f), 1.0f);
+        const float uy = F_SUB(F_MUL(F_DIV(F_SUB(p.y, sc.c_from.y), sc.c_den.y), 2.0f), 1.0f);
+        const float uz = F_SUB(F_MUL(F_DIV(F_SUB(p.z, sc.c_from.z), sc.c_den.z), 2.0f), 1.0f);
+        const float n = sc.contraction == 3 ? fmaxf(fmaxf(fabsf(ux), fabsf(uy)), fabsf(uz))
+                                            : F_SQRT(F_ADD(F_ADD(F_MUL(ux, ux), F_MUL(uy, uy)), F_MUL(uz, uz)));
+        const float f = fmaxf(n, 1.0f);
+        const float k = F_SUB(2.0f, F_DIV(1.0f, f));
+        return make_float3(F_ADD(F_DIV(F_MUL(k, F_DIV(ux, f)), 4.0f), 0.5f), F_ADD(F_DIV(F_MUL(k, F_DIV(uy, f)), 4.0f), 0.5f),
+                           F_ADD(F_DIV(F_MUL(k, F_DIV(uz, f)), 4.0f), 0.5f));
+    }
+    return p;
+}
+
+/* cam2froxel, include/raymarch_common.h:316-329 */
+__device__ __forceinline__ float3 cam2froxel(float3 c, const DevCam &cam, const DevSteps &st, float &t)
+{
+    const float sgn = cam.gl ? -1.f : 1.f;
+    const float z = F_MUL(c.z, sgn);
+    t = F_SQRT(dot3(c, c));
+    return make_float3(F_ADD(F_MUL(F_DIV(c.x, z), cam.fx), cam.px), F_ADD(F_MUL(F_DIV(F_MUL(c.y, sgn), z), cam.fy), cam.py),
+                       F_MUL(F_SUB(step_from_t(st, t), st.near_i), c.z < 0.0f ? -1.0f : 1.0f));
+}
+
+/* --------------------------------------------------------------------- */
+/* hash grid (Instant-NGP multiresolution hash encoding)                  */
+/* --------------------------------------------------------------------- */
+/* Encodes one position into 2*n_levels features (fp16) written to
+ * out[0 .. 2*n_levels) as half2 per level.  Corner and fraction in float32
+ * (p = fma(scale, x, 0.5), floor, subtract), accumulation in float32. */
+__device__ __forceinline__ void hash_encode(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out)
+{
+#pragma unroll 4
+    for (int l = 0; l < g.n_levels; ++l) {
+        const float sc = g.scale[l];
+        const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
+        const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+        const uint32_t gx = (uint32_t)(int)fx, gy = (uint32_t)(int)fy, gz = (uint32_t)(int)fz;
+        const float wx = __fsub_rn(px, fx), wy = __fsub_rn(py, fy), wz = __fsub_rn(pz, fz);
+        const uint32_t size = g.size[l];
+        uint32_t idx[8];
+        if ((g.dense_mask >> l) & 1u) {
+            const uint32_t r = g.res[l], r2 = g.res2[l];
+            const uint32_t b = gx + gy * r + gz * r2;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint32_t i = b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u);
+                idx[c] = i < size ? i : i % size;
+            }
+        } else {
+            const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;
+            const uint32_t hz0 = gz * 805459861u, hz1 = (gz + 1u) * 805459861u;
+            const uint32_t m = size - 1u; /* hashed levels hold 2^log2_T entries */
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                idx[c] = ((gx + ((c & 1) ? 1u : 0u)) ^ ((c & 2) ? hy1 : hy0) ^ ((c & 4) ? hz1 : hz0)) & m;
+        }
+        const __half2 *tl = table + g.offset[l];
+        __half2 v[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) v[c] = __ldg(tl + idx[c]);
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float w = ((c & 1) ? wx : 1.0f - wx) * ((c & 2) ? wy : 1.0f - wy) * ((c & 4) ? wz : 1.0f - wz);
+            const float2 f = __half22float2(v[c]);
+            ax = fmaf(w, f.x, ax);
+            ay = fmaf(w, f.y, ay);
+        }
+        out[l] = __floats2half2_rn(ax, ay);
+    }
+}
+
+/* SH degree 4 (16 values) of a unit_to_01 direction, written as 8 half2.
+ * Real SH of Sloan's "Stupid SH" recurrences, sign convention of
+ * src/my_fully_fused_mlp.cu:216-233. */
+__device__ __forceinline__ void sh16(float3 d01, __half2 *out)
+{
+    const float x = d01.x * 2.f - 1.f, y = d01.y * 2.f - 1.f, z = d01.z * 2.f - 1.f;
+    const float xy = x * y, xz = x * z, yz = y * z, x2 = x * x, y2 = y * y, z2 = z * z;
+    out[0] = __floats2half2_rn(0.28209479177387814f, -0.48860251190291987f * y);
+    out[1] = __floats2half2_rn(0.48860251190291987f * z, -0.48860251190291987f * x);
+    out[2] = __floats2half2_rn(1.0925484305920792f * xy, -1.0925484305920792f * yz);
+    out[3] = __floats2half2_rn(0.94617469575755997f * z2 - 0.31539156525251999f, -1.0925484305920792f * xz);
+    out[4] = __floats2half2_rn(0.54627421529603959f * x2 - 0.54627421529603959f * y2, 0.59004358992664352f * y * (-3.0f * x2 + y2));
+    out[5] = __floats2half2_rn(2.8906114426405538f * xy * z, 0.45704579946446572f * y * (1.0f - 5.0f * z2));
+    out[6] = __floats2half2_rn(0.3731763325901154f * z * (5.0f * z2 - 3.0f), 0.45704579946446572f * x * (1.0f - 5.0f * z2));
+    out[7] = __floats2half2_rn(1.4453057213202769f * z * (x2 - y2), 0.59004358992664352f * x * (-x2 + 3.0f * y2));
+}
+
+/* --------------------------------------------------------------------- */
+/* warp MLP on tensor cores                                               */
+/* --------------------------------------------------------------------- */
+__device__ __forceinline__ void mma16816(float (&c)[4], const uint32_t (&a)[4], uint2 b)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi)
+{
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+/* Tile layout: 32 rows x TILE_STRIDE halfs.
+ *   cols  0..31 : hash features (layer-1 input)
+ *   cols 16..31 : overwritten with the density-network output (head input part 1)
+ *   cols 32..47 : SH of the direction (head input part 2)
+ * Stride 56 halfs (112 B) makes the fragment loads bank-conflict free. */
+constexpr int TILE_STRIDE = 56;
+
+/* A fragments (m16 x k16) of rows [16*mt, 16*mt+16), cols [c0, c0+16) */
+__device__ __forceinline__ void load_a(const __half *tile, int mt, int c0, int lane, uint32_t (&a)[4])
+{
+    const int g = lane >> 2, t = lane & 3;
+    const __half *r0 = tile + (16 * mt + g) * TILE_STRIDE + c0 + 2 * t;
+    const __half *r1 = r0 + 8 * TILE_STRIDE;
+    a[0] = *reinterpret_cast<const uint32_t *>(r0);
+    a[1] = *reinterpret_cast<const uint32_t *>(r1);
+    a[2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
+    a[3] = *reinterpret_cast<const uint32_t *>(r1 + 8);
+}
+
+/* Density network on the 32 rows of a tile: layer 1 (64 x 32, ReLU) and
+ * layer 2 (16 x 64).  Writes the fp16 outputs into tile cols 16..31 and
+ * returns nothing; col 16 holds the log-density. */
+__device__ __forceinline__ void density_mlp(__half *tile, const uint2 *__restrict__ W, int lane)
+{
+    const int g = lane >> 2, t = lane & 3;
+    uint32_t a1[2][2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) load_a(tile, mt, 16 * s, lane, a1[mt][s]);
+    /* layer 1 -> A fragments of layer 2 (K = 64: 4 k-steps) */
+    uint32_t a2[2][4][4];
+#pragma unroll
+    for (int jp = 0; jp < 4; ++jp) {
+        float c[2][2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) c[mt][h][0] = c[mt][h][1] = c[mt][h][2] = c[mt][h][3] = 0.f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                const uint2 b = W[W_L1 + ((2 * jp + h) * 2 + s) * 32 + lane];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) mma16816(c[mt][h], a1[mt][s], b);
+            }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            a2[mt][jp][0] = pack_h2(fmaxf(c[mt][0][0], 0.f), fmaxf(c[mt][0][1], 0.f));
+            a2[mt][jp][1] = pack_h2(fmaxf(c[mt][0][2], 0.f), fmaxf(c[mt][0][3], 0.f));
+            a2[mt][jp][2] = pack_h2(fmaxf(c[mt][1][0], 0.f), fmaxf(c[mt][1][1], 0.f));
+            a2[mt][jp][3] = pack_h2(fmaxf(c[mt][1][2], 0.f), fmaxf(c[mt][1][3], 0.f));
+        }
+    }
+    __syncwarp();
+    /* layer 2: 16 outputs */
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        float c[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) c[mt][0] = c[mt][1] = c[mt][2] = c[mt][3] = 0.f;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const uint2 b = W[W_L2 + (j * 4 + s) * 32 + lane];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) mma16816(c[mt], a2[mt][s], b);
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            __half *r0 = tile + (16 * mt + g) * TILE_STRIDE + 16 + 8 * j + 2 * t;
+            *reinterpret_cast<uint32_t *>(r0) = pack_h2(c[mt][0], c[mt][1]);
+            *reinterpret_cast<uint32_t *>(r0 + 8 * TILE_STRIDE) = pack_h2(c[mt][2], c[mt][3]);
+        }
+    }
+    __syncwarp();
+}
+
+/* Color head on the 32 rows: input tile cols 16..47 (density-network
+ * outputs | SH), layer 3 (64 x 32 + bias from the 1-padding, ReLU),
+ * [layer 4 (64 x 64, ReLU)], layer 5 (16 x 64).  Returns for each lane the
+ * logits of rows (g, g+8) and (16+g, 24+g) at cols 2t, 2t+1 in out[mt][4]. */
+template <int HEAD_HIDDEN>
+__device__ __forceinline__ void color_mlp(const __half *tile, const uint2 *__restrict__ W, const float *__restrict__ bias3,
+                                          int lane, float (&out)[2][4])
+{
+    const int t = lane & 3;
+    uint32_t a3[2][2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) load_a(tile, mt, 16 + 16 * s, lane, a3[mt][s]);
+    uint32_t a4[2][4][4];
+#pragma unroll
+    for (int jp = 0; jp < 4; ++jp) {
+        float c[2][2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float b0 = bias3[8 * (2 * jp + h) + 2 * t], b1 = bias3[8 * (2 * jp + h) + 2 * t + 1];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) { c[mt][h][0] = b0; c[mt][h][1] = b1; c[mt][h][2] = b0; c[mt][h][3] = b1; }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                const uint2 b = W[W_L3 + ((2 * jp + h) * 2 + s) * 32 + lane];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) mma16816(c[mt][h], a3[mt][s], b);
+            }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            a4[mt][jp][0] = pack_h2(fmaxf(c[mt][0][0], 0.f), fmaxf(c[mt][0][1], 0.f));
+            a4[mt][jp][1] = pack_h2(fmaxf(c[mt][0][2], 0.f), fmaxf(c[mt][0][3], 0.f));
+            a4[mt][jp][2] = pack_h2(fmaxf(c[mt][1][0], 0.f), fmaxf(c[mt][1][1], 0.f));
+            a4[mt][jp][3] = pack_h2(fmaxf(c[mt][1][2], 0.f), fmaxf(c[mt][1][3], 0.f));
+        }
+    }
+    if (HEAD_HIDDEN == 2) {
+        uint32_t a5[2][4][4];
+#pragma unroll
+        for (int jp = 0; jp < 4; ++jp) {
+            float c[2][2][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) c[mt][h][0] = c[mt][h][1] = c[mt][h][2] = c[mt][h][3] = 0.f;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const uint2 b = W[W_L4 + ((2 * jp + h) * 4 + s) * 32 + lane];
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt) mma16816(c[mt][h], a4[mt][s], b);
+                }
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                a5[mt][jp][0] = pack_h2(fmaxf(c[mt][0][0], 0.f), fmaxf(c[mt][0][1], 0.f));
+                a5[mt][jp][1] = pack_h2(fmaxf(c[mt][0][2], 0.f), fmaxf(c[mt][0][3], 0.f));
+                a5[mt][jp][2] = pack_h2(fmaxf(c[mt][1][0], 0.f), fmaxf(c[mt][1][1], 0.f));
+                a5[mt][jp][3] = pack_h2(fmaxf(c[mt][1][2], 0.f), fmaxf(c[mt][1][3], 0.f));
+            }
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) a4[mt][s][q] = a5[mt][s][q];
+    }
+    /* layer 5: outputs 0..7 (only 0..2 used) */
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) out[mt][0] = out[mt][1] = out[mt][2] = out[mt][3] = 0.f;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const uint2 b = W[W_L5 + (0 * 4 + s) * 32 + lane];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) mma16816(out[mt], a4[mt][s], b);
+    }
+}
+
+}  // namespace fvc

@@ -1,0 +1,115 @@
+/*
+ * fvc_kernels.h - launch parameter blocks of the renderer's kernels.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fvc_device.cuh"
+
+namespace fvc {
+
+/* read-only view of a built frustum cache (Cache, include/cache.h:12-74):
+ * packed brick index [bZ][bY][bX] (x fastest; pack3D(slot) or -1),
+ * known_ranges_to [fH][fW], voxels [slots][512] of 32 bytes */
+struct CacheView {
+    const int32_t *packed_index;
+    const float *known_ranges;
+    const void *voxels;
+    int fW, fH, fD, bX, bY, bZ, dX, dY, dZ;
+    int n_valid_slots;          /* slots written by the last build; others read as zero */
+};
+
+struct RenderStatsDev {
+    unsigned long long n_samples, n_resamples, n_cache_hits, n_dropped, n_steps;
+    int n_rounds, pad;
+};
+
+struct RenderParams {
+    DevScene scene;
+    DevSteps steps;
+    DevCam cam;
+    DevGrid grid;
+    const uint8_t *bits;        /* Morton occupancy bitfield */
+    const __half2 *table;       /* hash tables, F = 2 */
+    const uint2 *weights;       /* fragment-ordered MLP weights, W_TOTAL entries */
+    const float *bias3;         /* head layer-1 bias from the 1-padding */
+    int latent_offset;
+    int *ray_counter;
+    int *guard;
+    RenderStatsDev *stats;
+    float4 *results;            /* rgb, transmittance per pixel (may be null) */
+    int4 *ray_counts;           /* per pixel: composited resample, composited cache, dropped, steps (may be null) */
+    uchar4 *image;              /* progressive uchar4 image (may be null) */
+    int sample_index;
+    int max_rounds;
+    int max_samples_per_ray;    /* 0 = unlimited */
+    /* cached render */
+    DevCam ccam;
+    DevSteps csteps;
+    CacheView cache;
+    int render_mode;            /* 0 default, 1 only cache, 2 only resampled */
+};
+
+struct InferenceParams {
+    DevGrid grid;
+    const __half2 *table;
+    const uint2 *weights;
+    const float *bias3;
+    const float *pos;           /* [n][3] contracted */
+    const float *dir;           /* [n][3] unit_to_01 or null (density only) */
+    int n;
+    float *out4;                /* [n][4] logits r,g,b, log-density (fp16 values) */
+    float *base_out;            /* [n][16] density-network outputs or null */
+    float *features;            /* [n][32] hash features or null */
+};
+
+struct CacheRay {
+    float3 o, d;
+    float far_, T;
+    int alive;
+};
+
+struct CacheBuildParams {
+    DevScene scene;
+    DevSteps steps;
+    DevCam cam;
+    DevGrid grid;
+    const uint8_t *bits;
+    const __half2 *table;
+    const uint2 *weights;
+    int latent_offset;
+    int bX, bY, bZ, fW, fH, fD, dX, dY, dZ, capacity;
+    CacheRay *rays;             /* [tiles][64] */
+    int *block_step;            /* [tiles] */
+    uint8_t *tile_alive;        /* [tiles] */
+    int *alive_list, *alive_list_next;
+    int *n_alive_tiles, *n_alive_next;
+    int *tile_n_samples;        /* [alive idx] */
+    uint8_t *tile_processed, *tile_need;
+    int *tile_n_alive;
+    void *staging;              /* [alive idx][512] voxels */
+    void *voxels;               /* [slots][512] voxels */
+    int32_t *packed_index;
+    float *known_ranges;
+    int *slot_counter;
+    int *jobs;                  /* [2 * tiles]: (alive idx, slot) */
+    int *n_jobs;
+    int *guard;
+    int max_search;
+};
+
+size_t render_smem_bytes();
+size_t build_smem_bytes();
+cudaError_t launch_render(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s);
+cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
+
+__global__ void cache_init_kernel(CacheBuildParams p);
+__global__ void cache_tile_kernel(CacheBuildParams p);
+__global__ void cache_assign_kernel(CacheBuildParams p);
+__global__ void cache_copy_kernel(CacheBuildParams p);
+__global__ void cache_known_ranges_kernel(CacheBuildParams p);
+__global__ void cache_compact_kernel(CacheBuildParams p, int n_tiles);
+
+}  // namespace fvc

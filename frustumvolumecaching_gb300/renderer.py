@@ -1,0 +1,266 @@
+"""Python mirror of the reference's renderer API over the C ABI.
+
+Same names and argument meanings as the reference's C++ classes
+(include/renderer.h, performance_renderer.h, cache_renderer.h,
+cache_performance_renderer.h, include/loader.h), so parity tests read like
+the reference's own call sites (src/eval.cu:208-227, 285-478):
+
+    loader = load_data(model_dir)
+    renderer = PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    renderer.resizeRenderbuffers((W, H))
+    renderer.render(rm_info, image_buffer)
+
+Errors are raised as FvcError (the reference throws std::runtime_error).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .camera import camera_dict, inverse
+
+RENDERER_BASIC, RENDERER_PERFORMANCE, RENDERER_CACHE_PERFORMANCE = 0, 1, 2
+
+
+class NerfNetwork:
+    """Loaded model (NerfNetwork<half> + the occupancy grid it came with)."""
+
+    def __init__(self, path: str):
+        lib = L.load()
+        h = C.c_void_p()
+        L.check(lib.fvc_model_load(path.encode(), C.byref(h)))
+        self.handle = h
+        self.path = path
+        self.scene_info = L.SceneInfo()
+        self.stepsize_info = L.StepsizeInfo()
+        L.check(lib.fvc_model_info(h, C.byref(self.scene_info), C.byref(self.stepsize_info)))
+
+    def inference(self, pos: np.ndarray, dir01: np.ndarray) -> np.ndarray:
+        """NerfNetwork::inference at given inputs: [n,4] = rgb logits, log-density."""
+        pos = np.ascontiguousarray(pos, np.float32)
+        dir01 = np.ascontiguousarray(dir01, np.float32)
+        out = np.zeros((pos.shape[0], 4), np.float32)
+        L.check(L.load().fvc_model_inference(self.handle, L.ptr(pos), L.ptr(dir01), pos.shape[0], L.ptr(out)))
+        return out
+
+    def density(self, pos: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float32)
+        out = np.zeros(pos.shape[0], np.float32)
+        L.check(L.load().fvc_model_density(self.handle, L.ptr(pos), pos.shape[0], L.ptr(out)))
+        return out
+
+    def debug_encode(self, pos: np.ndarray):
+        pos = np.ascontiguousarray(pos, np.float32)
+        f = np.zeros((pos.shape[0], 32), np.float32)
+        b = np.zeros((pos.shape[0], 16), np.float32)
+        L.check(L.load().fvc_model_debug_encode(self.handle, L.ptr(pos), pos.shape[0], L.ptr(f), L.ptr(b)))
+        return f, b
+
+    def __del__(self):
+        if getattr(self, "handle", None) and L._lib is not None:
+            L._lib.fvc_model_destroy(self.handle)
+            self.handle = None
+
+
+@dataclass
+class LoaderData:
+    """LoaderData, include/loader.h:32-47."""
+    scene_info: L.SceneInfo
+    stepsize_info: L.StepsizeInfo
+    nerf_network: NerfNetwork
+
+    @property
+    def occupancy_grid_morton_bitfield(self):
+        return self.nerf_network
+
+
+def load_data(path: str) -> LoaderData:
+    """load_data(fs::path, LoaderData&), src/loader.cu:287-300 (nerfacc export)."""
+    net = NerfNetwork(path)
+    return LoaderData(net.scene_info, net.stepsize_info, net)
+
+
+def camera_info(cam: dict) -> L.CameraInfo:
+    """CameraInfo from a camera dict of frustumvolumecaching_gb300.camera."""
+    ci = L.CameraInfo()
+    ci.resolution.x, ci.resolution.y = cam["resolution"]
+    ci.is_open_gl = int(bool(cam["is_open_gl"]))
+    ci.focal.x, ci.focal.y = cam["focal"]
+    ci.principal.x, ci.principal.y = cam["principal"]
+    c2w = np.asarray(cam["cam2world"], np.float32)
+    w2c = np.asarray(cam.get("world2cam", inverse(c2w)), np.float32)
+    for r, name in enumerate(["m0", "m1", "m2"]):
+        m = getattr(ci.cam2world, name)
+        m.x, m.y, m.z, m.w = [float(v) for v in c2w[r]]
+        m = getattr(ci.world2cam, name)
+        m.x, m.y, m.z, m.w = [float(v) for v in w2c[r]]
+    ci.aperature = 0.0
+    ci.focus_z = 1.0
+    return ci
+
+
+def raymarch_info(cam: dict, stepsize_info: L.StepsizeInfo, sample_index: int = 0) -> L.RaymarchInfo:
+    """RaymarchInfo as src/eval.cu:160-167 builds it (deterministic, no motion blur)."""
+    rm = L.RaymarchInfo()
+    rm.cam_info = camera_info(cam)
+    rm.next_cam_info = camera_info(cam)
+    rm.stepsize_info = stepsize_info
+    rm.sample_index = sample_index
+    rm.motion_blur = 0
+    rm.deterministic = 1
+    return rm
+
+
+class RenderBuffer:
+    """Headless image buffer (ImageBuffer, include/util/image_buffer.h) in host
+    memory: uchar4 image, float rgb+transmittance per ray, per-ray counts."""
+
+    def __init__(self, resolution):
+        W, H = resolution
+        self.resolution = (W, H)
+        self.image = np.zeros((H, W, 4), np.uint8)
+        self.results = np.zeros((H, W, 4), np.float32)
+        self.ray_counts = np.zeros((H, W, 4), np.int32)
+
+    def outputs(self) -> L.RenderOutputs:
+        o = L.RenderOutputs()
+        o.image_rgba8, o.results, o.ray_counts = L.ptr(self.image), L.ptr(self.results), L.ptr(self.ray_counts)
+        return o
+
+
+class Renderer:
+    """Renderer, include/renderer.h:77-119."""
+
+    kind = RENDERER_PERFORMANCE
+
+    def __init__(self, scene_info, occupancy_grid, nerf_network: NerfNetwork):
+        self._scene_info = scene_info
+        self._occupancy_grid = occupancy_grid
+        self._nerf_network = nerf_network
+        h = C.c_void_p()
+        L.check(L.load().fvc_renderer_create(nerf_network.handle, self.kind, C.byref(h)))
+        self.handle = h
+
+    def resizeRenderbuffers(self, resolution) -> None:
+        L.check(L.load().fvc_renderer_resize(self.handle, int(resolution[0]), int(resolution[1])))
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        L.check(L.load().fvc_renderer_set_stream(self.handle, stream_handle))
+
+    def set_max_samples_per_ray(self, n: int) -> None:
+        L.check(L.load().fvc_renderer_set_max_samples_per_ray(self.handle, n))
+
+    def render(self, rm_info: L.RaymarchInfo, render_buffer: RenderBuffer, debug_data=None) -> None:
+        """render(RaymarchInfo, RenderBuffer&) with host buffers (synchronous)."""
+        out = render_buffer.outputs()
+        L.check(L.load().fvc_render(self.handle, C.byref(rm_info), C.byref(out)))
+
+    def render_device(self, rm_info: L.RaymarchInfo, image=None, results=None, ray_counts=None) -> None:
+        """Enqueue a render into device buffers (pointers or torch tensors)."""
+        out = L.RenderOutputs()
+        out.image_rgba8, out.results, out.ray_counts = L.ptr(image), L.ptr(results), L.ptr(ray_counts)
+        L.check(L.load().fvc_render_device(self.handle, C.byref(rm_info), C.byref(out)))
+
+    @property
+    def _render_stats(self) -> L.RenderStats:
+        s = L.RenderStats()
+        L.check(L.load().fvc_render_stats(self.handle, C.byref(s)))
+        return s
+
+    def __del__(self):
+        if getattr(self, "handle", None) and L._lib is not None:
+            L._lib.fvc_renderer_destroy(self.handle)
+            self.handle = None
+
+
+class BasicRenderer(Renderer):
+    """BasicRenderer, include/basic_renderer.h (same method as PerformanceRenderer)."""
+    kind = RENDERER_BASIC
+
+
+class PerformanceRenderer(Renderer):
+    """PerformanceRenderer, include/performance_renderer.h:19-64."""
+    kind = RENDERER_PERFORMANCE
+
+
+class Cache:
+    """Cache, include/cache.h:12-74 (device storage owned by the library)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        L.check(L.load().fvc_cache_create(C.byref(h)))
+        self.handle = h
+
+    def dims(self):
+        f, b, d = L.Int3(), L.Int3(), L.Int3()
+        L.check(L.load().fvc_cache_dims(self.handle, C.byref(f), C.byref(b), C.byref(d)))
+        return (f.x, f.y, f.z), (b.x, b.y, b.z), (d.x, d.y, d.z)
+
+    def read(self, voxels: bool = True):
+        """packed brick index [bZ,bY,bX], known ranges [H,W], voxels [slots,512,8] u32 words."""
+        lib = L.load()
+        nb, nk, nv = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        L.check(lib.fvc_cache_read(self.handle, None, C.byref(nb), None, C.byref(nk), None, C.byref(nv)))
+        (fW, fH, fD), (bX, bY, bZ), _ = self.dims()
+        packed = np.zeros(nb.value, np.int32)
+        known = np.zeros(nk.value, np.float32)
+        vox = np.zeros(nv.value, np.uint32) if voxels else None
+        L.check(lib.fvc_cache_read(self.handle, L.ptr(packed), None, L.ptr(known), None, L.ptr(vox), None))
+        return packed.reshape(bZ, bY, bX), known.reshape(fH, fW), (vox.reshape(-1, 512, 8) if voxels else None)
+
+    def __del__(self):
+        if getattr(self, "handle", None) and L._lib is not None:
+            L._lib.fvc_cache_destroy(self.handle)
+            self.handle = None
+
+
+class CachePerformanceRenderer(Renderer):
+    """CachePerformanceRenderer, include/cache_performance_renderer.h:21-131,
+    with CacheRenderer's cache control (include/cache_renderer.h:34-109)."""
+
+    kind = RENDERER_CACHE_PERFORMANCE
+    ONLY_CACHE, ONLY_RESAMPLED, DEFAULT = 1, 2, 0
+
+    def __init__(self, scene_info, occupancy_grid, nerf_network, cache: Cache, next_cache: Cache):
+        super().__init__(scene_info, occupancy_grid, nerf_network)
+        self._cache, self._cache_next = cache, next_cache
+        L.check(L.load().fvc_renderer_set_caches(self.handle, cache.handle, next_cache.handle))
+
+    def resizeCache(self, resolution, stepsize_info) -> None:
+        L.check(L.load().fvc_cache_resize(self.handle, int(resolution[0]), int(resolution[1]), C.byref(stepsize_info)))
+
+    def initCacheBlockwise(self, rm_info: L.RaymarchInfo, debug_image_buffer=None) -> None:
+        L.check(L.load().fvc_cache_build(self.handle, C.byref(rm_info)))
+
+    def swapCache(self) -> None:
+        L.check(L.load().fvc_cache_swap(self.handle))
+        self._cache, self._cache_next = self._cache_next, self._cache
+
+    def setCacheSettings(self, settings: L.CacheSettings) -> None:
+        L.check(L.load().fvc_renderer_set_cache_settings(self.handle, C.byref(settings)))
+
+    def set_render_mode(self, mode: int) -> None:
+        L.check(L.load().fvc_renderer_set_render_mode(self.handle, mode))
+
+    @property
+    def _init_stats(self) -> L.CacheStats:
+        s = L.CacheStats()
+        L.check(L.load().fvc_cache_stats(self.handle, C.byref(s)))
+        return s
+
+
+def default_cache_settings() -> L.CacheSettings:
+    """CacheRenderer::default_cache_settings, include/cache_renderer.h:55-63."""
+    s = L.CacheSettings()
+    s.interpol_variant, s.interpol_function = 0, 0
+    s.use_hw_interpol = s.reweight_intermediates = s.disable_reweighting_first_intermediate = 1
+    s.use_inter_brick_interpolation = 1
+    return s
+
+
+__all__ = ["load_data", "LoaderData", "NerfNetwork", "Renderer", "BasicRenderer", "PerformanceRenderer", "Cache",
+           "CachePerformanceRenderer", "RenderBuffer", "raymarch_info", "camera_info", "camera_dict",
+           "default_cache_settings"]

@@ -1,0 +1,266 @@
+/*
+ * fvc.h - C ABI of the GB300 frustum-volume-caching NeRF renderer.
+ *
+ * Plain C (no CUDA, no torch types): every entry point takes plain pointers,
+ * sizes and POD structs, returns an int status (FVC_OK == 0) and records a
+ * thread-local message readable through fvc_last_error().
+ *
+ * The POD structs below have the byte layout of the reference's own structs
+ * (include/common.h:22-62 CameraMatrix, :74-91 SceneInfo, :93-164 StepsizeInfo,
+ * :166-195 CameraInfo, :210-218 RaymarchInfo; include/renderer_common.h:74-78
+ * BaseRayResult), so a caller holding the reference types can pass them by
+ * pointer unchanged.  fvc_abi.cpp static_asserts every size and offset.
+ *
+ * Each function names the reference interface it replaces.  Renderers render
+ * synchronously on their stream (the reference's render() is synchronous:
+ * src/performance_renderer.cu:283 CUDA_SYNC_CHECK_THROW); device-pointer
+ * variants (suffix _device) enqueue on the renderer's stream and return
+ * without synchronising, so a caller can time them with its own events.
+ */
+#ifndef FVC_H
+#define FVC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FVC_ALIGN(n) __attribute__((aligned(n)))
+#else
+#define FVC_ALIGN(n)
+#endif
+
+/* ---- status codes (reference: exceptions / bool returns, see each fn) ---- */
+#define FVC_OK 0
+#define FVC_ERR_CUDA 1          /* a CUDA runtime call failed                  */
+#define FVC_ERR_CONFIG 2        /* unsupported / malformed model or settings   */
+#define FVC_ERR_OOM 3           /* device allocation failed                    */
+#define FVC_ERR_CACHE_UNINIT 4  /* "Cache is not initialized!"                 */
+#define FVC_ERR_TIMEOUT 5       /* a bounded device wait ran out               */
+#define FVC_ERR_ARG 6           /* null handle / bad size / bad pointer        */
+#define FVC_ERR_IO 7            /* model file missing or truncated             */
+#define FVC_ERR_GUARD 8         /* a device-side guard fired (see message)     */
+
+/* ---- vector PODs with CUDA's alignment (float2/int2: 8, float4: 16) ---- */
+typedef struct FVC_ALIGN(8) { float x, y; } fvc_float2;
+typedef struct { float x, y, z; } fvc_float3;
+typedef struct FVC_ALIGN(16) { float x, y, z, w; } fvc_float4;
+typedef struct FVC_ALIGN(8) { int x, y; } fvc_int2;
+typedef struct { int x, y, z; } fvc_int3;
+
+/* CameraMatrix, include/common.h:22-62: 3x4 row-major [R|t]. */
+typedef struct { fvc_float4 m0, m1, m2; } fvc_camera_matrix;
+
+/* ContractionType, include/common.h:66-72. */
+enum { FVC_CONTRACTION_NONE = 0, FVC_CONTRACTION_AABB = 1,
+       FVC_CONTRACTION_WARP_AABB_L2 = 2, FVC_CONTRACTION_WARP_AABB_LINF = 3 };
+
+/* SceneInfo, include/common.h:74-91 (bool = 1 byte). */
+typedef struct {
+    int grid_resolution;
+    int grid_nlvl;
+    int vals_per_lvl;
+    uint8_t normalized;
+    fvc_float3 aabb_from;
+    fvc_float3 aabb_to;
+    fvc_float3 contraction_aabb_from;
+    fvc_float3 contraction_aabb_to;
+    int contraction_type;
+    uint8_t is_open_gl;
+    float alpha_thre;
+} fvc_scene_info;
+
+/* StepsizeInfo, include/common.h:93-164. */
+typedef struct {
+    float cone_angle, log1p_c, stepsize, near_, near_i, far_;
+    float dt_min, dt_max, t_min, t_max, i_min, i_max;
+} fvc_stepsize_info;
+
+/* CameraInfo, include/common.h:166-195. */
+typedef struct {
+    fvc_int2 resolution;
+    uint8_t is_open_gl;
+    fvc_float2 focal;
+    fvc_float2 principal;
+    fvc_camera_matrix cam2world;
+    fvc_camera_matrix world2cam;
+    float aperature;
+    float focus_z;
+} fvc_camera_info;
+
+/* RaymarchInfo, include/common.h:210-218. */
+typedef struct {
+    fvc_camera_info cam_info;
+    fvc_camera_info next_cam_info;
+    fvc_stepsize_info stepsize_info;
+    int sample_index;
+    uint8_t motion_blur;
+    uint8_t deterministic;
+} fvc_raymarch_info;
+
+/* BaseRayResult, include/renderer_common.h:74-78 (rgb + transmittance). */
+typedef struct FVC_ALIGN(16) { float r, g, b, transmittance; } fvc_ray_result;
+
+/* CacheSettings, include/cache_renderer.h:24-32 (enum fields as int). */
+typedef struct {
+    int interpol_variant;      /* DensityInterpolVariant: 0 Density (only one built) */
+    int interpol_function;     /* InterpolFunction: 0 Linear (only one built)       */
+    uint8_t use_hw_interpol;
+    uint8_t reweight_intermediates;
+    uint8_t disable_reweighting_first_intermediate;
+    uint8_t use_inter_brick_interpolation;
+} fvc_cache_settings;
+
+/* Renderer kinds: include/basic_renderer.h, performance_renderer.h,
+ * cache_performance_renderer.h. BASIC shares the PERFORMANCE kernels. */
+enum { FVC_RENDERER_BASIC = 0, FVC_RENDERER_PERFORMANCE = 1, FVC_RENDERER_CACHE_PERFORMANCE = 2 };
+
+/* Cache render modes: CachePerformanceRenderer::RenderMode
+ * (include/cache_performance_renderer.h). */
+enum { FVC_RENDER_MODE_DEFAULT = 0, FVC_RENDER_MODE_ONLY_CACHE = 1, FVC_RENDER_MODE_ONLY_RESAMPLED = 2 };
+
+typedef struct fvc_model fvc_model;
+typedef struct fvc_renderer fvc_renderer;
+typedef struct fvc_cache fvc_cache;
+
+/* Per-frame statistics: PerformanceRenderer::RenderStats and
+ * CachePerformanceRenderer::RenderStats / CacheRenderer::InitStats
+ * (include/performance_renderer.h:60-64, include/cache_renderer.h:104-109). */
+typedef struct {
+    double samples_ppx;              /* evaluated samples per pixel          */
+    long long n_samples;             /* samples evaluated (resample + cache) */
+    long long n_resamples;           /* samples through the full network     */
+    long long n_cache_hits;          /* samples served from the cache        */
+    long long n_dropped;             /* known-empty cache voxels skipped     */
+    long long n_steps;               /* marching steps taken                 */
+    int n_rounds;                    /* persistent-kernel rounds (max over warps) */
+    int guard_flags;                 /* device guard bits (0 = none fired)   */
+} fvc_render_stats_t;
+
+typedef struct {
+    int n_bricks_set;       /* bricks holding data                       */
+    int n_bricks_reserved;  /* brick capacity of the data array          */
+    int n_bricks_demanded;  /* allocations requested incl. overflowed    */
+    int overflow;           /* 1 if at least one allocation overflowed   */
+    int n_iterations;       /* depth-brick iterations of the build       */
+    long long n_samples;    /* samples evaluated by the density network  */
+} fvc_cache_stats_t;
+
+/* ------------------------------------------------------------------------ */
+/* errors                                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Thread-local message of the last failing call (reference: the what() of the
+ * std::runtime_error thrown by MY_CUDA_CHECK_THROW, include/util/cuda_helper.h:20-45). */
+const char *fvc_last_error(void);
+/* Library version string. */
+const char *fvc_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* model (reference: bool load_data(fs::path, LoaderData&), include/loader.h:49,   */
+/* src/loader.cu:232-300 nerfacc export: config.json + *.dat)                 */
+/* ------------------------------------------------------------------------ */
+int fvc_model_load(const char *data_dir, fvc_model **out);
+void fvc_model_destroy(fvc_model *m);
+/* Scene and step parameters of the loaded model (LoaderData::scene_info,
+ * ::stepsize_info after StepsizeInfo::setAdditionalInfo, include/common.h:109-131). */
+int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_stepsize_info *steps);
+/* Evaluate log-density (fp16-rounded density-network row 0) at n contracted
+ * positions pos[3*n] in [0,1]^3 (NerfNetwork::inferenceLatents row 0,
+ * include/nerf_network.h:173-202). Host buffers. */
+int fvc_model_density(fvc_model *m, const float *pos, int n, float *log_density_out);
+/* Full network at n samples: pos[3n] contracted, dir01[3n] = unit_to_01(dir);
+ * out[4n] = (rgb logits 0..2, log-density) as fp16-rounded floats
+ * (NerfNetwork::inference, include/nerf_network.h:160-171). Host buffers. */
+int fvc_model_inference(fvc_model *m, const float *pos, const float *dir01, int n, float *out);
+
+/* Diagnostics: hash-grid features features32[32n] and density-network
+ * outputs base_out16[16n] (fp16 values) at n contracted positions; either
+ * output may be NULL.  No reference counterpart (tcnn-internal values). */
+int fvc_model_debug_encode(fvc_model *m, const float *pos, int n, float *features32, float *base_out16);
+
+/* ------------------------------------------------------------------------ */
+/* renderers (reference: Renderer / PerformanceRenderer / CachePerformanceRenderer */
+/* constructors and virtual render / resizeRenderbuffers,                      */
+/* include/renderer.h:108-112, include/performance_renderer.h:22-26)          */
+/* ------------------------------------------------------------------------ */
+int fvc_renderer_create(fvc_model *m, int kind, fvc_renderer **out);
+void fvc_renderer_destroy(fvc_renderer *r);
+/* resizeRenderbuffers(int2), src/performance_renderer.cu:186-212. */
+int fvc_renderer_resize(fvc_renderer *r, int width, int height);
+/* Use the caller's CUDA stream (cudaStream_t as void*; NULL = internal stream). */
+int fvc_renderer_set_stream(fvc_renderer *r, void *cuda_stream);
+
+/* Output buffers of a render; any member may be NULL.
+ *   image_rgba8 [W*H*4]  uchar4 image after writeImageBuffer_performance_kernel
+ *                        (white background, progressive average over
+ *                        sample_index, src/performance_renderer.cu:127-149)
+ *   results     [W*H]    rgb + transmittance before background / quantisation
+ *                        (the final BaseRayResult of each ray)
+ *   ray_counts  [W*H*4]  per ray: composited resample samples, composited
+ *                        cache samples, known-empty cache voxels skipped,
+ *                        marching steps */
+typedef struct {
+    uint8_t *image_rgba8;
+    fvc_ray_result *results;
+    int32_t *ray_counts;
+} fvc_render_outputs;
+
+/* render(RaymarchInfo, RenderBuffer&, DebugData*) of the renderer's kind:
+ * PerformanceRenderer::render (src/performance_renderer.cu:214-286) or
+ * CachePerformanceRenderer::render (src/cache_performance_renderer.cu:1059-1263).
+ * Device pointers; enqueued on the renderer stream, not synchronised. */
+int fvc_render_device(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out);
+/* Same with host pointers: H2D of the previous image (progressive average),
+ * render, D2H of the outputs, synchronise. */
+int fvc_render(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out);
+/* Guard on the samples of one ray (0 = off, the reference default); a ray
+ * exceeding it sets a guard bit reported by fvc_render_stats. */
+int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
+/* Statistics of the last render (needs the stream synchronised). */
+int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *out);
+
+/* ------------------------------------------------------------------------ */
+/* frustum volume cache (reference: Cache, include/cache.h:12-74; CacheRenderer */
+/* resizeCache / initCacheBlockwise / swapCache / setCacheSettings,             */
+/* include/cache_renderer.h:243-267, src/cache_renderer.cu:832-1057)            */
+/* ------------------------------------------------------------------------ */
+int fvc_cache_create(fvc_cache **out);
+void fvc_cache_destroy(fvc_cache *c);
+/* Attach the render cache and the build cache ("next") to a cache renderer:
+ * CacheRenderer(..., Cache* cache, Cache* next_cache). They may be the same. */
+int fvc_renderer_set_caches(fvc_renderer *r, fvc_cache *cache, fvc_cache *next_cache);
+/* resizeCache(int2 resolution, StepsizeInfo), src/cache_renderer.cu:832-846. */
+int fvc_cache_resize(fvc_renderer *r, int width, int height, const fvc_stepsize_info *steps);
+/* setCacheSettings, include/cache_renderer.h:266-267. Only the reference
+ * defaults with interpol_variant Density are built (others -> FVC_ERR_CONFIG). */
+int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_settings *s);
+/* initCacheBlockwise(RaymarchInfo, RenderBuffer&), src/cache_renderer.cu:931-1051:
+ * fills the "next" cache. Synchronous. */
+int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info);
+/* swapCache(), src/cache_renderer.cu:1053-1057. */
+int fvc_cache_swap(fvc_renderer *r);
+int fvc_cache_stats(fvc_renderer *r, fvc_cache_stats_t *out);
+/* Cache render mode (CachePerformanceRenderer::_render_mode). */
+int fvc_renderer_set_render_mode(fvc_renderer *r, int mode);
+
+/* Copy cache tables to host for inspection (sizes in elements are returned
+ * through *_n when the destination pointer is NULL):
+ *   packed_index[bricks]  int32, pack3D(slot) or -1, x fastest
+ *                          (Cache::_packed_brick_index_array_3D)
+ *   known_ranges[W*H]     float (Cache::_known_ranges_to)
+ *   voxels[8*slots*512]   float: density, isset, 0, 0, then 4 words of
+ *                          8 fp16 latents, per voxel, slot-major   */
+int fvc_cache_read(fvc_cache *c, int32_t *packed_index, size_t *packed_index_n,
+                   float *known_ranges, size_t *known_ranges_n,
+                   uint32_t *voxels, size_t *voxels_n);
+/* Frustum dims (W, H, D), brick dims and data bricks per dim. */
+int fvc_cache_dims(fvc_cache *c, fvc_int3 *frustum_dims, fvc_int3 *brick_dims, fvc_int3 *data_bricks_per_dim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVC_H */

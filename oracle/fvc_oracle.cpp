@@ -1,0 +1,858 @@
+/*
+ * fvc_oracle.cpp - CPU oracle for the frustum-volume-caching renderer.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The product never links, loads or calls this
+ * file; tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it
+ * as the checker.
+ *
+ * A scalar restatement of the reference's hot path:
+ *   - marcher index math in float32, operation for operation in the order the
+ *     reference writes it (include/raymarch_common.h, include/common.h),
+ *     compiled with -ffp-contract=off so it is bit-identical to the device;
+ *   - network (hash grid + MLPs) and compositing in float64;
+ *   - cache build and cached render as single-pass loops equivalent to the
+ *     reference's sub-iterated kernels, with deterministic brick slots
+ *     (iteration-major, then tile index) in place of the reference's
+ *     atomicAdd order.
+ * Each function cites the reference lines it restates.  The hash grid and
+ * MLP restate the published Instant-NGP method (tiny-cuda-nn is not in the
+ * reference tree); parity against tiny-cuda-nn itself is unpinned.
+ */
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../frustumvolumecaching_gb300/csrc/fvc_detmath.h"
+
+namespace {
+
+struct V3 { float x, y, z; };
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+
+/* ---------------- parameter blocks passed from Python (ctypes) ----------- */
+extern "C" {
+struct OrcScene {
+    int grid_nlvl; int normalized; int contraction; int is_open_gl;
+    float aabb_from[3], aabb_to[3], c_from[3], c_to[3];
+    float alpha_thre;
+};
+struct OrcSteps {  /* StepsizeInfo, include/common.h:93-107, plus L_lo */
+    float cone_angle, log1p_c, stepsize, near_, near_i, far_;
+    float dt_min, dt_max, t_min, t_max, i_min, i_max;
+    float log1p_c_lo; int use_libm;
+};
+struct OrcCam {    /* CameraInfo, include/common.h:166-180 */
+    int W, H; int is_open_gl; float fx, fy, px, py;
+    float c2w[12]; float w2c[12];
+};
+struct OrcNet {
+    int n_levels, F;
+    float scale[32]; uint32_t res[32], size[32], offset[32], dense[32];
+    const uint16_t *table;   /* fp16 bits */
+    int width, enc_w, enc_w_pad, base_out_pad;
+    const uint16_t *base_w;  /* [width x enc_w_pad] then [base_out_pad x width] */
+    int head_layers;         /* number of weight matrices in the head (3 = 2 hidden) */
+    int head_in, head_in_pad, n_latents, latent_offset;
+    const uint16_t *head_w;  /* [width x head_in_pad], [width x width]*, [16 x width] */
+    int mimic_fp16;          /* round layer outputs to fp16 like the reference */
+};
+}
+
+/* ---------------- fp16 helpers ---------------- */
+inline double h2d(uint16_t h)
+{
+    const int s = h >> 15, e = (h >> 10) & 31, m = h & 1023;
+    double v;
+    if (e == 0) v = std::ldexp((double)m, -24);
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = std::ldexp((double)(m | 1024), e - 25);
+    return s ? -v : v;
+}
+inline double round_h(double x) { return (double)(_Float16)(float)x; }
+inline uint16_t d2h_bits(double x) { _Float16 h = (_Float16)(float)x; uint16_t b; std::memcpy(&b, &h, 2); return b; }
+
+/* ---------------- step grid: StepsizeInfo, include/common.h:133-163 ------ */
+inline float t_from_step(const OrcSteps &s, float step)
+{
+    if (s.cone_angle <= 0.0f) return step * s.dt_min;
+    if (step >= s.i_max) return s.t_max + (step - s.i_max) * s.dt_max;
+    if (step < s.i_min) return step * s.dt_min;
+    if (s.use_libm) return s.t_min * powf(1.f + s.cone_angle, step - s.i_min);
+    return s.t_min * fvc_pow_1pc(step - s.i_min, s.log1p_c, s.log1p_c_lo);
+}
+inline float step_from_t(const OrcSteps &s, float t)
+{
+    if (s.cone_angle <= 0.0f) return t / s.dt_min;
+    if (t >= s.t_max) return (t - s.t_max) / s.dt_max + s.i_max;
+    if (t < s.t_min) return t / s.dt_min;
+    const float lg = s.use_libm ? logf(t / s.t_min) : fvc_logf(t / s.t_min);
+    return lg / s.log1p_c + s.i_min;
+}
+/* calculate_stepsize + clamp, include/raymarch_common.h:274-284,
+ * include/util/helper_math.h:1169-1172 */
+inline float calc_step(const OrcSteps &s, float t)
+{
+    return fmaxf(s.dt_min, fminf(t * s.cone_angle, s.dt_max));
+}
+/* valid_t_from_t, include/raymarch_common.h:286-296 */
+inline float valid_t_from_t(const OrcSteps &s, float t)
+{
+    return t_from_step(s, roundf(step_from_t(s, fmaxf(t, s.near_)) - s.near_i) + s.near_i);
+}
+
+/* ---------------- vector helpers in the reference's order --------------- */
+inline float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float dot4(float ax, float ay, float az, float aw, const float *m)
+{
+    return ax * m[0] + ay * m[1] + az * m[2] + aw * m[3];
+}
+
+struct Ray { V3 o, d; };
+
+/* generateRayDir + generateRay (deterministic), include/raymarch_common.h:190-251 */
+inline Ray generate_ray(const OrcCam &c, int px, int py)
+{
+    const float sx = (float)px + 0.5f, sy = (float)py + 0.5f;
+    const float sgn = c.is_open_gl ? -1.f : 1.f;
+    const float dx = (sx - c.px) / c.fx;
+    const float dy = (sy - c.py) / c.fy * sgn;
+    const float dz = sgn;
+    V3 d = v3(dot4(dx, dy, dz, 0.f, c.c2w), dot4(dx, dy, dz, 0.f, c.c2w + 4), dot4(dx, dy, dz, 0.f, c.c2w + 8));
+    /* normalize(): rsqrtf as the reference header evaluates it on the host
+     * (nvcc host math: 1/sqrt in double, rounded once to float). */
+    const float inv = (float)(1.0 / std::sqrt((double)dot3(d, d)));
+    d = v3(d.x * inv, d.y * inv, d.z * inv);
+    return Ray{v3(c.c2w[3], c.c2w[7], c.c2w[11]), d};
+}
+
+/* ray_aabb_intersect, include/raymarch_common.h:482-532 */
+inline bool ray_aabb(const Ray &r, const float *from, const float *to, float &tn, float &tf)
+{
+    float tmin = (from[0] - r.o.x) / r.d.x, tmax = (to[0] - r.o.x) / r.d.x;
+    if (tmin > tmax) std::swap(tmin, tmax);
+    float tymin = (from[1] - r.o.y) / r.d.y, tymax = (to[1] - r.o.y) / r.d.y;
+    if (tymin > tymax) std::swap(tymin, tymax);
+    if (tmin > tymax || tymin > tmax) { tn = 1e10f; tf = 1e10f; return false; }
+    if (tymin > tmin) tmin = tymin;
+    if (tymax < tmax) tmax = tymax;
+    float tzmin = (from[2] - r.o.z) / r.d.z, tzmax = (to[2] - r.o.z) / r.d.z;
+    if (tzmin > tzmax) std::swap(tzmin, tzmax);
+    if (tmin > tzmax || tzmin > tmax) { tn = 1e10f; tf = 1e10f; return false; }
+    if (tzmin > tmin) tmin = tzmin;
+    if (tzmax < tmax) tmax = tzmax;
+    tn = tmin; tf = tmax;
+    return true;
+}
+
+/* morton3D, include/raymarch_common.h:98-110 */
+inline uint32_t expand_bits(uint32_t v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+inline uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) { return expand_bits(x) | (expand_bits(y) << 1) | (expand_bits(z) << 2); }
+inline uint32_t compact_bits(uint32_t x)  /* morton3D_invert, :90-97 */
+{
+    x = x & 0x49249249u;
+    x = (x | (x >> 2)) & 0xc30c30c3u;
+    x = (x | (x >> 4)) & 0x0f00f00fu;
+    x = (x | (x >> 8)) & 0xff0000ffu;
+    x = (x | (x >> 16)) & 0x0000ffffu;
+    return x;
+}
+
+constexpr int R = 128;  /* DEFAULT_GRID_RESOLUTION, include/renderer_common.h:10 */
+
+/* grid_occupied_at<128, true>, include/raymarch_common.h:660-710 */
+inline bool occupied(const OrcScene &sc, const uint8_t *bits, V3 p, int *cell_out = nullptr)
+{
+    V3 u = p;
+    if (!sc.normalized) {
+        const float s = (float)(1 << (sc.grid_nlvl - 1));
+        u = v3((p.x - sc.aabb_from[0] / s) / ((sc.aabb_to[0] - sc.aabb_from[0]) / s),
+               (p.y - sc.aabb_from[1] / s) / ((sc.aabb_to[1] - sc.aabb_from[1]) / s),
+               (p.z - sc.aabb_from[2] / s) / ((sc.aabb_to[2] - sc.aabb_from[2]) / s));
+    }
+    const float mx = fmaxf(fmaxf(fabsf(u.x - 0.5f), fabsf(u.y - 0.5f)), fabsf(u.z - 0.5f));
+    int e;
+    frexpf(mx, &e);
+    const int mip = std::max(0, e + 1);
+    if (mip >= sc.grid_nlvl) { if (cell_out) *cell_out = -1; return false; }
+    const float sm = scalbnf(1.0f, -mip);
+    const int ix = (int)(((u.x - 0.5f) * sm + 0.5f) * (float)R);
+    const int iy = (int)(((u.y - 0.5f) * sm + 0.5f) * (float)R);
+    const int iz = (int)(((u.z - 0.5f) * sm + 0.5f) * (float)R);
+    const int idx = (int)morton3((uint32_t)ix, (uint32_t)iy, (uint32_t)iz);
+    const int bidx = idx / 8 + (R * R * R * mip) / 8;
+    if (cell_out) *cell_out = bidx * 8 + idx % 8;
+    return (bits[bidx] & (1 << (idx % 8))) != 0;
+}
+
+/* apply_contraction, include/raymarch_common.h:610-653 */
+inline V3 contract(const OrcScene &sc, V3 p)
+{
+    if (sc.contraction == 1) {
+        return v3((p.x - sc.aabb_from[0]) / (sc.aabb_to[0] - sc.aabb_from[0]),
+                  (p.y - sc.aabb_from[1]) / (sc.aabb_to[1] - sc.aabb_from[1]),
+                  (p.z - sc.aabb_from[2]) / (sc.aabb_to[2] - sc.aabb_from[2]));
+    }
+    if (sc.contraction == 2 || sc.contraction == 3) {
+        V3 u = v3((p.x - sc.c_from[0]) / (sc.c_to[0] - sc.c_from[0]) * 2.0f - 1.0f,
+                  (p.y - sc.c_from[1]) / (sc.c_to[1] - sc.c_from[1]) * 2.0f - 1.0f,
+                  (p.z - sc.c_from[2]) / (sc.c_to[2] - sc.c_from[2]) * 2.0f - 1.0f);
+        const float n = sc.contraction == 3 ? fmaxf(fmaxf(fabsf(u.x), fabsf(u.y)), fabsf(u.z)) : sqrtf(dot3(u, u));
+        const float f = fmaxf(n, 1.0f);
+        const float k = 2.0f - 1.0f / f;
+        return v3(k * (u.x / f) / 4.0f + 0.5f, k * (u.y / f) / 4.0f + 0.5f, k * (u.z / f) / 4.0f + 0.5f);
+    }
+    return p;
+}
+
+/* transformRay, include/raymarch_common.h:253-262 */
+inline Ray transform_ray(const Ray &r, const float *m)
+{
+    return Ray{v3(dot4(r.o.x, r.o.y, r.o.z, 1.0f, m), dot4(r.o.x, r.o.y, r.o.z, 1.0f, m + 4), dot4(r.o.x, r.o.y, r.o.z, 1.0f, m + 8)),
+               v3(dot4(r.d.x, r.d.y, r.d.z, 0.0f, m), dot4(r.d.x, r.d.y, r.d.z, 0.0f, m + 4), dot4(r.d.x, r.d.y, r.d.z, 0.0f, m + 8))};
+}
+inline V3 at(const Ray &r, float t) { return v3(r.o.x + t * r.d.x, r.o.y + t * r.d.y, r.o.z + t * r.d.z); }
+
+/* cam2froxel, include/raymarch_common.h:316-329 */
+inline V3 cam2froxel(V3 c, const OrcCam &cam, const OrcSteps &st, float &t)
+{
+    const float sgn = cam.is_open_gl ? -1.f : 1.f;
+    const float z = c.z * sgn;
+    t = sqrtf(dot3(c, c));
+    return v3(c.x / z * cam.fx + cam.px, c.y * sgn / z * cam.fy + cam.py,
+              (step_from_t(st, t) - st.near_i) * (c.z < 0.0f ? -1.0f : 1.0f));
+}
+
+/* ---------------- network (float64) ---------------- */
+struct NetD {
+    const OrcNet *n;
+    std::vector<double> table, bw0, bw1, hw[4];
+};
+
+void prepare_net(const OrcNet *n, NetD &d)
+{
+    d.n = n;
+    size_t n_entries = (size_t)n->offset[n->n_levels - 1] + n->size[n->n_levels - 1];
+    d.table.resize(n_entries * n->F);
+    for (size_t i = 0; i < d.table.size(); ++i) d.table[i] = h2d(n->table[i]);
+    d.bw0.resize((size_t)n->width * n->enc_w_pad);
+    d.bw1.resize((size_t)n->base_out_pad * n->width);
+    for (size_t i = 0; i < d.bw0.size(); ++i) d.bw0[i] = h2d(n->base_w[i]);
+    for (size_t i = 0; i < d.bw1.size(); ++i) d.bw1[i] = h2d(n->base_w[d.bw0.size() + i]);
+    size_t off = 0;
+    for (int l = 0; l < n->head_layers; ++l) {
+        const int in = l == 0 ? n->head_in_pad : n->width;
+        const int out = l == n->head_layers - 1 ? 16 : n->width;
+        d.hw[l].resize((size_t)in * out);
+        for (size_t i = 0; i < d.hw[l].size(); ++i) d.hw[l][i] = h2d(n->head_w[off + i]);
+        off += (size_t)in * out;
+    }
+}
+
+/* Hash-grid encoding (Instant-NGP multiresolution hash grid): the corner and
+ * fraction in float32 exactly as the device computes them (p = fma(scale, x,
+ * 0.5), floor, subtract), weights and sums in float64. */
+void hash_encode(const NetD &d, V3 pos, double *feat)
+{
+    const OrcNet &n = *d.n;
+    const float px[3] = {pos.x, pos.y, pos.z};
+    for (int l = 0; l < n.n_levels; ++l) {
+        uint32_t g[3]; double fr[3];
+        for (int k = 0; k < 3; ++k) {
+            const float p = fmaf(n.scale[l], px[k], 0.5f);
+            const float fl = floorf(p);
+            g[k] = (uint32_t)(int)fl;
+            fr[k] = (double)(p - fl);
+        }
+        double acc[8] = {0};
+        for (int c = 0; c < 8; ++c) {
+            uint32_t q[3]; double w = 1.0;
+            for (int k = 0; k < 3; ++k) {
+                const int b = (c >> k) & 1;
+                q[k] = g[k] + (uint32_t)b;
+                w *= b ? fr[k] : 1.0 - fr[k];
+            }
+            uint32_t idx;
+            if (n.dense[l]) idx = q[0] + q[1] * n.res[l] + q[2] * n.res[l] * n.res[l];
+            else idx = (q[0] * 1u) ^ (q[1] * 2654435761u) ^ (q[2] * 805459861u);
+            idx %= n.size[l];
+            const double *e = &d.table[((size_t)n.offset[l] + idx) * n.F];
+            for (int f = 0; f < n.F; ++f) acc[f] += w * e[f];
+        }
+        for (int f = 0; f < n.F; ++f) feat[l * n.F + f] = n.mimic_fp16 ? round_h(acc[f]) : acc[f];
+    }
+    for (int i = n.n_levels * n.F; i < n.enc_w_pad; ++i) feat[i] = 0.0;
+}
+
+inline void dense_layer(const double *W, int out, int in, const double *x, double *y, bool relu, bool mimic)
+{
+    for (int o = 0; o < out; ++o) {
+        double s = 0.0;
+        const double *w = W + (size_t)o * in;
+        for (int i = 0; i < in; ++i) s += w[i] * x[i];
+        if (relu && s < 0.0) s = 0.0;
+        y[o] = mimic ? round_h(s) : s;
+    }
+}
+
+/* density network: NerfNetwork::inferenceLatents, include/nerf_network.h:173-202 */
+void base_forward(const NetD &d, V3 pos, double *out /* base_out_pad */)
+{
+    const OrcNet &n = *d.n;
+    double feat[64], h[128];
+    hash_encode(d, pos, feat);
+    dense_layer(d.bw0.data(), n.width, n.enc_w_pad, feat, h, true, n.mimic_fp16);
+    dense_layer(d.bw1.data(), n.base_out_pad, n.width, h, out, false, n.mimic_fp16);
+}
+
+/* SH degree 4 of unit_to_01 directions: x = 2*d01 - 1 (the constants of
+ * src/my_fully_fused_mlp.cu:216-233, Sloan's real SH) */
+void sh16(const float *d01, double *o)
+{
+    const double x = (double)(d01[0] * 2.f - 1.f), y = (double)(d01[1] * 2.f - 1.f), z = (double)(d01[2] * 2.f - 1.f);
+    const double xy = x * y, xz = x * z, yz = y * z, x2 = x * x, y2 = y * y, z2 = z * z;
+    const double pi = 3.14159265358979323846;
+    const double c0 = 1.0 / (2.0 * std::sqrt(pi)), c1 = std::sqrt(3.0) / (2.0 * std::sqrt(pi));
+    const double c2a = std::sqrt(15.0) / (2.0 * std::sqrt(pi)), c2b = std::sqrt(5.0) / (4.0 * std::sqrt(pi));
+    const double c2c = std::sqrt(15.0) / (4.0 * std::sqrt(pi)), c3a = std::sqrt(70.0) / (8.0 * std::sqrt(pi));
+    const double c3b = std::sqrt(105.0) / (2.0 * std::sqrt(pi)), c3c = std::sqrt(42.0) / (8.0 * std::sqrt(pi));
+    const double c3d = std::sqrt(7.0) / (4.0 * std::sqrt(pi)), c3e = std::sqrt(105.0) / (4.0 * std::sqrt(pi));
+    o[0] = c0; o[1] = -c1 * y; o[2] = c1 * z; o[3] = -c1 * x;
+    o[4] = c2a * xy; o[5] = -c2a * yz; o[6] = c2b * (3.0 * z2 - 1.0); o[7] = -c2a * xz;
+    o[8] = c2c * (x2 - y2); o[9] = c3a * y * (-3.0 * x2 + y2); o[10] = c3b * xy * z;
+    o[11] = c3c * y * (1.0 - 5.0 * z2); o[12] = c3d * z * (5.0 * z2 - 3.0); o[13] = c3c * x * (1.0 - 5.0 * z2);
+    o[14] = c3e * z * (x2 - y2); o[15] = c3a * x * (-x2 + 3.0 * y2);
+}
+
+/* color head: NerfNetwork::inferenceHead, include/nerf_network.h:204-257
+ * (latents, SH4 of the direction, padding with 1.0 to the padded width) */
+void head_forward(const NetD &d, const double *latents, const float *dir01, double *rgb_logits)
+{
+    const OrcNet &n = *d.n;
+    double in[128], a[128], b[128];
+    for (int i = 0; i < n.n_latents; ++i) in[i] = latents[i];
+    sh16(dir01, in + n.n_latents);
+    if (n.mimic_fp16) for (int i = n.n_latents; i < n.n_latents + 16; ++i) in[i] = round_h(in[i]);
+    for (int i = n.head_in; i < n.head_in_pad; ++i) in[i] = 1.0;
+    dense_layer(d.hw[0].data(), n.width, n.head_in_pad, in, a, true, n.mimic_fp16);
+    double *x = a, *y = b;
+    for (int l = 1; l < n.head_layers - 1; ++l) {
+        dense_layer(d.hw[l].data(), n.width, n.width, x, y, true, n.mimic_fp16);
+        std::swap(x, y);
+    }
+    double out[16];
+    dense_layer(d.hw[n.head_layers - 1].data(), 16, n.width, x, out, false, n.mimic_fp16);
+    for (int i = 0; i < 3; ++i) rgb_logits[i] = out[i];
+}
+
+inline double sigmoid(double x) { return 1.0 / (1.0 + std::exp(-x)); }
+
+/* one compositing step, accumulate_performance_kernel,
+ * src/performance_renderer.cu:101-120; returns true when T < 1e-4 */
+inline bool composite(double sigma, const double *logit, float dt, float alpha_thre, double *rgb, double &T)
+{
+    double alpha = 1.0 - std::exp(-sigma * (double)dt);
+    alpha = std::min(1.0, std::max(0.0, alpha));
+    if (alpha > (double)alpha_thre) {
+        const double w = alpha * T;
+        for (int k = 0; k < 3; ++k) rgb[k] += w * sigmoid(logit[k]);
+        T *= 1.0 - alpha;
+    }
+    return T < 1e-4;
+}
+
+template <class F>
+void parallel_rows(int n, int n_threads, F fn)
+{
+    if (n_threads <= 1) { for (int i = 0; i < n; ++i) fn(i); return; }
+    std::atomic<int> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t)
+        th.emplace_back([&]() { for (int i; (i = next.fetch_add(1)) < n;) fn(i); });
+    for (auto &t : th) t.join();
+}
+
+}  // namespace
+
+/* ========================================================================== */
+extern "C" {
+
+/* StepsizeInfo::setAdditionalInfo, include/common.h:109-131 (host double). */
+void orc_setup_steps(const OrcScene *sc, OrcSteps *s)
+{
+    s->dt_min = s->stepsize;
+    s->dt_max = fmaxf(fmaxf((sc->aabb_to[0] - sc->aabb_from[0]) / R * 1.732f, (sc->aabb_to[1] - sc->aabb_from[1]) / R * 1.732f),
+                      (sc->aabb_to[2] - sc->aabb_from[2]) / R * 1.732f);
+    s->t_min = ((double)s->dt_min) / s->cone_angle;
+    const double d_i_min = 1.0 / s->cone_angle;
+    s->i_min = d_i_min;
+    const double d_log1p_c = std::log(1.0 + s->cone_angle);
+    s->log1p_c = d_log1p_c;
+    s->log1p_c_lo = (float)(d_log1p_c - (double)s->log1p_c);
+    const double d_i_max = std::log(s->dt_max / (double)s->dt_min) / d_log1p_c + d_i_min;
+    s->i_max = d_i_max;
+    s->t_max = s->t_min * std::pow(1.0 + s->cone_angle, d_i_max - d_i_min);
+    s->near_i = step_from_t(*s, s->near_);
+}
+
+/* Morton bitfield from the export's uint8 grid (l*R^3 + x*R^2 + y*R + z):
+ * occupancy_grid_to_morton_kernel + uchar_to_bitfield, src/loader.cu:20-55. */
+void orc_grid_to_morton_bits(const uint8_t *grid, int nlvl, uint8_t *bits)
+{
+    const int vals = R * R * R;
+    std::memset(bits, 0, (size_t)vals * nlvl / 8);
+    for (int i = 0; i < vals * nlvl; ++i) {
+        const int lvl = i / vals, j = i % vals;
+        const uint32_t x = compact_bits((uint32_t)j), y = compact_bits((uint32_t)j >> 1), z = compact_bits((uint32_t)j >> 2);
+        if (grid[(size_t)lvl * vals + x * R * R + y * R + z]) bits[i / 8] |= (uint8_t)(1u << (i % 8));
+    }
+}
+
+/* Per-ray march trace for golden comparisons: sample_performance_kernel's
+ * step loop (src/performance_renderer.cu:39-62) without compositing.
+ * Writes per step the bits of t0 and the occupancy bit; returns steps. */
+int orc_trace_ray(const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                  int px, int py, int max_steps, uint32_t *t0_bits, uint8_t *occ, float *init /* start_t, far, hits */)
+{
+    const Ray r = generate_ray(*cam, px, py);
+    float tn, tf;
+    const bool hits = ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf);
+    const float far_ = hits ? fminf(tf, st->far_) : st->far_;
+    const float start = hits ? valid_t_from_t(*st, tn) : st->near_;
+    init[0] = start; init[1] = far_; init[2] = hits ? 1.f : 0.f;
+    if (!hits) return 0;
+    float t1 = start + 0.0f;
+    int n = 0;
+    for (; n < max_steps; ++n) {
+        const float t0 = t1;
+        const float dt = calc_step(*st, t0);
+        t1 = t0 + dt;
+        const float tm = (t0 + t1) * 0.5f;
+        if (tm > far_) break;
+        std::memcpy(&t0_bits[n], &t0, 4);
+        occ[n] = occupied(*sc, bits, at(r, tm)) ? 1 : 0;
+    }
+    return n;
+}
+
+/* Single-point helpers for golden vectors. */
+float orc_step_from_t(const OrcSteps *st, float t) { return step_from_t(*st, t); }
+float orc_t_from_step(const OrcSteps *st, float s) { return t_from_step(*st, s); }
+int orc_occupied(const OrcScene *sc, const uint8_t *bits, const float *p, int *cell)
+{
+    return occupied(*sc, bits, v3(p[0], p[1], p[2]), cell) ? 1 : 0;
+}
+void orc_contract(const OrcScene *sc, const float *p, float *out)
+{
+    V3 c = contract(*sc, v3(p[0], p[1], p[2]));
+    out[0] = c.x; out[1] = c.y; out[2] = c.z;
+}
+float orc_logf(float x) { return fvc_logf(x); }
+float orc_expf(float x) { return fvc_expf(x); }
+
+/* Network evaluation at given inputs (float64): out[4n] = rgb logits, log-density. */
+void orc_inference(const OrcNet *net, const float *pos, const float *dir01, int n, double *out, int n_threads)
+{
+    NetD d; prepare_net(net, d);
+    parallel_rows(n, n_threads, [&](int i) {
+        double bo[64];
+        base_forward(d, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), bo);
+        double lg[3];
+        head_forward(d, bo + net->latent_offset, dir01 + 3 * i, lg);
+        out[4 * i + 0] = lg[0]; out[4 * i + 1] = lg[1]; out[4 * i + 2] = lg[2]; out[4 * i + 3] = bo[0];
+    });
+}
+void orc_hash_encode(const OrcNet *net, const float *pos, int n, double *feat_out)
+{
+    NetD d; prepare_net(net, d);
+    for (int i = 0; i < n; ++i) hash_encode(d, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), feat_out + (size_t)i * net->enc_w_pad);
+}
+
+/* Plain render: PerformanceRenderer::render (src/performance_renderer.cu:214-286)
+ * as a single pass per ray (sub-iterations only batch the same sample sequence).
+ * results[4*W*H] = rgb, transmittance; n_samples[W*H]; n_steps[W*H]. */
+int orc_render_plain(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                     int row0, int row1, float *results, int32_t *n_samples, int32_t *n_steps, int n_threads)
+{
+    NetD d; prepare_net(net, d);
+    const int W = cam->W;
+    parallel_rows(row1 - row0, n_threads, [&](int rr) {
+        const int y = row0 + rr;
+        for (int x = 0; x < W; ++x) {
+            const size_t id = (size_t)y * W + x;
+            const Ray r = generate_ray(*cam, x, y);
+            float tn, tf;
+            const bool hits = ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf);
+            double rgb[3] = {0, 0, 0}, T = 1.0;
+            int ns = 0, nst = 0;
+            if (hits) {
+                const float far_ = fminf(tf, st->far_);
+                float t1 = valid_t_from_t(*st, tn) + 0.0f;
+                const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
+                for (;;) {
+                    const float t0 = t1;
+                    const float dt = calc_step(*st, t0);
+                    t1 = t0 + dt;
+                    const float tm = (t0 + t1) * 0.5f;
+                    ++nst;
+                    if (tm > far_) break;
+                    const V3 wp = at(r, tm);
+                    if (!occupied(*sc, bits, wp)) continue;
+                    double bo[64], lg[3];
+                    base_forward(d, contract(*sc, wp), bo);
+                    head_forward(d, bo + net->latent_offset, d01, lg);
+                    ++ns;
+                    if (composite(std::exp(bo[0]), lg, dt, sc->alpha_thre, rgb, T)) break;
+                }
+            }
+            results[4 * id + 0] = (float)rgb[0]; results[4 * id + 1] = (float)rgb[1];
+            results[4 * id + 2] = (float)rgb[2]; results[4 * id + 3] = (float)T;
+            if (n_samples) n_samples[id] = ns;
+            if (n_steps) n_steps[id] = nst;
+        }
+    });
+    return 0;
+}
+
+/* ---------------- frustum volume cache ---------------- */
+struct OrcCacheDims {
+    int fW, fH, fD;           /* frustum dims */
+    int bX, bY, bZ;           /* brick dims = ceil(frustum / 8) */
+    int dX, dY, dZ;           /* data bricks per dim (128, 128, z) */
+};
+
+/* CacheRenderer::resizeCache + Cache::resize (src/cache_renderer.cu:832-846,
+ * src/cache.cu:44-84). */
+void orc_cache_dims(const OrcScene *sc, const OrcSteps *st, int W, int H, OrcCacheDims *cd)
+{
+    const int n_rays = W * H;
+    const int est_samples = n_rays * 32;               /* INIT_ESTIMATED_N_SAMPLES_PER_RAY */
+    const int est_per_brick = (int)(0.5f * powf(8.0f, 3.0f)); /* INIT_ESTIMATED_BRICK_SPARSITY * 8^3 */
+    const int est_bricks = est_samples / est_per_brick;
+    const float dx = sc->aabb_to[0] - sc->aabb_from[0], dy = sc->aabb_to[1] - sc->aabb_from[1], dz = sc->aabb_to[2] - sc->aabb_from[2];
+    const float diag = sqrtf(dx * dx + dy * dy + dz * dz);  /* max_step_in_scene, include/raymarch_common.h:298-303 */
+    const int max_n_steps = (int)ceilf(step_from_t(*st, diag + st->near_));
+    const int depth = (max_n_steps + 3) / 4 * 4;
+    cd->fW = W; cd->fH = H; cd->fD = depth;
+    cd->bX = (W + 7) / 8; cd->bY = (H + 7) / 8; cd->bZ = (depth + 7) / 8;
+    cd->dX = 1024 / 8; cd->dY = 1024 / 8;
+    cd->dZ = (est_bricks + cd->dX * cd->dY - 1) / (cd->dX * cd->dY);
+}
+
+struct OrcCache {
+    OrcCacheDims dims;
+    int32_t *packed_index;   /* [bZ][bY][bX] (x fastest), pack3D(slot) or -1 */
+    float *known_ranges;     /* [H][W] */
+    float *vox_density;      /* [slots][512] */
+    float *vox_isset;        /* [slots][512] */
+    uint16_t *vox_latents;   /* [slots][512][8] fp16 */
+    /* stats out */
+    int n_bricks_set, n_demanded, n_iterations;
+    long long n_samples;
+    int32_t *slot_of_brick_order; /* optional: [capacity] tile index per slot (may be NULL) */
+};
+
+inline int pack3(int x, int y, int z) { return (x << 20) | (y << 10) | z; }
+
+/* Cache build: CacheRenderer::initCacheBlockwise and its kernels
+ * (src/cache_renderer.cu:18-569, 931-1051) with brick slots assigned in
+ * (iteration, tile index) order.  The cache camera's rays are generated
+ * per 8x8 tile including pixels beyond the image (as the reference does). */
+int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                    OrcCache *cc, int n_threads)
+{
+    NetD d; prepare_net(net, d);
+    const OrcCacheDims &cd = cc->dims;
+    const int nT = cd.bX * cd.bY;
+    const int capacity = cd.dX * cd.dY * cd.dZ;
+    struct RayS { Ray r; float far_; bool alive; double T; };
+    std::vector<RayS> rays((size_t)nT * 64);
+    std::vector<int> block_step(nT), alive_tile(nT), n_bricks(nT, 0);
+    std::fill(cc->packed_index, cc->packed_index + (size_t)cd.bX * cd.bY * cd.bZ, -1);
+    /* initPayloads_cache_init_kernel, :18-81 */
+    for (int t = 0; t < nT; ++t) {
+        const int tx = t % cd.bX, ty = t / cd.bX;
+        int n_alive = 0, min_start = 1 << 30;
+        for (int k = 0; k < 64; ++k) {
+            const int px = tx * 8 + (k % 8), py = ty * 8 + (k / 8);
+            RayS &rs = rays[(size_t)t * 64 + k];
+            rs.r = generate_ray(*cam, px, py);
+            float tn, tf;
+            const bool hits = ray_aabb(rs.r, sc->aabb_from, sc->aabb_to, tn, tf);
+            n_alive += hits;
+            const int start_step = std::max(0, (int)(step_from_t(*st, hits ? tn : st->near_) - st->near_i));
+            min_start = std::min(min_start, start_step);
+            rs.far_ = hits ? fminf(tf, st->far_) : st->far_;
+            rs.alive = hits; rs.T = 1.0;
+        }
+        block_step[t] = min_start / 8;
+        alive_tile[t] = n_alive > 0;
+    }
+    int counter = 0;
+    long long n_samples = 0;
+    int iter = 0;
+    struct TileWork { int n_steps; int need; std::vector<uint8_t> mask; std::vector<double> sig, lat; };
+    std::vector<TileWork> work(nT);
+    for (; iter < 1000; ++iter) {
+        std::vector<int> alive_list;
+        for (int t = 0; t < nT; ++t) if (alive_tile[t]) alive_list.push_back(t);
+        if (alive_list.empty()) break;
+        /* sample_cache_init_first_kernel (:83-190): find the next depth brick
+         * holding an occupied sample, then the network and the density-only
+         * compositing of accumulateNew_cache_init_second_kernel (:289-528). */
+        parallel_rows((int)alive_list.size(), n_threads, [&](int ai) {
+            const int t = alive_list[ai];
+            TileWork &w = work[t];
+            w.n_steps = 0; w.need = 0;
+            w.mask.assign(64, 0);
+            RayS *rs = &rays[(size_t)t * 64];
+            int total = 0;
+            for (;;) {
+                int n_alive = 0;
+                for (int k = 0; k < 64; ++k) n_alive += rs[k].alive;
+                if (n_alive <= 0) break;
+                /* bricks beyond the frustum depth (camera outside the scene
+                 * box) have no storage: the tile stops there */
+                if (block_step[t] >= cd.bZ) { for (int k = 0; k < 64; ++k) rs[k].alive = false; total = 0; break; }
+                const float t1s = t_from_step(*st, (float)(block_step[t] * 8) + st->near_i);
+                total = 0;
+                for (int k = 0; k < 64; ++k) {
+                    float t1 = t1s; uint8_t m = 0;
+                    for (int s = 0; s < 8; ++s) {
+                        const float t0 = t1; const float dt = calc_step(*st, t0); t1 = t0 + dt;
+                        const float tm = (t0 + t1) * 0.5f;
+                        if (tm > rs[k].far_) rs[k].alive = false;
+                        else if (occupied(*sc, bits, at(rs[k].r, tm))) { m |= (uint8_t)(1u << s); ++total; }
+                    }
+                    w.mask[k] = m;
+                }
+                if (total > 0) break;
+                block_step[t]++;
+            }
+            int n_alive = 0;
+            for (int k = 0; k < 64; ++k) n_alive += rs[k].alive;
+            alive_tile[t] = n_alive > 0;
+            w.n_steps = total;
+            if (total == 0 || !alive_tile[t]) return;
+            w.sig.assign(64 * 8, 0.0); w.lat.assign(64 * 8 * 8, 0.0);
+            const float t1s = t_from_step(*st, (float)(block_step[t] * 8) + st->near_i);
+            int visible = 0;
+            for (int k = 0; k < 64; ++k) {
+                float t1 = t1s;
+                double T = rs[k].T;
+                for (int s = 0; s < 8; ++s) {
+                    const float t0 = t1; const float dt = calc_step(*st, t0); t1 = t0 + dt;
+                    const float tm = (t0 + t1) * 0.5f;
+                    if (tm > rs[k].far_) { rs[k].alive = false; continue; }
+                    if (!(w.mask[k] >> s & 1)) continue;
+                    double bo[64];
+                    base_forward(d, contract(*sc, at(rs[k].r, tm)), bo);
+                    const double sigma = std::exp(bo[0]);
+                    double alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-sigma * (double)dt)));
+                    if (alpha > (double)sc->alpha_thre) { T *= 1.0 - alpha; ++visible; }
+                    if (T < 1e-4) rs[k].alive = false;
+                    w.sig[k * 8 + s] = sigma;
+                    for (int j = 0; j < 8; ++j) w.lat[(k * 8 + s) * 8 + j] = bo[net->latent_offset + j];
+                }
+                rs[k].T = T;
+            }
+            w.need = visible > 0;
+        });
+        /* deterministic slot assignment (tile order within the iteration) and fill */
+        for (int t : alive_list) n_samples += work[t].n_steps;  /* emitted and evaluated (:1003-1026) */
+        for (int t : alive_list) {
+            TileWork &w = work[t];
+            const bool processed = w.n_steps > 0 && !w.sig.empty();
+            if (!processed) continue;  /* reference returns early: no update */
+            RayS *rs = &rays[(size_t)t * 64];
+            int overflow = 0;
+            if (w.need) {
+                const int slot = counter++;
+                overflow = slot >= capacity;
+                const int tx = t % cd.bX, ty = t / cd.bX, bz = block_step[t];
+                const size_t bidx = ((size_t)bz * cd.bY + ty) * cd.bX + tx;
+                if (!overflow) {
+                    const int sx = slot / (cd.dY * cd.dZ), sy = (slot - sx * cd.dY * cd.dZ) / cd.dZ, sz = slot - sx * cd.dY * cd.dZ - sy * cd.dZ;
+                    cc->packed_index[bidx] = pack3(sx, sy, sz);
+                    n_bricks[t]++;
+                    for (int k = 0; k < 64; ++k)
+                        for (int s = 0; s < 8; ++s) {
+                            const size_t v = (size_t)slot * 512 + (size_t)s * 64 + k;
+                            if (w.mask[k] >> s & 1) {
+                                cc->vox_density[v] = (float)w.sig[k * 8 + s];
+                                cc->vox_isset[v] = 1.0f;
+                                for (int j = 0; j < 8; ++j) cc->vox_latents[v * 8 + j] = d2h_bits(w.lat[(k * 8 + s) * 8 + j]);
+                            }
+                        }
+                } else {
+                    cc->packed_index[bidx] = -1;
+                }
+            }
+            int n_alive = 0;
+            for (int k = 0; k < 64; ++k) n_alive += rs[k].alive;
+            block_step[t] += overflow ? 0 : 1;
+            alive_tile[t] = !overflow && n_alive > 0;
+            w.sig.clear();
+        }
+    }
+    /* writeImageBuffer_cache_init_kernel2, :530-569: known_ranges_to */
+    for (int t = 0; t < nT; ++t) {
+        const int tx = t % cd.bX, ty = t / cd.bX;
+        const float tr = t_from_step(*st, (float)(block_step[t] * 8) + st->near_i);
+        for (int k = 0; k < 64; ++k) {
+            const int px = tx * 8 + (k % 8), py = ty * 8 + (k / 8);
+            if (px < cd.fW && py < cd.fH) cc->known_ranges[(size_t)py * cd.fW + px] = tr;
+        }
+    }
+    int set = 0;
+    for (int t = 0; t < nT; ++t) set += n_bricks[t];
+    cc->n_bricks_set = set;
+    cc->n_demanded = counter;
+    cc->n_iterations = iter;
+    cc->n_samples = n_samples;
+    return 0;
+}
+
+/* voxel lookup through the data array's texel addressing (tex3D point with
+ * border addressing, include/util/cuda_readwrite_array.h:41-62) */
+struct Vox { double density, isset, lat[8]; };
+inline bool fetch_texel(const OrcCache &cc, int X, int Y, int Z, Vox &v)
+{
+    const OrcCacheDims &cd = cc.dims;
+    if (X < 0 || Y < 0 || Z < 0 || X >= cd.dX * 8 || Y >= cd.dY * 8 || Z >= cd.dZ * 8) return false;
+    const int slot = (X / 8) * cd.dY * cd.dZ + (Y / 8) * cd.dZ + (Z / 8);
+    const size_t i = (size_t)slot * 512 + (size_t)(Z % 8) * 64 + (Y % 8) * 8 + (X % 8);
+    v.density = cc.vox_density[i]; v.isset = cc.vox_isset[i];
+    for (int j = 0; j < 8; ++j) v.lat[j] = h2d(cc.vox_latents[i * 8 + j]);
+    return true;
+}
+
+inline int brick_lookup(const OrcCache &cc, int bx, int by, int bz)
+{
+    const OrcCacheDims &cd = cc.dims;
+    return cc.packed_index[((size_t)bz * cd.bY + by) * cd.bX + bx];
+}
+
+/* Cached render: CachePerformanceRenderer::render and its kernels
+ * (src/cache_performance_renderer.cu:22-313, 678-908, 1059-1263) as one pass
+ * per ray.  counts[4*W*H]: resample, cache, dropped, steps. */
+int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                      const OrcCache *cc, const OrcCam *ccam, const OrcSteps *cst, int mode,
+                      int row0, int row1, float *results, int32_t *counts, int n_threads)
+{
+    NetD d; prepare_net(net, d);
+    const OrcCacheDims &cd = cc->dims;
+    const int W = cam->W;
+    parallel_rows(row1 - row0, n_threads, [&](int rr) {
+        const int y = row0 + rr;
+        for (int x = 0; x < W; ++x) {
+            const size_t id = (size_t)y * W + x;
+            const Ray r = generate_ray(*cam, x, y);
+            float tn, tf;
+            const bool hits = ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf);
+            double rgb[3] = {0, 0, 0}, T = 1.0;
+            int n_res = 0, n_cache = 0, n_drop = 0, nst = 0;
+            if (hits) {
+                const Ray rc = transform_ray(r, ccam->w2c);
+                const float far_ = fminf(tf, st->far_);
+                float t1 = valid_t_from_t(*st, tn) + 0.0f;
+                const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
+                for (;;) {
+                    const float t0 = t1;
+                    const float dt = calc_step(*st, t0);
+                    t1 = t0 + dt;
+                    const float tm = (t0 + t1) * 0.5f;
+                    ++nst;
+                    if (tm > far_) break;
+                    const V3 wp = at(r, tm);
+                    if (!occupied(*sc, bits, wp)) continue;
+                    /* classification, sample_cache_performance_kernel :91-163 */
+                    float tfr;
+                    const V3 fp = cam2froxel(at(rc, tm), *ccam, *cst, tfr);
+                    const bool in_fov = fp.x >= 0 && fp.x < (float)cd.fW && fp.y >= 0 && fp.y < (float)cd.fH;
+                    const bool inside = in_fov && fp.z >= 0 && fp.z < (float)cd.fD;
+                    bool unsampled = true;
+                    if (in_fov) {
+                        const float kr = cc->known_ranges[(size_t)(int)floorf(fp.y) * cd.fW + (int)floorf(fp.x)];
+                        unsampled = tfr < cst->near_ || tfr > kr;
+                    }
+                    int kind = 0; /* 0 resample, 1 cache, 2 drop */
+                    if (!inside || unsampled) {
+                        if (mode == 1) continue;
+                        kind = 0;
+                    } else {
+                        if (mode == 2) continue;
+                        const int bx = (int)(fp.x / 8.0f), by = (int)(fp.y / 8.0f), bz = (int)(fp.z / 8.0f);
+                        const int packed = brick_lookup(*cc, bx, by, bz);
+                        kind = 2;
+                        if (packed >= 0) {
+                            const float ix = fp.x - (float)(bx * 8), iy = fp.y - (float)(by * 8), iz = fp.z - (float)(bz * 8);
+                            const float ax = (float)(((packed >> 20) & 1023) * 8) + ix;
+                            const float ay = (float)(((packed >> 10) & 1023) * 8) + iy;
+                            const float az = (float)((packed & 1023) * 8) + iz;
+                            Vox v;
+                            if (fetch_texel(*cc, (int)floorf(ax), (int)floorf(ay), (int)floorf(az), v) && v.density > 0.0) kind = 1;
+                        }
+                        if (kind == 2) { ++n_drop; continue; }
+                    }
+                    const float tmh = t0 + dt * 0.5f;  /* generateNetworkInput_* :234, :287 */
+                    double sigma, lg[3];
+                    if (kind == 0) {
+                        double bo[64];
+                        base_forward(d, contract(*sc, at(r, tmh)), bo);
+                        head_forward(d, bo + net->latent_offset, d01, lg);
+                        sigma = std::exp(bo[0]);
+                        ++n_res;
+                    } else {
+                        /* generateNetworkInput_cache_shfl_perf_kernel_cg :678-787 */
+                        float tfr2;
+                        const V3 f2 = cam2froxel(at(rc, tmh), *ccam, *cst, tfr2);
+                        const float fx0 = floorf(f2.x - 0.5f), fy0 = floorf(f2.y - 0.5f), fz0 = floorf(f2.z - 0.5f);
+                        const double lt[3] = {(double)(f2.x - 0.5f - fx0), (double)(f2.y - 0.5f - fy0), (double)(f2.z - 0.5f - fz0)};
+                        double wsum = 0, dsum = 0, lsum[8] = {0};
+                        for (int c = 0; c < 8; ++c) {
+                            const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+                            const double w = (ox ? lt[0] : 1.0 - lt[0]) * (oy ? lt[1] : 1.0 - lt[1]) * (oz ? lt[2] : 1.0 - lt[2]);
+                            const float cx = fx0 + (float)ox, cy = fy0 + (float)oy, cz = fz0 + (float)oz;
+                            const bool fov = cx >= 0 && cx < (float)cd.fW && cy >= 0 && cy < (float)cd.fH;
+                            if (!(fov && cz >= 0 && cz < (float)cd.fD)) continue;
+                            const int bx = (int)(cx / 8.0f), by = (int)(cy / 8.0f), bz = (int)(cz / 8.0f);
+                            const int packed = brick_lookup(*cc, bx, by, bz);
+                            if (packed < 0) continue;
+                            const int X = ((packed >> 20) & 1023) * 8 + ((int)cx - bx * 8);
+                            const int Y = ((packed >> 10) & 1023) * 8 + ((int)cy - by * 8);
+                            const int Z = (packed & 1023) * 8 + ((int)cz - bz * 8);
+                            Vox v;
+                            if (!fetch_texel(*cc, X, Y, Z, v)) continue;
+                            wsum += w * v.isset; dsum += w * v.density;
+                            for (int j = 0; j < 8; ++j) lsum[j] += w * v.lat[j];
+                        }
+                        double lat[8];
+                        for (int j = 0; j < 8; ++j) lat[j] = lsum[j] / wsum;
+                        head_forward(d, lat, d01, lg);
+                        sigma = std::max(dsum, 1e-6);
+                        ++n_cache;
+                    }
+                    if (composite(sigma, lg, dt, sc->alpha_thre, rgb, T)) break;
+                }
+            }
+            results[4 * id + 0] = (float)rgb[0]; results[4 * id + 1] = (float)rgb[1];
+            results[4 * id + 2] = (float)rgb[2]; results[4 * id + 3] = (float)T;
+            if (counts) { counts[4 * id] = n_res; counts[4 * id + 1] = n_cache; counts[4 * id + 2] = n_drop; counts[4 * id + 3] = nst; }
+        }
+    });
+    return 0;
+}
+
+}  /* extern "C" */

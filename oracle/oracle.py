@@ -1,0 +1,292 @@
+"""ctypes binding of the CPU oracle (fvc_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's cpu_baseline leg as the checker.  The product package never
+imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfvc_oracle.so")
+
+F3 = C.c_float * 3
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("grid_nlvl", C.c_int), ("normalized", C.c_int), ("contraction", C.c_int), ("is_open_gl", C.c_int),
+                ("aabb_from", F3), ("aabb_to", F3), ("c_from", F3), ("c_to", F3), ("alpha_thre", C.c_float)]
+
+
+class OrcSteps(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ["cone_angle", "log1p_c", "stepsize", "near_", "near_i", "far_", "dt_min",
+                                         "dt_max", "t_min", "t_max", "i_min", "i_max", "log1p_c_lo"]] + [("use_libm", C.c_int)]
+
+
+class OrcCam(C.Structure):
+    _fields_ = [("W", C.c_int), ("H", C.c_int), ("is_open_gl", C.c_int), ("fx", C.c_float), ("fy", C.c_float),
+                ("px", C.c_float), ("py", C.c_float), ("c2w", C.c_float * 12), ("w2c", C.c_float * 12)]
+
+
+class OrcNet(C.Structure):
+    _fields_ = [("n_levels", C.c_int), ("F", C.c_int), ("scale", C.c_float * 32), ("res", C.c_uint32 * 32),
+                ("size", C.c_uint32 * 32), ("offset", C.c_uint32 * 32), ("dense", C.c_uint32 * 32),
+                ("table", C.c_void_p), ("width", C.c_int), ("enc_w", C.c_int), ("enc_w_pad", C.c_int),
+                ("base_out_pad", C.c_int), ("base_w", C.c_void_p), ("head_layers", C.c_int), ("head_in", C.c_int),
+                ("head_in_pad", C.c_int), ("n_latents", C.c_int), ("latent_offset", C.c_int), ("head_w", C.c_void_p),
+                ("mimic_fp16", C.c_int)]
+
+
+class OrcCacheDims(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ["fW", "fH", "fD", "bX", "bY", "bZ", "dX", "dY", "dZ"]]
+
+
+class OrcCache(C.Structure):
+    _fields_ = [("dims", OrcCacheDims), ("packed_index", C.c_void_p), ("known_ranges", C.c_void_p),
+                ("vox_density", C.c_void_p), ("vox_isset", C.c_void_p), ("vox_latents", C.c_void_p),
+                ("n_bricks_set", C.c_int), ("n_demanded", C.c_int), ("n_iterations", C.c_int),
+                ("n_samples", C.c_longlong), ("slot_of_brick_order", C.c_void_p)]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "fvc_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-C", HERE, "_build/libfvc_oracle.so"], check=True, capture_output=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        P = C.POINTER
+        _lib.orc_setup_steps.argtypes = [P(OrcScene), P(OrcSteps)]
+        _lib.orc_grid_to_morton_bits.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_trace_ray.argtypes = [P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_trace_ray.restype = C.c_int
+        _lib.orc_step_from_t.argtypes = [P(OrcSteps), C.c_float]
+        _lib.orc_step_from_t.restype = C.c_float
+        _lib.orc_t_from_step.argtypes = [P(OrcSteps), C.c_float]
+        _lib.orc_t_from_step.restype = C.c_float
+        _lib.orc_occupied.argtypes = [P(OrcScene), C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_contract.argtypes = [P(OrcScene), C.c_void_p, C.c_void_p]
+        _lib.orc_logf.argtypes = [C.c_float]
+        _lib.orc_logf.restype = C.c_float
+        _lib.orc_expf.argtypes = [C.c_float]
+        _lib.orc_expf.restype = C.c_float
+        _lib.orc_inference.argtypes = [P(OrcNet), C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        _lib.orc_hash_encode.argtypes = [P(OrcNet), C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_render_plain.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, C.c_int, C.c_int,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_cache_dims.argtypes = [P(OrcScene), P(OrcSteps), C.c_int, C.c_int, P(OrcCacheDims)]
+        _lib.orc_cache_build.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache), C.c_int]
+        _lib.orc_render_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
+                                           P(OrcCam), P(OrcSteps), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                           C.c_int]
+    return _lib
+
+
+def ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def default_threads() -> int:
+    return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1)
+
+
+def make_scene(cfg_scene: dict) -> OrcScene:
+    s = OrcScene()
+    s.grid_nlvl = int(cfg_scene["grid_nlvl"])
+    s.normalized = 0
+    a = cfg_scene["aabb"]
+    s.aabb_from[:] = a[:3]
+    s.aabb_to[:] = a[3:]
+    if "contraction" in cfg_scene and "aabb" in cfg_scene["contraction"]:
+        s.contraction = 3
+        ca = cfg_scene["contraction"]["aabb"]
+        s.c_from[:] = ca[:3]
+        s.c_to[:] = ca[3:]
+    else:
+        s.contraction = 1
+    s.is_open_gl = int(bool(cfg_scene.get("is_open_gl", False)))
+    s.alpha_thre = float(cfg_scene["alpha_thre"])
+    return s
+
+
+def make_steps(scene: OrcScene, cone: float, stepsize: float, near: float, far: float, use_libm: bool = False) -> OrcSteps:
+    st = OrcSteps()
+    st.cone_angle, st.stepsize, st.near_, st.far_ = cone, stepsize, near, far
+    st.use_libm = int(use_libm)
+    lib().orc_setup_steps(C.byref(scene), C.byref(st))
+    return st
+
+
+def make_cam(cam: dict) -> OrcCam:
+    c = OrcCam()
+    c.W, c.H = cam["resolution"]
+    c.is_open_gl = int(bool(cam["is_open_gl"]))
+    c.fx, c.fy = cam["focal"]
+    c.px, c.py = cam["principal"]
+    c.c2w[:] = np.asarray(cam["cam2world"], np.float32).ravel().tolist()
+    c.w2c[:] = np.asarray(cam["world2cam"], np.float32).ravel().tolist()
+    return c
+
+
+class OracleModel:
+    """A nerfacc-format export held for the oracle (parsed independently of
+    the product's C++ loader)."""
+
+    def __init__(self, model_dir: str, mimic_fp16: bool = False, use_libm: bool = False):
+        from frustumvolumecaching_gb300.model import hash_grid_levels
+        with open(os.path.join(model_dir, "config.json")) as f:
+            cfg = json.load(f)
+        self.cfg = cfg
+        sc = cfg["scene"]
+        self.scene = make_scene(sc)
+        self.steps = make_steps(self.scene, sc["cone_angle"], sc["stepsize"], sc["near"], sc["far"], use_libm)
+        enc = cfg["mlp_base"]["encoding"]
+        self.levels = hash_grid_levels(enc["n_levels"], enc["base_resolution"], enc["per_level_scale"], enc["log2_hashmap_size"])
+        if "fvc_level_scales" in enc:
+            for lv, sc in zip(self.levels, enc["fvc_level_scales"]):
+                assert np.float32(sc) == np.float32(lv.scale)
+                lv.scale = float(np.float32(sc))
+        F = enc["n_features_per_level"]
+        self.table = np.fromfile(os.path.join(model_dir, "pos_enc.dat"), np.uint16)
+        n_entries = self.levels[-1].offset + self.levels[-1].size
+        assert self.table.size == n_entries * F, "pos_enc.dat size does not match the hash-grid layout"
+        width = cfg["mlp_base"]["network"]["n_neurons"]
+        enc_w = enc["n_levels"] * F
+        enc_w_pad = (enc_w + 15) // 16 * 16
+        n_out = cfg["mlp_base"]["n_output"]
+        base_out_pad = (n_out + 15) // 16 * 16
+        self.base_w = np.fromfile(os.path.join(model_dir, "mlp_base.dat"), np.uint16)
+        assert self.base_w.size == width * enc_w_pad + base_out_pad * width
+        head = cfg["mlp_head"]
+        n_hidden = head["network"]["n_hidden_layers"]
+        first_lat_dens = bool(head.get("first_latent_is_density", True))
+        n_lat = int(head.get("n_latents", n_out))
+        head_in = int(head.get("n_input", 16 + n_lat))
+        head_in_pad = (head_in + 15) // 16 * 16
+        self.head_w = np.fromfile(os.path.join(model_dir, "mlp_head.dat"), np.uint16)
+        assert self.head_w.size == width * head_in_pad + (n_hidden - 1) * width * width + 16 * width
+        grid = np.fromfile(os.path.join(model_dir, "occupancy_grid.dat"), np.uint8)
+        self.grid = grid
+        self.bits = np.zeros(grid.size // 8, np.uint8)
+        lib().orc_grid_to_morton_bits(ptr(grid), self.scene.grid_nlvl, ptr(self.bits))
+        n = OrcNet()
+        n.n_levels, n.F = enc["n_levels"], F
+        for i, lv in enumerate(self.levels):
+            n.scale[i], n.res[i], n.size[i], n.offset[i], n.dense[i] = lv.scale, lv.res, lv.size, lv.offset, int(lv.dense)
+        n.table = ptr(self.table)
+        n.width, n.enc_w, n.enc_w_pad, n.base_out_pad = width, enc_w, enc_w_pad, base_out_pad
+        n.base_w = ptr(self.base_w)
+        n.head_layers = n_hidden + 1
+        n.head_in, n.head_in_pad, n.n_latents = head_in, head_in_pad, n_lat
+        n.latent_offset = 0 if first_lat_dens else 1
+        n.head_w = ptr(self.head_w)
+        n.mimic_fp16 = int(mimic_fp16)
+        self.net = n
+
+    # -- evaluation --------------------------------------------------------
+    def inference(self, pos: np.ndarray, dir01: np.ndarray, threads: int | None = None) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float32)
+        dir01 = np.ascontiguousarray(dir01, np.float32)
+        out = np.zeros((pos.shape[0], 4), np.float64)
+        lib().orc_inference(C.byref(self.net), ptr(pos), ptr(dir01), pos.shape[0], ptr(out), threads or default_threads())
+        return out
+
+    def hash_encode(self, pos: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float32)
+        out = np.zeros((pos.shape[0], self.net.enc_w_pad), np.float64)
+        lib().orc_hash_encode(C.byref(self.net), ptr(pos), pos.shape[0], ptr(out))
+        return out
+
+    def render_plain(self, cam: dict, rows: tuple[int, int] | None = None, threads: int | None = None):
+        c = make_cam(cam)
+        W, H = c.W, c.H
+        r0, r1 = rows or (0, H)
+        res = np.zeros((H, W, 4), np.float32)
+        ns = np.zeros((H, W), np.int32)
+        nst = np.zeros((H, W), np.int32)
+        lib().orc_render_plain(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
+                               r0, r1, ptr(res), ptr(ns), ptr(nst), threads or default_threads())
+        return res, ns, nst
+
+    def cache_dims(self, W: int, H: int, steps: OrcSteps | None = None) -> OrcCacheDims:
+        d = OrcCacheDims()
+        lib().orc_cache_dims(C.byref(self.scene), C.byref(steps or self.steps), W, H, C.byref(d))
+        return d
+
+    def cache_build(self, cam: dict, threads: int | None = None) -> "OracleCache":
+        c = make_cam(cam)
+        cc = OracleCache(self.cache_dims(c.W, c.H), cam)
+        lib().orc_cache_build(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
+                              C.byref(cc.s), threads or default_threads())
+        return cc
+
+    def render_cached(self, cam: dict, cache: "OracleCache", mode: int = 0, rows=None, threads: int | None = None):
+        c = make_cam(cam)
+        cc = make_cam(cache.cam)
+        W, H = c.W, c.H
+        r0, r1 = rows or (0, H)
+        res = np.zeros((H, W, 4), np.float32)
+        counts = np.zeros((H, W, 4), np.int32)
+        lib().orc_render_cached(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
+                                C.byref(cache.s), C.byref(cc), C.byref(self.steps), mode, r0, r1, ptr(res), ptr(counts),
+                                threads or default_threads())
+        return res, counts
+
+
+class OracleCache:
+    def __init__(self, dims: OrcCacheDims, cam: dict):
+        self.cam = cam
+        self.dims = dims
+        nb = dims.bX * dims.bY * dims.bZ
+        slots = dims.dX * dims.dY * dims.dZ
+        self.packed_index = np.full(nb, -1, np.int32)
+        self.known_ranges = np.zeros(dims.fW * dims.fH, np.float32)
+        self.vox_density = np.zeros(slots * 512, np.float32)
+        self.vox_isset = np.zeros(slots * 512, np.float32)
+        self.vox_latents = np.zeros(slots * 512 * 8, np.uint16)
+        s = OrcCache()
+        s.dims = dims
+        s.packed_index, s.known_ranges = ptr(self.packed_index), ptr(self.known_ranges)
+        s.vox_density, s.vox_isset, s.vox_latents = ptr(self.vox_density), ptr(self.vox_isset), ptr(self.vox_latents)
+        s.slot_of_brick_order = None
+        self.s = s
+
+    @property
+    def n_bricks_set(self):
+        return self.s.n_bricks_set
+
+    @property
+    def n_demanded(self):
+        return self.s.n_demanded
+
+
+def composite_image(results: np.ndarray, sample_index: int = 0, prev: np.ndarray | None = None) -> np.ndarray:
+    """writeImageBuffer_performance_kernel (src/performance_renderer.cu:127-149):
+    white background, int(c*256) clamped to [0,255], progressive average."""
+    rgb = results[..., :3] + results[..., 3:4]
+    if prev is not None and sample_index > 0:
+        rgb = (rgb + prev[..., :3].astype(np.float32) / 255.0 * sample_index) / float(sample_index + 1)
+    q = np.clip((rgb.astype(np.float32) * 256.0).astype(np.int64), 0, 255).astype(np.uint8)
+    out = np.full(results.shape[:2] + (4,), 255, np.uint8)
+    out[..., :3] = q
+    return out
+
+
+def psnr(a: np.ndarray, b: np.ndarray, peak: float = 1.0) -> float:
+    mse = float(np.mean((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2))
+    return float("inf") if mse == 0 else 10.0 * math.log10(peak * peak / mse)

@@ -1,0 +1,229 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Bit-exact: per-ray step and sample counts, sample classification in the
+cached render, brick slot assignment, known ranges.  Within tolerance: pixel
+colours (max-abs 2e-3 against the float64 oracle, PSNR printed), network
+outputs, cached voxel data.
+"""
+import json
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+import frustumvolumecaching_gb300 as fvc
+from frustumvolumecaching_gb300 import camera as fcam
+from frustumvolumecaching_gb300 import model as fmodel
+from oracle import oracle as orc
+from tests.golden.golden_scenes import SCENES, occupancy_grid, pixels
+from tests.helpers import psnr, small_camera, tiny_model
+
+pytestmark = pytest.mark.gpu
+
+COLOR_ATOL = 2e-3  # max-abs pixel tolerance against the float64 oracle
+
+
+@pytest.fixture(scope="module")
+def model1():
+    d = tiny_model(7, 1)
+    return fvc.load_data(d), orc.OracleModel(d), d
+
+
+@pytest.fixture(scope="module")
+def model3():
+    d = tiny_model(9, 3)
+    return fvc.load_data(d), orc.OracleModel(d), d
+
+
+def test_network_matches_oracle(model1):
+    loader, om, _ = model1
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0, 1, (5000, 3)).astype(np.float32)
+    d01 = rng.uniform(0, 1, (5000, 3)).astype(np.float32)
+    gpu = loader.nerf_network.inference(pos, d01)
+    ref = om.inference(pos, d01)
+    assert np.abs(gpu - ref).max() < 1e-3, np.abs(gpu - ref).max(axis=0)
+    feats, base = loader.nerf_network.debug_encode(pos)
+    ref_f = om.hash_encode(pos)[:, :32]
+    assert np.abs(feats - ref_f).max() < 3e-5
+
+
+def _render(renderer_cls, loader, cam, **kw):
+    r = renderer_cls(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, **kw)
+    r.resizeRenderbuffers(cam["resolution"])
+    buf = fvc.RenderBuffer(cam["resolution"])
+    return r, buf
+
+
+@pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
+def test_plain_render_parity(request, fixture, W, H):
+    loader, om, _ = request.getfixturevalue(fixture)
+    cam = small_camera(1001, W, H)
+    r, buf = _render(fvc.PerformanceRenderer, loader, cam)
+    r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
+    ref, ns, nst = om.render_plain(cam)
+    # sample counts and steps per ray: bit-exact (rays that did not terminate early)
+    live = ref[..., 3] >= 1e-4
+    np.testing.assert_array_equal(buf.ray_counts[..., 0], ns)
+    np.testing.assert_array_equal(buf.ray_counts[..., 3][live], nst[live])
+    err = np.abs(buf.results - ref).max()
+    p = psnr(buf.results[..., :3] + buf.results[..., 3:], ref[..., :3] + ref[..., 3:])
+    print(f"\nplain {fixture} {W}x{H}: max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB, samples {ns.sum()}")
+    assert err <= COLOR_ATOL
+    img = orc.composite_image(buf.results)
+    np.testing.assert_array_equal(buf.image, img)
+    st = r._render_stats
+    assert st.n_samples == ns.sum() and st.guard_flags == 0
+
+
+def _golden_model(tmp_path, name, base_dir):
+    """A model directory holding the golden scene's occupancy grid and the
+    tiny network (the marcher golden vectors do not depend on the network)."""
+    sc = SCENES[name]
+    d = tmp_path / f"golden_{name}"
+    shutil.copytree(base_dir, d)
+    occupancy_grid(sc["nlvl"]).tofile(d / "occupancy_grid.dat")
+    return str(d)
+
+
+def _golden_cam(sc):
+    c2w = np.asarray(sc["c2w"], np.float32).reshape(3, 4)
+    return {"resolution": (sc["W"], sc["H"]), "is_open_gl": False, "focal": (sc["fx"], sc["fy"]),
+            "principal": (sc["px"], sc["py"]), "cam2world": c2w, "world2cam": fcam.inverse(c2w)}
+
+
+def test_march_matches_reference_golden_c1(tmp_path, model1):
+    """cone_angle 0: per-ray steps and occupied samples equal the reference
+    header's own march (tests/golden/march_c1.npz) bit for bit."""
+    _, _, base = model1
+    sc = SCENES["c1"]
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "march_c1.npz"))
+    loader = fvc.load_data(_golden_model(tmp_path, "c1", base))
+    cam = _golden_cam(sc)
+    r, buf = _render(fvc.PerformanceRenderer, loader, cam)
+    r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
+    pix = pixels(sc)
+    occ_counts = np.diff(g["occ_off"])
+    for i, (x, y) in enumerate(pix):
+        c = buf.ray_counts[y, x]
+        if not g["hits"][i]:
+            assert c[3] == 0
+            continue
+        assert buf.results[y, x, 3] >= 1e-4  # no early termination in this fog scene
+        assert c[3] == g["n_steps"][i] + 1, (i, c, g["n_steps"][i])
+        assert c[0] == occ_counts[i], (i, c, occ_counts[i])
+
+
+def test_march_c2_cone_matches_oracle_and_reference(tmp_path, model3):
+    """cone_angle > 0 with 3 cascades and the L-inf contraction: the GPU equals
+    the oracle's deterministic-math march exactly; against the reference's
+    libm march at most a tiny fraction of rays differs."""
+    _, _, base = model3
+    sc = SCENES["c2"]
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "march_c2.npz"))
+    d = _golden_model(tmp_path, "c2", base)
+    loader = fvc.load_data(d)
+    om = orc.OracleModel(d)
+    cam = _golden_cam(sc)
+    r, buf = _render(fvc.PerformanceRenderer, loader, cam)
+    r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
+    import ctypes as C
+    oc = orc.make_cam(cam)
+    max_steps = sc["max_steps"]
+    t0b = np.zeros(max_steps, np.uint32)
+    occ = np.zeros(max_steps, np.uint8)
+    init = np.zeros(3, np.float32)
+    occ_counts = np.diff(g["occ_off"])
+    mism_ref = 0
+    for i, (x, y) in enumerate(pixels(sc)):
+        n = orc.lib().orc_trace_ray(C.byref(om.scene), C.byref(om.steps), C.byref(oc), orc.ptr(om.bits), int(x), int(y),
+                                    max_steps, orc.ptr(t0b), orc.ptr(occ), orc.ptr(init))
+        c = buf.ray_counts[y, x]
+        if init[2] == 0:
+            assert c[3] == 0
+            continue
+        assert c[3] == n + 1 and c[0] == int(occ[:n].sum()), (i, c, n, int(occ[:n].sum()))
+        if c[3] != g["n_steps"][i] + 1 or c[0] != occ_counts[i]:
+            mism_ref += 1
+    assert mism_ref <= 0.02 * len(pixels(sc)), mism_ref
+
+
+def _cache_setup(loader, cam):
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    r.resizeCache(cam["resolution"], loader.stepsize_info)
+    r.resizeRenderbuffers(cam["resolution"])
+    r.setCacheSettings(fvc.default_cache_settings())
+    return r, c0, c1
+
+
+@pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
+def test_cache_build_parity(request, fixture, W, H):
+    loader, om, _ = request.getfixturevalue(fixture)
+    cam = small_camera(1001, W, H)
+    r, c0, c1 = _cache_setup(loader, cam)
+    r.initCacheBlockwise(fvc.raymarch_info(cam, loader.stepsize_info))
+    packed, known, vox = c1.read()
+    oc = om.cache_build(cam)
+    np.testing.assert_array_equal(packed.ravel(), oc.packed_index)  # slot assignment bit-exact
+    np.testing.assert_array_equal(known.ravel().view(np.uint32), oc.known_ranges.view(np.uint32))
+    st = r._init_stats
+    assert st.n_bricks_demanded == oc.n_demanded and st.n_bricks_set == oc.n_bricks_set
+    n = oc.n_bricks_set
+    v = vox[:n].view(np.float32)
+    dens, isset = v[..., 0], v[..., 1]
+    np.testing.assert_array_equal(isset.ravel(), oc.vox_isset[:n * 512])
+    odens = oc.vox_density[:n * 512].reshape(n, 512)
+    assert np.abs(dens - odens).max() <= 2e-3 * max(1.0, odens.max())
+    lat = vox[:n, :, 4:8].copy().view(np.float16).astype(np.float32).reshape(n, 512, 8)
+    olat = oc.vox_latents[:n * 512 * 8].view(np.float16).astype(np.float32).reshape(n, 512, 8)
+    assert np.abs(lat - olat).max() < 2e-3
+
+
+@pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
+def test_cached_render_parity(request, fixture, W, H):
+    loader, om, _ = request.getfixturevalue(fixture)
+    cam0 = small_camera(1001, W, H)
+    r, c0, c1 = _cache_setup(loader, cam0)
+    r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
+    r.swapCache()
+    oc = om.cache_build(cam0)
+    # a view rotated by 1 degree about the up axis (part of it leaves the cache frustum)
+    c2w = np.asarray(cam0["cam2world"], np.float64)
+    a = np.radians(1.0)
+    R = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+    c2w_new = np.concatenate([R @ c2w[:, :3], (R @ c2w[:, 3])[:, None]], axis=1)
+    cam1 = fcam.camera_dict(c2w_new, W, H)
+    buf = fvc.RenderBuffer((W, H))
+    r.render(fvc.raymarch_info(cam1, loader.stepsize_info), buf)
+    ref, counts = om.render_cached(cam1, oc)
+    live = ref[..., 3] >= 1e-4
+    np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])  # resample
+    np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])  # cache
+    np.testing.assert_array_equal(buf.ray_counts[..., 2][live], counts[..., 2][live])  # dropped
+    err = np.abs(buf.results - ref).max()
+    p = psnr(buf.results[..., :3] + buf.results[..., 3:], ref[..., :3] + ref[..., 3:])
+    hit = counts[..., 1].sum() / max(1, counts[..., :2].sum())
+    print(f"\ncached {fixture}: hit ratio {hit:.3f}, max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB")
+    assert hit > 0.3
+    assert err <= COLOR_ATOL
+
+
+def test_cached_render_without_cache_fails():
+    loader = fvc.load_data(tiny_model(7, 1))
+    cam = small_camera(1001, 16, 16)
+    r, c0, c1 = _cache_setup(loader, cam)
+    with pytest.raises(fvc._lib.FvcError) as e:
+        r.render(fvc.raymarch_info(cam, loader.stepsize_info), fvc.RenderBuffer((16, 16)))
+    assert e.value.code == 4
+
+
+def test_progressive_average_image(model1):
+    loader, om, _ = model1
+    cam = small_camera(1001, 32, 32)
+    r, buf = _render(fvc.PerformanceRenderer, loader, cam)
+    r.render(fvc.raymarch_info(cam, loader.stepsize_info, 0), buf)
+    first = buf.image.copy()
+    r.render(fvc.raymarch_info(cam, loader.stepsize_info, 3), buf)
+    np.testing.assert_array_equal(buf.image, orc.composite_image(buf.results, 3, first))

@@ -1,0 +1,59 @@
+"""The CPU oracle against an independent numpy restatement of the network,
+and its renderers' invariants (no GPU)."""
+import numpy as np
+import pytest
+
+from frustumvolumecaching_gb300 import model as fmodel
+from oracle import oracle as orc
+from tests.helpers import psnr, small_camera, tiny_model
+
+
+@pytest.fixture(scope="module")
+def om():
+    return orc.OracleModel(tiny_model())
+
+
+def test_hash_encoding_matches_numpy(om):
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0, 1, size=(2000, 3)).astype(np.float32)
+    sm = fmodel.SyntheticModel(fmodel.spec_tiny())
+    ref = fmodel.hash_encode(pos, sm.table.astype(np.float64), om.levels)
+    got = om.hash_encode(pos)[:, :32]
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9)
+
+
+def test_density_network_matches_numpy_fp16_path():
+    o = orc.OracleModel(tiny_model(), mimic_fp16=True)
+    sm = fmodel.SyntheticModel(fmodel.spec_tiny())
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(0, 1, size=(500, 3)).astype(np.float32)
+    d01 = rng.uniform(0, 1, size=(500, 3)).astype(np.float32)
+    ref = sm.base_outputs(pos)[:, 0]
+    got = o.inference(pos, d01)[:, 3]
+    np.testing.assert_allclose(got, ref, atol=2e-3)
+
+
+def test_plain_render_invariants(om):
+    cam = small_camera(1001, 24, 20)
+    res, ns, nst = om.render_plain(cam)
+    T = res[..., 3]
+    assert np.all(T > 0) and np.all(T <= 1)
+    assert np.all(res[..., :3] >= 0) and np.all(res[..., :3] <= 1 + 1e-6)
+    assert ns.max() > 0 and np.all(nst >= ns)
+
+
+def test_cache_build_and_cached_render_self_consistent(om):
+    cam = small_camera(1001, 32, 24)
+    c = om.cache_build(cam)
+    d = c.dims
+    assert d.fW == 32 and d.fH == 24 and d.bX == 4 and d.bY == 3
+    used = c.packed_index[c.packed_index >= 0]
+    assert used.size == c.n_bricks_set > 0
+    # slots are consecutive from 0 in (iteration, tile) order
+    slots = np.sort(((used >> 20) & 1023) * (d.dY * d.dZ) + ((used >> 10) & 1023) * d.dZ + (used & 1023))
+    np.testing.assert_array_equal(slots, np.arange(slots.size))
+    plain, _, _ = om.render_plain(cam)
+    cached, counts = om.render_cached(cam, c)
+    hit = counts[..., 1].sum() / max(1, counts[..., :2].sum())
+    assert hit > 0.5, hit
+    assert psnr(cached[..., :3] + cached[..., 3:], plain[..., :3] + plain[..., 3:]) > 30
