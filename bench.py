@@ -1,0 +1,402 @@
+"""Benchmark: 1080p frames/s of the frustum-cached camera path vs the plain
+renderer (the synthetic 1920x1080 workload with 3 cascades, 2^19 hash
+entries per level, 60-frame rotate + translate path, cache rebuilt when the
+reprojected coverage falls below 90 %).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fvc|reference]
+
+A step is one pass over the 60-frame camera path.  `value` is the cached
+path's frames/s with everything resident on the device; `e2e` is the same
+path through the host-buffer C-ABI call (fvc_render: D2H of each frame's
+image inside the timed region).  The plain path's frames/s and the cache
+statistics are reported beside it.  `--impl reference` times the CPU oracle
+(a float64 restatement of the reference's renderer; the reference's own CUDA
+build needs tiny-cuda-nn, which is not available) on the host cores on a
+bounded sample of frame 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1080p frames/s cached vs plain at dPSNR<=0.1dB vs FP64 oracle; backward Mrays/s"
+UNIT = "frames/s"
+PATH_FRAMES = 60
+RES = (1920, 1080)
+COVERAGE_REBUILD = 0.90
+FLOP_RESAMPLE = 16896  # per sample: density 2*(32*64+64*9) + color 2*(24*64+64*64+64*3)
+FLOP_CACHE = 11648     # per cache sample: color head only
+BYTES_HASH = 512       # per resampled sample: 16 levels x 8 corners x 2 fp16
+BYTES_CACHE = 8 * 24   # per cache sample: 8 corners x (density, isset, 8 fp16 latents)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "bf16_tflops": d.get("bf16_tflops", 1900.0),
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", 1700.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+# --------------------------------------------------------------------------
+# reference arm: the CPU oracle on the host cores
+# --------------------------------------------------------------------------
+def run_reference(args) -> dict:
+    from frustumvolumecaching_gb300 import camera as fcam
+    from frustumvolumecaching_gb300 import model as fmodel
+    from oracle import oracle as orc
+
+    d = fmodel.ensure_model(fmodel.spec_config2())
+    om = orc.OracleModel(d)
+    cam = fcam.rotation_path(fmodel.spec_config2().seed, n_frames=1, width=RES[0], height=RES[1])[0]
+    threads = orc.default_threads()
+    rows_per_step = args.ref_rows
+    H = RES[1]
+    times = []
+    row = H // 2 - rows_per_step * (args.warmup + args.steps) // 2
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        om.render_plain(cam, rows=(row, row + rows_per_step), threads=threads)
+        dt = time.perf_counter() - t
+        row += rows_per_step
+        if i >= args.warmup:
+            times.append(dt)
+    per_step = sum(times) / len(times)
+    fps = (rows_per_step / H) / per_step
+    sample = f"{rows_per_step} rows x {RES[0]} px of frame 0 (plain render, float64) per step, from the image centre"
+    return {"impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "higher_is_better": True,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "c2_cached_1080p_path (plain frame 0 rows, CPU)", "resolution": list(RES)},
+            "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def cpu_baseline_port(args) -> dict:
+    from frustumvolumecaching_gb300 import camera as fcam
+    from frustumvolumecaching_gb300 import model as fmodel
+    from oracle import oracle as orc
+
+    d = fmodel.ensure_model(fmodel.spec_config2())
+    om = orc.OracleModel(d)
+    cam = fcam.rotation_path(fmodel.spec_config2().seed, n_frames=1, width=RES[0], height=RES[1])[0]
+    threads = orc.default_threads()
+    rows = args.ref_rows
+    y0 = RES[1] // 2 - rows // 2
+    t = time.perf_counter()
+    om.render_plain(cam, rows=(y0, y0 + rows), threads=threads)
+    dt = time.perf_counter() - t
+    return {"value": (rows / RES[1]) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{rows} rows x {RES[0]} px of frame 0 (plain render, float64 oracle), {dt:.1f} s"}
+
+
+# --------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------
+def run_fvc(args) -> dict | None:
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import frustumvolumecaching_gb300 as fvc
+    from frustumvolumecaching_gb300 import build as fbuild
+    from frustumvolumecaching_gb300 import camera as fcam
+    from frustumvolumecaching_gb300 import model as fmodel
+
+    fbuild.build()
+    spec = fmodel.spec_config2()
+    d = fmodel.ensure_model(spec)
+    loader = fvc.load_data(d)
+    W, H = RES
+    n_frames = args.frames
+    cams = fcam.rotation_path(spec.seed, n_frames=n_frames, width=W, height=H)
+    infos = [fvc.raymarch_info(c, loader.stepsize_info) for c in cams]
+
+    stream = torch.cuda.Stream(dev)  # a real stream: handle 0 would select the library's internal stream
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    plain = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    plain.resizeRenderbuffers(RES)
+    plain.set_stream(sh)
+    caches = (fvc.Cache(), fvc.Cache())
+    cached = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network,
+                                          caches[0], caches[1])
+    cached.resizeCache(RES, loader.stepsize_info)
+    cached.resizeRenderbuffers(RES)
+    cached.setCacheSettings(fvc.default_cache_settings())
+    cached.set_stream(sh)
+
+    image = torch.zeros((H, W, 4), dtype=torch.uint8, device=dev)
+    results = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    log = {"render_plain_ms": [], "render_cached_ms": [], "build_ms": [], "rebuilds": 0, "coverage": [],
+           "plain_res": 0, "cache_res": 0, "cache_hits": 0, "launches": 0, "build_iters": 0, "overflow": 0,
+           "bricks_demanded": 0, "bricks_set": 0}
+
+    def plain_path(record: bool):
+        for info in infos:
+            a, b = ev(), ev()
+            a.record(stream)
+            plain.render_device(info, image=image, results=results)
+            b.record(stream)
+            if record:
+                log["_pending_plain"].append((a, b))
+        if record:
+            log["launches"] += len(infos)
+
+    def rebuild(info, record):
+        a, b = ev(), ev()
+        a.record(stream)
+        cached.initCacheBlockwise(info)
+        cached.swapCache()
+        b.record(stream)
+        st = cached._init_stats
+        if record:
+            log["_pending_build"].append((a, b))
+            log["rebuilds"] += 1
+            log["build_iters"] += st.n_iterations
+            log["launches"] += 3 + 3 * st.n_iterations
+            log["overflow"] = max(log["overflow"], st.overflow)
+            log["bricks_demanded"] = st.n_bricks_demanded
+            log["bricks_set"] = st.n_bricks_set
+
+    def cached_path(record: bool, host: bool = False, hbuf=None):
+        rebuild(infos[0], record)
+        for i, info in enumerate(infos):
+            a, b = ev(), ev()
+            a.record(stream)
+            if host:
+                cached.render(info, hbuf)
+            else:
+                cached.render_device(info, image=image, results=results)
+            b.record(stream)
+            st = cached._render_stats  # synchronises: the host reads the coverage like the viewer does
+            cov = st.n_cache_hits / max(1, st.n_cache_hits + st.n_resamples)
+            if record:
+                log["_pending_cached"].append((a, b))
+                log["coverage"].append(cov)
+                log["cache_res"] += st.n_resamples
+                log["cache_hits"] += st.n_cache_hits
+                log["launches"] += 1
+            if cov < COVERAGE_REBUILD and i + 1 < len(infos):
+                rebuild(info, record)
+
+    for k in ("_pending_plain", "_pending_cached", "_pending_build"):
+        log[k] = []
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warm-up
+    for _ in range(args.warmup):
+        plain_path(False)
+        cached_path(False)
+        flush.zero_()
+    barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    # plain path, K steps
+    t_plain = []
+    for _ in range(args.steps):
+        flush.zero_()
+        barrier()
+        s, e = ev(), ev()
+        s.record(stream)
+        plain_path(True)
+        e.record(stream)
+        barrier()
+        t_plain.append(s.elapsed_time(e))
+    st = plain._render_stats
+    # cached path, K steps
+    t_cached = []
+    for _ in range(args.steps):
+        flush.zero_()
+        barrier()
+        s, e = ev(), ev()
+        s.record(stream)
+        cached_path(True)
+        e.record(stream)
+        barrier()
+        t_cached.append(s.elapsed_time(e))
+    clk = clocks.stop()
+
+    # e2e: the cached path through the host-buffer C-ABI call (D2H of every frame)
+    hbuf = fvc.RenderBuffer(RES)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        cached_path(False, host=True, hbuf=hbuf)
+    torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
+
+    def mean_ms(pairs):
+        return sum(a.elapsed_time(b) for a, b in pairs) / max(1, len(pairs))
+
+    plain_launch_ms = mean_ms(log["_pending_plain"])
+    cached_launch_ms = mean_ms(log["_pending_cached"])
+    build_ms = mean_ms(log["_pending_build"])
+    steps_ms_cached = sum(t_cached) / len(t_cached)
+    steps_ms_plain = sum(t_plain) / len(t_plain)
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([steps_ms_cached, steps_ms_plain, e2e_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        steps_ms_cached, steps_ms_plain, e2e_s = tt.tolist()
+    fps_cached = ws * n_frames / (steps_ms_cached / 1e3)
+    fps_plain = ws * n_frames / (steps_ms_plain / 1e3)
+    fps_e2e = ws * n_frames / e2e_s
+
+    # roofline of the dominant kernel: the plain render kernel, tensor-pipe bound work
+    plain_samples_per_frame = st.n_resamples
+    peaks = measured_peaks()
+    flop = plain_samples_per_frame * FLOP_RESAMPLE
+    achieved_tf = flop / (plain_launch_ms / 1e3) / 1e12
+    n_frames_cached = len(log["_pending_cached"])
+    res_per_frame = log["cache_res"] / max(1, n_frames_cached)
+    hit_per_frame = log["cache_hits"] / max(1, n_frames_cached)
+    out = {
+        "metric": METRIC, "value": fps_cached, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": steps_ms_cached, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f16 (MLP, fp32 accumulate), f32 (marcher, compositing)", "data": "synthetic",
+        "config": {"workload": "c2_cached_1080p_path", "resolution": list(RES), "frames_per_step": n_frames,
+                   "hash_entries_per_level": 2 ** spec.log2_T, "cascades": spec.grid_nlvl,
+                   "occupancy_fraction": spec.occupancy_fraction, "rebuild_coverage": COVERAGE_REBUILD,
+                   "l2": "256 MiB buffer written between steps; cache data array (4 GiB) larger than L2",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "plain": {"value": fps_plain, "unit": UNIT, "ms_per_frame": steps_ms_plain / n_frames,
+                  "samples_per_frame": plain_samples_per_frame},
+        "cached": {"ms_per_frame": steps_ms_cached / n_frames, "render_ms": cached_launch_ms, "build_ms": build_ms,
+                   "rebuilds_per_path": log["rebuilds"] / args.steps, "mean_coverage": float(np.mean(log["coverage"])) if log["coverage"] else None,
+                   "resample_per_frame": res_per_frame, "cache_samples_per_frame": hit_per_frame,
+                   "bricks_demanded": log["bricks_demanded"], "bricks_set": log["bricks_set"], "overflow": bool(log["overflow"]),
+                   "speedup_vs_plain": fps_cached / fps_plain},
+        "roofline": {"kernel": "render_kernel<plain> (fused march + hash grid + MLPs + compositing)", "bound": "tensor",
+                     "achieved": achieved_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": achieved_tf / peaks["bf16_tflops"], "traffic": None,
+                     "peak_source": peaks["source"] + " bf16 dense burst",
+                     "work_per_launch": f"{plain_samples_per_frame} samples x {FLOP_RESAMPLE} FLOP",
+                     "launch_ms": plain_launch_ms,
+                     "hash_gather_gbs": plain_samples_per_frame * BYTES_HASH / (plain_launch_ms / 1e3) / 1e9},
+        "e2e": {"value": fps_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": n_frames * W * H * (4 + 16 + 16)},
+        "gpu_launches": log["launches"] // max(1, args.steps),
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_port(args)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fvc", choices=["fvc", "reference"])
+    ap.add_argument("--ref-rows", type=int, default=8)
+    ap.add_argument("--frames", type=int, default=PATH_FRAMES, help="frames of the camera path per step (60 for the metric)")
+    ap.add_argument("--res", default=None, help="WxH override for small profiling cases (the metric is 1920x1080)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    global RES
+    if args.res:
+        RES = tuple(int(v) for v in args.res.lower().split("x"))
+    ws, rank, _ = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    out = run_fvc(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

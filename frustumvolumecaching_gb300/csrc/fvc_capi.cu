@@ -337,6 +337,21 @@ struct fvc_renderer {
     uchar4 *d_image = nullptr;
     int4 *d_counts = nullptr;
     int *h_pinned = nullptr;          /* readback of build counters */
+    /* wavefront buffers (fvc_render.cu) */
+    RayState *d_states[2] = {nullptr, nullptr};
+    int4 *d_ray_rows = nullptr;
+    float4 *d_res_rows = nullptr, *d_cache_rows = nullptr;
+    float *d_res_t0 = nullptr, *d_cache_t0 = nullptr;
+    uint2 *d_res_out = nullptr, *d_cache_out = nullptr;
+    int *d_wf_counters = nullptr;
+    int row_capacity = 0;
+    int last_iterations = 0;
+    void release_wavefront()
+    {
+        dfree(d_states[0]); dfree(d_states[1]); dfree(d_ray_rows); dfree(d_res_rows); dfree(d_cache_rows);
+        dfree(d_res_t0); dfree(d_cache_t0); dfree(d_res_out); dfree(d_cache_out); dfree(d_wf_counters);
+        row_capacity = 0;
+    }
     fvc_cache *cache = nullptr, *next = nullptr;
     fvc_cache_settings settings{0, 0, 1, 1, 1, 1};
     int render_mode = 0;
@@ -347,6 +362,7 @@ struct fvc_renderer {
     {
         if (stream) cudaStreamSynchronize(stream);
         dfree(d_ctl); dfree(d_stats); dfree(d_results); dfree(d_image); dfree(d_counts);
+        release_wavefront();
         bs.release();
         if (h_pinned) cudaFreeHost(h_pinned);
         if (own_stream) cudaStreamDestroy(own_stream);
@@ -651,6 +667,24 @@ extern "C" int fvc_renderer_resize(fvc_renderer *r, int width, int height)
     if ((rc = dalloc(&r->d_image, n, "image"))) return rc;
     if ((rc = dalloc(&r->d_counts, n, "ray counts"))) return rc;
     CU(cudaMemset(r->d_image, 0, n * sizeof(uchar4)));
+    /* wavefront: alive-ray states (ping-pong) and up to 8 sample rows per
+     * ray and stream per sub-iteration (MAX_N_STEPS_PER_SUBITER) */
+    r->release_wavefront();
+    const size_t cap = std::min<size_t>(n * 8, (size_t)1 << 24);
+    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    if ((rc = dalloc(&r->d_states[0], n, "ray states"))) return rc;
+    if ((rc = dalloc(&r->d_states[1], n, "ray states"))) return rc;
+    if ((rc = dalloc(&r->d_ray_rows, n, "ray rows"))) return rc;
+    if ((rc = dalloc(&r->d_res_rows, cap, "resample rows"))) return rc;
+    if ((rc = dalloc(&r->d_res_t0, cap, "resample t0"))) return rc;
+    if ((rc = dalloc(&r->d_res_out, cap, "resample outputs"))) return rc;
+    if (cached) {
+        if ((rc = dalloc(&r->d_cache_rows, cap, "cache rows"))) return rc;
+        if ((rc = dalloc(&r->d_cache_t0, cap, "cache t0"))) return rc;
+        if ((rc = dalloc(&r->d_cache_out, cap, "cache outputs"))) return rc;
+    }
+    if ((rc = dalloc(&r->d_wf_counters, (size_t)8, "wavefront counters"))) return rc;
+    r->row_capacity = (int)cap;
     r->W = width; r->H = height;
     return FVC_OK;
 }
@@ -705,9 +739,21 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
         p.cache = c->view();
         p.render_mode = r->render_mode;
     }
+    if (info->cam_info.resolution.x != r->W || info->cam_info.resolution.y != r->H) {
+        const int rc = fvc_renderer_resize(r, info->cam_info.resolution.x, info->cam_info.resolution.y);
+        if (rc) return rc;
+    }
+    p.states[0] = r->d_states[0]; p.states[1] = r->d_states[1];
+    p.ray_rows = r->d_ray_rows;
+    p.res_rows = r->d_res_rows; p.res_t0 = r->d_res_t0; p.res_out = r->d_res_out;
+    p.cache_rows = r->d_cache_rows; p.cache_t0 = r->d_cache_t0; p.cache_out = r->d_cache_out;
+    p.counters = r->d_wf_counters;
+    p.row_capacity = r->row_capacity;
+    p.step_cap = 256;
     CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
     CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
-    CU(launch_render(p, cached, m->head_hidden, m->n_sms, r->stream));
+    CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));
+    CU(render_frame(p, cached, m->head_hidden, m->n_sms, r->stream, r->h_pinned + 8, 4, &r->last_iterations));
     return FVC_OK;
 }
 
@@ -753,7 +799,7 @@ extern "C" int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *o)
     o->n_cache_hits = (long long)s.n_cache_hits;
     o->n_dropped = (long long)s.n_dropped;
     o->n_steps = (long long)s.n_steps;
-    o->n_rounds = s.n_rounds;
+    o->n_rounds = r->last_iterations;
     o->samples_ppx = (double)s.n_samples / n_rays;
     o->guard_flags = ctl[1];
     return FVC_OK;

@@ -178,6 +178,7 @@ __device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__re
                         F_DIV(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z));
     const float ax = F_SUB(u.x, 0.5f), ay = F_SUB(u.y, 0.5f), az = F_SUB(u.z, 0.5f);
     const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
+    if (!(mx <= 3.0e38f)) return false; /* NaN / inf positions never index the grid */
     const int mip = max(0, frexp_exponent(mx) + 1);
     if (mip >= sc.nlvl) return false;
     const float sm = __int_as_float((127 - mip) << 23); /* scalbnf(1, -mip) */

@@ -1,15 +1,7 @@
 /*
  * fvc_kernels.cu - the renderer's CUDA kernels for sm_103a.
  *
- *  render_kernel<CACHED>   persistent, warp-synchronous renderer.  Each warp
- *                          owns 32 rays (one per lane) and runs rounds of
- *                          (refill rays from a global queue, lockstep march
- *                          into an on-chip sample list, network on 32-row
- *                          batches on the tensor cores, in-order compositing).
- *                          Plain: PerformanceRenderer::render,
- *                          src/performance_renderer.cu:15-149,214-286.
- *                          Cached: CachePerformanceRenderer::render,
- *                          src/cache_performance_renderer.cu:22-313,678-908.
+ *  (the renderer's wavefront kernels live in fvc_render.cu)
  *  cache_*_kernel          frustum cache build, one depth brick of every alive
  *                          8x8 tile per iteration with deterministic slots:
  *                          CacheRenderer::initCacheBlockwise,
@@ -29,379 +21,6 @@ constexpr unsigned FULL = 0xffffffffu;
 
 __device__ __forceinline__ unsigned lanemask_lt() { unsigned m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
 
-/* voxel of the cache data array: density, isset, 2 pad words, 8 fp16 latents */
-struct __align__(16) Voxel {
-    float density, isset, pad0, pad1;
-    uint4 lat;
-};
-
-/* ------------------------------------------------------------------------- */
-/* render kernel                                                             */
-/* ------------------------------------------------------------------------- */
-constexpr int RK_WARPS = 8;       /* warps per CTA */
-constexpr int KMAX = 4;           /* samples per lane per round */
-constexpr int ROWS = 32 * KMAX;   /* resample rows from the front, cache rows from the back */
-constexpr int ROUND_STEP_CAP = 256;
-constexpr int ROW_TARGET = 96;
-
-struct WarpSmem {
-    float4 rows[ROWS];                 /* pos or froxel point, .w = lane | seq<<8 */
-    __half tile[32 * TILE_STRIDE];
-    float comp_t0[KMAX][32];
-    uint2 comp_out[KMAX][32];          /* half logits r,g,b, half log-density */
-    uint8_t comp_kind[KMAX][32];       /* 0 resample, 1 cache */
-    float3 dir01[32];
-};
-
-struct RenderSmem {
-    uint2 W[W_TOTAL];
-    float bias3[64];
-    WarpSmem warp[RK_WARPS];
-};
-
-__device__ __forceinline__ void write_pixel(const RenderParams &p, int ray, float r, float g, float b, float T, int4 counts)
-{
-    if (p.results) p.results[ray] = make_float4(r, g, b, T);
-    if (p.ray_counts) p.ray_counts[ray] = counts;
-    if (p.image) {
-        /* writeImageBuffer_performance_kernel, src/performance_renderer.cu:127-149 */
-        float cr = r + T, cg = g + T, cb = b + T;
-        if (p.sample_index > 0) {
-            const uchar4 prev = p.image[ray];
-            const float si = (float)p.sample_index;
-            cr = (cr + (float)prev.x / 255.f * si) / (si + 1.f);
-            cg = (cg + (float)prev.y / 255.f * si) / (si + 1.f);
-            cb = (cb + (float)prev.z / 255.f * si) / (si + 1.f);
-        }
-        uchar4 o;
-        o.x = (unsigned char)min(255, max(0, (int)(cr * 256.f)));
-        o.y = (unsigned char)min(255, max(0, (int)(cg * 256.f)));
-        o.z = (unsigned char)min(255, max(0, (int)(cb * 256.f)));
-        o.w = 255;
-        p.image[ray] = o;
-    }
-}
-
-/* cache texel (X,Y,Z) of the data array -> voxel pointer (or null outside:
- * border addressing returns zeros) */
-__device__ __forceinline__ const Voxel *texel(const CacheView &c, int X, int Y, int Z)
-{
-    if (X < 0 || Y < 0 || Z < 0 || X >= c.dX * 8 || Y >= c.dY * 8 || Z >= c.dZ * 8) return nullptr;
-    const int slot = (X >> 3) * (c.dY * c.dZ) + (Y >> 3) * c.dZ + (Z >> 3);
-    if (slot >= c.n_valid_slots) return nullptr; /* the reference clears the data arrays per build */
-    return reinterpret_cast<const Voxel *>(c.voxels) + (size_t)slot * 512 + ((Z & 7) * 64 + (Y & 7) * 8 + (X & 7));
-}
-
-template <bool CACHED, int HEAD_HIDDEN>
-__global__ void __launch_bounds__(RK_WARPS * 32, 2) render_kernel(RenderParams p)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    RenderSmem &S = *reinterpret_cast<RenderSmem *>(smem_raw);
-    for (int i = threadIdx.x; i < W_TOTAL; i += blockDim.x) S.W[i] = p.weights[i];
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) S.bias3[i] = p.bias3[i];
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31;
-    WarpSmem &ws = S.warp[threadIdx.x >> 5];
-    const int n_rays = p.cam.W * p.cam.H;
-
-    int ray = -1;
-    float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0), oc = o, dc = o;
-    float far_ = 0.f, t1 = 0.f, cr = 0.f, cg = 0.f, cb = 0.f, T = 1.f;
-    bool done = false, term = false;
-    int nsamp = 0, c_res = 0, c_cache = 0, c_drop = 0, c_steps = 0;
-    bool exhausted = false;
-    long long st_samples = 0, st_res = 0, st_cache = 0, st_drop = 0, st_steps = 0;
-    int rounds = 0;
-
-    for (int round = 0; round < p.max_rounds; ++round) {
-        /* ---- refill lanes from the ray queue ---- */
-        for (int it = 0; it < 64 && !exhausted; ++it) {
-            const unsigned need = __ballot_sync(FULL, ray < 0);
-            if (need == 0) break;
-            int base = 0;
-            if (lane == 0) base = atomicAdd(p.ray_counter, __popc(need));
-            base = __shfl_sync(FULL, base, 0);
-            if (base + __popc(need) >= n_rays) exhausted = true;
-            if (ray < 0) {
-                const int id = base + __popc(need & lanemask_lt());
-                if (id < n_rays) {
-                    const int x = id % p.cam.W, y = id / p.cam.W;
-                    generate_ray(p.cam, x, y, o, d);
-                    float tn, tf;
-                    const bool hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
-                    if (!hits) {
-                        write_pixel(p, id, 0.f, 0.f, 0.f, 1.f, make_int4(0, 0, 0, 0));
-                    } else {
-                        ray = id;
-                        far_ = fminf(tf, p.steps.far_);
-                        t1 = F_ADD(valid_t_from_t(p.steps, tn), 0.0f);
-                        cr = cg = cb = 0.f; T = 1.f; done = false; term = false;
-                        nsamp = c_res = c_cache = c_drop = c_steps = 0;
-                        if (CACHED) transform_ray(p.ccam.w2c, o, d, oc, dc);
-                        ws.dir01[lane] = make_float3(F_DIV(F_ADD(d.x, 1.0f), 2.0f), F_DIV(F_ADD(d.y, 1.0f), 2.0f),
-                                                     F_DIV(F_ADD(d.z, 1.0f), 2.0f));
-                    }
-                }
-            }
-        }
-        if (__ballot_sync(FULL, ray >= 0) == 0) break;
-        ++rounds;
-
-        /* ---- lockstep march into the sample list ---- */
-        int n_res = 0, n_cache = 0, k = 0;
-        for (int it = 0; it < ROUND_STEP_CAP; ++it) {
-            const bool act = ray >= 0 && !done && k < KMAX;
-            if (!__any_sync(FULL, act) || n_res + n_cache >= ROW_TARGET) break;
-            int kind = -1;
-            float3 rv = make_float3(0.f, 0.f, 0.f);
-            float t0 = 0.f;
-            if (act) {
-                t0 = t1;
-                const float dt = calc_step(p.steps, t0);
-                t1 = F_ADD(t0, dt);
-                const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
-                ++st_steps;
-                ++c_steps;
-                if (tm > far_) {
-                    done = true;
-                } else {
-                    const float3 wp = at(o, d, tm);
-                    if (occupied(p.scene, p.bits, wp)) {
-                        if (!CACHED) {
-                            kind = 0;
-                            rv = contract(p.scene, wp);
-                        } else {
-                            /* classification, sample_cache_performance_kernel :91-163 */
-                            float tfr;
-                            const float3 fr = cam2froxel(at(oc, dc, tm), p.ccam, p.csteps, tfr);
-                            const CacheView &C = p.cache;
-                            const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
-                            const bool inside = in_fov && fr.z >= 0.f && fr.z < (float)C.fD;
-                            bool unsampled = true;
-                            if (in_fov) {
-                                const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
-                                unsampled = tfr < p.csteps.near_ || tfr > kr;
-                            }
-                            const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));  /* generateNetworkInput_*: t0 + dt/2 */
-                            if (!inside || unsampled) {
-                                if (p.render_mode != 1) { kind = 0; rv = contract(p.scene, at(o, d, tmh)); }
-                            } else if (p.render_mode != 2) {
-                                const int bx = (int)F_DIV(fr.x, 8.0f), by = (int)F_DIV(fr.y, 8.0f), bz = (int)F_DIV(fr.z, 8.0f);
-                                const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
-                                kind = 2;
-                                if (packed >= 0) {
-                                    const float ax = F_ADD((float)(((packed >> 20) & 1023) * 8), F_SUB(fr.x, (float)(bx * 8)));
-                                    const float ay = F_ADD((float)(((packed >> 10) & 1023) * 8), F_SUB(fr.y, (float)(by * 8)));
-                                    const float az = F_ADD((float)((packed & 1023) * 8), F_SUB(fr.z, (float)(bz * 8)));
-                                    const Voxel *v = texel(C, (int)floorf(ax), (int)floorf(ay), (int)floorf(az));
-                                    if (v && __ldg(&v->density) > 0.0f) {
-                                        kind = 1;
-                                        float tf2;
-                                        rv = cam2froxel(at(oc, dc, tmh), p.ccam, p.csteps, tf2);
-                                    }
-                                }
-                                if (kind == 2) { ++st_drop; ++c_drop; }
-                            }
-                        }
-                    }
-                }
-            }
-            const unsigned m0 = __ballot_sync(FULL, kind == 0), m1 = __ballot_sync(FULL, kind == 1);
-            if (kind == 0 || kind == 1) {
-                const int idx = kind == 0 ? n_res + __popc(m0 & lanemask_lt()) : ROWS - 1 - (n_cache + __popc(m1 & lanemask_lt()));
-                ws.rows[idx] = make_float4(rv.x, rv.y, rv.z, __int_as_float(lane | (k << 8)));
-                ws.comp_t0[k][lane] = t0;
-                ws.comp_kind[k][lane] = (uint8_t)kind;
-                ++k;
-                if (++nsamp > p.max_samples_per_ray && p.max_samples_per_ray > 0) atomicOr(p.guard, 1);
-            }
-            n_res += __popc(m0);
-            n_cache += __popc(m1);
-        }
-        __syncwarp();
-        st_res += n_res;
-        st_cache += n_cache;
-
-        /* ---- resample rows: hash grid + density net + color head ---- */
-        for (int b = 0; b < n_res; b += 32) {
-            const int r = b + lane;
-            __half *trow = ws.tile + lane * TILE_STRIDE;
-            if (r < n_res) {
-                const float4 rw = ws.rows[r];
-                hash_encode(p.grid, p.table, make_float3(rw.x, rw.y, rw.z), reinterpret_cast<__half2 *>(trow));
-                sh16(ws.dir01[__float_as_int(rw.w) & 31], reinterpret_cast<__half2 *>(trow + 32));
-            } else {
-                for (int c = 0; c < 24; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
-            }
-            __syncwarp();
-            density_mlp(ws.tile, S.W, lane);
-            float lo[2][4];
-            color_mlp<HEAD_HIDDEN>(ws.tile, S.W, S.bias3, lane, lo);
-            {
-                const int g = lane >> 2, t = lane & 3;
-                if (t < 2) {
-#pragma unroll
-                    for (int mt = 0; mt < 2; ++mt) {
-                        __half *r0 = ws.tile + (16 * mt + g) * TILE_STRIDE + 48 + 2 * t;
-                        *reinterpret_cast<uint32_t *>(r0) = pack_h2(lo[mt][0], lo[mt][1]);
-                        *reinterpret_cast<uint32_t *>(r0 + 8 * TILE_STRIDE) = pack_h2(lo[mt][2], lo[mt][3]);
-                    }
-                }
-            }
-            __syncwarp();
-            if (r < n_res) {
-                const int tag = __float_as_int(ws.rows[r].w);
-                const uint32_t rg = *reinterpret_cast<const uint32_t *>(trow + 48);
-                const uint32_t bs = (uint32_t)__half_as_ushort(trow[50]) | ((uint32_t)__half_as_ushort(trow[16]) << 16);
-                ws.comp_out[tag >> 8][tag & 31] = make_uint2(rg, bs);
-            }
-            __syncwarp();
-        }
-
-        /* ---- cache rows: trilinear lookup + color head ---- */
-        if (CACHED) {
-            for (int b = 0; b < n_cache; b += 32) {
-                const int r = b + lane;
-                __half *trow = ws.tile + lane * TILE_STRIDE;
-                if (r < n_cache) {
-                    const float4 rw = ws.rows[ROWS - 1 - r];
-                    const CacheView &C = p.cache;
-                    /* generateNetworkInput_cache_shfl_perf_kernel_cg :678-787 */
-                    const float fx = F_SUB(rw.x, 0.5f), fy = F_SUB(rw.y, 0.5f), fz = F_SUB(rw.z, 0.5f);
-                    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
-                    const float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
-                    float wsum = 0.f, dsum = 0.f, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) {
-                        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
-                        const float cx = x0 + (float)ox, cy = y0 + (float)oy, cz = z0 + (float)oz;
-                        const bool inside = cx >= 0.f && cx < (float)C.fW && cy >= 0.f && cy < (float)C.fH && cz >= 0.f && cz < (float)C.fD;
-                        if (!inside) continue;
-                        const int bx = (int)F_DIV(cx, 8.0f), by = (int)F_DIV(cy, 8.0f), bz = (int)F_DIV(cz, 8.0f);
-                        const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
-                        if (packed < 0) continue;
-                        const Voxel *v = texel(C, ((packed >> 20) & 1023) * 8 + ((int)cx - bx * 8),
-                                               ((packed >> 10) & 1023) * 8 + ((int)cy - by * 8), (packed & 1023) * 8 + ((int)cz - bz * 8));
-                        if (!v) continue;
-                        const float w = (ox ? lx : 1.0f - lx) * (oy ? ly : 1.0f - ly) * (oz ? lz : 1.0f - lz);
-                        const float2 di = __ldg(reinterpret_cast<const float2 *>(v));
-                        const uint4 lt = __ldg(&v->lat);
-                        wsum = fmaf(w, di.y, wsum);
-                        dsum = fmaf(w, di.x, dsum);
-                        const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&lw[q]));
-                            ls[2 * q] = fmaf(w, f.x, ls[2 * q]);
-                            ls[2 * q + 1] = fmaf(w, f.y, ls[2 * q + 1]);
-                        }
-                    }
-                    uint32_t *hin = reinterpret_cast<uint32_t *>(trow + 16);
-                    for (int c = 0; c < 8; ++c) hin[c] = 0u;
-                    trow[16] = __float2half_rn(logf(fmaxf(dsum, 1e-6f)));
-                    const float inv = 1.0f / wsum;
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) trow[16 + p.latent_offset + j] = __float2half_rn(ls[j] * inv);
-                    sh16(ws.dir01[__float_as_int(rw.w) & 31], reinterpret_cast<__half2 *>(trow + 32));
-                } else {
-                    for (int c = 8; c < 24; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
-                }
-                __syncwarp();
-                float lo[2][4];
-                color_mlp<HEAD_HIDDEN>(ws.tile, S.W, S.bias3, lane, lo);
-                {
-                    const int g = lane >> 2, t = lane & 3;
-                    if (t < 2) {
-#pragma unroll
-                        for (int mt = 0; mt < 2; ++mt) {
-                            __half *r0 = ws.tile + (16 * mt + g) * TILE_STRIDE + 48 + 2 * t;
-                            *reinterpret_cast<uint32_t *>(r0) = pack_h2(lo[mt][0], lo[mt][1]);
-                            *reinterpret_cast<uint32_t *>(r0 + 8 * TILE_STRIDE) = pack_h2(lo[mt][2], lo[mt][3]);
-                        }
-                    }
-                }
-                __syncwarp();
-                if (r < n_cache) {
-                    const int tag = __float_as_int(ws.rows[ROWS - 1 - r].w);
-                    const uint32_t rg = *reinterpret_cast<const uint32_t *>(trow + 48);
-                    const uint32_t bs = (uint32_t)__half_as_ushort(trow[50]) | ((uint32_t)__half_as_ushort(trow[16]) << 16);
-                    ws.comp_out[tag >> 8][tag & 31] = make_uint2(rg, bs);
-                }
-                __syncwarp();
-            }
-        }
-
-        /* ---- in-order compositing, accumulate_performance_kernel
-         *      (src/performance_renderer.cu:93-121) ---- */
-        for (int s = 0; s < k && !term; ++s) {
-            const float t0 = ws.comp_t0[s][lane];
-            const uint2 ov = ws.comp_out[s][lane];
-            const float2 rg = __half22float2(*reinterpret_cast<const __half2 *>(&ov.x));
-            const float lb = __half2float(__ushort_as_half((unsigned short)(ov.y & 0xffffu)));
-            const float ld = __half2float(__ushort_as_half((unsigned short)(ov.y >> 16)));
-            const float dt = calc_step(p.steps, t0);
-            if (ws.comp_kind[s][lane]) ++c_cache; else ++c_res;
-            const float sigma = expf(ld);
-            const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
-            if (alpha > p.scene.alpha_thre) {
-                const float w = alpha * T;
-                cr += w / (1.0f + expf(-rg.x));
-                cg += w / (1.0f + expf(-rg.y));
-                cb += w / (1.0f + expf(-lb));
-                T *= 1.0f - alpha;
-            }
-            if (T < 1e-4f) term = true;
-        }
-        st_samples += k;
-        __syncwarp();
-
-        /* ---- finish rays ---- */
-        if (ray >= 0 && (done || term)) {
-            write_pixel(p, ray, cr, cg, cb, T, make_int4(c_res, c_cache, c_drop, c_steps));
-            ray = -1;
-        }
-    }
-    if (ray >= 0) atomicOr(p.guard, 2); /* round limit reached with a ray in flight */
-
-    /* statistics: one atomic per warp */
-    const long long wsamp = __reduce_add_sync(FULL, (unsigned)st_samples);
-    const long long wres = __reduce_add_sync(FULL, (unsigned)st_res);
-    const long long wcache = __reduce_add_sync(FULL, (unsigned)st_cache);
-    const long long wdrop = __reduce_add_sync(FULL, (unsigned)st_drop);
-    const long long wsteps = __reduce_add_sync(FULL, (unsigned)st_steps);
-    if (lane == 0) {
-        atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->n_samples), (unsigned long long)wsamp);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->n_resamples), (unsigned long long)(CACHED ? wres : wsamp));
-        atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->n_cache_hits), (unsigned long long)wcache);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->n_dropped), (unsigned long long)wdrop);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->n_steps), (unsigned long long)wsteps);
-        atomicMax(&p.stats->n_rounds, rounds);
-    }
-}
-
-size_t render_smem_bytes() { return sizeof(RenderSmem); }
-
-template <bool CACHED, int HH>
-static cudaError_t launch_render_t(const RenderParams &p, int n_sms, cudaStream_t s)
-{
-    auto kern = render_kernel<CACHED, HH>;
-    const size_t smem = sizeof(RenderSmem);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RK_WARPS * 32, smem);
-    if (e != cudaSuccess) return e;
-    const int grid = max(1, per_sm) * n_sms;
-    kern<<<grid, RK_WARPS * 32, smem, s>>>(p);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_render(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s)
-{
-    if (cached) return head_hidden == 2 ? launch_render_t<true, 2>(p, n_sms, s) : launch_render_t<true, 1>(p, n_sms, s);
-    return head_hidden == 2 ? launch_render_t<false, 2>(p, n_sms, s) : launch_render_t<false, 1>(p, n_sms, s);
-}
 
 /* ------------------------------------------------------------------------- */
 /* network at given inputs (testing / occupancy generation)                   */

@@ -21,6 +21,21 @@ struct CacheView {
     int n_valid_slots;          /* slots written by the last build; others read as zero */
 };
 
+/* voxel of the cache data array: density, isset, 2 pad words, 8 fp16 latents */
+struct __align__(16) Voxel {
+    float density, isset, pad0, pad1;
+    uint4 lat;
+};
+
+/* state of one alive ray between sub-iterations (80 bytes) */
+struct __align__(16) RayState {
+    float4 of;    /* origin, far */
+    float4 dt;    /* direction, t1 (start of the next step) */
+    float4 acc;   /* rgb, transmittance */
+    int4 cnt;     /* pixel id, composited resample, composited cache, steps */
+    int4 cnt2;    /* dropped, done flag, samples pushed, - */
+};
+
 struct RenderStatsDev {
     unsigned long long n_samples, n_resamples, n_cache_hits, n_dropped, n_steps;
     int n_rounds, pad;
@@ -50,6 +65,18 @@ struct RenderParams {
     DevSteps csteps;
     CacheView cache;
     int render_mode;            /* 0 default, 1 only cache, 2 only resampled */
+    /* wavefront buffers */
+    RayState *states[2];        /* alive rays, ping-pong between sub-iterations */
+    int4 *ray_rows;             /* per alive ray: resample base, count, cache base, count */
+    float4 *res_rows;           /* contracted position, .w = alive slot */
+    float *res_t0;
+    uint2 *res_out;             /* fp16 logits r, g, b and log-density */
+    float4 *cache_rows;         /* froxel point, .w = alive slot */
+    float *cache_t0;
+    uint2 *cache_out;
+    int *counters;              /* [0], [1] alive rays (ping-pong), [2] resample rows, [3] cache rows */
+    int row_capacity;           /* rows per stream and sub-iteration */
+    int step_cap;               /* marching steps per ray and sub-iteration */
 };
 
 struct InferenceParams {
@@ -100,9 +127,12 @@ struct CacheBuildParams {
     int max_search;
 };
 
-size_t render_smem_bytes();
 size_t build_smem_bytes();
-cudaError_t launch_render(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s);
+/* One frame: ray generation, then sub-iterations of march / network /
+ * compositing until no ray is alive.  Reads the alive count back every
+ * `check_every` sub-iterations through h_pinned (page-locked, >= 1 int). */
+cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
+                         int check_every, int *n_iterations);
 cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
 
 __global__ void cache_init_kernel(CacheBuildParams p);

@@ -1,0 +1,562 @@
+/*
+ * fvc_render.cu - the renderer as a wavefront of small kernels per
+ * sub-iteration (PerformanceRenderer::render, src/performance_renderer.cu:
+ * 214-286, and CachePerformanceRenderer::render,
+ * src/cache_performance_renderer.cu:1059-1263):
+ *
+ *   raygen      one thread per pixel: generateRay + AABB clip; rays that hit
+ *               enter the alive list (initRayPayloads_split_kernel,
+ *               src/renderer.cu:86-134), the others are written out white.
+ *   march       one thread per alive ray: up to S occupied samples
+ *               (S = clamp(capacity / alive, 1, 8) as the reference's
+ *               n_steps), appended as compacted rows; in the cached render
+ *               each sample is classified (resample / cache / known empty)
+ *               (sample_performance_kernel :15-69,
+ *               sample_cache_performance_kernel :22-177).
+ *   net_*       one warp per 32 rows: hash grid + density net + color head
+ *               (resample rows) or trilinear cache lookup + color head (cache
+ *               rows) on the tensor cores (NerfNetwork::inference /
+ *               inferenceHead, generateNetworkInput_cache_shfl_perf_kernel_cg).
+ *   composite   one thread per alive ray: the ray's rows merged by t0 and
+ *               composited front to back with early termination; finished
+ *               rays are written out, the others compacted into the next
+ *               alive list (accumulate_performance_kernel :71-125,
+ *               accumulate_cache_perf_kernel :789-908,
+ *               compactPayloads_split_kernel src/renderer.cu:158-189).
+ *
+ * Counts live in device memory, so no kernel needs a host round trip; the
+ * host reads the alive count every few sub-iterations to stop the loop.
+ */
+#include "fvc_kernels.h"
+
+#include <cuda_fp16.h>
+
+namespace fvc {
+
+constexpr unsigned FULLMASK = 0xffffffffu;
+constexpr int S_MAX = 8;          /* MAX_N_STEPS_PER_SUBITER, include/performance_renderer.h:56 */
+constexpr int NET_WARPS = 8;
+
+__device__ __forceinline__ unsigned lane_lt() { unsigned m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+/* warp-aggregated atomicAdd: every active lane gets its offset */
+__device__ __forceinline__ int warp_alloc(int *ctr, int n)
+{
+    const unsigned act = __activemask();
+    int incl = n;
+    const int lane = lane_id();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(act, incl, o);
+        if (lane >= o && ((act >> (lane - o)) & 1u)) incl += v;
+    }
+    /* the above scan is valid only for a full warp; fall back to per-lane atomics otherwise */
+    if (act != FULLMASK) return atomicAdd(ctr, n);
+    const int total = __shfl_sync(FULLMASK, incl, 31);
+    int base = 0;
+    if (lane == 31) base = atomicAdd(ctr, total);
+    base = __shfl_sync(FULLMASK, base, 31);
+    return base + incl - n;
+}
+
+__device__ __forceinline__ void write_pixel(const RenderParams &p, int id, float4 acc, int4 counts)
+{
+    if (p.results) p.results[id] = acc;
+    if (p.ray_counts) p.ray_counts[id] = counts;
+    if (p.image) {
+        /* writeImageBuffer_performance_kernel, src/performance_renderer.cu:127-149 */
+        float cr = acc.x + acc.w, cg = acc.y + acc.w, cb = acc.z + acc.w;
+        if (p.sample_index > 0) {
+            const uchar4 prev = p.image[id];
+            const float si = (float)p.sample_index;
+            cr = (cr + (float)prev.x / 255.f * si) / (si + 1.f);
+            cg = (cg + (float)prev.y / 255.f * si) / (si + 1.f);
+            cb = (cb + (float)prev.z / 255.f * si) / (si + 1.f);
+        }
+        uchar4 o;
+        o.x = (unsigned char)min(255, max(0, (int)(cr * 256.f)));
+        o.y = (unsigned char)min(255, max(0, (int)(cg * 256.f)));
+        o.z = (unsigned char)min(255, max(0, (int)(cb * 256.f)));
+        o.w = 255;
+        p.image[id] = o;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* raygen                                                                    */
+/* ------------------------------------------------------------------------- */
+/* Pixels are visited in 8x4 tiles per warp so that a warp's rays are
+ * neighbours (coherent marching and gathers). */
+__global__ void __launch_bounds__(256) wf_raygen_kernel(RenderParams p)
+{
+    const int W = p.cam.W, H = p.cam.H;
+    const int tiles_x = (W + 7) / 8, tiles_y = (H + 3) / 4;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tile = gid >> 5, lane = lane_id();
+    if (tile >= tiles_x * tiles_y) return;
+    const int x = (tile % tiles_x) * 8 + (lane & 7), y = (tile / tiles_x) * 4 + (lane >> 3);
+    const bool valid = x < W && y < H;
+    bool hits = false;
+    float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
+    float tn = 0.f, tf = 0.f;
+    if (valid) {
+        generate_ray(p.cam, x, y, o, d);
+        hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
+    }
+    const int id = y * W + x;
+    if (valid && !hits) write_pixel(p, id, make_float4(0.f, 0.f, 0.f, 1.f), make_int4(0, 0, 0, 0));
+    const unsigned m = __ballot_sync(FULLMASK, hits);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(p.counters + 0, __popc(m));
+    base = __shfl_sync(FULLMASK, base, 0);
+    if (hits) {
+        RayState st;
+        st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
+        st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
+        st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        st.cnt = make_int4(id, 0, 0, 0);
+        st.cnt2 = make_int4(0, 0, 0, 0);
+        p.states[0][base + __popc(m & lane_lt())] = st;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* march                                                                     */
+/* ------------------------------------------------------------------------- */
+__device__ __forceinline__ const Voxel *texel(const CacheView &c, int X, int Y, int Z)
+{
+    if (X < 0 || Y < 0 || Z < 0 || X >= c.dX * 8 || Y >= c.dY * 8 || Z >= c.dZ * 8) return nullptr;
+    const int slot = (X >> 3) * (c.dY * c.dZ) + (Y >> 3) * c.dZ + (Z >> 3);
+    if (slot >= c.n_valid_slots) return nullptr; /* the reference clears the data arrays per build */
+    return reinterpret_cast<const Voxel *>(c.voxels) + (size_t)slot * 512 + ((Z & 7) * 64 + (Y & 7) * 8 + (X & 7));
+}
+
+enum : int { KIND_RESAMPLE = 0, KIND_CACHE = 1, KIND_DROP = 2, KIND_SKIP = 3 };
+
+/* Classification of one occupied sample, sample_cache_performance_kernel
+ * (src/cache_performance_renderer.cu:91-163). */
+__device__ __forceinline__ int classify(const RenderParams &p, float3 oc, float3 dc, float tm)
+{
+    float tfr;
+    const float3 fr = cam2froxel(at(oc, dc, tm), p.ccam, p.csteps, tfr);
+    const CacheView &C = p.cache;
+    const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
+    const bool inside = in_fov && fr.z >= 0.f && fr.z < (float)C.fD;
+    bool unsampled = true;
+    if (in_fov) {
+        const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
+        unsampled = tfr < p.csteps.near_ || tfr > kr;
+    }
+    if (!inside || unsampled) return p.render_mode == 1 ? KIND_SKIP : KIND_RESAMPLE;
+    if (p.render_mode == 2) return KIND_SKIP;
+    const int bx = (int)F_MUL(fr.x, 0.125f), by = (int)F_MUL(fr.y, 0.125f), bz = (int)F_MUL(fr.z, 0.125f);
+    const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
+    if (packed < 0) return KIND_DROP;
+    const float ax = F_ADD((float)(((packed >> 20) & 1023) * 8), F_SUB(fr.x, (float)(bx * 8)));
+    const float ay = F_ADD((float)(((packed >> 10) & 1023) * 8), F_SUB(fr.y, (float)(by * 8)));
+    const float az = F_ADD((float)((packed & 1023) * 8), F_SUB(fr.z, (float)(bz * 8)));
+    const Voxel *v = texel(C, (int)floorf(ax), (int)floorf(ay), (int)floorf(az));
+    if (!v || !(__ldg(&v->density) > 0.0f)) return KIND_DROP;
+    return KIND_CACHE;
+}
+
+template <bool CACHED>
+__global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
+{
+    const int n_alive = p.counters[it & 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) p.counters[(it + 1) & 1] = 0; /* next alive count */
+    const int S = max(1, min(S_MAX, p.row_capacity / max(1, n_alive)));
+    RayState *states = p.states[it & 1];
+    for (int base = blockIdx.x * blockDim.x; base < n_alive; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n_alive;
+        float t0s[S_MAX];
+        int kinds = 0; /* 2 bits per sample */
+        int n = 0, n_res = 0, n_cache = 0, steps = 0, drops = 0;
+        float4 of = make_float4(0, 0, 0, 0), dt4 = make_float4(0, 0, 0, 0);
+        int4 cnt2 = make_int4(0, 0, 0, 0);
+        bool done = false;
+        if (valid) {
+            of = states[i].of;
+            dt4 = states[i].dt;
+            cnt2 = states[i].cnt2;
+            const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
+            float3 oc = o, dc = d;
+            if (CACHED) transform_ray(p.ccam.w2c, o, d, oc, dc);
+            float t1 = dt4.w;
+            /* chunks of 4 steps: the occupancy loads of a chunk are issued together */
+            for (int c0 = 0; c0 < p.step_cap && n < S && !done; c0 += 4) {
+                float t0c[4], t1c[4];
+                bool past[4], occ[4];
+                float tt = t1;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    t0c[c] = tt;
+                    const float dtc = calc_step(p.steps, tt);
+                    t1c[c] = F_ADD(tt, dtc);
+                    const float tm = F_MUL(F_ADD(tt, t1c[c]), 0.5f);
+                    past[c] = tm > of.w;
+                    occ[c] = !past[c] && occupied(p.scene, p.bits, at(o, d, tm));
+                    tt = t1c[c];
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (done || n >= S) break;
+                    ++steps;
+                    if (past[c]) { done = true; break; }
+                    t1 = t1c[c];
+                    if (!occ[c]) continue;
+                    int kind = KIND_RESAMPLE;
+                    if (CACHED) {
+                        const float tm = F_MUL(F_ADD(t0c[c], t1c[c]), 0.5f);
+                        kind = classify(p, oc, dc, tm);
+                        if (kind == KIND_DROP) ++drops;
+                        if (kind >= KIND_DROP) continue;
+                    }
+                    t0s[n] = t0c[c];
+                    kinds |= kind << (2 * n);
+                    ++n;
+                    n_res += kind == KIND_RESAMPLE;
+                    n_cache += kind == KIND_CACHE;
+                }
+            }
+            dt4.w = t1;
+        }
+        const int rbase = warp_alloc(p.counters + 2, n_res);
+        const int cbase = CACHED ? warp_alloc(p.counters + 3, n_cache) : 0;
+        if (valid) {
+            const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
+            float3 oc = o, dc = d;
+            if (CACHED) transform_ray(p.ccam.w2c, o, d, oc, dc);
+            int r = rbase, cr = cbase;
+            for (int s = 0; s < n; ++s) {
+                const float t0 = t0s[s];
+                const float dtv = calc_step(p.steps, t0);
+                if (((kinds >> (2 * s)) & 3) == KIND_RESAMPLE) {
+                    /* plain: midpoint (t0+t1)/2 as sample_performance_kernel;
+                     * cached: t0 + dt/2 as generateNetworkInput_resample_perf_kernel :233-238 */
+                    const float tm = CACHED ? F_ADD(t0, F_MUL(dtv, 0.5f)) : F_MUL(F_ADD(t0, F_ADD(t0, dtv)), 0.5f);
+                    const float3 pc = contract(p.scene, at(o, d, tm));
+                    p.res_rows[r] = make_float4(pc.x, pc.y, pc.z, __int_as_float(i));
+                    p.res_t0[r] = t0;
+                    ++r;
+                } else {
+                    float tf2;
+                    const float3 fr = cam2froxel(at(oc, dc, F_ADD(t0, F_MUL(dtv, 0.5f))), p.ccam, p.csteps, tf2);
+                    p.cache_rows[cr] = make_float4(fr.x, fr.y, fr.z, __int_as_float(i));
+                    p.cache_t0[cr] = t0;
+                    ++cr;
+                }
+            }
+            p.ray_rows[i] = make_int4(rbase, n_res, cbase, n_cache);
+            states[i].dt = dt4;
+            cnt2.x += drops;
+            cnt2.y = done ? 1 : 0;
+            cnt2.z += n;
+            states[i].cnt2 = cnt2;
+            int4 c = states[i].cnt;
+            c.w += steps;
+            states[i].cnt = c;
+            if (p.max_samples_per_ray > 0 && cnt2.z > p.max_samples_per_ray) atomicOr(p.guard, 1);
+        }
+        /* statistics */
+        const int ws = __reduce_add_sync(FULLMASK, steps), wd = __reduce_add_sync(FULLMASK, drops);
+        if (lane_id() == 0) {
+            if (ws) atomicAdd(&p.stats->n_steps, (unsigned long long)ws);
+            if (wd) atomicAdd(&p.stats->n_dropped, (unsigned long long)wd);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* network over rows                                                         */
+/* ------------------------------------------------------------------------- */
+struct NetSmem {
+    uint2 W[W_TOTAL];
+    float bias3[64];
+    __half tile[NET_WARPS][32 * TILE_STRIDE];
+};
+
+__device__ __forceinline__ void store_logits(__half *tile, const float (&lo)[2][4], int lane)
+{
+    const int g = lane >> 2, t = lane & 3;
+    if (t < 2) {
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            __half *r0 = tile + (16 * mt + g) * TILE_STRIDE + 48 + 2 * t;
+            *reinterpret_cast<uint32_t *>(r0) = pack_h2(lo[mt][0], lo[mt][1]);
+            *reinterpret_cast<uint32_t *>(r0 + 8 * TILE_STRIDE) = pack_h2(lo[mt][2], lo[mt][3]);
+        }
+    }
+}
+
+__device__ __forceinline__ float3 dir01_of(const RayState *states, int slot)
+{
+    const float4 d = states[slot].dt;
+    return make_float3(F_DIV(F_ADD(d.x, 1.0f), 2.0f), F_DIV(F_ADD(d.y, 1.0f), 2.0f), F_DIV(F_ADD(d.z, 1.0f), 2.0f));
+}
+
+template <int HEAD_HIDDEN>
+__global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(RenderParams p, int it)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
+    const int n_rows = p.counters[2];
+    if (n_rows == 0) return;
+    for (int i = threadIdx.x; i < W_TOTAL; i += blockDim.x) S.W[i] = p.weights[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) S.bias3[i] = p.bias3[i];
+    __syncthreads();
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    __half *tile = S.tile[w];
+    __half *trow = tile + lane * TILE_STRIDE;
+    const RayState *states = p.states[it & 1];
+    const int n_batches = (n_rows + 31) / 32;
+    for (int b = blockIdx.x * NET_WARPS + w; b < n_batches; b += gridDim.x * NET_WARPS) {
+        const int r = b * 32 + lane;
+        if (r < n_rows) {
+            const float4 rw = p.res_rows[r];
+            hash_encode(p.grid, p.table, make_float3(rw.x, rw.y, rw.z), reinterpret_cast<__half2 *>(trow));
+            sh16(dir01_of(states, __float_as_int(rw.w)), reinterpret_cast<__half2 *>(trow + 32));
+        } else {
+#pragma unroll
+            for (int c = 0; c < 24; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
+        }
+        __syncwarp();
+        density_mlp(tile, S.W, lane);
+        float lo[2][4];
+        color_mlp<HEAD_HIDDEN>(tile, S.W, S.bias3, lane, lo);
+        store_logits(tile, lo, lane);
+        __syncwarp();
+        if (r < n_rows) {
+            const uint32_t rg = *reinterpret_cast<const uint32_t *>(trow + 48);
+            const uint32_t bs = (uint32_t)__half_as_ushort(trow[50]) | ((uint32_t)__half_as_ushort(trow[16]) << 16);
+            p.res_out[r] = make_uint2(rg, bs);
+        }
+        __syncwarp();
+    }
+}
+
+/* Trilinear, isset-weighted lookup of the cache for one froxel point,
+ * generateNetworkInput_cache_shfl_perf_kernel_cg
+ * (src/cache_performance_renderer.cu:678-787): head input = log of the
+ * interpolated density (not renormalised) and latents / interpolated isset. */
+__device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, int latent_offset, __half *trow)
+{
+    const float fx = F_SUB(f.x, 0.5f), fy = F_SUB(f.y, 0.5f), fz = F_SUB(f.z, 0.5f);
+    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
+    const float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
+    const Voxel *vp[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+        const float cx = x0 + (float)ox, cy = y0 + (float)oy, cz = z0 + (float)oz;
+        vp[c] = nullptr;
+        const bool inside = cx >= 0.f && cx < (float)C.fW && cy >= 0.f && cy < (float)C.fH && cz >= 0.f && cz < (float)C.fD;
+        if (inside) {
+            const int ix = (int)cx, iy = (int)cy, iz = (int)cz;
+            const int bx = ix >> 3, by = iy >> 3, bz = iz >> 3;
+            const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
+            if (packed >= 0)
+                vp[c] = texel(C, ((packed >> 20) & 1023) * 8 + (ix & 7), ((packed >> 10) & 1023) * 8 + (iy & 7),
+                              (packed & 1023) * 8 + (iz & 7));
+        }
+    }
+    float wsum = 0.f, dsum = 0.f, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (!vp[c]) continue;
+        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+        const float w = (ox ? lx : 1.0f - lx) * (oy ? ly : 1.0f - ly) * (oz ? lz : 1.0f - lz);
+        const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
+        const uint4 lt = __ldg(&vp[c]->lat);
+        wsum = fmaf(w, di.y, wsum);
+        dsum = fmaf(w, di.x, dsum);
+        const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 fq = __half22float2(*reinterpret_cast<const __half2 *>(&lw[q]));
+            ls[2 * q] = fmaf(w, fq.x, ls[2 * q]);
+            ls[2 * q + 1] = fmaf(w, fq.y, ls[2 * q + 1]);
+        }
+    }
+    uint32_t *hin = reinterpret_cast<uint32_t *>(trow + 16);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) hin[c] = 0u;
+    trow[16] = __float2half_rn(logf(fmaxf(dsum, 1e-6f)));
+    const float inv = 1.0f / wsum;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) trow[16 + latent_offset + j] = __float2half_rn(ls[j] * inv);
+}
+
+template <int HEAD_HIDDEN>
+__global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderParams p, int it)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
+    const int n_rows = p.counters[3];
+    if (n_rows == 0) return;
+    for (int i = threadIdx.x; i < W_TOTAL; i += blockDim.x) S.W[i] = p.weights[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) S.bias3[i] = p.bias3[i];
+    __syncthreads();
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    __half *tile = S.tile[w];
+    __half *trow = tile + lane * TILE_STRIDE;
+    const RayState *states = p.states[it & 1];
+    const int n_batches = (n_rows + 31) / 32;
+    for (int b = blockIdx.x * NET_WARPS + w; b < n_batches; b += gridDim.x * NET_WARPS) {
+        const int r = b * 32 + lane;
+        if (r < n_rows) {
+            const float4 rw = p.cache_rows[r];
+            cache_lookup(p.cache, make_float3(rw.x, rw.y, rw.z), p.latent_offset, trow);
+            sh16(dir01_of(states, __float_as_int(rw.w)), reinterpret_cast<__half2 *>(trow + 32));
+        } else {
+#pragma unroll
+            for (int c = 8; c < 24; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
+        }
+        __syncwarp();
+        float lo[2][4];
+        color_mlp<HEAD_HIDDEN>(tile, S.W, S.bias3, lane, lo);
+        store_logits(tile, lo, lane);
+        __syncwarp();
+        if (r < n_rows) {
+            const uint32_t rg = *reinterpret_cast<const uint32_t *>(trow + 48);
+            const uint32_t bs = (uint32_t)__half_as_ushort(trow[50]) | ((uint32_t)__half_as_ushort(trow[16]) << 16);
+            p.cache_out[r] = make_uint2(rg, bs);
+        }
+        __syncwarp();
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* composite + compaction                                                    */
+/* ------------------------------------------------------------------------- */
+__global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int it)
+{
+    const int n_alive = p.counters[it & 1];
+    RayState *cur = p.states[it & 1], *nxt = p.states[(it + 1) & 1];
+    for (int base = blockIdx.x * blockDim.x; base < n_alive; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n_alive;
+        bool keep = false;
+        RayState st;
+        int n_comp = 0;
+        if (valid) {
+            st = cur[i];
+            const int4 rr = p.ray_rows[i];
+            float4 acc = st.acc;
+            int c_res = st.cnt.y, c_cache = st.cnt.z;
+            int a = 0, b = 0;
+            bool term = false;
+            /* merge by t0, ties to the cache stream (accumulate_cache_perf_kernel :270-304) */
+            while (a < rr.y || b < rr.w) {
+                float t0_a = a < rr.y ? p.res_t0[rr.x + a] : 1e10f;
+                float t0_b = b < rr.w ? p.cache_t0[rr.z + b] : 1e10f;
+                uint2 ov;
+                float t0;
+                if (b >= rr.w || t0_a < t0_b) { ov = p.res_out[rr.x + a]; t0 = t0_a; ++a; ++c_res; }
+                else { ov = p.cache_out[rr.z + b]; t0 = t0_b; ++b; ++c_cache; }
+                ++n_comp;
+                const float2 rg = __half22float2(*reinterpret_cast<const __half2 *>(&ov.x));
+                const float lb = __half2float(__ushort_as_half((unsigned short)(ov.y & 0xffffu)));
+                const float ld = __half2float(__ushort_as_half((unsigned short)(ov.y >> 16)));
+                const float dt = calc_step(p.steps, t0);
+                const float sigma = expf(ld);
+                const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
+                if (alpha > p.scene.alpha_thre) {
+                    const float wgt = alpha * acc.w;
+                    acc.x += wgt / (1.0f + expf(-rg.x));
+                    acc.y += wgt / (1.0f + expf(-rg.y));
+                    acc.z += wgt / (1.0f + expf(-lb));
+                    acc.w *= 1.0f - alpha;
+                }
+                if (acc.w < 1e-4f) { term = true; break; }
+            }
+            st.acc = acc;
+            st.cnt.y = c_res;
+            st.cnt.z = c_cache;
+            if (term || st.cnt2.y) {
+                write_pixel(p, st.cnt.x, acc, make_int4(c_res, c_cache, st.cnt2.x, st.cnt.w));
+            } else {
+                keep = true;
+            }
+        }
+        const int ws = __reduce_add_sync(FULLMASK, n_comp);
+        if (lane_id() == 0 && ws) atomicAdd(&p.stats->n_samples, (unsigned long long)ws);
+        const unsigned m = __ballot_sync(FULLMASK, keep);
+        int nb = 0;
+        if (lane_id() == 0 && m) nb = atomicAdd(p.counters + ((it + 1) & 1), __popc(m));
+        nb = __shfl_sync(FULLMASK, nb, 0);
+        if (keep) nxt[nb + __popc(m & lane_lt())] = st;
+    }
+}
+
+/* resets the row counters after the network kernels consumed them */
+__global__ void wf_reset_rows_kernel(RenderParams p)
+{
+    if (threadIdx.x == 0) {
+        atomicAdd(&p.stats->n_resamples, (unsigned long long)p.counters[2]);
+        atomicAdd(&p.stats->n_cache_hits, (unsigned long long)p.counters[3]);
+        p.counters[2] = 0;
+        p.counters[3] = 0;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* host side                                                                 */
+/* ------------------------------------------------------------------------- */
+template <int HH>
+static cudaError_t set_net_attrs()
+{
+    const int smem = (int)sizeof(NetSmem);
+    cudaError_t e = cudaFuncSetAttribute(wf_net_resample_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_cache_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return e;
+}
+
+template <bool CACHED, int HH>
+static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, int *h_pinned, int check_every, int *n_iter)
+{
+    static bool attrs_set = false;
+    if (!attrs_set) {
+        cudaError_t e = set_net_attrs<HH>();
+        if (e != cudaSuccess) return e;
+        attrs_set = true;
+    }
+    const int W = p.cam.W, H = p.cam.H;
+    const int n_threads = ((W + 7) / 8) * ((H + 3) / 4) * 32;
+    wf_raygen_kernel<<<(n_threads + 255) / 256, 256, 0, s>>>(p);
+    const int grid_ray = n_sms * 16;
+    const int grid_net = n_sms * 2;
+    const size_t net_smem = sizeof(NetSmem);
+    int it = 0;
+    const int max_it = 1 << 20;
+    for (; it < max_it; ++it) {
+        wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+        wf_net_resample_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+        if (CACHED) wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+        wf_composite_kernel<<<grid_ray, 128, 0, s>>>(p, it);
+        wf_reset_rows_kernel<<<1, 32, 0, s>>>(p);
+        if ((it + 1) % check_every == 0) {
+            cudaError_t e = cudaMemcpyAsync(h_pinned, p.counters + ((it + 1) & 1), sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) return e;
+            e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            if (*h_pinned == 0) { ++it; break; }
+        }
+    }
+    if (n_iter) *n_iter = it;
+    return cudaGetLastError();
+}
+
+cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
+                         int check_every, int *n_iterations)
+{
+    if (cached)
+        return head_hidden == 2 ? run_frame<true, 2>(p, n_sms, s, h_pinned, check_every, n_iterations)
+                                : run_frame<true, 1>(p, n_sms, s, h_pinned, check_every, n_iterations);
+    return head_hidden == 2 ? run_frame<false, 2>(p, n_sms, s, h_pinned, check_every, n_iterations)
+                            : run_frame<false, 1>(p, n_sms, s, h_pinned, check_every, n_iterations);
+}
+
+}  // namespace fvc

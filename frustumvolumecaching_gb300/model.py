@@ -78,7 +78,8 @@ class HashLevel:
     dense: bool       # res^3 <= size: direct indexing instead of hashing
 
 
-def hash_grid_levels(n_levels: int, base_res: int, per_level_scale: float, log2_T: int) -> list[HashLevel]:
+def hash_grid_levels(n_levels: int, base_res: int, per_level_scale: float, log2_T: int,
+                     scales: list | None = None) -> list[HashLevel]:
     """Per-level layout of the multiresolution hash grid.
 
     Multiresolution levels with geometric growth (Mueller et al. 2022,
@@ -95,6 +96,8 @@ def hash_grid_levels(n_levels: int, base_res: int, per_level_scale: float, log2_
     off = 0
     for l in range(n_levels):
         scale = f32(np.exp2(f32(l) * log2_b, dtype=f32) * f32(base_res) - f32(1.0))
+        if scales is not None:  # explicit per-level scales (config.json fvc_level_scales)
+            scale = f32(scales[l])
         res = int(math.ceil(float(scale))) + 1
         n = res ** 3
         n = (n + 7) // 8 * 8

@@ -136,7 +136,7 @@ typedef struct {
     long long n_cache_hits;          /* samples served from the cache        */
     long long n_dropped;             /* known-empty cache voxels skipped     */
     long long n_steps;               /* marching steps taken                 */
-    int n_rounds;                    /* persistent-kernel rounds (max over warps) */
+    int n_rounds;                    /* sub-iterations of the last render */
     int guard_flags;                 /* device guard bits (0 = none fired)   */
 } fvc_render_stats_t;
 
@@ -212,7 +212,10 @@ typedef struct {
 /* render(RaymarchInfo, RenderBuffer&, DebugData*) of the renderer's kind:
  * PerformanceRenderer::render (src/performance_renderer.cu:214-286) or
  * CachePerformanceRenderer::render (src/cache_performance_renderer.cu:1059-1263).
- * Device pointers; enqueued on the renderer stream, not synchronised. */
+ * Device pointers.  The sub-iterations are enqueued on the renderer stream;
+ * the host reads the alive-ray count back every 4 sub-iterations, so the
+ * call returns once the last sub-iteration is enqueued (the final writes may
+ * still be in flight on the stream). */
 int fvc_render_device(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out);
 /* Same with host pointers: H2D of the previous image (progressive average),
  * render, D2H of the outputs, synchronise. */

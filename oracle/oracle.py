@@ -156,11 +156,8 @@ class OracleModel:
         self.scene = make_scene(sc)
         self.steps = make_steps(self.scene, sc["cone_angle"], sc["stepsize"], sc["near"], sc["far"], use_libm)
         enc = cfg["mlp_base"]["encoding"]
-        self.levels = hash_grid_levels(enc["n_levels"], enc["base_resolution"], enc["per_level_scale"], enc["log2_hashmap_size"])
-        if "fvc_level_scales" in enc:
-            for lv, sc in zip(self.levels, enc["fvc_level_scales"]):
-                assert np.float32(sc) == np.float32(lv.scale)
-                lv.scale = float(np.float32(sc))
+        self.levels = hash_grid_levels(enc["n_levels"], enc["base_resolution"], enc["per_level_scale"],
+                                       enc["log2_hashmap_size"], enc.get("fvc_level_scales"))
         F = enc["n_features_per_level"]
         self.table = np.fromfile(os.path.join(model_dir, "pos_enc.dat"), np.uint16)
         n_entries = self.levels[-1].offset + self.levels[-1].size
