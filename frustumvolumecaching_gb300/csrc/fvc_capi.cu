@@ -339,17 +339,20 @@ struct fvc_renderer {
     int *h_pinned = nullptr;          /* readback of build counters */
     /* wavefront buffers (fvc_render.cu) */
     RayState *d_states[2] = {nullptr, nullptr};
-    int4 *d_ray_rows = nullptr;
-    float4 *d_res_rows = nullptr, *d_cache_rows = nullptr;
-    float *d_res_t0 = nullptr, *d_cache_t0 = nullptr;
-    uint2 *d_res_out = nullptr, *d_cache_out = nullptr;
+    int2 *d_ray_rows = nullptr;
+    float *d_row_t0 = nullptr;
+    int *d_row_slot = nullptr;
+    uint8_t *d_row_kind = nullptr;
+    float4 *d_row_pay = nullptr;
+    uint2 *d_row_out = nullptr;
+    int *d_res_list = nullptr, *d_cache_list = nullptr;
     int *d_wf_counters = nullptr;
     int row_capacity = 0;
     int last_iterations = 0;
     void release_wavefront()
     {
-        dfree(d_states[0]); dfree(d_states[1]); dfree(d_ray_rows); dfree(d_res_rows); dfree(d_cache_rows);
-        dfree(d_res_t0); dfree(d_cache_t0); dfree(d_res_out); dfree(d_cache_out); dfree(d_wf_counters);
+        dfree(d_states[0]); dfree(d_states[1]); dfree(d_ray_rows); dfree(d_row_t0); dfree(d_row_slot);
+        dfree(d_row_kind); dfree(d_row_pay); dfree(d_row_out); dfree(d_res_list); dfree(d_cache_list); dfree(d_wf_counters);
         row_capacity = 0;
     }
     fvc_cache *cache = nullptr, *next = nullptr;
@@ -667,21 +670,22 @@ extern "C" int fvc_renderer_resize(fvc_renderer *r, int width, int height)
     if ((rc = dalloc(&r->d_image, n, "image"))) return rc;
     if ((rc = dalloc(&r->d_counts, n, "ray counts"))) return rc;
     CU(cudaMemset(r->d_image, 0, n * sizeof(uchar4)));
-    /* wavefront: alive-ray states (ping-pong) and up to 8 sample rows per
-     * ray and stream per sub-iteration (MAX_N_STEPS_PER_SUBITER) */
+    /* wavefront: alive-ray states (ping-pong) and up to 16 sample rows per
+     * ray and sub-iteration */
     r->release_wavefront();
-    const size_t cap = std::min<size_t>(n * 8, (size_t)1 << 24);
+    const size_t cap = std::min<size_t>(n * 16, (size_t)1 << 25);
     const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
     if ((rc = dalloc(&r->d_states[0], n, "ray states"))) return rc;
     if ((rc = dalloc(&r->d_states[1], n, "ray states"))) return rc;
     if ((rc = dalloc(&r->d_ray_rows, n, "ray rows"))) return rc;
-    if ((rc = dalloc(&r->d_res_rows, cap, "resample rows"))) return rc;
-    if ((rc = dalloc(&r->d_res_t0, cap, "resample t0"))) return rc;
-    if ((rc = dalloc(&r->d_res_out, cap, "resample outputs"))) return rc;
+    if ((rc = dalloc(&r->d_row_t0, cap, "row t0"))) return rc;
+    if ((rc = dalloc(&r->d_row_slot, cap, "row slots"))) return rc;
+    if ((rc = dalloc(&r->d_row_pay, cap, "row inputs"))) return rc;
+    if ((rc = dalloc(&r->d_row_out, cap, "row outputs"))) return rc;
     if (cached) {
-        if ((rc = dalloc(&r->d_cache_rows, cap, "cache rows"))) return rc;
-        if ((rc = dalloc(&r->d_cache_t0, cap, "cache t0"))) return rc;
-        if ((rc = dalloc(&r->d_cache_out, cap, "cache outputs"))) return rc;
+        if ((rc = dalloc(&r->d_row_kind, cap, "row kinds"))) return rc;
+        if ((rc = dalloc(&r->d_res_list, cap, "resample list"))) return rc;
+        if ((rc = dalloc(&r->d_cache_list, cap, "cache list"))) return rc;
     }
     if ((rc = dalloc(&r->d_wf_counters, (size_t)8, "wavefront counters"))) return rc;
     r->row_capacity = (int)cap;
@@ -745,11 +749,12 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
     }
     p.states[0] = r->d_states[0]; p.states[1] = r->d_states[1];
     p.ray_rows = r->d_ray_rows;
-    p.res_rows = r->d_res_rows; p.res_t0 = r->d_res_t0; p.res_out = r->d_res_out;
-    p.cache_rows = r->d_cache_rows; p.cache_t0 = r->d_cache_t0; p.cache_out = r->d_cache_out;
+    p.row_t0 = r->d_row_t0; p.row_slot = r->d_row_slot; p.row_kind = r->d_row_kind;
+    p.row_pay = r->d_row_pay; p.row_out = r->d_row_out;
+    p.res_list = r->d_res_list; p.cache_list = r->d_cache_list;
     p.counters = r->d_wf_counters;
     p.row_capacity = r->row_capacity;
-    p.step_cap = 256;
+    p.steps_per_iter = 64;
     CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
     CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));

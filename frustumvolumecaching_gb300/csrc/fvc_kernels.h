@@ -67,16 +67,16 @@ struct RenderParams {
     int render_mode;            /* 0 default, 1 only cache, 2 only resampled */
     /* wavefront buffers */
     RayState *states[2];        /* alive rays, ping-pong between sub-iterations */
-    int4 *ray_rows;             /* per alive ray: resample base, count, cache base, count */
-    float4 *res_rows;           /* contracted position, .w = alive slot */
-    float *res_t0;
-    uint2 *res_out;             /* fp16 logits r, g, b and log-density */
-    float4 *cache_rows;         /* froxel point, .w = alive slot */
-    float *cache_t0;
-    uint2 *cache_out;
-    int *counters;              /* [0], [1] alive rays (ping-pong), [2] resample rows, [3] cache rows */
-    int row_capacity;           /* rows per stream and sub-iteration */
-    int step_cap;               /* marching steps per ray and sub-iteration */
+    int2 *ray_rows;             /* per alive ray: first row, number of rows (in t order) */
+    float *row_t0;              /* per row: t0 of the sample */
+    int *row_slot;              /* per row: alive slot of its ray */
+    uint8_t *row_kind;          /* per row: resample / cache / known empty / skipped */
+    float4 *row_pay;            /* per row: contracted position or froxel point */
+    uint2 *row_out;             /* per row: fp16 logits r, g, b and log-density */
+    int *res_list, *cache_list; /* row ids of the two network streams */
+    int *counters;              /* [0], [1] alive rays (ping-pong), [2] rows, [3] resample, [4] cache */
+    int row_capacity;           /* rows per sub-iteration */
+    int steps_per_iter;         /* marching steps per ray and sub-iteration */
 };
 
 struct InferenceParams {

@@ -34,7 +34,7 @@
 namespace fvc {
 
 constexpr unsigned FULLMASK = 0xffffffffu;
-constexpr int S_MAX = 8;          /* MAX_N_STEPS_PER_SUBITER, include/performance_renderer.h:56 */
+constexpr int S_ROWS = 16;        /* rows per ray and sub-iteration (the reference keeps up to 8) */
 constexpr int NET_WARPS = 8;
 
 __device__ __forceinline__ unsigned lane_lt() { unsigned m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
@@ -161,32 +161,31 @@ __device__ __forceinline__ int classify(const RenderParams &p, float3 oc, float3
     return KIND_CACHE;
 }
 
+/* Marches every alive ray a fixed number of steps (lanes stay converged),
+ * keeping at most S_ROWS occupied samples; the samples become rows
+ * (t0, alive slot) that are contiguous and in t order per ray.  The plain
+ * renderer also contracts the sample position here; the cached renderer
+ * classifies the rows in wf_classify_kernel. */
 template <bool CACHED>
 __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
 {
     const int n_alive = p.counters[it & 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) p.counters[(it + 1) & 1] = 0; /* next alive count */
-    const int S = max(1, min(S_MAX, p.row_capacity / max(1, n_alive)));
+    const int S = max(1, min(S_ROWS, p.row_capacity / max(1, n_alive)));
     RayState *states = p.states[it & 1];
     for (int base = blockIdx.x * blockDim.x; base < n_alive; base += gridDim.x * blockDim.x) {
         const int i = base + threadIdx.x;
         const bool valid = i < n_alive;
-        float t0s[S_MAX];
-        int kinds = 0; /* 2 bits per sample */
-        int n = 0, n_res = 0, n_cache = 0, steps = 0, drops = 0;
+        float t0s[S_ROWS];
+        int n = 0, steps = 0;
         float4 of = make_float4(0, 0, 0, 0), dt4 = make_float4(0, 0, 0, 0);
-        int4 cnt2 = make_int4(0, 0, 0, 0);
         bool done = false;
         if (valid) {
             of = states[i].of;
             dt4 = states[i].dt;
-            cnt2 = states[i].cnt2;
             const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
-            float3 oc = o, dc = d;
-            if (CACHED) transform_ray(p.ccam.w2c, o, d, oc, dc);
             float t1 = dt4.w;
-            /* chunks of 4 steps: the occupancy loads of a chunk are issued together */
-            for (int c0 = 0; c0 < p.step_cap && n < S && !done; c0 += 4) {
+            for (int c0 = 0; c0 < p.steps_per_iter; c0 += 4) {
                 float t0c[4], t1c[4];
                 bool past[4], occ[4];
                 float tt = t1;
@@ -202,70 +201,92 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
                 }
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    if (done || n >= S) break;
-                    ++steps;
-                    if (past[c]) { done = true; break; }
-                    t1 = t1c[c];
-                    if (!occ[c]) continue;
-                    int kind = KIND_RESAMPLE;
-                    if (CACHED) {
-                        const float tm = F_MUL(F_ADD(t0c[c], t1c[c]), 0.5f);
-                        kind = classify(p, oc, dc, tm);
-                        if (kind == KIND_DROP) ++drops;
-                        if (kind >= KIND_DROP) continue;
+                    if (!done && n < S) {
+                        ++steps;
+                        if (past[c]) {
+                            done = true;
+                        } else {
+                            t1 = t1c[c];
+                            if (occ[c]) t0s[n++] = t0c[c];
+                        }
                     }
-                    t0s[n] = t0c[c];
-                    kinds |= kind << (2 * n);
-                    ++n;
-                    n_res += kind == KIND_RESAMPLE;
-                    n_cache += kind == KIND_CACHE;
                 }
+                if (done || n >= S) break;
             }
             dt4.w = t1;
         }
-        const int rbase = warp_alloc(p.counters + 2, n_res);
-        const int cbase = CACHED ? warp_alloc(p.counters + 3, n_cache) : 0;
+        const int rbase = warp_alloc(p.counters + 2, n);
         if (valid) {
-            const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
-            float3 oc = o, dc = d;
-            if (CACHED) transform_ray(p.ccam.w2c, o, d, oc, dc);
-            int r = rbase, cr = cbase;
             for (int s = 0; s < n; ++s) {
-                const float t0 = t0s[s];
-                const float dtv = calc_step(p.steps, t0);
-                if (((kinds >> (2 * s)) & 3) == KIND_RESAMPLE) {
-                    /* plain: midpoint (t0+t1)/2 as sample_performance_kernel;
-                     * cached: t0 + dt/2 as generateNetworkInput_resample_perf_kernel :233-238 */
-                    const float tm = CACHED ? F_ADD(t0, F_MUL(dtv, 0.5f)) : F_MUL(F_ADD(t0, F_ADD(t0, dtv)), 0.5f);
-                    const float3 pc = contract(p.scene, at(o, d, tm));
-                    p.res_rows[r] = make_float4(pc.x, pc.y, pc.z, __int_as_float(i));
-                    p.res_t0[r] = t0;
-                    ++r;
-                } else {
-                    float tf2;
-                    const float3 fr = cam2froxel(at(oc, dc, F_ADD(t0, F_MUL(dtv, 0.5f))), p.ccam, p.csteps, tf2);
-                    p.cache_rows[cr] = make_float4(fr.x, fr.y, fr.z, __int_as_float(i));
-                    p.cache_t0[cr] = t0;
-                    ++cr;
+                p.row_t0[rbase + s] = t0s[s];
+                p.row_slot[rbase + s] = i;
+                if (!CACHED) {
+                    /* sample_performance_kernel :52-58: midpoint (t0+t1)/2, contracted */
+                    const float t0 = t0s[s];
+                    const float tm = F_MUL(F_ADD(t0, F_ADD(t0, calc_step(p.steps, t0))), 0.5f);
+                    const float3 pc = contract(p.scene, at(make_float3(of.x, of.y, of.z), make_float3(dt4.x, dt4.y, dt4.z), tm));
+                    p.row_pay[rbase + s] = make_float4(pc.x, pc.y, pc.z, 0.f);
                 }
             }
-            p.ray_rows[i] = make_int4(rbase, n_res, cbase, n_cache);
+            p.ray_rows[i] = make_int2(rbase, n);
             states[i].dt = dt4;
-            cnt2.x += drops;
-            cnt2.y = done ? 1 : 0;
-            cnt2.z += n;
-            states[i].cnt2 = cnt2;
             int4 c = states[i].cnt;
             c.w += steps;
             states[i].cnt = c;
-            if (p.max_samples_per_ray > 0 && cnt2.z > p.max_samples_per_ray) atomicOr(p.guard, 1);
+            int4 c2 = states[i].cnt2;
+            c2.y = done ? 1 : 0;
+            c2.z += n;
+            states[i].cnt2 = c2;
+            if (p.max_samples_per_ray > 0 && c2.z > p.max_samples_per_ray) atomicOr(p.guard, 1);
         }
-        /* statistics */
-        const int ws = __reduce_add_sync(FULLMASK, steps), wd = __reduce_add_sync(FULLMASK, drops);
+        const int ws = __reduce_add_sync(FULLMASK, steps);
+        if (lane_id() == 0 && ws) atomicAdd(&p.stats->n_steps, (unsigned long long)ws);
+    }
+}
+
+/* One thread per row of the cached render: classification
+ * (sample_cache_performance_kernel :91-163) and the network input of the
+ * row (generateNetworkInput_resample_perf_kernel :231-238 /
+ * _preparation_perf_kernel :284-297 evaluate it at t0 + dt/2); appends the
+ * row id to the resample or cache list. */
+__global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it)
+{
+    const int n_rows = p.counters[2];
+    const RayState *states = p.states[it & 1];
+    for (int base = blockIdx.x * blockDim.x; base < n_rows; base += gridDim.x * blockDim.x) {
+        const int r = base + threadIdx.x;
+        int kind = KIND_SKIP;
+        if (r < n_rows) {
+            const int slot = p.row_slot[r];
+            const float t0 = p.row_t0[r];
+            const float4 of = states[slot].of, dt4 = states[slot].dt;
+            const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
+            float3 oc, dc;
+            transform_ray(p.ccam.w2c, o, d, oc, dc);
+            const float dt = calc_step(p.steps, t0);
+            const float tm = F_MUL(F_ADD(t0, F_ADD(t0, dt)), 0.5f);
+            kind = classify(p, oc, dc, tm);
+            const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));
+            if (kind == KIND_RESAMPLE) {
+                const float3 pc = contract(p.scene, at(o, d, tmh));
+                p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
+            } else if (kind == KIND_CACHE) {
+                float tf2;
+                const float3 fr = cam2froxel(at(oc, dc, tmh), p.ccam, p.csteps, tf2);
+                p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
+            }
+            p.row_kind[r] = (uint8_t)kind;
+        }
+        const unsigned m0 = __ballot_sync(FULLMASK, kind == KIND_RESAMPLE), m1 = __ballot_sync(FULLMASK, kind == KIND_CACHE);
+        int b0 = 0, b1 = 0;
         if (lane_id() == 0) {
-            if (ws) atomicAdd(&p.stats->n_steps, (unsigned long long)ws);
-            if (wd) atomicAdd(&p.stats->n_dropped, (unsigned long long)wd);
+            if (m0) b0 = atomicAdd(p.counters + 3, __popc(m0));
+            if (m1) b1 = atomicAdd(p.counters + 4, __popc(m1));
         }
+        b0 = __shfl_sync(FULLMASK, b0, 0);
+        b1 = __shfl_sync(FULLMASK, b1, 0);
+        if (kind == KIND_RESAMPLE) p.res_list[b0 + __popc(m0 & lane_lt())] = r;
+        if (kind == KIND_CACHE) p.cache_list[b1 + __popc(m1 & lane_lt())] = r;
     }
 }
 
@@ -297,12 +318,13 @@ __device__ __forceinline__ float3 dir01_of(const RayState *states, int slot)
     return make_float3(F_DIV(F_ADD(d.x, 1.0f), 2.0f), F_DIV(F_ADD(d.y, 1.0f), 2.0f), F_DIV(F_ADD(d.z, 1.0f), 2.0f));
 }
 
-template <int HEAD_HIDDEN>
+/* Network over the resample rows (all rows of the plain renderer). */
+template <int HEAD_HIDDEN, bool LIST>
 __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(RenderParams p, int it)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
-    const int n_rows = p.counters[2];
+    const int n_rows = LIST ? p.counters[3] : p.counters[2];
     if (n_rows == 0) return;
     for (int i = threadIdx.x; i < W_TOTAL; i += blockDim.x) S.W[i] = p.weights[i];
     for (int i = threadIdx.x; i < 64; i += blockDim.x) S.bias3[i] = p.bias3[i];
@@ -313,11 +335,12 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(Rend
     const RayState *states = p.states[it & 1];
     const int n_batches = (n_rows + 31) / 32;
     for (int b = blockIdx.x * NET_WARPS + w; b < n_batches; b += gridDim.x * NET_WARPS) {
-        const int r = b * 32 + lane;
-        if (r < n_rows) {
-            const float4 rw = p.res_rows[r];
-            hash_encode(p.grid, p.table, make_float3(rw.x, rw.y, rw.z), reinterpret_cast<__half2 *>(trow));
-            sh16(dir01_of(states, __float_as_int(rw.w)), reinterpret_cast<__half2 *>(trow + 32));
+        const int k = b * 32 + lane;
+        const int r = k < n_rows ? (LIST ? p.res_list[k] : k) : -1;
+        if (r >= 0) {
+            const float4 pw = p.row_pay[r];
+            hash_encode(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), reinterpret_cast<__half2 *>(trow));
+            sh16(dir01_of(states, p.row_slot[r]), reinterpret_cast<__half2 *>(trow + 32));
         } else {
 #pragma unroll
             for (int c = 0; c < 24; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
@@ -328,10 +351,10 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(Rend
         color_mlp<HEAD_HIDDEN>(tile, S.W, S.bias3, lane, lo);
         store_logits(tile, lo, lane);
         __syncwarp();
-        if (r < n_rows) {
+        if (r >= 0) {
             const uint32_t rg = *reinterpret_cast<const uint32_t *>(trow + 48);
             const uint32_t bs = (uint32_t)__half_as_ushort(trow[50]) | ((uint32_t)__half_as_ushort(trow[16]) << 16);
-            p.res_out[r] = make_uint2(rg, bs);
+            p.row_out[r] = make_uint2(rg, bs);
         }
         __syncwarp();
     }
@@ -394,7 +417,7 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
-    const int n_rows = p.counters[3];
+    const int n_rows = p.counters[4];
     if (n_rows == 0) return;
     for (int i = threadIdx.x; i < W_TOTAL; i += blockDim.x) S.W[i] = p.weights[i];
     for (int i = threadIdx.x; i < 64; i += blockDim.x) S.bias3[i] = p.bias3[i];
@@ -405,11 +428,12 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
     const RayState *states = p.states[it & 1];
     const int n_batches = (n_rows + 31) / 32;
     for (int b = blockIdx.x * NET_WARPS + w; b < n_batches; b += gridDim.x * NET_WARPS) {
-        const int r = b * 32 + lane;
-        if (r < n_rows) {
-            const float4 rw = p.cache_rows[r];
-            cache_lookup(p.cache, make_float3(rw.x, rw.y, rw.z), p.latent_offset, trow);
-            sh16(dir01_of(states, __float_as_int(rw.w)), reinterpret_cast<__half2 *>(trow + 32));
+        const int k = b * 32 + lane;
+        const int r = k < n_rows ? p.cache_list[k] : -1;
+        if (r >= 0) {
+            const float4 pw = p.row_pay[r];
+            cache_lookup(p.cache, make_float3(pw.x, pw.y, pw.z), p.latent_offset, trow);
+            sh16(dir01_of(states, p.row_slot[r]), reinterpret_cast<__half2 *>(trow + 32));
         } else {
 #pragma unroll
             for (int c = 8; c < 24; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
@@ -419,10 +443,10 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
         color_mlp<HEAD_HIDDEN>(tile, S.W, S.bias3, lane, lo);
         store_logits(tile, lo, lane);
         __syncwarp();
-        if (r < n_rows) {
+        if (r >= 0) {
             const uint32_t rg = *reinterpret_cast<const uint32_t *>(trow + 48);
             const uint32_t bs = (uint32_t)__half_as_ushort(trow[50]) | ((uint32_t)__half_as_ushort(trow[16]) << 16);
-            p.cache_out[r] = make_uint2(rg, bs);
+            p.row_out[r] = make_uint2(rg, bs);
         }
         __syncwarp();
     }
@@ -431,6 +455,7 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
 /* ------------------------------------------------------------------------- */
 /* composite + compaction                                                    */
 /* ------------------------------------------------------------------------- */
+template <bool CACHED>
 __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int it)
 {
     const int n_alive = p.counters[it & 1];
@@ -443,20 +468,23 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
         int n_comp = 0;
         if (valid) {
             st = cur[i];
-            const int4 rr = p.ray_rows[i];
+            const int2 rr = p.ray_rows[i];
             float4 acc = st.acc;
-            int c_res = st.cnt.y, c_cache = st.cnt.z;
-            int a = 0, b = 0;
+            int c_res = st.cnt.y, c_cache = st.cnt.z, c_drop = st.cnt2.x;
             bool term = false;
-            /* merge by t0, ties to the cache stream (accumulate_cache_perf_kernel :270-304) */
-            while (a < rr.y || b < rr.w) {
-                float t0_a = a < rr.y ? p.res_t0[rr.x + a] : 1e10f;
-                float t0_b = b < rr.w ? p.cache_t0[rr.z + b] : 1e10f;
-                uint2 ov;
-                float t0;
-                if (b >= rr.w || t0_a < t0_b) { ov = p.res_out[rr.x + a]; t0 = t0_a; ++a; ++c_res; }
-                else { ov = p.cache_out[rr.z + b]; t0 = t0_b; ++b; ++c_cache; }
+            /* rows are in t order: the merge of the resample and cache
+             * streams of accumulate_cache_perf_kernel (:270-304) */
+            for (int j = 0; j < rr.y; ++j) {
+                const int r = rr.x + j;
+                const int kind = CACHED ? (int)p.row_kind[r] : KIND_RESAMPLE;
+                if (kind >= KIND_DROP) {
+                    c_drop += kind == KIND_DROP;
+                    continue;
+                }
+                if (kind == KIND_CACHE) ++c_cache; else ++c_res;
                 ++n_comp;
+                const uint2 ov = p.row_out[r];
+                const float t0 = p.row_t0[r];
                 const float2 rg = __half22float2(*reinterpret_cast<const __half2 *>(&ov.x));
                 const float lb = __half2float(__ushort_as_half((unsigned short)(ov.y & 0xffffu)));
                 const float ld = __half2float(__ushort_as_half((unsigned short)(ov.y >> 16)));
@@ -475,8 +503,9 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
             st.acc = acc;
             st.cnt.y = c_res;
             st.cnt.z = c_cache;
+            st.cnt2.x = c_drop;
             if (term || st.cnt2.y) {
-                write_pixel(p, st.cnt.x, acc, make_int4(c_res, c_cache, st.cnt2.x, st.cnt.w));
+                write_pixel(p, st.cnt.x, acc, make_int4(c_res, c_cache, c_drop, st.cnt.w));
             } else {
                 keep = true;
             }
@@ -491,14 +520,16 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
     }
 }
 
-/* resets the row counters after the network kernels consumed them */
-__global__ void wf_reset_rows_kernel(RenderParams p)
+/* resets the row counters after the kernels of the sub-iteration consumed them */
+__global__ void wf_reset_rows_kernel(RenderParams p, int cached)
 {
     if (threadIdx.x == 0) {
-        atomicAdd(&p.stats->n_resamples, (unsigned long long)p.counters[2]);
-        atomicAdd(&p.stats->n_cache_hits, (unsigned long long)p.counters[3]);
+        atomicAdd(&p.stats->n_resamples, (unsigned long long)(cached ? p.counters[3] : p.counters[2]));
+        atomicAdd(&p.stats->n_cache_hits, (unsigned long long)p.counters[4]);
+        atomicAdd(&p.stats->n_dropped, (unsigned long long)(cached ? p.counters[2] - p.counters[3] - p.counters[4] : 0));
         p.counters[2] = 0;
         p.counters[3] = 0;
+        p.counters[4] = 0;
     }
 }
 
@@ -509,7 +540,8 @@ template <int HH>
 static cudaError_t set_net_attrs()
 {
     const int smem = (int)sizeof(NetSmem);
-    cudaError_t e = cudaFuncSetAttribute(wf_net_resample_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(wf_net_resample_kernel<HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_resample_kernel<HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_cache_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     return e;
 }
@@ -533,10 +565,15 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     const int max_it = 1 << 20;
     for (; it < max_it; ++it) {
         wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
-        wf_net_resample_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
-        if (CACHED) wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
-        wf_composite_kernel<<<grid_ray, 128, 0, s>>>(p, it);
-        wf_reset_rows_kernel<<<1, 32, 0, s>>>(p);
+        if (CACHED) {
+            wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
+            wf_net_resample_kernel<HH, true><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+        } else {
+            wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+        }
+        wf_composite_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+        wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, CACHED ? 1 : 0);
         if ((it + 1) % check_every == 0) {
             cudaError_t e = cudaMemcpyAsync(h_pinned, p.counters + ((it + 1) & 1), sizeof(int), cudaMemcpyDeviceToHost, s);
             if (e != cudaSuccess) return e;
