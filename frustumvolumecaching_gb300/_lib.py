@@ -126,6 +126,7 @@ SIGNATURES = {
     "fvc_renderer_set_render_mode": (c_int, [P, c_int]),
     "fvc_cache_read": (c_int, [P, P, C.POINTER(C.c_size_t), P, C.POINTER(C.c_size_t), P, C.POINTER(C.c_size_t)]),
     "fvc_cache_dims": (c_int, [P, C.POINTER(Int3), C.POINTER(Int3), C.POINTER(Int3)]),
+    "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
 }
 
 _lib = None

@@ -16,7 +16,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libfvc.so")
-SOURCES = ["fvc_kernels.cu", "fvc_render.cu", "fvc_capi.cu"]
+SOURCES = ["fvc_kernels.cu", "fvc_render.cu", "fvc_capi.cu", "fvc_noalloc.cu"]
 HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", os.path.join("..", "..", "include", "fvc.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -40,7 +40,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), ARCH, "-O3", "-std=c++17", "-lineinfo", "--threads", "3", "-shared", "-Xcompiler", "-fPIC",
+    cmd = [nvcc(), ARCH, "-O3", "-std=c++17", "-lineinfo", "--threads", "4", "-shared", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-o", tmp] + [os.path.join(CSRC, f) for f in SOURCES]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

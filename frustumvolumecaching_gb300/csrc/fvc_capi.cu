@@ -1028,3 +1028,23 @@ extern "C" int fvc_cache_read(fvc_cache *c, int32_t *packed, size_t *packed_n, f
     if (vox) CU(cudaMemcpy(vox, c->d_voxels, nv * 4, cudaMemcpyDeviceToHost));
     return FVC_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* views for the allocation-free render (fvc_noalloc.cu)                     */
+/* ------------------------------------------------------------------------ */
+namespace fvc_internal {
+int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms)
+{
+    p->scene = m->dscene;
+    p->grid = m->grid;
+    p->bits = m->d_bits;
+    p->table = m->d_table;
+    p->weights = m->d_weights;
+    p->bias3 = m->d_bias3;
+    p->latent_offset = m->latent_offset;
+    *head_hidden = m->head_hidden;
+    *n_sms = m->n_sms;
+    return FVC_OK;
+}
+void set_error(const char *msg) { g_err = msg; }
+}  // namespace fvc_internal

@@ -226,6 +226,22 @@ int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
 /* Statistics of the last render (needs the stream synchronised). */
 int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *out);
 
+/* Render without allocating (no counterpart in the reference).  For callers
+ * that cannot call cudaMalloc while rendering (a host with its own fixed GPU
+ * memory budget or allocator, per-frame callbacks with hard deadlines): the
+ * plain render of PerformanceRenderer with all scratch in one file-scope
+ * device array of FVC_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit.  Images up to FVC_NOALLOC_MAX_RAYS pixels;
+ * larger ones fail with FVC_ERR_ARG.  `out` holds DEVICE pointers; the work
+ * runs on `cuda_stream` (NULL = legacy default stream) and the call returns
+ * once the last sub-iteration is enqueued.  All calls share the scratch:
+ * calls whose GPU work overlaps race, so serialise them.  The first call on
+ * a device looks the scratch address up (cudaGetSymbolAddress); make it
+ * before any stream capture on that device. */
+#define FVC_NOALLOC_MAX_RAYS 65536
+#define FVC_NOALLOC_SCRATCH_BYTES (48u << 20)
+int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, const fvc_render_outputs *out, void *cuda_stream);
+
 /* ------------------------------------------------------------------------ */
 /* frustum volume cache (reference: Cache, include/cache.h:12-74; CacheRenderer */
 /* resizeCache / initCacheBlockwise / swapCache / setCacheSettings,             */
