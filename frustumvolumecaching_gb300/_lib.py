@@ -127,6 +127,7 @@ SIGNATURES = {
     "fvc_cache_read": (c_int, [P, P, C.POINTER(C.c_size_t), P, C.POINTER(C.c_size_t), P, C.POINTER(C.c_size_t)]),
     "fvc_cache_dims": (c_int, [P, C.POINTER(Int3), C.POINTER(Int3), C.POINTER(Int3)]),
     "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
+    "fvc_renderer_set_network_path": (c_int, [P, c_int]),
 }
 
 _lib = None

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libfvc.so")
 SOURCES = ["fvc_kernels.cu", "fvc_render.cu", "fvc_capi.cu", "fvc_noalloc.cu"]
-HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", os.path.join("..", "..", "include", "fvc.h")]
+HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", "fvc_tc.cuh", os.path.join("..", "..", "include", "fvc.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -269,11 +269,12 @@ struct fvc_model {
     uint8_t *d_bits = nullptr;
     __half2 *d_table = nullptr;
     uint2 *d_weights = nullptr;
+    uint8_t *d_weights_tc = nullptr;
     float *d_bias3 = nullptr;
     size_t table_entries = 0;
     ~fvc_model()
     {
-        dfree(d_bits); dfree(d_table); dfree(d_weights); dfree(d_bias3);
+        dfree(d_bits); dfree(d_table); dfree(d_weights); dfree(d_weights_tc); dfree(d_bias3);
     }
 };
 
@@ -359,6 +360,7 @@ struct fvc_renderer {
     fvc_cache_settings settings{0, 0, 1, 1, 1, 1};
     int render_mode = 0;
     int max_samples = 0;
+    int use_tc = 1;                   /* network kernels on tcgen05 (1) or mma.sync (0) */
     BuildScratch bs;
     std::mutex read_mutex, write_mutex;
     ~fvc_renderer()
@@ -525,6 +527,22 @@ static int load_model(const std::string &dir, fvc_model &m)
     }
     frag_pack(u16(wh, ho, 16 * 64), 16, 64, &W[W_L5]);
 
+    /* the same matrices as canonical K-major tiles for the tcgen05 kernels */
+    std::vector<uint8_t> Wt(TC_WBYTES, 0);
+    auto tc_pack = [&](const std::vector<uint16_t> &M, int N, int K, int off) {
+        for (int n = 0; n < N; ++n)
+            for (int k = 0; k < K; ++k) memcpy(&Wt[off + kmajor_offset(n, k, K)], &M[(size_t)n * K + k], 2);
+    };
+    tc_pack(u16(wb, 0, 64 * 32), 64, 32, TC_B1);
+    {
+        std::vector<uint16_t> w2 = u16(wb, 64 * 32, (size_t)base_out_pad * 64);
+        w2.resize(16 * 64, 0);
+        tc_pack(w2, 16, 64, TC_B2);
+    }
+    tc_pack(l3, 64, 32, TC_B3);
+    if (m.head_hidden == 2) tc_pack(u16(wh, 64 * 32, 64 * 64), 64, 64, TC_B4);
+    tc_pack(u16(wh, ho, 16 * 64), 16, 64, TC_B5);
+
     /* device scene block */
     DevScene &d = m.dscene;
     d.aabb_from = make_float3(s.aabb_from.x, s.aabb_from.y, s.aabb_from.z);
@@ -546,6 +564,8 @@ static int load_model(const std::string &dir, fvc_model &m)
     if ((rc = dalloc(&m.d_table, (size_t)off, "hash tables"))) return rc;
     if ((rc = dalloc(&m.d_weights, (size_t)W_TOTAL, "weights"))) return rc;
     if ((rc = dalloc(&m.d_bias3, (size_t)64, "bias"))) return rc;
+    if ((rc = dalloc(&m.d_weights_tc, (size_t)TC_WBYTES, "tcgen05 weights"))) return rc;
+    CU(cudaMemcpy(m.d_weights_tc, Wt.data(), TC_WBYTES, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_table, tab.data(), tab.size(), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_weights, W.data(), W.size() * sizeof(uint2), cudaMemcpyHostToDevice));
@@ -727,6 +747,8 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
     p.cam = dev_cam(info->cam_info);
     p.grid = m->grid;
     p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.bias3 = m->d_bias3;
+    p.weights_tc = m->d_weights_tc;
+    p.use_tc = r->use_tc;
     p.latent_offset = m->latent_offset;
     p.ray_counter = r->d_ctl; p.guard = r->d_ctl + 1; p.stats = r->d_stats;
     p.results = results; p.image = image; p.ray_counts = counts;
@@ -1040,6 +1062,8 @@ int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sm
     p->bits = m->d_bits;
     p->table = m->d_table;
     p->weights = m->d_weights;
+    p->weights_tc = m->d_weights_tc;
+    p->use_tc = 1;
     p->bias3 = m->d_bias3;
     p->latent_offset = m->latent_offset;
     *head_hidden = m->head_hidden;
@@ -1048,3 +1072,10 @@ int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sm
 }
 void set_error(const char *msg) { g_err = msg; }
 }  // namespace fvc_internal
+
+extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
+{
+    CHECK_ARG(r && (use_tcgen05 == 0 || use_tcgen05 == 1), "fvc_renderer_set_network_path: bad arguments");
+    r->use_tc = use_tcgen05;
+    return FVC_OK;
+}

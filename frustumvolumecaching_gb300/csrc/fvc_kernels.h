@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "fvc_device.cuh"
+#include "fvc_tc.cuh"
 
 namespace fvc {
 
@@ -20,6 +21,14 @@ struct CacheView {
     int fW, fH, fD, bX, bY, bZ, dX, dY, dZ;
     int n_valid_slots;          /* slots written by the last build; others read as zero */
 };
+
+/* weights of the tcgen05 network in canonical K-major tiles (bytes) */
+constexpr int TC_B1 = 0;        /* 64 x 32 */
+constexpr int TC_B2 = 4096;     /* 16 x 64 */
+constexpr int TC_B3 = 6144;     /* 64 x 32 */
+constexpr int TC_B4 = 10240;    /* 64 x 64 */
+constexpr int TC_B5 = 18432;    /* 16 x 64 */
+constexpr int TC_WBYTES = 20480;
 
 /* voxel of the cache data array: density, isset, 2 pad words, 8 fp16 latents */
 struct __align__(16) Voxel {
@@ -50,6 +59,8 @@ struct RenderParams {
     const __half2 *table;       /* hash tables, F = 2 */
     const uint2 *weights;       /* fragment-ordered MLP weights, W_TOTAL entries */
     const float *bias3;         /* head layer-1 bias from the 1-padding */
+    const uint8_t *weights_tc;  /* the same weights as canonical K-major tiles (tcgen05) */
+    int use_tc;                 /* 1: tcgen05 network kernels, 0: mma.sync */
     int latent_offset;
     int *ray_counter;
     int *guard;

@@ -453,6 +453,188 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
 }
 
 /* ------------------------------------------------------------------------- */
+/* network over rows on the 5th-generation tensor cores                      */
+/* ------------------------------------------------------------------------- */
+/* One CTA of 128 threads per 128-row tile; thread t owns row t and TMEM lane
+ * t.  Activations go through two shared-memory tiles in the canonical K-major
+ * layout, weights stay resident in shared memory, accumulators live in 128
+ * TMEM columns (cols 0..63 hidden layers, 64..79 the 16-wide output layers).
+ * One thread issues each layer's MMAs and commits them to an mbarrier; the
+ * CTA waits (bounded), reads its rows back with tcgen05.ld, applies
+ * ReLU / fp16 rounding and writes the next layer's operand. */
+struct __align__(128) TcSmem {
+    uint8_t W[TC_WBYTES];
+    uint8_t X[128 * 64 * 2];
+    uint8_t Y[128 * 64 * 2];
+    float bias3[64];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+constexpr long long TC_WAIT_LIMIT = 2000000000ll; /* ~1 s of SM clocks */
+
+/* row `row`'s 8 fp16 values of K-chunk c of a tile with K columns */
+__device__ __forceinline__ void st_chunk(uint8_t *tile, int row, int c, int K, uint4 v)
+{
+    *reinterpret_cast<uint4 *>(tile + kmajor_offset(row, 8 * c, K)) = v;
+}
+
+__device__ __forceinline__ uint4 pack8(const float *v)
+{
+    return make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
+}
+
+/* issue one layer: D[tmem_col] (+)= A (128 x K, tile at a) * B^T (N x K, tile at b) */
+__device__ __forceinline__ void tc_layer(uint32_t tmem, const uint8_t *a, const uint8_t *b, int K, int N)
+{
+    const uint32_t sbo = (uint32_t)(K / 8) * 128u;
+    const uint32_t id = idesc_f16(128, N, false);
+    const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
+    for (int kc = 0; kc < K / 16; ++kc)
+        tc_mma_f16(tmem, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
+}
+
+/* 64 accumulator columns of this thread's row -> (+bias) ReLU -> fp16 row of a K=64 tile */
+__device__ __forceinline__ void epi_hidden(uint32_t taddr, const float *bias, uint8_t *dst, int row)
+{
+#pragma unroll
+    for (int cg = 0; cg < 4; ++cg) {
+        float v[16];
+        tmem_ld16(taddr + 16 * cg, v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + (bias ? bias[16 * cg + i] : 0.0f), 0.0f);
+        st_chunk(dst, row, 2 * cg, 64, pack8(v));
+        st_chunk(dst, row, 2 * cg + 1, 64, pack8(v + 8));
+    }
+}
+
+template <int MODE, int HH, bool LIST>
+__global__ void __launch_bounds__(128, 4) wf_net_tc_kernel(RenderParams p, int it)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
+    const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : p.counters[4];
+    if (n_rows == 0) return;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < TC_WBYTES / 16; i += 128)
+        reinterpret_cast<uint4 *>(S.W)[i] = __ldg(reinterpret_cast<const uint4 *>(p.weights_tc) + i);
+    if (tid < 64) S.bias3[tid] = p.bias3[tid];
+    if (tid == 0) mbar_init(&S.mbar, 1);
+    if (warp == 0) tmem_alloc(&S.tmem_base, 128);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const RayState *states = p.states[it & 1];
+    uint32_t phase = 0;
+    bool failed = false;
+    const int n_tiles = (n_rows + 127) / 128;
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const int k = tile * 128 + tid;
+        const int r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : p.cache_list[k]) : -1;
+        __half2 sh[8];
+        uint16_t log_density = 0;
+        if (r >= 0) sh16(dir01_of(states, p.row_slot[r]), sh);
+        else for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+        bool ok = true;
+        if (MODE == 0) {
+            /* ---- hash features -> X (K = 32) ---- */
+            __half2 feat[16];
+            if (r >= 0) {
+                const float4 pw = p.row_pay[r];
+                hash_encode(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
+            } else {
+                for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
+            fence_proxy_async();
+            __syncthreads();
+            /* ---- layer 1: 32 -> 64 ---- */
+            if (tid == 0) { tc_fence_after(); tc_layer(tmem, S.X, S.W + TC_B1, 32, 64); tc_commit(&S.mbar); }
+            ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+            phase ^= 1u;
+            tc_fence_after();
+            epi_hidden(tmem + lane_base, nullptr, S.Y, tid);
+            fence_proxy_async();
+            tc_fence_before();
+            if (__syncthreads_or(!ok)) { failed = true; break; }
+            /* ---- layer 2: 64 -> 16 (log-density, latents) ---- */
+            if (tid == 0) { tc_fence_after(); tc_layer(tmem + 64, S.Y, S.W + TC_B2, 64, 16); tc_commit(&S.mbar); }
+            ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+            phase ^= 1u;
+            tc_fence_after();
+            float v[16];
+            tmem_ld16(tmem + lane_base + 64, v);
+            tmem_wait_ld();
+            const uint4 b0 = pack8(v), b1 = pack8(v + 8);
+            log_density = (uint16_t)(b0.x & 0xffffu);
+            st_chunk(S.X, tid, 0, 32, b0);
+            st_chunk(S.X, tid, 1, 32, b1);
+        } else {
+            /* ---- cache lookup -> head input (log-density, latents) ---- */
+            __half hin[32];
+            if (r >= 0) {
+                const float4 pw = p.row_pay[r];
+                cache_lookup(p.cache, make_float3(pw.x, pw.y, pw.z), p.latent_offset, hin);
+            } else {
+                for (int q = 16; q < 32; ++q) hin[q] = __float2half_rn(0.f);
+            }
+            log_density = __half_as_ushort(hin[16]);
+            st_chunk(S.X, tid, 0, 32, *reinterpret_cast<const uint4 *>(hin + 16));
+            st_chunk(S.X, tid, 1, 32, *reinterpret_cast<const uint4 *>(hin + 24));
+        }
+        st_chunk(S.X, tid, 2, 32, *reinterpret_cast<const uint4 *>(sh));
+        st_chunk(S.X, tid, 3, 32, *reinterpret_cast<const uint4 *>(sh + 4));
+        fence_proxy_async();
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        /* ---- head layer 1: (latents | SH) 32 -> 64, bias from the 1-padding ---- */
+        if (tid == 0) { tc_fence_after(); tc_layer(tmem, S.X, S.W + TC_B3, 32, 64); tc_commit(&S.mbar); }
+        ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+        phase ^= 1u;
+        tc_fence_after();
+        uint8_t *last = S.Y;
+        epi_hidden(tmem + lane_base, S.bias3, S.Y, tid);
+        fence_proxy_async();
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        if (HH == 2) {
+            /* ---- head layer 2: 64 -> 64 ---- */
+            if (tid == 0) { tc_fence_after(); tc_layer(tmem, S.Y, S.W + TC_B4, 64, 64); tc_commit(&S.mbar); }
+            ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+            phase ^= 1u;
+            tc_fence_after();
+            epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+            fence_proxy_async();
+            tc_fence_before();
+            if (__syncthreads_or(!ok)) { failed = true; break; }
+            last = S.X;
+        }
+        /* ---- output layer: 64 -> 16 (rgb logits in cols 0..2) ---- */
+        if (tid == 0) { tc_fence_after(); tc_layer(tmem + 64, last, S.W + TC_B5, 64, 16); tc_commit(&S.mbar); }
+        ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+        phase ^= 1u;
+        tc_fence_after();
+        float o[16];
+        tmem_ld16(tmem + lane_base + 64, o);
+        tmem_wait_ld();
+        if (r >= 0) p.row_out[r] = make_uint2(pack_h2(o[0], o[1]), (uint32_t)__half_as_ushort(__float2half_rn(o[2])) | ((uint32_t)log_density << 16));
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+    }
+    if (failed && tid == 0) atomicOr(p.guard, 16);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 128);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* composite + compaction                                                    */
 /* ------------------------------------------------------------------------- */
 template <bool CACHED>
@@ -543,6 +725,10 @@ static cudaError_t set_net_attrs()
     cudaError_t e = cudaFuncSetAttribute(wf_net_resample_kernel<HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_resample_kernel<HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_cache_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int tsmem = (int)sizeof(TcSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     return e;
 }
 
@@ -565,12 +751,20 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     const int max_it = 1 << 20;
     for (; it < max_it; ++it) {
         wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+        const size_t tc_smem = sizeof(TcSmem);
+        const int grid_tc = n_sms * 4; /* 4 CTAs x 128 TMEM columns fill an SM's 512 columns */
         if (CACHED) {
             wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
-            wf_net_resample_kernel<HH, true><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
-            wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            if (p.use_tc) {
+                wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+                wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            } else {
+                wf_net_resample_kernel<HH, true><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+                wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            }
         } else {
-            wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            if (p.use_tc) wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            else wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
         }
         wf_composite_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
         wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, CACHED ? 1 : 0);

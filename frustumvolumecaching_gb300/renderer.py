@@ -150,6 +150,10 @@ class Renderer:
     def set_stream(self, stream_handle: int | None) -> None:
         L.check(L.load().fvc_renderer_set_stream(self.handle, stream_handle))
 
+    def set_network_path(self, use_tcgen05: bool) -> None:
+        """tcgen05 (default) or mma.sync network kernels."""
+        L.check(L.load().fvc_renderer_set_network_path(self.handle, int(bool(use_tcgen05))))
+
     def set_max_samples_per_ray(self, n: int) -> None:
         L.check(L.load().fvc_renderer_set_max_samples_per_ray(self.handle, n))
 

@@ -223,6 +223,11 @@ int fvc_render(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_
 /* Guard on the samples of one ray (0 = off, the reference default); a ray
  * exceeding it sets a guard bit reported by fvc_render_stats. */
 int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
+/* Network kernels of the renderer: 1 = 5th-generation tensor cores
+ * (tcgen05.mma, TMEM accumulators; the default), 0 = warp-level mma.sync.
+ * Both compute the same layers in fp16 with fp32 accumulation.  No reference
+ * counterpart (the reference runs tiny-cuda-nn's FullyFusedMLP). */
+int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05);
 /* Statistics of the last render (needs the stream synchronised). */
 int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *out);
 

@@ -49,18 +49,20 @@ def test_network_matches_oracle(model1):
     assert np.abs(feats - ref_f).max() < 3e-5
 
 
-def _render(renderer_cls, loader, cam, **kw):
+def _render(renderer_cls, loader, cam, tcgen05=True, **kw):
     r = renderer_cls(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, **kw)
     r.resizeRenderbuffers(cam["resolution"])
+    r.set_network_path(tcgen05)
     buf = fvc.RenderBuffer(cam["resolution"])
     return r, buf
 
 
+@pytest.mark.parametrize("tcgen05", [False, True], ids=["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
-def test_plain_render_parity(request, fixture, W, H):
+def test_plain_render_parity(request, fixture, W, H, tcgen05):
     loader, om, _ = request.getfixturevalue(fixture)
     cam = small_camera(1001, W, H)
-    r, buf = _render(fvc.PerformanceRenderer, loader, cam)
+    r, buf = _render(fvc.PerformanceRenderer, loader, cam, tcgen05)
     r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
     ref, ns, nst = om.render_plain(cam)
     # sample counts and steps per ray: bit-exact (rays that did not terminate early)
@@ -69,7 +71,7 @@ def test_plain_render_parity(request, fixture, W, H):
     np.testing.assert_array_equal(buf.ray_counts[..., 3][live], nst[live])
     err = np.abs(buf.results - ref).max()
     p = psnr(buf.results[..., :3] + buf.results[..., 3:], ref[..., :3] + ref[..., 3:])
-    print(f"\nplain {fixture} {W}x{H}: max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB, samples {ns.sum()}")
+    print(f"\nplain {fixture} {W}x{H} {'tcgen05' if tcgen05 else 'mma.sync'}: max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB, samples {ns.sum()}")
     assert err <= COLOR_ATOL
     img = orc.composite_image(buf.results)
     np.testing.assert_array_equal(buf.image, img)
@@ -181,11 +183,13 @@ def test_cache_build_parity(request, fixture, W, H):
     assert np.abs(lat - olat).max() < 2e-3
 
 
+@pytest.mark.parametrize("tcgen05", [False, True], ids=["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
-def test_cached_render_parity(request, fixture, W, H):
+def test_cached_render_parity(request, fixture, W, H, tcgen05):
     loader, om, _ = request.getfixturevalue(fixture)
     cam0 = small_camera(1001, W, H)
     r, c0, c1 = _cache_setup(loader, cam0)
+    r.set_network_path(tcgen05)
     r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
     r.swapCache()
     oc = om.cache_build(cam0)
@@ -205,7 +209,7 @@ def test_cached_render_parity(request, fixture, W, H):
     err = np.abs(buf.results - ref).max()
     p = psnr(buf.results[..., :3] + buf.results[..., 3:], ref[..., :3] + ref[..., 3:])
     hit = counts[..., 1].sum() / max(1, counts[..., :2].sum())
-    print(f"\ncached {fixture}: hit ratio {hit:.3f}, max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB")
+    print(f"\ncached {fixture} {'tcgen05' if tcgen05 else 'mma.sync'}: hit ratio {hit:.3f}, max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB")
     assert hit > 0.3
     assert err <= COLOR_ATOL
 
