@@ -40,6 +40,11 @@ FLOP_RESAMPLE = 16896  # per sample: density 2*(32*64+64*9) + color 2*(24*64+64*
 FLOP_CACHE = 11648     # per cache sample: color head only
 BYTES_HASH = 512       # per resampled sample: 16 levels x 8 corners x 2 fp16
 BYTES_CACHE = 8 * 24   # per cache sample: 8 corners x (density, isset, 8 fp16 latents)
+BYTES_ROW_IO = 28 + 8  # per resampled sample: the 28 B sample record read + 4 fp16 outputs written
+NET_KERNEL = "wf_net_tc_kernel<0> (resample rows: hash-grid encode + density MLP + color head on tcgen05)"
+# DRAM bytes (read + write) per resample row of that kernel: dram__bytes_read.sum + dram__bytes_write.sum over all
+# its launches of 2 frames of the same scene at 960x540 / the rows they processed (4.420 GB / 116,864,373 rows)
+NET_TRAFFIC_PER_ROW = 37.8
 
 
 def dist_env():
@@ -210,7 +215,8 @@ def run_fvc(args) -> dict | None:
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     log = {"render_plain_ms": [], "render_cached_ms": [], "build_ms": [], "rebuilds": 0, "coverage": [],
            "plain_res": 0, "cache_res": 0, "cache_hits": 0, "launches": 0, "build_iters": 0, "overflow": 0,
-           "bricks_demanded": 0, "bricks_set": 0}
+           "bricks_demanded": 0, "bricks_set": 0, "net_ms": 0.0, "net_launches": 0, "net_rows": 0,
+           "plain_net_ms": 0.0, "plain_net_launches": 0, "plain_net_rows": 0, "plain_launches": 0}
 
     def plain_path(record: bool):
         for info in infos:
@@ -220,8 +226,11 @@ def run_fvc(args) -> dict | None:
             b.record(stream)
             if record:
                 log["_pending_plain"].append((a, b))
-        if record:
-            log["launches"] += len(infos)
+                st = plain._render_stats  # the frame already ended on a host check of the alive count
+                log["plain_net_ms"] += st.timed_kernel_ms
+                log["plain_net_launches"] += st.n_timed_launches
+                log["plain_net_rows"] += st.n_resamples
+                log["plain_launches"] += st.n_launches
 
     def rebuild(info, record):
         a, b = ev(), ev()
@@ -234,7 +243,7 @@ def run_fvc(args) -> dict | None:
             log["_pending_build"].append((a, b))
             log["rebuilds"] += 1
             log["build_iters"] += st.n_iterations
-            log["launches"] += 3 + 3 * st.n_iterations
+            log["launches"] += st.n_launches
             log["overflow"] = max(log["overflow"], st.overflow)
             log["bricks_demanded"] = st.n_bricks_demanded
             log["bricks_set"] = st.n_bricks_set
@@ -256,7 +265,10 @@ def run_fvc(args) -> dict | None:
                 log["coverage"].append(cov)
                 log["cache_res"] += st.n_resamples
                 log["cache_hits"] += st.n_cache_hits
-                log["launches"] += 1
+                log["launches"] += st.n_launches
+                log["net_ms"] += st.timed_kernel_ms
+                log["net_launches"] += st.n_timed_launches
+                log["net_rows"] += st.n_resamples
             if cov < COVERAGE_REBUILD and i + 1 < len(infos):
                 rebuild(info, record)
 
@@ -276,6 +288,8 @@ def run_fvc(args) -> dict | None:
         flush.zero_()
     barrier()
 
+    plain.set_kernel_timing(True)
+    cached.set_kernel_timing(True)
     clocks = ClockSampler(local)
     clocks.start()
     # plain path, K steps
@@ -290,6 +304,18 @@ def run_fvc(args) -> dict | None:
         barrier()
         t_plain.append(s.elapsed_time(e))
     st = plain._render_stats
+    # the same plain path with the warp-level mma.sync network kernels (one step)
+    plain.set_network_path(False)
+    flush.zero_()
+    barrier()
+    s, e = ev(), ev()
+    s.record(stream)
+    plain_path(False)
+    e.record(stream)
+    barrier()
+    t_plain_mma = s.elapsed_time(e)
+    plain.set_network_path(True)
+    plain.set_kernel_timing(False)
     # cached path, K steps
     t_cached = []
     for _ in range(args.steps):
@@ -302,6 +328,7 @@ def run_fvc(args) -> dict | None:
         barrier()
         t_cached.append(s.elapsed_time(e))
     clk = clocks.stop()
+    cached.set_kernel_timing(False)
 
     # e2e: the cached path through the host-buffer C-ABI call (D2H of every frame)
     hbuf = fvc.RenderBuffer(RES)
@@ -329,11 +356,16 @@ def run_fvc(args) -> dict | None:
     fps_plain = ws * n_frames / (steps_ms_plain / 1e3)
     fps_e2e = ws * n_frames / e2e_s
 
-    # roofline of the dominant kernel: the plain render kernel, tensor-pipe bound work
-    plain_samples_per_frame = st.n_resamples
+    # roofline of the dominant kernel (the resample network kernel, by the ncu launch list), over the
+    # cached path's timed region: algorithmic bytes of its rows / its summed CUDA-event launch time
     peaks = measured_peaks()
-    flop = plain_samples_per_frame * FLOP_RESAMPLE
-    achieved_tf = flop / (plain_launch_ms / 1e3) / 1e12
+    plain_samples_per_frame = st.n_resamples
+    net_ms = log["net_ms"]
+    net_bytes = log["net_rows"] * (BYTES_HASH + BYTES_ROW_IO)
+    achieved_gbs = net_bytes / (net_ms / 1e3) / 1e9 if net_ms > 0 else None
+    net_tflops = log["net_rows"] * FLOP_RESAMPLE / (net_ms / 1e3) / 1e12 if net_ms > 0 else None
+    plain_net_gbs = (log["plain_net_rows"] * (BYTES_HASH + BYTES_ROW_IO) / (log["plain_net_ms"] / 1e3) / 1e9
+                     if log["plain_net_ms"] > 0 else None)
     n_frames_cached = len(log["_pending_cached"])
     res_per_frame = log["cache_res"] / max(1, n_frames_cached)
     hit_per_frame = log["cache_hits"] / max(1, n_frames_cached)
@@ -347,22 +379,30 @@ def run_fvc(args) -> dict | None:
                    "l2": "256 MiB buffer written between steps; cache data array (4 GiB) larger than L2",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "plain": {"value": fps_plain, "unit": UNIT, "ms_per_frame": steps_ms_plain / n_frames,
-                  "samples_per_frame": plain_samples_per_frame},
+                  "samples_per_frame": plain_samples_per_frame, "network": "tcgen05",
+                  "ms_per_frame_mma_sync": t_plain_mma / n_frames},
         "cached": {"ms_per_frame": steps_ms_cached / n_frames, "render_ms": cached_launch_ms, "build_ms": build_ms,
                    "rebuilds_per_path": log["rebuilds"] / args.steps, "mean_coverage": float(np.mean(log["coverage"])) if log["coverage"] else None,
                    "resample_per_frame": res_per_frame, "cache_samples_per_frame": hit_per_frame,
                    "bricks_demanded": log["bricks_demanded"], "bricks_set": log["bricks_set"], "overflow": bool(log["overflow"]),
                    "speedup_vs_plain": fps_cached / fps_plain},
-        "roofline": {"kernel": "render_kernel<plain> (fused march + hash grid + MLPs + compositing)", "bound": "tensor",
-                     "achieved": achieved_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                     "frac": achieved_tf / peaks["bf16_tflops"], "traffic": None,
-                     "peak_source": peaks["source"] + " bf16 dense burst",
-                     "work_per_launch": f"{plain_samples_per_frame} samples x {FLOP_RESAMPLE} FLOP",
-                     "launch_ms": plain_launch_ms,
-                     "hash_gather_gbs": plain_samples_per_frame * BYTES_HASH / (plain_launch_ms / 1e3) / 1e9},
+        "roofline": {"kernel": NET_KERNEL, "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"] if achieved_gbs else None,
+                     "traffic": (NET_TRAFFIC_PER_ROW * log["net_rows"] / max(1, log["net_launches"])
+                                 if NET_TRAFFIC_PER_ROW else None),
+                     "peak_source": peaks["source"] + " HBM copy bandwidth",
+                     "algorithmic_bytes_per_row": BYTES_HASH + BYTES_ROW_IO,
+                     "rows_per_launch": log["net_rows"] / max(1, log["net_launches"]),
+                     "launch_ms": net_ms / max(1, log["net_launches"]), "launches_timed": log["net_launches"],
+                     "share_of_step": net_ms / (sum(t_cached)),
+                     "tensor_tflops": net_tflops, "tensor_peak": peaks["bf16_tflops"],
+                     "plain_path_achieved_gbs": plain_net_gbs,
+                     "note": "hash tables (32 MiB) are L2-resident: the gathers are served by L2, so DRAM traffic "
+                             "(ncu dram bytes, scaled per row) is far below the algorithmic bytes"},
         "e2e": {"value": fps_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": n_frames * W * H * (4 + 16 + 16)},
         "gpu_launches": log["launches"] // max(1, args.steps),
+        "gpu_launches_plain_path": log["plain_launches"] // max(1, args.steps),
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

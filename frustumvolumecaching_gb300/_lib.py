@@ -80,16 +80,23 @@ class RenderOutputs(C.Structure):
 class RenderStats(C.Structure):
     _fields_ = [("samples_ppx", C.c_double), ("n_samples", C.c_longlong), ("n_resamples", C.c_longlong),
                 ("n_cache_hits", C.c_longlong), ("n_dropped", C.c_longlong), ("n_steps", C.c_longlong),
-                ("n_rounds", c_int), ("guard_flags", c_int)]
+                ("n_rounds", c_int), ("guard_flags", c_int), ("n_launches", C.c_longlong),
+                ("n_timed_launches", c_int), ("timed_kernel_ms", C.c_float)]
+
+
+class ModelProps(C.Structure):
+    _fields_ = [("first_latent_is_density", c_int), ("head_hidden_layers", c_int), ("n_levels", c_int),
+                ("n_latents", c_int), ("occupancy_bitfield", C.c_void_p), ("occupancy_bytes", C.c_size_t)]
 
 
 class CacheStats(C.Structure):
     _fields_ = [("n_bricks_set", c_int), ("n_bricks_reserved", c_int), ("n_bricks_demanded", c_int),
-                ("overflow", c_int), ("n_iterations", c_int), ("n_samples", C.c_longlong)]
+                ("overflow", c_int), ("n_iterations", c_int), ("n_launches", c_int), ("n_samples", C.c_longlong)]
 
 
 assert C.sizeof(SceneInfo) == 76 and C.sizeof(StepsizeInfo) == 48
 assert C.sizeof(CameraInfo) == 144 and CameraInfo.cam2world.offset == 32 and CameraInfo.world2cam.offset == 80
+assert C.sizeof(RenderStats) == 72 and C.sizeof(CacheStats) == 32
 assert C.sizeof(RaymarchInfo) == 352 and RaymarchInfo.stepsize_info.offset == 288 and RaymarchInfo.sample_index.offset == 336
 
 FVC_OK = 0
@@ -128,6 +135,9 @@ SIGNATURES = {
     "fvc_cache_dims": (c_int, [P, C.POINTER(Int3), C.POINTER(Int3), C.POINTER(Int3)]),
     "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
+    "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
+    "fvc_model_properties": (c_int, [P, C.POINTER(ModelProps)]),
+    "fvc_renderer_synchronize": (c_int, [P]),
 }
 
 _lib = None

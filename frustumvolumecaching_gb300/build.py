@@ -1,9 +1,11 @@
-"""Builds libfvc.so (the CUDA kernels and the C ABI) in-tree for sm_103a.
+"""Builds libfvc.so (the CUDA kernels and the C ABI) in-tree for sm_103a, and
+the `eval` program on the C++ renderer API (include/fvc.hpp).
 
     python -m frustumvolumecaching_gb300.build
 
-Two translation units compiled in parallel by nvcc; host code without fused
-multiply-add contraction so its float setup matches the oracle's.
+The CUDA translation units are compiled in parallel by nvcc; host code
+without fused multiply-add contraction so its float setup matches the
+oracle's.  eval is plain g++ against libfvc.so and the CUDA runtime.
 """
 from __future__ import annotations
 
@@ -18,6 +20,9 @@ OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libfvc.so")
 SOURCES = ["fvc_kernels.cu", "fvc_render.cu", "fvc_capi.cu", "fvc_noalloc.cu"]
 HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", "fvc_tc.cuh", os.path.join("..", "..", "include", "fvc.h")]
+INCLUDE = os.path.join(PKG, "..", "include")
+EVAL_SRC = os.path.join(PKG, "cpp", "eval.cpp")
+EVAL = os.path.join(OUT_DIR, "eval")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -42,6 +47,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     cmd = [nvcc(), ARCH, "-O3", "-std=c++17", "-lineinfo", "--threads", "4", "-shared", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-o", tmp] + [os.path.join(CSRC, f) for f in SOURCES]
+    # tuning macros of the kernels (e.g. -DFVC_TC_CTAS_PER_SM=5), for launch-shape sweeps
+    cmd[1:1] = os.environ.get("FVC_NVCC_DEFINES", "").split()
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -53,5 +60,31 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+def cuda_root() -> str:
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+
+
+def build_eval(force: bool = False) -> str:
+    """g++ build of the eval program; needs libfvc.so first."""
+    lib = build()
+    deps = [EVAL_SRC, os.path.join(INCLUDE, "fvc.hpp"), os.path.join(INCLUDE, "fvc.h"), lib]
+    if not force and os.path.exists(EVAL) and all(os.path.getmtime(d) < os.path.getmtime(EVAL) for d in deps):
+        return EVAL
+    cuda = cuda_root()
+    cudalib = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib")) if os.path.isdir(d)), None)
+    if cudalib is None:
+        raise RuntimeError("CUDA runtime library directory not found under " + cuda)
+    tmp = EVAL + ".tmp"
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", INCLUDE, "-I", os.path.join(cuda, "include"),
+           EVAL_SRC, "-o", tmp, "-L", OUT_DIR, "-lfvc", "-L", cudalib, "-lcudart",
+           "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cudalib]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, EVAL)
+    return EVAL
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_eval(force="--force" in sys.argv))

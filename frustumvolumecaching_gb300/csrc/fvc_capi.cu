@@ -42,6 +42,7 @@ static_assert(sizeof(fvc_camera_info) == 144 && offsetof(fvc_camera_info, is_ope
 static_assert(sizeof(fvc_raymarch_info) == 352 && offsetof(fvc_raymarch_info, next_cam_info) == 144 &&
               offsetof(fvc_raymarch_info, stepsize_info) == 288 && offsetof(fvc_raymarch_info, sample_index) == 336 &&
               offsetof(fvc_raymarch_info, motion_blur) == 340 && offsetof(fvc_raymarch_info, deterministic) == 341, "RaymarchInfo layout");
+static_assert(sizeof(fvc_render_stats_t) == 72 && sizeof(fvc_cache_stats_t) == 32, "statistics layout");
 static_assert(sizeof(fvc_ray_result) == 16 && sizeof(fvc_camera_matrix) == 48, "BaseRayResult / CameraMatrix layout");
 
 /* ------------------------------------------------------------------------ */
@@ -350,6 +351,8 @@ struct fvc_renderer {
     int *d_wf_counters = nullptr;
     int row_capacity = 0;
     int last_iterations = 0;
+    LaunchLog log;                    /* kernel accounting of the last render */
+    std::vector<cudaEvent_t> events;  /* 2 x 4096 when kernel timing is on */
     void release_wavefront()
     {
         dfree(d_states[0]); dfree(d_states[1]); dfree(d_ray_rows); dfree(d_row_t0); dfree(d_row_slot);
@@ -370,6 +373,7 @@ struct fvc_renderer {
         release_wavefront();
         bs.release();
         if (h_pinned) cudaFreeHost(h_pinned);
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (own_stream) cudaStreamDestroy(own_stream);
         if (low_prio) cudaStreamDestroy(low_prio);
     }
@@ -780,7 +784,11 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
     CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
     CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));
-    CU(render_frame(p, cached, m->head_hidden, m->n_sms, r->stream, r->h_pinned + 8, 4, &r->last_iterations));
+    r->log.launches = 0;
+    r->log.n_timed = r->log.n_untimed = 0;
+    r->log.ev = r->events.empty() ? nullptr : r->events.data();
+    r->log.cap = (int)r->events.size() / 2;
+    CU(render_frame(p, cached, m->head_hidden, m->n_sms, r->stream, r->h_pinned + 8, 4, &r->last_iterations, &r->log));
     return FVC_OK;
 }
 
@@ -829,6 +837,54 @@ extern "C" int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *o)
     o->n_rounds = r->last_iterations;
     o->samples_ppx = (double)s.n_samples / n_rays;
     o->guard_flags = ctl[1];
+    o->n_launches = r->log.launches;
+    o->n_timed_launches = r->log.ev ? r->log.n_timed : 0;
+    o->timed_kernel_ms = 0.0f;
+    for (int i = 0; i < o->n_timed_launches; ++i) {
+        float ms = 0.0f;
+        CU(cudaEventElapsedTime(&ms, r->log.ev[2 * i], r->log.ev[2 * i + 1]));
+        o->timed_kernel_ms += ms;
+    }
+    return FVC_OK;
+}
+
+extern "C" int fvc_model_properties(const fvc_model *m, fvc_model_props *o)
+{
+    CHECK_ARG(m && o, "fvc_model_properties: null argument");
+    o->first_latent_is_density = m->latent_offset == 0;
+    o->head_hidden_layers = m->head_hidden;
+    o->n_levels = m->grid.n_levels;
+    o->n_latents = m->n_latents;
+    o->occupancy_bitfield = m->d_bits;
+    const size_t R = (size_t)m->scene.grid_resolution;
+    o->occupancy_bytes = R * R * R * (size_t)m->scene.grid_nlvl / 8;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_synchronize(fvc_renderer *r)
+{
+    CHECK_ARG(r, "fvc_renderer_synchronize: null renderer");
+    CU(cudaStreamSynchronize(r->stream));
+    int guard = 0;
+    CU(cudaMemcpy(&guard, r->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (guard) return fail(FVC_ERR_GUARD, "render guard fired: flags " + std::to_string(guard));
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_kernel_timing(fvc_renderer *r, int enable)
+{
+    CHECK_ARG(r && (enable == 0 || enable == 1), "fvc_renderer_set_kernel_timing: bad arguments");
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    CU(cudaStreamSynchronize(r->stream));
+    if (enable && r->events.empty()) {
+        r->events.resize(2 * 4096);
+        for (auto &e : r->events) CU(cudaEventCreate(&e));
+    } else if (!enable) {
+        for (cudaEvent_t e : r->events) cudaEventDestroy(e);
+        r->events.clear();
+    }
+    r->log.ev = nullptr;
+    r->log.n_timed = 0;
     return FVC_OK;
 }
 
@@ -975,6 +1031,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
 
     CU(cudaMemsetAsync(b.counters, 0, 8 * sizeof(int), s));
     CU(cudaMemsetAsync(c->d_packed, 0xff, (size_t)c->bX * c->bY * c->bZ * sizeof(int32_t), s));
+    int n_launches = 2;
     cache_init_kernel<<<n_tiles, 64, 0, s>>>(p);
     CU(cudaGetLastError());
     cache_compact_kernel<<<1, 1024, 0, s>>>(p, n_tiles);
@@ -995,6 +1052,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
         CU(cudaGetLastError());
         cache_copy_kernel<<<std::min(n_alive, 4 * m->n_sms), 256, 0, s>>>(p);
         CU(cudaGetLastError());
+        n_launches += 3;
         std::swap(p.alive_list, p.alive_list_next);
         std::swap(p.n_alive_tiles, p.n_alive_next);
         CU(cudaMemcpyAsync(r->h_pinned, p.n_alive_tiles, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1003,6 +1061,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     }
     cache_known_ranges_kernel<<<n_tiles, 64, 0, s>>>(p);
     CU(cudaGetLastError());
+    ++n_launches;
     CU(cudaMemcpyAsync(r->h_pinned, b.counters, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     const int demanded = r->h_pinned[2], guard = r->h_pinned[4];
@@ -1011,6 +1070,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     c->stats.n_bricks_set = std::min(demanded, c->capacity());
     c->stats.overflow = demanded > c->capacity();
     c->stats.n_iterations = iter;
+    c->stats.n_launches = n_launches;
     c->stats.n_samples = n_samples;
     c->built = true;
     if (guard) return fail(FVC_ERR_GUARD, "cache build guard fired: flags " + std::to_string(guard));

@@ -223,49 +223,78 @@ __device__ __forceinline__ float3 cam2froxel(float3 c, const DevCam &cam, const 
 /* --------------------------------------------------------------------- */
 /* hash grid (Instant-NGP multiresolution hash encoding)                  */
 /* --------------------------------------------------------------------- */
+/* packed fp32 pair arithmetic of sm_100+ (add/sub/fma .f32x2 on a 64-bit register pair) */
+__device__ __forceinline__ unsigned long long f2_bits(float2 a)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2_from_bits(unsigned long long r)
+{
+    float2 a;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+/* a + t * (b - a), each step rounded to nearest */
+__device__ __forceinline__ float2 f2_lerp(float2 a, float2 b, float t)
+{
+    unsigned long long d, r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(b)), "l"(f2_bits(a)));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_bits(make_float2(t, t))), "l"(d), "l"(f2_bits(a)));
+    return f2_from_bits(r);
+}
+
 /* Encodes one position into 2*n_levels features (fp16) written to
  * out[0 .. 2*n_levels) as half2 per level.  Corner and fraction in float32
- * (p = fma(scale, x, 0.5), floor, subtract), accumulation in float32. */
+ * (p = fma(scale, x, 0.5), floor, subtract); the trilinear interpolation in
+ * float32 as lerps along x, y, z (the same weighted sum of the 8 corners).
+ * Levels are processed in groups of LG: the 8*LG corner loads of a group are
+ * all issued before any of them is consumed, so a thread keeps 8*LG gathers
+ * in flight instead of 8. */
+template <int LG = 4>
 __device__ __forceinline__ void hash_encode(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out)
 {
-#pragma unroll 4
-    for (int l = 0; l < g.n_levels; ++l) {
-        const float sc = g.scale[l];
-        const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
-        const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
-        const uint32_t gx = (uint32_t)(int)fx, gy = (uint32_t)(int)fy, gz = (uint32_t)(int)fz;
-        const float wx = __fsub_rn(px, fx), wy = __fsub_rn(py, fy), wz = __fsub_rn(pz, fz);
-        const uint32_t size = g.size[l];
-        uint32_t idx[8];
-        if ((g.dense_mask >> l) & 1u) {
-            const uint32_t r = g.res[l], r2 = g.res2[l];
-            const uint32_t b = gx + gy * r + gz * r2;
+    for (int l0 = 0; l0 < g.n_levels; l0 += LG) {
+        __half2 v[LG][8];
+        float wx[LG], wy[LG], wz[LG];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                uint32_t i = b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u);
-                idx[c] = i < size ? i : i % size;
+        for (int j = 0; j < LG; ++j) {
+            const int l = l0 + j;
+            const float sc = g.scale[l];
+            const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
+            const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+            const uint32_t gx = (uint32_t)(int)fx, gy = (uint32_t)(int)fy, gz = (uint32_t)(int)fz;
+            wx[j] = __fsub_rn(px, fx); wy[j] = __fsub_rn(py, fy); wz[j] = __fsub_rn(pz, fz);
+            const uint32_t size = g.size[l];
+            const __half2 *tl = table + g.offset[l];
+            if ((g.dense_mask >> l) & 1u) {
+                const uint32_t r = g.res[l], r2 = g.res2[l];
+                const uint32_t b = gx + gy * r + gz * r2;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t i = b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u);
+                    if (i >= size) i -= size; /* == i % size: dense indices stay below 2*size */
+                    v[j][c] = __ldg(tl + i);
+                }
+            } else {
+                const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;
+                const uint32_t hz0 = gz * 805459861u, hz1 = (gz + 1u) * 805459861u;
+                const uint32_t m = size - 1u; /* hashed levels hold 2^log2_T entries */
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    v[j][c] = __ldg(tl + (((gx + ((c & 1) ? 1u : 0u)) ^ ((c & 2) ? hy1 : hy0) ^ ((c & 4) ? hz1 : hz0)) & m));
             }
-        } else {
-            const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;
-            const uint32_t hz0 = gz * 805459861u, hz1 = (gz + 1u) * 805459861u;
-            const uint32_t m = size - 1u; /* hashed levels hold 2^log2_T entries */
-#pragma unroll
-            for (int c = 0; c < 8; ++c)
-                idx[c] = ((gx + ((c & 1) ? 1u : 0u)) ^ ((c & 2) ? hy1 : hy0) ^ ((c & 4) ? hz1 : hz0)) & m;
         }
-        const __half2 *tl = table + g.offset[l];
-        __half2 v[8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) v[c] = __ldg(tl + idx[c]);
-        float ax = 0.f, ay = 0.f;
+        for (int j = 0; j < LG; ++j) {
+            /* trilinear interpolation as 7 lerps (x, then y, then z) on both features at once */
+            float2 e[4];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const float w = ((c & 1) ? wx : 1.0f - wx) * ((c & 2) ? wy : 1.0f - wy) * ((c & 4) ? wz : 1.0f - wz);
-            const float2 f = __half22float2(v[c]);
-            ax = fmaf(w, f.x, ax);
-            ay = fmaf(w, f.y, ay);
+            for (int k = 0; k < 4; ++k) e[k] = f2_lerp(__half22float2(v[j][2 * k]), __half22float2(v[j][2 * k + 1]), wx[j]);
+            const float2 g0 = f2_lerp(e[0], e[1], wy[j]), g1 = f2_lerp(e[2], e[3], wy[j]);
+            out[l0 + j] = __float22half2_rn(f2_lerp(g0, g1, wz[j]));
         }
-        out[l] = __floats2half2_rn(ax, ay);
     }
 }
 

@@ -142,8 +142,20 @@ size_t build_smem_bytes();
 /* One frame: ray generation, then sub-iterations of march / network /
  * compositing until no ray is alive.  Reads the alive count back every
  * `check_every` sub-iterations through h_pinned (page-locked, >= 1 int). */
+/* Kernel accounting of one frame: every kernel the frame launched, and
+ * (when `ev` holds 2 * cap events) a begin/end event pair recorded on the
+ * launching stream around each resample network launch, the frame's
+ * dominant kernel. */
+struct LaunchLog {
+    long long launches = 0;
+    cudaEvent_t *ev = nullptr;
+    int cap = 0;
+    int n_timed = 0;
+    int n_untimed = 0;
+};
+
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
-                         int check_every, int *n_iterations);
+                         int check_every, int *n_iterations, LaunchLog *log = nullptr);
 cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
 
 __global__ void cache_init_kernel(CacheBuildParams p);

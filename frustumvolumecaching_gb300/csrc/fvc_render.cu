@@ -36,6 +36,17 @@ namespace fvc {
 constexpr unsigned FULLMASK = 0xffffffffu;
 constexpr int S_ROWS = 16;        /* rows per ray and sub-iteration (the reference keeps up to 8) */
 constexpr int NET_WARPS = 8;
+/* tcgen05 network kernel: CTAs resident per SM (launch bound and grid) and
+ * hash levels whose gathers are in flight together.  Measured at 1080p on the
+ * 3-cascade scene (resample-kernel ms per frame, plain / cached path):
+ * 6 CTAs + groups of 2 (80 registers, spills) 37.2 / 34.5; 5 + 2: 30.0 / 22.5;
+ * 5 + 4 (96 registers): 29.1 / 22.1; 4 + 4: 30.6 / 22.6. */
+#ifndef FVC_TC_CTAS_PER_SM
+#define FVC_TC_CTAS_PER_SM 5
+#endif
+#ifndef FVC_TC_HASH_GROUP
+#define FVC_TC_HASH_GROUP 4
+#endif
 
 __device__ __forceinline__ unsigned lane_lt() { unsigned m; asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m)); return m; }
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
@@ -456,22 +467,27 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
 /* network over rows on the 5th-generation tensor cores                      */
 /* ------------------------------------------------------------------------- */
 /* One CTA of 128 threads per 128-row tile; thread t owns row t and TMEM lane
- * t.  Activations go through two shared-memory tiles in the canonical K-major
- * layout, weights stay resident in shared memory, accumulators live in 128
- * TMEM columns (cols 0..63 hidden layers, 64..79 the 16-wide output layers).
- * One thread issues each layer's MMAs and commits them to an mbarrier; the
- * CTA waits (bounded), reads its rows back with tcgen05.ld, applies
- * ReLU / fp16 rounding and writes the next layer's operand. */
+ * t.  The activations of a tile live in ONE shared-memory tile in the
+ * canonical K-major layout that each layer overwrites in place (a layer's
+ * epilogue runs only after its MMA has finished reading the tile); weights
+ * stay resident in shared memory; accumulators use 64 TMEM columns (hidden
+ * layers in cols 0..63, the 16-wide output layers in cols 0..15 once the
+ * previous accumulator has been read).  37 KB of shared memory and 64
+ * columns per CTA; FVC_TC_CTAS_PER_SM of them share an SM.  One thread issues each layer's MMAs and
+ * commits them to an mbarrier; the CTA waits (bounded), reads its rows back
+ * with tcgen05.ld, applies ReLU / fp16 rounding and writes the next layer's
+ * operand. */
 struct __align__(128) TcSmem {
     uint8_t W[TC_WBYTES];
     uint8_t X[128 * 64 * 2];
-    uint8_t Y[128 * 64 * 2];
     float bias3[64];
     uint64_t mbar;
     uint32_t tmem_base;
 };
 
 constexpr long long TC_WAIT_LIMIT = 2000000000ll; /* ~1 s of SM clocks */
+constexpr int TC_COLS = 64;
+static_assert(FVC_TC_CTAS_PER_SM * TC_COLS <= 512, "resident CTAs must fit in the SM's 512 TMEM columns");
 
 /* row `row`'s 8 fp16 values of K-chunk c of a tile with K columns */
 __device__ __forceinline__ void st_chunk(uint8_t *tile, int row, int c, int K, uint4 v)
@@ -484,7 +500,7 @@ __device__ __forceinline__ uint4 pack8(const float *v)
     return make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
 }
 
-/* issue one layer: D[tmem_col] (+)= A (128 x K, tile at a) * B^T (N x K, tile at b) */
+/* issue one layer: D[tmem_col] = A (128 x K, tile at a) * B^T (N x K, tile at b) */
 __device__ __forceinline__ void tc_layer(uint32_t tmem, const uint8_t *a, const uint8_t *b, int K, int N)
 {
     const uint32_t sbo = (uint32_t)(K / 8) * 128u;
@@ -498,19 +514,42 @@ __device__ __forceinline__ void tc_layer(uint32_t tmem, const uint8_t *a, const 
 __device__ __forceinline__ void epi_hidden(uint32_t taddr, const float *bias, uint8_t *dst, int row)
 {
 #pragma unroll
-    for (int cg = 0; cg < 4; ++cg) {
-        float v[16];
-        tmem_ld16(taddr + 16 * cg, v);
+    for (int h = 0; h < 2; ++h) {
+        float v[32];
+        tmem_ld32(taddr + 32 * h, v);
         tmem_wait_ld();
 #pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + (bias ? bias[16 * cg + i] : 0.0f), 0.0f);
-        st_chunk(dst, row, 2 * cg, 64, pack8(v));
-        st_chunk(dst, row, 2 * cg + 1, 64, pack8(v + 8));
+        for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + (bias ? bias[32 * h + i] : 0.0f), 0.0f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) st_chunk(dst, row, 4 * h + q, 64, pack8(v + 8 * q));
     }
 }
 
+/* the MMAs of one layer, then the bounded wait for their completion */
+__device__ __forceinline__ bool tc_run(TcSmem &S, uint32_t tmem, const uint8_t *b, int K, int N, uint32_t &phase)
+{
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        tc_layer(tmem, S.X, b, K, N);
+        tc_commit(&S.mbar);
+    }
+    const bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+/* after a thread rewrote its row of the operand tile: make it visible to the
+ * tensor core and order it after this thread's TMEM reads */
+__device__ __forceinline__ bool tc_publish(bool ok)
+{
+    fence_proxy_async();
+    tc_fence_before();
+    return __syncthreads_or(!ok) == 0;
+}
+
 template <int MODE, int HH, bool LIST>
-__global__ void __launch_bounds__(128, 4) wf_net_tc_kernel(RenderParams p, int it)
+__global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(RenderParams p, int it)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
@@ -521,7 +560,7 @@ __global__ void __launch_bounds__(128, 4) wf_net_tc_kernel(RenderParams p, int i
         reinterpret_cast<uint4 *>(S.W)[i] = __ldg(reinterpret_cast<const uint4 *>(p.weights_tc) + i);
     if (tid < 64) S.bias3[tid] = p.bias3[tid];
     if (tid == 0) mbar_init(&S.mbar, 1);
-    if (warp == 0) tmem_alloc(&S.tmem_base, 128);
+    if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -529,45 +568,35 @@ __global__ void __launch_bounds__(128, 4) wf_net_tc_kernel(RenderParams p, int i
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     const RayState *states = p.states[it & 1];
     uint32_t phase = 0;
-    bool failed = false;
+    bool ok = true;
     const int n_tiles = (n_rows + 127) / 128;
-    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const int k = tile * 128 + tid;
         const int r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : p.cache_list[k]) : -1;
         __half2 sh[8];
         uint16_t log_density = 0;
         if (r >= 0) sh16(dir01_of(states, p.row_slot[r]), sh);
         else for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
-        bool ok = true;
         if (MODE == 0) {
-            /* ---- hash features -> X (K = 32) ---- */
+            /* ---- hash features -> tile (K = 32) ---- */
             __half2 feat[16];
             if (r >= 0) {
                 const float4 pw = p.row_pay[r];
-                hash_encode(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
+                hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
             } else {
                 for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
             }
 #pragma unroll
             for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
-            fence_proxy_async();
-            __syncthreads();
-            /* ---- layer 1: 32 -> 64 ---- */
-            if (tid == 0) { tc_fence_after(); tc_layer(tmem, S.X, S.W + TC_B1, 32, 64); tc_commit(&S.mbar); }
-            ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
-            phase ^= 1u;
-            tc_fence_after();
-            epi_hidden(tmem + lane_base, nullptr, S.Y, tid);
-            fence_proxy_async();
-            tc_fence_before();
-            if (__syncthreads_or(!ok)) { failed = true; break; }
+            if (!(ok = tc_publish(ok))) break;
+            /* ---- layer 1: 32 -> 64, ReLU ---- */
+            ok = tc_run(S, tmem, S.W + TC_B1, 32, 64, phase);
+            epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+            if (!(ok = tc_publish(ok))) break;
             /* ---- layer 2: 64 -> 16 (log-density, latents) ---- */
-            if (tid == 0) { tc_fence_after(); tc_layer(tmem + 64, S.Y, S.W + TC_B2, 64, 16); tc_commit(&S.mbar); }
-            ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
-            phase ^= 1u;
-            tc_fence_after();
+            ok = tc_run(S, tmem, S.W + TC_B2, 64, 16, phase);
             float v[16];
-            tmem_ld16(tmem + lane_base + 64, v);
+            tmem_ld16(tmem + lane_base, v);
             tmem_wait_ld();
             const uint4 b0 = pack8(v), b1 = pack8(v + 8);
             log_density = (uint16_t)(b0.x & 0xffffu);
@@ -588,49 +617,34 @@ __global__ void __launch_bounds__(128, 4) wf_net_tc_kernel(RenderParams p, int i
         }
         st_chunk(S.X, tid, 2, 32, *reinterpret_cast<const uint4 *>(sh));
         st_chunk(S.X, tid, 3, 32, *reinterpret_cast<const uint4 *>(sh + 4));
-        fence_proxy_async();
-        tc_fence_before();
-        if (__syncthreads_or(!ok)) { failed = true; break; }
-        /* ---- head layer 1: (latents | SH) 32 -> 64, bias from the 1-padding ---- */
-        if (tid == 0) { tc_fence_after(); tc_layer(tmem, S.X, S.W + TC_B3, 32, 64); tc_commit(&S.mbar); }
-        ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
-        phase ^= 1u;
-        tc_fence_after();
-        uint8_t *last = S.Y;
-        epi_hidden(tmem + lane_base, S.bias3, S.Y, tid);
-        fence_proxy_async();
-        tc_fence_before();
-        if (__syncthreads_or(!ok)) { failed = true; break; }
+        if (!(ok = tc_publish(ok))) break;
+        /* ---- head layer 1: (latents | SH) 32 -> 64, bias from the 1-padding, ReLU ---- */
+        ok = tc_run(S, tmem, S.W + TC_B3, 32, 64, phase);
+        epi_hidden(tmem + lane_base, S.bias3, S.X, tid);
+        if (!(ok = tc_publish(ok))) break;
         if (HH == 2) {
-            /* ---- head layer 2: 64 -> 64 ---- */
-            if (tid == 0) { tc_fence_after(); tc_layer(tmem, S.Y, S.W + TC_B4, 64, 64); tc_commit(&S.mbar); }
-            ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
-            phase ^= 1u;
-            tc_fence_after();
+            /* ---- head layer 2: 64 -> 64, ReLU ---- */
+            ok = tc_run(S, tmem, S.W + TC_B4, 64, 64, phase);
             epi_hidden(tmem + lane_base, nullptr, S.X, tid);
-            fence_proxy_async();
-            tc_fence_before();
-            if (__syncthreads_or(!ok)) { failed = true; break; }
-            last = S.X;
+            if (!(ok = tc_publish(ok))) break;
         }
         /* ---- output layer: 64 -> 16 (rgb logits in cols 0..2) ---- */
-        if (tid == 0) { tc_fence_after(); tc_layer(tmem + 64, last, S.W + TC_B5, 64, 16); tc_commit(&S.mbar); }
-        ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
-        phase ^= 1u;
-        tc_fence_after();
+        ok = tc_run(S, tmem, S.W + TC_B5, 64, 16, phase);
         float o[16];
-        tmem_ld16(tmem + lane_base + 64, o);
+        tmem_ld16(tmem + lane_base, o);
         tmem_wait_ld();
-        if (r >= 0) p.row_out[r] = make_uint2(pack_h2(o[0], o[1]), (uint32_t)__half_as_ushort(__float2half_rn(o[2])) | ((uint32_t)log_density << 16));
+        if (r >= 0)
+            p.row_out[r] = make_uint2(pack_h2(o[0], o[1]),
+                                      (uint32_t)__half_as_ushort(__float2half_rn(o[2])) | ((uint32_t)log_density << 16));
         tc_fence_before();
-        if (__syncthreads_or(!ok)) { failed = true; break; }
+        if (__syncthreads_or(!ok)) { ok = false; break; }
     }
-    if (failed && tid == 0) atomicOr(p.guard, 16);
+    if (!ok && tid == 0) atomicOr(p.guard, 16);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tmem, 128);
+        tmem_dealloc(tmem, TC_COLS);
     }
 }
 
@@ -733,7 +747,8 @@ static cudaError_t set_net_attrs()
 }
 
 template <bool CACHED, int HH>
-static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, int *h_pinned, int check_every, int *n_iter)
+static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, int *h_pinned, int check_every, int *n_iter,
+                             LaunchLog *log)
 {
     static bool attrs_set = false;
     if (!attrs_set) {
@@ -741,33 +756,48 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
         if (e != cudaSuccess) return e;
         attrs_set = true;
     }
+    LaunchLog local;
+    LaunchLog &L = log ? *log : local;
+    auto timed_begin = [&]() {
+        if (L.ev && L.n_timed < L.cap) cudaEventRecord(L.ev[2 * L.n_timed], s);
+    };
+    auto timed_end = [&]() {
+        if (L.ev && L.n_timed < L.cap) cudaEventRecord(L.ev[2 * L.n_timed++ + 1], s);
+        else if (L.ev) ++L.n_untimed;
+    };
     const int W = p.cam.W, H = p.cam.H;
     const int n_threads = ((W + 7) / 8) * ((H + 3) / 4) * 32;
     wf_raygen_kernel<<<(n_threads + 255) / 256, 256, 0, s>>>(p);
+    ++L.launches;
     const int grid_ray = n_sms * 16;
     const int grid_net = n_sms * 2;
     const size_t net_smem = sizeof(NetSmem);
+    const size_t tc_smem = sizeof(TcSmem);
+    const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM; /* <= 8 CTAs x 64 TMEM columns per SM */
     int it = 0;
     const int max_it = 1 << 20;
     for (; it < max_it; ++it) {
         wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
-        const size_t tc_smem = sizeof(TcSmem);
-        const int grid_tc = n_sms * 4; /* 4 CTAs x 128 TMEM columns fill an SM's 512 columns */
+        ++L.launches;
         if (CACHED) {
             wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
-            if (p.use_tc) {
-                wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
-                wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
-            } else {
-                wf_net_resample_kernel<HH, true><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
-                wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
-            }
+            timed_begin();
+            if (p.use_tc) wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            else wf_net_resample_kernel<HH, true><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            timed_end();
+            if (p.use_tc) wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            else wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            L.launches += 3;
         } else {
+            timed_begin();
             if (p.use_tc) wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
             else wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            timed_end();
+            L.launches += 1;
         }
         wf_composite_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
         wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, CACHED ? 1 : 0);
+        L.launches += 2;
         if ((it + 1) % check_every == 0) {
             cudaError_t e = cudaMemcpyAsync(h_pinned, p.counters + ((it + 1) & 1), sizeof(int), cudaMemcpyDeviceToHost, s);
             if (e != cudaSuccess) return e;
@@ -781,13 +811,13 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
 }
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
-                         int check_every, int *n_iterations)
+                         int check_every, int *n_iterations, LaunchLog *log)
 {
     if (cached)
-        return head_hidden == 2 ? run_frame<true, 2>(p, n_sms, s, h_pinned, check_every, n_iterations)
-                                : run_frame<true, 1>(p, n_sms, s, h_pinned, check_every, n_iterations);
-    return head_hidden == 2 ? run_frame<false, 2>(p, n_sms, s, h_pinned, check_every, n_iterations)
-                            : run_frame<false, 1>(p, n_sms, s, h_pinned, check_every, n_iterations);
+        return head_hidden == 2 ? run_frame<true, 2>(p, n_sms, s, h_pinned, check_every, n_iterations, log)
+                                : run_frame<true, 1>(p, n_sms, s, h_pinned, check_every, n_iterations, log);
+    return head_hidden == 2 ? run_frame<false, 2>(p, n_sms, s, h_pinned, check_every, n_iterations, log)
+                            : run_frame<false, 1>(p, n_sms, s, h_pinned, check_every, n_iterations, log);
 }
 
 }  // namespace fvc

@@ -104,7 +104,8 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
 }
 
 /* wait for the given phase parity with a deadline of `limit_cycles` SM
- * clocks (non-blocking test_wait in a loop); false when the deadline passed */
+ * clocks; try_wait suspends the thread for at most ~20 us per attempt instead
+ * of spinning on the issue slots.  false when the deadline passed. */
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long long limit_cycles)
 {
     const uint32_t a = smem_u32(mbar);
@@ -112,13 +113,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long 
     for (;;) {
         uint32_t done;
         asm volatile(
-            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(20000)
             : "memory");
         if (done) return true;
         if (clock64() - t0 > limit_cycles) return false;
     }
+}
+
+/* 32 consecutive 32-bit columns of this thread's TMEM lane */
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 }  // namespace fvc

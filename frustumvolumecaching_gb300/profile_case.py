@@ -1,0 +1,73 @@
+"""A small, fixed rendering case for kernel profiles.
+
+    python -m frustumvolumecaching_gb300.profile_case --res 960x540 --frames 2 --path plain --network tc
+
+Renders `frames` frames of the benchmark's camera path (the synthetic
+3-cascade, 2^19-entry scene) at the given resolution through the C ABI and
+prints one JSON line per frame: resample rows, cache rows, kernels launched
+and the event-timed resample-kernel milliseconds.  The counts are
+deterministic, so a run under a profiler processes exactly the rows the
+plain run printed; per-row DRAM traffic is a capture's bytes divided by them.
+The cached path builds its cache at frame 0 and rebuilds it whenever the
+reprojected coverage drops below 0.9, like the benchmark.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import camera as fcam
+from . import model as fmodel
+from .renderer import (Cache, CachePerformanceRenderer, PerformanceRenderer, default_cache_settings, load_data,
+                       raymarch_info)
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--res", default="960x540")
+    ap.add_argument("--frames", type=int, default=2)
+    ap.add_argument("--path", choices=["plain", "cached"], default="plain")
+    ap.add_argument("--network", choices=["tc", "mma"], default="tc")
+    args = ap.parse_args(argv)
+    W, H = (int(v) for v in args.res.lower().split("x"))
+    spec = fmodel.spec_config2()
+    loader = load_data(fmodel.ensure_model(spec))
+    cams = fcam.rotation_path(spec.seed, n_frames=args.frames, width=W, height=H)
+    infos = [raymarch_info(c, loader.stepsize_info) for c in cams]
+    if args.path == "plain":
+        r = PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    else:
+        caches = (Cache(), Cache())
+        r = CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network,
+                                     caches[0], caches[1])
+        r.resizeCache((W, H), loader.stepsize_info)
+        r.setCacheSettings(default_cache_settings())
+    r.resizeRenderbuffers((W, H))
+    r.set_network_path(args.network == "tc")
+    r.set_kernel_timing(True)
+    for i, info in enumerate(infos):
+        build = None
+        if args.path == "cached" and i == 0:
+            r.initCacheBlockwise(info)
+            r.swapCache()
+            build = r._init_stats
+        r.render_device(info)
+        st = r._render_stats
+        line = {"frame": i, "resample_rows": st.n_resamples, "cache_rows": st.n_cache_hits,
+                "launches": st.n_launches, "resample_kernel_launches": st.n_timed_launches,
+                "resample_kernel_ms": round(st.timed_kernel_ms, 3), "guard": st.guard_flags}
+        if args.path == "cached":
+            cov = st.n_cache_hits / max(1, st.n_cache_hits + st.n_resamples)
+            line["coverage"] = round(cov, 4)
+            if cov < 0.9 and i + 1 < len(infos):
+                r.initCacheBlockwise(info)
+                r.swapCache()
+                build = r._init_stats
+            if build is not None:
+                line["build_launches"] = build.n_launches
+                line["bricks_demanded"] = build.n_bricks_demanded
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

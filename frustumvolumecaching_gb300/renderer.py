@@ -154,6 +154,10 @@ class Renderer:
         """tcgen05 (default) or mma.sync network kernels."""
         L.check(L.load().fvc_renderer_set_network_path(self.handle, int(bool(use_tcgen05))))
 
+    def set_kernel_timing(self, enable: bool) -> None:
+        """CUDA-event timing of each resample network launch (see _render_stats.timed_kernel_ms)."""
+        L.check(L.load().fvc_renderer_set_kernel_timing(self.handle, int(bool(enable))))
+
     def set_max_samples_per_ray(self, n: int) -> None:
         L.check(L.load().fvc_renderer_set_max_samples_per_ray(self.handle, n))
 

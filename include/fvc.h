@@ -138,6 +138,9 @@ typedef struct {
     long long n_steps;               /* marching steps taken                 */
     int n_rounds;                    /* sub-iterations of the last render */
     int guard_flags;                 /* device guard bits (0 = none fired)   */
+    long long n_launches;            /* kernels launched by the last render  */
+    int n_timed_launches;            /* resample network launches timed      */
+    float timed_kernel_ms;           /* their summed event time (0 = off)    */
 } fvc_render_stats_t;
 
 typedef struct {
@@ -146,6 +149,7 @@ typedef struct {
     int n_bricks_demanded;  /* allocations requested incl. overflowed    */
     int overflow;           /* 1 if at least one allocation overflowed   */
     int n_iterations;       /* depth-brick iterations of the build       */
+    int n_launches;         /* kernels launched by the build             */
     long long n_samples;    /* samples evaluated by the density network  */
 } fvc_cache_stats_t;
 
@@ -168,6 +172,20 @@ void fvc_model_destroy(fvc_model *m);
 /* Scene and step parameters of the loaded model (LoaderData::scene_info,
  * ::stepsize_info after StepsizeInfo::setAdditionalInfo, include/common.h:109-131). */
 int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_stepsize_info *steps);
+
+/* Network and occupancy-grid properties a caller of the reference reads from
+ * NerfNetwork / LoaderData: m_first_latent_is_density (include/nerf_network.h:342),
+ * the head depth, and the device Morton bitfield (LoaderData::
+ * occupancy_grid_morton_bitfield, include/loader.h:46; R^3 * nlvl / 8 bytes). */
+typedef struct {
+    int first_latent_is_density;
+    int head_hidden_layers;
+    int n_levels;
+    int n_latents;
+    const uint8_t *occupancy_bitfield;
+    size_t occupancy_bytes;
+} fvc_model_props;
+int fvc_model_properties(const fvc_model *m, fvc_model_props *out);
 /* Evaluate log-density (fp16-rounded density-network row 0) at n contracted
  * positions pos[3*n] in [0,1]^3 (NerfNetwork::inferenceLatents row 0,
  * include/nerf_network.h:173-202). Host buffers. */
@@ -220,6 +238,11 @@ int fvc_render_device(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_
 /* Same with host pointers: H2D of the previous image (progressive average),
  * render, D2H of the outputs, synchronise. */
 int fvc_render(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out);
+
+/* Block until everything enqueued on the renderer's stream finished (the
+ * reference's render() ends with CUDA_SYNC_CHECK_THROW,
+ * src/performance_renderer.cu:283); reports a device guard as FVC_ERR_GUARD. */
+int fvc_renderer_synchronize(fvc_renderer *r);
 /* Guard on the samples of one ray (0 = off, the reference default); a ray
  * exceeding it sets a guard bit reported by fvc_render_stats. */
 int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
@@ -230,6 +253,13 @@ int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
 int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05);
 /* Statistics of the last render (needs the stream synchronised). */
 int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *out);
+
+/* Record a CUDA event pair on the renderer's stream around every resample
+ * network launch of the following renders (up to 4096 per render), summed
+ * into fvc_render_stats.timed_kernel_ms.  No counterpart in the reference
+ * (its timers wrap whole phases, include/renderer.h:79-105); used by the
+ * benchmark to time the dominant kernel on its own stream. */
+int fvc_renderer_set_kernel_timing(fvc_renderer *r, int enable);
 
 /* Render without allocating (no counterpart in the reference).  For callers
  * that cannot call cudaMalloc while rendering (a host with its own fixed GPU
