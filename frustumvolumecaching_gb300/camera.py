@@ -87,3 +87,23 @@ def rotation_path(seed: int, n_frames: int = 60, deg_per_frame: float = 0.5, ste
         e = e * (np.linalg.norm(e) - step_per_frame * i) / np.linalg.norm(e)
         cams.append(camera_dict(look_at(e), width, height, fov_deg))
     return cams
+
+
+def write_nerfacc_camera_path(path: str, cams: list[dict], image_stem: str = "frame") -> None:
+    """The cameras as a nerfacc camera file (the format load_camerapath reads,
+    src/loader.cu:322-343 with include/parse_helper.h:66-107): width, height,
+    is_open_gl, 3x3 intrinsics and frames of 4x4 cam2world rows + image_path."""
+    import json
+
+    c0 = cams[0]
+    W, H = c0["resolution"]
+    (fx, fy), (cx, cy) = c0["focal"], c0["principal"]
+    frames = []
+    for i, c in enumerate(cams):
+        m = np.asarray(c["cam2world"], np.float64)
+        rows = [[float(v) for v in m[r]] for r in range(3)] + [[0.0, 0.0, 0.0, 1.0]]
+        frames.append({"transform_matrix": rows, "image_path": f"{image_stem}_{i:03d}"})
+    doc = {"width": int(W), "height": int(H), "is_open_gl": bool(c0["is_open_gl"]),
+           "intrinsics": [[float(fx), 0.0, float(cx)], [0.0, float(fy), float(cy)], [0.0, 0.0, 1.0]], "frames": frames}
+    with open(path, "w") as f:
+        json.dump(doc, f, indent=1)
