@@ -855,4 +855,243 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
     return 0;
 }
 
+
+}  /* extern "C" */
+
+/* ========================================================================== */
+/* Differentiable render: L2 loss of the plain render at a list of pixels and
+ * its adjoint with respect to the hash table and both MLPs (float64).
+ *
+ * Loss: L = (1/N) sum_rays sum_k (C_k + T - target_k)^2, the white-background
+ * pixel of the plain render (writeImageBuffer_performance_kernel,
+ * src/performance_renderer.cu:127-149, before the 8-bit conversion).
+ * Compositing adjoint, in sample order without division: with g = dL/dC,
+ * g_T = dL/dT, X_total = g.C + g_T T_final and X_i the prefix sum of
+ * T_j alpha_j g.c_j over used samples j <= i,
+ *   dL/dsigma_i = dt_i (T_{i+1} g.c_i - (X_total - X_i)),
+ *   dL/dc_i     = T_i alpha_i g;
+ * samples skipped by the alpha threshold carry no gradient, and the early
+ * termination (T < 1e-4) ends both passes at the same sample.  The network
+ * adjoint treats the fp16 rounding of activations (mimic_fp16) as identity;
+ * ReLU passes gradient where its output is > 0.
+ * Parameter blobs (and gradients) use the model file layouts: table
+ * [entries x F]; base [width x enc_w_pad][base_out_pad x width]; head
+ * [width x head_in_pad][width x width]*[16 x width].                         */
+/* ========================================================================== */
+namespace {
+
+struct Acts {
+    double feat[64], h1[128], out2[64], in[128], hid[4][128], out[16];
+};
+
+void forward_acts(const NetD &d, V3 pos, const float *d01, Acts &A)
+{
+    const OrcNet &n = *d.n;
+    hash_encode(d, pos, A.feat);
+    dense_layer(d.bw0.data(), n.width, n.enc_w_pad, A.feat, A.h1, true, n.mimic_fp16);
+    dense_layer(d.bw1.data(), n.base_out_pad, n.width, A.h1, A.out2, false, n.mimic_fp16);
+    for (int i = 0; i < n.n_latents; ++i) A.in[i] = A.out2[n.latent_offset + i];
+    sh16(d01, A.in + n.n_latents);
+    if (n.mimic_fp16) for (int i = n.n_latents; i < n.n_latents + 16; ++i) A.in[i] = round_h(A.in[i]);
+    for (int i = n.head_in; i < n.head_in_pad; ++i) A.in[i] = 1.0;
+    dense_layer(d.hw[0].data(), n.width, n.head_in_pad, A.in, A.hid[0], true, n.mimic_fp16);
+    for (int l = 1; l < n.head_layers - 1; ++l)
+        dense_layer(d.hw[l].data(), n.width, n.width, A.hid[l - 1], A.hid[l], true, n.mimic_fp16);
+    dense_layer(d.hw[n.head_layers - 1].data(), 16, n.width, A.hid[n.head_layers - 2], A.out, false, n.mimic_fp16);
+}
+
+/* y = W x (W: out x in) backward: gW += dy (x) x, dx = W^T dy (dx may be null) */
+inline void dense_backward(const double *W, int out, int in, const double *x, const double *dy, double *gW, double *dx)
+{
+    if (dx) for (int i = 0; i < in; ++i) dx[i] = 0.0;
+    for (int o = 0; o < out; ++o) {
+        const double g = dy[o];
+        if (g == 0.0) continue;
+        const double *w = W + (size_t)o * in;
+        if (gW) { double *gw = gW + (size_t)o * in; for (int i = 0; i < in; ++i) gw[i] += g * x[i]; }
+        if (dx) for (int i = 0; i < in; ++i) dx[i] += g * w[i];
+    }
+}
+
+/* hash-grid adjoint: scatter dfeat into the table gradient with the trilinear weights */
+void hash_backward(const NetD &d, V3 pos, const double *dfeat, double *g_table)
+{
+    const OrcNet &n = *d.n;
+    const float px[3] = {pos.x, pos.y, pos.z};
+    for (int l = 0; l < n.n_levels; ++l) {
+        uint32_t g[3]; double fr[3];
+        for (int k = 0; k < 3; ++k) {
+            const float p = fmaf(n.scale[l], px[k], 0.5f);
+            const float fl = floorf(p);
+            g[k] = (uint32_t)(int)fl;
+            fr[k] = (double)(p - fl);
+        }
+        for (int c = 0; c < 8; ++c) {
+            uint32_t q[3]; double w = 1.0;
+            for (int k = 0; k < 3; ++k) {
+                const int b = (c >> k) & 1;
+                q[k] = g[k] + (uint32_t)b;
+                w *= b ? fr[k] : 1.0 - fr[k];
+            }
+            uint32_t idx;
+            if (n.dense[l]) idx = q[0] + q[1] * n.res[l] + q[2] * n.res[l] * n.res[l];
+            else idx = (q[0] * 1u) ^ (q[1] * 2654435761u) ^ (q[2] * 805459861u);
+            idx %= n.size[l];
+            double *e = &g_table[((size_t)n.offset[l] + idx) * n.F];
+            for (int f = 0; f < n.F; ++f) e[f] += w * dfeat[l * n.F + f];
+        }
+    }
+}
+
+/* network adjoint of one sample given dL/d(log sigma) and dL/d(rgb logits) */
+void network_backward(const NetD &d, V3 pos, const Acts &A, double d_logsigma, const double *d_logit,
+                      double *g_table, double *g_base, double *g_head)
+{
+    const OrcNet &n = *d.n;
+    double dy[128], dx[128];
+    for (int i = 0; i < 16; ++i) dy[i] = i < 3 ? d_logit[i] : 0.0;
+    /* head, last layer back to its first */
+    size_t head_off[4], off = 0;
+    for (int l = 0; l < n.head_layers; ++l) {
+        head_off[l] = off;
+        off += (size_t)(l == 0 ? n.head_in_pad : n.width) * (l == n.head_layers - 1 ? 16 : n.width);
+    }
+    const int L = n.head_layers;
+    dense_backward(d.hw[L - 1].data(), 16, n.width, A.hid[L - 2], dy, g_head ? g_head + head_off[L - 1] : nullptr, dx);
+    for (int l = L - 2; l >= 0; --l) {
+        for (int i = 0; i < n.width; ++i) dy[i] = A.hid[l][i] > 0.0 ? dx[i] : 0.0;
+        const int in = l == 0 ? n.head_in_pad : n.width;
+        const double *x = l == 0 ? A.in : A.hid[l - 1];
+        dense_backward(d.hw[l].data(), n.width, in, x, dy, g_head ? g_head + head_off[l] : nullptr, dx);
+    }
+    /* density network */
+    double dout2[64];
+    for (int i = 0; i < n.base_out_pad; ++i) dout2[i] = 0.0;
+    dout2[0] += d_logsigma;
+    for (int j = 0; j < n.n_latents; ++j) dout2[n.latent_offset + j] += dx[j];
+    const size_t nb0 = (size_t)n.width * n.enc_w_pad;
+    double dh[128];
+    dense_backward(d.bw1.data(), n.base_out_pad, n.width, A.h1, dout2, g_base ? g_base + nb0 : nullptr, dh);
+    for (int i = 0; i < n.width; ++i) dh[i] = A.h1[i] > 0.0 ? dh[i] : 0.0;
+    double dfeat[64];
+    dense_backward(d.bw0.data(), n.width, n.enc_w_pad, A.feat, dh, g_base, dfeat);
+    if (g_table) hash_backward(d, pos, dfeat, g_table);
+}
+
+void apply_perturbations(NetD &d, const int32_t *group, const int64_t *index, const double *delta, int n)
+{
+    for (int i = 0; i < n; ++i) {
+        size_t k = (size_t)index[i];
+        if (group[i] == 0) { d.table[k] += delta[i]; continue; }
+        if (group[i] == 1) {
+            if (k < d.bw0.size()) d.bw0[k] += delta[i];
+            else d.bw1[k - d.bw0.size()] += delta[i];
+            continue;
+        }
+        for (int l = 0; l < d.n->head_layers; ++l) {
+            if (k < d.hw[l].size()) { d.hw[l][k] += delta[i]; break; }
+            k -= d.hw[l].size();
+        }
+    }
+}
+
+/* one ray of the differentiable render: forward, then (if grads) the adjoint */
+double ray_loss_grad(const NetD &d, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                     int px, int py, const float *target, double inv_n, double *pred,
+                     double *g_table, double *g_base, double *g_head)
+{
+    const OrcNet &n = *d.n;
+    const Ray r = generate_ray(*cam, px, py);
+    float tn, tf;
+    struct S { V3 pos; float dt; };
+    std::vector<S> samples;
+    std::vector<double> sig, rgbv;
+    double C[3] = {0, 0, 0}, T = 1.0;
+    const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
+    if (ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf)) {
+        const float far_ = fminf(tf, st->far_);
+        float t1 = valid_t_from_t(*st, tn) + 0.0f;
+        for (;;) {
+            const float t0 = t1;
+            const float dt = calc_step(*st, t0);
+            t1 = t0 + dt;
+            const float tm = (t0 + t1) * 0.5f;
+            if (tm > far_) break;
+            const V3 wp = at(r, tm);
+            if (!occupied(*sc, bits, wp)) continue;
+            const V3 cp = contract(*sc, wp);
+            Acts A;
+            forward_acts(d, cp, d01, A);
+            const double sigma = std::exp(A.out2[0]);
+            samples.push_back({cp, dt});
+            sig.push_back(sigma);
+            for (int k = 0; k < 3; ++k) rgbv.push_back(sigmoid(A.out[k]));
+            if (composite(sigma, A.out, dt, sc->alpha_thre, C, T)) break;
+        }
+    }
+    double loss = 0.0, g[3];
+    for (int k = 0; k < 3; ++k) {
+        const double e = C[k] + T - (double)target[k];
+        loss += e * e * inv_n;
+        g[k] = 2.0 * e * inv_n;
+    }
+    if (pred) { pred[0] = C[0]; pred[1] = C[1]; pred[2] = C[2]; pred[3] = T; }
+    if (!(g_table || g_base || g_head)) return loss;
+    const double gT = g[0] + g[1] + g[2];
+    const double x_total = g[0] * C[0] + g[1] * C[1] + g[2] * C[2] + gT * T;
+    double Ti = 1.0, x_prefix = 0.0;
+    for (size_t i = 0; i < samples.size(); ++i) {
+        const double sigma = sig[i];
+        const double *c = &rgbv[3 * i];
+        double alpha = 1.0 - std::exp(-sigma * (double)samples[i].dt);
+        alpha = std::min(1.0, std::max(0.0, alpha));
+        if (!(alpha > (double)sc->alpha_thre)) continue;
+        const double gc = g[0] * c[0] + g[1] * c[1] + g[2] * c[2];
+        x_prefix += Ti * alpha * gc;
+        const double T_next = Ti * (1.0 - alpha);
+        const double d_sigma = (double)samples[i].dt * (T_next * gc - (x_total - x_prefix));
+        double d_logit[3];
+        for (int k = 0; k < 3; ++k) d_logit[k] = g[k] * Ti * alpha * c[k] * (1.0 - c[k]);
+        Acts A;
+        forward_acts(d, samples[i].pos, d01, A);
+        network_backward(d, samples[i].pos, A, d_sigma * sigma, d_logit, g_table, g_base, g_head);
+        Ti = T_next;
+        if (Ti < 1e-4) break;
+    }
+    (void)n;
+    return loss;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Loss (and, when any gradient pointer is given, its float64 adjoint,
+ * accumulated into the given arrays) of the plain render at pixels[i]
+ * (y * W + x) against target[3 i .. 3 i + 2].  Perturbations
+ * (group 0 table, 1 base blob, 2 head blob; index; delta) are added to the
+ * float64 parameters first (finite differences).  pred[4 i] receives
+ * (C, T) when non-null.  Gradients run single-threaded (deterministic). */
+double orc_loss_grad(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                     const int32_t *pixels, int n_rays, const float *target, double *g_table, double *g_base, double *g_head,
+                     const int32_t *pert_group, const int64_t *pert_index, const double *pert_delta, int n_pert,
+                     int n_threads, double *pred)
+{
+    NetD d; prepare_net(net, d);
+    apply_perturbations(d, pert_group, pert_index, pert_delta, n_pert);
+    const double inv_n = 1.0 / (double)std::max(1, n_rays);
+    const bool grads = g_table || g_base || g_head;
+    std::vector<double> per_ray(n_rays, 0.0);
+    auto one = [&](int i) {
+        const int p = pixels[i];
+        per_ray[i] = ray_loss_grad(d, sc, st, cam, bits, p % cam->W, p / cam->W, target + 3 * (size_t)i, inv_n,
+                                   pred ? pred + 4 * (size_t)i : nullptr, g_table, g_base, g_head);
+    };
+    if (grads) for (int i = 0; i < n_rays; ++i) one(i);
+    else parallel_rows(n_rays, n_threads, one);
+    double loss = 0.0;
+    for (double v : per_ray) loss += v;
+    return loss;
+}
+
 }  /* extern "C" */

@@ -89,6 +89,10 @@ def lib():
         _lib.orc_hash_encode.argtypes = [P(OrcNet), C.c_void_p, C.c_int, C.c_void_p]
         _lib.orc_render_plain.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, C.c_int, C.c_int,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_loss_grad.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_int, C.c_void_p]
+        _lib.orc_loss_grad.restype = C.c_double
         _lib.orc_cache_dims.argtypes = [P(OrcScene), P(OrcSteps), C.c_int, C.c_int, P(OrcCacheDims)]
         _lib.orc_cache_build.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache), C.c_int]
         _lib.orc_render_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
@@ -219,6 +223,32 @@ class OracleModel:
         lib().orc_render_plain(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
                                r0, r1, ptr(res), ptr(ns), ptr(nst), threads or default_threads())
         return res, ns, nst
+
+    # -- differentiable render --------------------------------------------
+    def loss_grad(self, cam: dict, pixels: np.ndarray, target: np.ndarray, grads: bool = True,
+                  perturb=None, threads: int | None = None):
+        """Loss of the plain render at `pixels` (y*W+x) against target [n,3]
+        and, if grads, the float64 gradients (table, base blob, head blob).
+        perturb = (groups, indices, deltas) added to the parameters first.
+        Returns (loss, g_table, g_base, g_head, pred[n,4])."""
+        c = make_cam(cam)
+        px = np.ascontiguousarray(pixels, np.int32)
+        tg = np.ascontiguousarray(target, np.float32).reshape(-1)
+        pred = np.zeros((px.size, 4), np.float64)
+        gt = np.zeros(self.table.size, np.float64) if grads else None
+        gb = np.zeros(self.base_w.size, np.float64) if grads else None
+        gh = np.zeros(self.head_w.size, np.float64) if grads else None
+        if perturb is not None:
+            pg = np.ascontiguousarray(perturb[0], np.int32)
+            pi = np.ascontiguousarray(perturb[1], np.int64)
+            pd = np.ascontiguousarray(perturb[2], np.float64)
+            npert, pgp, pip, pdp = pg.size, ptr(pg), ptr(pi), ptr(pd)
+        else:
+            npert, pgp, pip, pdp = 0, None, None, None
+        loss = lib().orc_loss_grad(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
+                                   ptr(px), px.size, ptr(tg), ptr(gt) if grads else None, ptr(gb) if grads else None,
+                                   ptr(gh) if grads else None, pgp, pip, pdp, npert, threads or default_threads(), ptr(pred))
+        return loss, gt, gb, gh, pred
 
     def cache_dims(self, W: int, H: int, steps: OrcSteps | None = None) -> OrcCacheDims:
         d = OrcCacheDims()
