@@ -168,6 +168,73 @@ def cpu_baseline_port(args) -> dict:
 
 
 # --------------------------------------------------------------------------
+# differentiable render (backward Mrays/s)
+# --------------------------------------------------------------------------
+BWD_RAYS = 1 << 18
+BWD_RES = (800, 800)
+
+
+def run_backward_bench(args, torch, dev, stream) -> dict:
+    """Forward + adjoint of the plain render on 2^18 random rays of an 800x800
+    view against the image of a second seeded network (same architecture,
+    2^19 entries/level); one step = one fvc_render_backward call."""
+    import frustumvolumecaching_gb300 as fvc
+    from frustumvolumecaching_gb300 import camera as fcam
+    from frustumvolumecaching_gb300 import model as fmodel
+
+    spec = fmodel.spec_config5()
+    train = fvc.load_data(fmodel.ensure_model(spec))
+    target_net = fvc.load_data(fmodel.ensure_model(fmodel.spec_config5(target=True)))
+    W, H = BWD_RES
+    cam = fcam.seeded_camera(spec.seed, width=W, height=H)
+    rng = np.random.default_rng(spec.seed)
+    pix_h = rng.choice(W * H, BWD_RAYS, replace=False).astype(np.int32)
+    sh = stream.cuda_stream
+    tr = fvc.PerformanceRenderer(target_net.scene_info, target_net.occupancy_grid_morton_bitfield, target_net.nerf_network)
+    tr.set_stream(sh)
+    full = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    tr.render_device(fvc.raymarch_info(cam, target_net.stepsize_info), results=full)
+    torch.cuda.synchronize(dev)
+    pixels = torch.from_numpy(pix_h).to(dev)
+    flat = full.reshape(-1, 4)[pixels.long()]
+    target = (flat[:, :3] + flat[:, 3:4]).contiguous()
+    r = fvc.PerformanceRenderer(train.scene_info, train.occupancy_grid_morton_bitfield, train.nerf_network)
+    r.set_stream(sh)
+    r.resizeRenderbuffers(BWD_RES)
+    info = fvc.raymarch_info(cam, train.stepsize_info)
+    grads = fvc.Gradients(train.nerf_network)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for _ in range(args.warmup):
+        r.render_backward(info, pixels, target, grads)
+    torch.cuda.synchronize(dev)
+    times, loss, launches = [], None, 0
+    for _ in range(args.steps):
+        a, b = ev(), ev()
+        a.record(stream)
+        loss = r.render_backward(info, pixels, target, grads)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        times.append(a.elapsed_time(b))
+        launches += r._render_stats.n_launches
+    ms = sum(times) / len(times)
+    out = {"value": BWD_RAYS / (ms / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms, "rays_per_step": BWD_RAYS,
+           "resolution": list(BWD_RES), "loss": loss, "gpu_launches": launches // max(1, args.steps),
+           "workload": "c5 differentiable plain render: forward + adjoint (hash table, both MLPs), fp16 MLP",
+           "dtype": "f16 MLP (fp32 accumulate, loss-scaled fp16 gradient tiles), f32 compositing and gradients"}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        om = orc.OracleModel(fmodel.ensure_model(spec))
+        n = 256
+        tgt_h = target[:n].cpu().numpy()
+        t0 = time.perf_counter()
+        om.loss_grad(cam, pix_h[:n], tgt_h)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt / 1e6, "unit": "Mrays/s", "cores": 1, "kind": "port",
+                               "sample": f"{n} of the rays, float64 oracle adjoint (single thread), {dt:.2f} s"}
+    return out
+
+
+# --------------------------------------------------------------------------
 # GB300 arm
 # --------------------------------------------------------------------------
 def run_fvc(args) -> dict | None:
@@ -330,6 +397,8 @@ def run_fvc(args) -> dict | None:
     clk = clocks.stop()
     cached.set_kernel_timing(False)
 
+    backward = run_backward_bench(args, torch, dev, stream)
+
     # e2e: the cached path through the host-buffer C-ABI call (D2H of every frame)
     hbuf = fvc.RenderBuffer(RES)
     barrier()
@@ -401,6 +470,7 @@ def run_fvc(args) -> dict | None:
                              "(ncu dram bytes, scaled per row) is far below the algorithmic bytes"},
         "e2e": {"value": fps_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": n_frames * W * H * (4 + 16 + 16)},
+        "backward": backward,
         "gpu_launches": log["launches"] // max(1, args.steps),
         "gpu_launches_plain_path": log["plain_launches"] // max(1, args.steps),
         "clocks": clk,

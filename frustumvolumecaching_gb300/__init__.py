@@ -4,6 +4,6 @@ The compute path is libfvc.so (hand-written CUDA for sm_103a behind the C ABI
 of include/fvc.h); this package holds its ctypes binding, the Python mirror of
 the reference's renderer API, and the seeded synthetic-model generator.
 """
-from .renderer import (BasicRenderer, Cache, CachePerformanceRenderer, LoaderData, NerfNetwork,  # noqa: F401
+from .renderer import (BasicRenderer, Cache, CachePerformanceRenderer, Gradients, LoaderData, NerfNetwork,  # noqa: F401
                        PerformanceRenderer, RenderBuffer, Renderer, camera_info, default_cache_settings, load_data,
                        raymarch_info)

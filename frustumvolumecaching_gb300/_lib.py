@@ -138,6 +138,12 @@ SIGNATURES = {
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_model_properties": (c_int, [P, C.POINTER(ModelProps)]),
     "fvc_renderer_synchronize": (c_int, [P]),
+    "fvc_grad_create": (c_int, [P, PP]),
+    "fvc_grad_destroy": (None, [P]),
+    "fvc_grad_zero": (c_int, [P]),
+    "fvc_grad_sizes": (c_int, [P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "fvc_grad_read": (c_int, [P, P, P, P]),
+    "fvc_render_backward": (c_int, [P, P, C.POINTER(RaymarchInfo), P, c_int, P, C.POINTER(C.c_double), P]),
 }
 
 _lib = None

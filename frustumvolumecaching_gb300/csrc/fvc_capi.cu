@@ -267,6 +267,7 @@ struct fvc_model {
     DevScene dscene{};
     DevGrid grid{};
     int latent_offset = 1, n_latents = 8, head_hidden = 2;
+    std::vector<uint16_t> h_base, h_head;  /* fp16 weight blobs in the model file layouts */
     uint8_t *d_bits = nullptr;
     __half2 *d_table = nullptr;
     uint2 *d_weights = nullptr;
@@ -351,6 +352,9 @@ struct fvc_renderer {
     int *d_wf_counters = nullptr;
     int row_capacity = 0;
     int last_iterations = 0;
+    float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
+    int *d_grad_rows = nullptr;       /* rows with a gradient (plain renderers have no res_list) */
+    int bwd_capacity = 0;
     LaunchLog log;                    /* kernel accounting of the last render */
     std::vector<cudaEvent_t> events;  /* 2 x 4096 when kernel timing is on */
     void release_wavefront()
@@ -370,6 +374,7 @@ struct fvc_renderer {
     {
         if (stream) cudaStreamSynchronize(stream);
         dfree(d_ctl); dfree(d_stats); dfree(d_results); dfree(d_image); dfree(d_counts);
+        dfree(d_row_dout); dfree(d_grad_rows);
         release_wavefront();
         bs.release();
         if (h_pinned) cudaFreeHost(h_pinned);
@@ -503,6 +508,8 @@ static int load_model(const std::string &dir, fvc_model &m)
         memcpy(o.data(), v.data() + off_h * 2, n * 2);
         return o;
     };
+    m.h_base = u16(wb, 0, wb.size() / 2);
+    m.h_head = u16(wh, 0, wh.size() / 2);
     std::vector<uint2> W(W_TOTAL, make_uint2(0, 0));
     frag_pack(u16(wb, 0, 64 * 32), 64, 32, &W[W_L1]);
     {
@@ -740,11 +747,11 @@ static int check_info(const fvc_raymarch_info *info)
     return FVC_OK;
 }
 
-static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts)
+static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts,
+                               RenderParams &p)
 {
     fvc_model *m = r->m;
     const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
-    RenderParams p;
     memset(&p, 0, sizeof(p));
     p.scene = m->dscene;
     p.steps = dev_steps(info->stepsize_info);
@@ -781,13 +788,28 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
     p.counters = r->d_wf_counters;
     p.row_capacity = r->row_capacity;
     p.steps_per_iter = 64;
-    CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
-    CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
-    CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));
+    return FVC_OK;
+}
+
+static void reset_launch_log(fvc_renderer *r)
+{
     r->log.launches = 0;
     r->log.n_timed = r->log.n_untimed = 0;
     r->log.ev = r->events.empty() ? nullptr : r->events.data();
     r->log.cap = (int)r->events.size() / 2;
+}
+
+static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts)
+{
+    fvc_model *m = r->m;
+    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    RenderParams p;
+    int rc;
+    if ((rc = setup_render_params(r, info, results, image, counts, p))) return rc;
+    CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
+    CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
+    CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));
+    reset_launch_log(r);
     CU(render_frame(p, cached, m->head_hidden, m->n_sms, r->stream, r->h_pinned + 8, 4, &r->last_iterations, &r->log));
     return FVC_OK;
 }
@@ -1137,5 +1159,179 @@ extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
 {
     CHECK_ARG(r && (use_tcgen05 == 0 || use_tcgen05 == 1), "fvc_renderer_set_network_path: bad arguments");
     r->use_tc = use_tcgen05;
+    return FVC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* differentiable render                                                     */
+/* ------------------------------------------------------------------------ */
+struct fvc_grad {
+    fvc_model *m = nullptr;
+    size_t n_table = 0, n_base = 0, n_head = 0;
+    float *d_table = nullptr, *d_base = nullptr, *d_head = nullptr; /* dL/dparam, accumulated */
+    float *s_table = nullptr, *s_base = nullptr, *s_head = nullptr; /* loss-scaled, one call */
+    uint2 *d_w = nullptr;                                           /* BW_TOTAL weight packs */
+    float4 *d_ray_grad = nullptr;
+    int ray_cap = 0;
+    double *d_loss = nullptr;
+    ~fvc_grad()
+    {
+        dfree(d_table); dfree(d_base); dfree(d_head); dfree(s_table); dfree(s_base); dfree(s_head);
+        dfree(d_w); dfree(d_ray_grad); dfree(d_loss);
+    }
+};
+
+static constexpr float FVC_LOSS_SCALE = 1024.0f;
+
+extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
+{
+    CHECK_ARG(m && out, "fvc_grad_create: null argument");
+    *out = nullptr;
+    if (m->n_latents != 8 || m->grid.n_levels != 16)
+        return fail(FVC_ERR_CONFIG, "the backward kernels are built for 16 hash levels and 8 latents");
+    auto g = std::make_unique<fvc_grad>();
+    g->m = m;
+    g->n_table = m->table_entries * 2;
+    g->n_base = m->h_base.size();
+    g->n_head = m->h_head.size();
+    int rc;
+    if ((rc = dalloc(&g->d_table, g->n_table, "table gradient"))) return rc;
+    if ((rc = dalloc(&g->s_table, g->n_table, "table gradient"))) return rc;
+    if ((rc = dalloc(&g->d_base, g->n_base, "base gradient"))) return rc;
+    if ((rc = dalloc(&g->s_base, g->n_base, "base gradient"))) return rc;
+    if ((rc = dalloc(&g->d_head, g->n_head, "head gradient"))) return rc;
+    if ((rc = dalloc(&g->s_head, g->n_head, "head gradient"))) return rc;
+    if ((rc = dalloc(&g->d_loss, (size_t)1, "loss"))) return rc;
+    CU(cudaMemset(g->d_table, 0, g->n_table * 4)); CU(cudaMemset(g->s_table, 0, g->n_table * 4));
+    CU(cudaMemset(g->d_base, 0, g->n_base * 4)); CU(cudaMemset(g->s_base, 0, g->n_base * 4));
+    CU(cudaMemset(g->d_head, 0, g->n_head * 4)); CU(cudaMemset(g->s_head, 0, g->n_head * 4));
+    /* forward (B = W^T) and input-gradient (B = W) fragment packs of each layer */
+    auto slice = [](const std::vector<uint16_t> &v, size_t off, size_t n) {
+        return std::vector<uint16_t>(v.begin() + off, v.begin() + off + n);
+    };
+    auto transpose = [](const std::vector<uint16_t> &W, int R, int Cc) {
+        std::vector<uint16_t> T((size_t)R * Cc);
+        for (int i = 0; i < R; ++i)
+            for (int j = 0; j < Cc; ++j) T[(size_t)j * R + i] = W[(size_t)i * Cc + j];
+        return T;
+    };
+    const std::vector<uint16_t> W1 = slice(m->h_base, 0, 64 * 32), W2 = slice(m->h_base, 64 * 32, 16 * 64);
+    const std::vector<uint16_t> W3 = slice(m->h_head, 0, 64 * 32);
+    const size_t w5 = m->head_hidden == 2 ? 64 * 32 + 64 * 64 : 64 * 32;
+    const std::vector<uint16_t> W5 = slice(m->h_head, w5, 16 * 64);
+    std::vector<uint2> P(BW_TOTAL, make_uint2(0, 0));
+    frag_pack(W1, 64, 32, &P[BW_F1]);
+    frag_pack(W2, 16, 64, &P[BW_F2]);
+    frag_pack(W3, 64, 32, &P[BW_F3]);
+    frag_pack(W5, 16, 64, &P[BW_F5]);
+    frag_pack(transpose(W5, 16, 64), 64, 16, &P[BW_B5]);
+    frag_pack(transpose(W3, 64, 32), 32, 64, &P[BW_B3]);
+    frag_pack(transpose(W2, 16, 64), 64, 16, &P[BW_B2]);
+    frag_pack(transpose(W1, 64, 32), 32, 64, &P[BW_B1]);
+    if (m->head_hidden == 2) {
+        const std::vector<uint16_t> W4 = slice(m->h_head, 64 * 32, 64 * 64);
+        frag_pack(W4, 64, 64, &P[BW_F4]);
+        frag_pack(transpose(W4, 64, 64), 64, 64, &P[BW_B4]);
+    }
+    if ((rc = dalloc(&g->d_w, P.size(), "backward weights"))) return rc;
+    CU(cudaMemcpy(g->d_w, P.data(), P.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    *out = g.release();
+    return FVC_OK;
+}
+
+extern "C" void fvc_grad_destroy(fvc_grad *g) { delete g; }
+
+extern "C" int fvc_grad_zero(fvc_grad *g)
+{
+    CHECK_ARG(g, "fvc_grad_zero: null argument");
+    CU(cudaMemset(g->d_table, 0, g->n_table * 4));
+    CU(cudaMemset(g->d_base, 0, g->n_base * 4));
+    CU(cudaMemset(g->d_head, 0, g->n_head * 4));
+    return FVC_OK;
+}
+
+extern "C" int fvc_grad_sizes(const fvc_grad *g, size_t *n_table, size_t *n_base, size_t *n_head)
+{
+    CHECK_ARG(g, "fvc_grad_sizes: null argument");
+    if (n_table) *n_table = g->n_table;
+    if (n_base) *n_base = g->n_base;
+    if (n_head) *n_head = g->n_head;
+    return FVC_OK;
+}
+
+extern "C" int fvc_grad_read(fvc_grad *g, float *table, float *base, float *head)
+{
+    CHECK_ARG(g, "fvc_grad_read: null argument");
+    if (table) CU(cudaMemcpy(table, g->d_table, g->n_table * 4, cudaMemcpyDeviceToHost));
+    if (base) CU(cudaMemcpy(base, g->d_base, g->n_base * 4, cudaMemcpyDeviceToHost));
+    if (head) CU(cudaMemcpy(head, g->d_head, g->n_head * 4, cudaMemcpyDeviceToHost));
+    return FVC_OK;
+}
+
+extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_raymarch_info *info, const int32_t *pixels,
+                                   int n_rays, const float *target, double *loss_out, float *pred)
+{
+    CHECK_ARG(r && g && info && pixels && target && n_rays > 0, "fvc_render_backward: bad arguments");
+    CHECK_ARG(g->m == r->m, "fvc_render_backward: gradients belong to another model");
+    if (r->kind == FVC_RENDERER_CACHE_PERFORMANCE)
+        return fail(FVC_ERR_CONFIG, "fvc_render_backward: the differentiable render is built for the plain renderers");
+    int rc;
+    if ((rc = check_info(info))) return rc;
+    const long long n_pix = (long long)info->cam_info.resolution.x * info->cam_info.resolution.y;
+    CHECK_ARG(n_rays <= n_pix, "fvc_render_backward: more rays than pixels");
+    if ((rc = fvc_renderer_resize(r, info->cam_info.resolution.x, info->cam_info.resolution.y))) return rc;
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    fvc_model *m = r->m;
+    cudaStream_t s = r->stream;
+    if (r->bwd_capacity != r->row_capacity) {
+        dfree(r->d_row_dout); dfree(r->d_grad_rows);
+        if ((rc = dalloc(&r->d_row_dout, (size_t)r->row_capacity, "row gradients"))) return rc;
+        if ((rc = dalloc(&r->d_grad_rows, (size_t)r->row_capacity, "gradient rows"))) return rc;
+        r->bwd_capacity = r->row_capacity;
+    }
+    if (g->ray_cap < n_rays) {
+        dfree(g->d_ray_grad);
+        if ((rc = dalloc(&g->d_ray_grad, (size_t)n_rays, "ray gradients"))) return rc;
+        g->ray_cap = n_rays;
+    }
+    RenderParams p;
+    if ((rc = setup_render_params(r, info, r->d_results, nullptr, nullptr, p))) return rc;
+    p.pixel_list = pixels;
+    p.n_list = n_rays;
+    p.ray_grad = g->d_ray_grad;
+    p.row_dout = r->d_row_dout;
+    p.res_list = r->d_grad_rows;
+    BwdParams b;
+    b.w = g->d_w;
+    b.g_table = g->s_table; b.g_base = g->s_base; b.g_head = g->s_head;
+    b.head_w5 = m->head_hidden == 2 ? GH_W4 + 64 * 64 : GH_W4;
+    b.loss = g->d_loss;
+    b.target = target;
+    b.loss_scale = FVC_LOSS_SCALE;
+    reset_launch_log(r);
+    /* pass 1: forward render of the listed pixels into d_results */
+    CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), s));
+    CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), s));
+    CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), s));
+    CU(render_frame(p, false, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->last_iterations, &r->log));
+    /* loss and per-ray dL/dC */
+    CU(cudaMemsetAsync(g->d_loss, 0, sizeof(double), s));
+    CU(launch_loss(p, b, s));
+    /* pass 2: re-march, compositing adjoint, network adjoint */
+    CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), s));
+    CU(backward_frame(p, b, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->log));
+    const float inv = 1.0f / (FVC_LOSS_SCALE * (float)n_rays);
+    CU(launch_grad_finalize(g->s_table, g->d_table, g->n_table, inv, m->n_sms, s));
+    CU(launch_grad_finalize(g->s_base, g->d_base, g->n_base, inv, m->n_sms, s));
+    CU(launch_grad_finalize(g->s_head, g->d_head, g->n_head, inv, m->n_sms, s));
+    r->log.launches += 4;
+    if (pred) CU(cudaMemcpyAsync(pred, r->d_results, (size_t)n_rays * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    double loss = 0.0;
+    CU(cudaMemcpyAsync(&loss, g->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    int guard = 0;
+    CU(cudaMemcpy(&guard, r->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (guard) return fail(FVC_ERR_GUARD, "render guard fired: flags " + std::to_string(guard));
+    if (loss_out) *loss_out = loss / (double)n_rays;
     return FVC_OK;
 }

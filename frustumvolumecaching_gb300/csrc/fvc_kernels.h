@@ -88,7 +88,44 @@ struct RenderParams {
     int *counters;              /* [0], [1] alive rays (ping-pong), [2] rows, [3] resample, [4] cache */
     int row_capacity;           /* rows per sub-iteration */
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
+    /* differentiable render */
+    const int *pixel_list;      /* rays for these pixels (y * W + x) instead of the full image; ray id = list index */
+    int n_list;
+    const float4 *ray_grad;     /* per ray: dL/dC (loss-scaled) and X_total = g.C + g_T T */
+    float4 *row_dout;           /* per row: dL/d rgb logits, dL/d log-density (loss-scaled) */
 };
+
+/* Weights of the backward kernel: fragment packs (mma.sync m16n8k16 B
+ * operands, frag_pack order) of each layer W (out x in) for the forward
+ * recomputation (B[k][n] = W[n][k]) and for the input gradients
+ * (B[k][n] = W[k][n]); head layer 1 in the model's input order
+ * [latents | SH | 1-padding]. */
+constexpr int BW_F1 = 0;                   /* W1 64 x 32 : 8 ntiles x 2 ksteps */
+constexpr int BW_F2 = BW_F1 + 8 * 2 * 32;  /* W2 16 x 64 : 2 x 4 */
+constexpr int BW_F3 = BW_F2 + 2 * 4 * 32;  /* W3 64 x 32 : 8 x 2 */
+constexpr int BW_F4 = BW_F3 + 8 * 2 * 32;  /* W4 64 x 64 : 8 x 4 */
+constexpr int BW_F5 = BW_F4 + 8 * 4 * 32;  /* W5 16 x 64 : 2 x 4 */
+constexpr int BW_B5 = BW_F5 + 2 * 4 * 32;  /* W5^T pack: N = 64, K = 16 : 8 x 1 */
+constexpr int BW_B4 = BW_B5 + 8 * 1 * 32;  /* W4: N = 64, K = 64 : 8 x 4 */
+constexpr int BW_B3 = BW_B4 + 8 * 4 * 32;  /* W3: N = 32, K = 64 : 4 x 4 */
+constexpr int BW_B2 = BW_B3 + 4 * 4 * 32;  /* W2: N = 64, K = 16 : 8 x 1 */
+constexpr int BW_B1 = BW_B2 + 8 * 1 * 32;  /* W1: N = 32, K = 64 : 4 x 4 */
+constexpr int BW_TOTAL = BW_B1 + 4 * 4 * 32;
+/* gradient blob offsets (floats): the model file layouts */
+constexpr int GB_W1 = 0, GB_W2 = 64 * 32, GB_BASE = GB_W2 + 16 * 64;
+constexpr int GH_W3 = 0, GH_W4 = 64 * 32;
+
+struct BwdParams {
+    const uint2 *w;             /* BW_TOTAL fragment entries */
+    float *g_table;             /* [entries][2] fp32 */
+    float *g_base;              /* GB_BASE floats */
+    float *g_head;              /* head blob floats */
+    int head_w5;                /* offset of W5 in the head blob */
+    double *loss;               /* sum of squared pixel errors (device) */
+    const float *target;        /* [n_list][3] */
+    float loss_scale;           /* gradients carry this factor until read out */
+};
+
 
 struct InferenceParams {
     DevGrid grid;
@@ -156,6 +193,13 @@ struct LaunchLog {
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
                          int check_every, int *n_iterations, LaunchLog *log = nullptr);
+
+/* differentiable render (fvc_backward.cu): pass 1 is render_frame over p.pixel_list */
+cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, int head_hidden, int n_sms, cudaStream_t s,
+                           int *h_pinned, int check_every, LaunchLog *log = nullptr);
+cudaError_t launch_loss(const RenderParams &p, const BwdParams &b, cudaStream_t s);
+cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int head_hidden, int it, int n_sms, cudaStream_t s);
+cudaError_t launch_grad_finalize(float *scratch, float *out, size_t n, float inv_scale, int n_sms, cudaStream_t s);
 cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
 
 __global__ void cache_init_kernel(CacheBuildParams p);

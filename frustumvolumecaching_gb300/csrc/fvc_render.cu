@@ -132,6 +132,37 @@ __global__ void __launch_bounds__(256) wf_raygen_kernel(RenderParams p)
     }
 }
 
+/* rays for a list of pixels (differentiable render): ray id = list index,
+ * results[id] is written for rays that miss the scene box */
+__global__ void __launch_bounds__(256) wf_raygen_list_kernel(RenderParams p)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = p.cam.W, H = p.cam.H;
+    const int pix = i < p.n_list ? p.pixel_list[i] : -1;
+    const bool valid = pix >= 0 && pix < W * H;
+    bool hits = false;
+    float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
+    float tn = 0.f, tf = 0.f;
+    if (valid) {
+        generate_ray(p.cam, pix % W, pix / W, o, d);
+        hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
+    }
+    if (i < p.n_list && !hits) write_pixel(p, i, make_float4(0.f, 0.f, 0.f, 1.f), make_int4(0, 0, 0, 0));
+    const unsigned m = __ballot_sync(FULLMASK, hits);
+    int base = 0;
+    if (lane_id() == 0 && m) base = atomicAdd(p.counters + 0, __popc(m));
+    base = __shfl_sync(FULLMASK, base, 0);
+    if (hits) {
+        RayState st;
+        st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
+        st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
+        st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        st.cnt = make_int4(i, 0, 0, 0);
+        st.cnt2 = make_int4(0, 0, 0, 0);
+        p.states[0][base + __popc(m & lane_lt())] = st;
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* march                                                                     */
 /* ------------------------------------------------------------------------- */
@@ -716,6 +747,86 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
     }
 }
 
+/* Adjoint of front-to-back compositing for this sub-iteration's rows (plain
+ * path).  Per ray, in sample order, with g = dL/dC and X_total from the loss
+ * kernel, X_prefix in acc.x and T in acc.w of the ray state:
+ *   X_prefix += T alpha g.c;  T' = T (1 - alpha);
+ *   dL/dsigma = dt (T' g.c - (X_total - X_prefix));  dL/dc = T alpha g.
+ * The alpha threshold and the T < 1e-4 termination follow the forward
+ * compositing exactly, so the rows that composited get gradients and no
+ * other.  Rows with a gradient are listed in res_list (counters[3]). */
+__global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, int it)
+{
+    const int n_alive = p.counters[it & 1];
+    RayState *cur = p.states[it & 1], *nxt = p.states[(it + 1) & 1];
+    for (int base = blockIdx.x * blockDim.x; base < n_alive; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n_alive;
+        bool keep = false;
+        RayState st;
+        int n_grad = 0;
+        int2 rr = make_int2(0, 0);
+        uint32_t gmask = 0;
+        if (valid) {
+            st = cur[i];
+            rr = p.ray_rows[i];
+            const float4 rg = p.ray_grad[st.cnt.x];
+            float T = st.acc.w, xp = st.acc.x;
+            bool term = false;
+            for (int j = 0; j < rr.y; ++j) {
+                const int r = rr.x + j;
+                float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (!term) {
+                    const uint2 ov = p.row_out[r];
+                    const float t0 = p.row_t0[r];
+                    const float2 lg = __half22float2(*reinterpret_cast<const __half2 *>(&ov.x));
+                    const float lb = __half2float(__ushort_as_half((unsigned short)(ov.y & 0xffffu)));
+                    const float ld = __half2float(__ushort_as_half((unsigned short)(ov.y >> 16)));
+                    const float dt = calc_step(p.steps, t0);
+                    const float sigma = expf(ld);
+                    const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
+                    if (alpha > p.scene.alpha_thre) {
+                        const float c0 = 1.0f / (1.0f + expf(-lg.x)), c1 = 1.0f / (1.0f + expf(-lg.y)),
+                                    c2 = 1.0f / (1.0f + expf(-lb));
+                        const float gc = rg.x * c0 + rg.y * c1 + rg.z * c2;
+                        const float ta = T * alpha;
+                        xp += ta * gc;
+                        const float Tn = T * (1.0f - alpha);
+                        const float dsig = dt * (Tn * gc - (rg.w - xp));
+                        dout = make_float4(rg.x * ta * c0 * (1.0f - c0), rg.y * ta * c1 * (1.0f - c1), rg.z * ta * c2 * (1.0f - c2),
+                                           dsig * sigma);
+                        T = Tn;
+                        gmask |= 1u << j;
+                        ++n_grad;
+                    }
+                    if (T < 1e-4f) term = true;
+                }
+                p.row_dout[r] = dout;
+            }
+            st.acc.x = xp;
+            st.acc.w = T;
+            keep = !(term || st.cnt2.y);
+        }
+        /* list the rows with a gradient (one atomic per warp) */
+        int incl = n_grad;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULLMASK, incl, o);
+            if (lane_id() >= o) incl += v;
+        }
+        const int total = __shfl_sync(FULLMASK, incl, 31);
+        int lb = 0;
+        if (lane_id() == 0 && total) lb = atomicAdd(p.counters + 3, total);
+        lb = __shfl_sync(FULLMASK, lb, 0) + incl - n_grad;
+        for (uint32_t mm = gmask; mm; mm &= mm - 1) p.res_list[lb++] = rr.x + __ffs(mm) - 1;
+        const unsigned m = __ballot_sync(FULLMASK, keep);
+        int nb = 0;
+        if (lane_id() == 0 && m) nb = atomicAdd(p.counters + ((it + 1) & 1), __popc(m));
+        nb = __shfl_sync(FULLMASK, nb, 0);
+        if (keep) nxt[nb + __popc(m & lane_lt())] = st;
+    }
+}
+
 /* resets the row counters after the kernels of the sub-iteration consumed them */
 __global__ void wf_reset_rows_kernel(RenderParams p, int cached)
 {
@@ -767,7 +878,8 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     };
     const int W = p.cam.W, H = p.cam.H;
     const int n_threads = ((W + 7) / 8) * ((H + 3) / 4) * 32;
-    wf_raygen_kernel<<<(n_threads + 255) / 256, 256, 0, s>>>(p);
+    if (p.pixel_list) wf_raygen_list_kernel<<<(p.n_list + 255) / 256, 256, 0, s>>>(p);
+    else wf_raygen_kernel<<<(n_threads + 255) / 256, 256, 0, s>>>(p);
     ++L.launches;
     const int grid_ray = n_sms * 16;
     const int grid_net = n_sms * 2;
@@ -808,6 +920,55 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     }
     if (n_iter) *n_iter = it;
     return cudaGetLastError();
+}
+
+/* Pass 2 of the differentiable render (pass 1 is run_frame over the pixel
+ * list, then the loss kernel): the same march and network forward per
+ * sub-iteration, then the compositing adjoint and the network adjoint. */
+template <int HH>
+static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n_sms, cudaStream_t s, int *h_pinned,
+                                int check_every, LaunchLog *log)
+{
+    static bool attrs_set = false;
+    if (!attrs_set) {
+        cudaError_t e = set_net_attrs<HH>();
+        if (e != cudaSuccess) return e;
+        attrs_set = true;
+    }
+    LaunchLog local;
+    LaunchLog &L = log ? *log : local;
+    wf_raygen_list_kernel<<<(p.n_list + 255) / 256, 256, 0, s>>>(p);
+    ++L.launches;
+    const int grid_ray = n_sms * 16;
+    const int grid_net = n_sms * 2;
+    const size_t net_smem = sizeof(NetSmem);
+    const size_t tc_smem = sizeof(TcSmem);
+    const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
+    for (int it = 0; it < (1 << 20); ++it) {
+        wf_march_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
+        if (p.use_tc) wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
+        else wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+        wf_composite_bwd_kernel<<<grid_ray, 128, 0, s>>>(p, it);
+        cudaError_t e = launch_net_backward(p, b, HH, it, n_sms, s);
+        if (e != cudaSuccess) return e;
+        wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, 0);
+        L.launches += 5;
+        if ((it + 1) % check_every == 0) {
+            e = cudaMemcpyAsync(h_pinned, p.counters + ((it + 1) & 1), sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) return e;
+            e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            if (*h_pinned == 0) break;
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, int head_hidden, int n_sms, cudaStream_t s,
+                           int *h_pinned, int check_every, LaunchLog *log)
+{
+    return head_hidden == 2 ? run_backward<2>(p, b, n_sms, s, h_pinned, check_every, log)
+                            : run_backward<1>(p, b, n_sms, s, h_pinned, check_every, log);
 }
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,

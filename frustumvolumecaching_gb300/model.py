@@ -198,6 +198,14 @@ def spec_config2() -> ModelSpec:
                      contraction="linf", cone_angle=1.0 / 256.0, stepsize=math.sqrt(3.0) / 1024.0, log2_T=19)
 
 
+def spec_config5(target: bool = False) -> ModelSpec:
+    """Differentiable-render workload: the config-1 architecture and scene box
+    with 2^19 entries/level; the target image comes from a second network of
+    the same architecture seeded differently."""
+    return ModelSpec(name="c5_target" if target else "c5_train", seed=1105 if target else 1005,
+                     aabb=[-1.5, -1.5, -1.5, 1.5, 1.5, 1.5], log2_T=19)
+
+
 def spec_tiny(seed: int = 7, nlvl: int = 1, cone: float = 0.0, log2_T: int = 12) -> ModelSpec:
     """Small model for fast CPU tests (tables 2^12, 16 levels)."""
     if nlvl == 1:

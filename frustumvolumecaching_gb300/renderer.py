@@ -172,6 +172,16 @@ class Renderer:
         out.image_rgba8, out.results, out.ray_counts = L.ptr(image), L.ptr(results), L.ptr(ray_counts)
         L.check(L.load().fvc_render_device(self.handle, C.byref(rm_info), C.byref(out)))
 
+    def render_backward(self, rm_info: L.RaymarchInfo, pixels, target, grads: "Gradients", pred=None, n_rays=None) -> float:
+        """Forward + adjoint of the plain render at device `pixels` (int32 y*W+x)
+        against device `target` [n,3]: adds dL/dparam to `grads`, returns the
+        mean squared error L; `pred` (device [n,4]) receives (C, T)."""
+        n = int(n_rays if n_rays is not None else pixels.numel())
+        loss = C.c_double()
+        L.check(L.load().fvc_render_backward(self.handle, grads.handle, C.byref(rm_info), L.ptr(pixels), n, L.ptr(target),
+                                             C.byref(loss), L.ptr(pred)))
+        return loss.value
+
     @property
     def _render_stats(self) -> L.RenderStats:
         s = L.RenderStats()
@@ -192,6 +202,34 @@ class BasicRenderer(Renderer):
 class PerformanceRenderer(Renderer):
     """PerformanceRenderer, include/performance_renderer.h:19-64."""
     kind = RENDERER_PERFORMANCE
+
+
+class Gradients:
+    """fp32 gradients of a model's parameters in the model file layouts:
+    hash table [entries, 2], density-MLP blob, color-head blob (fvc_grad)."""
+
+    def __init__(self, nerf_network: NerfNetwork):
+        lib = L.load()
+        h = C.c_void_p()
+        L.check(lib.fvc_grad_create(nerf_network.handle, C.byref(h)))
+        self.handle = h
+        self._net = nerf_network
+        a, b, c = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        L.check(lib.fvc_grad_sizes(h, C.byref(a), C.byref(b), C.byref(c)))
+        self.sizes = (a.value, b.value, c.value)
+
+    def zero(self) -> None:
+        L.check(L.load().fvc_grad_zero(self.handle))
+
+    def read(self):
+        t, b, h = (np.zeros(n, np.float32) for n in self.sizes)
+        L.check(L.load().fvc_grad_read(self.handle, L.ptr(t), L.ptr(b), L.ptr(h)))
+        return t, b, h
+
+    def __del__(self):
+        if getattr(self, "handle", None) and L._lib is not None:
+            L._lib.fvc_grad_destroy(self.handle)
+            self.handle = None
 
 
 class Cache:
@@ -269,6 +307,6 @@ def default_cache_settings() -> L.CacheSettings:
     return s
 
 
-__all__ = ["load_data", "LoaderData", "NerfNetwork", "Renderer", "BasicRenderer", "PerformanceRenderer", "Cache",
+__all__ = ["load_data", "LoaderData", "NerfNetwork", "Renderer", "BasicRenderer", "PerformanceRenderer", "Cache", "Gradients",
            "CachePerformanceRenderer", "RenderBuffer", "raymarch_info", "camera_info", "camera_dict",
            "default_cache_settings"]

@@ -314,6 +314,33 @@ int fvc_cache_read(fvc_cache *c, int32_t *packed_index, size_t *packed_index_n,
 /* Frustum dims (W, H, D), brick dims and data bricks per dim. */
 int fvc_cache_dims(fvc_cache *c, fvc_int3 *frustum_dims, fvc_int3 *brick_dims, fvc_int3 *data_bricks_per_dim);
 
+/* ------------------------------------------------------------------------ */
+/* differentiable render (no counterpart in the reference)                   */
+/* ------------------------------------------------------------------------ */
+
+/* Gradients of a model's parameters in fp32, in the model file layouts:
+ * hash table [entries x 2] (pos_enc.dat), density MLP blob (mlp_base.dat),
+ * color head blob (mlp_head.dat).  Gradients accumulate across
+ * fvc_render_backward calls until fvc_grad_zero. */
+typedef struct fvc_grad fvc_grad;
+int fvc_grad_create(fvc_model *m, fvc_grad **out);
+void fvc_grad_destroy(fvc_grad *g);
+int fvc_grad_zero(fvc_grad *g);
+int fvc_grad_sizes(const fvc_grad *g, size_t *n_table, size_t *n_base, size_t *n_head);
+/* copies the accumulated gradients to host arrays (any may be null) */
+int fvc_grad_read(fvc_grad *g, float *table, float *base, float *head);
+
+/* Forward and adjoint of the plain render (renderer kinds BASIC/PERFORMANCE)
+ * at n_rays pixels (device int32 y * W + x, at most W * H of the camera):
+ * L = mean over the rays of sum_k (C_k + T - target_k)^2, the
+ * white-background pixel of writeImageBuffer_performance_kernel
+ * (src/performance_renderer.cu:127-149) against device target [n_rays x 3].
+ * Adds dL/dparam to g, writes L to *loss_out and, if pred is non-null, the
+ * forward (C, T) per ray to device pred [n_rays x 4].  The forward is
+ * recomputed per sub-iteration instead of stored.  Synchronous. */
+int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_raymarch_info *info, const int32_t *pixels, int n_rays,
+                        const float *target, double *loss_out, float *pred);
+
 #ifdef __cplusplus
 }
 #endif
