@@ -168,6 +168,63 @@ def cpu_baseline_port(args) -> dict:
 
 
 # --------------------------------------------------------------------------
+# precision sweep (config 1 path and scene)
+# --------------------------------------------------------------------------
+PREC_RES = (256, 256)
+PREC_FRAMES = 20
+PREC_ROWS = (120, 136)  # image rows compared with the float64 oracle
+
+
+def run_precision_bench(args, torch, dev, stream) -> dict:
+    """Plain 256x256 render of the config-1 scene with FP16, BF16 and FP8-E4M3
+    MLPs (tcgen05, fp32 accumulation, Kahan compositing): frames/s and the
+    error of the white-background image against the float64 oracle."""
+    import frustumvolumecaching_gb300 as fvc
+    from frustumvolumecaching_gb300 import camera as fcam
+    from frustumvolumecaching_gb300 import model as fmodel
+    from oracle import oracle as orc
+
+    spec = fmodel.spec_config1()
+    d = fmodel.ensure_model(spec)
+    loader = fvc.load_data(d)
+    W, H = PREC_RES
+    cam = fcam.seeded_camera(spec.seed, width=W, height=H)
+    info = fvc.raymarch_info(cam, loader.stepsize_info)
+    r0, r1 = PREC_ROWS
+    ref, _, _ = orc.OracleModel(d).render_plain(cam, rows=(r0, r1), threads=orc.default_threads())
+    ref_img = (ref[..., :3] + ref[..., 3:4])[r0:r1]
+    r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    r.set_stream(stream.cuda_stream)
+    r.resizeRenderbuffers(PREC_RES)
+    res = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    out = {}
+    for prec, name in ((0, "fp16"), (1, "bf16"), (2, "fp8_e4m3")):
+        r.set_precision(prec)
+        for _ in range(args.warmup):
+            r.render_device(info, results=res)
+        torch.cuda.synchronize(dev)
+        times = []
+        for _ in range(args.steps):
+            a, b = ev(), ev()
+            a.record(stream)
+            for _ in range(PREC_FRAMES):
+                r.render_device(info, results=res)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(a.elapsed_time(b) / PREC_FRAMES)
+        img = res.cpu().numpy()
+        img = (img[..., :3] + img[..., 3:4])[r0:r1]
+        mse = float(np.mean((img.astype(np.float64) - ref_img) ** 2))
+        ms = sum(times) / len(times)
+        out[name] = {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "max_abs": float(np.abs(img - ref_img).max()),
+                     "psnr_db": (10.0 * math.log10(1.0 / mse)) if mse > 0 else None}
+    r.set_precision(0)
+    return {"workload": "c1 plain 256x256 (1 cascade, 2^16 entries/level), tcgen05 MLPs",
+            "error_rows": f"rows {r0}-{r1 - 1} against the float64 oracle", "per_precision": out}
+
+
+# --------------------------------------------------------------------------
 # differentiable render (backward Mrays/s)
 # --------------------------------------------------------------------------
 BWD_RAYS = 1 << 18
@@ -398,6 +455,7 @@ def run_fvc(args) -> dict | None:
     cached.set_kernel_timing(False)
 
     backward = run_backward_bench(args, torch, dev, stream)
+    precision = run_precision_bench(args, torch, dev, stream)
 
     # e2e: the cached path through the host-buffer C-ABI call (D2H of every frame)
     hbuf = fvc.RenderBuffer(RES)
@@ -471,6 +529,7 @@ def run_fvc(args) -> dict | None:
         "e2e": {"value": fps_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": n_frames * W * H * (4 + 16 + 16)},
         "backward": backward,
+        "precision": precision,
         "gpu_launches": log["launches"] // max(1, args.steps),
         "gpu_launches_plain_path": log["plain_launches"] // max(1, args.steps),
         "clocks": clk,

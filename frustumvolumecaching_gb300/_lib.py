@@ -136,6 +136,7 @@ SIGNATURES = {
     "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
+    "fvc_renderer_set_precision": (c_int, [P, c_int]),
     "fvc_model_properties": (c_int, [P, C.POINTER(ModelProps)]),
     "fvc_renderer_synchronize": (c_int, [P]),
     "fvc_grad_create": (c_int, [P, PP]),

@@ -9,6 +9,8 @@
  * records a thread-local message.
  */
 #include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -272,11 +274,14 @@ struct fvc_model {
     __half2 *d_table = nullptr;
     uint2 *d_weights = nullptr;
     uint8_t *d_weights_tc = nullptr;
+    uint8_t *d_weights_tc_bf16 = nullptr, *d_weights_tc_fp8 = nullptr;
+    float *d_fp8_iw = nullptr;
     float *d_bias3 = nullptr;
     size_t table_entries = 0;
     ~fvc_model()
     {
         dfree(d_bits); dfree(d_table); dfree(d_weights); dfree(d_weights_tc); dfree(d_bias3);
+        dfree(d_weights_tc_bf16); dfree(d_weights_tc_fp8); dfree(d_fp8_iw);
     }
 };
 
@@ -368,6 +373,7 @@ struct fvc_renderer {
     int render_mode = 0;
     int max_samples = 0;
     int use_tc = 1;                   /* network kernels on tcgen05 (1) or mma.sync (0) */
+    int precision = FVC_PRECISION_FP16;
     BuildScratch bs;
     std::mutex read_mutex, write_mutex;
     ~fvc_renderer()
@@ -553,6 +559,40 @@ static int load_model(const std::string &dir, fvc_model &m)
     tc_pack(l3, 64, 32, TC_B3);
     if (m.head_hidden == 2) tc_pack(u16(wh, 64 * 32, 64 * 64), 64, 64, TC_B4);
     tc_pack(u16(wh, ho, 16 * 64), 16, 64, TC_B5);
+
+    /* reduced-precision copies: bf16 tiles (same layout) and e4m3 tiles
+     * (8-bit K-major layout), each e4m3 layer scaled by 448 / amax(W) */
+    {
+        std::vector<uint8_t> Wb(TC_WBYTES, 0), W8(TC8_WBYTES, 0);
+        float iw[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
+        auto pack_low = [&](const std::vector<uint16_t> &M, int N, int K, int off16, int off8, int layer) {
+            float amax = 0.f;
+            for (uint16_t h : M) amax = std::max(amax, std::fabs(h2f(h)));
+            const float sc = amax > 0.f ? 448.0f / amax : 1.0f;
+            iw[layer] = 1.0f / sc;
+            for (int n = 0; n < N; ++n)
+                for (int k = 0; k < K; ++k) {
+                    const float v = h2f(M[(size_t)n * K + k]);
+                    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+                    memcpy(&Wb[off16 + kmajor_offset(n, k, K)], &b, 2);
+                    W8[off8 + kmajor_offset8(n, k, K)] = (uint8_t)__nv_cvt_float_to_fp8(v * sc, __NV_SATFINITE, __NV_E4M3);
+                }
+        };
+        pack_low(u16(wb, 0, 64 * 32), 64, 32, TC_B1, TC8_B1, 0);
+        std::vector<uint16_t> w2 = u16(wb, 64 * 32, (size_t)base_out_pad * 64);
+        w2.resize(16 * 64, 0);
+        pack_low(w2, 16, 64, TC_B2, TC8_B2, 1);
+        pack_low(l3, 64, 32, TC_B3, TC8_B3, 2);
+        if (m.head_hidden == 2) pack_low(u16(wh, 64 * 32, 64 * 64), 64, 64, TC_B4, TC8_B4, 3);
+        pack_low(u16(wh, ho, 16 * 64), 16, 64, TC_B5, TC8_B5, 4);
+        int rc;
+        if ((rc = dalloc(&m.d_weights_tc_bf16, (size_t)TC_WBYTES, "bf16 weights"))) return rc;
+        if ((rc = dalloc(&m.d_weights_tc_fp8, (size_t)TC8_WBYTES, "fp8 weights"))) return rc;
+        if ((rc = dalloc(&m.d_fp8_iw, (size_t)8, "fp8 scales"))) return rc;
+        CU(cudaMemcpy(m.d_weights_tc_bf16, Wb.data(), TC_WBYTES, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.d_weights_tc_fp8, W8.data(), TC8_WBYTES, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.d_fp8_iw, iw, sizeof(iw), cudaMemcpyHostToDevice));
+    }
 
     /* device scene block */
     DevScene &d = m.dscene;
@@ -760,6 +800,12 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.bias3 = m->d_bias3;
     p.weights_tc = m->d_weights_tc;
     p.use_tc = r->use_tc;
+    p.precision = r->precision;
+    p.weights_tc_bf16 = m->d_weights_tc_bf16;
+    p.weights_tc_fp8 = m->d_weights_tc_fp8;
+    p.tc_fp8_iw = m->d_fp8_iw;
+    if (r->precision != FVC_PRECISION_FP16 && (cached || !r->use_tc))
+        return fail(FVC_ERR_CONFIG, "BF16 and FP8 MLPs are built for the plain renderers on the tcgen05 network path");
     p.latent_offset = m->latent_offset;
     p.ray_counter = r->d_ctl; p.guard = r->d_ctl + 1; p.stats = r->d_stats;
     p.results = results; p.image = image; p.ray_counts = counts;
@@ -1275,6 +1321,8 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     CHECK_ARG(g->m == r->m, "fvc_render_backward: gradients belong to another model");
     if (r->kind == FVC_RENDERER_CACHE_PERFORMANCE)
         return fail(FVC_ERR_CONFIG, "fvc_render_backward: the differentiable render is built for the plain renderers");
+    if (r->precision != FVC_PRECISION_FP16)
+        return fail(FVC_ERR_CONFIG, "fvc_render_backward: the network adjoint is built for FP16 MLPs");
     int rc;
     if ((rc = check_info(info))) return rc;
     const long long n_pix = (long long)info->cam_info.resolution.x * info->cam_info.resolution.y;
@@ -1333,5 +1381,12 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     CU(cudaMemcpy(&guard, r->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost));
     if (guard) return fail(FVC_ERR_GUARD, "render guard fired: flags " + std::to_string(guard));
     if (loss_out) *loss_out = loss / (double)n_rays;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_precision(fvc_renderer *r, int precision)
+{
+    CHECK_ARG(r && precision >= FVC_PRECISION_FP16 && precision <= FVC_PRECISION_FP8_E4M3, "fvc_renderer_set_precision: bad arguments");
+    r->precision = precision;
     return FVC_OK;
 }

@@ -29,6 +29,8 @@ constexpr int TC_B3 = 6144;     /* 64 x 32 */
 constexpr int TC_B4 = 10240;    /* 64 x 64 */
 constexpr int TC_B5 = 18432;    /* 16 x 64 */
 constexpr int TC_WBYTES = 20480;
+/* the same in e4m3 (8-bit K-major tiles) for the FP8 network */
+constexpr int TC8_B1 = 0, TC8_B2 = 2048, TC8_B3 = 3072, TC8_B4 = 5120, TC8_B5 = 9216, TC8_WBYTES = 10240;
 
 /* voxel of the cache data array: density, isset, 2 pad words, 8 fp16 latents */
 struct __align__(16) Voxel {
@@ -36,11 +38,12 @@ struct __align__(16) Voxel {
     uint4 lat;
 };
 
-/* state of one alive ray between sub-iterations (80 bytes) */
+/* state of one alive ray between sub-iterations (96 bytes) */
 struct __align__(16) RayState {
     float4 of;    /* origin, far */
     float4 dt;    /* direction, t1 (start of the next step) */
     float4 acc;   /* rgb, transmittance */
+    float4 comp;  /* Kahan compensation of the rgb sums */
     int4 cnt;     /* pixel id, composited resample, composited cache, steps */
     int4 cnt2;    /* dropped, done flag, samples pushed, - */
 };
@@ -61,6 +64,10 @@ struct RenderParams {
     const float *bias3;         /* head layer-1 bias from the 1-padding */
     const uint8_t *weights_tc;  /* the same weights as canonical K-major tiles (tcgen05) */
     int use_tc;                 /* 1: tcgen05 network kernels, 0: mma.sync */
+    int precision;              /* plain-path MLP precision: 0 fp16, 1 bf16, 2 fp8-e4m3 (tcgen05 only) */
+    const uint8_t *weights_tc_bf16; /* the tcgen05 tiles in bf16 */
+    const uint8_t *weights_tc_fp8;  /* e4m3 tiles, each layer scaled by 448 / amax */
+    const float *tc_fp8_iw;     /* per layer amax / 448 (undoes the weight scale) */
     int latent_offset;
     int *ray_counter;
     int *guard;

@@ -27,6 +27,9 @@
  * Counts live in device memory, so no kernel needs a host round trip; the
  * host reads the alive count every few sub-iterations to stop the loop.
  */
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+
 #include "fvc_kernels.h"
 
 #include <cuda_fp16.h>
@@ -69,6 +72,15 @@ __device__ __forceinline__ int warp_alloc(int *ctr, int n)
     if (lane == 31) base = atomicAdd(ctr, total);
     base = __shfl_sync(FULLMASK, base, 31);
     return base + incl - n;
+}
+
+/* compensated (Kahan) summation: sum += v with the running error in c */
+__device__ __forceinline__ void kahan_add(float &sum, float &c, float v)
+{
+    const float y = __fsub_rn(v, c);
+    const float t = __fadd_rn(sum, y);
+    c = __fsub_rn(__fsub_rn(t, sum), y);
+    sum = t;
 }
 
 __device__ __forceinline__ void write_pixel(const RenderParams &p, int id, float4 acc, int4 counts)
@@ -126,6 +138,7 @@ __global__ void __launch_bounds__(256) wf_raygen_kernel(RenderParams p)
         st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
         st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
         st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
         st.cnt = make_int4(id, 0, 0, 0);
         st.cnt2 = make_int4(0, 0, 0, 0);
         p.states[0][base + __popc(m & lane_lt())] = st;
@@ -157,6 +170,7 @@ __global__ void __launch_bounds__(256) wf_raygen_list_kernel(RenderParams p)
         st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
         st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
         st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
         st.cnt = make_int4(i, 0, 0, 0);
         st.cnt2 = make_int4(0, 0, 0, 0);
         p.states[0][base + __popc(m & lane_lt())] = st;
@@ -364,7 +378,7 @@ __device__ __forceinline__ float3 dir01_of(const RayState *states, int slot)
 template <int HEAD_HIDDEN, bool LIST>
 __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(RenderParams p, int it)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
     const int n_rows = LIST ? p.counters[3] : p.counters[2];
     if (n_rows == 0) return;
@@ -457,7 +471,7 @@ __device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, int l
 template <int HEAD_HIDDEN>
 __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderParams p, int it)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
     const int n_rows = p.counters[4];
     if (n_rows == 0) return;
@@ -680,6 +694,210 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
 }
 
 /* ------------------------------------------------------------------------- */
+/* tcgen05 network kernel at reduced precision (plain path, resample rows)   */
+/* ------------------------------------------------------------------------- */
+/* PREC 1, BF16: kind::f16 with bf16 operands; hash features, SH and every
+ * layer output are rounded to bf16.
+ * PREC 2, FP8-E4M3: kind::f8f6f4 (K = 32 per MMA, the same 8-row x 16-byte
+ * core matrices).  Each weight matrix is stored scaled by 448 / amax(W) (per
+ * layer, on the host); each activation row is scaled by 448 / amax(row) before
+ * its e4m3 conversion.  The thread that owns a row divides both scales out of
+ * its fp32 accumulator row in the epilogue.
+ * Layer structure, TMEM use, waits and the guard are those of
+ * wf_net_tc_kernel; compositing stays fp32. */
+__device__ __forceinline__ uint32_t pack_bf2(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ uint32_t pack_e4m3x4(float a, float b, float c, float d)
+{
+    const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
+    const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(c, d), __NV_SATFINITE, __NV_E4M3);
+    return lo | (hi << 16);
+}
+
+/* writes this thread's row of K values into the operand tile in the kernel's
+ * precision; returns the factor that undoes the row's scale (1 for bf16) */
+template <int PREC, int K>
+__device__ __forceinline__ float put_row(uint8_t *tile, int row, const float *v)
+{
+    if (PREC == 1) {
+#pragma unroll
+        for (int c = 0; c < K / 8; ++c)
+            *reinterpret_cast<uint4 *>(tile + kmajor_offset(row, 8 * c, K)) =
+                make_uint4(pack_bf2(v[8 * c], v[8 * c + 1]), pack_bf2(v[8 * c + 2], v[8 * c + 3]),
+                           pack_bf2(v[8 * c + 4], v[8 * c + 5]), pack_bf2(v[8 * c + 6], v[8 * c + 7]));
+        return 1.0f;
+    } else {
+        float amax = 0.0f;
+#pragma unroll
+        for (int i = 0; i < K; ++i) amax = fmaxf(amax, fabsf(v[i]));
+        const float sc = amax > 0.0f ? 448.0f / amax : 1.0f;
+#pragma unroll
+        for (int c = 0; c < K / 16; ++c) {
+            const float *w = v + 16 * c;
+            *reinterpret_cast<uint4 *>(tile + kmajor_offset8(row, 16 * c, K)) =
+                make_uint4(pack_e4m3x4(w[0] * sc, w[1] * sc, w[2] * sc, w[3] * sc),
+                           pack_e4m3x4(w[4] * sc, w[5] * sc, w[6] * sc, w[7] * sc),
+                           pack_e4m3x4(w[8] * sc, w[9] * sc, w[10] * sc, w[11] * sc),
+                           pack_e4m3x4(w[12] * sc, w[13] * sc, w[14] * sc, w[15] * sc));
+        }
+        return 1.0f / sc;
+    }
+}
+
+template <int PREC>
+__device__ __forceinline__ bool tc_run_prec(TcSmem &S, uint32_t tmem, const uint8_t *b, int K, int N, uint32_t &phase)
+{
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(S.X), b0 = smem_u32(b);
+        if (PREC == 1) {
+            const uint32_t sbo = (uint32_t)(K / 8) * 128u, id = idesc_f16(128, N, true);
+            for (int kc = 0; kc < K / 16; ++kc)
+                tc_mma_f16(tmem, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
+        } else {
+            const uint32_t sbo = (uint32_t)(K / 16) * 128u, id = idesc_f8_e4m3(128, N);
+            for (int kc = 0; kc < K / 32; ++kc)
+                tc_mma_f8(tmem, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
+        }
+        tc_commit(&S.mbar);
+    }
+    const bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+/* 64 accumulator columns -> scale, (+bias), ReLU -> next operand row */
+template <int PREC>
+__device__ __forceinline__ float epi_hidden_prec(uint32_t taddr, float deq, const float *bias, uint8_t *dst, int row)
+{
+    float v[64];
+    tmem_ld32(taddr, *reinterpret_cast<float(*)[32]>(v));
+    tmem_ld32(taddr + 32, *reinterpret_cast<float(*)[32]>(v + 32));
+    tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = fmaxf(v[i] * deq + (bias ? bias[i] : 0.0f), 0.0f);
+    return put_row<PREC, 64>(dst, row, v);
+}
+
+constexpr int TC_PREC_CTAS_PER_SM = 4; /* 128 registers: the fp32 rows of the scaled epilogues */
+
+template <int PREC, int HH>
+__global__ void __launch_bounds__(128, TC_PREC_CTAS_PER_SM) wf_net_tc_prec_kernel(RenderParams p, int it)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
+    const int n_rows = p.counters[2];
+    if (n_rows == 0) return;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint8_t *wsrc = PREC == 1 ? p.weights_tc_bf16 : p.weights_tc_fp8;
+    const int wbytes = PREC == 1 ? TC_WBYTES : TC8_WBYTES;
+    for (int i = tid; i < wbytes / 16; i += 128)
+        reinterpret_cast<uint4 *>(S.W)[i] = __ldg(reinterpret_cast<const uint4 *>(wsrc) + i);
+    if (tid < 64) S.bias3[tid] = p.bias3[tid];
+    if (tid == 0) mbar_init(&S.mbar, 1);
+    if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    float iw[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
+    if (PREC == 2)
+#pragma unroll
+        for (int l = 0; l < 5; ++l) iw[l] = __ldg(p.tc_fp8_iw + l);
+    const int o1 = PREC == 1 ? TC_B1 : TC8_B1, o2 = PREC == 1 ? TC_B2 : TC8_B2, o3 = PREC == 1 ? TC_B3 : TC8_B3,
+              o4 = PREC == 1 ? TC_B4 : TC8_B4, o5 = PREC == 1 ? TC_B5 : TC8_B5;
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const RayState *states = p.states[it & 1];
+    uint32_t phase = 0;
+    bool ok = true;
+    const int n_tiles = (n_rows + 127) / 128;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int r = tile * 128 + tid < n_rows ? tile * 128 + tid : -1;
+        float in[32];
+        __half2 feat[16];
+        float3 d01 = make_float3(0.5f, 0.5f, 0.5f);
+        if (r >= 0) {
+            const float4 pw = p.row_pay[r];
+            hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
+            d01 = dir01_of(states, p.row_slot[r]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const float2 f = __half22float2(feat[q]);
+            in[2 * q] = f.x;
+            in[2 * q + 1] = f.y;
+        }
+        float deq = put_row<PREC, 32>(S.X, tid, in);
+        if (!(ok = tc_publish(ok))) break;
+        /* density network */
+        ok = tc_run_prec<PREC>(S, tmem, S.W + o1, 32, 64, phase);
+        deq = epi_hidden_prec<PREC>(tmem + lane_base, deq * iw[0], nullptr, S.X, tid);
+        if (!(ok = tc_publish(ok))) break;
+        ok = tc_run_prec<PREC>(S, tmem, S.W + o2, 64, 16, phase);
+        float o[16];
+        tmem_ld16(tmem + lane_base, o);
+        tmem_wait_ld();
+        const float dq2 = deq * iw[1];
+        const float log_density = o[0] * dq2;
+        /* head input [layer-2 outputs (latents only) | SH] in the remapped order of W3 */
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int lat = j - p.latent_offset;
+            const float v = o[j] * dq2;
+            in[j] = (lat >= 0 && lat < 8) ? (PREC == 1 ? __bfloat162float(__float2bfloat16_rn(v)) : v) : 0.0f;
+        }
+        {
+            __half2 sh[8];
+            sh16(d01, sh);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 f = __half22float2(sh[q]);
+                in[16 + 2 * q] = f.x;
+                in[17 + 2 * q] = f.y;
+            }
+        }
+        deq = put_row<PREC, 32>(S.X, tid, in);
+        if (!(ok = tc_publish(ok))) break;
+        /* color head */
+        ok = tc_run_prec<PREC>(S, tmem, S.W + o3, 32, 64, phase);
+        deq = epi_hidden_prec<PREC>(tmem + lane_base, deq * iw[2], S.bias3, S.X, tid);
+        if (!(ok = tc_publish(ok))) break;
+        if (HH == 2) {
+            ok = tc_run_prec<PREC>(S, tmem, S.W + o4, 64, 64, phase);
+            deq = epi_hidden_prec<PREC>(tmem + lane_base, deq * iw[3], nullptr, S.X, tid);
+            if (!(ok = tc_publish(ok))) break;
+        }
+        ok = tc_run_prec<PREC>(S, tmem, S.W + o5, 64, 16, phase);
+        tmem_ld16(tmem + lane_base, o);
+        tmem_wait_ld();
+        const float dq5 = deq * iw[4];
+        /* outputs in the network's precision, stored as fp16 like the fp16 path */
+        auto rnd = [](float v) { return PREC == 1 ? __bfloat162float(__float2bfloat16_rn(v)) : v; };
+        if (r >= 0)
+            p.row_out[r] = make_uint2(pack_h2(rnd(o[0] * dq5), rnd(o[1] * dq5)),
+                                      (uint32_t)__half_as_ushort(__float2half_rn(rnd(o[2] * dq5))) |
+                                          ((uint32_t)__half_as_ushort(__float2half_rn(rnd(log_density))) << 16));
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+    }
+    if (!ok && tid == 0) atomicOr(p.guard, 16);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TC_COLS);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* composite + compaction                                                    */
 /* ------------------------------------------------------------------------- */
 template <bool CACHED>
@@ -696,7 +914,7 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
         if (valid) {
             st = cur[i];
             const int2 rr = p.ray_rows[i];
-            float4 acc = st.acc;
+            float4 acc = st.acc, comp = st.comp;
             int c_res = st.cnt.y, c_cache = st.cnt.z, c_drop = st.cnt2.x;
             bool term = false;
             /* rows are in t order: the merge of the resample and cache
@@ -720,14 +938,15 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
                 const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
                 if (alpha > p.scene.alpha_thre) {
                     const float wgt = alpha * acc.w;
-                    acc.x += wgt / (1.0f + expf(-rg.x));
-                    acc.y += wgt / (1.0f + expf(-rg.y));
-                    acc.z += wgt / (1.0f + expf(-lb));
+                    kahan_add(acc.x, comp.x, wgt / (1.0f + expf(-rg.x)));
+                    kahan_add(acc.y, comp.y, wgt / (1.0f + expf(-rg.y)));
+                    kahan_add(acc.z, comp.z, wgt / (1.0f + expf(-lb)));
                     acc.w *= 1.0f - alpha;
                 }
                 if (acc.w < 1e-4f) { term = true; break; }
             }
             st.acc = acc;
+            st.comp = comp;
             st.cnt.y = c_res;
             st.cnt.z = c_cache;
             st.cnt2.x = c_drop;
@@ -854,7 +1073,21 @@ static cudaError_t set_net_attrs()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<1, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<2, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     return e;
+}
+
+/* the network kernel of the plain path's rows in the renderer's network path and precision */
+template <int HH>
+static void launch_plain_net(const RenderParams &p, int it, int n_sms, cudaStream_t s)
+{
+    const size_t tc_smem = sizeof(TcSmem);
+    const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
+    if (!p.use_tc) wf_net_resample_kernel<HH, false><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
+    else if (p.precision == 1) wf_net_tc_prec_kernel<1, HH><<<n_sms * TC_PREC_CTAS_PER_SM, 128, tc_smem, s>>>(p, it);
+    else if (p.precision == 2) wf_net_tc_prec_kernel<2, HH><<<n_sms * TC_PREC_CTAS_PER_SM, 128, tc_smem, s>>>(p, it);
+    else wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
 }
 
 template <bool CACHED, int HH>
@@ -902,8 +1135,7 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
             L.launches += 3;
         } else {
             timed_begin();
-            if (p.use_tc) wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
-            else wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+            launch_plain_net<HH>(p, it, n_sms, s);
             timed_end();
             L.launches += 1;
         }
@@ -940,14 +1172,9 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
     wf_raygen_list_kernel<<<(p.n_list + 255) / 256, 256, 0, s>>>(p);
     ++L.launches;
     const int grid_ray = n_sms * 16;
-    const int grid_net = n_sms * 2;
-    const size_t net_smem = sizeof(NetSmem);
-    const size_t tc_smem = sizeof(TcSmem);
-    const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
     for (int it = 0; it < (1 << 20); ++it) {
         wf_march_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
-        if (p.use_tc) wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
-        else wf_net_resample_kernel<HH, false><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
+        launch_plain_net<HH>(p, it, n_sms, s); /* the forward kernel of pass 1, so both passes composite the same values */
         wf_composite_bwd_kernel<<<grid_ray, 128, 0, s>>>(p, it);
         cudaError_t e = launch_net_backward(p, b, HH, it, n_sms, s);
         if (e != cudaSuccess) return e;

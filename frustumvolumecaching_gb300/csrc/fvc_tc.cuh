@@ -47,6 +47,31 @@ __device__ __forceinline__ uint32_t idesc_f16(int M, int N, bool bf16)
     return (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+/* byte offset of element (row, k) in a canonical K-major tile of K 8-bit
+ * columns: 8 rows x 16 elements per 128-byte core matrix */
+__host__ __device__ __forceinline__ uint32_t kmajor_offset8(int row, int k, int K)
+{
+    return (uint32_t)(((row >> 3) * (K >> 4) + (k >> 4)) * 128 + (row & 7) * 16 + (k & 15));
+}
+
+/* instruction descriptor of kind::f8f6f4 with E4M3 A and B (format 0), fp32
+ * accumulate, both K-major, M x N */
+__device__ __forceinline__ uint32_t idesc_f8_e4m3(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+/* one MMA of K = 32 8-bit elements */
+__device__ __forceinline__ void tc_mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n"
+        :
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 __device__ __forceinline__ void tc_mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate)
 {
     asm volatile(

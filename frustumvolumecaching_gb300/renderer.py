@@ -154,6 +154,12 @@ class Renderer:
         """tcgen05 (default) or mma.sync network kernels."""
         L.check(L.load().fvc_renderer_set_network_path(self.handle, int(bool(use_tcgen05))))
 
+    FP16, BF16, FP8_E4M3 = 0, 1, 2
+
+    def set_precision(self, precision: int) -> None:
+        """MLP precision of the plain tcgen05 path: FP16 (default), BF16 or FP8_E4M3."""
+        L.check(L.load().fvc_renderer_set_precision(self.handle, int(precision)))
+
     def set_kernel_timing(self, enable: bool) -> None:
         """CUDA-event timing of each resample network launch (see _render_stats.timed_kernel_ms)."""
         L.check(L.load().fvc_renderer_set_kernel_timing(self.handle, int(bool(enable))))

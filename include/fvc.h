@@ -251,6 +251,13 @@ int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
  * Both compute the same layers in fp16 with fp32 accumulation.  No reference
  * counterpart (the reference runs tiny-cuda-nn's FullyFusedMLP). */
 int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05);
+
+/* MLP precision of the plain renderers on the tcgen05 path (no counterpart
+ * in the reference, whose MLPs are fp16): FP16 (default), BF16, or
+ * FP8-E4M3 with per-layer weight scaling and per-row activation scaling;
+ * fp32 accumulation and fp32 Kahan-compensated compositing in every case. */
+enum { FVC_PRECISION_FP16 = 0, FVC_PRECISION_BF16 = 1, FVC_PRECISION_FP8_E4M3 = 2 };
+int fvc_renderer_set_precision(fvc_renderer *r, int precision);
 /* Statistics of the last render (needs the stream synchronised). */
 int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *out);
 
