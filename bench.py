@@ -225,6 +225,56 @@ def run_precision_bench(args, torch, dev, stream) -> dict:
 
 
 # --------------------------------------------------------------------------
+# batched multi-view render (config 4)
+# --------------------------------------------------------------------------
+BATCH_VIEWS = 64
+BATCH_SIZES = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+
+
+def run_batch_bench(args, torch, dev, stream) -> dict:
+    """64 seeded cameras (resolutions drawn uniformly from the four sizes) of
+    the config-1 scene rendered as one batch: one CUDA-graph launch per step,
+    the sub-iteration loop on the device; the autotuner picks the network tile
+    and marching batch first (untimed)."""
+    import frustumvolumecaching_gb300 as fvc
+    from frustumvolumecaching_gb300 import camera as fcam
+    from frustumvolumecaching_gb300 import model as fmodel
+
+    spec = fmodel.spec_config1()
+    loader = fvc.load_data(fmodel.ensure_model(spec))
+    rng = np.random.default_rng([1004, 2])
+    sizes = [BATCH_SIZES[i] for i in rng.integers(0, len(BATCH_SIZES), BATCH_VIEWS)]
+    cams = [fcam.seeded_camera(1004 * 1000 + v, width=W, height=H) for v, (W, H) in enumerate(sizes)]
+    infos = [fvc.raymarch_info(c, loader.stepsize_info) for c in cams]
+    n = sum(W * H for W, H in sizes)
+    res = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    img = torch.zeros((n, 4), dtype=torch.uint8, device=dev)
+    r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    r.set_stream(stream.cuda_stream)
+    tuned = r.autotune(infos, image=img, results=res)
+    for _ in range(args.warmup):
+        r.render_batch(infos, image=img, results=res)
+    torch.cuda.synchronize(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    times = []
+    for _ in range(args.steps):
+        a, b = ev(), ev()
+        a.record(stream)
+        r.render_batch(infos, image=img, results=res)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        times.append(a.elapsed_time(b))
+    st = r._render_stats
+    ms = sum(times) / len(times)
+    return {"value": n / (ms / 1e3) / 1e6, "unit": "Mrays/s", "views_per_s": BATCH_VIEWS / (ms / 1e3), "ms_per_batch": ms,
+            "views": BATCH_VIEWS, "rays": n, "samples": st.n_samples, "sub_iterations": st.n_rounds,
+            "gpu_launches": st.n_launches, "host_launches_per_batch": 1,
+            "autotune": {"m_tile": tuned.m_tile, "steps_per_iter": tuned.steps_per_iter,
+                         "rows_per_iteration": tuned.rows_per_iteration, "ms": tuned.ms, "candidates": tuned.n_candidates},
+            "workload": "c4: 64 views of the config-1 scene, resolutions uniform over 320x240..1920x1080, plain render"}
+
+
+# --------------------------------------------------------------------------
 # differentiable render (backward Mrays/s)
 # --------------------------------------------------------------------------
 BWD_RAYS = 1 << 18
@@ -456,6 +506,7 @@ def run_fvc(args) -> dict | None:
 
     backward = run_backward_bench(args, torch, dev, stream)
     precision = run_precision_bench(args, torch, dev, stream)
+    batch = run_batch_bench(args, torch, dev, stream)
 
     # e2e: the cached path through the host-buffer C-ABI call (D2H of every frame)
     hbuf = fvc.RenderBuffer(RES)
@@ -530,6 +581,7 @@ def run_fvc(args) -> dict | None:
                 "d2h_bytes_per_step": n_frames * W * H * (4 + 16 + 16)},
         "backward": backward,
         "precision": precision,
+        "batch": batch,
         "gpu_launches": log["launches"] // max(1, args.steps),
         "gpu_launches_plain_path": log["plain_launches"] // max(1, args.steps),
         "clocks": clk,

@@ -89,6 +89,11 @@ class ModelProps(C.Structure):
                 ("n_latents", c_int), ("occupancy_bitfield", C.c_void_p), ("occupancy_bytes", C.c_size_t)]
 
 
+class AutotuneResult(C.Structure):
+    _fields_ = [("m_tile", c_int), ("steps_per_iter", c_int), ("rows_per_iteration", C.c_longlong), ("ms", C.c_float),
+                ("n_candidates", c_int)]
+
+
 class CacheStats(C.Structure):
     _fields_ = [("n_bricks_set", c_int), ("n_bricks_reserved", c_int), ("n_bricks_demanded", c_int),
                 ("overflow", c_int), ("n_iterations", c_int), ("n_launches", c_int), ("n_samples", C.c_longlong)]
@@ -96,7 +101,7 @@ class CacheStats(C.Structure):
 
 assert C.sizeof(SceneInfo) == 76 and C.sizeof(StepsizeInfo) == 48
 assert C.sizeof(CameraInfo) == 144 and CameraInfo.cam2world.offset == 32 and CameraInfo.world2cam.offset == 80
-assert C.sizeof(RenderStats) == 72 and C.sizeof(CacheStats) == 32
+assert C.sizeof(RenderStats) == 72 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 24
 assert C.sizeof(RaymarchInfo) == 352 and RaymarchInfo.stepsize_info.offset == 288 and RaymarchInfo.sample_index.offset == 336
 
 FVC_OK = 0
@@ -137,6 +142,8 @@ SIGNATURES = {
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_renderer_set_precision": (c_int, [P, c_int]),
+    "fvc_render_batch": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs)]),
+    "fvc_renderer_autotune": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs), C.POINTER(AutotuneResult)]),
     "fvc_model_properties": (c_int, [P, C.POINTER(ModelProps)]),
     "fvc_renderer_synchronize": (c_int, [P]),
     "fvc_grad_create": (c_int, [P, PP]),

@@ -357,6 +357,16 @@ struct fvc_renderer {
     int *d_wf_counters = nullptr;
     int row_capacity = 0;
     int last_iterations = 0;
+    /* batched views in one graph launch */
+    DevCam *d_views = nullptr;
+    int *d_view_off = nullptr;
+    int views_cap = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    RenderParams graph_params;        /* the parameters the graph holds by value */
+    int graph_head_hidden = 0;
+    int graph_kernels = 0;            /* kernels of one loop body + prologue */
+    bool last_was_graph = false;
+    int steps_per_iter = 64;          /* marching steps per sub-iteration (autotuned) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
     int *d_grad_rows = nullptr;       /* rows with a gradient (plain renderers have no res_list) */
     int bwd_capacity = 0;
@@ -381,6 +391,8 @@ struct fvc_renderer {
         if (stream) cudaStreamSynchronize(stream);
         dfree(d_ctl); dfree(d_stats); dfree(d_results); dfree(d_image); dfree(d_counts);
         dfree(d_row_dout); dfree(d_grad_rows);
+        dfree(d_views); dfree(d_view_off);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
         release_wavefront();
         bs.release();
         if (h_pinned) cudaFreeHost(h_pinned);
@@ -744,7 +756,9 @@ extern "C" int fvc_renderer_resize(fvc_renderer *r, int width, int height)
     /* wavefront: alive-ray states (ping-pong) and up to 16 sample rows per
      * ray and sub-iteration */
     r->release_wavefront();
-    const size_t cap = std::min<size_t>(n * 16, (size_t)1 << 25);
+    /* at least one row per ray: the march gives each alive ray
+     * min(16, capacity / alive) rows, so capacity >= rays keeps that >= 1 */
+    const size_t cap = std::max(n, std::min<size_t>(n * 16, (size_t)1 << 25));
     const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
     if ((rc = dalloc(&r->d_states[0], n, "ray states"))) return rc;
     if ((rc = dalloc(&r->d_states[1], n, "ray states"))) return rc;
@@ -833,7 +847,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.res_list = r->d_res_list; p.cache_list = r->d_cache_list;
     p.counters = r->d_wf_counters;
     p.row_capacity = r->row_capacity;
-    p.steps_per_iter = 64;
+    p.steps_per_iter = r->steps_per_iter;
     return FVC_OK;
 }
 
@@ -856,6 +870,7 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
     CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));
     reset_launch_log(r);
+    r->last_was_graph = false;
     CU(render_frame(p, cached, m->head_hidden, m->n_sms, r->stream, r->h_pinned + 8, 4, &r->last_iterations, &r->log));
     return FVC_OK;
 }
@@ -906,6 +921,12 @@ extern "C" int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *o)
     o->samples_ppx = (double)s.n_samples / n_rays;
     o->guard_flags = ctl[1];
     o->n_launches = r->log.launches;
+    if (r->last_was_graph) { /* the device loop: prologue + one body per two sub-iterations */
+        int iters = 0;
+        CU(cudaMemcpy(&iters, r->d_wf_counters + 5, sizeof(int), cudaMemcpyDeviceToHost));
+        o->n_rounds = iters;
+        o->n_launches = 1 + (long long)(r->graph_kernels - 1) * (iters / 2);
+    }
     o->n_timed_launches = r->log.ev ? r->log.n_timed : 0;
     o->timed_kernel_ms = 0.0f;
     for (int i = 0; i < o->n_timed_launches; ++i) {
@@ -1388,5 +1409,135 @@ extern "C" int fvc_renderer_set_precision(fvc_renderer *r, int precision)
 {
     CHECK_ARG(r && precision >= FVC_PRECISION_FP16 && precision <= FVC_PRECISION_FP8_E4M3, "fvc_renderer_set_precision: bad arguments");
     r->precision = precision;
+    return FVC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* batched views: one graph launch per batch                                 */
+/* ------------------------------------------------------------------------ */
+static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
+                       RenderParams &p, int &n_rays)
+{
+    CHECK_ARG(r && infos && n_views > 0, "fvc_render_batch: bad arguments");
+    if (r->kind == FVC_RENDERER_CACHE_PERFORMANCE)
+        return fail(FVC_ERR_CONFIG, "fvc_render_batch: batched views are built for the plain renderers");
+    long long total = 0;
+    int rc;
+    for (int v = 0; v < n_views; ++v) {
+        if ((rc = check_info(&infos[v]))) return rc;
+        if (memcmp(&infos[v].stepsize_info, &infos[0].stepsize_info, sizeof(fvc_stepsize_info)) != 0)
+            return fail(FVC_ERR_ARG, "fvc_render_batch: the views of a batch share one StepsizeInfo");
+        total += (long long)infos[v].cam_info.resolution.x * infos[v].cam_info.resolution.y;
+    }
+    if (total > (1ll << 30)) return fail(FVC_ERR_ARG, "fvc_render_batch: more than 2^30 rays");
+    n_rays = (int)total;
+    if ((rc = fvc_renderer_resize(r, n_rays, 1))) return rc;
+    if (r->views_cap < n_views) {
+        dfree(r->d_views); dfree(r->d_view_off);
+        if ((rc = dalloc(&r->d_views, (size_t)n_views, "views"))) return rc;
+        if ((rc = dalloc(&r->d_view_off, (size_t)n_views + 1, "view offsets"))) return rc;
+        r->views_cap = n_views;
+    }
+    std::vector<DevCam> cams(n_views);
+    std::vector<int> off(n_views + 1, 0);
+    for (int v = 0; v < n_views; ++v) {
+        cams[v] = dev_cam(infos[v].cam_info);
+        off[v + 1] = off[v] + infos[v].cam_info.resolution.x * infos[v].cam_info.resolution.y;
+    }
+    /* pageable sources: staged before the calls return, so the vectors may go */
+    CU(cudaMemcpyAsync(r->d_views, cams.data(), cams.size() * sizeof(DevCam), cudaMemcpyHostToDevice, r->stream));
+    CU(cudaMemcpyAsync(r->d_view_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, r->stream));
+    fvc_raymarch_info first = infos[0];
+    first.cam_info.resolution.x = n_rays;
+    first.cam_info.resolution.y = 1;
+    if ((rc = setup_render_params(r, &first, out ? (float4 *)out->results : nullptr, out ? (uchar4 *)out->image_rgba8 : nullptr,
+                                  out ? (int4 *)out->ray_counts : nullptr, p)))
+        return rc;
+    p.views = r->d_views;
+    p.view_off = r->d_view_off;
+    p.n_views = n_views;
+    p.max_iterations = 1 << 14;
+    return FVC_OK;
+}
+
+static int batch_launch(fvc_renderer *r, const RenderParams &p, int n_rays)
+{
+    fvc_model *m = r->m;
+    if (!r->graph_exec || r->graph_head_hidden != m->head_hidden || memcmp(&r->graph_params, &p, sizeof(RenderParams)) != 0) {
+        if (r->graph_exec) {
+            CU(cudaStreamSynchronize(r->stream));
+            cudaGraphExecDestroy(r->graph_exec);
+            r->graph_exec = nullptr;
+        }
+        CU(build_batch_graph(p, m->head_hidden, m->n_sms, r->stream, n_rays, &r->graph_exec, &r->graph_kernels));
+        memcpy(&r->graph_params, &p, sizeof(RenderParams));
+        r->graph_head_hidden = m->head_hidden;
+    }
+    CU(cudaGraphLaunch(r->graph_exec, r->stream));
+    reset_launch_log(r);
+    r->last_was_graph = true;
+    return FVC_OK;
+}
+
+extern "C" int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out)
+{
+    CHECK_ARG(r, "fvc_render_batch: null renderer");
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    RenderParams p;
+    int n_rays = 0, rc;
+    if ((rc = batch_setup(r, infos, n_views, out, p, n_rays))) return rc;
+    return batch_launch(r, p, n_rays);
+}
+
+extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
+                                     fvc_autotune_result *res)
+{
+    CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    const int tiles[2] = {128, 32};        /* tcgen05 CTA tile, mma.sync warp tile */
+    const int steps[4] = {16, 32, 64, 128}; /* marching steps per ray and sub-iteration */
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_tile = 128, best_steps = 64, n_cand = 0, rc = FVC_OK;
+    long long best_rows = 0;
+    for (int ti = 0; ti < 2 && rc == FVC_OK; ++ti)
+        for (int si = 0; si < 4 && rc == FVC_OK; ++si) {
+            r->use_tc = tiles[ti] == 128;
+            r->steps_per_iter = steps[si];
+            RenderParams p;
+            int n_rays = 0;
+            if ((rc = batch_setup(r, infos, n_views, out, p, n_rays))) break;
+            if ((rc = batch_launch(r, p, n_rays))) break; /* builds the graph, warms up */
+            cudaEventRecord(e0, r->stream);
+            for (int k = 0; k < 2 && rc == FVC_OK; ++k) rc = batch_launch(r, p, n_rays);
+            cudaEventRecord(e1, r->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(FVC_ERR_CUDA, "fvc_renderer_autotune: launch failed"); break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms *= 0.5f;
+            ++n_cand;
+            RenderStatsDev st;
+            int iters = 0;
+            cudaMemcpy(&st, r->d_stats, sizeof(st), cudaMemcpyDeviceToHost);
+            cudaMemcpy(&iters, r->d_wf_counters + 5, sizeof(int), cudaMemcpyDeviceToHost);
+            if (ms < best) {
+                best = ms;
+                best_tile = tiles[ti];
+                best_steps = steps[si];
+                best_rows = (long long)st.n_samples / std::max(1, iters);
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    r->use_tc = best_tile == 128;
+    r->steps_per_iter = best_steps;
+    if (rc) return rc;
+    res->m_tile = best_tile;
+    res->steps_per_iter = best_steps;
+    res->rows_per_iteration = best_rows;
+    res->ms = best;
+    res->n_candidates = n_cand;
     return FVC_OK;
 }

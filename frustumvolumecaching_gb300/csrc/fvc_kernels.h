@@ -95,6 +95,12 @@ struct RenderParams {
     int *counters;              /* [0], [1] alive rays (ping-pong), [2] rows, [3] resample, [4] cache */
     int row_capacity;           /* rows per sub-iteration */
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
+    /* batched views: rays of n_views cameras (device array), view v's pixel
+     * (x, y) at ray id view_off[v] + y * W_v + x; view_off[n_views] = rays */
+    const DevCam *views;
+    const int *view_off;
+    int n_views;
+    int max_iterations;         /* bound of the device-side sub-iteration loop */
     /* differentiable render */
     const int *pixel_list;      /* rays for these pixels (y * W + x) instead of the full image; ray id = list index */
     int n_list;
@@ -200,6 +206,14 @@ struct LaunchLog {
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
                          int check_every, int *n_iterations, LaunchLog *log = nullptr);
+
+/* The plain render of p.views as one CUDA graph: counter resets, raygen, and
+ * a conditional WHILE node whose body runs two sub-iterations and then lets
+ * the device decide whether rays are still alive (at most p.max_iterations
+ * sub-iterations; the iteration count is left in p.counters[5]).  The graph
+ * holds p by value: it is valid while the buffers p points to are. */
+cudaError_t build_batch_graph(const RenderParams &p, int head_hidden, int n_sms, cudaStream_t s, int n_rays,
+                              cudaGraphExec_t *exec, int *n_kernels);
 
 /* differentiable render (fvc_backward.cu): pass 1 is render_frame over p.pixel_list */
 cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, int head_hidden, int n_sms, cudaStream_t s,

@@ -30,6 +30,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 
+#include <vector>
+
 #include "fvc_kernels.h"
 
 #include <cuda_fp16.h>
@@ -175,6 +177,54 @@ __global__ void __launch_bounds__(256) wf_raygen_list_kernel(RenderParams p)
         st.cnt2 = make_int4(0, 0, 0, 0);
         p.states[0][base + __popc(m & lane_lt())] = st;
     }
+}
+
+/* rays of a batch of views (one thread per pixel of the concatenated views) */
+__global__ void __launch_bounds__(256) wf_raygen_views_kernel(RenderParams p)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = p.view_off[p.n_views];
+    const bool valid = i < n;
+    bool hits = false;
+    float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
+    float tn = 0.f, tf = 0.f;
+    if (valid) {
+        int lo = 0, hi = p.n_views - 1; /* the view holding ray i: last offset <= i */
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (p.view_off[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        const DevCam &cam = p.views[lo];
+        const int local = i - p.view_off[lo];
+        generate_ray(cam, local % cam.W, local / cam.W, o, d);
+        hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
+    }
+    if (valid && !hits) write_pixel(p, i, make_float4(0.f, 0.f, 0.f, 1.f), make_int4(0, 0, 0, 0));
+    const unsigned m = __ballot_sync(FULLMASK, hits);
+    int base = 0;
+    if (lane_id() == 0 && m) base = atomicAdd(p.counters + 0, __popc(m));
+    base = __shfl_sync(FULLMASK, base, 0);
+    if (hits) {
+        RayState st;
+        st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
+        st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
+        st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
+        st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
+        st.cnt = make_int4(i, 0, 0, 0);
+        st.cnt2 = make_int4(0, 0, 0, 0);
+        p.states[0][base + __popc(m & lane_lt())] = st;
+    }
+}
+
+/* end of a graph-loop body (two sub-iterations): continue while rays are
+ * alive and the iteration bound is not reached (guard bit 32 if it is) */
+__global__ void wf_loop_cond_kernel(RenderParams p, cudaGraphConditionalHandle handle)
+{
+    const int iters = p.counters[5] + 2;
+    p.counters[5] = iters;
+    const bool alive = p.counters[0] > 0;
+    if (alive && iters >= p.max_iterations) atomicOr(p.guard, 32);
+    cudaGraphSetConditional(handle, (alive && iters < p.max_iterations) ? 1u : 0u);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1196,6 +1246,82 @@ cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, int head_h
 {
     return head_hidden == 2 ? run_backward<2>(p, b, n_sms, s, h_pinned, check_every, log)
                             : run_backward<1>(p, b, n_sms, s, h_pinned, check_every, log);
+}
+
+template <int HH>
+static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStream_t s, int n_rays, cudaGraphExec_t *exec,
+                                       int *n_kernels)
+{
+    static bool attrs_set = false;
+    if (!attrs_set) {
+        cudaError_t e = set_net_attrs<HH>();
+        if (e != cudaSuccess) return e;
+        attrs_set = true;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle handle;
+    e = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault);
+    /* prologue: counters, statistics, raygen */
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(s, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaMemsetAsync(p.ray_counter, 0, 4 * sizeof(int), s);
+        cudaMemsetAsync(p.stats, 0, sizeof(RenderStatsDev), s);
+        cudaMemsetAsync(p.counters, 0, 8 * sizeof(int), s);
+        wf_raygen_views_kernel<<<(n_rays + 255) / 256, 256, 0, s>>>(p);
+        cudaGraph_t g2 = nullptr;
+        e = cudaStreamEndCapture(s, &g2);
+    }
+    /* the loop: a WHILE node after the prologue's last node */
+    cudaGraphNode_t prologue_tail = nullptr;
+    if (e == cudaSuccess) {
+        size_t n = 0;
+        e = cudaGraphGetNodes(graph, nullptr, &n);
+        std::vector<cudaGraphNode_t> nodes(n);
+        if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nodes.data(), &n);
+        for (cudaGraphNode_t nd : nodes) { /* the node nothing depends on */
+            size_t nout = 0;
+            if (cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout) == cudaSuccess && nout == 0) prologue_tail = nd;
+        }
+    }
+    cudaGraphNode_t loop = nullptr;
+    cudaGraph_t body = nullptr;
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        e = cudaGraphAddNode(&loop, graph, &prologue_tail, nullptr, prologue_tail ? 1 : 0, &cp);
+        if (e == cudaSuccess) body = cp.conditional.phGraph_out[0];
+    }
+    int kernels = 1;
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const int grid_ray = n_sms * 16;
+        for (int it = 0; it < 2; ++it) {
+            wf_march_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
+            launch_plain_net<HH>(p, it, n_sms, s);
+            wf_composite_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
+            wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, 0);
+        }
+        wf_loop_cond_kernel<<<1, 1, 0, s>>>(p, handle);
+        kernels += 9;
+        cudaGraph_t g3 = nullptr;
+        e = cudaStreamEndCapture(s, &g3);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (n_kernels) *n_kernels = kernels;
+    return e;
+}
+
+cudaError_t build_batch_graph(const RenderParams &p, int head_hidden, int n_sms, cudaStream_t s, int n_rays,
+                              cudaGraphExec_t *exec, int *n_kernels)
+{
+    return head_hidden == 2 ? build_batch_graph_t<2>(p, n_sms, s, n_rays, exec, n_kernels)
+                            : build_batch_graph_t<1>(p, n_sms, s, n_rays, exec, n_kernels);
 }
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,

@@ -188,6 +188,29 @@ class Renderer:
                                              C.byref(loss), L.ptr(pred)))
         return loss.value
 
+    @staticmethod
+    def _batch_args(infos, image, results, ray_counts):
+        arr = (L.RaymarchInfo * len(infos))(*infos)
+        out = L.RenderOutputs()
+        out.image_rgba8, out.results, out.ray_counts = L.ptr(image), L.ptr(results), L.ptr(ray_counts)
+        return arr, out
+
+    def render_batch(self, infos, image=None, results=None, ray_counts=None) -> None:
+        """Render several views in one CUDA-graph launch into device buffers
+        holding the views back to back (asynchronous on the renderer's stream)."""
+        arr, out = self._batch_args(infos, image, results, ray_counts)
+        L.check(L.load().fvc_render_batch(self.handle, arr, len(infos), C.byref(out)))
+
+    def autotune(self, infos, image=None, results=None, ray_counts=None) -> L.AutotuneResult:
+        """Pick the network tile and marching batch that render this batch fastest."""
+        arr, out = self._batch_args(infos, image, results, ray_counts)
+        res = L.AutotuneResult()
+        L.check(L.load().fvc_renderer_autotune(self.handle, arr, len(infos), C.byref(out), C.byref(res)))
+        return res
+
+    def synchronize(self) -> None:
+        L.check(L.load().fvc_renderer_synchronize(self.handle))
+
     @property
     def _render_stats(self) -> L.RenderStats:
         s = L.RenderStats()

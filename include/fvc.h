@@ -322,6 +322,32 @@ int fvc_cache_read(fvc_cache *c, int32_t *packed_index, size_t *packed_index_n,
 int fvc_cache_dims(fvc_cache *c, fvc_int3 *frustum_dims, fvc_int3 *brick_dims, fvc_int3 *data_bricks_per_dim);
 
 /* ------------------------------------------------------------------------ */
+/* batched views (no counterpart in the reference)                           */
+/* ------------------------------------------------------------------------ */
+
+/* Plain render of n_views cameras (own resolutions, one shared
+ * StepsizeInfo) in one CUDA-graph launch: the sub-iteration loop runs on the
+ * device (a conditional WHILE node), with no host round trip per
+ * sub-iteration.  Outputs are device buffers holding the views back to back
+ * (view v's pixel (x, y) at sum_{u<v} W_u H_u + y * W_v + x).  Asynchronous
+ * on the renderer's stream; the graph is rebuilt when the parameters it holds
+ * (buffers, counts, path, precision) change. */
+int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out);
+
+/* Times each candidate network tile (128-row tcgen05 CTA tiles or 32-row
+ * mma.sync warp tiles) and marching batch (16, 32, 64 or 128 steps per ray
+ * and sub-iteration) on this batch, keeps the fastest for the renderer. */
+typedef struct {
+    int m_tile;                  /* rows per network tile of the winner */
+    int steps_per_iter;          /* marching steps per ray and sub-iteration */
+    long long rows_per_iteration;/* samples per sub-iteration it produced (compaction batch) */
+    float ms;                    /* its time per batch */
+    int n_candidates;
+} fvc_autotune_result;
+int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
+                          fvc_autotune_result *res);
+
+/* ------------------------------------------------------------------------ */
 /* differentiable render (no counterpart in the reference)                   */
 /* ------------------------------------------------------------------------ */
 
