@@ -32,7 +32,7 @@ namespace fvc {
 constexpr unsigned FULLMASK = 0xffffffffu;
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
-constexpr int BW_WARPS = 4;
+constexpr int BW_WARPS = 8; /* 8 x 23.5 KB of row tiles + 40 KB of dW: one CTA of 8 warps per SM */
 constexpr int S32 = 40;  /* tile strides in halfs: 80 B and 144 B rows, 16-byte aligned for ldmatrix */
 constexpr int S64 = 72;
 constexpr int DF_STRIDE = 36; /* fp32 feature-gradient rows (aliases the A3 tile) */
@@ -118,8 +118,13 @@ __device__ __forceinline__ void ldsm4t(uint32_t (&r)[4], const __half *p)
                  : "r"(smem_u32(p)));
 }
 
-/* dW (O x I, row-major fp32, shared) += G^T X over the warp's 32 rows;
- * G: 32 x O, X: 32 x I, both fp16 shared tiles. */
+/* the shared dW copy keeps row-major rows of I floats with the column
+ * XOR-swizzled by 4 * (row % 8): the 32 lanes of an accumulator fragment
+ * (rows g, columns 2q) then fall into 16 banks instead of 4 */
+__device__ __forceinline__ int dw_col(int row, int col) { return col ^ ((row & 7) << 2); }
+
+/* dW (O x I, row-major fp32, shared, swizzled) += G^T X over the warp's 32
+ * rows; G: 32 x O, X: 32 x I, both fp16 shared tiles. */
 template <int O, int I>
 __device__ __forceinline__ void warp_dw(const __half *G, int sg, const __half *X, int sx, float *dW, int lane)
 {
@@ -142,12 +147,11 @@ __device__ __forceinline__ void warp_dw(const __half *G, int sg, const __half *X
             }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                float *w0 = dW + (16 * mt + g) * I + 8 * (nt + h) + 2 * q;
-                float *w1 = w0 + 8 * I;
-                atomicAdd(w0, d[h][0]);
-                atomicAdd(w0 + 1, d[h][1]);
-                atomicAdd(w1, d[h][2]);
-                atomicAdd(w1 + 1, d[h][3]);
+                const int r0 = 16 * mt + g, r1 = r0 + 8, c = 8 * (nt + h) + 2 * q;
+                atomicAdd(dW + r0 * I + dw_col(r0, c), d[h][0]);
+                atomicAdd(dW + r0 * I + dw_col(r0, c + 1), d[h][1]);
+                atomicAdd(dW + r1 * I + dw_col(r1, c), d[h][2]);
+                atomicAdd(dW + r1 * I + dw_col(r1, c + 1), d[h][3]);
             }
         }
     }
@@ -341,15 +345,19 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
         __syncwarp();
     }
     __syncthreads();
-    const int head_floats = b.head_w5 + 16 * 64;
-    for (int i = threadIdx.x; i < GB_BASE; i += blockDim.x) {
-        const float v = dWb[i];
-        if (v != 0.f) atomicAdd(b.g_base + i, v);
-    }
-    for (int i = threadIdx.x; i < head_floats; i += blockDim.x) {
-        const float v = dWh[i];
-        if (v != 0.f) atomicAdd(b.g_head + i, v);
-    }
+    /* un-swizzle each layer's rows while adding to the global gradients */
+    auto flush = [&](const float *src, float *dst, int n, int I) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int row = i / I, col = i - row * I;
+            const float v = src[row * I + dw_col(row, col)];
+            if (v != 0.f) atomicAdd(dst + i, v);
+        }
+    };
+    flush(dWb + GB_W1, b.g_base + GB_W1, 64 * 32, 32);
+    flush(dWb + GB_W2, b.g_base + GB_W2, 16 * 64, 64);
+    flush(dWh + GH_W3, b.g_head + GH_W3, 64 * 32, 32);
+    if (HH == 2) flush(dWh + GH_W4, b.g_head + GH_W4, 64 * 64, 64);
+    flush(dWh + b.head_w5, b.g_head + b.head_w5, 16 * 64, 64);
 }
 
 /* per ray: squared error of the white-background pixel, dL/dC (loss-scaled,

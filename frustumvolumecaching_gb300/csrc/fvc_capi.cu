@@ -322,10 +322,15 @@ struct BuildScratch {
     int *tile_n_alive = nullptr;
     void *staging = nullptr;
     int *jobs = nullptr;
+    float4 *rows = nullptr;   /* per-iteration sample rows (tiles x 512) */
+    __half *den = nullptr;
+    uint4 *lat = nullptr;
+    int *row_of = nullptr;
     void release()
     {
         dfree(rays); dfree(block_step); dfree(tile_alive); dfree(alive_a); dfree(alive_b); dfree(counters);
         dfree(tile_n_samples); dfree(tile_processed); dfree(tile_need); dfree(tile_n_alive); dfree(jobs);
+        dfree(rows); dfree(den); dfree(lat); dfree(row_of);
         if (staging) cudaFree(staging);
         staging = nullptr;
         n_tiles = 0;
@@ -1076,6 +1081,10 @@ static int ensure_build_scratch(fvc_renderer *r, int n_tiles)
     if ((rc = dalloc(&b.tile_need, (size_t)n_tiles, "tile flags"))) return rc;
     if ((rc = dalloc(&b.tile_n_alive, (size_t)n_tiles, "tile alive counts"))) return rc;
     if ((rc = dalloc(&b.jobs, (size_t)2 * n_tiles, "copy jobs"))) return rc;
+    if ((rc = dalloc(&b.rows, (size_t)n_tiles * 512, "build rows"))) return rc;
+    if ((rc = dalloc(&b.den, (size_t)n_tiles * 512, "build densities"))) return rc;
+    if ((rc = dalloc(&b.lat, (size_t)n_tiles * 512, "build latents"))) return rc;
+    if ((rc = dalloc(&b.row_of, (size_t)n_tiles * 512, "build row map"))) return rc;
     cudaError_t e = cudaMalloc(&b.staging, (size_t)n_tiles * 512 * 32);
     if (e != cudaSuccess) { cudaGetLastError(); b.staging = nullptr; return fail(FVC_ERR_OOM, "cudaMalloc build staging"); }
     b.n_tiles = n_tiles;
@@ -1117,6 +1126,8 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     p.tile_n_alive = b.tile_n_alive; p.staging = b.staging; p.voxels = c->d_voxels;
     p.packed_index = c->d_packed; p.known_ranges = c->d_known; p.jobs = b.jobs;
     p.max_search = c->bZ + 4;
+    p.build_rows = b.rows; p.build_den = b.den; p.build_lat = b.lat; p.build_row_of = b.row_of;
+    p.build_row_counter = b.counters + 5;
 
     CU(cudaMemsetAsync(b.counters, 0, 8 * sizeof(int), s));
     CU(cudaMemsetAsync(c->d_packed, 0xff, (size_t)c->bX * c->bY * c->bZ * sizeof(int32_t), s));
@@ -1125,8 +1136,6 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     CU(cudaGetLastError());
     cache_compact_kernel<<<1, 1024, 0, s>>>(p, n_tiles);
     CU(cudaGetLastError());
-    const size_t smem = build_smem_bytes();
-    CU(cudaFuncSetAttribute(cache_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CU(cudaMemcpyAsync(r->h_pinned, b.counters, sizeof(int), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     int n_alive = r->h_pinned[0];
@@ -1135,13 +1144,18 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     const int max_iter = c->bZ + 8;
     std::vector<int> dummy;
     for (; iter < max_iter && n_alive > 0; ++iter) {
-        cache_tile_kernel<<<std::min(n_alive, 1 << 16), 64, smem, s>>>(p);
+        CU(cudaMemsetAsync(p.build_row_counter, 0, sizeof(int), s));
+        cache_search_kernel<<<std::min(n_alive, 1 << 16), 64, 0, s>>>(p);
+        CU(cudaGetLastError());
+        cache_density_kernel<<<m->n_sms * 8, 128, 0, s>>>(p);
+        CU(cudaGetLastError());
+        cache_composite_kernel<<<std::min(n_alive, 1 << 16), 64, 0, s>>>(p);
         CU(cudaGetLastError());
         cache_assign_kernel<<<1, 1024, 0, s>>>(p);
         CU(cudaGetLastError());
         cache_copy_kernel<<<std::min(n_alive, 4 * m->n_sms), 256, 0, s>>>(p);
         CU(cudaGetLastError());
-        n_launches += 3;
+        n_launches += 5;
         std::swap(p.alive_list, p.alive_list_next);
         std::swap(p.n_alive_tiles, p.n_alive_next);
         CU(cudaMemcpyAsync(r->h_pinned, p.n_alive_tiles, sizeof(int), cudaMemcpyDeviceToHost, s));

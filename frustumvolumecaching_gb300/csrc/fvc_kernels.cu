@@ -3,7 +3,8 @@
  *
  *  (the renderer's wavefront kernels live in fvc_render.cu)
  *  cache_*_kernel          frustum cache build, one depth brick of every alive
- *                          8x8 tile per iteration with deterministic slots:
+ *                          8x8 tile per iteration (search, density network,
+ *                          compositing, then deterministic slots):
  *                          CacheRenderer::initCacheBlockwise,
  *                          src/cache_renderer.cu:18-569,931-1051.
  *  inference_kernel        network at given inputs (NerfNetwork::inference).
@@ -122,48 +123,44 @@ __global__ void __launch_bounds__(64) cache_init_kernel(CacheBuildParams p)
     }
 }
 
-struct BuildSmem {
-    uint2 W[W_L3];                /* density network weights only */
-    float4 rows[512];             /* contracted position, .w = ray | step<<6 */
-    __half tile[2][32 * TILE_STRIDE];
-    __half out[512][9];           /* per row: log-density + 8 latents (fp16) */
-    short row_of[64][8];          /* row index of (ray, step) or -1 */
-    int red[4];
-};
-
-/* One depth brick per alive tile: sample_cache_init_first_kernel (search),
- * sample_cache_init_second_kernel (samples), inferenceLatents, and the
- * density-only compositing of accumulateNew_cache_init_second_kernel
- * (src/cache_renderer.cu:83-528).  The brick's voxels go to a staging area
- * indexed by the tile's position in the alive list; slots are assigned by
- * cache_assign_kernel afterwards. */
-__global__ void __launch_bounds__(64) cache_tile_kernel(CacheBuildParams p)
+/* The blockwise cache build (CacheRenderer::initCacheBlockwise,
+ * src/cache_renderer.cu:931-1051) as a wavefront per depth-brick iteration:
+ *   cache_search_kernel    per alive tile: the next depth brick holding an
+ *                          occupied sample, its samples appended to a row list
+ *                          (sample_cache_init_first/second_kernel :83-287);
+ *   cache_density_kernel   the density network on all rows of the iteration
+ *                          (inferenceLatents), warp-level tensor-core MLP;
+ *   cache_composite_kernel per processed tile: density-only compositing and
+ *                          the brick's 512 voxels into the staging area
+ *                          (accumulateNew_cache_init_second_kernel :289-528);
+ * then cache_assign_kernel / cache_copy_kernel give bricks their slots. */
+__device__ __forceinline__ int tile_block_sum(int v, int *red)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    BuildSmem &S = *reinterpret_cast<BuildSmem *>(smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int w = __reduce_add_sync(FULL, (unsigned)v);
+    __syncthreads();
+    if (lane == 0) red[wid] = w;
+    __syncthreads();
+    return red[0] + red[1];
+}
+
+__global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
+{
+    __shared__ int red[4];
+    __shared__ int row_base;
     const int k = threadIdx.x, lane = k & 31, wid = k >> 5;
-    for (int i = k; i < W_L3; i += 64) S.W[i] = p.weights[i];
     const int n_alive_tiles = *p.n_alive_tiles;
     for (int ai = blockIdx.x; ai < n_alive_tiles; ai += gridDim.x) {
         __syncthreads();
         const int tile = p.alive_list[ai];
         CacheRay cr = p.rays[(size_t)tile * 64 + k];
         int bstep = p.block_step[tile];
-        auto block_sum = [&](int v) -> int {
-            const int w = __reduce_add_sync(FULL, (unsigned)v);
-            __syncthreads();
-            if (lane == 0) S.red[wid] = w;
-            __syncthreads();
-            return S.red[0] + S.red[1];
-        };
-        /* ---- search for the next depth brick with an occupied sample ---- */
         int total = 0;
         uint32_t mask = 0;
         for (int guard = 0; guard < p.max_search; ++guard) {
-            if (block_sum(cr.alive) <= 0) break;
+            if (tile_block_sum(cr.alive, red) <= 0) break;
             if (bstep >= p.bZ) { cr.alive = 0; total = 0; break; } /* beyond the frustum depth: stop the tile */
-            const float t1s = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
-            float t1 = t1s;
+            float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
             mask = 0;
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
@@ -174,12 +171,12 @@ __global__ void __launch_bounds__(64) cache_tile_kernel(CacheBuildParams p)
                 if (tm > cr.far_) cr.alive = 0;
                 else if (occupied(p.scene, p.bits, at(cr.o, cr.d, tm))) mask |= 1u << s;
             }
-            total = block_sum(__popc(mask));
+            total = tile_block_sum(__popc(mask), red);
             if (total > 0) break;
             ++bstep;
             if (guard == p.max_search - 1) atomicOr(p.guard, 4);
         }
-        const int n_alive = block_sum(cr.alive);
+        const int n_alive = tile_block_sum(cr.alive, red);
         const bool processed = total > 0 && n_alive > 0;
         if (k == 0) {
             p.tile_n_samples[ai] = total;
@@ -187,11 +184,9 @@ __global__ void __launch_bounds__(64) cache_tile_kernel(CacheBuildParams p)
             p.tile_alive[tile] = n_alive > 0;
             p.block_step[tile] = bstep;
         }
-        if (!processed) {
-            p.rays[(size_t)tile * 64 + k] = cr;
-            continue;
-        }
-        /* ---- emit samples (compact over the tile) ---- */
+        p.rays[(size_t)tile * 64 + k] = cr;
+        if (!processed) continue;
+        /* append the brick's samples to the iteration's rows, in (ray, step) order */
         const int cnt = __popc(mask);
         int incl = cnt;
 #pragma unroll
@@ -199,50 +194,79 @@ __global__ void __launch_bounds__(64) cache_tile_kernel(CacheBuildParams p)
             const int v = __shfl_up_sync(FULL, incl, off);
             if (lane >= off) incl += v;
         }
-        if (lane == 31) S.red[2 + wid] = incl;
+        if (lane == 31) red[2 + wid] = incl;
+        if (k == 0) row_base = atomicAdd(p.build_row_counter, total);
         __syncthreads();
-        int base = incl - cnt + (wid ? S.red[2] : 0);
-        {
-            float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
+        int row = row_base + incl - cnt + (wid ? red[2] : 0);
+        int *rof = p.build_row_of + (size_t)ai * 512;
+        float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
 #pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                const float t0 = t1;
-                const float dt = calc_step(p.steps, t0);
-                t1 = F_ADD(t0, dt);
-                const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
-                if ((mask >> s) & 1u) {
-                    const float3 cp = contract(p.scene, at(cr.o, cr.d, tm));
-                    S.rows[base] = make_float4(cp.x, cp.y, cp.z, __int_as_float(k | (s << 6)));
-                    S.row_of[k][s] = (short)base;
-                    ++base;
-                } else {
-                    S.row_of[k][s] = -1;
-                }
-            }
-        }
-        __syncthreads();
-        /* ---- density network on 32-row batches (warp w: batches w, w+2, ...) ---- */
-        __half *tile_w = S.tile[wid];
-        for (int b = wid * 32; b < total; b += 64) {
-            const int r = b + lane;
-            __half *trow = tile_w + lane * TILE_STRIDE;
-            if (r < total) {
-                const float4 rw = S.rows[r];
-                hash_encode(p.grid, p.table, make_float3(rw.x, rw.y, rw.z), reinterpret_cast<__half2 *>(trow));
+        for (int s = 0; s < 8; ++s) {
+            const float t0 = t1;
+            const float dt = calc_step(p.steps, t0);
+            t1 = F_ADD(t0, dt);
+            const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
+            if ((mask >> s) & 1u) {
+                const float3 cp = contract(p.scene, at(cr.o, cr.d, tm));
+                p.build_rows[row] = make_float4(cp.x, cp.y, cp.z, 0.f);
+                rof[s * 64 + k] = row++;
             } else {
-                for (int c = 0; c < 16; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
+                rof[s * 64 + k] = -1;
             }
-            __syncwarp();
-            density_mlp(tile_w, S.W, lane);
-            if (r < total) {
-                S.out[r][0] = trow[16];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) S.out[r][1 + j] = trow[16 + p.latent_offset + j];
-            }
-            __syncwarp();
         }
-        __syncthreads();
-        /* ---- density-only compositing (accumulateNew_cache_init_second_kernel :349-393) ---- */
+    }
+}
+
+/* density network on every row of the iteration: log-density and the 8
+ * latents (fp16, as NerfNetwork::inferenceLatents stores them) */
+__global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
+{
+    __shared__ uint2 Wsm[W_L3];
+    __shared__ __align__(16) __half tiles[4][32 * TILE_STRIDE];
+    for (int i = threadIdx.x; i < W_L3; i += blockDim.x) Wsm[i] = p.weights[i];
+    __syncthreads();
+    const int n = *p.build_row_counter;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __half *tile = tiles[w];
+    __half *trow = tile + lane * TILE_STRIDE;
+    const int lo = p.latent_offset;
+    for (int b = blockIdx.x * 4 + w; b < (n + 31) / 32; b += gridDim.x * 4) {
+        const int r = b * 32 + lane;
+        if (r < n) {
+            const float4 rw = p.build_rows[r];
+            hash_encode(p.grid, p.table, make_float3(rw.x, rw.y, rw.z), reinterpret_cast<__half2 *>(trow));
+        } else {
+            for (int c = 0; c < 16; ++c) reinterpret_cast<uint32_t *>(trow)[c] = 0u;
+        }
+        __syncwarp();
+        density_mlp(tile, Wsm, lane);
+        if (r < n) {
+            p.build_den[r] = trow[16];
+            uint32_t lw[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                lw[q] = (uint32_t)__half_as_ushort(trow[16 + lo + 2 * q]) | ((uint32_t)__half_as_ushort(trow[17 + lo + 2 * q]) << 16);
+            p.build_lat[r] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(64) cache_composite_kernel(CacheBuildParams p)
+{
+    __shared__ int red[4];
+    const int k = threadIdx.x;
+    const int n_alive_tiles = *p.n_alive_tiles;
+    for (int ai = blockIdx.x; ai < n_alive_tiles; ai += gridDim.x) {
+        if (!p.tile_processed[ai]) continue; /* uniform over the block */
+        const int tile = p.alive_list[ai];
+        CacheRay cr = p.rays[(size_t)tile * 64 + k];
+        const int bstep = p.block_step[tile];
+        const int *rof = p.build_row_of + (size_t)ai * 512;
+        int rows[8];
+#pragma unroll
+        for (int s = 0; s < 8; ++s) rows[s] = rof[s * 64 + k];
+        /* density-only compositing (accumulateNew_cache_init_second_kernel :349-393) */
         int visible = 0;
         {
             float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
@@ -254,36 +278,31 @@ __global__ void __launch_bounds__(64) cache_tile_kernel(CacheBuildParams p)
                 t1 = F_ADD(t0, dt);
                 const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
                 if (tm > cr.far_) { cr.alive = 0; continue; }
-                if (!((mask >> s) & 1u)) continue;
-                const float sigma = expf(__half2float(S.out[S.row_of[k][s]][0]));
+                if (rows[s] < 0) continue;
+                const float sigma = expf(__half2float(p.build_den[rows[s]]));
                 const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
                 if (alpha > p.scene.alpha_thre) { T *= 1.0f - alpha; ++visible; }
                 if (T < 1e-4f) cr.alive = 0;
             }
             cr.T = T;
         }
-        const int n_visible = block_sum(visible);
-        const int n_alive_post = block_sum(cr.alive);
+        const int n_visible = tile_block_sum(visible, red);
+        const int n_alive_post = tile_block_sum(cr.alive, red);
         if (k == 0) {
             p.tile_need[ai] = n_visible > 0;
             p.tile_n_alive[ai] = n_alive_post;
         }
         p.rays[(size_t)tile * 64 + k] = cr;
-        /* ---- staging: all 512 voxels of the brick (zeros where no sample) ---- */
+        /* staging: all 512 voxels of the brick (zeros where no sample) */
         if (n_visible > 0) {
             Voxel *st = reinterpret_cast<Voxel *>(p.staging) + (size_t)ai * 512;
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
                 Voxel v;
-                const int r = S.row_of[k][s];
-                if (r >= 0) {
-                    v.density = expf(__half2float(S.out[r][0]));
+                if (rows[s] >= 0) {
+                    v.density = expf(__half2float(p.build_den[rows[s]]));
                     v.isset = 1.0f;
-                    uint32_t lw[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        lw[q] = (uint32_t)__half_as_ushort(S.out[r][1 + 2 * q]) | ((uint32_t)__half_as_ushort(S.out[r][2 + 2 * q]) << 16);
-                    v.lat = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                    v.lat = p.build_lat[rows[s]];
                 } else {
                     v.density = 0.f; v.isset = 0.f; v.lat = make_uint4(0, 0, 0, 0);
                 }
@@ -291,10 +310,9 @@ __global__ void __launch_bounds__(64) cache_tile_kernel(CacheBuildParams p)
                 st[s * 64 + k] = v;
             }
         }
+        __syncthreads();
     }
 }
-
-size_t build_smem_bytes() { return sizeof(BuildSmem); }
 
 /* Exclusive scan over a 1024-thread block; *total receives the block sum.
  * s_w must hold 33 ints. */

@@ -186,9 +186,14 @@ struct CacheBuildParams {
     int *n_jobs;
     int *guard;
     int max_search;
+    /* rows of one build iteration (capacity: tiles x 512) */
+    float4 *build_rows;         /* contracted sample position */
+    __half *build_den;          /* log-density (fp16) */
+    uint4 *build_lat;           /* 8 latents (fp16) */
+    int *build_row_of;          /* [alive idx][step][ray]: row or -1 */
+    int *build_row_counter;
 };
 
-size_t build_smem_bytes();
 /* One frame: ray generation, then sub-iterations of march / network /
  * compositing until no ray is alive.  Reads the alive count back every
  * `check_every` sub-iterations through h_pinned (page-locked, >= 1 int). */
@@ -224,7 +229,9 @@ cudaError_t launch_grad_finalize(float *scratch, float *out, size_t n, float inv
 cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
 
 __global__ void cache_init_kernel(CacheBuildParams p);
-__global__ void cache_tile_kernel(CacheBuildParams p);
+__global__ void cache_search_kernel(CacheBuildParams p);
+__global__ void cache_density_kernel(CacheBuildParams p);
+__global__ void cache_composite_kernel(CacheBuildParams p);
 __global__ void cache_assign_kernel(CacheBuildParams p);
 __global__ void cache_copy_kernel(CacheBuildParams p);
 __global__ void cache_known_ranges_kernel(CacheBuildParams p);

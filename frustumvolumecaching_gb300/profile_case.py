@@ -1,6 +1,7 @@
 """A small, fixed rendering case for kernel profiles.
 
     python -m frustumvolumecaching_gb300.profile_case --res 960x540 --frames 2 --path plain --network tc
+    python -m frustumvolumecaching_gb300.profile_case --res 400x400 --frames 2 --path backward --rays 65536
 
 Renders `frames` frames of the benchmark's camera path (the synthetic
 3-cascade, 2^19-entry scene) at the given resolution through the C ABI and
@@ -26,10 +27,13 @@ def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--res", default="960x540")
     ap.add_argument("--frames", type=int, default=2)
-    ap.add_argument("--path", choices=["plain", "cached"], default="plain")
+    ap.add_argument("--path", choices=["plain", "cached", "backward"], default="plain")
     ap.add_argument("--network", choices=["tc", "mma"], default="tc")
+    ap.add_argument("--rays", type=int, default=1 << 16, help="rays per backward step")
     args = ap.parse_args(argv)
     W, H = (int(v) for v in args.res.lower().split("x"))
+    if args.path == "backward":
+        return backward_case(args, W, H)
     spec = fmodel.spec_config2()
     loader = load_data(fmodel.ensure_model(spec))
     cams = fcam.rotation_path(spec.seed, n_frames=args.frames, width=W, height=H)
@@ -67,6 +71,37 @@ def main(argv=None) -> None:
                 line["build_launches"] = build.n_launches
                 line["bricks_demanded"] = build.n_bricks_demanded
         print(json.dumps(line), flush=True)
+
+
+def backward_case(args, W: int, H: int) -> None:
+    """`frames` steps of the differentiable render on the config-5 model pair:
+    random rays of a WxH view against the second network's image."""
+    import numpy as np
+    import torch
+
+    from .renderer import Gradients
+
+    spec = fmodel.spec_config5()
+    train = load_data(fmodel.ensure_model(spec))
+    target_net = load_data(fmodel.ensure_model(fmodel.spec_config5(target=True)))
+    cam = fcam.seeded_camera(spec.seed, width=W, height=H)
+    pix = np.random.default_rng(spec.seed).choice(W * H, min(args.rays, W * H), replace=False).astype(np.int32)
+    tr = PerformanceRenderer(target_net.scene_info, target_net.occupancy_grid_morton_bitfield, target_net.nerf_network)
+    full = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    tr.render_device(raymarch_info(cam, target_net.stepsize_info), results=full)
+    tr.synchronize()
+    pixels = torch.from_numpy(pix).cuda()
+    flat = full.reshape(-1, 4)[pixels.long()]
+    target = (flat[:, :3] + flat[:, 3:4]).contiguous()
+    r = PerformanceRenderer(train.scene_info, train.occupancy_grid_morton_bitfield, train.nerf_network)
+    r.set_network_path(args.network == "tc")
+    g = Gradients(train.nerf_network)
+    info = raymarch_info(cam, train.stepsize_info)
+    for i in range(args.frames):
+        loss = r.render_backward(info, pixels, target, g)
+        st = r._render_stats
+        print(json.dumps({"step": i, "rays": int(pix.size), "loss": loss, "samples": st.n_samples,
+                          "launches": st.n_launches}), flush=True)
 
 
 if __name__ == "__main__":
