@@ -324,7 +324,21 @@ def run_backward_bench(args, torch, dev, stream) -> dict:
         times.append(a.elapsed_time(b))
         launches += r._render_stats.n_launches
     ms = sum(times) / len(times)
+    # the same step with BF16 MLPs
+    r.set_precision(fvc.PerformanceRenderer.BF16)
+    r.render_backward(info, pixels, target, grads)
+    bf = []
+    for _ in range(args.steps):
+        a, b = ev(), ev()
+        a.record(stream)
+        loss_bf16 = r.render_backward(info, pixels, target, grads)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        bf.append(a.elapsed_time(b))
+    r.set_precision(fvc.PerformanceRenderer.FP16)
+    ms_bf = sum(bf) / len(bf)
     out = {"value": BWD_RAYS / (ms / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms, "rays_per_step": BWD_RAYS,
+           "bf16": {"value": BWD_RAYS / (ms_bf / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms_bf, "loss": loss_bf16},
            "resolution": list(BWD_RES), "loss": loss, "gpu_launches": launches // max(1, args.steps),
            "workload": "c5 differentiable plain render: forward + adjoint (hash table, both MLPs), fp16 MLP",
            "dtype": "f16 MLP (fp32 accumulate, loss-scaled fp16 gradient tiles), f32 compositing and gradients"}

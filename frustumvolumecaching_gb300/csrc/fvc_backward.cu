@@ -8,8 +8,8 @@
  * white-background pixel (C + T, writeImageBuffer_performance_kernel,
  * src/performance_renderer.cu:127-149).
  *
- * Network backward, one warp per 32 rows (mma.sync m16n8k16, fp16 operands,
- * fp32 accumulation): the forward activations of the rows (hash features,
+ * Network backward, one warp per 32 rows (mma.sync m16n8k16, fp16 or bf16
+ * operands like the forward MLP, fp32 accumulation): the forward activations of the rows (hash features,
  * density hidden layer, head input [latents | SH | 1-padding], head hidden
  * layers) are recomputed into shared memory; the gradient tile then walks
  * back through the layers.  Input gradients are tile x weight-pack products;
@@ -25,12 +25,41 @@
  */
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "fvc_kernels.h"
 
 namespace fvc {
 
 constexpr unsigned FULLMASK = 0xffffffffu;
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+/* the 16-bit element type of the MLP: fp16 (PREC 0) or bf16 (PREC 1); tiles
+ * hold raw 16-bit values */
+template <int PREC> struct E16;
+template <> struct E16<0> {
+    static __device__ __forceinline__ uint32_t pack(float a, float b) { return pack_h2(a, b); }
+    static __device__ __forceinline__ float2 unpack(uint32_t v) { return __half22float2(*reinterpret_cast<__half2 *>(&v)); }
+    static __device__ __forceinline__ uint16_t one(float v) { return __half_as_ushort(__float2half_rn(v)); }
+    static __device__ __forceinline__ float flt(uint16_t v) { return __half2float(__ushort_as_half(v)); }
+    static __device__ __forceinline__ void mma(float (&c)[4], const uint32_t (&a)[4], uint2 b) { mma16816(c, a, b); }
+};
+template <> struct E16<1> {
+    static __device__ __forceinline__ uint32_t pack(float a, float b)
+    {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+    static __device__ __forceinline__ float2 unpack(uint32_t v) { return __bfloat1622float2(*reinterpret_cast<__nv_bfloat162 *>(&v)); }
+    static __device__ __forceinline__ uint16_t one(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
+    static __device__ __forceinline__ float flt(uint16_t v) { return __bfloat162float(__ushort_as_bfloat16(v)); }
+    static __device__ __forceinline__ void mma(float (&c)[4], const uint32_t (&a)[4], uint2 b)
+    {
+        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                     : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                     : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+    }
+};
 
 constexpr int BW_WARPS = 8; /* 8 x 23.5 KB of row tiles + 40 KB of dW: one CTA of 8 warps per SM */
 constexpr int S32 = 40;  /* tile strides in halfs: 80 B and 144 B rows, 16-byte aligned for ldmatrix */
@@ -39,12 +68,12 @@ constexpr int DF_STRIDE = 36; /* fp32 feature-gradient rows (aliases the A3 tile
 constexpr int DW_FLOATS = GB_BASE + 64 * 32 + 64 * 64 + 16 * 64;
 
 struct __align__(16) BwdWarp {
-    __half F[32 * S32];   /* hash features */
-    __half H1[32 * S64];  /* density hidden layer (ReLU) */
-    __half IN[32 * S32];  /* head input: latents 0..7, SH 8..23, 1.0 at 24..31 */
-    __half A3[32 * S64];  /* head hidden 1; later the fp32 feature gradients */
-    __half A4[32 * S64];  /* head hidden 2 */
-    __half G[32 * S64];   /* the gradient tile walking back */
+    uint16_t F[32 * S32];   /* hash features */
+    uint16_t H1[32 * S64];  /* density hidden layer (ReLU) */
+    uint16_t IN[32 * S32];  /* head input: latents 0..7, SH 8..23, 1.0 at 24..31 */
+    uint16_t A3[32 * S64];  /* head hidden 1; later the fp32 feature gradients */
+    uint16_t A4[32 * S64];  /* head hidden 2 */
+    uint16_t G[32 * S64];   /* the gradient tile walking back */
 };
 
 struct __align__(16) BwdSmem {
@@ -52,11 +81,11 @@ struct __align__(16) BwdSmem {
     BwdWarp w[BW_WARPS];
 };
 
-__device__ __forceinline__ void lda_tile(const __half *t, int stride, int m0, int k0, int lane, uint32_t (&a)[4])
+__device__ __forceinline__ void lda_tile(const uint16_t *t, int stride, int m0, int k0, int lane, uint32_t (&a)[4])
 {
     const int g = lane >> 2, q = lane & 3;
-    const __half *r0 = t + (m0 + g) * stride + k0 + 2 * q;
-    const __half *r1 = r0 + 8 * stride;
+    const uint16_t *r0 = t + (m0 + g) * stride + k0 + 2 * q;
+    const uint16_t *r1 = r0 + 8 * stride;
     a[0] = *reinterpret_cast<const uint32_t *>(r0);
     a[1] = *reinterpret_cast<const uint32_t *>(r1);
     a[2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
@@ -64,8 +93,8 @@ __device__ __forceinline__ void lda_tile(const __half *t, int stride, int m0, in
 }
 
 /* c[32 x N] = A[32 x K] (shared tile) * B (fragment pack, N/8 n-tiles x K/16 k-steps) */
-template <int K, int N>
-__device__ __forceinline__ void warp_mm(const __half *A, int sa, const uint2 *__restrict__ Bp, int lane, float (&c)[2][N / 8][4])
+template <int PREC, int K, int N>
+__device__ __forceinline__ void warp_mm(const uint16_t *A, int sa, const uint2 *__restrict__ Bp, int lane, float (&c)[2][N / 8][4])
 {
 #pragma unroll
     for (int m = 0; m < 2; ++m)
@@ -79,8 +108,8 @@ __device__ __forceinline__ void warp_mm(const __half *A, int sa, const uint2 *__
 #pragma unroll
         for (int j = 0; j < N / 8; ++j) {
             const uint2 b = __ldg(&Bp[(j * (K / 16) + s) * 32 + lane]);
-            mma16816(c[0][j], a0, b);
-            mma16816(c[1][j], a1, b);
+            E16<PREC>::mma(c[0][j], a0, b);
+            E16<PREC>::mma(c[1][j], a1, b);
         }
     }
 }
@@ -88,9 +117,9 @@ __device__ __forceinline__ void warp_mm(const __half *A, int sa, const uint2 *__
 __device__ __forceinline__ float clamp_h(float v) { return fminf(fmaxf(v, -65000.f), 65000.f); }
 
 /* c -> fp16 tile; mode 0 as is, 1 ReLU, 2 zero where the mask tile is not > 0 */
-template <int N>
-__device__ __forceinline__ void st_tile(__half *T, int st, const float (&c)[2][N / 8][4], int lane, int mode,
-                                        const __half *M = nullptr, int sm = 0)
+template <int PREC, int N>
+__device__ __forceinline__ void st_tile(uint16_t *T, int st, const float (&c)[2][N / 8][4], int lane, int mode,
+                                        const uint16_t *M = nullptr, int sm = 0)
 {
     const int g = lane >> 2, q = lane & 3;
 #pragma unroll
@@ -103,15 +132,15 @@ __device__ __forceinline__ void st_tile(__half *T, int st, const float (&c)[2][N
                 float v0 = c[m][j][2 * h], v1 = c[m][j][2 * h + 1];
                 if (mode == 1) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
                 if (mode == 2) {
-                    const float2 mk = __half22float2(*reinterpret_cast<const __half2 *>(M + row * sm + col));
+                    const float2 mk = E16<PREC>::unpack(*reinterpret_cast<const uint32_t *>(M + row * sm + col));
                     if (!(mk.x > 0.f)) v0 = 0.f;
                     if (!(mk.y > 0.f)) v1 = 0.f;
                 }
-                *reinterpret_cast<uint32_t *>(T + row * st + col) = pack_h2(clamp_h(v0), clamp_h(v1));
+                *reinterpret_cast<uint32_t *>(T + row * st + col) = E16<PREC>::pack(clamp_h(v0), clamp_h(v1));
             }
 }
 
-__device__ __forceinline__ void ldsm4t(uint32_t (&r)[4], const __half *p)
+__device__ __forceinline__ void ldsm4t(uint32_t (&r)[4], const uint16_t *p)
 {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
@@ -125,8 +154,8 @@ __device__ __forceinline__ int dw_col(int row, int col) { return col ^ ((row & 7
 
 /* dW (O x I, row-major fp32, shared, swizzled) += G^T X over the warp's 32
  * rows; G: 32 x O, X: 32 x I, both fp16 shared tiles. */
-template <int O, int I>
-__device__ __forceinline__ void warp_dw(const __half *G, int sg, const __half *X, int sx, float *dW, int lane)
+template <int PREC, int O, int I>
+__device__ __forceinline__ void warp_dw(const uint16_t *G, int sg, const uint16_t *X, int sx, float *dW, int lane)
 {
     const int g = lane >> 2, q = lane & 3;
 #pragma unroll
@@ -142,8 +171,8 @@ __device__ __forceinline__ void warp_dw(const __half *G, int sg, const __half *X
             for (int s = 0; s < 2; ++s) {
                 uint32_t b[4];
                 ldsm4t(b, X + (16 * s + (lane & 7) + ((lane >> 3) & 1) * 8) * sx + 8 * (nt + (lane >> 4)));
-                mma16816(d[0], a[s], make_uint2(b[0], b[1]));
-                mma16816(d[1], a[s], make_uint2(b[2], b[3]));
+                E16<PREC>::mma(d[0], a[s], make_uint2(b[0], b[1]));
+                E16<PREC>::mma(d[1], a[s], make_uint2(b[2], b[3]));
             }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -198,7 +227,7 @@ __device__ __forceinline__ float3 row_dir01(const RayState *states, int slot)
     return make_float3((d.x + 1.0f) / 2.0f, (d.y + 1.0f) / 2.0f, (d.z + 1.0f) / 2.0f);
 }
 
-template <int HH>
+template <int PREC, int HH>
 __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderParams p, BwdParams b, int it)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -213,8 +242,9 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
     const RayState *states = p.states[it & 1];
     const int lo = p.latent_offset;
     const int n_tiles = (n_rows + 31) / 32;
-    __half *inr = W.IN + lane * S32;
-    __half *gr = W.G + lane * S64;
+    uint16_t *inr = W.IN + lane * S32;
+    uint16_t *gr = W.G + lane * S64;
+    using T16 = E16<PREC>;
     for (int tile = blockIdx.x * BW_WARPS + warp; tile < n_tiles; tile += gridDim.x * BW_WARPS) {
         const int k = tile * 32 + lane;
         const int r = k < n_rows ? p.res_list[k] : -1;
@@ -233,23 +263,30 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
         /* ---- forward recomputation ---- */
         __half2 feat[16];
         hash_encode<4>(p.grid, p.table, pos, feat);
+        uint32_t *fr = reinterpret_cast<uint32_t *>(W.F + lane * S32);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) reinterpret_cast<uint4 *>(W.F + lane * S32)[c] = reinterpret_cast<const uint4 *>(feat)[c];
+        for (int q = 0; q < 16; ++q) {
+            const float2 f = __half22float2(feat[q]);
+            fr[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&feat[q]) : T16::pack(f.x, f.y);
+        }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) reinterpret_cast<__half2 *>(inr + 8)[q] = sh[q];
+        for (int q = 0; q < 8; ++q) {
+            const float2 f = __half22float2(sh[q]);
+            reinterpret_cast<uint32_t *>(inr + 8)[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&sh[q]) : T16::pack(f.x, f.y);
+        }
 #pragma unroll
-        for (int q = 24; q < 32; ++q) inr[q] = __float2half_rn(1.0f);
+        for (int q = 24; q < 32; ++q) inr[q] = T16::one(1.0f);
         __syncwarp();
         {
             float c[2][8][4];
-            warp_mm<32, 64>(W.F, S32, b.w + BW_F1, lane, c);
-            st_tile<64>(W.H1, S64, c, lane, 1);
+            warp_mm<PREC, 32, 64>(W.F, S32, b.w + BW_F1, lane, c);
+            st_tile<PREC, 64>(W.H1, S64, c, lane, 1);
         }
         __syncwarp();
         {
             float c[2][2][4];
-            warp_mm<64, 16>(W.H1, S64, b.w + BW_F2, lane, c);
-            st_tile<16>(W.G, S64, c, lane, 0);
+            warp_mm<PREC, 64, 16>(W.H1, S64, b.w + BW_F2, lane, c);
+            st_tile<PREC, 16>(W.G, S64, c, lane, 0);
         }
         __syncwarp();
 #pragma unroll
@@ -257,49 +294,49 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
         __syncwarp();
         {
             float c[2][8][4];
-            warp_mm<32, 64>(W.IN, S32, b.w + BW_F3, lane, c);
-            st_tile<64>(W.A3, S64, c, lane, 1);
+            warp_mm<PREC, 32, 64>(W.IN, S32, b.w + BW_F3, lane, c);
+            st_tile<PREC, 64>(W.A3, S64, c, lane, 1);
         }
         __syncwarp();
-        const __half *last = W.A3;
+        const uint16_t *last = W.A3;
         if (HH == 2) {
             float c[2][8][4];
-            warp_mm<64, 64>(W.A3, S64, b.w + BW_F4, lane, c);
-            st_tile<64>(W.A4, S64, c, lane, 1);
+            warp_mm<PREC, 64, 64>(W.A3, S64, b.w + BW_F4, lane, c);
+            st_tile<PREC, 64>(W.A4, S64, c, lane, 1);
             __syncwarp();
             last = W.A4;
         }
         /* ---- backward: output layer ---- */
-        gr[0] = __float2half_rn(clamp_h(dout.x));
-        gr[1] = __float2half_rn(clamp_h(dout.y));
-        gr[2] = __float2half_rn(clamp_h(dout.z));
+        gr[0] = T16::one(clamp_h(dout.x));
+        gr[1] = T16::one(clamp_h(dout.y));
+        gr[2] = T16::one(clamp_h(dout.z));
 #pragma unroll
-        for (int q = 3; q < 16; ++q) gr[q] = __float2half_rn(0.f);
+        for (int q = 3; q < 16; ++q) gr[q] = 0;
         __syncwarp();
-        warp_dw<16, 64>(W.G, S64, last, S64, dWh + b.head_w5, lane);
+        warp_dw<PREC, 16, 64>(W.G, S64, last, S64, dWh + b.head_w5, lane);
         {
             float c[2][8][4];
-            warp_mm<16, 64>(W.G, S64, b.w + BW_B5, lane, c);
+            warp_mm<PREC, 16, 64>(W.G, S64, b.w + BW_B5, lane, c);
             __syncwarp();
-            st_tile<64>(W.G, S64, c, lane, 2, last, S64);
+            st_tile<PREC, 64>(W.G, S64, c, lane, 2, last, S64);
         }
         __syncwarp();
         if (HH == 2) {
-            warp_dw<64, 64>(W.G, S64, W.A3, S64, dWh + GH_W4, lane);
+            warp_dw<PREC, 64, 64>(W.G, S64, W.A3, S64, dWh + GH_W4, lane);
             float c[2][8][4];
-            warp_mm<64, 64>(W.G, S64, b.w + BW_B4, lane, c);
+            warp_mm<PREC, 64, 64>(W.G, S64, b.w + BW_B4, lane, c);
             __syncwarp();
-            st_tile<64>(W.G, S64, c, lane, 2, W.A3, S64);
+            st_tile<PREC, 64>(W.G, S64, c, lane, 2, W.A3, S64);
             __syncwarp();
         }
         /* ---- head layer 1: G = dA3 ---- */
-        warp_dw<64, 32>(W.G, S64, W.IN, S32, dWh + GH_W3, lane);
+        warp_dw<PREC, 64, 32>(W.G, S64, W.IN, S32, dWh + GH_W3, lane);
         float dl[2][1][4];
-        warp_mm<64, 8>(W.G, S64, b.w + BW_B3, lane, dl); /* d latents = head-input cols 0..7 */
+        warp_mm<PREC, 64, 8>(W.G, S64, b.w + BW_B3, lane, dl); /* d latents = head-input cols 0..7 */
         __syncwarp();
         /* ---- density network: G = d(out2) ---- */
 #pragma unroll
-        for (int q = 0; q < 16; ++q) gr[q] = __float2half_rn(0.f);
+        for (int q = 0; q < 16; ++q) gr[q] = 0;
         __syncwarp();
         {
             const int g = lane >> 2, q = lane & 3;
@@ -307,27 +344,27 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
             for (int m = 0; m < 2; ++m)
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    __half *d = W.G + (16 * m + g + 8 * h) * S64 + lo + 2 * q;
-                    d[0] = __float2half_rn(clamp_h(dl[m][0][2 * h]));
-                    d[1] = __float2half_rn(clamp_h(dl[m][0][2 * h + 1]));
+                    uint16_t *d = W.G + (16 * m + g + 8 * h) * S64 + lo + 2 * q;
+                    d[0] = T16::one(clamp_h(dl[m][0][2 * h]));
+                    d[1] = T16::one(clamp_h(dl[m][0][2 * h + 1]));
                 }
         }
         __syncwarp();
-        gr[0] = __float2half_rn(clamp_h(__half2float(gr[0]) + dout.w));
+        gr[0] = T16::one(clamp_h(T16::flt(gr[0]) + dout.w));
         __syncwarp();
-        warp_dw<16, 64>(W.G, S64, W.H1, S64, dWb + GB_W2, lane);
+        warp_dw<PREC, 16, 64>(W.G, S64, W.H1, S64, dWb + GB_W2, lane);
         {
             float c[2][8][4];
-            warp_mm<16, 64>(W.G, S64, b.w + BW_B2, lane, c);
+            warp_mm<PREC, 16, 64>(W.G, S64, b.w + BW_B2, lane, c);
             __syncwarp();
-            st_tile<64>(W.G, S64, c, lane, 2, W.H1, S64);
+            st_tile<PREC, 64>(W.G, S64, c, lane, 2, W.H1, S64);
         }
         __syncwarp();
-        warp_dw<64, 32>(W.G, S64, W.F, S32, dWb + GB_W1, lane);
+        warp_dw<PREC, 64, 32>(W.G, S64, W.F, S32, dWb + GB_W1, lane);
         float *dF = reinterpret_cast<float *>(W.A3);
         {
             float c[2][4][4];
-            warp_mm<64, 32>(W.G, S64, b.w + BW_B1, lane, c);
+            warp_mm<PREC, 64, 32>(W.G, S64, b.w + BW_B1, lane, c);
             const int g = lane >> 2, q = lane & 3;
 #pragma unroll
             for (int m = 0; m < 2; ++m)
@@ -396,13 +433,21 @@ cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int h
     static bool attrs = false;
     const int smem = (int)sizeof(BwdSmem);
     if (!attrs) {
-        cudaError_t e = cudaFuncSetAttribute(wf_net_bwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = cudaFuncSetAttribute(wf_net_bwd_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         attrs = true;
     }
-    if (head_hidden == 2) wf_net_bwd_kernel<2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
-    else wf_net_bwd_kernel<1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
+    const bool bf16 = p.precision == 1;
+    if (head_hidden == 2) {
+        if (bf16) wf_net_bwd_kernel<1, 2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
+        else wf_net_bwd_kernel<0, 2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
+    } else {
+        if (bf16) wf_net_bwd_kernel<1, 1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
+        else wf_net_bwd_kernel<0, 1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
+    }
     return cudaGetLastError();
 }
 

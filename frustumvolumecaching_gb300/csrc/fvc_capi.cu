@@ -1251,14 +1251,15 @@ struct fvc_grad {
     size_t n_table = 0, n_base = 0, n_head = 0;
     float *d_table = nullptr, *d_base = nullptr, *d_head = nullptr; /* dL/dparam, accumulated */
     float *s_table = nullptr, *s_base = nullptr, *s_head = nullptr; /* loss-scaled, one call */
-    uint2 *d_w = nullptr;                                           /* BW_TOTAL weight packs */
+    uint2 *d_w = nullptr;                                           /* BW_TOTAL weight packs, fp16 */
+    uint2 *d_w_bf16 = nullptr;                                      /* the same in bf16 */
     float4 *d_ray_grad = nullptr;
     int ray_cap = 0;
     double *d_loss = nullptr;
     ~fvc_grad()
     {
         dfree(d_table); dfree(d_base); dfree(d_head); dfree(s_table); dfree(s_base); dfree(s_head);
-        dfree(d_w); dfree(d_ray_grad); dfree(d_loss);
+        dfree(d_w); dfree(d_w_bf16); dfree(d_ray_grad); dfree(d_loss);
     }
 };
 
@@ -1296,26 +1297,38 @@ extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
             for (int j = 0; j < Cc; ++j) T[(size_t)j * R + i] = W[(size_t)i * Cc + j];
         return T;
     };
-    const std::vector<uint16_t> W1 = slice(m->h_base, 0, 64 * 32), W2 = slice(m->h_base, 64 * 32, 16 * 64);
-    const std::vector<uint16_t> W3 = slice(m->h_head, 0, 64 * 32);
-    const size_t w5 = m->head_hidden == 2 ? 64 * 32 + 64 * 64 : 64 * 32;
-    const std::vector<uint16_t> W5 = slice(m->h_head, w5, 16 * 64);
-    std::vector<uint2> P(BW_TOTAL, make_uint2(0, 0));
-    frag_pack(W1, 64, 32, &P[BW_F1]);
-    frag_pack(W2, 16, 64, &P[BW_F2]);
-    frag_pack(W3, 64, 32, &P[BW_F3]);
-    frag_pack(W5, 16, 64, &P[BW_F5]);
-    frag_pack(transpose(W5, 16, 64), 64, 16, &P[BW_B5]);
-    frag_pack(transpose(W3, 64, 32), 32, 64, &P[BW_B3]);
-    frag_pack(transpose(W2, 16, 64), 64, 16, &P[BW_B2]);
-    frag_pack(transpose(W1, 64, 32), 32, 64, &P[BW_B1]);
-    if (m->head_hidden == 2) {
-        const std::vector<uint16_t> W4 = slice(m->h_head, 64 * 32, 64 * 64);
-        frag_pack(W4, 64, 64, &P[BW_F4]);
-        frag_pack(transpose(W4, 64, 64), 64, 64, &P[BW_B4]);
+    auto bf16_bits = [](const std::vector<uint16_t> &v) { /* fp16 bits -> bf16 bits (round to nearest even) */
+        std::vector<uint16_t> o(v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+            const __nv_bfloat16 b = __float2bfloat16_rn(h2f(v[i]));
+            memcpy(&o[i], &b, 2);
+        }
+        return o;
+    };
+    for (int variant = 0; variant < 2; ++variant) {
+        auto cv = [&](const std::vector<uint16_t> &v) { return variant ? bf16_bits(v) : v; };
+        const std::vector<uint16_t> W1 = cv(slice(m->h_base, 0, 64 * 32)), W2 = cv(slice(m->h_base, 64 * 32, 16 * 64));
+        const std::vector<uint16_t> W3 = cv(slice(m->h_head, 0, 64 * 32));
+        const size_t w5 = m->head_hidden == 2 ? 64 * 32 + 64 * 64 : 64 * 32;
+        const std::vector<uint16_t> W5 = cv(slice(m->h_head, w5, 16 * 64));
+        std::vector<uint2> P(BW_TOTAL, make_uint2(0, 0));
+        frag_pack(W1, 64, 32, &P[BW_F1]);
+        frag_pack(W2, 16, 64, &P[BW_F2]);
+        frag_pack(W3, 64, 32, &P[BW_F3]);
+        frag_pack(W5, 16, 64, &P[BW_F5]);
+        frag_pack(transpose(W5, 16, 64), 64, 16, &P[BW_B5]);
+        frag_pack(transpose(W3, 64, 32), 32, 64, &P[BW_B3]);
+        frag_pack(transpose(W2, 16, 64), 64, 16, &P[BW_B2]);
+        frag_pack(transpose(W1, 64, 32), 32, 64, &P[BW_B1]);
+        if (m->head_hidden == 2) {
+            const std::vector<uint16_t> W4 = cv(slice(m->h_head, 64 * 32, 64 * 64));
+            frag_pack(W4, 64, 64, &P[BW_F4]);
+            frag_pack(transpose(W4, 64, 64), 64, 64, &P[BW_B4]);
+        }
+        uint2 *&dst = variant ? g->d_w_bf16 : g->d_w;
+        if ((rc = dalloc(&dst, P.size(), "backward weights"))) return rc;
+        CU(cudaMemcpy(dst, P.data(), P.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     }
-    if ((rc = dalloc(&g->d_w, P.size(), "backward weights"))) return rc;
-    CU(cudaMemcpy(g->d_w, P.data(), P.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     *out = g.release();
     return FVC_OK;
 }
@@ -1356,8 +1369,8 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     CHECK_ARG(g->m == r->m, "fvc_render_backward: gradients belong to another model");
     if (r->kind == FVC_RENDERER_CACHE_PERFORMANCE)
         return fail(FVC_ERR_CONFIG, "fvc_render_backward: the differentiable render is built for the plain renderers");
-    if (r->precision != FVC_PRECISION_FP16)
-        return fail(FVC_ERR_CONFIG, "fvc_render_backward: the network adjoint is built for FP16 MLPs");
+    if (r->precision == FVC_PRECISION_FP8_E4M3)
+        return fail(FVC_ERR_CONFIG, "fvc_render_backward: the network adjoint is built for FP16 and BF16 MLPs");
     int rc;
     if ((rc = check_info(info))) return rc;
     const long long n_pix = (long long)info->cam_info.resolution.x * info->cam_info.resolution.y;
@@ -1385,7 +1398,7 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     p.row_dout = r->d_row_dout;
     p.res_list = r->d_grad_rows;
     BwdParams b;
-    b.w = g->d_w;
+    b.w = r->precision == FVC_PRECISION_BF16 ? g->d_w_bf16 : g->d_w;
     b.g_table = g->s_table; b.g_base = g->s_base; b.g_head = g->s_head;
     b.head_w5 = m->head_hidden == 2 ? GH_W4 + 64 * 64 : GH_W4;
     b.loss = g->d_loss;

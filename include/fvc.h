@@ -363,7 +363,8 @@ int fvc_grad_sizes(const fvc_grad *g, size_t *n_table, size_t *n_base, size_t *n
 /* copies the accumulated gradients to host arrays (any may be null) */
 int fvc_grad_read(fvc_grad *g, float *table, float *base, float *head);
 
-/* Forward and adjoint of the plain render (renderer kinds BASIC/PERFORMANCE)
+/* Forward and adjoint of the plain render (renderer kinds BASIC/PERFORMANCE;
+ * FP16 or BF16 MLPs per fvc_renderer_set_precision)
  * at n_rays pixels (device int32 y * W + x, at most W * H of the camera):
  * L = mean over the rays of sum_k (C_k + T - target_k)^2, the
  * white-background pixel of writeImageBuffer_performance_kernel

@@ -943,6 +943,41 @@ void hash_backward(const NetD &d, V3 pos, const double *dfeat, double *g_table)
     }
 }
 
+/* head forward from given latents (the cached path's head input) */
+void forward_head_acts(const NetD &d, const double *lat, const float *d01, Acts &A)
+{
+    const OrcNet &n = *d.n;
+    for (int i = 0; i < n.n_latents; ++i) A.in[i] = lat[i];
+    sh16(d01, A.in + n.n_latents);
+    if (n.mimic_fp16) for (int i = n.n_latents; i < n.n_latents + 16; ++i) A.in[i] = round_h(A.in[i]);
+    for (int i = n.head_in; i < n.head_in_pad; ++i) A.in[i] = 1.0;
+    dense_layer(d.hw[0].data(), n.width, n.head_in_pad, A.in, A.hid[0], true, n.mimic_fp16);
+    for (int l = 1; l < n.head_layers - 1; ++l)
+        dense_layer(d.hw[l].data(), n.width, n.width, A.hid[l - 1], A.hid[l], true, n.mimic_fp16);
+    dense_layer(d.hw[n.head_layers - 1].data(), 16, n.width, A.hid[n.head_layers - 2], A.out, false, n.mimic_fp16);
+}
+
+/* head adjoint: weight gradients into g_head, dL/d(head input) into din */
+void head_backward(const NetD &d, const Acts &A, const double *d_logit, double *g_head, double *din)
+{
+    const OrcNet &n = *d.n;
+    double dy[128];
+    for (int i = 0; i < 16; ++i) dy[i] = i < 3 ? d_logit[i] : 0.0;
+    size_t head_off[4], off = 0;
+    for (int l = 0; l < n.head_layers; ++l) {
+        head_off[l] = off;
+        off += (size_t)(l == 0 ? n.head_in_pad : n.width) * (l == n.head_layers - 1 ? 16 : n.width);
+    }
+    const int L = n.head_layers;
+    dense_backward(d.hw[L - 1].data(), 16, n.width, A.hid[L - 2], dy, g_head ? g_head + head_off[L - 1] : nullptr, din);
+    for (int l = L - 2; l >= 0; --l) {
+        for (int i = 0; i < n.width; ++i) dy[i] = A.hid[l][i] > 0.0 ? din[i] : 0.0;
+        const int in = l == 0 ? n.head_in_pad : n.width;
+        const double *x = l == 0 ? A.in : A.hid[l - 1];
+        dense_backward(d.hw[l].data(), n.width, in, x, dy, g_head ? g_head + head_off[l] : nullptr, din);
+    }
+}
+
 /* network adjoint of one sample given dL/d(log sigma) and dL/d(rgb logits) */
 void network_backward(const NetD &d, V3 pos, const Acts &A, double d_logsigma, const double *d_logit,
                       double *g_table, double *g_base, double *g_head)
@@ -1062,9 +1097,192 @@ double ray_loss_grad(const NetD &d, const OrcScene *sc, const OrcSteps *st, cons
     return loss;
 }
 
+/* one ray of the cached differentiable render: the classification and
+ * lookups of orc_render_cached with voxel latents taken from `lat`
+ * (index into [slots][512][8]), then the adjoint; cache rows pass dL/dlatents
+ * to their corners with weight w_c / sum(w isset).  Density voxels get no
+ * gradient. */
+struct LatentSource { /* the cache's fp16 latents plus perturbations (index, delta) */
+    const uint16_t *lat16;
+    const int64_t *pidx;
+    const double *pdel;
+    int npert;
+    double operator()(size_t i) const
+    {
+        double v = h2d(lat16[i]);
+        for (int k = 0; k < npert; ++k)
+            if ((size_t)pidx[k] == i) v += pdel[k];
+        return v;
+    }
+};
+
+double ray_loss_grad_cached(const NetD &d, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                            const OrcCache *cc, const OrcCam *ccam, const OrcSteps *cst, const LatentSource &lat, int px, int py,
+                            const float *target, double inv_n, double *pred, double *g_table, double *g_base, double *g_head,
+                            double *g_lat)
+{
+    const OrcNet &n = *d.n;
+    const OrcCacheDims &cd = cc->dims;
+    struct S { int kind; V3 pos; float dt; double sigma; double lat[8]; int nc; size_t vi[8]; double w[8]; double wsum; };
+    std::vector<S> samples;
+    std::vector<double> rgbv;
+    double C[3] = {0, 0, 0}, T = 1.0;
+    const Ray r = generate_ray(*cam, px, py);
+    const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
+    float tn, tf;
+    if (ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf)) {
+        const Ray rc = transform_ray(r, ccam->w2c);
+        const float far_ = fminf(tf, st->far_);
+        float t1 = valid_t_from_t(*st, tn) + 0.0f;
+        for (;;) {
+            const float t0 = t1;
+            const float dt = calc_step(*st, t0);
+            t1 = t0 + dt;
+            const float tm = (t0 + t1) * 0.5f;
+            if (tm > far_) break;
+            const V3 wp = at(r, tm);
+            if (!occupied(*sc, bits, wp)) continue;
+            float tfr;
+            const V3 fp = cam2froxel(at(rc, tm), *ccam, *cst, tfr);
+            const bool in_fov = fp.x >= 0 && fp.x < (float)cd.fW && fp.y >= 0 && fp.y < (float)cd.fH;
+            const bool inside = in_fov && fp.z >= 0 && fp.z < (float)cd.fD;
+            bool unsampled = true;
+            if (in_fov) {
+                const float kr = cc->known_ranges[(size_t)(int)floorf(fp.y) * cd.fW + (int)floorf(fp.x)];
+                unsampled = tfr < cst->near_ || tfr > kr;
+            }
+            int kind = 0;
+            if (inside && !unsampled) {
+                const int bx = (int)(fp.x / 8.0f), by = (int)(fp.y / 8.0f), bz = (int)(fp.z / 8.0f);
+                const int packed = brick_lookup(*cc, bx, by, bz);
+                kind = 2;
+                if (packed >= 0) {
+                    const float ix = fp.x - (float)(bx * 8), iy = fp.y - (float)(by * 8), iz = fp.z - (float)(bz * 8);
+                    const float ax = (float)(((packed >> 20) & 1023) * 8) + ix;
+                    const float ay = (float)(((packed >> 10) & 1023) * 8) + iy;
+                    const float az = (float)((packed & 1023) * 8) + iz;
+                    Vox v;
+                    if (fetch_texel(*cc, (int)floorf(ax), (int)floorf(ay), (int)floorf(az), v) && v.density > 0.0) kind = 1;
+                }
+                if (kind == 2) continue;
+            }
+            const float tmh = t0 + dt * 0.5f;
+            S smp{};
+            smp.kind = kind;
+            smp.dt = dt;
+            Acts A;
+            if (kind == 0) {
+                smp.pos = contract(*sc, at(r, tmh));
+                forward_acts(d, smp.pos, d01, A);
+                smp.sigma = std::exp(A.out2[0]);
+            } else {
+                float tfr2;
+                const V3 f2 = cam2froxel(at(rc, tmh), *ccam, *cst, tfr2);
+                const float fx0 = floorf(f2.x - 0.5f), fy0 = floorf(f2.y - 0.5f), fz0 = floorf(f2.z - 0.5f);
+                const double lt[3] = {(double)(f2.x - 0.5f - fx0), (double)(f2.y - 0.5f - fy0), (double)(f2.z - 0.5f - fz0)};
+                double dsum = 0, lsum[8] = {0};
+                smp.wsum = 0;
+                smp.nc = 0;
+                for (int c = 0; c < 8; ++c) {
+                    const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+                    const double w = (ox ? lt[0] : 1.0 - lt[0]) * (oy ? lt[1] : 1.0 - lt[1]) * (oz ? lt[2] : 1.0 - lt[2]);
+                    const float cx = fx0 + (float)ox, cy = fy0 + (float)oy, cz = fz0 + (float)oz;
+                    const bool fov = cx >= 0 && cx < (float)cd.fW && cy >= 0 && cy < (float)cd.fH;
+                    if (!(fov && cz >= 0 && cz < (float)cd.fD)) continue;
+                    const int bx = (int)(cx / 8.0f), by = (int)(cy / 8.0f), bz = (int)(cz / 8.0f);
+                    const int packed = brick_lookup(*cc, bx, by, bz);
+                    if (packed < 0) continue;
+                    const int X = ((packed >> 20) & 1023) * 8 + ((int)cx - bx * 8);
+                    const int Y = ((packed >> 10) & 1023) * 8 + ((int)cy - by * 8);
+                    const int Z = (packed & 1023) * 8 + ((int)cz - bz * 8);
+                    if (X < 0 || Y < 0 || Z < 0 || X >= cd.dX * 8 || Y >= cd.dY * 8 || Z >= cd.dZ * 8) continue;
+                    const int slot = (X / 8) * cd.dY * cd.dZ + (Y / 8) * cd.dZ + (Z / 8);
+                    const size_t vi = (size_t)slot * 512 + (size_t)(Z % 8) * 64 + (Y % 8) * 8 + (X % 8);
+                    smp.wsum += w * cc->vox_isset[vi];
+                    dsum += w * cc->vox_density[vi];
+                    for (int j = 0; j < 8; ++j) lsum[j] += w * lat(vi * 8 + j);
+                    smp.vi[smp.nc] = vi;
+                    smp.w[smp.nc++] = w;
+                }
+                for (int j = 0; j < 8; ++j) smp.lat[j] = lsum[j] / smp.wsum;
+                forward_head_acts(d, smp.lat, d01, A);
+                smp.sigma = std::max(dsum, 1e-6);
+            }
+            samples.push_back(smp);
+            for (int k = 0; k < 3; ++k) rgbv.push_back(sigmoid(A.out[k]));
+            if (composite(smp.sigma, A.out, dt, sc->alpha_thre, C, T)) break;
+        }
+    }
+    double loss = 0.0, g[3];
+    for (int k = 0; k < 3; ++k) {
+        const double e = C[k] + T - (double)target[k];
+        loss += e * e * inv_n;
+        g[k] = 2.0 * e * inv_n;
+    }
+    if (pred) { pred[0] = C[0]; pred[1] = C[1]; pred[2] = C[2]; pred[3] = T; }
+    if (!(g_table || g_base || g_head || g_lat)) return loss;
+    const double gT = g[0] + g[1] + g[2];
+    const double x_total = g[0] * C[0] + g[1] * C[1] + g[2] * C[2] + gT * T;
+    double Ti = 1.0, x_prefix = 0.0;
+    for (size_t i = 0; i < samples.size(); ++i) {
+        const S &smp = samples[i];
+        const double *c = &rgbv[3 * i];
+        double alpha = 1.0 - std::exp(-smp.sigma * (double)smp.dt);
+        alpha = std::min(1.0, std::max(0.0, alpha));
+        if (!(alpha > (double)sc->alpha_thre)) continue;
+        const double gc = g[0] * c[0] + g[1] * c[1] + g[2] * c[2];
+        x_prefix += Ti * alpha * gc;
+        const double T_next = Ti * (1.0 - alpha);
+        const double d_sigma = (double)smp.dt * (T_next * gc - (x_total - x_prefix));
+        double d_logit[3];
+        for (int k = 0; k < 3; ++k) d_logit[k] = g[k] * Ti * alpha * c[k] * (1.0 - c[k]);
+        Acts A;
+        if (smp.kind == 0) {
+            forward_acts(d, smp.pos, d01, A);
+            network_backward(d, smp.pos, A, d_sigma * smp.sigma, d_logit, g_table, g_base, g_head);
+        } else {
+            forward_head_acts(d, smp.lat, d01, A);
+            double din[128];
+            head_backward(d, A, d_logit, g_head, din);
+            if (g_lat)
+                for (int q = 0; q < smp.nc; ++q)
+                    for (int j = 0; j < 8; ++j) g_lat[smp.vi[q] * 8 + j] += din[j] * smp.w[q] / smp.wsum;
+        }
+        Ti = T_next;
+        if (Ti < 1e-4) break;
+    }
+    (void)n;
+    return loss;
+}
+
 }  // namespace
 
 extern "C" {
+
+/* The cached render's loss and adjoint (see ray_loss_grad_cached), with the
+ * voxel latents perturbed by (index into [slots][512][8], delta) pairs. */
+double orc_loss_grad_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                            const OrcCache *cc, const OrcCam *ccam, const OrcSteps *cst, const int32_t *pixels, int n_rays,
+                            const float *target, double *g_table, double *g_base, double *g_head, double *g_lat,
+                            const int64_t *pert_index, const double *pert_delta, int n_pert, int n_threads, double *pred)
+{
+    NetD d; prepare_net(net, d);
+    const LatentSource lat{cc->vox_latents, pert_index, pert_delta, n_pert};
+    const double inv_n = 1.0 / (double)std::max(1, n_rays);
+    const bool grads = g_table || g_base || g_head || g_lat;
+    std::vector<double> per_ray(n_rays, 0.0);
+    auto one = [&](int i) {
+        const int p = pixels[i];
+        per_ray[i] = ray_loss_grad_cached(d, sc, st, cam, bits, cc, ccam, cst, lat, p % cam->W, p / cam->W,
+                                          target + 3 * (size_t)i, inv_n, pred ? pred + 4 * (size_t)i : nullptr,
+                                          g_table, g_base, g_head, g_lat);
+    };
+    if (grads) for (int i = 0; i < n_rays; ++i) one(i);
+    else parallel_rows(n_rays, n_threads, one);
+    double loss = 0.0;
+    for (double v : per_ray) loss += v;
+    return loss;
+}
 
 /* Loss (and, when any gradient pointer is given, its float64 adjoint,
  * accumulated into the given arrays) of the plain render at pixels[i]

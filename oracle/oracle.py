@@ -93,6 +93,11 @@ def lib():
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_int, C.c_int, C.c_void_p]
         _lib.orc_loss_grad.restype = C.c_double
+        _lib.orc_loss_grad_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
+                                              P(OrcCam), P(OrcSteps), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                              C.c_void_p]
+        _lib.orc_loss_grad_cached.restype = C.c_double
         _lib.orc_cache_dims.argtypes = [P(OrcScene), P(OrcSteps), C.c_int, C.c_int, P(OrcCacheDims)]
         _lib.orc_cache_build.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache), C.c_int]
         _lib.orc_render_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
@@ -262,6 +267,30 @@ class OracleModel:
                               C.byref(cc.s), threads or default_threads())
         return cc
 
+    def loss_grad_cached(self, cam: dict, cache: "OracleCache", pixels: np.ndarray, target: np.ndarray, grads: bool = True,
+                         perturb=None, threads: int | None = None):
+        """Cached-render loss at `pixels` against target [n,3] and, if grads, the
+        float64 gradients (table, base blob, head blob, voxel latents
+        [slots*512*8]).  perturb = (latent indices, deltas)."""
+        c = make_cam(cam)
+        cc = make_cam(cache.cam)
+        px = np.ascontiguousarray(pixels, np.int32)
+        tg = np.ascontiguousarray(target, np.float32).reshape(-1)
+        pred = np.zeros((px.size, 4), np.float64)
+        outs = [np.zeros(n, np.float64) if grads else None
+                for n in (self.table.size, self.base_w.size, self.head_w.size, cache.vox_latents.size)]
+        if perturb is not None:
+            pi = np.ascontiguousarray(perturb[0], np.int64)
+            pd = np.ascontiguousarray(perturb[1], np.float64)
+            npert, pip, pdp = pi.size, ptr(pi), ptr(pd)
+        else:
+            npert, pip, pdp = 0, None, None
+        loss = lib().orc_loss_grad_cached(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c),
+                                          ptr(self.bits), C.byref(cache.s), C.byref(cc), C.byref(self.steps), ptr(px), px.size,
+                                          ptr(tg), *[ptr(o) if o is not None else None for o in outs], pip, pdp, npert,
+                                          threads or default_threads(), ptr(pred))
+        return (loss, *outs, pred)
+
     def render_cached(self, cam: dict, cache: "OracleCache", mode: int = 0, rows=None, threads: int | None = None):
         c = make_cam(cam)
         cc = make_cam(cache.cam)
@@ -292,6 +321,18 @@ class OracleCache:
         s.vox_density, s.vox_isset, s.vox_latents = ptr(self.vox_density), ptr(self.vox_isset), ptr(self.vox_latents)
         s.slot_of_brick_order = None
         self.s = s
+
+    def load_device_cache(self, packed: np.ndarray, known: np.ndarray, voxels: np.ndarray) -> None:
+        """Use a device-built cache (fvc_cache_read: packed index, known ranges,
+        voxels as [slots, 512, 8] u32 words: density f32, isset f32, 2 pad,
+        8 fp16 latents) instead of the oracle's own build."""
+        self.packed_index[:] = packed.reshape(-1)
+        self.known_ranges[:] = known.reshape(-1)
+        v = voxels.reshape(-1, 8)
+        n = min(v.shape[0], self.vox_density.size)
+        self.vox_density[:n] = v[:n, 0].view(np.float32)
+        self.vox_isset[:n] = v[:n, 1].view(np.float32)
+        self.vox_latents[:n * 8] = np.ascontiguousarray(v[:n, 4:8]).view(np.uint16).reshape(-1)
 
     @property
     def n_bricks_set(self):

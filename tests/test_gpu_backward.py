@@ -32,9 +32,10 @@ def _case(seed=7, W=32, H=32, n=384):
     return torch, d, loader, cam, pix, tgt
 
 
-def _gpu(torch, loader, cam, pix, tgt, tcgen05=True, grads=None, calls=1):
+def _gpu(torch, loader, cam, pix, tgt, tcgen05=True, grads=None, calls=1, precision=0):
     r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
     r.set_network_path(tcgen05)
+    r.set_precision(precision)
     info = fvc.raymarch_info(cam, loader.stepsize_info)
     g = grads or fvc.Gradients(loader.nerf_network)
     dp = torch.from_numpy(pix).cuda()
@@ -85,3 +86,22 @@ def test_backward_same_on_both_forward_paths():
     for a, b in zip(g1.read(), g2.read()):
         cos, rel = _compare(a.astype(np.float64), b.astype(np.float64))
         assert cos > 0.999 and rel < 0.05
+
+
+def test_bf16_backward_against_float64_adjoint():
+    """BF16 MLPs (forward on tcgen05 kind::f16 with bf16 operands, backward on
+    bf16 mma.sync) against the float64 adjoint without fp16 rounding."""
+    torch, d, loader, cam, pix, tgt = _case()
+    loss, g, _ = _gpu(torch, loader, cam, pix, tgt, precision=fvc.PerformanceRenderer.BF16)
+    oloss, ot, ob, oh, _ = orc.OracleModel(d, mimic_fp16=False).loss_grad(cam, pix, tgt)
+    assert abs(loss - oloss) <= 1e-3 * oloss
+    for name, a, b in zip(("table", "base", "head"), g.read(), (ot, ob, oh)):
+        cos, rel = _compare(a.astype(np.float64), b)
+        print(f"bf16 {name}: cos {cos:.6f} rel {rel:.3e}")
+        assert cos > 0.999 and rel < 3e-2, (name, cos, rel)  # measured: table 1.1e-2, base 8e-4, head 4e-3
+
+
+def test_fp8_backward_is_refused():
+    torch, d, loader, cam, pix, tgt = _case(n=32)
+    with pytest.raises(fvc._lib.FvcError):
+        _gpu(torch, loader, cam, pix, tgt, precision=fvc.PerformanceRenderer.FP8_E4M3)

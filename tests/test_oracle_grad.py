@@ -44,7 +44,7 @@ def test_adjoint_matches_central_differences(case, group):
     g = grads[group]
     nz = np.flatnonzero(g)
     assert nz.size > 100
-    pick = rng.choice(nz, 40, replace=False)
+    pick = rng.choice(nz, 86, replace=False)  # 3 groups x 86 = 258 sampled parameters
     fd = []
     for k in pick:
         lp = om.loss_grad(cam, pix, tgt, grads=False, perturb=([group], [k], [H_FD]))[0]
@@ -58,5 +58,33 @@ def test_adjoint_matches_central_differences(case, group):
     assert np.median(rel) < 1e-4, rel
     assert np.mean(rel < 1e-3) >= 0.75, rel
     assert np.mean(rel < 5e-2) >= 0.95, rel
+    cos = float(an @ fd / (np.linalg.norm(an) * np.linalg.norm(fd)))
+    assert cos > 0.9999
+
+
+def test_cached_adjoint_latents_match_central_differences():
+    """The cached render's adjoint with respect to the cache brick latents
+    (cache rows blend the 8 corner latents with w_c / sum(w isset)) against
+    central differences of the oracle's own cached loss."""
+    om = orc.OracleModel(tiny_model(7, 1), mimic_fp16=False)
+    W = H = 24
+    cam = small_camera(1001, W, H)
+    cache = om.cache_build(cam)
+    rng = np.random.default_rng(8)
+    pix = rng.choice(W * H, 64, replace=False).astype(np.int32)
+    tgt = rng.uniform(0, 1, (64, 3)).astype(np.float32)
+    loss, gt, gb, gh, gl, pred = om.loss_grad_cached(cam, cache, pix, tgt)
+    res, _ = om.render_cached(cam, cache)
+    np.testing.assert_allclose(pred, res.reshape(-1, 4)[pix], atol=1e-6)
+    nz = np.flatnonzero(gl)
+    assert nz.size > 100 and np.count_nonzero(gh) > 100
+    pick = rng.choice(nz, 86, replace=False)
+    fd = np.array([(om.loss_grad_cached(cam, cache, pix, tgt, grads=False, perturb=([k], [H_FD]))[0] -
+                    om.loss_grad_cached(cam, cache, pix, tgt, grads=False, perturb=([k], [-H_FD]))[0]) / (2 * H_FD)
+                   for k in pick])
+    an = gl[pick]
+    rel = np.abs(an - fd) / np.maximum(np.abs(fd), 1e-9)
+    assert np.median(rel) < 1e-4, rel
+    assert np.mean(rel < 1e-3) >= 0.75, rel
     cos = float(an @ fd / (np.linalg.norm(an) * np.linalg.norm(fd)))
     assert cos > 0.9999
