@@ -337,8 +337,38 @@ def run_backward_bench(args, torch, dev, stream) -> dict:
         bf.append(a.elapsed_time(b))
     r.set_precision(fvc.PerformanceRenderer.FP16)
     ms_bf = sum(bf) / len(bf)
+    # the cached form: cache built at the view, gradients at a view rotated by 1 degree (resample rows give
+    # hash-table and MLP gradients, cache rows head and brick-latent gradients)
+    caches = (fvc.Cache(), fvc.Cache())
+    rc = fvc.CachePerformanceRenderer(train.scene_info, train.occupancy_grid_morton_bitfield, train.nerf_network,
+                                      caches[0], caches[1])
+    rc.set_stream(sh)
+    rc.resizeCache(BWD_RES, train.stepsize_info)
+    rc.resizeRenderbuffers(BWD_RES)
+    rc.setCacheSettings(fvc.default_cache_settings())
+    rc.initCacheBlockwise(info)
+    rc.swapCache()
+    c2w = np.asarray(cam["cam2world"], np.float64)
+    ang = math.radians(1.0)
+    rot = np.array([[math.cos(ang), -math.sin(ang), 0.0], [math.sin(ang), math.cos(ang), 0.0], [0.0, 0.0, 1.0]])
+    cam1 = fcam.camera_dict(np.concatenate([rot @ c2w[:, :3], (rot @ c2w[:, 3])[:, None]], axis=1), W, H)
+    info1 = fvc.raymarch_info(cam1, train.stepsize_info)
+    rc.render_backward(info1, pixels, target, grads)
+    cb = []
+    for _ in range(args.steps):
+        a, b = ev(), ev()
+        a.record(stream)
+        loss_cached = rc.render_backward(info1, pixels, target, grads)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        cb.append(a.elapsed_time(b))
+    cst = rc._render_stats
+    ms_c = sum(cb) / len(cb)
     out = {"value": BWD_RAYS / (ms / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms, "rays_per_step": BWD_RAYS,
            "bf16": {"value": BWD_RAYS / (ms_bf / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms_bf, "loss": loss_bf16},
+           "cached": {"value": BWD_RAYS / (ms_c / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms_c, "loss": loss_cached,
+                      "cache_rows": cst.n_cache_hits, "resample_rows": cst.n_resamples,
+                      "note": "gradients of the hash table, MLPs and cache brick latents"},
            "resolution": list(BWD_RES), "loss": loss, "gpu_launches": launches // max(1, args.steps),
            "workload": "c5 differentiable plain render: forward + adjoint (hash table, both MLPs), fp16 MLP",
            "dtype": "f16 MLP (fp32 accumulate, loss-scaled fp16 gradient tiles), f32 compositing and gradients"}

@@ -151,6 +151,7 @@ SIGNATURES = {
     "fvc_grad_zero": (c_int, [P]),
     "fvc_grad_sizes": (c_int, [P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "fvc_grad_read": (c_int, [P, P, P, P]),
+    "fvc_grad_cache_latents": (c_int, [P, P, C.POINTER(C.c_size_t)]),
     "fvc_render_backward": (c_int, [P, P, C.POINTER(RaymarchInfo), P, c_int, P, C.POINTER(C.c_double), P]),
 }
 

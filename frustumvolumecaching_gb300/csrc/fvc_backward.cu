@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BwdSmem &S = *reinterpret_cast<BwdSmem *>(smem_raw);
-    const int n_rows = p.counters[3];
+    const int n_rows = p.counters[6];
     if (n_rows == 0) return;
     for (int i = threadIdx.x; i < DW_FLOATS; i += blockDim.x) S.dW[i] = 0.f;
     __syncthreads();
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
     using T16 = E16<PREC>;
     for (int tile = blockIdx.x * BW_WARPS + warp; tile < n_tiles; tile += gridDim.x * BW_WARPS) {
         const int k = tile * 32 + lane;
-        const int r = k < n_rows ? p.res_list[k] : -1;
+        const int r = k < n_rows ? p.grad_res_list[k] : -1;
         float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
         float3 pos = make_float3(0.f, 0.f, 0.f);
         __half2 sh[8];
@@ -397,6 +397,156 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
     flush(dWh + b.head_w5, b.g_head + b.head_w5, 16 * 64, 64);
 }
 
+/* Cache rows of the cached differentiable render: the head input is the
+ * trilinear blend of the 8 corner voxels' latents (divided by sum(w isset),
+ * generateNetworkInput_cache_shfl_perf_kernel_cg), so the head's input
+ * gradient goes to each corner with weight w_c / sum(w isset).  One warp per
+ * 32 cache rows: lookup, head forward, head backward (weight gradients into
+ * the per-CTA head blob), latent scatter with red.global.add.v2.f32.  The
+ * voxel densities get no gradient. */
+template <int PREC, int HH>
+__global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_cache_bwd_kernel(RenderParams p, BwdParams b, int it)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BwdSmem &S = *reinterpret_cast<BwdSmem *>(smem_raw);
+    const int n_rows = p.counters[7];
+    if (n_rows == 0) return;
+    float *dWh = S.dW + GB_BASE;
+    for (int i = threadIdx.x; i < DW_FLOATS - GB_BASE; i += blockDim.x) dWh[i] = 0.f;
+    __syncthreads();
+    using T16 = E16<PREC>;
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    BwdWarp &W = S.w[warp];
+    const RayState *states = p.states[it & 1];
+    uint16_t *inr = W.IN + lane * S32;
+    uint16_t *gr = W.G + lane * S64;
+    const int n_tiles = (n_rows + 31) / 32;
+    const Voxel *voxels = reinterpret_cast<const Voxel *>(p.cache.voxels);
+    for (int tile = blockIdx.x * BW_WARPS + warp; tile < n_tiles; tile += gridDim.x * BW_WARPS) {
+        const int k = tile * 32 + lane;
+        const int r = k < n_rows ? p.grad_cache_list[k] : -1;
+        float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
+        const Voxel *vp[8];
+        float wc[8];
+        float wsum = 0.f, ls[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        __half2 sh[8];
+        if (r >= 0) {
+            dout = p.row_dout[r];
+            const float4 pw = p.row_pay[r];
+            cache_corners(p.cache, make_float3(pw.x, pw.y, pw.z), vp, wc);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                if (!vp[c]) continue;
+                const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
+                const uint4 lt = __ldg(&vp[c]->lat);
+                wsum = fmaf(wc[c], di.y, wsum);
+                const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float2 fq = __half22float2(*reinterpret_cast<const __half2 *>(&lw[q]));
+                    ls[2 * q] = fmaf(wc[c], fq.x, ls[2 * q]);
+                    ls[2 * q + 1] = fmaf(wc[c], fq.y, ls[2 * q + 1]);
+                }
+            }
+            sh16(row_dir01(states, p.row_slot[r]), sh);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) vp[c] = nullptr;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+        }
+        /* head input [latents (fp16 as the forward lookup rounds them) | SH | 1-padding] */
+        const float inv = wsum != 0.f ? 1.0f / wsum : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) inr[j] = T16::one(__half2float(__float2half_rn(ls[j] * inv)));
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float2 f = __half22float2(sh[q]);
+            reinterpret_cast<uint32_t *>(inr + 8)[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&sh[q]) : T16::pack(f.x, f.y);
+        }
+#pragma unroll
+        for (int q = 24; q < 32; ++q) inr[q] = T16::one(1.0f);
+        __syncwarp();
+        {
+            float c[2][8][4];
+            warp_mm<PREC, 32, 64>(W.IN, S32, b.w + BW_F3, lane, c);
+            st_tile<PREC, 64>(W.A3, S64, c, lane, 1);
+        }
+        __syncwarp();
+        const uint16_t *last = W.A3;
+        if (HH == 2) {
+            float c[2][8][4];
+            warp_mm<PREC, 64, 64>(W.A3, S64, b.w + BW_F4, lane, c);
+            st_tile<PREC, 64>(W.A4, S64, c, lane, 1);
+            __syncwarp();
+            last = W.A4;
+        }
+        gr[0] = T16::one(clamp_h(dout.x));
+        gr[1] = T16::one(clamp_h(dout.y));
+        gr[2] = T16::one(clamp_h(dout.z));
+#pragma unroll
+        for (int q = 3; q < 16; ++q) gr[q] = 0;
+        __syncwarp();
+        warp_dw<PREC, 16, 64>(W.G, S64, last, S64, dWh + b.head_w5, lane);
+        {
+            float c[2][8][4];
+            warp_mm<PREC, 16, 64>(W.G, S64, b.w + BW_B5, lane, c);
+            __syncwarp();
+            st_tile<PREC, 64>(W.G, S64, c, lane, 2, last, S64);
+        }
+        __syncwarp();
+        if (HH == 2) {
+            warp_dw<PREC, 64, 64>(W.G, S64, W.A3, S64, dWh + GH_W4, lane);
+            float c[2][8][4];
+            warp_mm<PREC, 64, 64>(W.G, S64, b.w + BW_B4, lane, c);
+            __syncwarp();
+            st_tile<PREC, 64>(W.G, S64, c, lane, 2, W.A3, S64);
+            __syncwarp();
+        }
+        warp_dw<PREC, 64, 32>(W.G, S64, W.IN, S32, dWh + GH_W3, lane);
+        float dl[2][1][4];
+        warp_mm<PREC, 64, 8>(W.G, S64, b.w + BW_B3, lane, dl);
+        /* d latents of each row (fp32, in the A3 tile) -> the row's corners */
+        float *dL = reinterpret_cast<float *>(W.A3);
+        __syncwarp();
+        {
+            const int g = lane >> 2, q = lane & 3;
+#pragma unroll
+            for (int m = 0; m < 2; ++m)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    float *d = dL + (16 * m + g + 8 * h) * DF_STRIDE + 2 * q;
+                    d[0] = dl[m][0][2 * h];
+                    d[1] = dl[m][0][2 * h + 1];
+                }
+        }
+        __syncwarp();
+        if (r >= 0 && wsum != 0.f) {
+            const float *dr = dL + lane * DF_STRIDE;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                if (!vp[c]) continue;
+                const float f = wc[c] * inv;
+                float *gl = b.g_lat + (size_t)(vp[c] - voxels) * 8;
+#pragma unroll
+                for (int j = 0; j < 8; j += 2) red_add2(gl + j, f * dr[j], f * dr[j + 1]);
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    auto flush = [&](const float *src, float *dst, int n, int I) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int row = i / I, col = i - row * I;
+            const float v = src[row * I + dw_col(row, col)];
+            if (v != 0.f) atomicAdd(dst + i, v);
+        }
+    };
+    flush(dWh + GH_W3, b.g_head + GH_W3, 64 * 32, 32);
+    if (HH == 2) flush(dWh + GH_W4, b.g_head + GH_W4, 64 * 64, 64);
+    flush(dWh + b.head_w5, b.g_head + b.head_w5, 16 * 64, 64);
+}
+
 /* per ray: squared error of the white-background pixel, dL/dC (loss-scaled,
  * without the 1/N of the mean) and X_total = g.C + g_T T */
 __global__ void loss_kernel(RenderParams p, BwdParams b)
@@ -448,6 +598,21 @@ cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int h
         if (bf16) wf_net_bwd_kernel<1, 1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
         else wf_net_bwd_kernel<0, 1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cache_backward(const RenderParams &p, const BwdParams &b, int head_hidden, int it, int n_sms, cudaStream_t s)
+{
+    static bool attrs = false;
+    const int smem = (int)sizeof(BwdSmem);
+    if (!attrs) {
+        cudaError_t e = cudaFuncSetAttribute(wf_cache_bwd_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_cache_bwd_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attrs = true;
+    }
+    if (head_hidden == 2) wf_cache_bwd_kernel<0, 2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
+    else wf_cache_bwd_kernel<0, 1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
     return cudaGetLastError();
 }
 

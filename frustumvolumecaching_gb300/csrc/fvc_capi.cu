@@ -373,7 +373,8 @@ struct fvc_renderer {
     bool last_was_graph = false;
     int steps_per_iter = 64;          /* marching steps per sub-iteration (autotuned) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
-    int *d_grad_rows = nullptr;       /* rows with a gradient (plain renderers have no res_list) */
+    int *d_grad_rows = nullptr;       /* resample rows with a gradient */
+    int *d_grad_cache_rows = nullptr; /* cache rows with a gradient */
     int bwd_capacity = 0;
     LaunchLog log;                    /* kernel accounting of the last render */
     std::vector<cudaEvent_t> events;  /* 2 x 4096 when kernel timing is on */
@@ -395,7 +396,7 @@ struct fvc_renderer {
     {
         if (stream) cudaStreamSynchronize(stream);
         dfree(d_ctl); dfree(d_stats); dfree(d_results); dfree(d_image); dfree(d_counts);
-        dfree(d_row_dout); dfree(d_grad_rows);
+        dfree(d_row_dout); dfree(d_grad_rows); dfree(d_grad_cache_rows);
         dfree(d_views); dfree(d_view_off);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         release_wavefront();
@@ -1256,9 +1257,12 @@ struct fvc_grad {
     float4 *d_ray_grad = nullptr;
     int ray_cap = 0;
     double *d_loss = nullptr;
+    float *d_lat = nullptr, *s_lat = nullptr;                       /* cache-latent gradients [slots][512][8] */
+    size_t n_lat = 0;
     ~fvc_grad()
     {
         dfree(d_table); dfree(d_base); dfree(d_head); dfree(s_table); dfree(s_base); dfree(s_head);
+        dfree(d_lat); dfree(s_lat);
         dfree(d_w); dfree(d_w_bf16); dfree(d_ray_grad); dfree(d_loss);
     }
 };
@@ -1338,6 +1342,7 @@ extern "C" void fvc_grad_destroy(fvc_grad *g) { delete g; }
 extern "C" int fvc_grad_zero(fvc_grad *g)
 {
     CHECK_ARG(g, "fvc_grad_zero: null argument");
+    if (g->n_lat) CU(cudaMemset(g->d_lat, 0, g->n_lat * 4));
     CU(cudaMemset(g->d_table, 0, g->n_table * 4));
     CU(cudaMemset(g->d_base, 0, g->n_base * 4));
     CU(cudaMemset(g->d_head, 0, g->n_head * 4));
@@ -1350,6 +1355,14 @@ extern "C" int fvc_grad_sizes(const fvc_grad *g, size_t *n_table, size_t *n_base
     if (n_table) *n_table = g->n_table;
     if (n_base) *n_base = g->n_base;
     if (n_head) *n_head = g->n_head;
+    return FVC_OK;
+}
+
+extern "C" int fvc_grad_cache_latents(fvc_grad *g, float *latents, size_t *n)
+{
+    CHECK_ARG(g, "fvc_grad_cache_latents: null argument");
+    if (n) *n = g->n_lat;
+    if (latents && g->n_lat) CU(cudaMemcpy(latents, g->d_lat, g->n_lat * 4, cudaMemcpyDeviceToHost));
     return FVC_OK;
 }
 
@@ -1367,8 +1380,7 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
 {
     CHECK_ARG(r && g && info && pixels && target && n_rays > 0, "fvc_render_backward: bad arguments");
     CHECK_ARG(g->m == r->m, "fvc_render_backward: gradients belong to another model");
-    if (r->kind == FVC_RENDERER_CACHE_PERFORMANCE)
-        return fail(FVC_ERR_CONFIG, "fvc_render_backward: the differentiable render is built for the plain renderers");
+    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
     if (r->precision == FVC_PRECISION_FP8_E4M3)
         return fail(FVC_ERR_CONFIG, "fvc_render_backward: the network adjoint is built for FP16 and BF16 MLPs");
     int rc;
@@ -1380,10 +1392,24 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     fvc_model *m = r->m;
     cudaStream_t s = r->stream;
     if (r->bwd_capacity != r->row_capacity) {
-        dfree(r->d_row_dout); dfree(r->d_grad_rows);
+        dfree(r->d_row_dout); dfree(r->d_grad_rows); dfree(r->d_grad_cache_rows);
         if ((rc = dalloc(&r->d_row_dout, (size_t)r->row_capacity, "row gradients"))) return rc;
         if ((rc = dalloc(&r->d_grad_rows, (size_t)r->row_capacity, "gradient rows"))) return rc;
+        if ((rc = dalloc(&r->d_grad_cache_rows, (size_t)r->row_capacity, "gradient rows"))) return rc;
         r->bwd_capacity = r->row_capacity;
+    }
+    if (cached) {
+        if (!r->cache || !r->cache->built) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
+        const size_t n_lat = (size_t)r->cache->capacity() * 512 * 8;
+        if (g->n_lat != n_lat) {
+            dfree(g->d_lat); dfree(g->s_lat);
+            g->n_lat = 0;
+            if ((rc = dalloc(&g->d_lat, n_lat, "cache-latent gradient"))) return rc;
+            if ((rc = dalloc(&g->s_lat, n_lat, "cache-latent gradient"))) return rc;
+            CU(cudaMemset(g->d_lat, 0, n_lat * 4));
+            CU(cudaMemset(g->s_lat, 0, n_lat * 4));
+            g->n_lat = n_lat;
+        }
     }
     if (g->ray_cap < n_rays) {
         dfree(g->d_ray_grad);
@@ -1396,7 +1422,8 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     p.n_list = n_rays;
     p.ray_grad = g->d_ray_grad;
     p.row_dout = r->d_row_dout;
-    p.res_list = r->d_grad_rows;
+    p.grad_res_list = r->d_grad_rows;
+    p.grad_cache_list = r->d_grad_cache_rows;
     BwdParams b;
     b.w = r->precision == FVC_PRECISION_BF16 ? g->d_w_bf16 : g->d_w;
     b.g_table = g->s_table; b.g_base = g->s_base; b.g_head = g->s_head;
@@ -1404,23 +1431,25 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     b.loss = g->d_loss;
     b.target = target;
     b.loss_scale = FVC_LOSS_SCALE;
+    b.g_lat = cached ? g->s_lat : nullptr;
     reset_launch_log(r);
     /* pass 1: forward render of the listed pixels into d_results */
     CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), s));
     CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), s));
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), s));
-    CU(render_frame(p, false, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->last_iterations, &r->log));
+    CU(render_frame(p, cached, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->last_iterations, &r->log));
     /* loss and per-ray dL/dC */
     CU(cudaMemsetAsync(g->d_loss, 0, sizeof(double), s));
     CU(launch_loss(p, b, s));
     /* pass 2: re-march, compositing adjoint, network adjoint */
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), s));
-    CU(backward_frame(p, b, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->log));
+    CU(backward_frame(p, b, cached, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->log));
     const float inv = 1.0f / (FVC_LOSS_SCALE * (float)n_rays);
     CU(launch_grad_finalize(g->s_table, g->d_table, g->n_table, inv, m->n_sms, s));
     CU(launch_grad_finalize(g->s_base, g->d_base, g->n_base, inv, m->n_sms, s));
     CU(launch_grad_finalize(g->s_head, g->d_head, g->n_head, inv, m->n_sms, s));
-    r->log.launches += 4;
+    if (cached) CU(launch_grad_finalize(g->s_lat, g->d_lat, g->n_lat, inv, m->n_sms, s));
+    r->log.launches += cached ? 5 : 4;
     if (pred) CU(cudaMemcpyAsync(pred, r->d_results, (size_t)n_rays * sizeof(float4), cudaMemcpyDeviceToDevice, s));
     double loss = 0.0;
     CU(cudaMemcpyAsync(&loss, g->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));

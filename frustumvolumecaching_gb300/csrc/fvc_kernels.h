@@ -38,6 +38,45 @@ struct __align__(16) Voxel {
     uint4 lat;
 };
 
+enum : int { KIND_RESAMPLE = 0, KIND_CACHE = 1, KIND_DROP = 2, KIND_SKIP = 3 };
+
+/* voxel (X, Y, Z) of the data array, or null outside it or in a slot the
+ * last build did not write (the reference clears its arrays per build) */
+__device__ __forceinline__ const Voxel *texel(const CacheView &c, int X, int Y, int Z)
+{
+    if (X < 0 || Y < 0 || Z < 0 || X >= c.dX * 8 || Y >= c.dY * 8 || Z >= c.dZ * 8) return nullptr;
+    const int slot = (X >> 3) * (c.dY * c.dZ) + (Y >> 3) * c.dZ + (Z >> 3);
+    if (slot >= c.n_valid_slots) return nullptr;
+    return reinterpret_cast<const Voxel *>(c.voxels) + (size_t)slot * 512 + ((Z & 7) * 64 + (Y & 7) * 8 + (X & 7));
+}
+
+/* the 8 trilinear corners of froxel point f (unnormalised texel
+ * coordinates, border -> none; include/util/cuda_readwrite_array.h:41-62):
+ * voxel or null, and weight (generateNetworkInput_cache_shfl_perf_kernel_cg,
+ * src/cache_performance_renderer.cu:678-787) */
+__device__ __forceinline__ void cache_corners(const CacheView &C, float3 f, const Voxel *(&vp)[8], float (&w)[8])
+{
+    const float fx = F_SUB(f.x, 0.5f), fy = F_SUB(f.y, 0.5f), fz = F_SUB(f.z, 0.5f);
+    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
+    const float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+        const float cx = x0 + (float)ox, cy = y0 + (float)oy, cz = z0 + (float)oz;
+        vp[c] = nullptr;
+        w[c] = (ox ? lx : 1.0f - lx) * (oy ? ly : 1.0f - ly) * (oz ? lz : 1.0f - lz);
+        const bool inside = cx >= 0.f && cx < (float)C.fW && cy >= 0.f && cy < (float)C.fH && cz >= 0.f && cz < (float)C.fD;
+        if (inside) {
+            const int ix = (int)cx, iy = (int)cy, iz = (int)cz;
+            const int bx = ix >> 3, by = iy >> 3, bz = iz >> 3;
+            const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
+            if (packed >= 0)
+                vp[c] = texel(C, ((packed >> 20) & 1023) * 8 + (ix & 7), ((packed >> 10) & 1023) * 8 + (iy & 7),
+                              (packed & 1023) * 8 + (iz & 7));
+        }
+    }
+}
+
 /* state of one alive ray between sub-iterations (96 bytes) */
 struct __align__(16) RayState {
     float4 of;    /* origin, far */
@@ -106,6 +145,8 @@ struct RenderParams {
     int n_list;
     const float4 *ray_grad;     /* per ray: dL/dC (loss-scaled) and X_total = g.C + g_T T */
     float4 *row_dout;           /* per row: dL/d rgb logits, dL/d log-density (loss-scaled) */
+    int *grad_res_list;         /* rows with a gradient: resample rows (counters[6]) */
+    int *grad_cache_list;       /*                       cache rows (counters[7]) */
 };
 
 /* Weights of the backward kernel: fragment packs (mma.sync m16n8k16 B
@@ -137,6 +178,7 @@ struct BwdParams {
     double *loss;               /* sum of squared pixel errors (device) */
     const float *target;        /* [n_list][3] */
     float loss_scale;           /* gradients carry this factor until read out */
+    float *g_lat;               /* [slots][512][8] fp32 cache-latent gradients (cached path) */
 };
 
 
@@ -221,10 +263,11 @@ cudaError_t build_batch_graph(const RenderParams &p, int head_hidden, int n_sms,
                               cudaGraphExec_t *exec, int *n_kernels);
 
 /* differentiable render (fvc_backward.cu): pass 1 is render_frame over p.pixel_list */
-cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, int head_hidden, int n_sms, cudaStream_t s,
+cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, bool cached, int head_hidden, int n_sms, cudaStream_t s,
                            int *h_pinned, int check_every, LaunchLog *log = nullptr);
 cudaError_t launch_loss(const RenderParams &p, const BwdParams &b, cudaStream_t s);
 cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int head_hidden, int it, int n_sms, cudaStream_t s);
+cudaError_t launch_cache_backward(const RenderParams &p, const BwdParams &b, int head_hidden, int it, int n_sms, cudaStream_t s);
 cudaError_t launch_grad_finalize(float *scratch, float *out, size_t n, float inv_scale, int n_sms, cudaStream_t s);
 cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
 

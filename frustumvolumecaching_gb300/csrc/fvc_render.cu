@@ -230,15 +230,6 @@ __global__ void wf_loop_cond_kernel(RenderParams p, cudaGraphConditionalHandle h
 /* ------------------------------------------------------------------------- */
 /* march                                                                     */
 /* ------------------------------------------------------------------------- */
-__device__ __forceinline__ const Voxel *texel(const CacheView &c, int X, int Y, int Z)
-{
-    if (X < 0 || Y < 0 || Z < 0 || X >= c.dX * 8 || Y >= c.dY * 8 || Z >= c.dZ * 8) return nullptr;
-    const int slot = (X >> 3) * (c.dY * c.dZ) + (Y >> 3) * c.dZ + (Z >> 3);
-    if (slot >= c.n_valid_slots) return nullptr; /* the reference clears the data arrays per build */
-    return reinterpret_cast<const Voxel *>(c.voxels) + (size_t)slot * 512 + ((Z & 7) * 64 + (Y & 7) * 8 + (X & 7));
-}
-
-enum : int { KIND_RESAMPLE = 0, KIND_CACHE = 1, KIND_DROP = 2, KIND_SKIP = 3 };
 
 /* Classification of one occupied sample, sample_cache_performance_kernel
  * (src/cache_performance_renderer.cu:91-163). */
@@ -472,31 +463,14 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(Rend
  * interpolated density (not renormalised) and latents / interpolated isset. */
 __device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, int latent_offset, __half *trow)
 {
-    const float fx = F_SUB(f.x, 0.5f), fy = F_SUB(f.y, 0.5f), fz = F_SUB(f.z, 0.5f);
-    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
-    const float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
     const Voxel *vp[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
-        const float cx = x0 + (float)ox, cy = y0 + (float)oy, cz = z0 + (float)oz;
-        vp[c] = nullptr;
-        const bool inside = cx >= 0.f && cx < (float)C.fW && cy >= 0.f && cy < (float)C.fH && cz >= 0.f && cz < (float)C.fD;
-        if (inside) {
-            const int ix = (int)cx, iy = (int)cy, iz = (int)cz;
-            const int bx = ix >> 3, by = iy >> 3, bz = iz >> 3;
-            const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
-            if (packed >= 0)
-                vp[c] = texel(C, ((packed >> 20) & 1023) * 8 + (ix & 7), ((packed >> 10) & 1023) * 8 + (iy & 7),
-                              (packed & 1023) * 8 + (iz & 7));
-        }
-    }
+    float wc[8];
+    cache_corners(C, f, vp, wc);
     float wsum = 0.f, dsum = 0.f, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         if (!vp[c]) continue;
-        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
-        const float w = (ox ? lx : 1.0f - lx) * (oy ? ly : 1.0f - ly) * (oz ? lz : 1.0f - lz);
+        const float w = wc[c];
         const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
         const uint4 lt = __ldg(&vp[c]->lat);
         wsum = fmaf(w, di.y, wsum);
@@ -1023,7 +997,10 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
  *   dL/dsigma = dt (T' g.c - (X_total - X_prefix));  dL/dc = T alpha g.
  * The alpha threshold and the T < 1e-4 termination follow the forward
  * compositing exactly, so the rows that composited get gradients and no
- * other.  Rows with a gradient are listed in res_list (counters[3]). */
+ * other; rows the forward skipped (known-empty cache voxels) get none.  Rows
+ * with a gradient are listed per stream: grad_res_list (counters[6]),
+ * grad_cache_list (counters[7]). */
+template <bool CACHED>
 __global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, int it)
 {
     const int n_alive = p.counters[it & 1];
@@ -1033,9 +1010,9 @@ __global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, i
         const bool valid = i < n_alive;
         bool keep = false;
         RayState st;
-        int n_grad = 0;
+        int n_res = 0, n_cch = 0;
         int2 rr = make_int2(0, 0);
-        uint32_t gmask = 0;
+        uint32_t gmask = 0, cmask = 0;
         if (valid) {
             st = cur[i];
             rr = p.ray_rows[i];
@@ -1045,7 +1022,8 @@ __global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, i
             for (int j = 0; j < rr.y; ++j) {
                 const int r = rr.x + j;
                 float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (!term) {
+                const int kind = CACHED ? (int)p.row_kind[r] : KIND_RESAMPLE;
+                if (!term && kind < KIND_DROP) {
                     const uint2 ov = p.row_out[r];
                     const float t0 = p.row_t0[r];
                     const float2 lg = __half22float2(*reinterpret_cast<const __half2 *>(&ov.x));
@@ -1065,8 +1043,8 @@ __global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, i
                         dout = make_float4(rg.x * ta * c0 * (1.0f - c0), rg.y * ta * c1 * (1.0f - c1), rg.z * ta * c2 * (1.0f - c2),
                                            dsig * sigma);
                         T = Tn;
-                        gmask |= 1u << j;
-                        ++n_grad;
+                        if (kind == KIND_CACHE) { cmask |= 1u << j; ++n_cch; }
+                        else { gmask |= 1u << j; ++n_res; }
                     }
                     if (T < 1e-4f) term = true;
                 }
@@ -1076,18 +1054,22 @@ __global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, i
             st.acc.w = T;
             keep = !(term || st.cnt2.y);
         }
-        /* list the rows with a gradient (one atomic per warp) */
-        int incl = n_grad;
+        /* list the rows with a gradient per network stream (one atomic per warp and list) */
+        auto append = [&](int n, uint32_t mask, int *list, int *counter) {
+            int incl = n;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(FULLMASK, incl, o);
-            if (lane_id() >= o) incl += v;
-        }
-        const int total = __shfl_sync(FULLMASK, incl, 31);
-        int lb = 0;
-        if (lane_id() == 0 && total) lb = atomicAdd(p.counters + 3, total);
-        lb = __shfl_sync(FULLMASK, lb, 0) + incl - n_grad;
-        for (uint32_t mm = gmask; mm; mm &= mm - 1) p.res_list[lb++] = rr.x + __ffs(mm) - 1;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULLMASK, incl, o);
+                if (lane_id() >= o) incl += v;
+            }
+            const int total = __shfl_sync(FULLMASK, incl, 31);
+            int lb = 0;
+            if (lane_id() == 0 && total) lb = atomicAdd(counter, total);
+            lb = __shfl_sync(FULLMASK, lb, 0) + incl - n;
+            for (uint32_t mm = mask; mm; mm &= mm - 1) list[lb++] = rr.x + __ffs(mm) - 1;
+        };
+        append(n_res, gmask, p.grad_res_list, p.counters + 6);
+        if (CACHED) append(n_cch, cmask, p.grad_cache_list, p.counters + 7);
         const unsigned m = __ballot_sync(FULLMASK, keep);
         int nb = 0;
         if (lane_id() == 0 && m) nb = atomicAdd(p.counters + ((it + 1) & 1), __popc(m));
@@ -1106,6 +1088,8 @@ __global__ void wf_reset_rows_kernel(RenderParams p, int cached)
         p.counters[2] = 0;
         p.counters[3] = 0;
         p.counters[4] = 0;
+        p.counters[6] = 0;
+        p.counters[7] = 0;
     }
 }
 
@@ -1207,7 +1191,7 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
 /* Pass 2 of the differentiable render (pass 1 is run_frame over the pixel
  * list, then the loss kernel): the same march and network forward per
  * sub-iteration, then the compositing adjoint and the network adjoint. */
-template <int HH>
+template <bool CACHED, int HH>
 static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n_sms, cudaStream_t s, int *h_pinned,
                                 int check_every, LaunchLog *log)
 {
@@ -1223,13 +1207,30 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
     ++L.launches;
     const int grid_ray = n_sms * 16;
     for (int it = 0; it < (1 << 20); ++it) {
-        wf_march_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
-        launch_plain_net<HH>(p, it, n_sms, s); /* the forward kernel of pass 1, so both passes composite the same values */
-        wf_composite_bwd_kernel<<<grid_ray, 128, 0, s>>>(p, it);
+        wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+        /* the forward kernels of pass 1, so both passes composite the same values */
+        if (CACHED) {
+            const size_t tc_smem = sizeof(TcSmem);
+            const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
+            wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
+            if (p.use_tc) {
+                wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+                wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            } else {
+                wf_net_resample_kernel<HH, true><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
+                wf_net_cache_kernel<HH><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
+            }
+            L.launches += 3;
+        } else {
+            launch_plain_net<HH>(p, it, n_sms, s);
+            L.launches += 1;
+        }
+        wf_composite_bwd_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
         cudaError_t e = launch_net_backward(p, b, HH, it, n_sms, s);
+        if (e == cudaSuccess && CACHED) e = launch_cache_backward(p, b, HH, it, n_sms, s);
         if (e != cudaSuccess) return e;
-        wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, 0);
-        L.launches += 5;
+        wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, CACHED ? 1 : 0);
+        L.launches += CACHED ? 5 : 4;
         if ((it + 1) % check_every == 0) {
             e = cudaMemcpyAsync(h_pinned, p.counters + ((it + 1) & 1), sizeof(int), cudaMemcpyDeviceToHost, s);
             if (e != cudaSuccess) return e;
@@ -1241,11 +1242,14 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
     return cudaGetLastError();
 }
 
-cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, int head_hidden, int n_sms, cudaStream_t s,
+cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, bool cached, int head_hidden, int n_sms, cudaStream_t s,
                            int *h_pinned, int check_every, LaunchLog *log)
 {
-    return head_hidden == 2 ? run_backward<2>(p, b, n_sms, s, h_pinned, check_every, log)
-                            : run_backward<1>(p, b, n_sms, s, h_pinned, check_every, log);
+    if (cached)
+        return head_hidden == 2 ? run_backward<true, 2>(p, b, n_sms, s, h_pinned, check_every, log)
+                                : run_backward<true, 1>(p, b, n_sms, s, h_pinned, check_every, log);
+    return head_hidden == 2 ? run_backward<false, 2>(p, b, n_sms, s, h_pinned, check_every, log)
+                            : run_backward<false, 1>(p, b, n_sms, s, h_pinned, check_every, log);
 }
 
 template <int HH>

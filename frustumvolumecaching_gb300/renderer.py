@@ -250,6 +250,15 @@ class Gradients:
     def zero(self) -> None:
         L.check(L.load().fvc_grad_zero(self.handle))
 
+    def cache_latents(self) -> np.ndarray:
+        """Gradients of the cache brick latents [slots, 512, 8] (cached backward)."""
+        n = C.c_size_t()
+        L.check(L.load().fvc_grad_cache_latents(self.handle, None, C.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        if n.value:
+            L.check(L.load().fvc_grad_cache_latents(self.handle, L.ptr(out), C.byref(n)))
+        return out.reshape(-1, 512, 8)
+
     def read(self):
         t, b, h = (np.zeros(n, np.float32) for n in self.sizes)
         L.check(L.load().fvc_grad_read(self.handle, L.ptr(t), L.ptr(b), L.ptr(h)))

@@ -362,9 +362,15 @@ int fvc_grad_zero(fvc_grad *g);
 int fvc_grad_sizes(const fvc_grad *g, size_t *n_table, size_t *n_base, size_t *n_head);
 /* copies the accumulated gradients to host arrays (any may be null) */
 int fvc_grad_read(fvc_grad *g, float *table, float *base, float *head);
+/* gradients of the cache brick latents after cached backward calls: *n =
+ * slots x 512 x 8 floats in the cache's [slot][z][y][x][latent] order (0
+ * before any cached call); copied to latents when non-null */
+int fvc_grad_cache_latents(fvc_grad *g, float *latents, size_t *n);
 
 /* Forward and adjoint of the plain render (renderer kinds BASIC/PERFORMANCE;
- * FP16 or BF16 MLPs per fvc_renderer_set_precision)
+ * FP16 or BF16 MLPs per fvc_renderer_set_precision) or of the cached render
+ * (CACHE_PERFORMANCE with a built cache, FP16; cache rows also give
+ * gradients of the brick latents, fvc_grad_cache_latents)
  * at n_rays pixels (device int32 y * W + x, at most W * H of the camera):
  * L = mean over the rays of sum_k (C_k + T - target_k)^2, the
  * white-background pixel of writeImageBuffer_performance_kernel
