@@ -43,8 +43,8 @@ BYTES_CACHE = 8 * 24   # per cache sample: 8 corners x (density, isset, 8 fp16 l
 BYTES_ROW_IO = 28 + 8  # per resampled sample: the 28 B sample record read + 4 fp16 outputs written
 NET_KERNEL = "wf_net_tc_kernel<0> (resample rows: hash-grid encode + density MLP + color head on tcgen05)"
 # DRAM bytes (read + write) per resample row of that kernel: dram__bytes_read.sum + dram__bytes_write.sum over all
-# its launches of 2 frames of the same scene at 960x540 / the rows they processed (4.420 GB / 116,864,373 rows)
-NET_TRAFFIC_PER_ROW = 37.8
+# its launches of 2 frames of the same scene at 960x540 / the rows they processed (4.616 GB / 116,864,373 rows)
+NET_TRAFFIC_PER_ROW = 39.5
 
 
 def dist_env():
