@@ -143,6 +143,7 @@ SIGNATURES = {
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_renderer_set_precision": (c_int, [P, c_int]),
     "fvc_render_batch": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs)]),
+    "fvc_render_batch_cached": (c_int, [P, C.POINTER(RaymarchInfo), c_int, PP, C.POINTER(RenderOutputs)]),
     "fvc_renderer_autotune": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs), C.POINTER(AutotuneResult)]),
     "fvc_model_properties": (c_int, [P, C.POINTER(ModelProps)]),
     "fvc_renderer_synchronize": (c_int, [P]),

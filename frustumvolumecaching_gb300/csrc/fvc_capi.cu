@@ -365,6 +365,7 @@ struct fvc_renderer {
     /* batched views in one graph launch */
     DevCam *d_views = nullptr;
     int *d_view_off = nullptr;
+    ViewCache *d_view_caches = nullptr;
     int views_cap = 0;
     cudaGraphExec_t graph_exec = nullptr;
     RenderParams graph_params;        /* the parameters the graph holds by value */
@@ -397,7 +398,7 @@ struct fvc_renderer {
         if (stream) cudaStreamSynchronize(stream);
         dfree(d_ctl); dfree(d_stats); dfree(d_results); dfree(d_image); dfree(d_counts);
         dfree(d_row_dout); dfree(d_grad_rows); dfree(d_grad_cache_rows);
-        dfree(d_views); dfree(d_view_off);
+        dfree(d_views); dfree(d_view_off); dfree(d_view_caches);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         release_wavefront();
         bs.release();
@@ -808,7 +809,7 @@ static int check_info(const fvc_raymarch_info *info)
 }
 
 static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts,
-                               RenderParams &p)
+                               RenderParams &p, bool per_view_caches = false)
 {
     fvc_model *m = r->m;
     const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
@@ -833,14 +834,16 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.max_rounds = 1 << 26;
     p.max_samples_per_ray = r->max_samples;
     if (cached) {
-        fvc_cache *c = r->cache;
-        if (!c || !c->initialized || !c->built) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
         if (m->latent_offset != 1)
             return fail(FVC_ERR_CONFIG, "the Density cache variant needs a model whose first latent is not the density");
-        p.ccam = dev_cam(c->rm_info.cam_info);
-        p.csteps = dev_steps(c->rm_info.stepsize_info);
-        p.cache = c->view();
         p.render_mode = r->render_mode;
+        if (!per_view_caches) {
+            fvc_cache *c = r->cache;
+            if (!c || !c->initialized || !c->built) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
+            p.ccam = dev_cam(c->rm_info.cam_info);
+            p.csteps = dev_steps(c->rm_info.stepsize_info);
+            p.cache = c->view();
+        }
     }
     if (info->cam_info.resolution.x != r->W || info->cam_info.resolution.y != r->H) {
         const int rc = fvc_renderer_resize(r, info->cam_info.resolution.x, info->cam_info.resolution.y);
@@ -1472,11 +1475,17 @@ extern "C" int fvc_renderer_set_precision(fvc_renderer *r, int precision)
 /* batched views: one graph launch per batch                                 */
 /* ------------------------------------------------------------------------ */
 static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
-                       RenderParams &p, int &n_rays)
+                       RenderParams &p, int &n_rays, fvc_cache *const *caches = nullptr)
 {
     CHECK_ARG(r && infos && n_views > 0, "fvc_render_batch: bad arguments");
-    if (r->kind == FVC_RENDERER_CACHE_PERFORMANCE)
-        return fail(FVC_ERR_CONFIG, "fvc_render_batch: batched views are built for the plain renderers");
+    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    if (cached != (caches != nullptr))
+        return fail(FVC_ERR_CONFIG, "fvc_render_batch: plain renderers take no caches, cache renderers take one per view "
+                                    "(fvc_render_batch_cached)");
+    if (caches)
+        for (int v = 0; v < n_views; ++v)
+            if (!caches[v] || !caches[v]->initialized || !caches[v]->built)
+                return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
     long long total = 0;
     int rc;
     for (int v = 0; v < n_views; ++v) {
@@ -1489,10 +1498,20 @@ static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_vi
     n_rays = (int)total;
     if ((rc = fvc_renderer_resize(r, n_rays, 1))) return rc;
     if (r->views_cap < n_views) {
-        dfree(r->d_views); dfree(r->d_view_off);
+        dfree(r->d_views); dfree(r->d_view_off); dfree(r->d_view_caches);
         if ((rc = dalloc(&r->d_views, (size_t)n_views, "views"))) return rc;
         if ((rc = dalloc(&r->d_view_off, (size_t)n_views + 1, "view offsets"))) return rc;
+        if ((rc = dalloc(&r->d_view_caches, (size_t)n_views, "view caches"))) return rc;
         r->views_cap = n_views;
+    }
+    if (caches) {
+        std::vector<ViewCache> vcs(n_views);
+        for (int v = 0; v < n_views; ++v) {
+            vcs[v].cache = caches[v]->view();
+            vcs[v].ccam = dev_cam(caches[v]->rm_info.cam_info);
+            vcs[v].csteps = dev_steps(caches[v]->rm_info.stepsize_info);
+        }
+        CU(cudaMemcpyAsync(r->d_view_caches, vcs.data(), vcs.size() * sizeof(ViewCache), cudaMemcpyHostToDevice, r->stream));
     }
     std::vector<DevCam> cams(n_views);
     std::vector<int> off(n_views + 1, 0);
@@ -1507,8 +1526,9 @@ static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_vi
     first.cam_info.resolution.x = n_rays;
     first.cam_info.resolution.y = 1;
     if ((rc = setup_render_params(r, &first, out ? (float4 *)out->results : nullptr, out ? (uchar4 *)out->image_rgba8 : nullptr,
-                                  out ? (int4 *)out->ray_counts : nullptr, p)))
+                                  out ? (int4 *)out->ray_counts : nullptr, p, cached)))
         return rc;
+    p.view_caches = caches ? r->d_view_caches : nullptr;
     p.views = r->d_views;
     p.view_off = r->d_view_off;
     p.n_views = n_views;
@@ -1525,7 +1545,8 @@ static int batch_launch(fvc_renderer *r, const RenderParams &p, int n_rays)
             cudaGraphExecDestroy(r->graph_exec);
             r->graph_exec = nullptr;
         }
-        CU(build_batch_graph(p, m->head_hidden, m->n_sms, r->stream, n_rays, &r->graph_exec, &r->graph_kernels));
+        CU(build_batch_graph(p, p.view_caches != nullptr, m->head_hidden, m->n_sms, r->stream, n_rays, &r->graph_exec,
+                             &r->graph_kernels));
         memcpy(&r->graph_params, &p, sizeof(RenderParams));
         r->graph_head_hidden = m->head_hidden;
     }
@@ -1542,6 +1563,17 @@ extern "C" int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos,
     RenderParams p;
     int n_rays = 0, rc;
     if ((rc = batch_setup(r, infos, n_views, out, p, n_rays))) return rc;
+    return batch_launch(r, p, n_rays);
+}
+
+extern "C" int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, fvc_cache *const *caches,
+                                       const fvc_render_outputs *out)
+{
+    CHECK_ARG(r && caches, "fvc_render_batch_cached: null argument");
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    RenderParams p;
+    int n_rays = 0, rc;
+    if ((rc = batch_setup(r, infos, n_views, out, p, n_rays, caches))) return rc;
     return batch_launch(r, p, n_rays);
 }
 

@@ -92,6 +92,13 @@ struct RenderStatsDev {
     int n_rounds, pad;
 };
 
+/* one view's frustum cache with the camera and step grid it was built for */
+struct ViewCache {
+    CacheView cache;
+    DevCam ccam;
+    DevSteps csteps;
+};
+
 struct RenderParams {
     DevScene scene;
     DevSteps steps;
@@ -135,7 +142,10 @@ struct RenderParams {
     int row_capacity;           /* rows per sub-iteration */
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
     /* batched views: rays of n_views cameras (device array), view v's pixel
-     * (x, y) at ray id view_off[v] + y * W_v + x; view_off[n_views] = rays */
+     * (x, y) at ray id view_off[v] + y * W_v + x; view_off[n_views] = rays;
+     * a ray's view is in its state's cnt2.w.  With view_caches, each view
+     * renders against its own frustum cache instead of `cache`. */
+    const ViewCache *view_caches;
     const DevCam *views;
     const int *view_off;
     int n_views;
@@ -259,7 +269,7 @@ cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, in
  * the device decide whether rays are still alive (at most p.max_iterations
  * sub-iterations; the iteration count is left in p.counters[5]).  The graph
  * holds p by value: it is valid while the buffers p points to are. */
-cudaError_t build_batch_graph(const RenderParams &p, int head_hidden, int n_sms, cudaStream_t s, int n_rays,
+cudaError_t build_batch_graph(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int n_rays,
                               cudaGraphExec_t *exec, int *n_kernels);
 
 /* differentiable render (fvc_backward.cu): pass 1 is render_frame over p.pixel_list */

@@ -188,12 +188,14 @@ __global__ void __launch_bounds__(256) wf_raygen_views_kernel(RenderParams p)
     bool hits = false;
     float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
     float tn = 0.f, tf = 0.f;
+    int view = 0;
     if (valid) {
         int lo = 0, hi = p.n_views - 1; /* the view holding ray i: last offset <= i */
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (p.view_off[mid] <= i) lo = mid; else hi = mid - 1;
         }
+        view = lo;
         const DevCam &cam = p.views[lo];
         const int local = i - p.view_off[lo];
         generate_ray(cam, local % cam.W, local / cam.W, o, d);
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(256) wf_raygen_views_kernel(RenderParams p)
         st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
         st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
         st.cnt = make_int4(i, 0, 0, 0);
-        st.cnt2 = make_int4(0, 0, 0, 0);
+        st.cnt2 = make_int4(0, 0, 0, view);
         p.states[0][base + __popc(m & lane_lt())] = st;
     }
 }
@@ -233,17 +235,17 @@ __global__ void wf_loop_cond_kernel(RenderParams p, cudaGraphConditionalHandle h
 
 /* Classification of one occupied sample, sample_cache_performance_kernel
  * (src/cache_performance_renderer.cu:91-163). */
-__device__ __forceinline__ int classify(const RenderParams &p, float3 oc, float3 dc, float tm)
+__device__ __forceinline__ int classify(const RenderParams &p, const CacheView &C, const DevCam &ccam, const DevSteps &cst,
+                                        float3 oc, float3 dc, float tm)
 {
     float tfr;
-    const float3 fr = cam2froxel(at(oc, dc, tm), p.ccam, p.csteps, tfr);
-    const CacheView &C = p.cache;
+    const float3 fr = cam2froxel(at(oc, dc, tm), ccam, cst, tfr);
     const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
     const bool inside = in_fov && fr.z >= 0.f && fr.z < (float)C.fD;
     bool unsampled = true;
     if (in_fov) {
         const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
-        unsampled = tfr < p.csteps.near_ || tfr > kr;
+        unsampled = tfr < cst.near_ || tfr > kr;
     }
     if (!inside || unsampled) return p.render_mode == 1 ? KIND_SKIP : KIND_RESAMPLE;
     if (p.render_mode == 2) return KIND_SKIP;
@@ -358,18 +360,22 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
             const float t0 = p.row_t0[r];
             const float4 of = states[slot].of, dt4 = states[slot].dt;
             const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
+            const ViewCache *vc = p.view_caches ? p.view_caches + states[slot].cnt2.w : nullptr;
+            const CacheView &C = vc ? vc->cache : p.cache;
+            const DevCam &ccam = vc ? vc->ccam : p.ccam;
+            const DevSteps &cst = vc ? vc->csteps : p.csteps;
             float3 oc, dc;
-            transform_ray(p.ccam.w2c, o, d, oc, dc);
+            transform_ray(ccam.w2c, o, d, oc, dc);
             const float dt = calc_step(p.steps, t0);
             const float tm = F_MUL(F_ADD(t0, F_ADD(t0, dt)), 0.5f);
-            kind = classify(p, oc, dc, tm);
+            kind = classify(p, C, ccam, cst, oc, dc, tm);
             const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));
             if (kind == KIND_RESAMPLE) {
                 const float3 pc = contract(p.scene, at(o, d, tmh));
                 p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
             } else if (kind == KIND_CACHE) {
                 float tf2;
-                const float3 fr = cam2froxel(at(oc, dc, tmh), p.ccam, p.csteps, tf2);
+                const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
                 p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
             }
             p.row_kind[r] = (uint8_t)kind;
@@ -461,6 +467,12 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(Rend
  * generateNetworkInput_cache_shfl_perf_kernel_cg
  * (src/cache_performance_renderer.cu:678-787): head input = log of the
  * interpolated density (not renormalised) and latents / interpolated isset. */
+/* the cache a row's ray renders against: its view's cache in a batch, else the renderer's */
+__device__ __forceinline__ const CacheView &row_cache(const RenderParams &p, const RayState *states, int r)
+{
+    return p.view_caches ? p.view_caches[states[p.row_slot[r]].cnt2.w].cache : p.cache;
+}
+
 __device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, int latent_offset, __half *trow)
 {
     const Voxel *vp[8];
@@ -512,7 +524,7 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
         const int r = k < n_rows ? p.cache_list[k] : -1;
         if (r >= 0) {
             const float4 pw = p.row_pay[r];
-            cache_lookup(p.cache, make_float3(pw.x, pw.y, pw.z), p.latent_offset, trow);
+            cache_lookup(row_cache(p, states, r), make_float3(pw.x, pw.y, pw.z), p.latent_offset, trow);
             sh16(dir01_of(states, p.row_slot[r]), reinterpret_cast<__half2 *>(trow + 32));
         } else {
 #pragma unroll
@@ -676,7 +688,7 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
             __half hin[32];
             if (r >= 0) {
                 const float4 pw = p.row_pay[r];
-                cache_lookup(p.cache, make_float3(pw.x, pw.y, pw.z), p.latent_offset, hin);
+                cache_lookup(row_cache(p, states, r), make_float3(pw.x, pw.y, pw.z), p.latent_offset, hin);
             } else {
                 for (int q = 16; q < 32; ++q) hin[q] = __float2half_rn(0.f);
             }
@@ -1252,7 +1264,7 @@ cudaError_t backward_frame(const RenderParams &p, const BwdParams &b, bool cache
                             : run_backward<false, 1>(p, b, n_sms, s, h_pinned, check_every, log);
 }
 
-template <int HH>
+template <bool CACHED, int HH>
 static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStream_t s, int n_rays, cudaGraphExec_t *exec,
                                        int *n_kernels)
 {
@@ -1305,13 +1317,29 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
     if (e == cudaSuccess) {
         const int grid_ray = n_sms * 16;
         for (int it = 0; it < 2; ++it) {
-            wf_march_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
-            launch_plain_net<HH>(p, it, n_sms, s);
-            wf_composite_kernel<false><<<grid_ray, 128, 0, s>>>(p, it);
-            wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, 0);
+            wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+            if (CACHED) {
+                const size_t tc_smem = sizeof(TcSmem);
+                const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
+                wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
+                if (p.use_tc) {
+                    wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+                    wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+                } else {
+                    wf_net_resample_kernel<HH, true><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
+                    wf_net_cache_kernel<HH><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
+                }
+                kernels += 3;
+            } else {
+                launch_plain_net<HH>(p, it, n_sms, s);
+                kernels += 1;
+            }
+            wf_composite_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+            wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, CACHED ? 1 : 0);
+            kernels += 3;
         }
         wf_loop_cond_kernel<<<1, 1, 0, s>>>(p, handle);
-        kernels += 9;
+        kernels += 1;
         cudaGraph_t g3 = nullptr;
         e = cudaStreamEndCapture(s, &g3);
     }
@@ -1321,11 +1349,14 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
     return e;
 }
 
-cudaError_t build_batch_graph(const RenderParams &p, int head_hidden, int n_sms, cudaStream_t s, int n_rays,
+cudaError_t build_batch_graph(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int n_rays,
                               cudaGraphExec_t *exec, int *n_kernels)
 {
-    return head_hidden == 2 ? build_batch_graph_t<2>(p, n_sms, s, n_rays, exec, n_kernels)
-                            : build_batch_graph_t<1>(p, n_sms, s, n_rays, exec, n_kernels);
+    if (cached)
+        return head_hidden == 2 ? build_batch_graph_t<true, 2>(p, n_sms, s, n_rays, exec, n_kernels)
+                                : build_batch_graph_t<true, 1>(p, n_sms, s, n_rays, exec, n_kernels);
+    return head_hidden == 2 ? build_batch_graph_t<false, 2>(p, n_sms, s, n_rays, exec, n_kernels)
+                            : build_batch_graph_t<false, 1>(p, n_sms, s, n_rays, exec, n_kernels);
 }
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,

@@ -201,6 +201,12 @@ class Renderer:
         arr, out = self._batch_args(infos, image, results, ray_counts)
         L.check(L.load().fvc_render_batch(self.handle, arr, len(infos), C.byref(out)))
 
+    def render_batch_cached(self, infos, caches, image=None, results=None, ray_counts=None) -> None:
+        """Cache renderers: view v renders against its own built cache caches[v]."""
+        arr, out = self._batch_args(infos, image, results, ray_counts)
+        handles = (C.c_void_p * len(caches))(*[c.handle.value for c in caches])
+        L.check(L.load().fvc_render_batch_cached(self.handle, arr, len(infos), handles, C.byref(out)))
+
     def autotune(self, infos, image=None, results=None, ray_counts=None) -> L.AutotuneResult:
         """Pick the network tile and marching batch that render this batch fastest."""
         arr, out = self._batch_args(infos, image, results, ray_counts)
@@ -312,6 +318,11 @@ class CachePerformanceRenderer(Renderer):
         super().__init__(scene_info, occupancy_grid, nerf_network)
         self._cache, self._cache_next = cache, next_cache
         L.check(L.load().fvc_renderer_set_caches(self.handle, cache.handle, next_cache.handle))
+
+    def attach_caches(self, cache: Cache, next_cache: Cache) -> None:
+        """Render from `cache`, build into `next_cache` (the constructor's pair)."""
+        L.check(L.load().fvc_renderer_set_caches(self.handle, cache.handle, next_cache.handle))
+        self._cache, self._cache_next = cache, next_cache
 
     def resizeCache(self, resolution, stepsize_info) -> None:
         L.check(L.load().fvc_cache_resize(self.handle, int(resolution[0]), int(resolution[1]), C.byref(stepsize_info)))

@@ -334,6 +334,13 @@ int fvc_cache_dims(fvc_cache *c, fvc_int3 *frustum_dims, fvc_int3 *brick_dims, f
  * (buffers, counts, path, precision) change. */
 int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out);
 
+/* The same for a cache renderer (CACHE_PERFORMANCE): view v renders against
+ * its own built frustum cache caches[v] (built with fvc_cache_build after
+ * fvc_renderer_set_caches(r, caches[v], caches[v]) at the view's cache pose),
+ * as CachePerformanceRenderer::render does for one view. */
+int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, fvc_cache *const *caches,
+                            const fvc_render_outputs *out);
+
 /* Times each candidate network tile (128-row tcgen05 CTA tiles or 32-row
  * mma.sync warp tiles) and marching batch (16, 32, 64 or 128 steps per ray
  * and sub-iteration) on this batch, keeps the fastest for the renderer. */

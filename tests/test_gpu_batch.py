@@ -80,3 +80,44 @@ def test_autotune_picks_a_valid_configuration():
     assert tuned.ms > 0 and tuned.rows_per_iteration > 0
     # the batch ran with the winner's network path: compare with single views on the same path
     _check(_single(loader, cams, tcgen05=tuned.m_tile == 128), res, cnt, img)
+
+
+def test_batch_with_per_view_caches_matches_single_cached_renders():
+    """Each view of a batch renders against its own frustum cache (built at
+    the view's pose; rendered from a pose rotated by 1 degree): the batch must
+    reproduce the per-view cached renders bit for bit."""
+    torch = pytest.importorskip("torch")
+    from frustumvolumecaching_gb300 import camera as fcam
+
+    loader = fvc.load_data(tiny_model(7, 1))
+    cams0 = _views(1500)
+    a = np.radians(1.0)
+    R = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+    cams1 = []
+    for c in cams0:
+        m = np.asarray(c["cam2world"], np.float64)
+        W, H = c["resolution"]
+        cams1.append(fcam.camera_dict(np.concatenate([R @ m[:, :3], (R @ m[:, 3])[:, None]], axis=1), W, H))
+    caches = [fvc.Cache() for _ in cams0]
+    r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network,
+                                     caches[0], caches[0])
+    r.setCacheSettings(fvc.default_cache_settings())
+    for c, cam in zip(caches, cams0):
+        r.attach_caches(c, c)
+        r.initCacheBlockwise(fvc.raymarch_info(cam, loader.stepsize_info))
+    n = sum(W * H for W, H in SIZES)
+    res = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    cnt = torch.zeros((n, 4), dtype=torch.int32, device="cuda")
+    img = torch.zeros((n, 4), dtype=torch.uint8, device="cuda")
+    infos1 = [fvc.raymarch_info(c, loader.stepsize_info) for c in cams1]
+    r.render_batch_cached(infos1, caches, image=img, results=res, ray_counts=cnt)
+    r.synchronize()
+    single = []
+    for c, cam in zip(caches, cams1):
+        r.attach_caches(c, c)
+        buf = fvc.RenderBuffer(cam["resolution"])
+        r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
+        single.append(buf)
+    counts = cnt.cpu().numpy()
+    assert counts[:, 1].sum() > 0 and counts[:, 0].sum() > 0  # both cache rows and resampled rows
+    _check(single, res.cpu().numpy(), counts, img.cpu().numpy())
