@@ -5,5 +5,5 @@ of include/fvc.h); this package holds its ctypes binding, the Python mirror of
 the reference's renderer API, and the seeded synthetic-model generator.
 """
 from .renderer import (BasicRenderer, Cache, CachePerformanceRenderer, Gradients, LoaderData, NerfNetwork,  # noqa: F401
-                       PerformanceRenderer, RenderBuffer, Renderer, camera_info, default_cache_settings, load_data,
-                       raymarch_info)
+                       PerformanceRenderer, RenderBuffer, Renderer, camera_info, default_cache_settings, ingp_export,
+                       load_data, raymarch_info)

@@ -114,6 +114,7 @@ SIGNATURES = {
     "fvc_last_error": (C.c_char_p, []),
     "fvc_version": (C.c_char_p, []),
     "fvc_model_load": (c_int, [C.c_char_p, PP]),
+    "fvc_ingp_export": (c_int, [C.c_char_p, C.c_char_p]),
     "fvc_model_destroy": (None, [P]),
     "fvc_model_info": (c_int, [P, C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
     "fvc_model_density": (c_int, [P, P, c_int, P]),

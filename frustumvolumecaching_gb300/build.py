@@ -18,8 +18,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libfvc.so")
-SOURCES = ["fvc_kernels.cu", "fvc_render.cu", "fvc_capi.cu", "fvc_noalloc.cu", "fvc_backward.cu"]
-HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", "fvc_tc.cuh", os.path.join("..", "..", "include", "fvc.h")]
+SOURCES = ["fvc_kernels.cu", "fvc_render.cu", "fvc_capi.cu", "fvc_noalloc.cu", "fvc_backward.cu", "fvc_ingp.cpp"]
+HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", "fvc_tc.cuh", "fvc_ingp.h", os.path.join("..", "..", "include", "fvc.h")]
 INCLUDE = os.path.join(PKG, "..", "include")
 EVAL_SRC = os.path.join(PKG, "cpp", "eval.cpp")
 EVAL = os.path.join(OUT_DIR, "eval")

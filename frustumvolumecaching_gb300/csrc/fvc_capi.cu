@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <map>
 #include <memory>
@@ -27,6 +28,7 @@
 #include <vector>
 
 #include "../../include/fvc.h"
+#include "fvc_ingp.h"
 #include "fvc_kernels.h"
 
 using namespace fvc;
@@ -412,13 +414,12 @@ struct fvc_renderer {
 /* ------------------------------------------------------------------------ */
 /* model loading                                                             */
 /* ------------------------------------------------------------------------ */
-static int load_model(const std::string &dir, fvc_model &m)
+/* The model from its configuration (the nerfacc config.json schema) and its
+ * four binary blobs: hash tables, density MLP, color head (fp16) and the
+ * linear occupancy grid (uchar [cascade][x][y][z]). */
+static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char> &wb, std::vector<char> &wh,
+                       std::vector<char> &occ, fvc_model &m)
 {
-    std::vector<char> txt;
-    if (!read_file(dir + "/config.json", txt)) return fail(FVC_ERR_IO, "Could not load config file: " + dir + "/config.json");
-    JParser jp{txt.data(), txt.data() + txt.size()};
-    JVal cfg = jp.parse();
-    if (!jp.ok || cfg.kind != JVal::OBJ) return fail(FVC_ERR_CONFIG, "config.json: parse error");
     const JVal &sc = cfg["scene"];
     if (sc.kind != JVal::OBJ) return fail(FVC_ERR_CONFIG, "config.json: missing scene");
     /* parse(SceneInfo&), include/parse_helper.h:25-54 */
@@ -426,7 +427,7 @@ static int load_model(const std::string &dir, fvc_model &m)
     s.grid_resolution = (int)sc.num_or("grid_resolution", 0);
     s.grid_nlvl = (int)sc.num_or("grid_nlvl", 0);
     s.vals_per_lvl = s.grid_resolution * s.grid_resolution * s.grid_resolution;
-    s.normalized = 0;
+    s.normalized = sc.bool_or("normalized", false); /* nerfacc exports: false (include/parse_helper.h:30) */
     if (s.grid_resolution != 128) return fail(FVC_ERR_CONFIG, "Performance Renderer only supports fixed grid resolution!");
     if (s.grid_nlvl < 1 || s.grid_nlvl > 8) return fail(FVC_ERR_CONFIG, "grid_nlvl out of range");
     const JVal &ab = sc["aabb"];
@@ -500,16 +501,11 @@ static int load_model(const std::string &dir, fvc_model &m)
         off += size;
     }
     m.table_entries = off;
-    std::vector<char> tab, wb, wh, occ;
-    if (!read_file(dir + "/pos_enc.dat", tab)) return fail(FVC_ERR_IO, "missing pos_enc.dat");
     if (tab.size() != (size_t)off * F * 2)
         return fail(FVC_ERR_IO, "pos_enc.dat: " + std::to_string(tab.size()) + " bytes, hash grid needs " + std::to_string((size_t)off * F * 2));
-    if (!read_file(dir + "/mlp_base.dat", wb)) return fail(FVC_ERR_IO, "missing mlp_base.dat");
     const int base_out_pad = (n_out + 15) / 16 * 16;
     if (wb.size() != (size_t)(64 * 32 + base_out_pad * 64) * 2) return fail(FVC_ERR_IO, "mlp_base.dat has the wrong size");
-    if (!read_file(dir + "/mlp_head.dat", wh)) return fail(FVC_ERR_IO, "missing mlp_head.dat");
     if (wh.size() != (size_t)(64 * 32 + (m.head_hidden - 1) * 64 * 64 + 16 * 64) * 2) return fail(FVC_ERR_IO, "mlp_head.dat has the wrong size");
-    if (!read_file(dir + "/occupancy_grid.dat", occ)) return fail(FVC_ERR_IO, "missing occupancy_grid.dat");
     const size_t vals = (size_t)128 * 128 * 128;
     if (occ.size() != vals * s.grid_nlvl) return fail(FVC_ERR_IO, "occupancy_grid.dat has the wrong size");
 
@@ -640,6 +636,191 @@ static int load_model(const std::string &dir, fvc_model &m)
     CU(cudaMemcpy(m.d_table, tab.data(), tab.size(), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_weights, W.data(), W.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_bias3, bias3.data(), 64 * sizeof(float), cudaMemcpyHostToDevice));
+    return FVC_OK;
+}
+
+/* load_nerfacc_export (src/loader.cu:232-285): config.json and four blobs */
+static int load_nerfacc(const std::string &dir, fvc_model &m)
+{
+    std::vector<char> txt, tab, wb, wh, occ;
+    if (!read_file(dir + "/config.json", txt)) return fail(FVC_ERR_IO, "Could not load config file: " + dir + "/config.json");
+    JParser jp{txt.data(), txt.data() + txt.size()};
+    JVal cfg = jp.parse();
+    if (!jp.ok || cfg.kind != JVal::OBJ) return fail(FVC_ERR_CONFIG, "config.json: parse error");
+    if (!read_file(dir + "/pos_enc.dat", tab)) return fail(FVC_ERR_IO, "missing pos_enc.dat");
+    if (!read_file(dir + "/mlp_base.dat", wb)) return fail(FVC_ERR_IO, "missing mlp_base.dat");
+    if (!read_file(dir + "/mlp_head.dat", wh)) return fail(FVC_ERR_IO, "missing mlp_head.dat");
+    if (!read_file(dir + "/occupancy_grid.dat", occ)) return fail(FVC_ERR_IO, "missing occupancy_grid.dat");
+    return build_model(cfg, tab, wb, wh, occ, m);
+}
+
+/* load_ingp_snapshot (src/loader.cu:146-230): the scene, step grid and
+ * network configuration the reference derives from an instant-ngp snapshot,
+ * the parameter blob split in its set_params order (density MLP, color MLP,
+ * hash grid; include/nerf_network.h:284-298), and the occupancy grid from the
+ * density grid thresholded at min(0.01, mean density of the first cascade)
+ * (ingp_density_grid_to_occupancy_grid, :73-114; the mean in float64). */
+static int ingp_to_export(const std::string &file, JVal &cfg, std::vector<char> &tab, std::vector<char> &wb,
+                          std::vector<char> &wh, std::vector<char> &occ)
+{
+    fvc_ingp::Snapshot sn;
+    std::string err;
+    if (!fvc_ingp::read_snapshot(file, sn, err)) return fail(FVC_ERR_IO, err);
+    auto num = [](double v) { JVal j; j.kind = JVal::NUM; j.num = v; return j; };
+    auto flag = [](bool v) { JVal j; j.kind = JVal::BOOL; j.b = v; return j; };
+    auto obj = []() { JVal j; j.kind = JVal::OBJ; return j; };
+    if (sn.aabb_scale < 1 || (sn.aabb_scale & (sn.aabb_scale - 1))) return fail(FVC_ERR_CONFIG, "aabb_scale must be a power of two");
+    const int nlvl = (int)std::log2((double)sn.aabb_scale) + 1;
+    JVal scene = obj();
+    scene.obj["grid_resolution"] = num(128);
+    scene.obj["grid_nlvl"] = num(nlvl);
+    scene.obj["normalized"] = flag(true);
+    JVal aabb;
+    aabb.kind = JVal::ARR;
+    for (int k = 0; k < 3; ++k) aabb.arr.push_back(num(sn.aabb_min[k]));
+    for (int k = 0; k < 3; ++k) aabb.arr.push_back(num(sn.aabb_max[k]));
+    scene.obj["aabb"] = aabb;
+    scene.obj["is_open_gl"] = flag(false);
+    scene.obj["alpha_thre"] = num(0.0);
+    scene.obj["cone_angle"] = num(nlvl <= 1 ? 0.0f : 1.0f / 256.0f);
+    scene.obj["stepsize"] = num(std::sqrt(3.0f) / 1024.f);
+    scene.obj["near"] = num(0.0);
+    scene.obj["far"] = num(1e10f);
+    JVal enc = obj();
+    enc.obj["n_levels"] = num(sn.n_levels);
+    enc.obj["n_features_per_level"] = num(sn.n_features);
+    enc.obj["log2_hashmap_size"] = num(sn.log2_hashmap_size);
+    enc.obj["base_resolution"] = num(sn.base_resolution);
+    const float pls = std::exp(std::log(2048.f * (float)sn.aabb_scale / (float)sn.base_resolution) / (float)(sn.n_levels - 1.f));
+    enc.obj["per_level_scale"] = num(pls);
+    JVal bnet = obj(), hnet = obj();
+    bnet.obj["n_neurons"] = num(sn.base_neurons);
+    bnet.obj["n_hidden_layers"] = num(sn.base_hidden);
+    hnet.obj["n_neurons"] = num(sn.head_neurons);
+    hnet.obj["n_hidden_layers"] = num(sn.head_hidden);
+    JVal base = obj(), head = obj();
+    base.obj["encoding"] = enc;
+    base.obj["network"] = bnet;
+    base.obj["n_output"] = num(16);
+    head.obj["network"] = hnet;
+    head.obj["first_latent_is_density"] = flag(true); /* NerfNetwork::init keeps the default */
+    head.obj["n_latents"] = num(16);
+    head.obj["n_input"] = num(32);
+    JVal nested;
+    nested.kind = JVal::ARR;
+    JVal sh = obj();
+    sh.obj["degree"] = num(sn.sh_degree);
+    nested.arr.push_back(sh);
+    JVal dir_enc = obj();
+    dir_enc.obj["nested"] = nested;
+    head.obj["encoding"] = dir_enc;
+    cfg = obj();
+    cfg.obj["scene"] = scene;
+    cfg.obj["mlp_base"] = base;
+    cfg.obj["mlp_head"] = head;
+    /* parameter blob: density MLP [64 x 32][16 x 64], color MLP [64 x 32]([64 x 64])[16 x 64], hash grid */
+    const size_t n_base = 64 * 32 + 16 * 64;
+    const size_t n_head = 64 * 32 + (size_t)std::max(0, sn.head_hidden - 1) * 64 * 64 + 16 * 64;
+    if (sn.params.size() < n_base + n_head) return fail(FVC_ERR_IO, file + ": params_binary too small for the networks");
+    auto bytes = [&](size_t off, size_t n) {
+        std::vector<char> v(n * 2);
+        std::memcpy(v.data(), sn.params.data() + off, n * 2);
+        return v;
+    };
+    wb = bytes(0, n_base);
+    wh = bytes(n_base, n_head);
+    tab = bytes(n_base + n_head, sn.params.size() - n_base - n_head);
+    /* occupancy: density grid (Morton order per cascade) -> linear uchar [cascade][x][y][z] */
+    const size_t vals = (size_t)128 * 128 * 128;
+    if (sn.density_grid.size() != vals * nlvl) return fail(FVC_ERR_IO, file + ": density_grid_binary does not hold the cascades");
+    double mean = 0.0;
+    for (size_t i = 0; i < vals; ++i) mean += std::max(0.0f, h2f(sn.density_grid[i])) / (double)vals;
+    const float thresh = std::min(0.01f, (float)mean);
+    auto compact = [](uint32_t x) {
+        x &= 0x49249249u; x = (x | (x >> 2)) & 0xc30c30c3u; x = (x | (x >> 4)) & 0x0f00f00fu;
+        x = (x | (x >> 8)) & 0xff0000ffu; x = (x | (x >> 16)) & 0x0000ffffu; return x;
+    };
+    occ.assign(vals * nlvl, 0);
+    for (size_t i = 0; i < vals * nlvl; ++i) {
+        const size_t lvl = i / vals;
+        const uint32_t j = (uint32_t)(i % vals);
+        const uint32_t x = compact(j), y = compact(j >> 1), z = compact(j >> 2);
+        occ[lvl * vals + (size_t)x * 16384 + y * 128 + z] = h2f(sn.density_grid[i]) > thresh ? 1 : 0;
+    }
+    return FVC_OK;
+}
+
+static int load_ingp(const std::string &file, fvc_model &m)
+{
+    JVal cfg;
+    std::vector<char> tab, wb, wh, occ;
+    if (int rc = ingp_to_export(file, cfg, tab, wb, wh, occ)) return rc;
+    return build_model(cfg, tab, wb, wh, occ, m);
+}
+
+static void write_json(const JVal &v, std::string &o)
+{
+    char buf[40];
+    switch (v.kind) {
+        case JVal::NUL: o += "null"; break;
+        case JVal::BOOL: o += v.b ? "true" : "false"; break;
+        case JVal::NUM: std::snprintf(buf, sizeof buf, "%.17g", v.num); o += buf; break;
+        case JVal::STR: o += '"' + v.str + '"'; break;
+        case JVal::ARR:
+            o += '[';
+            for (size_t i = 0; i < v.arr.size(); ++i) {
+                if (i) o += ", ";
+                write_json(v.arr[i], o);
+            }
+            o += ']';
+            break;
+        case JVal::OBJ: {
+            o += '{';
+            bool first = true;
+            for (const auto &kv : v.obj) {
+                if (!first) o += ", ";
+                first = false;
+                o += '"' + kv.first + "\": ";
+                write_json(kv.second, o);
+            }
+            o += '}';
+            break;
+        }
+    }
+}
+
+static bool write_blob(const std::string &path, const std::string &data)
+{
+    std::ofstream f(path, std::ios::binary);
+    f.write(data.data(), (std::streamsize)data.size());
+    return (bool)f;
+}
+
+/* load_data (src/loader.cu:287-300): an .ingp snapshot file or a nerfacc export directory */
+static bool is_ingp(const std::string &path) { return std::filesystem::path(path).extension() == ".ingp"; }
+
+static int load_model(const std::string &path, fvc_model &m)
+{
+    return is_ingp(path) ? load_ingp(path, m) : load_nerfacc(path, m);
+}
+
+/* host only: an .ingp snapshot rewritten as the equivalent nerfacc export */
+extern "C" int fvc_ingp_export(const char *snapshot, const char *export_dir)
+{
+    CHECK_ARG(snapshot && export_dir, "fvc_ingp_export: null argument");
+    JVal cfg;
+    std::vector<char> tab, wb, wh, occ;
+    if (int rc = ingp_to_export(snapshot, cfg, tab, wb, wh, occ)) return rc;
+    std::error_code ec;
+    std::filesystem::create_directories(export_dir, ec);
+    const std::string dir(export_dir);
+    std::string js;
+    write_json(cfg, js);
+    auto str = [](const std::vector<char> &v) { return std::string(v.data(), v.size()); };
+    if (!write_blob(dir + "/config.json", js) || !write_blob(dir + "/pos_enc.dat", str(tab)) ||
+        !write_blob(dir + "/mlp_base.dat", str(wb)) || !write_blob(dir + "/mlp_head.dat", str(wh)) ||
+        !write_blob(dir + "/occupancy_grid.dat", str(occ)))
+        return fail(FVC_ERR_IO, "fvc_ingp_export: could not write " + dir);
     return FVC_OK;
 }
 

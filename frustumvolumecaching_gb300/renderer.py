@@ -15,6 +15,7 @@ Errors are raised as FvcError (the reference throws std::runtime_error).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -52,6 +53,13 @@ class NerfNetwork:
         L.check(L.load().fvc_model_density(self.handle, L.ptr(pos), pos.shape[0], L.ptr(out)))
         return out
 
+    def properties(self) -> dict:
+        """First-latent-is-density, head depth, hash levels, latents and the
+        device occupancy bitfield (fvc_model_properties)."""
+        p = L.ModelProps()
+        L.check(L.load().fvc_model_properties(self.handle, C.byref(p)))
+        return {k: getattr(p, k) for k, _ in p._fields_}
+
     def debug_encode(self, pos: np.ndarray):
         pos = np.ascontiguousarray(pos, np.float32)
         f = np.zeros((pos.shape[0], 32), np.float32)
@@ -71,6 +79,7 @@ class LoaderData:
     scene_info: L.SceneInfo
     stepsize_info: L.StepsizeInfo
     nerf_network: NerfNetwork
+    data_source: str = "nerfacc"  # DataSource INGP / NERFACC (include/loader.h:15-19)
 
     @property
     def occupancy_grid_morton_bitfield(self):
@@ -78,9 +87,18 @@ class LoaderData:
 
 
 def load_data(path: str) -> LoaderData:
-    """load_data(fs::path, LoaderData&), src/loader.cu:287-300 (nerfacc export)."""
-    net = NerfNetwork(path)
-    return LoaderData(net.scene_info, net.stepsize_info, net)
+    """load_data(fs::path, LoaderData&), src/loader.cu:287-300: an instant-ngp
+    snapshot (``.ingp``) or a nerfacc export directory."""
+    net = NerfNetwork(str(path))
+    src = "ingp" if os.path.splitext(str(path))[1] == ".ingp" else "nerfacc"
+    return LoaderData(net.scene_info, net.stepsize_info, net, src)
+
+
+def ingp_export(snapshot: str, export_dir: str) -> str:
+    """Rewrites an instant-ngp snapshot as the equivalent nerfacc export
+    directory (host only; no GPU needed)."""
+    L.check(L.load().fvc_ingp_export(str(snapshot).encode(), str(export_dir).encode()))
+    return str(export_dir)
 
 
 def camera_info(cam: dict) -> L.CameraInfo:

@@ -165,9 +165,18 @@ const char *fvc_version(void);
 
 /* ------------------------------------------------------------------------ */
 /* model (reference: bool load_data(fs::path, LoaderData&), include/loader.h:49,   */
-/* src/loader.cu:232-300 nerfacc export: config.json + *.dat)                 */
+/* src/loader.cu:146-300): a path ending in ".ingp" is an instant-ngp snapshot */
+/* (load_ingp_snapshot), any other path a nerfacc export directory            */
+/* (load_nerfacc_export: config.json + *.dat)                                 */
 /* ------------------------------------------------------------------------ */
 int fvc_model_load(const char *data_dir, fvc_model **out);
+/* Host only (no device work): the .ingp snapshot rewritten as the equivalent
+ * nerfacc export directory - the scene, step and network configuration that
+ * load_ingp_snapshot derives (src/loader.cu:176-213), the parameter blob split
+ * into hash grid / density MLP / color MLP, and the occupancy grid thresholded
+ * from the density grid (:73-114).  Loading the directory renders the same as
+ * loading the snapshot. */
+int fvc_ingp_export(const char *snapshot, const char *export_dir);
 void fvc_model_destroy(fvc_model *m);
 /* Scene and step parameters of the loaded model (LoaderData::scene_info,
  * ::stepsize_info after StepsizeInfo::setAdditionalInfo, include/common.h:109-131). */

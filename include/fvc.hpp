@@ -416,9 +416,9 @@ struct LoaderData {
     }
 };
 
-/* load_data(fs::path, LoaderData&), src/loader.cu:287-300: the nerfacc export
- * directory (config.json + tables/weights/occupancy).  Prints the reason and
- * returns false on failure. */
+/* load_data(fs::path, LoaderData&), src/loader.cu:287-300: an instant-ngp
+ * snapshot (extension .ingp) or a nerfacc export directory (config.json +
+ * tables/weights/occupancy).  Prints the reason and returns false on failure. */
 inline bool load_data(fs::path data_dir, LoaderData &d)
 {
     fvc_model *m = nullptr;
@@ -430,7 +430,7 @@ inline bool load_data(fs::path data_dir, LoaderData &d)
     fvc_model_props props{};
     fvc_model_info(m, reinterpret_cast<fvc_scene_info *>(&d.scene_info), reinterpret_cast<fvc_stepsize_info *>(&d.stepsize_info));
     fvc_model_properties(m, &props);
-    d.data_source = NERFACC;
+    d.data_source = data_dir.extension() == fs::path(".ingp") ? INGP : NERFACC;
     d.nerf_network._model = m;
     d.nerf_network.m_first_latent_is_density = props.first_latent_is_density != 0;
     d.nerf_network.m_head_hidden_layers = props.head_hidden_layers;

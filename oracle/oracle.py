@@ -117,7 +117,7 @@ def default_threads() -> int:
 def make_scene(cfg_scene: dict) -> OrcScene:
     s = OrcScene()
     s.grid_nlvl = int(cfg_scene["grid_nlvl"])
-    s.normalized = 0
+    s.normalized = int(bool(cfg_scene.get("normalized", False)))  # nerfacc exports: false; .ingp snapshots: true
     a = cfg_scene["aabb"]
     s.aabb_from[:] = a[:3]
     s.aabb_to[:] = a[3:]
