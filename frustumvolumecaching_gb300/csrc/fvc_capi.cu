@@ -989,6 +989,33 @@ static int check_info(const fvc_raymarch_info *info)
     return FVC_OK;
 }
 
+/* The head input layout each variant produces must match the model's
+ * latent_offset: DensityIntermediates puts the density in latent 0 (a model
+ * whose first latent is the density), the others put log-density in row 0
+ * ahead of the latents (a model whose first latent is not).  eval picks the
+ * variant from the model the same way (src/eval.cu:215-222). */
+static int check_variant(const fvc_renderer *r)
+{
+    /* the cache stores 8 latents per voxel (two half4 arrays, include/cache.h:24-27) */
+    if (r->m->n_latents > 8)
+        return fail(FVC_ERR_CONFIG, "the cache stores 8 latents per voxel; this model's head reads " +
+                                        std::to_string(r->m->n_latents));
+    const bool di = r->settings.interpol_variant == VARIANT_DENSITY_INTERMEDIATES;
+    if (di && r->m->latent_offset != 0)
+        return fail(FVC_ERR_CONFIG, "the DensityIntermediates cache variant needs a model whose first latent is the density");
+    if (!di && r->m->latent_offset != 1)
+        return fail(FVC_ERR_CONFIG, "the " + std::string(r->settings.interpol_variant == VARIANT_DENSITY ? "Density" : "Alpha") +
+                                        " cache variants need a model whose first latent is not the density "
+                                        "(use DensityIntermediates)");
+    return FVC_OK;
+}
+
+static void apply_settings(const fvc_renderer *r, CacheView &v)
+{
+    v.interp = r->settings.interpol_function;
+    v.first_latent_is_density = r->settings.interpol_variant == VARIANT_DENSITY_INTERMEDIATES;
+}
+
 static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts,
                                RenderParams &p, bool per_view_caches = false)
 {
@@ -1015,8 +1042,8 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.max_rounds = 1 << 26;
     p.max_samples_per_ray = r->max_samples;
     if (cached) {
-        if (m->latent_offset != 1)
-            return fail(FVC_ERR_CONFIG, "the Density cache variant needs a model whose first latent is not the density");
+        int rc;
+        if ((rc = check_variant(r))) return rc;
         p.render_mode = r->render_mode;
         if (!per_view_caches) {
             fvc_cache *c = r->cache;
@@ -1024,6 +1051,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
             p.ccam = dev_cam(c->rm_info.cam_info);
             p.csteps = dev_steps(c->rm_info.stepsize_info);
             p.cache = c->view();
+            apply_settings(r, p.cache);
         }
     }
     if (info->cam_info.resolution.x != r->W || info->cam_info.resolution.y != r->H) {
@@ -1191,11 +1219,22 @@ extern "C" int fvc_renderer_set_caches(fvc_renderer *r, fvc_cache *cache, fvc_ca
 extern "C" int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_settings *s)
 {
     CHECK_ARG(r && s, "fvc_renderer_set_cache_settings: null argument");
-    if (s->interpol_variant != 0 || s->interpol_function != 0 || !s->use_inter_brick_interpolation)
-        return fail(FVC_ERR_CONFIG, "only the default cache settings (Density, Linear, inter-brick) are built");
+    if (s->interpol_function < INTERP_LINEAR || s->interpol_function > INTERP_NEAREST)
+        return fail(FVC_ERR_ARG, "fvc_renderer_set_cache_settings: unknown InterpolFunction");
+    if (s->interpol_variant < VARIANT_DENSITY || s->interpol_variant > VARIANT_ALPHA_INTERMEDIATES)
+        return fail(FVC_ERR_ARG, "fvc_renderer_set_cache_settings: unknown DensityInterpolVariant");
+    /* the performance renderer never writes the density slot in this variant,
+     * so it classifies no sample as a cache sample */
+    if (s->interpol_variant == VARIANT_INTERMEDIATES)
+        return fail(FVC_ERR_CONFIG, "the Intermediates variant stores no density, which the cached performance renderer "
+                                    "needs to classify cache samples");
+    /* use_hw_interpol, reweight_intermediates, disable_reweighting_first_intermediate and
+     * use_inter_brick_interpolation steer CacheBasicRenderer only; the performance
+     * renderer ignores them, as the reference's does */
     r->settings = *s;
     return FVC_OK;
 }
+
 
 /* Cache::resize (src/cache.cu:44-84) with the sizing of
  * CacheRenderer::resizeCache (src/cache_renderer.cu:832-846). */
@@ -1284,8 +1323,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     int rc;
     if ((rc = check_info(info))) return rc;
     fvc_model *m = r->m;
-    if (m->latent_offset != 1)
-        return fail(FVC_ERR_CONFIG, "the Density cache variant needs a model whose first latent is not the density");
+    if ((rc = check_variant(r))) return rc;
     std::lock_guard<std::mutex> lk(r->write_mutex);
     fvc_cache *c = r->next;
     const int W = info->cam_info.resolution.x, H = info->cam_info.resolution.y;
@@ -1301,6 +1339,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     memset(&p, 0, sizeof(p));
     p.scene = m->dscene; p.steps = dev_steps(info->stepsize_info); p.cam = dev_cam(info->cam_info); p.grid = m->grid;
     p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.latent_offset = m->latent_offset;
+    p.variant = r->settings.interpol_variant;
     p.bX = c->bX; p.bY = c->bY; p.bZ = c->bZ; p.fW = c->fW; p.fH = c->fH; p.fD = c->fD;
     p.dX = c->dX; p.dY = c->dY; p.dZ = c->dZ; p.capacity = c->capacity();
     p.rays = b.rays; p.block_step = b.block_step; p.tile_alive = b.tile_alive;
@@ -1584,6 +1623,9 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     }
     if (cached) {
         if (!r->cache || !r->cache->built) return fail(FVC_ERR_CACHE_UNINIT, "Cache is not initialized!");
+        if (r->settings.interpol_variant == VARIANT_DENSITY_INTERMEDIATES)
+            return fail(FVC_ERR_CONFIG, "fvc_render_backward: the cache-latent adjoint is built for the variants that keep "
+                                        "the density out of the latents");
         const size_t n_lat = (size_t)r->cache->capacity() * 512 * 8;
         if (g->n_lat != n_lat) {
             dfree(g->d_lat); dfree(g->s_lat);
@@ -1689,6 +1731,7 @@ static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_vi
         std::vector<ViewCache> vcs(n_views);
         for (int v = 0; v < n_views; ++v) {
             vcs[v].cache = caches[v]->view();
+            apply_settings(r, vcs[v].cache);
             vcs[v].ccam = dev_cam(caches[v]->rm_info.cam_info);
             vcs[v].csteps = dev_steps(caches[v]->rm_info.stepsize_info);
         }

@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(64) cache_composite_kernel(CacheBuildParams p)
         for (int s = 0; s < 8; ++s) rows[s] = rof[s * 64 + k];
         /* density-only compositing (accumulateNew_cache_init_second_kernel :349-393) */
         int visible = 0;
+        float alphas[8];
         {
             float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
             float T = cr.T;
@@ -277,10 +278,12 @@ __global__ void __launch_bounds__(64) cache_composite_kernel(CacheBuildParams p)
                 const float dt = calc_step(p.steps, t0);
                 t1 = F_ADD(t0, dt);
                 const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
+                alphas[s] = 0.f;
                 if (tm > cr.far_) { cr.alive = 0; continue; }
                 if (rows[s] < 0) continue;
                 const float sigma = expf(__half2float(p.build_den[rows[s]]));
                 const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
+                alphas[s] = alpha;
                 if (alpha > p.scene.alpha_thre) { T *= 1.0f - alpha; ++visible; }
                 if (T < 1e-4f) cr.alive = 0;
             }
@@ -300,9 +303,15 @@ __global__ void __launch_bounds__(64) cache_composite_kernel(CacheBuildParams p)
             for (int s = 0; s < 8; ++s) {
                 Voxel v;
                 if (rows[s] >= 0) {
-                    v.density = expf(__half2float(p.build_den[rows[s]]));
+                    /* the voxel's density slot and latent 0 per interpol_variant
+                     * (accumulateNew_cache_init_second_kernel :459-507) */
+                    const float sigma = expf(__half2float(p.build_den[rows[s]]));
+                    const bool by_alpha = p.variant == VARIANT_ALPHA || p.variant == VARIANT_ALPHA_INTERMEDIATES;
+                    v.density = by_alpha ? alphas[s] : sigma;
                     v.isset = 1.0f;
                     v.lat = p.build_lat[rows[s]];
+                    if (p.variant == VARIANT_DENSITY_INTERMEDIATES || p.variant == VARIANT_ALPHA_INTERMEDIATES)
+                        v.lat.x = (v.lat.x & 0xffff0000u) | (uint32_t)__half_as_ushort(__float2half_rn(v.density));
                 } else {
                     v.density = 0.f; v.isset = 0.f; v.lat = make_uint4(0, 0, 0, 0);
                 }

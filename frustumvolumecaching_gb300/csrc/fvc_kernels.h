@@ -20,7 +20,25 @@ struct CacheView {
     const void *voxels;
     int fW, fH, fD, bX, bY, bZ, dX, dY, dZ;
     int n_valid_slots;          /* slots written by the last build; others read as zero */
+    int interp;                 /* CacheSettings::interpol_function of the render (InterpolFunction) */
+    int first_latent_is_density; /* interpol_variant DensityIntermediates: latent 0 holds the density */
 };
+
+enum : int { INTERP_LINEAR = 0, INTERP_SMOOTHSTEP = 1, INTERP_SMOOTHERSTEP = 2, INTERP_NEAREST = 3 };
+enum : int { VARIANT_DENSITY = 0, VARIANT_ALPHA = 1, VARIANT_INTERMEDIATES = 2, VARIANT_DENSITY_INTERMEDIATES = 3,
+             VARIANT_ALPHA_INTERMEDIATES = 4 };
+
+/* applyInterpolationFunction (include/raymarch_common.h:393-402) on one
+ * trilinear fraction t in [0, 1): smoothstep t^2 (3 - 2t), smootherstep
+ * t^3 (t (6t - 15) + 10) (include/util/helper_math_extension.h:146-181),
+ * nearest = round half to even */
+__device__ __forceinline__ float interp_weight(float t, int fn)
+{
+    if (fn == INTERP_SMOOTHSTEP) return (t * t) * (3.0f - 2.0f * t);
+    if (fn == INTERP_SMOOTHERSTEP) return ((t * t) * t) * (t * (6.0f * t - 15.0f) + 10.0f);
+    if (fn == INTERP_NEAREST) return rintf(t);
+    return t;
+}
 
 /* weights of the tcgen05 network in canonical K-major tiles (bytes) */
 constexpr int TC_B1 = 0;        /* 64 x 32 */
@@ -58,7 +76,12 @@ __device__ __forceinline__ void cache_corners(const CacheView &C, float3 f, cons
 {
     const float fx = F_SUB(f.x, 0.5f), fy = F_SUB(f.y, 0.5f), fz = F_SUB(f.z, 0.5f);
     const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
-    const float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
+    float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
+    if (C.interp != INTERP_LINEAR) {
+        lx = interp_weight(lx, C.interp);
+        ly = interp_weight(ly, C.interp);
+        lz = interp_weight(lz, C.interp);
+    }
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
@@ -220,6 +243,7 @@ struct CacheBuildParams {
     const __half2 *table;
     const uint2 *weights;
     int latent_offset;
+    int variant;                /* CacheSettings::interpol_variant: what the voxels' density and latent 0 hold */
     int bX, bY, bZ, fW, fH, fD, dX, dY, dZ, capacity;
     CacheRay *rays;             /* [tiles][64] */
     int *block_step;            /* [tiles] */

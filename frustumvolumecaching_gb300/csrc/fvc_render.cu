@@ -498,8 +498,17 @@ __device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, int l
     uint32_t *hin = reinterpret_cast<uint32_t *>(trow + 16);
 #pragma unroll
     for (int c = 0; c < 8; ++c) hin[c] = 0u;
-    trow[16] = __float2half_rn(logf(fmaxf(dsum, 1e-6f)));
     const float inv = 1.0f / wsum;
+    if (C.first_latent_is_density) {
+        /* DensityIntermediates (:776-781): latent 0 holds the density; the
+         * head input is log(sum w density) * wsum / wsum, the other latents
+         * are renormalised by the interpolated isset */
+        trow[16] = __float2half_rn(__fdiv_rn(logf(ls[0]) * wsum, wsum));
+#pragma unroll
+        for (int j = 1; j < 8; ++j) trow[16 + latent_offset + j] = __float2half_rn(ls[j] * inv);
+        return;
+    }
+    trow[16] = __float2half_rn(logf(fmaxf(dsum, 1e-6f)));
 #pragma unroll
     for (int j = 0; j < 8; ++j) trow[16 + latent_offset + j] = __float2half_rn(ls[j] * inv);
 }

@@ -57,7 +57,7 @@ def main(argv=None) -> None:
             build = r._init_stats
         r.render_device(info)
         st = r._render_stats
-        line = {"frame": i, "resample_rows": st.n_resamples, "cache_rows": st.n_cache_hits,
+        line = {"frame": i, "resample_rows": st.n_resamples, "cache_rows": st.n_cache_hits, "steps": st.n_steps,
                 "launches": st.n_launches, "resample_kernel_launches": st.n_timed_launches,
                 "resample_kernel_ms": round(st.timed_kernel_ms, 3), "guard": st.guard_flags}
         if args.path == "cached":

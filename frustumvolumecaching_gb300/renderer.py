@@ -365,15 +365,30 @@ class CachePerformanceRenderer(Renderer):
         return s
 
 
-def default_cache_settings() -> L.CacheSettings:
-    """CacheRenderer::default_cache_settings, include/cache_renderer.h:55-63."""
+# DensityInterpolVariant and InterpolFunction (include/cache_renderer.h:14-22, include/common.h:221-227)
+DENSITY, ALPHA, INTERMEDIATES, DENSITY_INTERMEDIATES, ALPHA_INTERMEDIATES = range(5)
+LINEAR, SMOOTHSTEP, SMOOTHERSTEP, NEAREST = range(4)
+
+
+def default_cache_settings(interpol_variant: int = DENSITY, interpol_function: int = LINEAR) -> L.CacheSettings:
+    """CacheRenderer::default_cache_settings, include/cache_renderer.h:55-63,
+    optionally with another variant / interpolation function."""
     s = L.CacheSettings()
-    s.interpol_variant, s.interpol_function = 0, 0
+    s.interpol_variant, s.interpol_function = interpol_variant, interpol_function
     s.use_hw_interpol = s.reweight_intermediates = s.disable_reweighting_first_intermediate = 1
     s.use_inter_brick_interpolation = 1
     return s
 
 
+def eval_cache_settings(loader) -> L.CacheSettings:
+    """The settings eval gives the cache renderer (src/eval.cu:215-222):
+    DensityIntermediates for a model whose first latent is the density,
+    else Density; Linear interpolation."""
+    fld = bool(loader.nerf_network.properties()["first_latent_is_density"])
+    return default_cache_settings(DENSITY_INTERMEDIATES if fld else DENSITY, LINEAR)
+
+
 __all__ = ["load_data", "LoaderData", "NerfNetwork", "Renderer", "BasicRenderer", "PerformanceRenderer", "Cache", "Gradients",
            "CachePerformanceRenderer", "RenderBuffer", "raymarch_info", "camera_info", "camera_dict",
-           "default_cache_settings"]
+           "default_cache_settings", "eval_cache_settings", "DENSITY", "ALPHA", "INTERMEDIATES", "DENSITY_INTERMEDIATES",
+           "ALPHA_INTERMEDIATES", "LINEAR", "SMOOTHSTEP", "SMOOTHERSTEP", "NEAREST"]

@@ -106,8 +106,10 @@ typedef struct FVC_ALIGN(16) { float r, g, b, transmittance; } fvc_ray_result;
 
 /* CacheSettings, include/cache_renderer.h:24-32 (enum fields as int). */
 typedef struct {
-    int interpol_variant;      /* DensityInterpolVariant: 0 Density (only one built) */
-    int interpol_function;     /* InterpolFunction: 0 Linear (only one built)       */
+    int interpol_variant;      /* DensityInterpolVariant: 0 Density, 1 Alpha, 3 DensityIntermediates,
+                                  4 AlphaIntermediates (2 Intermediates -> FVC_ERR_CONFIG) */
+    int interpol_function;     /* InterpolFunction (include/common.h:221-227): 0 Linear, 1 Smoothstep,
+                                  2 Smootherstep, 3 Nearest */
     uint8_t use_hw_interpol;
     uint8_t reweight_intermediates;
     uint8_t disable_reweighting_first_intermediate;
@@ -305,8 +307,15 @@ void fvc_cache_destroy(fvc_cache *c);
 int fvc_renderer_set_caches(fvc_renderer *r, fvc_cache *cache, fvc_cache *next_cache);
 /* resizeCache(int2 resolution, StepsizeInfo), src/cache_renderer.cu:832-846. */
 int fvc_cache_resize(fvc_renderer *r, int width, int height, const fvc_stepsize_info *steps);
-/* setCacheSettings, include/cache_renderer.h:266-267. Only the reference
- * defaults with interpol_variant Density are built (others -> FVC_ERR_CONFIG). */
+/* setCacheSettings, include/cache_renderer.h:75. The settings the cached
+ * performance renderer reads (src/cache_performance_renderer.cu:1094,
+ * 491, 617, 714): interpol_function for the trilinear weights, and
+ * interpol_variant for what a build stores in the voxels' density slot and
+ * latent 0 and how a lookup forms the head input. DensityIntermediates
+ * needs a model whose first latent is the density, the other variants one
+ * whose first latent is not (FVC_ERR_CONFIG at build / render otherwise);
+ * Intermediates -> FVC_ERR_CONFIG. The remaining flags only steer the basic
+ * cache renderer and are ignored here, as in the reference. */
 int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_settings *s);
 /* initCacheBlockwise(RaymarchInfo, RenderBuffer&), src/cache_renderer.cu:931-1051:
  * fills the "next" cache. Synchronous. */

@@ -709,9 +709,9 @@ struct Cache {
 };
 
 enum DensityInterpolVariant { Density = 0, Alpha = 1, Intermediates = 2, DensityIntermediates = 3, AlphaIntermediates = 4 };
-enum InterpolFunction { Linear = 0 };
+enum InterpolFunction { Linear = 0, Smoothstep = 1, Smootherstep = 2, Nearest = 3 };
 
-/* CacheSettings, include/cache_renderer.h:24-32 (only the default combination is built). */
+/* CacheSettings, include/cache_renderer.h:24-32. */
 struct CacheSettings {
     DensityInterpolVariant interpol_variant;
     InterpolFunction interpol_function;

@@ -301,7 +301,11 @@ inline void dense_layer(const double *W, int out, int in, const double *x, doubl
         double s = 0.0;
         const double *w = W + (size_t)o * in;
         for (int i = 0; i < in; ++i) s += w[i] * x[i];
-        if (relu && s < 0.0) s = 0.0;
+        /* ReLU maps NaN to 0, as fmaxf(x, 0) does on the GPU: a cache lookup
+         * whose interpolated isset is 0 (possible with Nearest interpolation,
+         * whose texel can differ from the classification's) yields 0/0
+         * latents in the reference's formula */
+        if (relu && !(s > 0.0)) s = 0.0;
         y[o] = mimic ? round_h(s) : s;
     }
 }
@@ -561,7 +565,22 @@ struct OrcCache {
     int n_bricks_set, n_demanded, n_iterations;
     long long n_samples;
     int32_t *slot_of_brick_order; /* optional: [capacity] tile index per slot (may be NULL) */
+    /* CacheSettings (include/cache_renderer.h:24-32): interpol_variant steers
+     * what a build stores and how a lookup forms the head input;
+     * interpol_function the trilinear weights of a lookup */
+    int variant, interp;
 };
+
+/* applyInterpolationFunction, include/raymarch_common.h:393-402, with the
+ * smoothstep / smootherstep polynomials of
+ * include/util/helper_math_extension.h:146-181; float as the reference */
+inline float interp_fn(float t, int fn)
+{
+    if (fn == 1) return (t * t) * (3.0f - 2.0f * t);
+    if (fn == 2) return ((t * t) * t) * (t * (6.0f * t - 15.0f) + 10.0f);
+    if (fn == 3) return nearbyintf(t);
+    return t;
+}
 
 inline int pack3(int x, int y, int z) { return (x << 20) | (y << 10) | z; }
 
@@ -602,7 +621,7 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
     int counter = 0;
     long long n_samples = 0;
     int iter = 0;
-    struct TileWork { int n_steps; int need; std::vector<uint8_t> mask; std::vector<double> sig, lat; };
+    struct TileWork { int n_steps; int need; std::vector<uint8_t> mask; std::vector<double> sig, alpha, lat; };
     std::vector<TileWork> work(nT);
     for (; iter < 1000; ++iter) {
         std::vector<int> alive_list;
@@ -645,7 +664,7 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
             alive_tile[t] = n_alive > 0;
             w.n_steps = total;
             if (total == 0 || !alive_tile[t]) return;
-            w.sig.assign(64 * 8, 0.0); w.lat.assign(64 * 8 * 8, 0.0);
+            w.sig.assign(64 * 8, 0.0); w.alpha.assign(64 * 8, 0.0); w.lat.assign(64 * 8 * 8, 0.0);
             const float t1s = t_from_step(*st, (float)(block_step[t] * 8) + st->near_i);
             int visible = 0;
             for (int k = 0; k < 64; ++k) {
@@ -663,6 +682,7 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
                     if (alpha > (double)sc->alpha_thre) { T *= 1.0 - alpha; ++visible; }
                     if (T < 1e-4) rs[k].alive = false;
                     w.sig[k * 8 + s] = sigma;
+                    w.alpha[k * 8 + s] = alpha;
                     for (int j = 0; j < 8; ++j) w.lat[(k * 8 + s) * 8 + j] = bo[net->latent_offset + j];
                 }
                 rs[k].T = T;
@@ -690,9 +710,14 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
                         for (int s = 0; s < 8; ++s) {
                             const size_t v = (size_t)slot * 512 + (size_t)s * 64 + k;
                             if (w.mask[k] >> s & 1) {
-                                cc->vox_density[v] = (float)w.sig[k * 8 + s];
+                                /* accumulateNew_cache_init_second_kernel :459-507 */
+                                const double sig = w.sig[k * 8 + s];
+                                const bool by_alpha = cc->variant == 1 || cc->variant == 4;
+                                const double val = by_alpha ? w.alpha[k * 8 + s] : sig;
+                                cc->vox_density[v] = (float)val;
                                 cc->vox_isset[v] = 1.0f;
                                 for (int j = 0; j < 8; ++j) cc->vox_latents[v * 8 + j] = d2h_bits(w.lat[(k * 8 + s) * 8 + j]);
+                                if (cc->variant == 3 || cc->variant == 4) cc->vox_latents[v * 8] = d2h_bits(val);
                             }
                         }
                 } else {
@@ -819,7 +844,9 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         float tfr2;
                         const V3 f2 = cam2froxel(at(rc, tmh), *ccam, *cst, tfr2);
                         const float fx0 = floorf(f2.x - 0.5f), fy0 = floorf(f2.y - 0.5f), fz0 = floorf(f2.z - 0.5f);
-                        const double lt[3] = {(double)(f2.x - 0.5f - fx0), (double)(f2.y - 0.5f - fy0), (double)(f2.z - 0.5f - fz0)};
+                        const double lt[3] = {(double)interp_fn(f2.x - 0.5f - fx0, cc->interp),
+                                              (double)interp_fn(f2.y - 0.5f - fy0, cc->interp),
+                                              (double)interp_fn(f2.z - 0.5f - fz0, cc->interp)};
                         double wsum = 0, dsum = 0, lsum[8] = {0};
                         for (int c = 0; c < 8; ++c) {
                             const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
@@ -840,8 +867,16 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         }
                         double lat[8];
                         for (int j = 0; j < 8; ++j) lat[j] = lsum[j] / wsum;
-                        head_forward(d, lat, d01, lg);
-                        sigma = std::max(dsum, 1e-6);
+                        if (cc->variant == 3) {
+                            /* DensityIntermediates (:776-781): latent 0 is the density,
+                             * log(sum w density) enters the head and gives sigma */
+                            lat[0] = net->mimic_fp16 ? round_h(std::log(lsum[0])) : std::log(lsum[0]);
+                            head_forward(d, lat, d01, lg);
+                            sigma = std::exp(lat[0]);
+                        } else {
+                            head_forward(d, lat, d01, lg);
+                            sigma = std::max(dsum, 1e-6);
+                        }
                         ++n_cache;
                     }
                     if (composite(sigma, lg, dt, sc->alpha_thre, rgb, T)) break;
@@ -1179,7 +1214,9 @@ double ray_loss_grad_cached(const NetD &d, const OrcScene *sc, const OrcSteps *s
                 float tfr2;
                 const V3 f2 = cam2froxel(at(rc, tmh), *ccam, *cst, tfr2);
                 const float fx0 = floorf(f2.x - 0.5f), fy0 = floorf(f2.y - 0.5f), fz0 = floorf(f2.z - 0.5f);
-                const double lt[3] = {(double)(f2.x - 0.5f - fx0), (double)(f2.y - 0.5f - fy0), (double)(f2.z - 0.5f - fz0)};
+                const double lt[3] = {(double)interp_fn(f2.x - 0.5f - fx0, cc->interp),
+                                      (double)interp_fn(f2.y - 0.5f - fy0, cc->interp),
+                                      (double)interp_fn(f2.z - 0.5f - fz0, cc->interp)};
                 double dsum = 0, lsum[8] = {0};
                 smp.wsum = 0;
                 smp.nc = 0;

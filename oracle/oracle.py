@@ -52,7 +52,7 @@ class OrcCache(C.Structure):
     _fields_ = [("dims", OrcCacheDims), ("packed_index", C.c_void_p), ("known_ranges", C.c_void_p),
                 ("vox_density", C.c_void_p), ("vox_isset", C.c_void_p), ("vox_latents", C.c_void_p),
                 ("n_bricks_set", C.c_int), ("n_demanded", C.c_int), ("n_iterations", C.c_int),
-                ("n_samples", C.c_longlong), ("slot_of_brick_order", C.c_void_p)]
+                ("n_samples", C.c_longlong), ("slot_of_brick_order", C.c_void_p), ("variant", C.c_int), ("interp", C.c_int)]
 
 
 def build(force: bool = False) -> str:
@@ -260,9 +260,14 @@ class OracleModel:
         lib().orc_cache_dims(C.byref(self.scene), C.byref(steps or self.steps), W, H, C.byref(d))
         return d
 
-    def cache_build(self, cam: dict, threads: int | None = None) -> "OracleCache":
+    def cache_build(self, cam: dict, threads: int | None = None, variant: int = 0, interp: int = 0) -> "OracleCache":
+        """Blockwise build; `variant` / `interp` are CacheSettings'
+        interpol_variant and interpol_function (the latter used by lookups
+        through the returned cache; change `cache.s.interp` to render with
+        another)."""
         c = make_cam(cam)
         cc = OracleCache(self.cache_dims(c.W, c.H), cam)
+        cc.s.variant, cc.s.interp = variant, interp
         lib().orc_cache_build(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
                               C.byref(cc.s), threads or default_threads())
         return cc

@@ -155,3 +155,12 @@ def test_snapshot_renders_like_its_export_and_the_oracle(tmp_path):
     p = psnr(outs[0][0][..., :3] + outs[0][0][..., 3:], ref[..., :3] + ref[..., 3:])
     print(f"\n.ingp plain 64x48: max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB, samples {ns.sum()}")
     assert err <= 2e-3
+    # the snapshot's head reads 16 latents, a cache voxel holds 8: the cache renderer refuses it
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    rc = fvc.CachePerformanceRenderer(a.scene_info, a.occupancy_grid_morton_bitfield, a.nerf_network, c0, c1)
+    rc.resizeCache(cam_c["resolution"], a.stepsize_info)
+    rc.resizeRenderbuffers(cam_c["resolution"])
+    rc.setCacheSettings(fvc.eval_cache_settings(a))
+    with pytest.raises(fvc._lib.FvcError) as e:
+        rc.initCacheBlockwise(fvc.raymarch_info(cam_c, a.stepsize_info))
+    assert e.value.code == 2 and "8 latents" in str(e.value)
