@@ -359,6 +359,7 @@ struct fvc_renderer {
     int *d_row_slot = nullptr;
     uint8_t *d_row_kind = nullptr;
     float4 *d_row_pay = nullptr;
+    uint4 *d_row_lat = nullptr;
     uint2 *d_row_out = nullptr;
     int *d_res_list = nullptr, *d_cache_list = nullptr;
     int *d_wf_counters = nullptr;
@@ -385,6 +386,7 @@ struct fvc_renderer {
     {
         dfree(d_states[0]); dfree(d_states[1]); dfree(d_ray_rows); dfree(d_row_t0); dfree(d_row_slot);
         dfree(d_row_kind); dfree(d_row_pay); dfree(d_row_out); dfree(d_res_list); dfree(d_cache_list); dfree(d_wf_counters);
+        dfree(d_row_lat);
         row_capacity = 0;
     }
     fvc_cache *cache = nullptr, *next = nullptr;
@@ -959,6 +961,7 @@ extern "C" int fvc_renderer_resize(fvc_renderer *r, int width, int height)
         if ((rc = dalloc(&r->d_row_kind, cap, "row kinds"))) return rc;
         if ((rc = dalloc(&r->d_res_list, cap, "resample list"))) return rc;
         if ((rc = dalloc(&r->d_cache_list, cap, "cache list"))) return rc;
+        if ((rc = dalloc(&r->d_row_lat, cap, "cache-row head inputs"))) return rc;
     }
     if ((rc = dalloc(&r->d_wf_counters, (size_t)8, "wavefront counters"))) return rc;
     r->row_capacity = (int)cap;
@@ -1061,7 +1064,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.states[0] = r->d_states[0]; p.states[1] = r->d_states[1];
     p.ray_rows = r->d_ray_rows;
     p.row_t0 = r->d_row_t0; p.row_slot = r->d_row_slot; p.row_kind = r->d_row_kind;
-    p.row_pay = r->d_row_pay; p.row_out = r->d_row_out;
+    p.row_pay = r->d_row_pay; p.row_out = r->d_row_out; p.row_lat = r->d_row_lat;
     p.res_list = r->d_res_list; p.cache_list = r->d_cache_list;
     p.counters = r->d_wf_counters;
     p.row_capacity = r->row_capacity;

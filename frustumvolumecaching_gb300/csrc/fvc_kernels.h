@@ -160,6 +160,7 @@ struct RenderParams {
     uint8_t *row_kind;          /* per row: resample / cache / known empty / skipped */
     float4 *row_pay;            /* per row: contracted position or froxel point */
     uint2 *row_out;             /* per row: fp16 logits r, g, b and log-density */
+    uint4 *row_lat;             /* per place in the cache list: the 8 looked-up head inputs from K = latent_offset (fp16) */
     int *res_list, *cache_list; /* row ids of the two network streams */
     int *counters;              /* [0], [1] alive rays (ping-pong), [2] rows, [3] resample, [4] cache */
     int row_capacity;           /* rows per sub-iteration */

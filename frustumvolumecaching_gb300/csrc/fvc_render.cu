@@ -343,11 +343,61 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
     }
 }
 
+/* the cache a row's ray renders against: its view's cache in a batch, else the renderer's */
+__device__ __forceinline__ const CacheView &row_cache(const RenderParams &p, const RayState *states, int r)
+{
+    return p.view_caches ? p.view_caches[states[p.row_slot[r]].cnt2.w].cache : p.cache;
+}
+
+/* Trilinear, isset-weighted lookup of the cache for one froxel point,
+ * generateNetworkInput_cache_shfl_perf_kernel_cg
+ * (src/cache_performance_renderer.cu:678-787): head input = log of the
+ * interpolated density (not renormalised) and latents / interpolated isset. */
+__device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, float &logd, float (&lat)[8])
+{
+    const Voxel *vp[8];
+    float wc[8];
+    cache_corners(C, f, vp, wc);
+    float wsum = 0.f, dsum = 0.f, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (!vp[c]) continue;
+        const float w = wc[c];
+        const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
+        const uint4 lt = __ldg(&vp[c]->lat);
+        wsum = fmaf(w, di.y, wsum);
+        dsum = fmaf(w, di.x, dsum);
+        const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 fq = __half22float2(*reinterpret_cast<const __half2 *>(&lw[q]));
+            ls[2 * q] = fmaf(w, fq.x, ls[2 * q]);
+            ls[2 * q + 1] = fmaf(w, fq.y, ls[2 * q + 1]);
+        }
+    }
+    const float inv = 1.0f / wsum;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) lat[j] = ls[j] * inv;
+    if (C.first_latent_is_density) {
+        /* DensityIntermediates (:776-781): latent 0 holds the density; the
+         * head input is log(sum w density) * wsum / wsum, the other latents
+         * are renormalised by the interpolated isset */
+        lat[0] = __fdiv_rn(logf(ls[0]) * wsum, wsum);
+        logd = lat[0];
+    } else {
+        logd = logf(fmaxf(dsum, 1e-6f));
+    }
+}
+
 /* One thread per row of the cached render: classification
  * (sample_cache_performance_kernel :91-163) and the network input of the
  * row (generateNetworkInput_resample_perf_kernel :231-238 /
- * _preparation_perf_kernel :284-297 evaluate it at t0 + dt/2); appends the
- * row id to the resample or cache list. */
+ * _preparation_perf_kernel :284-297 evaluate it at t0 + dt/2): the
+ * contracted position of a resample row, the trilinear cache lookup of a
+ * cache row (its 8 head inputs from K = latent_offset go to row_lat at the
+ * row's place in the cache list, its log-density to the high half of
+ * row_out.y; the froxel point stays in row_pay for the adjoint); appends
+ * the row id to the resample or cache list. */
 __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it)
 {
     const int n_rows = p.counters[2];
@@ -355,6 +405,7 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
     for (int base = blockIdx.x * blockDim.x; base < n_rows; base += gridDim.x * blockDim.x) {
         const int r = base + threadIdx.x;
         int kind = KIND_SKIP;
+        float logd = 0.f, lat[8];
         if (r < n_rows) {
             const int slot = p.row_slot[r];
             const float t0 = p.row_t0[r];
@@ -377,6 +428,7 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                 float tf2;
                 const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
                 p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
+                cache_lookup(C, fr, logd, lat);
             }
             p.row_kind[r] = (uint8_t)kind;
         }
@@ -389,7 +441,12 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
         b0 = __shfl_sync(FULLMASK, b0, 0);
         b1 = __shfl_sync(FULLMASK, b1, 0);
         if (kind == KIND_RESAMPLE) p.res_list[b0 + __popc(m0 & lane_lt())] = r;
-        if (kind == KIND_CACHE) p.cache_list[b1 + __popc(m1 & lane_lt())] = r;
+        if (kind == KIND_CACHE) {
+            const int kc = b1 + __popc(m1 & lane_lt());
+            p.cache_list[kc] = r;
+            p.row_lat[kc] = make_uint4(pack_h2(lat[0], lat[1]), pack_h2(lat[2], lat[3]), pack_h2(lat[4], lat[5]), pack_h2(lat[6], lat[7]));
+            p.row_out[r] = make_uint2(0u, (uint32_t)__half_as_ushort(__float2half_rn(logd)) << 16);
+        }
     }
 }
 
@@ -463,54 +520,26 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(Rend
     }
 }
 
-/* Trilinear, isset-weighted lookup of the cache for one froxel point,
- * generateNetworkInput_cache_shfl_perf_kernel_cg
- * (src/cache_performance_renderer.cu:678-787): head input = log of the
- * interpolated density (not renormalised) and latents / interpolated isset. */
-/* the cache a row's ray renders against: its view's cache in a batch, else the renderer's */
-__device__ __forceinline__ const CacheView &row_cache(const RenderParams &p, const RayState *states, int r)
+/* the head input of cache row r (place k in the cache list) as
+ * classification looked it up: halves 16..31
+ * of trow (log-density at 16 when latent_offset is 1, the latents from
+ * 16 + latent_offset, zeros after) */
+__device__ __forceinline__ void cache_row_input(const RenderParams &p, int k, int r, __half *trow)
 {
-    return p.view_caches ? p.view_caches[states[p.row_slot[r]].cnt2.w].cache : p.cache;
-}
-
-__device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, int latent_offset, __half *trow)
-{
-    const Voxel *vp[8];
-    float wc[8];
-    cache_corners(C, f, vp, wc);
-    float wsum = 0.f, dsum = 0.f, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        if (!vp[c]) continue;
-        const float w = wc[c];
-        const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
-        const uint4 lt = __ldg(&vp[c]->lat);
-        wsum = fmaf(w, di.y, wsum);
-        dsum = fmaf(w, di.x, dsum);
-        const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float2 fq = __half22float2(*reinterpret_cast<const __half2 *>(&lw[q]));
-            ls[2 * q] = fmaf(w, fq.x, ls[2 * q]);
-            ls[2 * q + 1] = fmaf(w, fq.y, ls[2 * q + 1]);
-        }
+    const uint4 lt = p.row_lat[k];
+    const uint32_t ld = p.row_out[r].y >> 16;
+    uint32_t *h = reinterpret_cast<uint32_t *>(trow + 16);
+    if (p.latent_offset == 0) {
+        h[0] = lt.x; h[1] = lt.y; h[2] = lt.z; h[3] = lt.w;
+        h[4] = h[5] = h[6] = h[7] = 0u;
+    } else {
+        h[0] = ld | (lt.x << 16);
+        h[1] = (lt.x >> 16) | (lt.y << 16);
+        h[2] = (lt.y >> 16) | (lt.z << 16);
+        h[3] = (lt.z >> 16) | (lt.w << 16);
+        h[4] = lt.w >> 16;
+        h[5] = h[6] = h[7] = 0u;
     }
-    uint32_t *hin = reinterpret_cast<uint32_t *>(trow + 16);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) hin[c] = 0u;
-    const float inv = 1.0f / wsum;
-    if (C.first_latent_is_density) {
-        /* DensityIntermediates (:776-781): latent 0 holds the density; the
-         * head input is log(sum w density) * wsum / wsum, the other latents
-         * are renormalised by the interpolated isset */
-        trow[16] = __float2half_rn(__fdiv_rn(logf(ls[0]) * wsum, wsum));
-#pragma unroll
-        for (int j = 1; j < 8; ++j) trow[16 + latent_offset + j] = __float2half_rn(ls[j] * inv);
-        return;
-    }
-    trow[16] = __float2half_rn(logf(fmaxf(dsum, 1e-6f)));
-#pragma unroll
-    for (int j = 0; j < 8; ++j) trow[16 + latent_offset + j] = __float2half_rn(ls[j] * inv);
 }
 
 template <int HEAD_HIDDEN>
@@ -532,8 +561,7 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
         const int k = b * 32 + lane;
         const int r = k < n_rows ? p.cache_list[k] : -1;
         if (r >= 0) {
-            const float4 pw = p.row_pay[r];
-            cache_lookup(row_cache(p, states, r), make_float3(pw.x, pw.y, pw.z), p.latent_offset, trow);
+            cache_row_input(p, k, r, trow);
             sh16(dir01_of(states, p.row_slot[r]), reinterpret_cast<__half2 *>(trow + 32));
         } else {
 #pragma unroll
@@ -696,8 +724,7 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
             /* ---- cache lookup -> head input (log-density, latents) ---- */
             __half hin[32];
             if (r >= 0) {
-                const float4 pw = p.row_pay[r];
-                cache_lookup(row_cache(p, states, r), make_float3(pw.x, pw.y, pw.z), p.latent_offset, hin);
+                cache_row_input(p, k, r, hin);
             } else {
                 for (int q = 16; q < 32; ++q) hin[q] = __float2half_rn(0.f);
             }
@@ -1331,7 +1358,7 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
                 const size_t tc_smem = sizeof(TcSmem);
                 const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
                 wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
-                if (p.use_tc) {
+                    if (p.use_tc) {
                     wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
                     wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
                 } else {
