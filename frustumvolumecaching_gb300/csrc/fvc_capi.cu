@@ -322,7 +322,6 @@ struct BuildScratch {
     int *tile_n_samples = nullptr;
     uint8_t *tile_processed = nullptr, *tile_need = nullptr;
     int *tile_n_alive = nullptr;
-    void *staging = nullptr;
     int *jobs = nullptr;
     float4 *rows = nullptr;   /* per-iteration sample rows (tiles x 512) */
     __half *den = nullptr;
@@ -333,8 +332,6 @@ struct BuildScratch {
         dfree(rays); dfree(block_step); dfree(tile_alive); dfree(alive_a); dfree(alive_b); dfree(counters);
         dfree(tile_n_samples); dfree(tile_processed); dfree(tile_need); dfree(tile_n_alive); dfree(jobs);
         dfree(rows); dfree(den); dfree(lat); dfree(row_of);
-        if (staging) cudaFree(staging);
-        staging = nullptr;
         n_tiles = 0;
     }
 };
@@ -1307,13 +1304,11 @@ static int ensure_build_scratch(fvc_renderer *r, int n_tiles)
     if ((rc = dalloc(&b.tile_processed, (size_t)n_tiles, "tile flags"))) return rc;
     if ((rc = dalloc(&b.tile_need, (size_t)n_tiles, "tile flags"))) return rc;
     if ((rc = dalloc(&b.tile_n_alive, (size_t)n_tiles, "tile alive counts"))) return rc;
-    if ((rc = dalloc(&b.jobs, (size_t)2 * n_tiles, "copy jobs"))) return rc;
+    if ((rc = dalloc(&b.jobs, (size_t)2 * n_tiles, "fill jobs"))) return rc;
     if ((rc = dalloc(&b.rows, (size_t)n_tiles * 512, "build rows"))) return rc;
     if ((rc = dalloc(&b.den, (size_t)n_tiles * 512, "build densities"))) return rc;
     if ((rc = dalloc(&b.lat, (size_t)n_tiles * 512, "build latents"))) return rc;
     if ((rc = dalloc(&b.row_of, (size_t)n_tiles * 512, "build row map"))) return rc;
-    cudaError_t e = cudaMalloc(&b.staging, (size_t)n_tiles * 512 * 32);
-    if (e != cudaSuccess) { cudaGetLastError(); b.staging = nullptr; return fail(FVC_ERR_OOM, "cudaMalloc build staging"); }
     b.n_tiles = n_tiles;
     return FVC_OK;
 }
@@ -1350,7 +1345,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     p.n_alive_tiles = b.counters + 0; p.n_alive_next = b.counters + 1;
     p.slot_counter = b.counters + 2; p.n_jobs = b.counters + 3; p.guard = b.counters + 4;
     p.tile_n_samples = b.tile_n_samples; p.tile_processed = b.tile_processed; p.tile_need = b.tile_need;
-    p.tile_n_alive = b.tile_n_alive; p.staging = b.staging; p.voxels = c->d_voxels;
+    p.tile_n_alive = b.tile_n_alive; p.voxels = c->d_voxels;
     p.packed_index = c->d_packed; p.known_ranges = c->d_known; p.jobs = b.jobs;
     p.max_search = c->bZ + 4;
     p.build_rows = b.rows; p.build_den = b.den; p.build_lat = b.lat; p.build_row_of = b.row_of;
@@ -1376,11 +1371,11 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
         CU(cudaGetLastError());
         cache_density_kernel<<<m->n_sms * 8, 128, 0, s>>>(p);
         CU(cudaGetLastError());
-        cache_composite_kernel<<<std::min(n_alive, 1 << 16), 64, 0, s>>>(p);
+        cache_composite_kernel<<<std::min((n_alive + 3) / 4, 1 << 16), 128, 0, s>>>(p);
         CU(cudaGetLastError());
         cache_assign_kernel<<<1, 1024, 0, s>>>(p);
         CU(cudaGetLastError());
-        cache_copy_kernel<<<std::min(n_alive, 4 * m->n_sms), 256, 0, s>>>(p);
+        cache_fill_kernel<<<std::min(n_alive, 8 * m->n_sms), 256, 0, s>>>(p);
         CU(cudaGetLastError());
         n_launches += 5;
         std::swap(p.alive_list, p.alive_list_next);

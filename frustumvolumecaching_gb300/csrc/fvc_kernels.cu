@@ -131,9 +131,10 @@ __global__ void __launch_bounds__(64) cache_init_kernel(CacheBuildParams p)
  *   cache_density_kernel   the density network on all rows of the iteration
  *                          (inferenceLatents), warp-level tensor-core MLP;
  *   cache_composite_kernel per processed tile: density-only compositing and
- *                          the brick's 512 voxels into the staging area
+ *                          the brick's need of a slot
  *                          (accumulateNew_cache_init_second_kernel :289-528);
- * then cache_assign_kernel / cache_copy_kernel give bricks their slots. */
+ * then cache_assign_kernel gives bricks their slots and cache_fill_kernel
+ * writes their voxels. */
 __device__ __forceinline__ int tile_block_sum(int v, int *red)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -252,25 +253,27 @@ __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
     }
 }
 
-__global__ void __launch_bounds__(64) cache_composite_kernel(CacheBuildParams p)
+/* One warp per processed tile, rays lane and lane + 32 per lane:
+ * density-only compositing over the brick's 8 steps
+ * (accumulateNew_cache_init_second_kernel :349-393) and whether the brick
+ * needs a slot (a visible sample). */
+__global__ void __launch_bounds__(128) cache_composite_kernel(CacheBuildParams p)
 {
-    __shared__ int red[4];
-    const int k = threadIdx.x;
+    const int lane = threadIdx.x & 31;
     const int n_alive_tiles = *p.n_alive_tiles;
-    for (int ai = blockIdx.x; ai < n_alive_tiles; ai += gridDim.x) {
-        if (!p.tile_processed[ai]) continue; /* uniform over the block */
+    const int n_warps = gridDim.x * (blockDim.x >> 5);
+    for (int ai = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ai < n_alive_tiles; ai += n_warps) {
+        if (!p.tile_processed[ai]) continue; /* uniform over the warp */
         const int tile = p.alive_list[ai];
-        CacheRay cr = p.rays[(size_t)tile * 64 + k];
         const int bstep = p.block_step[tile];
         const int *rof = p.build_row_of + (size_t)ai * 512;
-        int rows[8];
+        const float t1s = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
+        int visible = 0, alive = 0;
 #pragma unroll
-        for (int s = 0; s < 8; ++s) rows[s] = rof[s * 64 + k];
-        /* density-only compositing (accumulateNew_cache_init_second_kernel :349-393) */
-        int visible = 0;
-        float alphas[8];
-        {
-            float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
+        for (int h = 0; h < 2; ++h) {
+            const int k = h * 32 + lane;
+            CacheRay cr = p.rays[(size_t)tile * 64 + k];
+            float t1 = t1s;
             float T = cr.T;
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
@@ -278,48 +281,24 @@ __global__ void __launch_bounds__(64) cache_composite_kernel(CacheBuildParams p)
                 const float dt = calc_step(p.steps, t0);
                 t1 = F_ADD(t0, dt);
                 const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
-                alphas[s] = 0.f;
                 if (tm > cr.far_) { cr.alive = 0; continue; }
-                if (rows[s] < 0) continue;
-                const float sigma = expf(__half2float(p.build_den[rows[s]]));
+                const int row = rof[s * 64 + k];
+                if (row < 0) continue;
+                const float sigma = expf(__half2float(p.build_den[row]));
                 const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
-                alphas[s] = alpha;
                 if (alpha > p.scene.alpha_thre) { T *= 1.0f - alpha; ++visible; }
                 if (T < 1e-4f) cr.alive = 0;
             }
             cr.T = T;
+            alive += cr.alive;
+            p.rays[(size_t)tile * 64 + k] = cr;
         }
-        const int n_visible = tile_block_sum(visible, red);
-        const int n_alive_post = tile_block_sum(cr.alive, red);
-        if (k == 0) {
+        const int n_visible = (int)__reduce_add_sync(FULL, (unsigned)visible);
+        const int n_alive_post = (int)__reduce_add_sync(FULL, (unsigned)alive);
+        if (lane == 0) {
             p.tile_need[ai] = n_visible > 0;
             p.tile_n_alive[ai] = n_alive_post;
         }
-        p.rays[(size_t)tile * 64 + k] = cr;
-        /* staging: all 512 voxels of the brick (zeros where no sample) */
-        if (n_visible > 0) {
-            Voxel *st = reinterpret_cast<Voxel *>(p.staging) + (size_t)ai * 512;
-#pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                Voxel v;
-                if (rows[s] >= 0) {
-                    /* the voxel's density slot and latent 0 per interpol_variant
-                     * (accumulateNew_cache_init_second_kernel :459-507) */
-                    const float sigma = expf(__half2float(p.build_den[rows[s]]));
-                    const bool by_alpha = p.variant == VARIANT_ALPHA || p.variant == VARIANT_ALPHA_INTERMEDIATES;
-                    v.density = by_alpha ? alphas[s] : sigma;
-                    v.isset = 1.0f;
-                    v.lat = p.build_lat[rows[s]];
-                    if (p.variant == VARIANT_DENSITY_INTERMEDIATES || p.variant == VARIANT_ALPHA_INTERMEDIATES)
-                        v.lat.x = (v.lat.x & 0xffff0000u) | (uint32_t)__half_as_ushort(__float2half_rn(v.density));
-                } else {
-                    v.density = 0.f; v.isset = 0.f; v.lat = make_uint4(0, 0, 0, 0);
-                }
-                v.pad0 = v.pad1 = 0.f;
-                st[s * 64 + k] = v;
-            }
-        }
-        __syncthreads();
     }
 }
 
@@ -359,7 +338,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int &total, int *s_w)
  * the tiles needing a brick get consecutive slots in alive-list (= tile
  * index) order.  Applies the per-tile updates of :518-527 (block step
  * advances unless the allocation overflowed; the tile stays alive while it
- * has alive rays and did not overflow), emits the staging->slot copy jobs and
+ * has alive rays and did not overflow), emits the (tile, slot) fill jobs and
  * the next alive list.  One CTA of 1024 threads. */
 __global__ void __launch_bounds__(1024) cache_assign_kernel(CacheBuildParams p)
 {
@@ -421,15 +400,51 @@ __global__ void __launch_bounds__(1024) cache_assign_kernel(CacheBuildParams p)
     }
 }
 
-/* staging -> data array for the bricks that got a slot */
-__global__ void __launch_bounds__(256) cache_copy_kernel(CacheBuildParams p)
+/* The 512 voxels of each brick that got a slot, written straight from the
+ * iteration's network rows (zeros where the brick has no sample): density
+ * slot and latent 0 per interpol_variant
+ * (accumulateNew_cache_init_second_kernel :459-507).  Runs after
+ * cache_assign_kernel, which advanced the tile's block step past the brick. */
+__global__ void __launch_bounds__(256) cache_fill_kernel(CacheBuildParams p)
 {
+    __shared__ float s_dt[8];
     const int n_jobs = *p.n_jobs;
+    const bool by_alpha = p.variant == VARIANT_ALPHA || p.variant == VARIANT_ALPHA_INTERMEDIATES;
+    const bool lat0 = p.variant == VARIANT_DENSITY_INTERMEDIATES || p.variant == VARIANT_ALPHA_INTERMEDIATES;
     for (int j = blockIdx.x; j < n_jobs; j += gridDim.x) {
         const int ai = p.jobs[2 * j], slot = p.jobs[2 * j + 1];
-        const uint4 *src = reinterpret_cast<const uint4 *>(p.staging) + (size_t)ai * 1024;
-        uint4 *dst = reinterpret_cast<uint4 *>(p.voxels) + (size_t)slot * 1024;
-        for (int i = threadIdx.x; i < 1024; i += blockDim.x) dst[i] = __ldcs(src + i);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int bstep = p.block_step[p.alive_list[ai]] - 1;
+            float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
+            for (int s = 0; s < 8; ++s) {
+                const float dt = calc_step(p.steps, t1);
+                s_dt[s] = dt;
+                t1 = F_ADD(t1, dt);
+            }
+        }
+        __syncthreads();
+        const int *rof = p.build_row_of + (size_t)ai * 512;
+        Voxel *dst = reinterpret_cast<Voxel *>(p.voxels) + (size_t)slot * 512;
+        for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+            const int row = rof[i];
+            Voxel v;
+            v.pad0 = v.pad1 = 0.f;
+            if (row >= 0) {
+                const float sigma = expf(__half2float(p.build_den[row]));
+                const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * s_dt[i >> 6])));
+                v.density = by_alpha ? alpha : sigma;
+                v.isset = 1.0f;
+                v.lat = p.build_lat[row];
+                if (lat0) v.lat.x = (v.lat.x & 0xffff0000u) | (uint32_t)__half_as_ushort(__float2half_rn(v.density));
+            } else {
+                v.density = 0.f;
+                v.isset = 0.f;
+                v.lat = make_uint4(0, 0, 0, 0);
+            }
+            __stcs(reinterpret_cast<float4 *>(dst + i), make_float4(v.density, v.isset, 0.f, 0.f));
+            __stcs(reinterpret_cast<uint4 *>(dst + i) + 1, v.lat);
+        }
     }
 }
 

@@ -254,7 +254,6 @@ struct CacheBuildParams {
     int *tile_n_samples;        /* [alive idx] */
     uint8_t *tile_processed, *tile_need;
     int *tile_n_alive;
-    void *staging;              /* [alive idx][512] voxels */
     void *voxels;               /* [slots][512] voxels */
     int32_t *packed_index;
     float *known_ranges;
@@ -311,7 +310,7 @@ __global__ void cache_search_kernel(CacheBuildParams p);
 __global__ void cache_density_kernel(CacheBuildParams p);
 __global__ void cache_composite_kernel(CacheBuildParams p);
 __global__ void cache_assign_kernel(CacheBuildParams p);
-__global__ void cache_copy_kernel(CacheBuildParams p);
+__global__ void cache_fill_kernel(CacheBuildParams p);
 __global__ void cache_known_ranges_kernel(CacheBuildParams p);
 __global__ void cache_compact_kernel(CacheBuildParams p, int n_tiles);
 
