@@ -6,5 +6,5 @@ the reference's renderer API, and the seeded synthetic-model generator.
 """
 from .renderer import (BasicRenderer, Cache, CachePerformanceRenderer, Gradients, LoaderData, NerfNetwork,  # noqa: F401
                        PerformanceRenderer, RenderBuffer, Renderer, camera_info, default_cache_settings, ingp_export,
-                       load_data, raymarch_info, eval_cache_settings, DENSITY, ALPHA, INTERMEDIATES,
+                       load_data, raymarch_info, eval_cache_settings, change_sampling_rate, DENSITY, ALPHA, INTERMEDIATES,
                        DENSITY_INTERMEDIATES, ALPHA_INTERMEDIATES, LINEAR, SMOOTHSTEP, SMOOTHERSTEP, NEAREST)

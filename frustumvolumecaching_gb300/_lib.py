@@ -117,6 +117,7 @@ SIGNATURES = {
     "fvc_ingp_export": (c_int, [C.c_char_p, C.c_char_p]),
     "fvc_model_destroy": (None, [P]),
     "fvc_model_info": (c_int, [P, C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
+    "fvc_stepsize_setup": (c_int, [C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
     "fvc_model_density": (c_int, [P, P, c_int, P]),
     "fvc_model_inference": (c_int, [P, P, P, c_int, P]),
     "fvc_model_debug_encode": (c_int, [P, P, c_int, P, P]),

@@ -844,6 +844,14 @@ extern "C" int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_ste
     return FVC_OK;
 }
 
+extern "C" int fvc_stepsize_setup(const fvc_scene_info *scene, fvc_stepsize_info *steps)
+{
+    CHECK_ARG(scene && steps, "fvc_stepsize_setup: null argument");
+    CHECK_ARG(steps->stepsize > 0.0f && steps->cone_angle >= 0.0f, "fvc_stepsize_setup: stepsize must be > 0, cone_angle >= 0");
+    setup_steps(*scene, *steps);
+    return FVC_OK;
+}
+
 static int run_inference(fvc_model *m, const float *pos, const float *dir, int n, float *out4, float *base_out, float *features)
 {
     CHECK_ARG(m && pos && n >= 0, "inference: bad arguments");

@@ -365,6 +365,17 @@ class CachePerformanceRenderer(Renderer):
         return s
 
 
+def change_sampling_rate(stepsize_info: L.StepsizeInfo, factor: float, scene_info: L.SceneInfo) -> L.StepsizeInfo:
+    """StepsizeInfo::changeSamplingRate (include/common.h:130-135) on a copy:
+    cone angle and step size divided by ``factor``, derived fields refilled
+    (setAdditionalInfo, include/common.h:109-131)."""
+    s = L.StepsizeInfo.from_buffer_copy(stepsize_info)
+    s.cone_angle /= factor
+    s.stepsize /= factor
+    L.check(L.load().fvc_stepsize_setup(C.byref(scene_info), C.byref(s)))
+    return s
+
+
 # DensityInterpolVariant and InterpolFunction (include/cache_renderer.h:14-22, include/common.h:221-227)
 DENSITY, ALPHA, INTERMEDIATES, DENSITY_INTERMEDIATES, ALPHA_INTERMEDIATES = range(5)
 LINEAR, SMOOTHSTEP, SMOOTHERSTEP, NEAREST = range(4)
@@ -390,5 +401,5 @@ def eval_cache_settings(loader) -> L.CacheSettings:
 
 __all__ = ["load_data", "LoaderData", "NerfNetwork", "Renderer", "BasicRenderer", "PerformanceRenderer", "Cache", "Gradients",
            "CachePerformanceRenderer", "RenderBuffer", "raymarch_info", "camera_info", "camera_dict",
-           "default_cache_settings", "eval_cache_settings", "DENSITY", "ALPHA", "INTERMEDIATES", "DENSITY_INTERMEDIATES",
+           "default_cache_settings", "eval_cache_settings", "change_sampling_rate", "DENSITY", "ALPHA", "INTERMEDIATES", "DENSITY_INTERMEDIATES",
            "ALPHA_INTERMEDIATES", "LINEAR", "SMOOTHSTEP", "SMOOTHERSTEP", "NEAREST"]

@@ -183,6 +183,12 @@ void fvc_model_destroy(fvc_model *m);
 /* Scene and step parameters of the loaded model (LoaderData::scene_info,
  * ::stepsize_info after StepsizeInfo::setAdditionalInfo, include/common.h:109-131). */
 int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_stepsize_info *steps);
+/* StepsizeInfo::setAdditionalInfo (include/common.h:109-131): fills the
+ * derived fields (dt_min/max, t_min/max, i_min/max, log1p_c, near_i) from
+ * cone_angle, stepsize, near and far for the scene's grid.  Used by
+ * StepsizeInfo::changeSamplingRate (include/common.h:130-135), e.g. a cache
+ * built at twice the render's sampling rate. */
+int fvc_stepsize_setup(const fvc_scene_info *scene, fvc_stepsize_info *steps);
 
 /* Network and occupancy-grid properties a caller of the reference reads from
  * NerfNetwork / LoaderData: m_first_latent_is_density (include/nerf_network.h:342),

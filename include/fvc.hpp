@@ -95,10 +95,21 @@ struct SceneInfo {
     float alpha_thre;
 };
 
-/* StepsizeInfo, include/common.h:93-164 (the derived fields are filled by the loader). */
+struct SceneInfo;
+
+/* StepsizeInfo, include/common.h:93-164 (the derived fields are filled by the
+ * loader, or by setAdditionalInfo). */
 struct StepsizeInfo {
     float cone_angle, log1p_c, stepsize, near, near_i, far;
     float dt_min, dt_max, t_min, t_max, i_min, i_max;
+
+    inline void setAdditionalInfo(const SceneInfo &scene_info);
+    void changeSamplingRate(const float factor, const SceneInfo &scene_info)
+    {
+        cone_angle /= factor;
+        stepsize /= factor;
+        setAdditionalInfo(scene_info);
+    }
 };
 
 /* CameraInfo, include/common.h:166-195. */
@@ -159,7 +170,13 @@ static_assert(sizeof(RaymarchInfo) == sizeof(fvc_raymarch_info) &&
 namespace fvc_cpp {
 inline const fvc_raymarch_info *abi(const RaymarchInfo &r) { return reinterpret_cast<const fvc_raymarch_info *>(&r); }
 inline const fvc_stepsize_info *abi(const StepsizeInfo &s) { return reinterpret_cast<const fvc_stepsize_info *>(&s); }
+inline const fvc_scene_info *abi(const SceneInfo &s) { return reinterpret_cast<const fvc_scene_info *>(&s); }
 }  // namespace fvc_cpp
+
+inline void StepsizeInfo::setAdditionalInfo(const SceneInfo &scene_info)
+{
+    fvc_cpp::check(fvc_stepsize_setup(fvc_cpp::abi(scene_info), reinterpret_cast<fvc_stepsize_info *>(this)));
+}
 
 /* ------------------------------------------------------------------------ */
 /* device memory                                                             */

@@ -260,15 +260,18 @@ class OracleModel:
         lib().orc_cache_dims(C.byref(self.scene), C.byref(steps or self.steps), W, H, C.byref(d))
         return d
 
-    def cache_build(self, cam: dict, threads: int | None = None, variant: int = 0, interp: int = 0) -> "OracleCache":
+    def cache_build(self, cam: dict, threads: int | None = None, variant: int = 0, interp: int = 0,
+                    steps: OrcSteps | None = None) -> "OracleCache":
         """Blockwise build; `variant` / `interp` are CacheSettings'
         interpol_variant and interpol_function (the latter used by lookups
         through the returned cache; change `cache.s.interp` to render with
-        another)."""
+        another); `steps` the cache's StepsizeInfo (default: the model's)."""
         c = make_cam(cam)
-        cc = OracleCache(self.cache_dims(c.W, c.H), cam)
+        st = steps or self.steps
+        cc = OracleCache(self.cache_dims(c.W, c.H, st), cam)
+        cc.steps = st
         cc.s.variant, cc.s.interp = variant, interp
-        lib().orc_cache_build(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
+        lib().orc_cache_build(C.byref(self.net), C.byref(self.scene), C.byref(st), C.byref(c), ptr(self.bits),
                               C.byref(cc.s), threads or default_threads())
         return cc
 
@@ -304,8 +307,8 @@ class OracleModel:
         res = np.zeros((H, W, 4), np.float32)
         counts = np.zeros((H, W, 4), np.int32)
         lib().orc_render_cached(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
-                                C.byref(cache.s), C.byref(cc), C.byref(self.steps), mode, r0, r1, ptr(res), ptr(counts),
-                                threads or default_threads())
+                                C.byref(cache.s), C.byref(cc), C.byref(cache.steps or self.steps), mode, r0, r1, ptr(res),
+                                ptr(counts), threads or default_threads())
         return res, counts
 
 
@@ -313,6 +316,7 @@ class OracleCache:
     def __init__(self, dims: OrcCacheDims, cam: dict):
         self.cam = cam
         self.dims = dims
+        self.steps = None  # the StepsizeInfo the cache was built with (None: the model's)
         nb = dims.bX * dims.bY * dims.bZ
         slots = dims.dX * dims.dY * dims.dZ
         self.packed_index = np.full(nb, -1, np.int32)

@@ -86,3 +86,33 @@ def test_null_arguments_are_rejected():
     assert lib.fvc_model_load(None, None) == 6
     assert lib.fvc_renderer_resize(None, 4, 4) == 6
     assert lib.fvc_render(None, None, None) == 6
+
+
+@pytest.mark.parametrize("aabb,cone,step,near", [((-1.5, 1.5), 0.0, 3 / 1024, 0.0), ((-6.0, 6.0), 1 / 256, 3 ** 0.5 / 1024, 0.0),
+                                                  ((-6.0, 6.0), 1 / 512, 3 ** 0.5 / 2048, 0.2), ((-2.0, 3.0), 1 / 256, 0.004, 0.05)])
+def test_stepsize_setup_matches_the_oracle(aabb, cone, step, near):
+    """fvc_stepsize_setup (StepsizeInfo::setAdditionalInfo, host only) fills
+    the same derived fields as the oracle's restatement, bit for bit; and
+    change_sampling_rate(2) equals a setup at half the cone and step."""
+    import ctypes as C
+    from frustumvolumecaching_gb300.renderer import change_sampling_rate
+    from oracle import oracle as orc
+    sc = L.SceneInfo()
+    sc.grid_resolution, sc.grid_nlvl = 128, 1
+    for f in ("x", "y", "z"):
+        setattr(sc.aabb_from, f, aabb[0])
+        setattr(sc.aabb_to, f, aabb[1])
+    st = L.StepsizeInfo()
+    st.cone_angle, st.stepsize, st.near, st.far = cone, step, near, 1e10
+    L.check(L.load().fvc_stepsize_setup(C.byref(sc), C.byref(st)))
+    osc = orc.make_scene({"grid_nlvl": 1, "aabb": [aabb[0]] * 3 + [aabb[1]] * 3, "alpha_thre": 0.0})
+    ost = orc.make_steps(osc, cone, step, near, 1e10)
+    names = ["dt_min", "dt_max", "t_min", "t_max", "i_min", "i_max", "near_i"] + (["log1p_c"] if cone > 0 else [])
+    for n in names:
+        a, b = np.float32(getattr(st, n)), np.float32(getattr(ost, "near_i" if n == "near_i" else n))
+        assert a.view(np.uint32) == b.view(np.uint32), (n, a, b)
+    half = change_sampling_rate(st, 2.0, sc)
+    ref = orc.make_steps(osc, np.float32(cone) / np.float32(2), np.float32(step) / np.float32(2), near, 1e10)
+    for n in names:
+        a, b = np.float32(getattr(half, n)), np.float32(getattr(ref, n))
+        assert a.view(np.uint32) == b.view(np.uint32), (n, a, b)

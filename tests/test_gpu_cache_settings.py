@@ -133,3 +133,38 @@ def test_eval_settings_follow_the_model(models):
     with pytest.raises(fvc._lib.FvcError) as e:
         r.setCacheSettings(fvc.default_cache_settings(fvc.DENSITY, 7))
     assert e.value.code != 0
+
+
+@pytest.mark.parametrize("key", ["lo1", "lo1_c3"])
+def test_cache_built_at_double_sampling_rate(models, key):
+    """The viewer's m_cache_double_sampling_rate (realtime_viewer/src/
+    application.cu:73-74): the cache is sized and built with
+    StepsizeInfo::changeSamplingRate(2) and the frame renders at the model's
+    rate; reprojection and classification use the cache's own step grid."""
+    loader, om = models[key]
+    W, H = (48, 40) if key.endswith("c3") else (64, 48)
+    cam0 = small_camera(1001, W, H)
+    cst = fvc.change_sampling_rate(loader.stepsize_info, 2.0, loader.scene_info)
+    assert cst.stepsize == np.float32(loader.stepsize_info.stepsize) / np.float32(2)
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    r.resizeCache((W, H), cst)
+    r.resizeRenderbuffers((W, H))
+    r.setCacheSettings(fvc.default_cache_settings())
+    r.initCacheBlockwise(fvc.raymarch_info(cam0, cst))
+    r.swapCache()
+    ost = orc.make_steps(om.scene, cst.cone_angle, cst.stepsize, cst.near, cst.far)
+    oc = om.cache_build(cam0, steps=ost)
+    cam1 = _rotated(cam0, W, H)
+    buf = fvc.RenderBuffer((W, H))
+    r.render(fvc.raymarch_info(cam1, loader.stepsize_info), buf)
+    ref, counts = om.render_cached(cam1, oc)
+    live = ref[..., 3] >= 1e-4
+    np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])
+    np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])
+    np.testing.assert_array_equal(buf.ray_counts[..., 2][live], counts[..., 2][live])
+    err = np.abs(buf.results - ref).max()
+    hit = counts[..., 1].sum() / max(1, counts[..., :2].sum())
+    print(f"\n{key} cache at 2x sampling rate: hit {hit:.3f}, max-abs {err:.2e}")
+    assert hit > 0.2
+    assert err <= COLOR_ATOL
