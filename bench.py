@@ -105,6 +105,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(values: list[float], ws: int, device=None) -> list[float]:
+    """Each value's maximum over the ranks of a replica run (the slowest
+    rank's time), through one all_reduce; unchanged on one rank."""
+    if ws <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(ws: int, units_per_rank: float, seconds: float) -> float:
+    """Units per second of the whole job: every replica processed
+    units_per_rank in (at most) the slowest rank's time."""
+    return ws * units_per_rank / seconds
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -606,14 +624,10 @@ def run_fvc(args) -> dict | None:
     build_ms = mean_ms(log["_pending_build"])
     steps_ms_cached = sum(t_cached) / len(t_cached)
     steps_ms_plain = sum(t_plain) / len(t_plain)
-    if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([steps_ms_cached, steps_ms_plain, e2e_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        steps_ms_cached, steps_ms_plain, e2e_s = tt.tolist()
-    fps_cached = ws * n_frames / (steps_ms_cached / 1e3)
-    fps_plain = ws * n_frames / (steps_ms_plain / 1e3)
-    fps_e2e = ws * n_frames / e2e_s
+    steps_ms_cached, steps_ms_plain, e2e_s = max_over_ranks([steps_ms_cached, steps_ms_plain, e2e_s], ws, dev)
+    fps_cached = whole_job_rate(ws, n_frames, steps_ms_cached / 1e3)
+    fps_plain = whole_job_rate(ws, n_frames, steps_ms_plain / 1e3)
+    fps_e2e = whole_job_rate(ws, n_frames, e2e_s)
 
     # roofline of the dominant kernel (the resample network kernel, by the ncu launch list), over the
     # cached path's timed region: algorithmic bytes of its rows / its summed CUDA-event launch time
