@@ -628,18 +628,29 @@ __device__ __forceinline__ void tc_layer(uint32_t tmem, const uint8_t *a, const 
         tc_mma_f16(tmem, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
 }
 
-/* 64 accumulator columns of this thread's row -> (+bias) ReLU -> fp16 row of a K=64 tile */
+/* 64 accumulator columns of this thread's row -> (+bias) ReLU -> fp16 row of
+ * a K=64 tile.  The bias is added in fp32 (packed f32x2), and the ReLU runs on
+ * the rounded half2 pairs: rounding is monotonic and maps 0 to 0, and
+ * __hmax2, like fmaxf, returns the non-NaN operand and prefers +0, so the
+ * bits equal fmaxf-then-round with one instruction per pair instead of two. */
 __device__ __forceinline__ void epi_hidden(uint32_t taddr, const float *bias, uint8_t *dst, int row)
 {
+    const __half2 zero = __float2half2_rn(0.0f);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         float v[32];
         tmem_ld32(taddr + 32 * h, v);
         tmem_wait_ld();
+        uint32_t w[16];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + (bias ? bias[32 * h + i] : 0.0f), 0.0f);
+        for (int i = 0; i < 16; ++i) {
+            float2 x = make_float2(v[2 * i], v[2 * i + 1]);
+            if (bias) x = __fadd2_rn(x, make_float2(bias[32 * h + 2 * i], bias[32 * h + 2 * i + 1]));
+            const __half2 r = __hmax2(__float22half2_rn(x), zero);
+            w[i] = *reinterpret_cast<const uint32_t *>(&r);
+        }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) st_chunk(dst, row, 4 * h + q, 64, pack8(v + 8 * q));
+        for (int q = 0; q < 4; ++q) st_chunk(dst, row, 4 * h + q, 64, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
     }
 }
 
