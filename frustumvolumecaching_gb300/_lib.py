@@ -135,6 +135,7 @@ SIGNATURES = {
     "fvc_cache_resize": (c_int, [P, c_int, c_int, C.POINTER(StepsizeInfo)]),
     "fvc_renderer_set_cache_settings": (c_int, [P, C.POINTER(CacheSettings)]),
     "fvc_cache_build": (c_int, [P, C.POINTER(RaymarchInfo)]),
+    "fvc_cache_build_per_ray": (c_int, [P, C.POINTER(RaymarchInfo)]),
     "fvc_cache_swap": (c_int, [P]),
     "fvc_cache_stats": (c_int, [P, C.POINTER(CacheStats)]),
     "fvc_renderer_set_render_mode": (c_int, [P, c_int]),

@@ -336,6 +336,21 @@ struct BuildScratch {
     }
 };
 
+/* scratch of the per-ray cache fill (fvc_cache_build_per_ray) */
+struct PerRayScratch {
+    uint8_t *flag = nullptr, *set = nullptr;  /* per brick of the frustum */
+    int *col_count = nullptr, *col_base = nullptr;
+    int *slots = nullptr;                      /* [0] slot counter, [1] its value before the sub-iteration */
+    __half *den = nullptr;                     /* per row */
+    uint4 *lat = nullptr;
+    size_t n_bricks = 0, n_cols = 0, n_rows = 0;
+    void release()
+    {
+        dfree(flag); dfree(set); dfree(col_count); dfree(col_base); dfree(slots); dfree(den); dfree(lat);
+        n_bricks = n_cols = n_rows = 0;
+    }
+};
+
 struct fvc_renderer {
     fvc_model *m = nullptr;
     int kind = FVC_RENDERER_PERFORMANCE;
@@ -393,6 +408,7 @@ struct fvc_renderer {
     int use_tc = 1;                   /* network kernels on tcgen05 (1) or mma.sync (0) */
     int precision = FVC_PRECISION_FP16;
     BuildScratch bs;
+    PerRayScratch pr;
     std::mutex read_mutex, write_mutex;
     ~fvc_renderer()
     {
@@ -403,6 +419,7 @@ struct fvc_renderer {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         release_wavefront();
         bs.release();
+        pr.release();
         if (h_pinned) cudaFreeHost(h_pinned);
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (own_stream) cudaStreamDestroy(own_stream);
@@ -1408,6 +1425,108 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     c->built = true;
     if (guard) return fail(FVC_ERR_GUARD, "cache build guard fired: flags " + std::to_string(guard));
     if (n_alive > 0) return fail(FVC_ERR_GUARD, "cache build did not converge within the frustum depth");
+    return FVC_OK;
+}
+
+/* CacheRenderer::initCache, src/cache_renderer.cu:848-928: the per-ray fill
+ * of the "next" cache.  The cache camera's rays march like a plain render,
+ * TARGET_BATCH_SIZE / alive (1..8) occupied samples per ray and sub-iteration;
+ * each sub-iteration marks the bricks of the visible samples, reserves slots
+ * for the new ones and writes the voxels (see PerRayFillParams).  Slots are
+ * reserved per sub-iteration in (brick column, depth) order instead of by
+ * atomicAdd, so the fill is reproducible. */
+extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info *info)
+{
+    CHECK_ARG(r && info, "fvc_cache_build_per_ray: null argument");
+    CHECK_ARG(r->next, "fvc_cache_build_per_ray: caches not attached (fvc_renderer_set_caches)");
+    int rc;
+    if ((rc = check_info(info))) return rc;
+    fvc_model *m = r->m;
+    if ((rc = check_variant(r))) return rc;
+    std::scoped_lock lk(r->read_mutex, r->write_mutex); /* the fill runs on the renderer's wavefront buffers */
+    fvc_cache *c = r->next;
+    const int W = info->cam_info.resolution.x, H = info->cam_info.resolution.y;
+    if ((rc = cache_resize(r, c, W, H, info->stepsize_info))) return rc;
+    c->rm_info = *info;
+    c->built = false;
+    RenderParams p;
+    if ((rc = setup_render_params(r, info, nullptr, nullptr, nullptr, p, true))) return rc;
+    p.steps_per_iter = 1 << 30; /* sample_common_kernel marches until it has its samples */
+    PerRayScratch &x = r->pr;
+    const size_t n_bricks = (size_t)c->bX * c->bY * c->bZ, n_cols = (size_t)c->bX * c->bY, n_rows = (size_t)r->row_capacity;
+    if (x.n_bricks < n_bricks || x.n_cols < n_cols || x.n_rows < n_rows) {
+        x.release();
+        if ((rc = dalloc(&x.flag, n_bricks, "fill brick marks"))) return rc;
+        if ((rc = dalloc(&x.set, n_bricks, "fill brick flags"))) return rc;
+        if ((rc = dalloc(&x.col_count, n_cols, "fill column counts"))) return rc;
+        if ((rc = dalloc(&x.col_base, n_cols, "fill column bases"))) return rc;
+        if ((rc = dalloc(&x.slots, (size_t)2, "fill slot counter"))) return rc;
+        if ((rc = dalloc(&x.den, n_rows, "fill densities"))) return rc;
+        if ((rc = dalloc(&x.lat, n_rows, "fill latents"))) return rc;
+        x.n_bricks = n_bricks; x.n_cols = n_cols; x.n_rows = n_rows;
+    }
+    PerRayFillParams f;
+    memset(&f, 0, sizeof(f));
+    f.scene = m->dscene; f.steps = p.steps; f.W = W; f.H = H;
+    f.states[0] = p.states[0]; f.states[1] = p.states[1];
+    f.ray_rows = p.ray_rows; f.row_t0 = p.row_t0; f.den = x.den; f.lat = x.lat; f.counters = p.counters;
+    f.flag = x.flag; f.set = x.set; f.packed_index = c->d_packed; f.known_ranges = c->d_known; f.voxels = c->d_voxels;
+    f.bX = c->bX; f.bY = c->bY; f.bZ = c->bZ; f.dX = c->dX; f.dY = c->dY; f.dZ = c->dZ; f.capacity = c->capacity();
+    f.variant = r->settings.interpol_variant;
+    f.slot_counter = x.slots; f.col_count = x.col_count; f.col_base = x.col_base;
+    CacheBuildParams q; /* the density network over the sub-iteration's rows */
+    memset(&q, 0, sizeof(q));
+    q.grid = m->grid; q.table = m->d_table; q.weights = m->d_weights; q.latent_offset = m->latent_offset;
+    q.build_rows = p.row_pay; q.build_den = x.den; q.build_lat = x.lat; q.build_row_counter = p.counters + 2;
+    cudaStream_t s = r->stream;
+    CU(cudaMemsetAsync(x.flag, 0, n_bricks, s));
+    CU(cudaMemsetAsync(x.set, 0, n_bricks, s));
+    CU(cudaMemsetAsync(x.slots, 0, 2 * sizeof(int), s));
+    CU(cudaMemsetAsync(c->d_packed, 0xff, n_bricks * sizeof(int32_t), s));
+    CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), s));
+    CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), s));
+    CU(cudaMemsetAsync(p.counters, 0, 8 * sizeof(int), s));
+    const int n_sms = m->n_sms;
+    pr_known_init_kernel<<<n_sms * 4, 256, 0, s>>>(f);
+    CU(launch_fill_raygen(p, s));
+    int n_launches = 2;
+    CU(cudaMemcpyAsync(r->h_pinned, p.counters, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    int n_alive = r->h_pinned[0];
+    long long n_samples = 0;
+    int it = 0;
+    for (; it < 1000 && n_alive > 0; ++it) { /* MAX_SUBITER */
+        const int n_steps = std::min(8, std::max(1, (1 << 21) / n_alive)); /* TARGET_BATCH_SIZE / n_alive */
+        p.row_capacity = n_steps * n_alive;                                 /* the march gives every ray n_steps rows */
+        n_samples += ((long long)n_alive * n_steps + 255) / 256 * 256;     /* next_multiple(batch, 256) */
+        CU(cudaMemsetAsync(p.counters + 2, 0, sizeof(int), s));
+        CU(launch_fill_march(p, it, n_sms, s));
+        cache_density_kernel<<<n_sms * 8, 128, 0, s>>>(q);
+        pr_mark_kernel<<<n_sms * 16, 128, 0, s>>>(f, it);
+        pr_count_kernel<<<(int)((n_cols + 255) / 256), 256, 0, s>>>(f);
+        pr_scan_kernel<<<1, 1024, 0, s>>>(f);
+        pr_reserve_kernel<<<(int)((n_cols + 255) / 256), 256, 0, s>>>(f);
+        pr_zero_kernel<<<n_sms * 4, 256, 0, s>>>(f);
+        pr_write_kernel<<<n_sms * 16, 128, 0, s>>>(f, it);
+        CU(cudaGetLastError());
+        n_launches += 8;
+        CU(cudaMemcpyAsync(r->h_pinned, p.counters + ((it + 1) & 1), sizeof(int), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        n_alive = r->h_pinned[0];
+    }
+    CU(cudaMemcpyAsync(r->h_pinned, x.slots, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(r->h_pinned + 1, r->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    const int demanded = r->h_pinned[0], guard = r->h_pinned[1];
+    c->stats.n_bricks_demanded = demanded;
+    c->stats.n_bricks_reserved = c->capacity();
+    c->stats.n_bricks_set = std::min(demanded, c->capacity());
+    c->stats.overflow = demanded > c->capacity();
+    c->stats.n_iterations = it;
+    c->stats.n_launches = n_launches;
+    c->stats.n_samples = n_samples;
+    c->built = true;
+    if (guard) return fail(FVC_ERR_GUARD, "per-ray cache fill guard fired: flags " + std::to_string(guard));
     return FVC_OK;
 }
 

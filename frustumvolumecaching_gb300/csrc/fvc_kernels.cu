@@ -480,4 +480,212 @@ __global__ void __launch_bounds__(1024) cache_compact_kernel(CacheBuildParams p,
     if (tid == 0) *p.n_alive_tiles = s_carry;
 }
 
+/* ------------------------------------------------------------------------- */
+/* per-ray cache fill (CacheRenderer::initCache, src/cache_renderer.cu:571-928) */
+/* ------------------------------------------------------------------------- */
+/* known_ranges_to starts at StepsizeInfo::far, the RayPayload
+ * termination_depth of rays that end neither by opacity nor by overflow
+ * (initRayPayloads_common_kernel, src/renderer.cu:62-78) */
+__global__ void pr_known_init_kernel(PerRayFillParams p)
+{
+    const int n = p.W * p.H;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p.known_ranges[i] = p.steps.far_;
+}
+
+/* the froxel brick of a sample of pixel id at the midpoint tm, or -1 past the
+ * frustum depth (bin = floor(step_from_t(t_mid) - near_i), :598-604) */
+__device__ __forceinline__ int pr_brick(const PerRayFillParams &p, int id, float tm, int &bin)
+{
+    bin = (int)floorf(F_SUB(step_from_t(p.steps, tm), p.steps.near_i));
+    const int bz = bin >> 3;
+    if (bin < 0 || bz >= p.bZ) return -1;
+    const int x = id % p.W, y = id / p.W;
+    return (bz * p.bY + (y >> 3)) * p.bX + (x >> 3);
+}
+
+/* accumulate_cache_init_first_kernel (:571-623): per alive ray, the bricks of
+ * its visible samples of this sub-iteration, until the transmittance falls
+ * below 1e-4 (unclamped density) */
+__global__ void __launch_bounds__(128) pr_mark_kernel(PerRayFillParams p, int it)
+{
+    const int n_alive = p.counters[it & 1];
+    const RayState *states = p.states[it & 1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_alive; i += gridDim.x * blockDim.x) {
+        const int2 rr = p.ray_rows[i];
+        const int id = states[i].cnt.x;
+        float T = states[i].acc.w;
+        for (int k = 0; k < rr.y; ++k) {
+            const int row = rr.x + k;
+            const float density = expf(__half2float(p.den[row]));
+            const float t0 = p.row_t0[row];
+            const float dt = calc_step(p.steps, t0);
+            const float t1 = F_ADD(t0, dt);
+            const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
+            const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-density * dt)));
+            if (alpha > p.scene.alpha_thre) {
+                T *= 1.0f - alpha;
+                int bin;
+                const int b = pr_brick(p, id, tm, bin);
+                if (b < 0) break; /* beyond the frustum depth: pr_write ends the ray here */
+                p.flag[b] = 1;
+            }
+            if (T < 1e-4f) break;
+        }
+    }
+}
+
+/* reserveNewBricks_kernel (:775-805) made deterministic: per brick column,
+ * the number of bricks marked in this sub-iteration that hold no slot yet */
+__global__ void __launch_bounds__(256) pr_count_kernel(PerRayFillParams p)
+{
+    const int n_cols = p.bX * p.bY;
+    const size_t plane = (size_t)n_cols;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cols; c += gridDim.x * blockDim.x) {
+        int n = 0;
+        for (int z = 0; z < p.bZ; ++z) {
+            const size_t b = (size_t)z * plane + c;
+            n += p.flag[b] && !p.set[b];
+        }
+        p.col_count[c] = n;
+    }
+}
+
+/* exclusive scan of the column counts from the slot counter (one CTA of 1024) */
+__global__ void __launch_bounds__(1024) pr_scan_kernel(PerRayFillParams p)
+{
+    __shared__ int s_w[33];
+    __shared__ int s_carry;
+    const int n_cols = p.bX * p.bY;
+    if (threadIdx.x == 0) {
+        s_carry = p.slot_counter[0];
+        p.slot_counter[1] = s_carry;
+    }
+    __syncthreads();
+    for (int c0 = 0; c0 < n_cols; c0 += 1024) {
+        const int c = c0 + threadIdx.x;
+        const int v = c < n_cols ? p.col_count[c] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, total, s_w);
+        if (c < n_cols) p.col_base[c] = s_carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) p.slot_counter[0] = s_carry;
+}
+
+/* slots in (column, depth) order; a slot beyond the capacity leaves the brick
+ * without one (packed index -1), as the reference's overflow does; clears the
+ * marks for the next sub-iteration */
+__global__ void __launch_bounds__(256) pr_reserve_kernel(PerRayFillParams p)
+{
+    const int n_cols = p.bX * p.bY;
+    const size_t plane = (size_t)n_cols;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cols; c += gridDim.x * blockDim.x) {
+        int slot = p.col_base[c];
+        for (int z = 0; z < p.bZ; ++z) {
+            const size_t b = (size_t)z * plane + c;
+            if (!p.flag[b]) continue;
+            p.flag[b] = 0;
+            if (p.set[b]) continue;
+            const bool overflow = slot >= p.capacity;
+            if (!overflow) {
+                const int sx = slot / (p.dY * p.dZ), sy = (slot - sx * p.dY * p.dZ) / p.dZ;
+                const int sz = slot - sx * p.dY * p.dZ - sy * p.dZ;
+                p.packed_index[b] = (sx << 20) | (sy << 10) | sz;
+                p.set[b] = 1;
+            } else {
+                p.packed_index[b] = -1;
+            }
+            ++slot;
+        }
+    }
+}
+
+/* the slots reserved in this sub-iteration start out empty (Cache::
+ * setDataArraysZero, src/cache_renderer.cu:854) */
+__global__ void __launch_bounds__(256) pr_zero_kernel(PerRayFillParams p)
+{
+    const int s0 = min(p.slot_counter[1], p.capacity), s1 = min(p.slot_counter[0], p.capacity);
+    uint4 *v = reinterpret_cast<uint4 *>(p.voxels);
+    const size_t n = (size_t)(s1 - s0) * 1024;
+    const size_t base = (size_t)s0 * 1024;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        v[base + i] = make_uint4(0, 0, 0, 0);
+}
+
+/* accumulate_cache_init_second_kernel (:625-773): per alive ray, the voxels of
+ * its visible samples (density clamped to exp(10)), the density slot and
+ * latent 0 per interpol_variant; a sample whose brick got no slot (or lies
+ * beyond the frustum depth) ends the ray at its t0, transmittance below 1e-4
+ * at its t1.  Rays that end write their termination depth to known_ranges_to
+ * (writeImageBuffer_cache_init_kernel, :807-827); the others are compacted
+ * into the next alive list. */
+__global__ void __launch_bounds__(128) pr_write_kernel(PerRayFillParams p, int it)
+{
+    const int n_alive = p.counters[it & 1];
+    RayState *states = p.states[it & 1];
+    RayState *next = p.states[(it + 1) & 1];
+    const bool by_alpha = p.variant == VARIANT_ALPHA || p.variant == VARIANT_ALPHA_INTERMEDIATES;
+    const bool lat0 = p.variant == VARIANT_DENSITY_INTERMEDIATES || p.variant == VARIANT_ALPHA_INTERMEDIATES;
+    Voxel *vox = reinterpret_cast<Voxel *>(p.voxels);
+    for (int base = blockIdx.x * blockDim.x; base < n_alive; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        bool alive = false;
+        RayState st;
+        if (i < n_alive) {
+            st = states[i];
+            const int2 rr = p.ray_rows[i];
+            const int id = st.cnt.x;
+            float T = st.acc.w, term = p.steps.far_;
+            alive = st.cnt2.y == 0; /* the march ended the ray past its far bound */
+            for (int k = 0; k < rr.y; ++k) {
+                const int row = rr.x + k;
+                const float density = expf(fminf(__half2float(p.den[row]), 10.0f));
+                const float t0 = p.row_t0[row];
+                const float dt = calc_step(p.steps, t0);
+                const float t1 = F_ADD(t0, dt);
+                const float tm = F_MUL(F_ADD(t0, t1), 0.5f);
+                const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-density * dt)));
+                if (alpha > p.scene.alpha_thre) {
+                    T *= 1.0f - alpha;
+                    int bin;
+                    const int b = pr_brick(p, id, tm, bin);
+                    const int packed = b >= 0 ? p.packed_index[b] : -1;
+                    if (packed < 0) { /* no slot: the cache overflowed here */
+                        alive = false;
+                        term = t0;
+                        break;
+                    }
+                    const int x = id % p.W, y = id / p.W;
+                    const int slot = ((packed >> 20) & 1023) * (p.dY * p.dZ) + ((packed >> 10) & 1023) * p.dZ + (packed & 1023);
+                    Voxel v;
+                    v.density = by_alpha ? alpha : density;
+                    v.isset = 1.0f;
+                    v.pad0 = v.pad1 = 0.f;
+                    v.lat = p.lat[row];
+                    if (lat0) v.lat.x = (v.lat.x & 0xffff0000u) | (uint32_t)__half_as_ushort(__float2half_rn(v.density));
+                    vox[(size_t)slot * 512 + (bin & 7) * 64 + (y & 7) * 8 + (x & 7)] = v;
+                }
+                if (T < 1e-4f) {
+                    alive = false;
+                    term = t1;
+                    break;
+                }
+            }
+            st.acc.w = T;
+            if (!alive) p.known_ranges[id] = term;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, alive);
+        int wbase = 0;
+        if ((threadIdx.x & 31) == 0 && m) wbase = atomicAdd(p.counters + ((it + 1) & 1), __popc(m));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (alive) {
+            unsigned lt;
+            asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+            next[wbase + __popc(m & lt)] = st;
+        }
+    }
+}
+
 }  // namespace fvc

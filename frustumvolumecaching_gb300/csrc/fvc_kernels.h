@@ -285,6 +285,43 @@ struct LaunchLog {
     int n_untimed = 0;
 };
 
+/* The per-ray cache fill (CacheRenderer::initCache, src/cache_renderer.cu:
+ * 571-928): the cache camera's own rays marched like a plain render, their
+ * occupied samples through the density network, then per sub-iteration
+ * pr_mark (bricks holding a visible sample), the deterministic per-column
+ * slot reservation (pr_count / pr_scan / pr_reserve, then pr_zero clears the
+ * new slots) and pr_write (voxels, termination, compaction, known ranges). */
+struct PerRayFillParams {
+    DevScene scene;
+    DevSteps steps;
+    int W, H;
+    RayState *states[2];        /* the renderer's alive-ray states (ping-pong) */
+    const int2 *ray_rows;       /* per alive ray: first row, row count */
+    const float *row_t0;
+    const __half *den;          /* per row: log-density (fp16) */
+    const uint4 *lat;           /* per row: latents latent_offset + 0..7 (fp16) */
+    int *counters;              /* the renderer's wavefront counters: [0], [1] alive rays (ping-pong) */
+    uint8_t *flag;              /* [bZ][bY][bX]: brick marked in this sub-iteration */
+    uint8_t *set;               /* [bZ][bY][bX]: brick holds a slot */
+    int32_t *packed_index;      /* [bZ][bY][bX] */
+    float *known_ranges;        /* [fH][fW] */
+    void *voxels;               /* [slots][512] */
+    int bX, bY, bZ, dX, dY, dZ, capacity, variant;
+    int *slot_counter;          /* [0] slots reserved so far (overflowing ones included), [1] its value before this
+                                   sub-iteration */
+    int *col_count, *col_base;  /* per brick column (bY x bX) */
+};
+
+__global__ void pr_known_init_kernel(PerRayFillParams p);
+__global__ void pr_mark_kernel(PerRayFillParams p, int it);
+__global__ void pr_count_kernel(PerRayFillParams p);
+__global__ void pr_scan_kernel(PerRayFillParams p);
+__global__ void pr_reserve_kernel(PerRayFillParams p);
+__global__ void pr_zero_kernel(PerRayFillParams p);
+__global__ void pr_write_kernel(PerRayFillParams p, int it);
+cudaError_t launch_fill_march(const RenderParams &p, int it, int n_sms, cudaStream_t s);
+cudaError_t launch_fill_raygen(const RenderParams &p, cudaStream_t s);
+
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,
                          int check_every, int *n_iterations, LaunchLog *log = nullptr);
 

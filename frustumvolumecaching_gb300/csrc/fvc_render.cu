@@ -1247,6 +1247,20 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     return cudaGetLastError();
 }
 
+/* the plain renderer's raygen and march, for the per-ray cache fill */
+cudaError_t launch_fill_raygen(const RenderParams &p, cudaStream_t s)
+{
+    const int n_threads = ((p.cam.W + 7) / 8) * ((p.cam.H + 3) / 4) * 32;
+    wf_raygen_kernel<<<(n_threads + 255) / 256, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_march(const RenderParams &p, int it, int n_sms, cudaStream_t s)
+{
+    wf_march_kernel<false><<<n_sms * 16, 128, 0, s>>>(p, it);
+    return cudaGetLastError();
+}
+
 /* Pass 2 of the differentiable render (pass 1 is run_frame over the pixel
  * list, then the loss kernel): the same march and network forward per
  * sub-iteration, then the compositing adjoint and the network adjoint. */

@@ -348,6 +348,10 @@ class CachePerformanceRenderer(Renderer):
     def initCacheBlockwise(self, rm_info: L.RaymarchInfo, debug_image_buffer=None) -> None:
         L.check(L.load().fvc_cache_build(self.handle, C.byref(rm_info)))
 
+    def initCache(self, rm_info: L.RaymarchInfo, debug_image_buffer=None) -> None:
+        """The per-ray fill (CacheRenderer::initCache, src/cache_renderer.cu:848-928)."""
+        L.check(L.load().fvc_cache_build_per_ray(self.handle, C.byref(rm_info)))
+
     def swapCache(self) -> None:
         L.check(L.load().fvc_cache_swap(self.handle))
         self._cache, self._cache_next = self._cache_next, self._cache

@@ -326,6 +326,15 @@ int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_settings *s
 /* initCacheBlockwise(RaymarchInfo, RenderBuffer&), src/cache_renderer.cu:931-1051:
  * fills the "next" cache. Synchronous. */
 int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info);
+/* initCache(RaymarchInfo, RenderBuffer&), src/cache_renderer.cu:848-928: the
+ * per-ray fill of the "next" cache (each cache-camera ray marched to its
+ * termination, voxels written per visible sample, a ray ending where its
+ * brick finds no slot). Slots are reserved per sub-iteration in (brick
+ * column, depth) order, not by atomicAdd, so the result is reproducible.
+ * Runs on the renderer's render buffers (sized to the cache view) and takes
+ * both of its locks. Synchronous; fvc_cache_stats reports n_samples as the
+ * reference counts them (padded batches). */
+int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info *info);
 /* swapCache(), src/cache_renderer.cu:1053-1057. */
 int fvc_cache_swap(fvc_renderer *r);
 int fvc_cache_stats(fvc_renderer *r, fvc_cache_stats_t *out);

@@ -751,10 +751,20 @@ struct CacheRenderer : public Renderer {
     {
         fvc_cpp::check(fvc_cache_resize(_handle, resolution.x, resolution.y, fvc_cpp::abi(stepsize_info)));
     }
-    /* the per-ray cache fill (src/cache_renderer.cu:571-928) is not built */
-    void initCache(RaymarchInfo, RenderBuffer &)
+    /* the per-ray fill of the next cache (src/cache_renderer.cu:848-928): sizes
+     * the cache and the render buffers to the view as the reference does; the
+     * debug buffer is not written */
+    void initCache(RaymarchInfo rm_info, RenderBuffer &)
     {
-        throw std::runtime_error("initCache (per-ray cache fill) is not available; use initCacheBlockwise");
+        resizeCache(rm_info.cam_info.resolution, rm_info.stepsize_info);
+        fvc_cpp::check(fvc_renderer_resize(_handle, rm_info.cam_info.resolution.x, rm_info.cam_info.resolution.y));
+        fvc_cpp::check(fvc_cache_build_per_ray(_handle, fvc_cpp::abi(rm_info)));
+        fvc_cache_stats_t st{};
+        fvc_cpp::check(fvc_cache_stats(_handle, &st));
+        const float n_rays = (float)std::max(1, rm_info.cam_info.resolution.x * rm_info.cam_info.resolution.y);
+        _init_stats.samples_ppx = (float)st.n_samples / n_rays; /* :920 */
+        _init_stats.n_bricks_set = st.n_bricks_set;
+        _init_stats.n_bricks_reserved = st.n_bricks_reserved;
     }
     /* fills the next cache (src/cache_renderer.cu:931-1051); the debug buffer is not written */
     void initCacheBlockwise(RaymarchInfo rm_info, RenderBuffer &)

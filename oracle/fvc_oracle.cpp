@@ -749,6 +749,150 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
     return 0;
 }
 
+/* Per-ray cache fill: CacheRenderer::initCache and its kernels
+ * (src/cache_renderer.cu:571-928, sample_common_kernel src/renderer.cu:
+ * 192-245).  Every cache-camera ray that hits the scene box marches in
+ * sub-iterations of TARGET_BATCH_SIZE / alive (1..8) occupied samples; per
+ * sub-iteration the bricks of visible samples are marked (unclamped density,
+ * until T < 1e-4), new bricks get slots in (brick column, depth) order (the
+ * reference's atomicAdd order is unspecified), and the voxels are written
+ * (density clamped to exp(10)); a sample whose brick has no slot, or lies
+ * beyond the frustum depth, ends its ray at t0, T < 1e-4 at t1.
+ * known_ranges_to = the termination depth, StepsizeInfo::far for rays that
+ * end otherwise.  cc->n_samples counts the padded batches as the reference. */
+int orc_cache_build_per_ray(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
+                            OrcCache *cc, int n_threads)
+{
+    NetD d; prepare_net(net, d);
+    const OrcCacheDims &cd = cc->dims;
+    const int W = cam->W, H = cam->H;
+    const int capacity = cd.dX * cd.dY * cd.dZ;
+    const size_t n_bricks = (size_t)cd.bX * cd.bY * cd.bZ, plane = (size_t)cd.bX * cd.bY;
+    std::fill(cc->packed_index, cc->packed_index + n_bricks, -1);
+    std::vector<uint8_t> flag(n_bricks, 0), set(n_bricks, 0);
+    for (int i = 0; i < W * H; ++i) cc->known_ranges[i] = st->far_;
+    struct R { Ray r; int id; float far_, t1; double T; bool done; };
+    std::vector<R> alive;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            R q;
+            q.r = generate_ray(*cam, x, y);
+            float tn, tf;
+            if (!ray_aabb(q.r, sc->aabb_from, sc->aabb_to, tn, tf)) continue;
+            q.id = y * W + x;
+            q.far_ = fminf(tf, st->far_);
+            q.t1 = valid_t_from_t(*st, tn) + 0.0f;
+            q.T = 1.0;
+            q.done = false;
+            alive.push_back(q);
+        }
+    auto brick_of = [&](int id, float tm, int &bin) -> long long {
+        bin = (int)floorf(step_from_t(*st, tm) - st->near_i);
+        const int bz = bin >> 3;
+        if (bin < 0 || bz >= cd.bZ) return -1;
+        const int x = id % W, y = id / W;
+        return ((long long)bz * cd.bY + (y >> 3)) * cd.bX + (x >> 3);
+    };
+    long long counter = 0, n_samples = 0;
+    int iter = 0;
+    struct S { float t0; double lat[8], logd; };
+    for (; iter < 1000 && !alive.empty(); ++iter) {
+        const int n_alive = (int)alive.size();
+        const int n_steps = std::min(8, std::max(1, (1 << 21) / n_alive));
+        n_samples += ((long long)n_alive * n_steps + 255) / 256 * 256;
+        std::vector<std::vector<S>> smp(n_alive);
+        /* sample_common_kernel + inferenceLatents */
+        parallel_rows(n_alive, n_threads, [&](int i) {
+            R &q = alive[i];
+            while ((int)smp[i].size() < n_steps) {
+                const float t0 = q.t1, dt = calc_step(*st, t0), t1 = t0 + dt, tm = (t0 + t1) * 0.5f;
+                if (tm > q.far_) { q.done = true; break; }
+                q.t1 = t1;
+                if (!occupied(*sc, bits, at(q.r, tm))) continue;
+                double bo[64];
+                base_forward(d, contract(*sc, at(q.r, tm)), bo);
+                S e;
+                e.t0 = t0;
+                e.logd = bo[0];
+                for (int j = 0; j < 8; ++j) e.lat[j] = bo[net->latent_offset + j];
+                smp[i].push_back(e);
+            }
+        });
+        /* accumulate_cache_init_first_kernel */
+        for (int i = 0; i < n_alive; ++i) {
+            double T = alive[i].T;
+            for (const S &e : smp[i]) {
+                const float dt = calc_step(*st, e.t0), tm = (e.t0 + (e.t0 + dt)) * 0.5f;
+                const double alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-std::exp(e.logd) * (double)dt)));
+                if (alpha > (double)sc->alpha_thre) {
+                    T *= 1.0 - alpha;
+                    int bin;
+                    const long long b = brick_of(alive[i].id, tm, bin);
+                    if (b < 0) break;
+                    flag[b] = 1;
+                }
+                if (T < 1e-4) break;
+            }
+        }
+        /* reserveNewBricks_kernel, in (column, depth) order */
+        for (size_t c = 0; c < plane; ++c)
+            for (int z = 0; z < cd.bZ; ++z) {
+                const size_t b = (size_t)z * plane + c;
+                if (!flag[b]) continue;
+                flag[b] = 0;
+                if (set[b]) continue;
+                const long long slot = counter++;
+                if (slot < capacity) {
+                    const int sx = (int)(slot / (cd.dY * cd.dZ)), sy = (int)((slot - (long long)sx * cd.dY * cd.dZ) / cd.dZ);
+                    const int sz = (int)(slot - (long long)sx * cd.dY * cd.dZ - (long long)sy * cd.dZ);
+                    cc->packed_index[b] = pack3(sx, sy, sz);
+                    set[b] = 1;
+                } else {
+                    cc->packed_index[b] = -1;
+                }
+            }
+        /* accumulate_cache_init_second_kernel */
+        std::vector<R> next;
+        for (int i = 0; i < n_alive; ++i) {
+            R &q = alive[i];
+            double T = q.T;
+            float term = st->far_;
+            bool live = !q.done;
+            for (const S &e : smp[i]) {
+                const float dt = calc_step(*st, e.t0), t1 = e.t0 + dt, tm = (e.t0 + t1) * 0.5f;
+                const double density = std::exp(std::min(e.logd, 10.0));
+                const double alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-density * (double)dt)));
+                if (alpha > (double)sc->alpha_thre) {
+                    T *= 1.0 - alpha;
+                    int bin;
+                    const long long b = brick_of(q.id, tm, bin);
+                    const int packed = b >= 0 ? cc->packed_index[b] : -1;
+                    if (packed < 0) { live = false; term = e.t0; break; }
+                    const int slot = ((packed >> 20) & 1023) * cd.dY * cd.dZ + ((packed >> 10) & 1023) * cd.dZ + (packed & 1023);
+                    const int x = q.id % W, y = q.id / W;
+                    const size_t v = (size_t)slot * 512 + (size_t)(bin & 7) * 64 + (y & 7) * 8 + (x & 7);
+                    const bool by_alpha = cc->variant == 1 || cc->variant == 4;
+                    const double val = by_alpha ? alpha : density;
+                    cc->vox_density[v] = (float)val;
+                    cc->vox_isset[v] = 1.0f;
+                    for (int j = 0; j < 8; ++j) cc->vox_latents[v * 8 + j] = d2h_bits(e.lat[j]);
+                    if (cc->variant == 3 || cc->variant == 4) cc->vox_latents[v * 8] = d2h_bits(val);
+                }
+                if (T < 1e-4) { live = false; term = t1; break; }
+            }
+            q.T = T;
+            if (live) next.push_back(q);
+            else cc->known_ranges[q.id] = term;
+        }
+        alive.swap(next);
+    }
+    cc->n_demanded = (int)counter;
+    cc->n_bricks_set = (int)std::min<long long>(counter, capacity);
+    cc->n_iterations = iter;
+    cc->n_samples = n_samples;
+    return 0;
+}
+
 /* voxel lookup through the data array's texel addressing (tex3D point with
  * border addressing, include/util/cuda_readwrite_array.h:41-62) */
 struct Vox { double density, isset, lat[8]; };

@@ -100,6 +100,8 @@ def lib():
         _lib.orc_loss_grad_cached.restype = C.c_double
         _lib.orc_cache_dims.argtypes = [P(OrcScene), P(OrcSteps), C.c_int, C.c_int, P(OrcCacheDims)]
         _lib.orc_cache_build.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache), C.c_int]
+        _lib.orc_cache_build_per_ray.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
+                                                 C.c_int]
         _lib.orc_render_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
                                            P(OrcCam), P(OrcSteps), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                            C.c_int]
@@ -275,6 +277,15 @@ class OracleModel:
                               C.byref(cc.s), threads or default_threads())
         return cc
 
+    def cache_build_per_ray(self, cam: dict, threads: int | None = None, variant: int = 0) -> "OracleCache":
+        """The per-ray fill (CacheRenderer::initCache) with the model's steps."""
+        c = make_cam(cam)
+        cc = OracleCache(self.cache_dims(c.W, c.H), cam)
+        cc.s.variant = variant
+        lib().orc_cache_build_per_ray(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
+                                      C.byref(cc.s), threads or default_threads())
+        return cc
+
     def loss_grad_cached(self, cam: dict, cache: "OracleCache", pixels: np.ndarray, target: np.ndarray, grads: bool = True,
                          perturb=None, threads: int | None = None):
         """Cached-render loss at `pixels` against target [n,3] and, if grads, the
@@ -350,6 +361,10 @@ class OracleCache:
     @property
     def n_demanded(self):
         return self.s.n_demanded
+
+    @property
+    def n_samples(self):
+        return self.s.n_samples
 
 
 def composite_image(results: np.ndarray, sample_index: int = 0, prev: np.ndarray | None = None) -> np.ndarray:

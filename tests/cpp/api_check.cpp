@@ -55,6 +55,25 @@ int main(int argc, char **argv)
     big.resize(make_int2(80, 60));
     CHECK(std::fabs(big.focal.y - 2.0f * ci.focal.y) < 1e-4f && big.principal.x == 40.0f);
 
+    /* StepsizeInfo::setAdditionalInfo / changeSamplingRate (host only, through the library) */
+    SceneInfo sc{};
+    sc.grid_resolution = 128;
+    sc.grid_nlvl = 1;
+    sc.aabb_from = make_float3(-1.5f, -1.5f, -1.5f);
+    sc.aabb_to = make_float3(1.5f, 1.5f, 1.5f);
+    StepsizeInfo st{};
+    st.cone_angle = 1.0f / 256.0f;
+    st.stepsize = 0.002f;
+    st.near = 0.0f;
+    st.far = 1e10f;
+    st.setAdditionalInfo(sc);
+    StepsizeInfo half = st;
+    half.changeSamplingRate(2.0f, sc);
+    CHECK(st.dt_min == st.stepsize && st.i_max > st.i_min && st.t_max > st.t_min);
+    CHECK(half.stepsize == st.stepsize / 2.0f && half.dt_min == half.stepsize && half.i_max > st.i_max);
+    void (CacheRenderer::*fill)(RaymarchInfo, RenderBuffer &) = &CacheRenderer::initCache;
+    CHECK(fill != nullptr);
+
     std::vector<uint8_t> px(7 * 5 * 4);
     for (size_t i = 0; i < px.size(); ++i) px[i] = (uint8_t)(i * 37);
     CHECK(fvc_cpp::write_png(argv[2], px.data(), 7, 5));
