@@ -117,6 +117,8 @@ SIGNATURES = {
     "fvc_ingp_export": (c_int, [C.c_char_p, C.c_char_p]),
     "fvc_model_destroy": (None, [P]),
     "fvc_model_info": (c_int, [P, C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
+    "fvc_debug_fail_allocation": (c_int, [C.c_longlong]),
+    "fvc_selftest_wait_timeout": (c_int, [C.c_double, C.POINTER(C.c_double)]),
     "fvc_stepsize_setup": (c_int, [C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
     "fvc_model_density": (c_int, [P, P, c_int, P]),
     "fvc_model_inference": (c_int, [P, P, P, c_int, P]),

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstddef>
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <filesystem>
@@ -240,11 +241,25 @@ DevCam dev_cam(const fvc_camera_info &c)
     return d;
 }
 
+/* fvc_debug_fail_allocation: the library's device allocations still to
+ * succeed before one fails (-1: none fails) */
+static std::atomic<long long> g_allocs_before_failure{-1};
+
+static bool alloc_failure_due()
+{
+    long long n = g_allocs_before_failure.load();
+    while (n >= 0) {
+        if (g_allocs_before_failure.compare_exchange_weak(n, n - 1)) return n == 0;
+    }
+    return false;
+}
+
 template <class T>
 int dalloc(T **p, size_t n, const char *what)
 {
     *p = nullptr;
     if (n == 0) return FVC_OK;
+    if (alloc_failure_due()) return fail(FVC_ERR_OOM, std::string("cudaMalloc ") + what + ": injected allocation failure");
     cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
     if (e != cudaSuccess) {
         *p = nullptr;
@@ -858,6 +873,33 @@ extern "C" int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_ste
     CHECK_ARG(m, "fvc_model_info: null model");
     if (scene) *scene = m->scene;
     if (steps) *steps = m->steps;
+    return FVC_OK;
+}
+
+extern "C" int fvc_debug_fail_allocation(long long n)
+{
+    CHECK_ARG(n >= -1, "fvc_debug_fail_allocation: n must be >= -1");
+    g_allocs_before_failure.store(n);
+    return FVC_OK;
+}
+
+extern "C" int fvc_selftest_wait_timeout(double limit_ms, double *waited_ms)
+{
+    CHECK_ARG(limit_ms > 0.0 && limit_ms <= 1000.0, "fvc_selftest_wait_timeout: limit must be in (0, 1000] ms");
+    int dev = 0, khz = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+    long long *d = nullptr;
+    int rc;
+    if ((rc = dalloc(&d, (size_t)2, "wait self-test"))) return rc;
+    long long h[2] = {0, 0};
+    const long long limit = (long long)(limit_ms * (double)khz);
+    cudaError_t e = launch_wait_selftest(limit, d, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    dfree(d);
+    if (e != cudaSuccess) return fail(FVC_ERR_CUDA, std::string("wait self-test: ") + cudaGetErrorString(e));
+    if (waited_ms) *waited_ms = (double)h[1] / (double)khz;
+    if (h[0]) return fail(FVC_ERR_TIMEOUT, "bounded device wait gave up after " + std::to_string((double)h[1] / khz) + " ms");
     return FVC_OK;
 }
 

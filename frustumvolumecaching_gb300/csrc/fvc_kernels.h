@@ -320,6 +320,7 @@ __global__ void pr_reserve_kernel(PerRayFillParams p);
 __global__ void pr_zero_kernel(PerRayFillParams p);
 __global__ void pr_write_kernel(PerRayFillParams p, int it);
 cudaError_t launch_fill_march(const RenderParams &p, int it, int n_sms, cudaStream_t s);
+cudaError_t launch_wait_selftest(long long limit_cycles, long long *d_out, cudaStream_t s);
 cudaError_t launch_fill_raygen(const RenderParams &p, cudaStream_t s);
 
 cudaError_t render_frame(const RenderParams &p, bool cached, int head_hidden, int n_sms, cudaStream_t s, int *h_pinned,

@@ -1247,6 +1247,30 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     return cudaGetLastError();
 }
 
+/* Self-test of the bounded device wait: one warp waits on an mbarrier that
+ * nothing arrives at; mbar_wait gives up after limit_cycles SM clocks and the
+ * kernel reports it (out[0] = 1 when the wait ran out, out[1] = the cycles
+ * waited) instead of hanging. */
+__global__ void __launch_bounds__(32) wait_selftest_kernel(long long limit_cycles, long long *out)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const long long t0 = clock64();
+    const bool ok = mbar_wait(&bar, 0, limit_cycles);
+    const long long t1 = clock64();
+    if (threadIdx.x == 0) {
+        out[0] = ok ? 0 : 1;
+        out[1] = t1 - t0;
+    }
+}
+
+cudaError_t launch_wait_selftest(long long limit_cycles, long long *d_out, cudaStream_t s)
+{
+    wait_selftest_kernel<<<1, 32, 0, s>>>(limit_cycles, d_out);
+    return cudaGetLastError();
+}
+
 /* the plain renderer's raygen and march, for the per-ray cache fill */
 cudaError_t launch_fill_raygen(const RenderParams &p, cudaStream_t s)
 {

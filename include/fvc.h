@@ -183,6 +183,18 @@ void fvc_model_destroy(fvc_model *m);
 /* Scene and step parameters of the loaded model (LoaderData::scene_info,
  * ::stepsize_info after StepsizeInfo::setAdditionalInfo, include/common.h:109-131). */
 int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_stepsize_info *steps);
+/* Failure-path checks (no counterpart in the reference).
+ * fvc_debug_fail_allocation(n): the library's next n device allocations
+ * succeed and the one after fails with FVC_ERR_OOM, as a full device would
+ * make it fail (-1: off).  The call that hit it returns the error and leaves
+ * the handle usable; a later call allocates again.
+ * fvc_selftest_wait_timeout: runs the kernels' bounded device wait on an
+ * mbarrier that nothing completes, with a limit of limit_ms; returns
+ * FVC_ERR_TIMEOUT once the wait gave up (the normal outcome) with the time
+ * waited, and leaves the CUDA context usable.  The network kernels use the
+ * same wait (about 1 s) and report a run-out through the render guard. */
+int fvc_debug_fail_allocation(long long n);
+int fvc_selftest_wait_timeout(double limit_ms, double *waited_ms);
 /* StepsizeInfo::setAdditionalInfo (include/common.h:109-131): fills the
  * derived fields (dt_min/max, t_min/max, i_min/max, log1p_c, near_i) from
  * cone_angle, stepsize, near and far for the scene's grid.  Used by
