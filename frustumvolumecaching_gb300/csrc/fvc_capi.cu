@@ -241,6 +241,9 @@ DevCam dev_cam(const fvc_camera_info &c)
     return d;
 }
 
+/* the renderer kinds that render against a frustum cache */
+static bool is_cache_kind(int kind) { return kind == FVC_RENDERER_CACHE_PERFORMANCE || kind == FVC_RENDERER_CACHE_BASIC; }
+
 /* fvc_debug_fail_allocation: the library's device allocations still to
  * succeed before one fails (-1: none fails) */
 static std::atomic<long long> g_allocs_before_failure{-1};
@@ -323,6 +326,7 @@ struct fvc_cache {
         v.packed_index = d_packed; v.known_ranges = d_known; v.voxels = d_voxels;
         v.fW = fW; v.fH = fH; v.fD = fD; v.bX = bX; v.bY = bY; v.bZ = bZ; v.dX = dX; v.dY = dY; v.dZ = dZ;
         v.n_valid_slots = std::min(stats.n_bricks_demanded, capacity());
+        v.interp = 0; v.first_latent_is_density = 0; v.variant = 0; v.reweight = 1; v.keep_first = 1; v.inter_brick = 1;
         return v;
     }
 };
@@ -966,7 +970,7 @@ extern "C" int fvc_model_debug_encode(fvc_model *m, const float *pos, int n, flo
 extern "C" int fvc_renderer_create(fvc_model *m, int kind, fvc_renderer **out)
 {
     CHECK_ARG(m && out, "fvc_renderer_create: null argument");
-    CHECK_ARG(kind >= FVC_RENDERER_BASIC && kind <= FVC_RENDERER_CACHE_PERFORMANCE, "fvc_renderer_create: unknown kind");
+    CHECK_ARG(kind >= FVC_RENDERER_BASIC && kind <= FVC_RENDERER_CACHE_BASIC, "fvc_renderer_create: unknown kind");
     *out = nullptr;
     auto r = std::make_unique<fvc_renderer>();
     r->m = m;
@@ -1013,7 +1017,7 @@ extern "C" int fvc_renderer_resize(fvc_renderer *r, int width, int height)
     /* at least one row per ray: the march gives each alive ray
      * min(16, capacity / alive) rows, so capacity >= rays keeps that >= 1 */
     const size_t cap = std::max(n, std::min<size_t>(n * 16, (size_t)1 << 25));
-    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    const bool cached = is_cache_kind(r->kind);
     if ((rc = dalloc(&r->d_states[0], n, "ray states"))) return rc;
     if ((rc = dalloc(&r->d_states[1], n, "ray states"))) return rc;
     if ((rc = dalloc(&r->d_ray_rows, n, "ray rows"))) return rc;
@@ -1067,6 +1071,9 @@ static int check_variant(const fvc_renderer *r)
     if (r->m->n_latents > 8)
         return fail(FVC_ERR_CONFIG, "the cache stores 8 latents per voxel; this model's head reads " +
                                         std::to_string(r->m->n_latents));
+    /* the basic cache renderer puts its 8 interpolated intermediates where the
+     * head reads them whatever the variant (src/cache_basic_renderer.cu:187) */
+    if (r->kind == FVC_RENDERER_CACHE_BASIC) return FVC_OK;
     const bool di = r->settings.interpol_variant == VARIANT_DENSITY_INTERMEDIATES;
     if (di && r->m->latent_offset != 0)
         return fail(FVC_ERR_CONFIG, "the DensityIntermediates cache variant needs a model whose first latent is the density");
@@ -1079,15 +1086,20 @@ static int check_variant(const fvc_renderer *r)
 
 static void apply_settings(const fvc_renderer *r, CacheView &v)
 {
-    v.interp = r->settings.interpol_function;
-    v.first_latent_is_density = r->settings.interpol_variant == VARIANT_DENSITY_INTERMEDIATES;
+    const fvc_cache_settings &c = r->settings;
+    v.interp = c.interpol_function;
+    v.first_latent_is_density = c.interpol_variant == VARIANT_DENSITY_INTERMEDIATES;
+    v.variant = c.interpol_variant;
+    v.reweight = c.reweight_intermediates ? 1 : 0;
+    v.keep_first = c.disable_reweighting_first_intermediate ? 1 : 0;
+    v.inter_brick = c.use_inter_brick_interpolation ? 1 : 0;
 }
 
 static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts,
                                RenderParams &p, bool per_view_caches = false)
 {
     fvc_model *m = r->m;
-    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    const bool cached = is_cache_kind(r->kind);
     memset(&p, 0, sizeof(p));
     p.scene = m->dscene;
     p.steps = dev_steps(info->stepsize_info);
@@ -1103,6 +1115,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     if (r->precision != FVC_PRECISION_FP16 && (cached || !r->use_tc))
         return fail(FVC_ERR_CONFIG, "BF16 and FP8 MLPs are built for the plain renderers on the tcgen05 network path");
     p.latent_offset = m->latent_offset;
+    p.basic_cache = r->kind == FVC_RENDERER_CACHE_BASIC;
     p.ray_counter = r->d_ctl; p.guard = r->d_ctl + 1; p.stats = r->d_stats;
     p.results = results; p.image = image; p.ray_counts = counts;
     p.sample_index = info->sample_index;
@@ -1147,7 +1160,7 @@ static void reset_launch_log(fvc_renderer *r)
 static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts)
 {
     fvc_model *m = r->m;
-    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    const bool cached = is_cache_kind(r->kind);
     RenderParams p;
     int rc;
     if ((rc = setup_render_params(r, info, results, image, counts, p))) return rc;
@@ -1292,12 +1305,14 @@ extern "C" int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_
         return fail(FVC_ERR_ARG, "fvc_renderer_set_cache_settings: unknown DensityInterpolVariant");
     /* the performance renderer never writes the density slot in this variant,
      * so it classifies no sample as a cache sample */
-    if (s->interpol_variant == VARIANT_INTERMEDIATES)
+    if (s->interpol_variant == VARIANT_INTERMEDIATES && r->kind != FVC_RENDERER_CACHE_BASIC)
         return fail(FVC_ERR_CONFIG, "the Intermediates variant stores no density, which the cached performance renderer "
                                     "needs to classify cache samples");
-    /* use_hw_interpol, reweight_intermediates, disable_reweighting_first_intermediate and
-     * use_inter_brick_interpolation steer CacheBasicRenderer only; the performance
-     * renderer ignores them, as the reference's does */
+    /* reweight_intermediates, disable_reweighting_first_intermediate and
+     * use_inter_brick_interpolation steer the basic cache renderer only; the
+     * performance renderer ignores them, as the reference's does.  use_hw_interpol
+     * is unused in both (the texture fetches decide, include/raymarch_common.h:
+     * 420-424) */
     r->settings = *s;
     return FVC_OK;
 }
@@ -1770,9 +1785,11 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
 {
     CHECK_ARG(r && g && info && pixels && target && n_rays > 0, "fvc_render_backward: bad arguments");
     CHECK_ARG(g->m == r->m, "fvc_render_backward: gradients belong to another model");
-    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    const bool cached = is_cache_kind(r->kind);
     if (r->precision == FVC_PRECISION_FP8_E4M3)
         return fail(FVC_ERR_CONFIG, "fvc_render_backward: the network adjoint is built for FP16 and BF16 MLPs");
+    if (r->kind == FVC_RENDERER_CACHE_BASIC)
+        return fail(FVC_ERR_CONFIG, "fvc_render_backward: the cached adjoint is built for the performance cache renderer");
     int rc;
     if ((rc = check_info(info))) return rc;
     const long long n_pix = (long long)info->cam_info.resolution.x * info->cam_info.resolution.y;
@@ -1868,7 +1885,7 @@ static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_vi
                        RenderParams &p, int &n_rays, fvc_cache *const *caches = nullptr)
 {
     CHECK_ARG(r && infos && n_views > 0, "fvc_render_batch: bad arguments");
-    const bool cached = r->kind == FVC_RENDERER_CACHE_PERFORMANCE;
+    const bool cached = is_cache_kind(r->kind);
     if (cached != (caches != nullptr))
         return fail(FVC_ERR_CONFIG, "fvc_render_batch: plain renderers take no caches, cache renderers take one per view "
                                     "(fvc_render_batch_cached)");

@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(256) cache_fill_kernel(CacheBuildParams p)
             if (row >= 0) {
                 const float sigma = expf(__half2float(p.build_den[row]));
                 const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * s_dt[i >> 6])));
-                v.density = by_alpha ? alpha : sigma;
+                v.density = p.variant == VARIANT_INTERMEDIATES ? 0.f : by_alpha ? alpha : sigma; /* Intermediates: slot unwritten */
                 v.isset = 1.0f;
                 v.lat = p.build_lat[row];
                 if (lat0) v.lat.x = (v.lat.x & 0xffff0000u) | (uint32_t)__half_as_ushort(__float2half_rn(v.density));
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(128) pr_write_kernel(PerRayFillParams p, int i
                     const int x = id % p.W, y = id / p.W;
                     const int slot = ((packed >> 20) & 1023) * (p.dY * p.dZ) + ((packed >> 10) & 1023) * p.dZ + (packed & 1023);
                     Voxel v;
-                    v.density = by_alpha ? alpha : density;
+                    v.density = p.variant == VARIANT_INTERMEDIATES ? 0.f : by_alpha ? alpha : density;
                     v.isset = 1.0f;
                     v.pad0 = v.pad1 = 0.f;
                     v.lat = p.lat[row];

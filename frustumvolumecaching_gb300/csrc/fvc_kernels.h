@@ -22,6 +22,8 @@ struct CacheView {
     int n_valid_slots;          /* slots written by the last build; others read as zero */
     int interp;                 /* CacheSettings::interpol_function of the render (InterpolFunction) */
     int first_latent_is_density; /* interpol_variant DensityIntermediates: latent 0 holds the density */
+    /* the rest of CacheSettings, read by the basic cache renderer */
+    int variant, reweight, keep_first, inter_brick;
 };
 
 enum : int { INTERP_LINEAR = 0, INTERP_SMOOTHSTEP = 1, INTERP_SMOOTHERSTEP = 2, INTERP_NEAREST = 3 };
@@ -165,6 +167,7 @@ struct RenderParams {
     int *counters;              /* [0], [1] alive rays (ping-pong), [2] rows, [3] resample, [4] cache */
     int row_capacity;           /* rows per sub-iteration */
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
+    int basic_cache;            /* 1: CacheBasicRenderer semantics for the cached rows (classify_basic) */
     /* batched views: rays of n_views cameras (device array), view v's pixel
      * (x, y) at ray id view_off[v] + y * W_v + x; view_off[n_views] = rays;
      * a ray's view is in its state's cnt2.w.  With view_caches, each view

@@ -260,6 +260,131 @@ __device__ __forceinline__ int classify(const RenderParams &p, const CacheView &
     return KIND_CACHE;
 }
 
+/* CacheBasicRenderer's per-sample decision and cache lookup
+ * (sample_cache_kernel, src/cache_basic_renderer.cu:20-210; froxel2data and
+ * fetchBrickTex3DInterpol, include/raymarch_common.h:331-444), all at the
+ * sample's midpoint tm in the cache's froxel grid:
+ *   - outside the frustum or the known range: resample;
+ *   - brick without a slot, or the voxel under the point not set: dropped;
+ *   - else the isset weight, the density slot and the 8 latents are
+ *     interpolated: within the data array when the interpolation is Linear
+ *     and the point lies inside its brick (or inter-brick interpolation is
+ *     off, which clamps the point into the brick), by nearest texel for
+ *     Nearest, otherwise over the 8 froxel corners each fetched through its
+ *     own brick with the interpolation function's weights (unset -> 0, no
+ *     isset weighting);
+ *   - the variant turns the interpolated slot (or latent 0) into density and
+ *     alpha and rewrites latent 0 (log of the density for the
+ *     *Intermediates variants); with reweight_intermediates the latents are
+ *     divided by the interpolated isset, latent 0 first multiplied by it when
+ *     disable_reweighting_first_intermediate is set;
+ *   - a cache sample needs alpha > alpha_thre, else it is dropped.
+ * The texture unit's 8-bit fixed-point weights are not emulated: weights are
+ * full float. */
+__device__ __forceinline__ void basic_corners_array(const CacheView &C, float3 dp, const Voxel *(&vp)[8], float (&w)[8])
+{
+    const float fx = F_SUB(dp.x, 0.5f), fy = F_SUB(dp.y, 0.5f), fz = F_SUB(dp.z, 0.5f);
+    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
+    const float lx = F_SUB(fx, x0), ly = F_SUB(fy, y0), lz = F_SUB(fz, z0);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+        w[c] = (ox ? lx : 1.0f - lx) * (oy ? ly : 1.0f - ly) * (oz ? lz : 1.0f - lz);
+        vp[c] = texel(C, (int)x0 + ox, (int)y0 + oy, (int)z0 + oz);
+    }
+}
+
+__device__ __forceinline__ int classify_basic(const RenderParams &p, const CacheView &C, const DevCam &ccam, const DevSteps &cst,
+                                              float3 oc, float3 dc, float tm, float dt, float (&lat)[8], float &density)
+{
+    float tfr;
+    const float3 fr = cam2froxel(at(oc, dc, tm), ccam, cst, tfr);
+    const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
+    const bool inside = in_fov && fr.z >= 0.f && fr.z < (float)C.fD;
+    bool unsampled = true;
+    if (in_fov) {
+        const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
+        unsampled = tfr < cst.near_ || tfr > kr;
+    }
+    if (!inside || unsampled) return KIND_RESAMPLE;
+    /* froxel2data */
+    const int bx = (int)F_MUL(fr.x, 0.125f), by = (int)F_MUL(fr.y, 0.125f), bz = (int)F_MUL(fr.z, 0.125f);
+    float ix = F_SUB(fr.x, (float)(bx * 8)), iy = F_SUB(fr.y, (float)(by * 8)), iz = F_SUB(fr.z, (float)(bz * 8));
+    bool inside_brick = true;
+    if (C.inter_brick) {
+        inside_brick = ix >= 0.5f && ix < 7.5f && iy >= 0.5f && iy < 7.5f && iz >= 0.5f && iz < 7.5f;
+    } else {
+        ix = fminf(fmaxf(ix, 0.5f), 7.5f);
+        iy = fminf(fmaxf(iy, 0.5f), 7.5f);
+        iz = fminf(fmaxf(iz, 0.5f), 7.5f);
+    }
+    const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
+    if (packed < 0) return KIND_DROP;
+    const float3 dp = make_float3(F_ADD((float)(((packed >> 20) & 1023) * 8), ix), F_ADD((float)(((packed >> 10) & 1023) * 8), iy),
+                                  F_ADD((float)((packed & 1023) * 8), iz));
+    const Voxel *vc = texel(C, (int)floorf(dp.x), (int)floorf(dp.y), (int)floorf(dp.z));
+    if (!vc || !(__ldg(&vc->isset) > 0.0f)) return KIND_DROP;
+    /* fetchBrickTex3DInterpol for isset, the density slot and the latents */
+    const Voxel *vp[8];
+    float wc[8];
+    if (C.interp == INTERP_NEAREST) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) { vp[c] = c == 0 ? vc : nullptr; wc[c] = c == 0 ? 1.0f : 0.0f; }
+    } else if (C.interp == INTERP_LINEAR && inside_brick) {
+        basic_corners_array(C, dp, vp, wc);
+    } else {
+        cache_corners(C, fr, vp, wc);
+    }
+    float weight = 0.f, dac = 0.f, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (!vp[c]) continue;
+        const float w = wc[c];
+        const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
+        const uint4 lt = __ldg(&vp[c]->lat);
+        weight = fmaf(w, di.y, weight);
+        dac = fmaf(w, di.x, dac);
+        const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 fq = __half22float2(*reinterpret_cast<const __half2 *>(&lw[q]));
+            ls[2 * q] = fmaf(w, fq.x, ls[2 * q]);
+            ls[2 * q + 1] = fmaf(w, fq.y, ls[2 * q + 1]);
+        }
+    }
+    float alpha;
+    switch (C.variant) {
+    case VARIANT_ALPHA:
+        alpha = dac;
+        density = -logf(fmaxf(1.0f - alpha, 1e-6f)) / dt;
+        break;
+    case VARIANT_INTERMEDIATES:
+        density = expf(ls[0] / weight);
+        alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-density * dt)));
+        break;
+    case VARIANT_DENSITY_INTERMEDIATES:
+        density = ls[0];
+        alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-density * dt)));
+        ls[0] = logf(density);
+        break;
+    case VARIANT_ALPHA_INTERMEDIATES:
+        alpha = ls[0];
+        density = -logf(fmaxf(1.0f - alpha, 1e-6f)) / dt;
+        ls[0] = logf(density);
+        break;
+    default: /* Density */
+        density = dac;
+        alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-density * dt)));
+        break;
+    }
+    if (C.reweight && C.keep_first) ls[0] *= weight;
+    if (!(alpha > p.scene.alpha_thre)) return KIND_DROP;
+    const float div = C.reweight ? weight : 1.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) lat[j] = ls[j] / div;
+    return KIND_CACHE;
+}
+
 /* Marches every alive ray a fixed number of steps (lanes stay converged),
  * keeping at most S_ROWS occupied samples; the samples become rows
  * (t0, alive slot) that are contiguous and in t order per ray.  The plain
@@ -419,16 +544,30 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
             transform_ray(ccam.w2c, o, d, oc, dc);
             const float dt = calc_step(p.steps, t0);
             const float tm = F_MUL(F_ADD(t0, F_ADD(t0, dt)), 0.5f);
-            kind = classify(p, C, ccam, cst, oc, dc, tm);
-            const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));
-            if (kind == KIND_RESAMPLE) {
-                const float3 pc = contract(p.scene, at(o, d, tmh));
-                p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
-            } else if (kind == KIND_CACHE) {
-                float tf2;
-                const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
-                p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
-                cache_lookup(C, fr, logd, lat);
+            if (p.basic_cache) {
+                /* CacheBasicRenderer: lookup and resample position at the midpoint;
+                 * a cache row keeps its looked-up density for compositing */
+                float density = 0.f;
+                kind = classify_basic(p, C, ccam, cst, oc, dc, tm, dt, lat, density);
+                if (kind == KIND_RESAMPLE) {
+                    const float3 pc = contract(p.scene, at(o, d, tm));
+                    p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
+                } else if (kind == KIND_CACHE) {
+                    p.row_pay[r] = make_float4(0.f, 0.f, 0.f, density);
+                    logd = logf(density);
+                }
+            } else {
+                const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));
+                kind = classify(p, C, ccam, cst, oc, dc, tm);
+                if (kind == KIND_RESAMPLE) {
+                    const float3 pc = contract(p.scene, at(o, d, tmh));
+                    p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
+                } else if (kind == KIND_CACHE) {
+                    float tf2;
+                    const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
+                    p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
+                    cache_lookup(C, fr, logd, lat);
+                }
             }
             p.row_kind[r] = (uint8_t)kind;
         }
@@ -1017,7 +1156,9 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
                 const float lb = __half2float(__ushort_as_half((unsigned short)(ov.y & 0xffffu)));
                 const float ld = __half2float(__ushort_as_half((unsigned short)(ov.y >> 16)));
                 const float dt = calc_step(p.steps, t0);
-                const float sigma = expf(ld);
+                /* the basic cache renderer composites a cache row with its looked-up density
+                 * (accumulate_cache_render_kernel, src/cache_basic_renderer.cu:255-258) */
+                const float sigma = CACHED && p.basic_cache && kind == KIND_CACHE ? p.row_pay[r].w : expf(ld);
                 const float alpha = fminf(1.0f, fmaxf(0.0f, 1.0f - expf(-sigma * dt)));
                 if (alpha > p.scene.alpha_thre) {
                     const float wgt = alpha * acc.w;

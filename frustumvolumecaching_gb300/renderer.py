@@ -23,7 +23,7 @@ import numpy as np
 from . import _lib as L
 from .camera import camera_dict, inverse
 
-RENDERER_BASIC, RENDERER_PERFORMANCE, RENDERER_CACHE_PERFORMANCE = 0, 1, 2
+RENDERER_BASIC, RENDERER_PERFORMANCE, RENDERER_CACHE_PERFORMANCE, RENDERER_CACHE_BASIC = 0, 1, 2, 3
 
 
 class NerfNetwork:
@@ -369,6 +369,14 @@ class CachePerformanceRenderer(Renderer):
         return s
 
 
+class CacheBasicRenderer(CachePerformanceRenderer):
+    """CacheBasicRenderer, include/cache_basic_renderer.h:10-40: the cached
+    render with the basic renderer's per-sample semantics (every CacheSettings
+    field applies; a cache sample composites with its looked-up density)."""
+
+    kind = RENDERER_CACHE_BASIC
+
+
 def change_sampling_rate(stepsize_info: L.StepsizeInfo, factor: float, scene_info: L.SceneInfo) -> L.StepsizeInfo:
     """StepsizeInfo::changeSamplingRate (include/common.h:130-135) on a copy:
     cone angle and step size divided by ``factor``, derived fields refilled
@@ -404,6 +412,6 @@ def eval_cache_settings(loader) -> L.CacheSettings:
 
 
 __all__ = ["load_data", "LoaderData", "NerfNetwork", "Renderer", "BasicRenderer", "PerformanceRenderer", "Cache", "Gradients",
-           "CachePerformanceRenderer", "RenderBuffer", "raymarch_info", "camera_info", "camera_dict",
+           "CachePerformanceRenderer", "CacheBasicRenderer", "RenderBuffer", "raymarch_info", "camera_info", "camera_dict",
            "default_cache_settings", "eval_cache_settings", "change_sampling_rate", "DENSITY", "ALPHA", "INTERMEDIATES", "DENSITY_INTERMEDIATES",
            "ALPHA_INTERMEDIATES", "LINEAR", "SMOOTHSTEP", "SMOOTHERSTEP", "NEAREST"]

@@ -117,8 +117,11 @@ typedef struct {
 } fvc_cache_settings;
 
 /* Renderer kinds: include/basic_renderer.h, performance_renderer.h,
- * cache_performance_renderer.h. BASIC shares the PERFORMANCE kernels. */
-enum { FVC_RENDERER_BASIC = 0, FVC_RENDERER_PERFORMANCE = 1, FVC_RENDERER_CACHE_PERFORMANCE = 2 };
+ * cache_performance_renderer.h, cache_basic_renderer.h. BASIC shares the
+ * PERFORMANCE kernels; CACHE_BASIC the cached ones, with the basic
+ * renderer's per-sample cache semantics (isset decides, every CacheSettings
+ * field applies, cache samples composite with their looked-up density). */
+enum { FVC_RENDERER_BASIC = 0, FVC_RENDERER_PERFORMANCE = 1, FVC_RENDERER_CACHE_PERFORMANCE = 2, FVC_RENDERER_CACHE_BASIC = 3 };
 
 /* Cache render modes: CachePerformanceRenderer::RenderMode
  * (include/cache_performance_renderer.h). */

@@ -740,8 +740,9 @@ struct CacheSettings {
 
 /* CacheRenderer, include/cache_renderer.h:34-109. */
 struct CacheRenderer : public Renderer {
-    CacheRenderer(SceneInfo s, CudaBuffer<uint8_t> &g, NerfNetwork<half> &n, Cache *cache, Cache *next_cache)
-        : Renderer(s, g, n, FVC_RENDERER_CACHE_PERFORMANCE), _cache(cache), _cache_next(next_cache)
+    CacheRenderer(SceneInfo s, CudaBuffer<uint8_t> &g, NerfNetwork<half> &n, Cache *cache, Cache *next_cache,
+                  int kind = FVC_RENDERER_CACHE_PERFORMANCE)
+        : Renderer(s, g, n, kind), _cache(cache), _cache_next(next_cache)
     {
         fvc_cpp::check(fvc_renderer_set_caches(_handle, cache->_handle, next_cache->_handle));
         setCacheSettings(default_cache_settings);
@@ -831,4 +832,63 @@ struct CachePerformanceRenderer : public CacheRenderer {
         uint64_t n_resamples = 0;
         uint64_t n_cache_hits = 0;
     } _render_stats;
+};
+
+/* CacheBasicRenderer, include/cache_basic_renderer.h:10-40: the cached render
+ * with the basic renderer's per-sample semantics (the cache decides by the
+ * voxel's isset; every CacheSettings field applies; a cache sample composites
+ * with its looked-up density). */
+struct CacheBasicRenderer : public CacheRenderer {
+    CacheBasicRenderer(SceneInfo s, CudaBuffer<uint8_t> &g, NerfNetwork<half> &n, Cache *cache, Cache *next_cache)
+        : CacheRenderer(s, g, n, cache, next_cache, FVC_RENDERER_CACHE_BASIC) {}
+
+    void render(RaymarchInfo rm_info, RenderBuffer &b, DebugData * = nullptr) override
+    {
+        const int2 r = b.resolution();
+        if (r.x != rm_info.cam_info.resolution.x || r.y != rm_info.cam_info.resolution.y)
+            throw std::runtime_error("render buffer resolution does not match the camera");
+        if (_counts.size() != (size_t)r.x * r.y) _counts.resize((size_t)r.x * r.y);
+        fvc_render_outputs out{};
+        out.image_rgba8 = reinterpret_cast<uint8_t *>(b.image_device());
+        out.results = reinterpret_cast<fvc_ray_result *>(b.results_device());
+        out.ray_counts = reinterpret_cast<int32_t *>(_counts.data());
+        fvc_cpp::check(fvc_render_device(_handle, fvc_cpp::abi(rm_info), &out));
+        fvc_cpp::check(fvc_renderer_synchronize(_handle));
+        fvc_render_stats_t st{};
+        fvc_cpp::check(fvc_render_stats(_handle, &st));
+        _render_stats.total_n_evaluated_samples_resample = (int)st.n_resamples;
+        _render_stats.total_n_evaluated_samples_cache = (int)st.n_cache_hits;
+    }
+    void resizeRenderbuffers(int2 r) override { fvc_cpp::check(fvc_renderer_resize(_handle, r.x, r.y)); }
+
+    /* writeImageBuffer_cacheBasic_postRender_kernel (src/cache_basic_renderer.cu:
+     * 308-330): white where a cache sample contributed, and the contributing
+     * sample totals, from the last render's per-pixel counts */
+    void postRender(RaymarchInfo rm_info, RenderBuffer &additional_image_buffer)
+    {
+        const size_t n = (size_t)rm_info.cam_info.resolution.x * rm_info.cam_info.resolution.y;
+        if (_counts.size() != n) throw std::runtime_error("postRender: no render at this resolution");
+        std::vector<int4> counts;
+        _counts.download(counts);
+        std::vector<uchar4> img(n);
+        long long res = 0, cache = 0;
+        for (size_t i = 0; i < n; ++i) {
+            res += counts[i].x;
+            cache += counts[i].y;
+            const unsigned char v = counts[i].y > 0 ? 255 : 0;
+            img[i] = make_uchar4(v, v, v, 255);
+        }
+        fvc_cpp::check_cuda(cudaMemcpy(additional_image_buffer.image_device(), img.data(), n * sizeof(uchar4), cudaMemcpyHostToDevice),
+                            "postRender image");
+        _render_stats.total_n_contributing_samples_resample = (int)res;
+        _render_stats.total_n_contributing_samples_cache = (int)cache;
+    }
+
+    struct RenderStats {
+        int total_n_evaluated_samples_resample = 0;
+        int total_n_contributing_samples_resample = 0;
+        int total_n_evaluated_samples_cache = 0;
+        int total_n_contributing_samples_cache = 0;
+    } _render_stats;
+    CudaBuffer<int4> _counts; /* per pixel: resample, cache, dropped samples, steps */
 };

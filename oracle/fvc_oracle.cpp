@@ -569,6 +569,9 @@ struct OrcCache {
      * what a build stores and how a lookup forms the head input;
      * interpol_function the trilinear weights of a lookup */
     int variant, interp;
+    /* the basic cache renderer's semantics (CacheBasicRenderer) and the
+     * CacheSettings flags only it reads */
+    int basic, reweight, keep_first, inter_brick;
 };
 
 /* applyInterpolationFunction, include/raymarch_common.h:393-402, with the
@@ -714,7 +717,7 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
                                 const double sig = w.sig[k * 8 + s];
                                 const bool by_alpha = cc->variant == 1 || cc->variant == 4;
                                 const double val = by_alpha ? w.alpha[k * 8 + s] : sig;
-                                cc->vox_density[v] = (float)val;
+                                cc->vox_density[v] = cc->variant == 2 ? 0.0f : (float)val; /* Intermediates: slot unwritten */
                                 cc->vox_isset[v] = 1.0f;
                                 for (int j = 0; j < 8; ++j) cc->vox_latents[v * 8 + j] = d2h_bits(w.lat[(k * 8 + s) * 8 + j]);
                                 if (cc->variant == 3 || cc->variant == 4) cc->vox_latents[v * 8] = d2h_bits(val);
@@ -873,7 +876,7 @@ int orc_cache_build_per_ray(const OrcNet *net, const OrcScene *sc, const OrcStep
                     const size_t v = (size_t)slot * 512 + (size_t)(bin & 7) * 64 + (y & 7) * 8 + (x & 7);
                     const bool by_alpha = cc->variant == 1 || cc->variant == 4;
                     const double val = by_alpha ? alpha : density;
-                    cc->vox_density[v] = (float)val;
+                    cc->vox_density[v] = cc->variant == 2 ? 0.0f : (float)val;
                     cc->vox_isset[v] = 1.0f;
                     for (int j = 0; j < 8; ++j) cc->vox_latents[v * 8 + j] = d2h_bits(e.lat[j]);
                     if (cc->variant == 3 || cc->variant == 4) cc->vox_latents[v * 8] = d2h_bits(val);
@@ -911,6 +914,81 @@ inline int brick_lookup(const OrcCache &cc, int bx, int by, int bz)
 {
     const OrcCacheDims &cd = cc.dims;
     return cc.packed_index[((size_t)bz * cd.bY + by) * cd.bX + bx];
+}
+
+/* CacheBasicRenderer's cache decision and lookup at froxel point fp
+ * (sample_cache_kernel, src/cache_basic_renderer.cu:95-210; froxel2data and
+ * fetchBrickTex3DInterpol, include/raymarch_common.h:331-444): 0 resample,
+ * 1 cache (lat = head inputs, sigma = density), 2 dropped.  Texture weights
+ * in full precision (the texture unit's 8-bit weights are not emulated). */
+int basic_sample(const OrcCache &cc, const OrcScene *sc, V3 fp, float dt, double *lat, double &sigma)
+{
+    const OrcCacheDims &cd = cc.dims;
+    const int bx = (int)(fp.x / 8.0f), by = (int)(fp.y / 8.0f), bz = (int)(fp.z / 8.0f);
+    float ix = fp.x - (float)(bx * 8), iy = fp.y - (float)(by * 8), iz = fp.z - (float)(bz * 8);
+    bool inside_brick = true;
+    if (cc.inter_brick) {
+        inside_brick = ix >= 0.5f && ix < 7.5f && iy >= 0.5f && iy < 7.5f && iz >= 0.5f && iz < 7.5f;
+    } else {
+        ix = std::min(std::max(ix, 0.5f), 7.5f);
+        iy = std::min(std::max(iy, 0.5f), 7.5f);
+        iz = std::min(std::max(iz, 0.5f), 7.5f);
+    }
+    const int packed = brick_lookup(cc, bx, by, bz);
+    if (packed < 0) return 2;
+    const float dx = (float)(((packed >> 20) & 1023) * 8) + ix, dy = (float)(((packed >> 10) & 1023) * 8) + iy,
+                dz = (float)((packed & 1023) * 8) + iz;
+    Vox v0;
+    if (!fetch_texel(cc, (int)floorf(dx), (int)floorf(dy), (int)floorf(dz), v0) || !(v0.isset > 0.0)) return 2;
+    double weight = 0, dac = 0, ls[8] = {0};
+    auto add = [&](const Vox &v, double w) {
+        weight += w * v.isset; dac += w * v.density;
+        for (int j = 0; j < 8; ++j) ls[j] += w * v.lat[j];
+    };
+    if (cc.interp == 3) {
+        add(v0, 1.0);
+    } else if (cc.interp == 0 && inside_brick) { /* tex3D linear inside the data array */
+        const float ax = dx - 0.5f, ay = dy - 0.5f, az = dz - 0.5f;
+        const float x0 = floorf(ax), y0 = floorf(ay), z0 = floorf(az);
+        const double l[3] = {(double)(ax - x0), (double)(ay - y0), (double)(az - z0)};
+        for (int c = 0; c < 8; ++c) {
+            const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+            const double w = (ox ? l[0] : 1.0 - l[0]) * (oy ? l[1] : 1.0 - l[1]) * (oz ? l[2] : 1.0 - l[2]);
+            Vox v;
+            if (fetch_texel(cc, (int)x0 + ox, (int)y0 + oy, (int)z0 + oz, v)) add(v, w);
+        }
+    } else { /* 8 froxel corners, each through its own brick */
+        const float fx0 = floorf(fp.x - 0.5f), fy0 = floorf(fp.y - 0.5f), fz0 = floorf(fp.z - 0.5f);
+        const double l[3] = {(double)interp_fn(fp.x - 0.5f - fx0, cc.interp), (double)interp_fn(fp.y - 0.5f - fy0, cc.interp),
+                             (double)interp_fn(fp.z - 0.5f - fz0, cc.interp)};
+        for (int c = 0; c < 8; ++c) {
+            const int ox = (c >> 2) & 1, oy = (c >> 1) & 1, oz = c & 1;
+            const double w = (ox ? l[0] : 1.0 - l[0]) * (oy ? l[1] : 1.0 - l[1]) * (oz ? l[2] : 1.0 - l[2]);
+            const float cx = fx0 + (float)ox, cy = fy0 + (float)oy, cz = fz0 + (float)oz;
+            if (!(cx >= 0 && cx < (float)cd.fW && cy >= 0 && cy < (float)cd.fH && cz >= 0 && cz < (float)cd.fD)) continue;
+            const int cbx = (int)(cx / 8.0f), cby = (int)(cy / 8.0f), cbz = (int)(cz / 8.0f);
+            const int pk = brick_lookup(cc, cbx, cby, cbz);
+            if (pk < 0) continue;
+            Vox v;
+            if (fetch_texel(cc, ((pk >> 20) & 1023) * 8 + ((int)cx - cbx * 8), ((pk >> 10) & 1023) * 8 + ((int)cy - cby * 8),
+                            (pk & 1023) * 8 + ((int)cz - cbz * 8), v))
+                add(v, w);
+        }
+    }
+    double alpha, density;
+    switch (cc.variant) {
+    case 1: alpha = dac; density = -std::log(std::max(1.0 - alpha, 1e-6)) / dt; break;
+    case 2: density = std::exp(ls[0] / weight); alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-density * dt))); break;
+    case 3: density = ls[0]; alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-density * dt))); ls[0] = std::log(density); break;
+    case 4: alpha = ls[0]; density = -std::log(std::max(1.0 - alpha, 1e-6)) / dt; ls[0] = std::log(density); break;
+    default: density = dac; alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-density * dt))); break;
+    }
+    if (cc.reweight && cc.keep_first) ls[0] *= weight;
+    if (!(alpha > (double)sc->alpha_thre)) return 2;
+    const double div = cc.reweight ? weight : 1.0;
+    for (int j = 0; j < 8; ++j) lat[j] = ls[j] / div;
+    sigma = density;
+    return 1;
 }
 
 /* Cached render: CachePerformanceRenderer::render and its kernels
@@ -957,7 +1035,12 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         unsampled = tfr < cst->near_ || tfr > kr;
                     }
                     int kind = 0; /* 0 resample, 1 cache, 2 drop */
-                    if (!inside || unsampled) {
+                    double blat[8], bsigma = 0.0;
+                    if (cc->basic) {
+                        /* CacheBasicRenderer: decided and looked up at the midpoint */
+                        kind = (!inside || unsampled) ? 0 : basic_sample(*cc, sc, fp, dt, blat, bsigma);
+                        if (kind == 2) { ++n_drop; continue; }
+                    } else if (!inside || unsampled) {
                         if (mode == 1) continue;
                         kind = 0;
                     } else {
@@ -975,9 +1058,13 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         }
                         if (kind == 2) { ++n_drop; continue; }
                     }
-                    const float tmh = t0 + dt * 0.5f;  /* generateNetworkInput_* :234, :287 */
+                    const float tmh = cc->basic ? tm : t0 + dt * 0.5f;  /* generateNetworkInput_* :234, :287 */
                     double sigma, lg[3];
-                    if (kind == 0) {
+                    if (kind == 1 && cc->basic) {
+                        head_forward(d, blat, d01, lg);
+                        sigma = bsigma;
+                        ++n_cache;
+                    } else if (kind == 0) {
                         double bo[64];
                         base_forward(d, contract(*sc, at(r, tmh)), bo);
                         head_forward(d, bo + net->latent_offset, d01, lg);

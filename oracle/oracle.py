@@ -52,7 +52,8 @@ class OrcCache(C.Structure):
     _fields_ = [("dims", OrcCacheDims), ("packed_index", C.c_void_p), ("known_ranges", C.c_void_p),
                 ("vox_density", C.c_void_p), ("vox_isset", C.c_void_p), ("vox_latents", C.c_void_p),
                 ("n_bricks_set", C.c_int), ("n_demanded", C.c_int), ("n_iterations", C.c_int),
-                ("n_samples", C.c_longlong), ("slot_of_brick_order", C.c_void_p), ("variant", C.c_int), ("interp", C.c_int)]
+                ("n_samples", C.c_longlong), ("slot_of_brick_order", C.c_void_p), ("variant", C.c_int), ("interp", C.c_int),
+                ("basic", C.c_int), ("reweight", C.c_int), ("keep_first", C.c_int), ("inter_brick", C.c_int)]
 
 
 def build(force: bool = False) -> str:
@@ -328,6 +329,7 @@ class OracleCache:
         self.cam = cam
         self.dims = dims
         self.steps = None  # the StepsizeInfo the cache was built with (None: the model's)
+        self.settings = None  # set below, once the ctypes struct exists
         nb = dims.bX * dims.bY * dims.bZ
         slots = dims.dX * dims.dY * dims.dZ
         self.packed_index = np.full(nb, -1, np.int32)
@@ -340,7 +342,15 @@ class OracleCache:
         s.packed_index, s.known_ranges = ptr(self.packed_index), ptr(self.known_ranges)
         s.vox_density, s.vox_isset, s.vox_latents = ptr(self.vox_density), ptr(self.vox_isset), ptr(self.vox_latents)
         s.slot_of_brick_order = None
+        s.reweight = s.keep_first = s.inter_brick = 1  # CacheRenderer::default_cache_settings
         self.s = s
+
+    def render_as_basic(self, variant: int = 0, interp: int = 0, reweight: bool = True, keep_first: bool = True,
+                        inter_brick: bool = True) -> "OracleCache":
+        """Look up with CacheBasicRenderer's semantics and these settings."""
+        self.s.basic, self.s.variant, self.s.interp = 1, variant, interp
+        self.s.reweight, self.s.keep_first, self.s.inter_brick = int(reweight), int(keep_first), int(inter_brick)
+        return self
 
     def load_device_cache(self, packed: np.ndarray, known: np.ndarray, voxels: np.ndarray) -> None:
         """Use a device-built cache (fvc_cache_read: packed index, known ranges,

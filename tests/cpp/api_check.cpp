@@ -73,6 +73,8 @@ int main(int argc, char **argv)
     CHECK(half.stepsize == st.stepsize / 2.0f && half.dt_min == half.stepsize && half.i_max > st.i_max);
     void (CacheRenderer::*fill)(RaymarchInfo, RenderBuffer &) = &CacheRenderer::initCache;
     CHECK(fill != nullptr);
+    void (CacheBasicRenderer::*post)(RaymarchInfo, RenderBuffer &) = &CacheBasicRenderer::postRender;
+    CHECK(post != nullptr);
 
     std::vector<uint8_t> px(7 * 5 * 4);
     for (size_t i = 0; i < px.size(); ++i) px[i] = (uint8_t)(i * 37);
