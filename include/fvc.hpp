@@ -7,7 +7,8 @@
  * (include/common.h:22-218), the same loader entry points (include/loader.h:
  * 32-51), the same renderer classes and members (include/renderer.h:77-119,
  * basic_renderer.h, performance_renderer.h:19-64, cache_renderer.h:34-109,
- * cache_performance_renderer.h:21-131) and the same error behaviour
+ * cache_performance_renderer.h:21-131, cache_basic_renderer.h:10-40) and the
+ * same error behaviour
  * (std::runtime_error; loaders return false).  Renders are synchronous like
  * the reference's.
  *
@@ -15,7 +16,8 @@
  *  - NerfNetwork is a handle to the model inside libfvc.so (no tcnn objects);
  *  - RenderBuffer is a headless device buffer (uchar4 image + float4 rgb/T)
  *    instead of a CUDA surface, and writeToFile writes PNG only;
- *  - CacheRenderer::initCache (the per-ray fill) is not built and throws;
+ *  - cache brick slots are assigned in a fixed order (the reference uses
+ *    atomicAdd), so builds are reproducible;
  *  - DebugData contribution buffers are accepted and left untouched;
  *  - Renderer::_timer records whole-render wall time and the event-timed
  *    resample network kernel, not the reference's nine phases.
