@@ -824,10 +824,14 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
     const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : p.counters[4];
     if (n_rows == 0) return;
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int i = tid; i < TC_WBYTES / 16; i += 128)
-        reinterpret_cast<uint4 *>(S.W)[i] = __ldg(reinterpret_cast<const uint4 *>(p.weights_tc) + i);
+    /* the weights arrive by one bulk copy on the TMA engine, completing the
+     * mbarrier's phase 0; the layers' MMA commits complete the later phases */
+    if (tid == 0) {
+        mbar_init(&S.mbar, 1);
+        mbar_arrive_expect_tx(&S.mbar, TC_WBYTES);
+        bulk_copy_g2s(S.W, p.weights_tc, TC_WBYTES, &S.mbar);
+    }
     if (tid < 64) S.bias3[tid] = p.bias3[tid];
-    if (tid == 0) mbar_init(&S.mbar, 1);
     if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
     tc_fence_before();
     __syncthreads();
@@ -836,7 +840,8 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     const RayState *states = p.states[it & 1];
     uint32_t phase = 0;
-    bool ok = true;
+    bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
     const int n_tiles = (n_rows + 127) / 128;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const int k = tile * 128 + tid;
@@ -1018,10 +1023,12 @@ __global__ void __launch_bounds__(128, TC_PREC_CTAS_PER_SM) wf_net_tc_prec_kerne
     const int tid = threadIdx.x, warp = tid >> 5;
     const uint8_t *wsrc = PREC == 1 ? p.weights_tc_bf16 : p.weights_tc_fp8;
     const int wbytes = PREC == 1 ? TC_WBYTES : TC8_WBYTES;
-    for (int i = tid; i < wbytes / 16; i += 128)
-        reinterpret_cast<uint4 *>(S.W)[i] = __ldg(reinterpret_cast<const uint4 *>(wsrc) + i);
+    if (tid == 0) { /* the weights by one bulk copy, completing phase 0 (as wf_net_tc_kernel) */
+        mbar_init(&S.mbar, 1);
+        mbar_arrive_expect_tx(&S.mbar, (uint32_t)wbytes);
+        bulk_copy_g2s(S.W, wsrc, (uint32_t)wbytes, &S.mbar);
+    }
     if (tid < 64) S.bias3[tid] = p.bias3[tid];
-    if (tid == 0) mbar_init(&S.mbar, 1);
     if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
     tc_fence_before();
     __syncthreads();
@@ -1036,7 +1043,8 @@ __global__ void __launch_bounds__(128, TC_PREC_CTAS_PER_SM) wf_net_tc_prec_kerne
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
     const RayState *states = p.states[it & 1];
     uint32_t phase = 0;
-    bool ok = true;
+    bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
     const int n_tiles = (n_rows + 127) / 128;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const int r = tile * 128 + tid < n_rows ? tile * 128 + tid : -1;

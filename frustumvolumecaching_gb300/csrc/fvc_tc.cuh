@@ -128,6 +128,23 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
+/* the calling thread's arrival on mbar, announcing `bytes` of asynchronous
+ * copies that complete the phase */
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+
+/* one bulk copy on the TMA engine from global memory into this CTA's shared
+ * memory, completing `bytes` of mbar's transaction count; both addresses
+ * 16-byte aligned and bytes a multiple of 16 */
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+                 : "memory");
+}
+
 /* wait for the given phase parity with a deadline of `limit_cycles` SM
  * clocks; try_wait suspends the thread for at most ~20 us per attempt instead
  * of spinning on the issue slots.  false when the deadline passed. */
