@@ -8,7 +8,11 @@
  * white-background pixel (C + T, writeImageBuffer_performance_kernel,
  * src/performance_renderer.cu:127-149).
  *
- * Network backward, one warp per 32 rows (mma.sync m16n8k16, fp16 or bf16
+ * Two forms of the network backward.  wf_net_bwd_tc_kernel (the default) runs
+ * it on the tcgen05 tensor cores, 128 rows per CTA, with the weight gradients
+ * accumulated in TMEM (its comment block below has the layout).
+ * wf_net_bwd_kernel (the mma.sync network path) takes one warp per 32 rows
+ * (mma.sync m16n8k16, fp16 or bf16
  * operands like the forward MLP, fp32 accumulation): the forward activations of the rows (hash features,
  * density hidden layer, head input [latents | SH | 1-padding], head hidden
  * layers) are recomputed into shared memory; the gradient tile then walks
@@ -397,6 +401,466 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
     flush(dWh + b.head_w5, b.g_head + b.head_w5, 16 * 64, 64);
 }
 
+/* ------------------------------------------------------------------------- */
+/* network adjoint on the 5th-generation tensor cores                        */
+/* ------------------------------------------------------------------------- */
+/* One CTA of 128 threads per 128-row tile (thread t owns row t and TMEM lane
+ * t), two CTAs per SM.  Each activation and gradient of the tile sits in its
+ * own canonical K-major shared tile (8-row x 16-byte core matrices, see
+ * fvc_tc.cuh), so that it serves two MMAs:
+ *   - as the K-major A operand of the next layer (forward: X W^T; input
+ *     gradient: G W, with W^T tiles as B);
+ *   - as an MN-major operand of the weight-gradient MMA dW = G^T X, whose
+ *     contraction runs over the tile's 128 rows.  Read MN-major, a tile of C
+ *     columns has its 8-column groups SBO = 128 bytes apart and its 8-row
+ *     groups LBO = C / 8 * 128 bytes apart.
+ * The weight gradients accumulate in TMEM over every tile the CTA takes and
+ * are added to the global blobs once per launch; no shared-memory atomics.
+ * The weight-gradient MMAs use M = 128 with their 64 meaningful rows in TMEM
+ * lanes 0..63: a 64-column tile read MN-major with M = 128 runs up to 1023
+ * bytes past its end, which stays inside the next tile or the pad.
+ * Gradient tiles reuse the activation tile whose mask they need, in place,
+ * once the MMAs that read that tile have completed.
+ * TMEM columns: 0..63 layer accumulator; 64..127 dW4; 128..159 dW3;
+ * 160..191 dW1; 192..207 dW5^T; 208..223 dW2^T. */
+constexpr int BT_COLS = 256;
+constexpr int BT_D0 = 0, BT_DW4 = 64, BT_DW3 = 128, BT_DW1 = 160, BT_DW5T = 192, BT_DW2T = 208;
+constexpr long long BT_WAIT_LIMIT = 2000000000ll; /* ~1 s of SM clocks */
+
+struct __align__(128) BtSmem {
+    uint8_t W[TB_BYTES];
+    uint8_t F[128 * 32 * 2];   /* hash features */
+    uint8_t IN[128 * 32 * 2];  /* head input [latents | SH | 1.0] */
+    uint8_t G16[128 * 16 * 2]; /* output-layer gradient, later the density-network output gradient */
+    uint8_t H1[128 * 64 * 2];  /* density hidden layer, later its gradient */
+    uint8_t A3[128 * 64 * 2];  /* head hidden 1, later its gradient */
+    uint8_t A4[128 * 64 * 2];  /* head hidden 2, later its gradient */
+    uint8_t pad[1024];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+static_assert(2 * (sizeof(BtSmem) + 1024) <= 228 * 1024, "two CTAs per SM");
+static_assert(2 * BT_COLS <= 512, "two CTAs per SM in TMEM");
+
+__device__ __forceinline__ void bt_st(uint8_t *tile, int row, int c, int K, uint4 v)
+{
+    *reinterpret_cast<uint4 *>(tile + kmajor_offset(row, 8 * c, K)) = v;
+}
+__device__ __forceinline__ uint4 bt_ld(const uint8_t *tile, int row, int c, int K)
+{
+    return *reinterpret_cast<const uint4 *>(tile + kmajor_offset(row, 8 * c, K));
+}
+
+/* D = A (128 x K, K-major tile) * B^T (N x K, K-major tile) */
+__device__ __forceinline__ void bt_mma_k(uint32_t d, const uint8_t *a, const uint8_t *b, int K, int N, bool bf16)
+{
+    const uint32_t sbo = (uint32_t)(K / 8) * 128u, id = idesc_f16(128, N, bf16);
+    const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
+    for (int kc = 0; kc < K / 16; ++kc)
+        tc_mma_f16(d, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
+}
+
+/* D (+)= A^T B over the 128 tile rows: A a tile of ca columns (M = 128 read
+ * from it), B a tile of N columns, both MN-major */
+__device__ __forceinline__ void bt_mma_mn(uint32_t d, const uint8_t *a, int ca, const uint8_t *b, int N, bool bf16, bool acc)
+{
+    const uint32_t id = idesc_f16(128, N, bf16) | (1u << 15) | (1u << 16);
+    const uint32_t la = (uint32_t)(ca / 8) * 128u, lb = (uint32_t)(N / 8) * 128u;
+    const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
+    for (int s = 0; s < 8; ++s)
+        tc_mma_f16(d, umma_desc(a0 + 2u * la * s, la, 128u), umma_desc(b0 + 2u * lb * s, lb, 128u), id, (acc || s > 0) ? 1u : 0u);
+}
+
+/* the MMAs issued by thread 0 are committed; every thread waits (bounded) */
+__device__ __forceinline__ bool bt_wait(BtSmem &S, uint32_t &phase)
+{
+    const bool ok = mbar_wait(&S.mbar, phase, BT_WAIT_LIMIT);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+/* rewritten rows visible to the tensor core, TMEM reads ordered before the next MMA */
+__device__ __forceinline__ bool bt_publish(bool ok)
+{
+    fence_proxy_async();
+    tc_fence_before();
+    return __syncthreads_or(!ok) == 0;
+}
+
+/* 64 accumulator columns -> ReLU -> 16-bit row of a 64-column tile */
+template <int PREC>
+__device__ __forceinline__ void bt_epi_act(uint32_t taddr, uint8_t *dst, int row)
+{
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float v[32];
+        tmem_ld32(taddr + 32 * h, v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int c = 8 * q + 2 * i;
+                w[i] = E16<PREC>::pack(clamp_h(fmaxf(v[c], 0.f)), clamp_h(fmaxf(v[c + 1], 0.f)));
+            }
+            bt_st(dst, row, 4 * h + q, 64, make_uint4(w[0], w[1], w[2], w[3]));
+        }
+    }
+}
+
+/* 64 accumulator columns, zeroed where the activation row is not > 0, written
+ * over that activation row (64-column tile) */
+template <int PREC>
+__device__ __forceinline__ void bt_epi_grad(uint32_t taddr, uint8_t *tile, int row)
+{
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float v[32];
+        tmem_ld32(taddr + 32 * h, v);
+        uint4 mk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) mk[q] = bt_ld(tile, row, 4 * h + q, 64);
+        tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t m4[4] = {mk[q].x, mk[q].y, mk[q].z, mk[q].w};
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int c = 8 * q + 2 * i;
+                const float2 m = E16<PREC>::unpack(m4[i]);
+                const float a = m.x > 0.f ? v[c] : 0.f, b = m.y > 0.f ? v[c + 1] : 0.f;
+                w[i] = E16<PREC>::pack(clamp_h(a), clamp_h(b));
+            }
+            bt_st(tile, row, 4 * h + q, 64, make_uint4(w[0], w[1], w[2], w[3]));
+        }
+    }
+}
+
+__device__ __forceinline__ void red_add4(float *a, float x, float y, float z, float w)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(w) : "memory");
+}
+
+/* levels at which consecutive samples of a ray usually share a cell (cells
+ * wider than about one step) */
+constexpr int SC_PAIR_LEVELS = 10;
+
+/* Adjoint of hash_encode for the 16-level grid, called by all 32 lanes of a
+ * warp (rows without a gradient pass zeros).  Per level:
+ *   - lanes 2j and 2j+1 in the same cell at a coarse level merge: the odd
+ *     lane hands its trilinear weights and feature gradient to the even lane,
+ *     which adds both rows' contributions to the 8 corners;
+ *   - x-neighbour corners whose table entries form an aligned pair
+ *     {2i, 2i+1} (a hashed level's cell with even x, or adjacent dense
+ *     indices) go out as one 16-byte red.global.add.v4.f32.
+ * The table receives the same sums with fewer L2 atomics. */
+__device__ __forceinline__ void hash_scatter16(const DevGrid &g, float *gt, float3 pos, const float (&dF)[32], int lane)
+{
+#pragma unroll
+    for (int l = 0; l < 16; ++l) {
+        float ax = dF[2 * l], ay = dF[2 * l + 1];
+        const float sc = g.scale[l];
+        const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
+        const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+        const uint32_t gx = (uint32_t)(int)fx, gy = (uint32_t)(int)fy, gz = (uint32_t)(int)fz;
+        const float wx = __fsub_rn(px, fx), wy = __fsub_rn(py, fy), wz = __fsub_rn(pz, fz);
+        float nwx = 0.f, nwy = 0.f, nwz = 0.f, nax = 0.f, nay = 0.f;
+        bool take = false;
+        if (l < SC_PAIR_LEVELS && sc < 60000.f) { /* cell coordinates below 2^16 */
+            const uint32_t kxy = gx | (gy << 16);
+            const uint32_t okxy = __shfl_xor_sync(FULLMASK, kxy, 1), okz = __shfl_xor_sync(FULLMASK, gz, 1);
+            nwx = __shfl_xor_sync(FULLMASK, wx, 1);
+            nwy = __shfl_xor_sync(FULLMASK, wy, 1);
+            nwz = __shfl_xor_sync(FULLMASK, wz, 1);
+            nax = __shfl_xor_sync(FULLMASK, ax, 1);
+            nay = __shfl_xor_sync(FULLMASK, ay, 1);
+            if (okxy == kxy && okz == gz) {
+                if (lane & 1) ax = ay = 0.f;
+                else take = nax != 0.f || nay != 0.f;
+            }
+        }
+        if (ax == 0.f && ay == 0.f && !take) continue;
+        const uint32_t size = g.size[l];
+        float *tl = gt + 2 * (size_t)g.offset[l];
+        const bool dense = (g.dense_mask >> l) & 1u;
+        const bool even_off = (g.offset[l] & 1u) == 0u;
+#pragma unroll
+        for (int cp = 0; cp < 4; ++cp) {
+            const uint32_t cy = gy + (cp & 1), cz = gz + (cp >> 1);
+            uint32_t i0, i1;
+            if (dense) {
+                i0 = gx + cy * g.res[l] + cz * g.res2[l];
+                if (i0 >= size) i0 -= size;
+                i1 = i0 + 1u;
+                if (i1 >= size) i1 -= size;
+            } else {
+                const uint32_t h = (cy * 2654435761u) ^ (cz * 805459861u);
+                i0 = (gx ^ h) & (size - 1u);
+                i1 = ((gx + 1u) ^ h) & (size - 1u);
+            }
+            const float wyz = ((cp & 1) ? wy : 1.0f - wy), wzz = ((cp & 2) ? wz : 1.0f - wz);
+            const float w0 = ((1.0f - wx) * wyz) * wzz, w1 = (wx * wyz) * wzz;
+            float v0x = w0 * ax, v0y = w0 * ay, v1x = w1 * ax, v1y = w1 * ay;
+            if (take) {
+                const float nyz = ((cp & 1) ? nwy : 1.0f - nwy), nzz = ((cp & 2) ? nwz : 1.0f - nwz);
+                const float n0 = ((1.0f - nwx) * nyz) * nzz, n1 = (nwx * nyz) * nzz;
+                v0x = fmaf(n0, nax, v0x); v0y = fmaf(n0, nay, v0y);
+                v1x = fmaf(n1, nax, v1x); v1y = fmaf(n1, nay, v1y);
+            }
+            if ((i0 ^ i1) == 1u && even_off) {
+                if (i0 & 1u) red_add4(tl + 2 * (size_t)i1, v1x, v1y, v0x, v0y);
+                else red_add4(tl + 2 * (size_t)i0, v0x, v0y, v1x, v1y);
+            } else {
+                red_add2(tl + 2 * (size_t)i0, v0x, v0y);
+                red_add2(tl + 2 * (size_t)i1, v1x, v1y);
+            }
+        }
+    }
+}
+
+template <int PREC, int HH>
+__global__ void __launch_bounds__(128, 2) wf_net_bwd_tc_kernel(RenderParams p, BwdParams b, int it)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    BtSmem &S = *reinterpret_cast<BtSmem *>(smem_raw);
+    const int n_rows = p.counters[6];
+    if (n_rows == 0) return;
+    using T16 = E16<PREC>;
+    constexpr bool BF = PREC == 1;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&S.mbar, 1);
+        mbar_arrive_expect_tx(&S.mbar, TB_BYTES);
+        bulk_copy_g2s(S.W, b.wtc, TB_BYTES, &S.mbar);
+    }
+    for (int i = tid; i < 1024 / 16; i += 128) reinterpret_cast<uint4 *>(S.pad)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) tmem_alloc(&S.tmem_base, BT_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t lrow = tmem + ((uint32_t)(warp * 32) << 16);
+    const RayState *states = p.states[it & 1];
+    const int lo = p.latent_offset;
+    uint32_t phase = 0;
+    bool ok = mbar_wait(&S.mbar, phase, BT_WAIT_LIMIT);
+    phase ^= 1u;
+    tc_fence_after();
+    uint8_t *last = HH == 2 ? S.A4 : S.A3;
+    bool acc = false; /* dW accumulators hold this launch's sums */
+    const int n_tiles = (n_rows + 127) / 128;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int k = tile * 128 + tid;
+        const int r = k < n_rows ? p.grad_res_list[k] : -1;
+        float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 pos = make_float3(0.f, 0.f, 0.f);
+        __half2 feat[16], sh[8];
+        if (r >= 0) {
+            dout = p.row_dout[r];
+            const float4 pw = p.row_pay[r];
+            pos = make_float3(pw.x, pw.y, pw.z);
+            sh16(row_dir01(states, p.row_slot[r]), sh);
+            hash_encode<4>(p.grid, p.table, pos, feat);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+        }
+        /* ---- F, head input (SH, 1-padding) and the output-layer gradient ---- */
+        {
+            uint32_t f[16], s[8];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const float2 v = __half22float2(feat[q]);
+                f[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&feat[q]) : T16::pack(v.x, v.y);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float2 v = __half22float2(sh[q]);
+                s[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&sh[q]) : T16::pack(v.x, v.y);
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bt_st(S.F, tid, c, 32, make_uint4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]));
+            bt_st(S.IN, tid, 1, 32, make_uint4(s[0], s[1], s[2], s[3]));
+            bt_st(S.IN, tid, 2, 32, make_uint4(s[4], s[5], s[6], s[7]));
+            const uint32_t one2 = T16::pack(1.0f, 1.0f);
+            bt_st(S.IN, tid, 3, 32, make_uint4(one2, one2, one2, one2));
+            bt_st(S.G16, tid, 0, 16, make_uint4(T16::pack(clamp_h(dout.x), clamp_h(dout.y)), T16::pack(clamp_h(dout.z), 0.f), 0u, 0u));
+            bt_st(S.G16, tid, 1, 16, make_uint4(0u, 0u, 0u, 0u));
+        }
+        if (!(ok = bt_publish(ok))) break;
+        /* ---- density layer 1: F W1^T -> H1 ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.F, S.W + TB_W1, 32, 64, BF);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        bt_epi_act<PREC>(lrow + BT_D0, S.H1, tid);
+        if (!(ok = bt_publish(ok))) break;
+        /* ---- density layer 2: H1 W2^T -> latents of the head input ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.H1, S.W + TB_W2, 64, 16, BF);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        {
+            float v[16];
+            tmem_ld16(lrow + BT_D0, v);
+            tmem_wait_ld();
+            uint32_t w[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) /* latent_offset is 0 or 1 */
+                w[i] = T16::pack(clamp_h(lo ? v[2 * i + 1] : v[2 * i]), clamp_h(lo ? v[2 * i + 2] : v[2 * i + 1]));
+            bt_st(S.IN, tid, 0, 32, make_uint4(w[0], w[1], w[2], w[3]));
+        }
+        if (!(ok = bt_publish(ok))) break;
+        /* ---- head layer 1 (bias from the 1-padding) -> A3 ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.IN, S.W + TB_W3, 32, 64, BF);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        bt_epi_act<PREC>(lrow + BT_D0, S.A3, tid);
+        if (!(ok = bt_publish(ok))) break;
+        if (HH == 2) {
+            /* ---- head layer 2 -> A4 ---- */
+            if (tid == 0) {
+                tc_fence_after();
+                bt_mma_k(tmem + BT_D0, S.A3, S.W + TB_W4, 64, 64, BF);
+                tc_commit(&S.mbar);
+            }
+            ok = bt_wait(S, phase);
+            bt_epi_act<PREC>(lrow + BT_D0, S.A4, tid);
+            if (!(ok = bt_publish(ok))) break;
+        }
+        /* ---- output layer: G5 W5 -> gradient of the last hidden layer; dW5^T += last^T G5 ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.G16, S.W + TB_W5T, 16, 64, BF);
+            bt_mma_mn(tmem + BT_DW5T, last, 64, S.G16, 16, BF, acc);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        bt_epi_grad<PREC>(lrow + BT_D0, last, tid);
+        if (!(ok = bt_publish(ok))) break;
+        if (HH == 2) {
+            /* ---- head layer 2: G4 W4 -> G3 (mask A3); dW4 += G4^T A3 ---- */
+            if (tid == 0) {
+                tc_fence_after();
+                bt_mma_k(tmem + BT_D0, S.A4, S.W + TB_W4T, 64, 64, BF);
+                bt_mma_mn(tmem + BT_DW4, S.A4, 64, S.A3, 64, BF, acc);
+                tc_commit(&S.mbar);
+            }
+            ok = bt_wait(S, phase);
+            bt_epi_grad<PREC>(lrow + BT_D0, S.A3, tid);
+            if (!(ok = bt_publish(ok))) break;
+        }
+        /* ---- head layer 1: G3 W3 -> latent gradients; dW3 += G3^T IN ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.A3, S.W + TB_W3T, 64, 16, BF);
+            bt_mma_mn(tmem + BT_DW3, S.A3, 64, S.IN, 32, BF, acc);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        {
+            float v[16];
+            tmem_ld16(lrow + BT_D0, v);
+            tmem_wait_ld();
+            /* gradient of the density-network outputs: latents at lo.., the log-density gradient added to column 0 */
+            float gv[16];
+            float dl[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) dl[j] = T16::flt(T16::one(clamp_h(v[j])));
+#pragma unroll
+            for (int j = 0; j < 16; ++j) gv[j] = 0.f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) { /* latent_offset is 0 or 1 */
+                if (lo) gv[j + 1] = dl[j];
+                else gv[j] = dl[j];
+            }
+            gv[0] = clamp_h(gv[0] + dout.w);
+            uint32_t w[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) w[i] = T16::pack(gv[2 * i], gv[2 * i + 1]);
+            bt_st(S.G16, tid, 0, 16, make_uint4(w[0], w[1], w[2], w[3]));
+            bt_st(S.G16, tid, 1, 16, make_uint4(w[4], w[5], w[6], w[7]));
+        }
+        if (!(ok = bt_publish(ok))) break;
+        /* ---- density layer 2: G2 W2 -> G1 (mask H1); dW2^T += H1^T G2 ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.G16, S.W + TB_W2T, 16, 64, BF);
+            bt_mma_mn(tmem + BT_DW2T, S.H1, 64, S.G16, 16, BF, acc);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        bt_epi_grad<PREC>(lrow + BT_D0, S.H1, tid);
+        if (!(ok = bt_publish(ok))) break;
+        /* ---- density layer 1: G1 W1 -> feature gradients; dW1 += G1^T F ---- */
+        if (tid == 0) {
+            tc_fence_after();
+            bt_mma_k(tmem + BT_D0, S.H1, S.W + TB_W1T, 64, 32, BF);
+            bt_mma_mn(tmem + BT_DW1, S.H1, 64, S.F, 32, BF, acc);
+            tc_commit(&S.mbar);
+        }
+        ok = bt_wait(S, phase);
+        acc = true;
+        float dF[32];
+        tmem_ld32(lrow + BT_D0, dF);
+        tmem_wait_ld();
+        tc_fence_before();
+        if (ok) { /* every lane: the scatter pairs neighbouring lanes; rows without a gradient carry zeros */
+            if (r < 0)
+#pragma unroll
+                for (int q = 0; q < 32; ++q) dF[q] = 0.f;
+            hash_scatter16(p.grid, b.g_table, pos, dF, tid & 31);
+        }
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+    }
+    if (!ok && tid == 0) atomicOr(p.guard, 16);
+    /* the CTA's weight gradients (TMEM lanes 0..63) into the global blobs */
+    if (ok && acc && warp < 2) {
+        float *gh = b.g_head, *gb = b.g_base;
+        auto add_rows = [&](uint32_t col, float *dst, int width) { /* lane t = output o: dst[o * width + i] */
+            for (int c0 = 0; c0 < width; c0 += 32) {
+                float v[32];
+                tmem_ld32(lrow + col + c0, v);
+                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                    if (v[i] != 0.f) atomicAdd(dst + tid * width + c0 + i, v[i]);
+            }
+        };
+        auto add_cols = [&](uint32_t col, float *dst) { /* lane t = input i: dst[o * 64 + i] */
+            float v[16];
+            tmem_ld16(lrow + col, v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int o = 0; o < 16; ++o)
+                if (v[o] != 0.f) atomicAdd(dst + o * 64 + tid, v[o]);
+        };
+        if (HH == 2) add_rows(BT_DW4, gh + GH_W4, 64);
+        add_rows(BT_DW3, gh + GH_W3, 32);
+        add_rows(BT_DW1, gb + GB_W1, 32);
+        add_cols(BT_DW5T, gh + b.head_w5);
+        add_cols(BT_DW2T, gb + GB_W2);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, BT_COLS);
+    }
+}
+
 /* Cache rows of the cached differentiable render: the head input is the
  * trilinear blend of the 8 corner voxels' latents (divided by sum(w isset),
  * generateNetworkInput_cache_shfl_perf_kernel_cg), so the head's input
@@ -591,6 +1055,27 @@ cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int h
         attrs = true;
     }
     const bool bf16 = p.precision == 1;
+    if (p.use_tc) {
+        static bool tc_attrs = false;
+        const int tsmem = (int)sizeof(BtSmem);
+        if (!tc_attrs) {
+            cudaError_t e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+            if (e != cudaSuccess) return e;
+            tc_attrs = true;
+        }
+        const int grid = 2 * n_sms;
+        if (head_hidden == 2) {
+            if (bf16) wf_net_bwd_tc_kernel<1, 2><<<grid, 128, tsmem, s>>>(p, b, it);
+            else wf_net_bwd_tc_kernel<0, 2><<<grid, 128, tsmem, s>>>(p, b, it);
+        } else {
+            if (bf16) wf_net_bwd_tc_kernel<1, 1><<<grid, 128, tsmem, s>>>(p, b, it);
+            else wf_net_bwd_tc_kernel<0, 1><<<grid, 128, tsmem, s>>>(p, b, it);
+        }
+        return cudaGetLastError();
+    }
     if (head_hidden == 2) {
         if (bf16) wf_net_bwd_kernel<1, 2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
         else wf_net_bwd_kernel<0, 2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);

@@ -1659,6 +1659,7 @@ struct fvc_grad {
     float *s_table = nullptr, *s_base = nullptr, *s_head = nullptr; /* loss-scaled, one call */
     uint2 *d_w = nullptr;                                           /* BW_TOTAL weight packs, fp16 */
     uint2 *d_w_bf16 = nullptr;                                      /* the same in bf16 */
+    uint8_t *d_wtc = nullptr, *d_wtc_bf16 = nullptr;                /* TB_BYTES K-major tiles, fp16 / bf16 */
     float4 *d_ray_grad = nullptr;
     int ray_cap = 0;
     double *d_loss = nullptr;
@@ -1668,7 +1669,7 @@ struct fvc_grad {
     {
         dfree(d_table); dfree(d_base); dfree(d_head); dfree(s_table); dfree(s_base); dfree(s_head);
         dfree(d_lat); dfree(s_lat);
-        dfree(d_w); dfree(d_w_bf16); dfree(d_ray_grad); dfree(d_loss);
+        dfree(d_w); dfree(d_w_bf16); dfree(d_wtc); dfree(d_wtc_bf16); dfree(d_ray_grad); dfree(d_loss);
     }
 };
 
@@ -1737,6 +1738,28 @@ extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
         uint2 *&dst = variant ? g->d_w_bf16 : g->d_w;
         if ((rc = dalloc(&dst, P.size(), "backward weights"))) return rc;
         CU(cudaMemcpy(dst, P.data(), P.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        /* the tcgen05 kernel's B tiles: T[n][k] = W[n][k] (forward) or W[k][n] (input gradients) */
+        std::vector<uint8_t> T(TB_BYTES, 0);
+        auto put = [&](const std::vector<uint16_t> &Wm, int cols, int N, int K, int off, bool tr) {
+            for (int n = 0; n < N; ++n)
+                for (int k = 0; k < K; ++k)
+                    memcpy(&T[off + kmajor_offset(n, k, K)], &Wm[tr ? (size_t)k * cols + n : (size_t)n * cols + k], 2);
+        };
+        put(W1, 32, 64, 32, TB_W1, false);
+        put(W2, 64, 16, 64, TB_W2, false);
+        put(W3, 32, 64, 32, TB_W3, false);
+        put(W5, 64, 64, 16, TB_W5T, true);
+        put(W3, 32, 16, 64, TB_W3T, true);
+        put(W2, 64, 64, 16, TB_W2T, true);
+        put(W1, 32, 32, 64, TB_W1T, true);
+        if (m->head_hidden == 2) {
+            const std::vector<uint16_t> W4 = cv(slice(m->h_head, 64 * 32, 64 * 64));
+            put(W4, 64, 64, 64, TB_W4, false);
+            put(W4, 64, 64, 64, TB_W4T, true);
+        }
+        uint8_t *&dt = variant ? g->d_wtc_bf16 : g->d_wtc;
+        if ((rc = dalloc(&dt, T.size(), "backward weight tiles"))) return rc;
+        CU(cudaMemcpy(dt, T.data(), T.size(), cudaMemcpyHostToDevice));
     }
     *out = g.release();
     return FVC_OK;
@@ -1836,6 +1859,7 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     p.grad_cache_list = r->d_grad_cache_rows;
     BwdParams b;
     b.w = r->precision == FVC_PRECISION_BF16 ? g->d_w_bf16 : g->d_w;
+    b.wtc = r->precision == FVC_PRECISION_BF16 ? g->d_wtc_bf16 : g->d_wtc;
     b.g_table = g->s_table; b.g_base = g->s_base; b.g_head = g->s_head;
     b.head_w5 = m->head_hidden == 2 ? GH_W4 + 64 * 64 : GH_W4;
     b.loss = g->d_loss;

@@ -16,6 +16,7 @@ import pytest
 
 import frustumvolumecaching_gb300 as fvc
 from frustumvolumecaching_gb300 import camera as fcam
+from frustumvolumecaching_gb300 import model as fmodel
 from oracle import oracle as orc
 from tests.helpers import small_camera, tiny_model
 
@@ -148,3 +149,25 @@ def test_cached_backward_with_latent_gradients():
         cos, rel = _compare(a_.astype(np.float64), b_)
         print(f"cached {name}: cos {cos:.6f} rel {rel:.3e}")
         assert cos > 0.9999 and rel < 2e-3, (name, cos, rel)  # measured: 1.5e-4 / 1.6e-5 / 5.4e-6 / 3.6e-4
+
+
+@pytest.mark.parametrize("tcgen05", [True, False], ids=["tcgen05", "mma_sync"])
+def test_backward_one_hidden_layer_head(tcgen05):
+    """A color head with one hidden layer (the tcgen05 adjoint's HH = 1 form:
+    the output-layer gradient is masked by head hidden 1 directly)."""
+    torch = pytest.importorskip("torch")
+    spec = fmodel.spec_tiny(seed=21)
+    spec.name, spec.head_hidden_layers = f"{spec.name}_h1", 1
+    d = fmodel.ensure_model(spec)
+    loader = fvc.load_data(d)
+    cam = small_camera(1001, 32, 32)
+    rng = np.random.default_rng(13)
+    pix = rng.choice(32 * 32, 384, replace=False).astype(np.int32)
+    tgt = rng.uniform(0, 1, (384, 3)).astype(np.float32)
+    loss, g, _ = _gpu(torch, loader, cam, pix, tgt, tcgen05=tcgen05)
+    oloss, ot, ob, oh, _ = orc.OracleModel(d, mimic_fp16=True).loss_grad(cam, pix, tgt)
+    assert abs(loss - oloss) <= 1e-4 * oloss
+    for name, a, b in zip(("table", "base", "head"), g.read(), (ot, ob, oh)):
+        cos, rel = _compare(a.astype(np.float64), b)
+        print(f"one-hidden-layer head {name}: cos {cos:.6f} rel {rel:.3e}")
+        assert cos > 0.9999 and rel < 2e-3, (name, cos, rel)
