@@ -423,6 +423,9 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
  * once the MMAs that read that tile have completed.
  * TMEM columns: 0..63 layer accumulator; 64..127 dW4; 128..159 dW3;
  * 160..191 dW1; 192..207 dW5^T; 208..223 dW2^T. */
+#ifndef FVC_BT_HASH_GROUP
+#define FVC_BT_HASH_GROUP 4 /* hash levels whose gathers are in flight together */
+#endif
 constexpr int BT_COLS = 256;
 constexpr int BT_D0 = 0, BT_DW4 = 64, BT_DW3 = 128, BT_DW1 = 160, BT_DW5T = 192, BT_DW2T = 208;
 constexpr long long BT_WAIT_LIMIT = 2000000000ll; /* ~1 s of SM clocks */
@@ -624,8 +627,8 @@ __device__ __forceinline__ void hash_scatter16(const DevGrid &g, float *gt, floa
 template <int PREC, int HH>
 __global__ void __launch_bounds__(128, 2) wf_net_bwd_tc_kernel(RenderParams p, BwdParams b, int it)
 {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    BtSmem &S = *reinterpret_cast<BtSmem *>(smem_raw);
+    extern __shared__ __align__(128) unsigned char bt_smem_raw[];
+    BtSmem &S = *reinterpret_cast<BtSmem *>(bt_smem_raw);
     const int n_rows = p.counters[6];
     if (n_rows == 0) return;
     using T16 = E16<PREC>;
@@ -663,7 +666,7 @@ __global__ void __launch_bounds__(128, 2) wf_net_bwd_tc_kernel(RenderParams p, B
             const float4 pw = p.row_pay[r];
             pos = make_float3(pw.x, pw.y, pw.z);
             sh16(row_dir01(states, p.row_slot[r]), sh);
-            hash_encode<4>(p.grid, p.table, pos, feat);
+            hash_encode<FVC_BT_HASH_GROUP>(p.grid, p.table, pos, feat);
         } else {
 #pragma unroll
             for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
