@@ -28,6 +28,7 @@
  * out together with the 1/N of the mean.
  */
 #include <algorithm>
+#include <cstddef>
 
 #include <cuda_bf16.h>
 
@@ -404,46 +405,68 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
 /* ------------------------------------------------------------------------- */
 /* network adjoint on the 5th-generation tensor cores                        */
 /* ------------------------------------------------------------------------- */
-/* One CTA of 128 threads per 128-row tile (thread t owns row t and TMEM lane
- * t), two CTAs per SM.  Each activation and gradient of the tile sits in its
- * own canonical K-major shared tile (8-row x 16-byte core matrices, see
- * fvc_tc.cuh), so that it serves two MMAs:
- *   - as the K-major A operand of the next layer (forward: X W^T; input
- *     gradient: G W, with W^T tiles as B);
- *   - as an MN-major operand of the weight-gradient MMA dW = G^T X, whose
- *     contraction runs over the tile's 128 rows.  Read MN-major, a tile of C
- *     columns has its 8-column groups SBO = 128 bytes apart and its 8-row
- *     groups LBO = C / 8 * 128 bytes apart.
+/* Warp-specialised: two CTAs of 256 threads per SM, each CTA persistent
+ * over 128-row tiles.
+ *   - MMA warps 0..3: thread t owns row t of a tile and TMEM lane t; thread 0
+ *     issues the tcgen05 MMAs, the warps wait (bounded) and run the
+ *     epilogues.  They synchronise among themselves with named barrier 1.
+ *   - hash warps 4..7: thread 128 + t fetches row t of the next tile, runs
+ *     its hash encode into a double-buffered feature / head-input tile, and
+ *     scatters the feature gradients of the tile before, read from TMEM.
+ * The hash gathers and the table-gradient atomics (L2-bound) thus overlap the
+ * MMA stage chain of another tile.  Handoffs use mbarriers:
+ *   in_full[b]  hash -> MMA: F[b], IN[b] (SH, 1-padding) and dout[b] written;
+ *   df_full     MMA -> hash: the tile's feature gradients sit in TMEM columns
+ *               224..255 and its last MMAs (which read F[b], IN[b]) are done;
+ *   df_empty    hash -> MMA: those columns have been read.
+ * Each activation and gradient of a tile sits in its own canonical K-major
+ * shared tile (8-row x 16-byte core matrices, see fvc_tc.cuh), so it serves
+ * as the K-major A operand of the next layer (forward X W^T, input gradient
+ * G W) and as an MN-major operand of the weight-gradient MMA dW = G^T X,
+ * whose contraction runs over the tile's 128 rows.  Read MN-major, a tile of
+ * C columns has its 8-column groups SBO = 128 bytes apart and its 8-row
+ * groups LBO = C / 8 * 128 bytes apart.  The input-gradient MMAs read the
+ * forward weight tiles MN-major as their B = W, so one copy of each weight
+ * serves both directions.
  * The weight gradients accumulate in TMEM over every tile the CTA takes and
  * are added to the global blobs once per launch; no shared-memory atomics.
  * The weight-gradient MMAs use M = 128 with their 64 meaningful rows in TMEM
  * lanes 0..63: a 64-column tile read MN-major with M = 128 runs up to 1023
- * bytes past its end, which stays inside the next tile or the pad.
+ * bytes past its end, which stays inside the next tile.
  * Gradient tiles reuse the activation tile whose mask they need, in place,
  * once the MMAs that read that tile have completed.
  * TMEM columns: 0..63 layer accumulator; 64..127 dW4; 128..159 dW3;
- * 160..191 dW1; 192..207 dW5^T; 208..223 dW2^T. */
+ * 160..191 dW1; 192..207 dW5^T; 208..223 dW2^T; 224..255 feature gradients. */
 #ifndef FVC_BT_HASH_GROUP
 #define FVC_BT_HASH_GROUP 4 /* hash levels whose gathers are in flight together */
 #endif
 constexpr int BT_COLS = 256;
-constexpr int BT_D0 = 0, BT_DW4 = 64, BT_DW3 = 128, BT_DW1 = 160, BT_DW5T = 192, BT_DW2T = 208;
+constexpr int BT_D0 = 0, BT_DW4 = 64, BT_DW3 = 128, BT_DW1 = 160, BT_DW5T = 192, BT_DW2T = 208, BT_DF = 224;
 constexpr long long BT_WAIT_LIMIT = 2000000000ll; /* ~1 s of SM clocks */
+#ifndef FVC_BT_HASH_SPLIT
+#define FVC_BT_HASH_SPLIT 1 /* hash threads per row (each takes 16 / split levels); 1 and 2 measured alike */
+#endif
+constexpr int BT_SPLIT = FVC_BT_HASH_SPLIT, BT_NL = 16 / BT_SPLIT;
+constexpr int BT_HASH_THREADS = 128 * BT_SPLIT, BT_THREADS = 128 + BT_HASH_THREADS;
+static_assert(BT_SPLIT == 1 || BT_SPLIT == 2, "1 or 2 hash threads per row");
 
 struct __align__(128) BtSmem {
     uint8_t W[TB_BYTES];
-    uint8_t F[128 * 32 * 2];   /* hash features */
-    uint8_t IN[128 * 32 * 2];  /* head input [latents | SH | 1.0] */
-    uint8_t G16[128 * 16 * 2]; /* output-layer gradient, later the density-network output gradient */
-    uint8_t H1[128 * 64 * 2];  /* density hidden layer, later its gradient */
-    uint8_t A3[128 * 64 * 2];  /* head hidden 1, later its gradient */
-    uint8_t A4[128 * 64 * 2];  /* head hidden 2, later its gradient */
-    uint8_t pad[1024];
-    uint64_t mbar;
+    uint8_t H1[128 * 64 * 2];     /* density hidden layer, later its gradient */
+    uint8_t A3[128 * 64 * 2];     /* head hidden 1, later its gradient */
+    uint8_t A4[128 * 64 * 2];     /* head hidden 2, later its gradient */
+    uint8_t F[2][128 * 32 * 2];   /* hash features */
+    uint8_t IN[2][128 * 32 * 2];  /* head input [latents | SH | 1.0] */
+    uint8_t G16[128 * 16 * 2];    /* output-layer gradient, later the density-network output gradient */
+    float4 dout[2][128];          /* the rows' output gradients */
+    uint64_t mbar, in_full[2], df_full, df_empty;
     uint32_t tmem_base;
 };
 static_assert(2 * (sizeof(BtSmem) + 1024) <= 228 * 1024, "two CTAs per SM");
 static_assert(2 * BT_COLS <= 512, "two CTAs per SM in TMEM");
+static_assert(offsetof(BtSmem, F) - offsetof(BtSmem, A4) == 128 * 64 * 2 && offsetof(BtSmem, A3) - offsetof(BtSmem, H1) == 128 * 64 * 2 &&
+                  offsetof(BtSmem, A4) - offsetof(BtSmem, A3) == 128 * 64 * 2 && sizeof(BtSmem::F) >= 1024,
+              "each 64-column tile read MN-major with M = 128 is followed by 1 KB of other tiles");
 
 __device__ __forceinline__ void bt_st(uint8_t *tile, int row, int c, int K, uint4 v)
 {
@@ -463,6 +486,18 @@ __device__ __forceinline__ void bt_mma_k(uint32_t d, const uint8_t *a, const uin
         tc_mma_f16(d, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
 }
 
+/* D = A (128 x K, K-major tile) * W (K x N) where W is a weight tile stored
+ * K-major for the forward (bw columns per row, row = the K index here), read
+ * MN-major */
+__device__ __forceinline__ void bt_mma_kw(uint32_t d, const uint8_t *a, const uint8_t *w, int bw, int K, int N, bool bf16)
+{
+    const uint32_t sbo = (uint32_t)(K / 8) * 128u, id = idesc_f16(128, N, bf16) | (1u << 16);
+    const uint32_t lb = (uint32_t)(bw / 8) * 128u;
+    const uint32_t a0 = smem_u32(a), b0 = smem_u32(w);
+    for (int kc = 0; kc < K / 16; ++kc)
+        tc_mma_f16(d, umma_desc(a0 + 256u * kc, 128u, sbo), umma_desc(b0 + 2u * lb * kc, lb, 128u), id, kc > 0 ? 1u : 0u);
+}
+
 /* D (+)= A^T B over the 128 tile rows: A a tile of ca columns (M = 128 read
  * from it), B a tile of N columns, both MN-major */
 __device__ __forceinline__ void bt_mma_mn(uint32_t d, const uint8_t *a, int ca, const uint8_t *b, int N, bool bf16, bool acc)
@@ -474,21 +509,31 @@ __device__ __forceinline__ void bt_mma_mn(uint32_t d, const uint8_t *a, int ca, 
         tc_mma_f16(d, umma_desc(a0 + 2u * la * s, la, 128u), umma_desc(b0 + 2u * lb * s, lb, 128u), id, (acc || s > 0) ? 1u : 0u);
 }
 
-/* the MMAs issued by thread 0 are committed; every thread waits (bounded) */
-__device__ __forceinline__ bool bt_wait(BtSmem &S, uint32_t &phase)
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
 {
-    const bool ok = mbar_wait(&S.mbar, phase, BT_WAIT_LIMIT);
-    phase ^= 1u;
-    tc_fence_after();
-    return ok;
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(mbar)) : "memory");
 }
 
-/* rewritten rows visible to the tensor core, TMEM reads ordered before the next MMA */
+/* bounded wait on a phase parity; a phase that never completes clears ok */
+__device__ __forceinline__ void bt_wait_on(uint64_t *mbar, uint32_t parity, bool &ok)
+{
+    if (ok && !mbar_wait(mbar, parity, BT_WAIT_LIMIT)) ok = false;
+    tc_fence_after();
+}
+
+/* MMA warps: rewritten rows visible to the tensor core, TMEM reads ordered
+ * before the next MMA; named barrier 1 over the 128 MMA-warp threads, OR of
+ * the failure flags */
 __device__ __forceinline__ bool bt_publish(bool ok)
 {
     fence_proxy_async();
     tc_fence_before();
-    return __syncthreads_or(!ok) == 0;
+    uint32_t bad;
+    asm volatile("{\n .reg .pred p, q;\n setp.eq.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(bad)
+                 : "r"(ok ? 1u : 0u)
+                 : "memory");
+    return bad == 0u;
 }
 
 /* 64 accumulator columns -> ReLU -> 16-bit row of a 64-column tile */
@@ -551,8 +596,9 @@ __device__ __forceinline__ void red_add4(float *a, float x, float y, float z, fl
  * wider than about one step) */
 constexpr int SC_PAIR_LEVELS = 10;
 
-/* Adjoint of hash_encode for the 16-level grid, called by all 32 lanes of a
- * warp (rows without a gradient pass zeros).  Per level:
+/* Adjoint of hash_encode over levels l0 .. l0 + NL - 1 of the 16-level grid,
+ * called by all 32 lanes of a warp (rows without a gradient pass zeros).
+ * Per level:
  *   - lanes 2j and 2j+1 in the same cell at a coarse level merge: the odd
  *     lane hands its trilinear weights and feature gradient to the even lane,
  *     which adds both rows' contributions to the 8 corners;
@@ -560,11 +606,13 @@ constexpr int SC_PAIR_LEVELS = 10;
  *     {2i, 2i+1} (a hashed level's cell with even x, or adjacent dense
  *     indices) go out as one 16-byte red.global.add.v4.f32.
  * The table receives the same sums with fewer L2 atomics. */
-__device__ __forceinline__ void hash_scatter16(const DevGrid &g, float *gt, float3 pos, const float (&dF)[32], int lane)
+template <int NL>
+__device__ __forceinline__ void hash_scatter_levels(const DevGrid &g, float *gt, float3 pos, int l0, const float (&dF)[2 * NL], int lane)
 {
 #pragma unroll
-    for (int l = 0; l < 16; ++l) {
-        float ax = dF[2 * l], ay = dF[2 * l + 1];
+    for (int j = 0; j < NL; ++j) {
+        const int l = l0 + j;
+        float ax = dF[2 * j], ay = dF[2 * j + 1];
         const float sc = g.scale[l];
         const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
         const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
@@ -624,8 +672,59 @@ __device__ __forceinline__ void hash_scatter16(const DevGrid &g, float *gt, floa
     }
 }
 
+__device__ __forceinline__ void tmem_ld_n(uint32_t taddr, float (&v)[16]) { tmem_ld16(taddr, v); }
+__device__ __forceinline__ void tmem_ld_n(uint32_t taddr, float (&v)[32]) { tmem_ld32(taddr, v); }
+
+/* hash_encode restricted to levels l0 .. l0 + NL - 1, LG levels' gathers in
+ * flight together; the same arithmetic, so the same features */
+template <int NL, int LG>
+__device__ __forceinline__ void encode_levels(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, int l0, __half2 (&out)[NL])
+{
+#pragma unroll
+    for (int j0 = 0; j0 < NL; j0 += LG) {
+        __half2 v[LG][8];
+        float wx[LG], wy[LG], wz[LG];
+#pragma unroll
+        for (int j = 0; j < LG; ++j) {
+            const int l = l0 + j0 + j;
+            const float sc = g.scale[l];
+            const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
+            const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+            const uint32_t gx = (uint32_t)(int)fx, gy = (uint32_t)(int)fy, gz = (uint32_t)(int)fz;
+            wx[j] = __fsub_rn(px, fx); wy[j] = __fsub_rn(py, fy); wz[j] = __fsub_rn(pz, fz);
+            const uint32_t size = g.size[l];
+            const __half2 *tl = table + g.offset[l];
+            if ((g.dense_mask >> l) & 1u) {
+                const uint32_t rr = g.res[l], r2 = g.res2[l];
+                const uint32_t b0 = gx + gy * rr + gz * r2;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t i = b0 + ((c & 1) ? 1u : 0u) + ((c & 2) ? rr : 0u) + ((c & 4) ? r2 : 0u);
+                    if (i >= size) i -= size;
+                    v[j][c] = __ldg(tl + i);
+                }
+            } else {
+                const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;
+                const uint32_t hz0 = gz * 805459861u, hz1 = (gz + 1u) * 805459861u;
+                const uint32_t m = size - 1u;
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    v[j][c] = __ldg(tl + (((gx + ((c & 1) ? 1u : 0u)) ^ ((c & 2) ? hy1 : hy0) ^ ((c & 4) ? hz1 : hz0)) & m));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < LG; ++j) {
+            float2 e[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) e[q] = f2_lerp(__half22float2(v[j][2 * q]), __half22float2(v[j][2 * q + 1]), wx[j]);
+            const float2 g0 = f2_lerp(e[0], e[1], wy[j]), g1 = f2_lerp(e[2], e[3], wy[j]);
+            out[j0 + j] = __float22half2_rn(f2_lerp(g0, g1, wz[j]));
+        }
+    }
+}
+
 template <int PREC, int HH>
-__global__ void __launch_bounds__(128, 2) wf_net_bwd_tc_kernel(RenderParams p, BwdParams b, int it)
+__global__ void __launch_bounds__(BT_THREADS, 2) wf_net_bwd_tc_kernel(RenderParams p, BwdParams b, int it)
 {
     extern __shared__ __align__(128) unsigned char bt_smem_raw[];
     BtSmem &S = *reinterpret_cast<BtSmem *>(bt_smem_raw);
@@ -636,226 +735,234 @@ __global__ void __launch_bounds__(128, 2) wf_net_bwd_tc_kernel(RenderParams p, B
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0) {
         mbar_init(&S.mbar, 1);
+        mbar_init(&S.in_full[0], BT_HASH_THREADS);
+        mbar_init(&S.in_full[1], BT_HASH_THREADS);
+        mbar_init(&S.df_full, 1);
+        mbar_init(&S.df_empty, BT_HASH_THREADS);
         mbar_arrive_expect_tx(&S.mbar, TB_BYTES);
         bulk_copy_g2s(S.W, b.wtc, TB_BYTES, &S.mbar);
     }
-    for (int i = tid; i < 1024 / 16; i += 128) reinterpret_cast<uint4 *>(S.pad)[i] = make_uint4(0, 0, 0, 0);
     if (warp == 0) tmem_alloc(&S.tmem_base, BT_COLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem_base;
-    const uint32_t lrow = tmem + ((uint32_t)(warp * 32) << 16);
-    const RayState *states = p.states[it & 1];
-    const int lo = p.latent_offset;
-    uint32_t phase = 0;
-    bool ok = mbar_wait(&S.mbar, phase, BT_WAIT_LIMIT);
-    phase ^= 1u;
-    tc_fence_after();
-    uint8_t *last = HH == 2 ? S.A4 : S.A3;
-    bool acc = false; /* dW accumulators hold this launch's sums */
+    const uint32_t lrow = tmem + ((uint32_t)((warp & 3) * 32) << 16); /* this thread's TMEM lane */
+    const int row = tid & 127;
     const int n_tiles = (n_rows + 127) / 128;
-    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        const int k = tile * 128 + tid;
-        const int r = k < n_rows ? p.grad_res_list[k] : -1;
-        float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
-        float3 pos = make_float3(0.f, 0.f, 0.f);
-        __half2 feat[16], sh[8];
-        if (r >= 0) {
-            dout = p.row_dout[r];
-            const float4 pw = p.row_pay[r];
-            pos = make_float3(pw.x, pw.y, pw.z);
-            sh16(row_dir01(states, p.row_slot[r]), sh);
-            hash_encode<FVC_BT_HASH_GROUP>(p.grid, p.table, pos, feat);
-        } else {
+    const int n_mine = blockIdx.x < n_tiles ? (n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    bool ok = true;
+    if (warp >= 4) {
+        /* ================= hash warps ================= */
+        /* thread 128 + h: row h & 127, levels l0 .. l0 + BT_NL - 1; the first set also writes SH and dout */
+        const int l0 = ((tid - 128) >> 7) * BT_NL;
+        const bool lead = l0 == 0;
+        const RayState *states = p.states[it & 1];
+        int r_prev = -1;
+        float3 pos_prev = make_float3(0.f, 0.f, 0.f);
+        for (int i = 0; i <= n_mine && ok; ++i) {
+            int r = -1;
+            float3 pos = make_float3(0.f, 0.f, 0.f);
+            if (i < n_mine) {
+                /* tile i into buffer i & 1 (its last reader, tile i - 2, finished before df_full of i - 2,
+                 * which this loop waited for one iteration ago) */
+                const int bb = i & 1;
+                const int k = ((int)blockIdx.x + i * (int)gridDim.x) * 128 + row;
+                r = k < n_rows ? p.grad_res_list[k] : -1;
+                float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
+                __half2 feat[BT_NL], sh[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+                for (int q = 0; q < BT_NL; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
-        }
-        /* ---- F, head input (SH, 1-padding) and the output-layer gradient ---- */
-        {
-            uint32_t f[16], s[8];
+                for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+                if (r >= 0) {
+                    const float4 pw = p.row_pay[r];
+                    pos = make_float3(pw.x, pw.y, pw.z);
+                    if (lead) {
+                        dout = p.row_dout[r];
+                        sh16(row_dir01(states, p.row_slot[r]), sh);
+                    }
+                    encode_levels<BT_NL, FVC_BT_HASH_GROUP>(p.grid, p.table, pos, l0, feat);
+                }
+                uint32_t f[BT_NL];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const float2 v = __half22float2(feat[q]);
-                f[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&feat[q]) : T16::pack(v.x, v.y);
+                for (int q = 0; q < BT_NL; ++q) {
+                    const float2 v = __half22float2(feat[q]);
+                    f[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&feat[q]) : T16::pack(v.x, v.y);
+                }
+#pragma unroll
+                for (int c = 0; c < BT_NL / 4; ++c)
+                    bt_st(S.F[bb], row, l0 / 4 + c, 32, make_uint4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]));
+                if (lead) {
+                    uint32_t sv[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float2 v = __half22float2(sh[q]);
+                        sv[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&sh[q]) : T16::pack(v.x, v.y);
+                    }
+                    bt_st(S.IN[bb], row, 1, 32, make_uint4(sv[0], sv[1], sv[2], sv[3]));
+                    bt_st(S.IN[bb], row, 2, 32, make_uint4(sv[4], sv[5], sv[6], sv[7]));
+                    const uint32_t one2 = T16::pack(1.0f, 1.0f);
+                    bt_st(S.IN[bb], row, 3, 32, make_uint4(one2, one2, one2, one2));
+                    S.dout[bb][row] = dout;
+                }
+                fence_proxy_async();
+                mbar_arrive(&S.in_full[bb]);
             }
+            if (i >= 1) {
+                /* feature gradients of tile i - 1 -> table */
+                bt_wait_on(&S.df_full, (uint32_t)((i - 1) & 1), ok);
+                ok = __all_sync(FULLMASK, ok); /* the TMEM load and the scatter's shuffles take whole warps */
+                if (!ok) break;
+                float dF[2 * BT_NL];
+                tmem_ld_n(lrow + BT_DF + 2 * l0, dF);
+                tmem_wait_ld();
+                tc_fence_before();
+                mbar_arrive(&S.df_empty);
+                if (r_prev < 0)
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const float2 v = __half22float2(sh[q]);
-                s[q] = PREC == 0 ? *reinterpret_cast<const uint32_t *>(&sh[q]) : T16::pack(v.x, v.y);
+                    for (int q = 0; q < 2 * BT_NL; ++q) dF[q] = 0.f;
+                hash_scatter_levels<BT_NL>(p.grid, b.g_table, pos_prev, l0, dF, tid & 31);
             }
+            r_prev = r;
+            pos_prev = pos;
+        }
+    } else {
+        /* ================= MMA warps ================= */
+        const int lo = p.latent_offset;
+        uint32_t phase = 0;
+        bt_wait_on(&S.mbar, phase, ok); /* the weights */
+        phase ^= 1u;
+        ok = bt_publish(ok); /* every decision to leave the loop is taken by all MMA threads together */
+        uint8_t *last = HH == 2 ? S.A4 : S.A3;
+        bool acc = false; /* dW accumulators hold this launch's sums */
+#define BT_STAGE(...)                                   \
+    if (tid == 0) {                                     \
+        tc_fence_after();                               \
+        __VA_ARGS__;                                    \
+        tc_commit(&S.mbar);                             \
+    }                                                   \
+    bt_wait_on(&S.mbar, phase, ok);                     \
+    phase ^= 1u;
+        for (int i = 0; i < n_mine && ok; ++i) {
+            const int bb = i & 1;
+            uint8_t *F = S.F[bb], *IN = S.IN[bb];
+            bt_wait_on(&S.in_full[bb], (uint32_t)((i >> 1) & 1), ok);
+            const float4 dout = S.dout[bb][row];
+            bt_st(S.G16, row, 0, 16, make_uint4(T16::pack(clamp_h(dout.x), clamp_h(dout.y)), T16::pack(clamp_h(dout.z), 0.f), 0u, 0u));
+            bt_st(S.G16, row, 1, 16, make_uint4(0u, 0u, 0u, 0u));
+            if (!(ok = bt_publish(ok))) break;
+            /* ---- density layer 1: F W1^T -> H1 ---- */
+            BT_STAGE(bt_mma_k(tmem + BT_D0, F, S.W + TB_W1, 32, 64, BF));
+            bt_epi_act<PREC>(lrow + BT_D0, S.H1, row);
+            if (!(ok = bt_publish(ok))) break;
+            /* ---- density layer 2: H1 W2^T -> latents of the head input ---- */
+            BT_STAGE(bt_mma_k(tmem + BT_D0, S.H1, S.W + TB_W2, 64, 16, BF));
+            {
+                float v[16];
+                tmem_ld16(lrow + BT_D0, v);
+                tmem_wait_ld();
+                uint32_t w[4];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) bt_st(S.F, tid, c, 32, make_uint4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]));
-            bt_st(S.IN, tid, 1, 32, make_uint4(s[0], s[1], s[2], s[3]));
-            bt_st(S.IN, tid, 2, 32, make_uint4(s[4], s[5], s[6], s[7]));
-            const uint32_t one2 = T16::pack(1.0f, 1.0f);
-            bt_st(S.IN, tid, 3, 32, make_uint4(one2, one2, one2, one2));
-            bt_st(S.G16, tid, 0, 16, make_uint4(T16::pack(clamp_h(dout.x), clamp_h(dout.y)), T16::pack(clamp_h(dout.z), 0.f), 0u, 0u));
-            bt_st(S.G16, tid, 1, 16, make_uint4(0u, 0u, 0u, 0u));
-        }
-        if (!(ok = bt_publish(ok))) break;
-        /* ---- density layer 1: F W1^T -> H1 ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.F, S.W + TB_W1, 32, 64, BF);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        bt_epi_act<PREC>(lrow + BT_D0, S.H1, tid);
-        if (!(ok = bt_publish(ok))) break;
-        /* ---- density layer 2: H1 W2^T -> latents of the head input ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.H1, S.W + TB_W2, 64, 16, BF);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        {
-            float v[16];
-            tmem_ld16(lrow + BT_D0, v);
-            tmem_wait_ld();
-            uint32_t w[4];
+                for (int q = 0; q < 4; ++q) /* latent_offset is 0 or 1 */
+                    w[q] = T16::pack(clamp_h(lo ? v[2 * q + 1] : v[2 * q]), clamp_h(lo ? v[2 * q + 2] : v[2 * q + 1]));
+                bt_st(IN, row, 0, 32, make_uint4(w[0], w[1], w[2], w[3]));
+            }
+            if (!(ok = bt_publish(ok))) break;
+            /* ---- head layer 1 (bias from the 1-padding) -> A3 ---- */
+            BT_STAGE(bt_mma_k(tmem + BT_D0, IN, S.W + TB_W3, 32, 64, BF));
+            bt_epi_act<PREC>(lrow + BT_D0, S.A3, row);
+            if (!(ok = bt_publish(ok))) break;
+            if (HH == 2) {
+                /* ---- head layer 2 -> A4 ---- */
+                BT_STAGE(bt_mma_k(tmem + BT_D0, S.A3, S.W + TB_W4, 64, 64, BF));
+                bt_epi_act<PREC>(lrow + BT_D0, S.A4, row);
+                if (!(ok = bt_publish(ok))) break;
+            }
+            /* ---- output layer: G5 W5 -> gradient of the last hidden layer; dW5^T += last^T G5 ---- */
+            BT_STAGE(bt_mma_kw(tmem + BT_D0, S.G16, S.W + TB_W5, 64, 16, 64, BF); bt_mma_mn(tmem + BT_DW5T, last, 64, S.G16, 16, BF, acc));
+            bt_epi_grad<PREC>(lrow + BT_D0, last, row);
+            if (!(ok = bt_publish(ok))) break;
+            if (HH == 2) {
+                /* ---- head layer 2: G4 W4 -> G3 (mask A3); dW4 += G4^T A3 ---- */
+                BT_STAGE(bt_mma_kw(tmem + BT_D0, S.A4, S.W + TB_W4, 64, 64, 64, BF); bt_mma_mn(tmem + BT_DW4, S.A4, 64, S.A3, 64, BF, acc));
+                bt_epi_grad<PREC>(lrow + BT_D0, S.A3, row);
+                if (!(ok = bt_publish(ok))) break;
+            }
+            /* ---- head layer 1: G3 W3 -> latent gradients; dW3 += G3^T IN ---- */
+            BT_STAGE(bt_mma_kw(tmem + BT_D0, S.A3, S.W + TB_W3, 32, 64, 16, BF); bt_mma_mn(tmem + BT_DW3, S.A3, 64, IN, 32, BF, acc));
+            {
+                float v[16];
+                tmem_ld16(lrow + BT_D0, v);
+                tmem_wait_ld();
+                /* gradient of the density-network outputs: latents at lo.., the log-density gradient added to column 0 */
+                float dl[8], gv[16];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) /* latent_offset is 0 or 1 */
-                w[i] = T16::pack(clamp_h(lo ? v[2 * i + 1] : v[2 * i]), clamp_h(lo ? v[2 * i + 2] : v[2 * i + 1]));
-            bt_st(S.IN, tid, 0, 32, make_uint4(w[0], w[1], w[2], w[3]));
-        }
-        if (!(ok = bt_publish(ok))) break;
-        /* ---- head layer 1 (bias from the 1-padding) -> A3 ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.IN, S.W + TB_W3, 32, 64, BF);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        bt_epi_act<PREC>(lrow + BT_D0, S.A3, tid);
-        if (!(ok = bt_publish(ok))) break;
-        if (HH == 2) {
-            /* ---- head layer 2 -> A4 ---- */
+                for (int j = 0; j < 8; ++j) dl[j] = T16::flt(T16::one(clamp_h(v[j])));
+#pragma unroll
+                for (int j = 0; j < 16; ++j) gv[j] = 0.f;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) { /* latent_offset is 0 or 1 */
+                    if (lo) gv[j + 1] = dl[j];
+                    else gv[j] = dl[j];
+                }
+                gv[0] = clamp_h(gv[0] + dout.w);
+                uint32_t w[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) w[q] = T16::pack(gv[2 * q], gv[2 * q + 1]);
+                bt_st(S.G16, row, 0, 16, make_uint4(w[0], w[1], w[2], w[3]));
+                bt_st(S.G16, row, 1, 16, make_uint4(w[4], w[5], w[6], w[7]));
+            }
+            if (!(ok = bt_publish(ok))) break;
+            /* ---- density layer 2: G2 W2 -> G1 (mask H1); dW2^T += H1^T G2 ---- */
+            BT_STAGE(bt_mma_kw(tmem + BT_D0, S.G16, S.W + TB_W2, 64, 16, 64, BF); bt_mma_mn(tmem + BT_DW2T, S.H1, 64, S.G16, 16, BF, acc));
+            bt_epi_grad<PREC>(lrow + BT_D0, S.H1, row);
+            if (!(ok = bt_publish(ok))) break;
+            /* ---- density layer 1: G1 W1 -> feature gradients (for the hash warps); dW1 += G1^T F ---- */
+            if (i >= 1) bt_wait_on(&S.df_empty, (uint32_t)((i - 1) & 1), ok); /* tile i - 1's gradients were read */
+            if (!(ok = bt_publish(ok))) break;
             if (tid == 0) {
                 tc_fence_after();
-                bt_mma_k(tmem + BT_D0, S.A3, S.W + TB_W4, 64, 64, BF);
+                bt_mma_kw(tmem + BT_DF, S.H1, S.W + TB_W1, 32, 64, 32, BF);
+                bt_mma_mn(tmem + BT_DW1, S.H1, 64, F, 32, BF, acc);
+                tc_commit(&S.df_full);
                 tc_commit(&S.mbar);
             }
-            ok = bt_wait(S, phase);
-            bt_epi_act<PREC>(lrow + BT_D0, S.A4, tid);
-            if (!(ok = bt_publish(ok))) break;
+            bt_wait_on(&S.mbar, phase, ok);
+            phase ^= 1u;
+            acc = true;
+            ok = bt_publish(ok);
         }
-        /* ---- output layer: G5 W5 -> gradient of the last hidden layer; dW5^T += last^T G5 ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.G16, S.W + TB_W5T, 16, 64, BF);
-            bt_mma_mn(tmem + BT_DW5T, last, 64, S.G16, 16, BF, acc);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        bt_epi_grad<PREC>(lrow + BT_D0, last, tid);
-        if (!(ok = bt_publish(ok))) break;
-        if (HH == 2) {
-            /* ---- head layer 2: G4 W4 -> G3 (mask A3); dW4 += G4^T A3 ---- */
-            if (tid == 0) {
-                tc_fence_after();
-                bt_mma_k(tmem + BT_D0, S.A4, S.W + TB_W4T, 64, 64, BF);
-                bt_mma_mn(tmem + BT_DW4, S.A4, 64, S.A3, 64, BF, acc);
-                tc_commit(&S.mbar);
-            }
-            ok = bt_wait(S, phase);
-            bt_epi_grad<PREC>(lrow + BT_D0, S.A3, tid);
-            if (!(ok = bt_publish(ok))) break;
-        }
-        /* ---- head layer 1: G3 W3 -> latent gradients; dW3 += G3^T IN ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.A3, S.W + TB_W3T, 64, 16, BF);
-            bt_mma_mn(tmem + BT_DW3, S.A3, 64, S.IN, 32, BF, acc);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        {
-            float v[16];
-            tmem_ld16(lrow + BT_D0, v);
-            tmem_wait_ld();
-            /* gradient of the density-network outputs: latents at lo.., the log-density gradient added to column 0 */
-            float gv[16];
-            float dl[8];
+#undef BT_STAGE
+        /* the CTA's weight gradients (TMEM lanes 0..63) into the global blobs */
+        if (ok && acc && warp < 2) {
+            float *gh = b.g_head, *gb = b.g_base;
+            auto add_rows = [&](uint32_t col, float *dst, int width) { /* lane t = output o: dst[o * width + i] */
+                for (int c0 = 0; c0 < width; c0 += 32) {
+                    float v[32];
+                    tmem_ld32(lrow + col + c0, v);
+                    tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 8; ++j) dl[j] = T16::flt(T16::one(clamp_h(v[j])));
-#pragma unroll
-            for (int j = 0; j < 16; ++j) gv[j] = 0.f;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) { /* latent_offset is 0 or 1 */
-                if (lo) gv[j + 1] = dl[j];
-                else gv[j] = dl[j];
-            }
-            gv[0] = clamp_h(gv[0] + dout.w);
-            uint32_t w[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) w[i] = T16::pack(gv[2 * i], gv[2 * i + 1]);
-            bt_st(S.G16, tid, 0, 16, make_uint4(w[0], w[1], w[2], w[3]));
-            bt_st(S.G16, tid, 1, 16, make_uint4(w[4], w[5], w[6], w[7]));
-        }
-        if (!(ok = bt_publish(ok))) break;
-        /* ---- density layer 2: G2 W2 -> G1 (mask H1); dW2^T += H1^T G2 ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.G16, S.W + TB_W2T, 16, 64, BF);
-            bt_mma_mn(tmem + BT_DW2T, S.H1, 64, S.G16, 16, BF, acc);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        bt_epi_grad<PREC>(lrow + BT_D0, S.H1, tid);
-        if (!(ok = bt_publish(ok))) break;
-        /* ---- density layer 1: G1 W1 -> feature gradients; dW1 += G1^T F ---- */
-        if (tid == 0) {
-            tc_fence_after();
-            bt_mma_k(tmem + BT_D0, S.H1, S.W + TB_W1T, 64, 32, BF);
-            bt_mma_mn(tmem + BT_DW1, S.H1, 64, S.F, 32, BF, acc);
-            tc_commit(&S.mbar);
-        }
-        ok = bt_wait(S, phase);
-        acc = true;
-        float dF[32];
-        tmem_ld32(lrow + BT_D0, dF);
-        tmem_wait_ld();
-        tc_fence_before();
-        if (ok) { /* every lane: the scatter pairs neighbouring lanes; rows without a gradient carry zeros */
-            if (r < 0)
-#pragma unroll
-                for (int q = 0; q < 32; ++q) dF[q] = 0.f;
-            hash_scatter16(p.grid, b.g_table, pos, dF, tid & 31);
-        }
-        if (__syncthreads_or(!ok)) { ok = false; break; }
-    }
-    if (!ok && tid == 0) atomicOr(p.guard, 16);
-    /* the CTA's weight gradients (TMEM lanes 0..63) into the global blobs */
-    if (ok && acc && warp < 2) {
-        float *gh = b.g_head, *gb = b.g_base;
-        auto add_rows = [&](uint32_t col, float *dst, int width) { /* lane t = output o: dst[o * width + i] */
-            for (int c0 = 0; c0 < width; c0 += 32) {
-                float v[32];
-                tmem_ld32(lrow + col + c0, v);
+                    for (int q = 0; q < 32; ++q)
+                        if (v[q] != 0.f) atomicAdd(dst + tid * width + c0 + q, v[q]);
+                }
+            };
+            auto add_cols = [&](uint32_t col, float *dst) { /* lane t = input i: dst[o * 64 + i] */
+                float v[16];
+                tmem_ld16(lrow + col, v);
                 tmem_wait_ld();
 #pragma unroll
-                for (int i = 0; i < 32; ++i)
-                    if (v[i] != 0.f) atomicAdd(dst + tid * width + c0 + i, v[i]);
-            }
-        };
-        auto add_cols = [&](uint32_t col, float *dst) { /* lane t = input i: dst[o * 64 + i] */
-            float v[16];
-            tmem_ld16(lrow + col, v);
-            tmem_wait_ld();
-#pragma unroll
-            for (int o = 0; o < 16; ++o)
-                if (v[o] != 0.f) atomicAdd(dst + o * 64 + tid, v[o]);
-        };
-        if (HH == 2) add_rows(BT_DW4, gh + GH_W4, 64);
-        add_rows(BT_DW3, gh + GH_W3, 32);
-        add_rows(BT_DW1, gb + GB_W1, 32);
-        add_cols(BT_DW5T, gh + b.head_w5);
-        add_cols(BT_DW2T, gb + GB_W2);
+                for (int o = 0; o < 16; ++o)
+                    if (v[o] != 0.f) atomicAdd(dst + o * 64 + tid, v[o]);
+            };
+            if (HH == 2) add_rows(BT_DW4, gh + GH_W4, 64);
+            add_rows(BT_DW3, gh + GH_W3, 32);
+            add_rows(BT_DW1, gb + GB_W1, 32);
+            add_cols(BT_DW5T, gh + b.head_w5);
+            add_cols(BT_DW2T, gb + GB_W2);
+        }
     }
+    if (!ok) atomicOr(p.guard, 16);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -1071,11 +1178,11 @@ cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int h
         }
         const int grid = 2 * n_sms;
         if (head_hidden == 2) {
-            if (bf16) wf_net_bwd_tc_kernel<1, 2><<<grid, 128, tsmem, s>>>(p, b, it);
-            else wf_net_bwd_tc_kernel<0, 2><<<grid, 128, tsmem, s>>>(p, b, it);
+            if (bf16) wf_net_bwd_tc_kernel<1, 2><<<grid, BT_THREADS, tsmem, s>>>(p, b, it);
+            else wf_net_bwd_tc_kernel<0, 2><<<grid, BT_THREADS, tsmem, s>>>(p, b, it);
         } else {
-            if (bf16) wf_net_bwd_tc_kernel<1, 1><<<grid, 128, tsmem, s>>>(p, b, it);
-            else wf_net_bwd_tc_kernel<0, 1><<<grid, 128, tsmem, s>>>(p, b, it);
+            if (bf16) wf_net_bwd_tc_kernel<1, 1><<<grid, BT_THREADS, tsmem, s>>>(p, b, it);
+            else wf_net_bwd_tc_kernel<0, 1><<<grid, BT_THREADS, tsmem, s>>>(p, b, it);
         }
         return cudaGetLastError();
     }

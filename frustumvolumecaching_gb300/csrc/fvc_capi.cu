@@ -1738,25 +1738,17 @@ extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
         uint2 *&dst = variant ? g->d_w_bf16 : g->d_w;
         if ((rc = dalloc(&dst, P.size(), "backward weights"))) return rc;
         CU(cudaMemcpy(dst, P.data(), P.size() * sizeof(uint2), cudaMemcpyHostToDevice));
-        /* the tcgen05 kernel's B tiles: T[n][k] = W[n][k] (forward) or W[k][n] (input gradients) */
+        /* the tcgen05 kernel's weight tiles: each layer [out][in] K-major */
         std::vector<uint8_t> T(TB_BYTES, 0);
-        auto put = [&](const std::vector<uint16_t> &Wm, int cols, int N, int K, int off, bool tr) {
+        auto put = [&](const std::vector<uint16_t> &Wm, int N, int K, int off) {
             for (int n = 0; n < N; ++n)
-                for (int k = 0; k < K; ++k)
-                    memcpy(&T[off + kmajor_offset(n, k, K)], &Wm[tr ? (size_t)k * cols + n : (size_t)n * cols + k], 2);
+                for (int k = 0; k < K; ++k) memcpy(&T[off + kmajor_offset(n, k, K)], &Wm[(size_t)n * K + k], 2);
         };
-        put(W1, 32, 64, 32, TB_W1, false);
-        put(W2, 64, 16, 64, TB_W2, false);
-        put(W3, 32, 64, 32, TB_W3, false);
-        put(W5, 64, 64, 16, TB_W5T, true);
-        put(W3, 32, 16, 64, TB_W3T, true);
-        put(W2, 64, 64, 16, TB_W2T, true);
-        put(W1, 32, 32, 64, TB_W1T, true);
-        if (m->head_hidden == 2) {
-            const std::vector<uint16_t> W4 = cv(slice(m->h_head, 64 * 32, 64 * 64));
-            put(W4, 64, 64, 64, TB_W4, false);
-            put(W4, 64, 64, 64, TB_W4T, true);
-        }
+        put(W1, 64, 32, TB_W1);
+        put(W2, 16, 64, TB_W2);
+        put(W3, 64, 32, TB_W3);
+        put(W5, 16, 64, TB_W5);
+        if (m->head_hidden == 2) put(cv(slice(m->h_head, 64 * 32, 64 * 64)), 64, 64, TB_W4);
         uint8_t *&dt = variant ? g->d_wtc_bf16 : g->d_wtc;
         if ((rc = dalloc(&dt, T.size(), "backward weight tiles"))) return rc;
         CU(cudaMemcpy(dt, T.data(), T.size(), cudaMemcpyHostToDevice));

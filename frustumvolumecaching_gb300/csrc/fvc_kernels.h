@@ -206,21 +206,16 @@ constexpr int BW_TOTAL = BW_B1 + 4 * 4 * 32;
 constexpr int GB_W1 = 0, GB_W2 = 64 * 32, GB_BASE = GB_W2 + 16 * 64;
 constexpr int GH_W3 = 0, GH_W4 = 64 * 32;
 
-/* Weights of the tcgen05 backward kernel as canonical K-major B tiles (N x K,
- * bytes): the forward layers (B[n][k] = W[n][k]) and the input-gradient
- * layers (B[n][k] = W[k][n]); head layer 1 in the model's input order
- * [latents | SH | 1-padding], its transpose cut to the 16 input columns that
- * hold the latents. */
-constexpr int TB_W1 = 0;       /* N 64, K 32 */
-constexpr int TB_W2 = 4096;    /* N 16, K 64 */
-constexpr int TB_W3 = 6144;    /* N 64, K 32 */
-constexpr int TB_W4 = 10240;   /* N 64, K 64 */
-constexpr int TB_W5T = 18432;  /* N 64, K 16 */
-constexpr int TB_W4T = 20480;  /* N 64, K 64 */
-constexpr int TB_W3T = 28672;  /* N 16, K 64 */
-constexpr int TB_W2T = 30720;  /* N 64, K 16 */
-constexpr int TB_W1T = 32768;  /* N 32, K 64 */
-constexpr int TB_BYTES = 36864;
+/* Weights of the tcgen05 backward kernel: each layer W (out x in) once, as a
+ * canonical K-major tile [out][in] (bytes).  The forward MMAs read it as
+ * B^T = W^T; the input-gradient MMAs read the same tile MN-major as B = W.
+ * Head layer 1 in the model's input order [latents | SH | 1-padding]. */
+constexpr int TB_W1 = 0;       /* 64 x 32 */
+constexpr int TB_W2 = 4096;    /* 16 x 64 */
+constexpr int TB_W3 = 6144;    /* 64 x 32 */
+constexpr int TB_W4 = 10240;   /* 64 x 64 */
+constexpr int TB_W5 = 18432;   /* 16 x 64 */
+constexpr int TB_BYTES = 20480;
 
 struct BwdParams {
     const uint8_t *wtc;         /* TB_BYTES of K-major weight tiles (tcgen05 backward) */
