@@ -375,7 +375,8 @@ struct fvc_renderer {
     int kind = FVC_RENDERER_PERFORMANCE;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
-    cudaStream_t low_prio = nullptr;
+    cudaStream_t low_prio = nullptr;  /* the blockwise cache build's stream (lowest priority) */
+    cudaEvent_t build_after = nullptr; /* orders a build after the work queued on `stream` */
     int W = 0, H = 0;
     int *d_ctl = nullptr;             /* [0] ray counter, [1] guard */
     RenderStatsDev *d_stats = nullptr;
@@ -443,6 +444,7 @@ struct fvc_renderer {
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (own_stream) cudaStreamDestroy(own_stream);
         if (low_prio) cudaStreamDestroy(low_prio);
+        if (build_after) cudaEventDestroy(build_after);
     }
 };
 
@@ -980,6 +982,7 @@ extern "C" int fvc_renderer_create(fvc_model *m, int kind, fvc_renderer **out)
     int lo = 0, hi = 0;
     CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     CU(cudaStreamCreateWithPriority(&r->low_prio, cudaStreamNonBlocking, lo)); /* src/cache_renderer.cu:822-825 */
+    CU(cudaEventCreateWithFlags(&r->build_after, cudaEventDisableTiming));
     int rc;
     if ((rc = dalloc(&r->d_ctl, (size_t)4, "control words"))) return rc;
     if ((rc = dalloc(&r->d_stats, (size_t)1, "stats"))) return rc;
@@ -1413,7 +1416,14 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     const int n_tiles = c->bX * c->bY;
     if ((rc = ensure_build_scratch(r, n_tiles))) return rc;
     BuildScratch &b = r->bs;
-    cudaStream_t s = r->stream;
+    /* the build runs on the renderer's lowest-priority stream, as the
+     * reference's _low_priority_stream (src/cache_renderer.cu:937-1044), so a
+     * build called from another thread overlaps the renders on `stream`.  It
+     * first waits for the work already queued there, which may still read the
+     * cache being rebuilt; it returns once the build has finished. */
+    cudaStream_t s = r->low_prio;
+    CU(cudaEventRecord(r->build_after, r->stream));
+    CU(cudaStreamWaitEvent(s, r->build_after, 0));
 
     CacheBuildParams p;
     memset(&p, 0, sizeof(p));

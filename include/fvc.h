@@ -339,7 +339,13 @@ int fvc_cache_resize(fvc_renderer *r, int width, int height, const fvc_stepsize_
  * cache renderer and are ignored here, as in the reference. */
 int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_settings *s);
 /* initCacheBlockwise(RaymarchInfo, RenderBuffer&), src/cache_renderer.cu:931-1051:
- * fills the "next" cache. Synchronous. */
+ * fills the "next" cache. Synchronous: returns when the build has finished.
+ * It runs on the renderer's lowest-priority stream (the reference's
+ * _low_priority_stream) after the work already queued on the renderer's
+ * stream, under the write lock, so a build called from another thread
+ * overlaps the renders of the current cache (the viewer's double buffering,
+ * realtime_viewer/src/application.cu:168-184); fvc_cache_swap then waits for
+ * both locks. */
 int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info);
 /* initCache(RaymarchInfo, RenderBuffer&), src/cache_renderer.cu:848-928: the
  * per-ray fill of the "next" cache (each cache-camera ray marched to its
