@@ -289,7 +289,11 @@ struct fvc_model {
     DevScene dscene{};
     DevGrid grid{};
     int latent_offset = 1, n_latents = 8, head_hidden = 2;
+    int view_dependent = 0;                 /* split head with an initial view direction (mlp_first_head) */
     std::vector<uint16_t> h_base, h_head;  /* fp16 weight blobs in the model file layouts */
+    std::vector<uint16_t> h_first;         /* the first head's blob (view-dependent models) */
+    uint8_t *d_weights_vd = nullptr;        /* VD_WBYTES of K-major tiles (view-dependent models) */
+    uint2 *d_weights_fh = nullptr;          /* the first head as W_L1 / W_L2 fragment packs */
     uint8_t *d_bits = nullptr;
     __half2 *d_table = nullptr;
     uint2 *d_weights = nullptr;
@@ -301,7 +305,7 @@ struct fvc_model {
     ~fvc_model()
     {
         dfree(d_bits); dfree(d_table); dfree(d_weights); dfree(d_weights_tc); dfree(d_bias3);
-        dfree(d_weights_tc_bf16); dfree(d_weights_tc_fp8); dfree(d_fp8_iw);
+        dfree(d_weights_tc_bf16); dfree(d_weights_tc_fp8); dfree(d_fp8_iw); dfree(d_weights_vd); dfree(d_weights_fh);
     }
 };
 
@@ -346,8 +350,10 @@ struct BuildScratch {
     __half *den = nullptr;
     uint4 *lat = nullptr;
     int *row_of = nullptr;
+    float4 *dirs = nullptr;   /* per-row ray directions (view-dependent models) */
     void release()
     {
+        dfree(dirs);
         dfree(rays); dfree(block_step); dfree(tile_alive); dfree(alive_a); dfree(alive_b); dfree(counters);
         dfree(tile_n_samples); dfree(tile_processed); dfree(tile_need); dfree(tile_n_alive); dfree(jobs);
         dfree(rows); dfree(den); dfree(lat); dfree(row_of);
@@ -455,7 +461,7 @@ struct fvc_renderer {
  * four binary blobs: hash tables, density MLP, color head (fp16) and the
  * linear occupancy grid (uchar [cascade][x][y][z]). */
 static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char> &wb, std::vector<char> &wh,
-                       std::vector<char> &occ, fvc_model &m)
+                       std::vector<char> &occ, fvc_model &m, const std::vector<char> *wf = nullptr)
 {
     const JVal &sc = cfg["scene"];
     if (sc.kind != JVal::OBJ) return fail(FVC_ERR_CONFIG, "config.json: missing scene");
@@ -504,16 +510,37 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         return fail(FVC_ERR_CONFIG, "density network must be 32 -> 64 -> out (1 hidden layer of 64)");
     const int n_out = (int)base.num_or("n_output", 16);
     if (n_out < 1 || n_out > 16) return fail(FVC_ERR_CONFIG, "mlp_base.n_output must be 1..16");
-    const bool first_lat_dens = head.bool_or("first_latent_is_density", true);
+    /* the view-dependent split network (NerfNetwork::init_viewdep, include/nerf_network.h:120-158,
+     * loaded when the config has mlp_first_head, src/loader.cu:251-262): the latents come from a first
+     * head on [density outputs | SH of the initial view direction], and the color head reads
+     * [latents | SH | SH difference to the initial direction] */
+    const JVal &fh = cfg["mlp_first_head"];
+    m.view_dependent = fh.kind == JVal::OBJ;
+    const bool first_lat_dens = m.view_dependent ? fh.bool_or("first_latent_is_density", true)
+                                                 : head.bool_or("first_latent_is_density", true);
     m.latent_offset = first_lat_dens ? 0 : 1;
-    m.n_latents = (int)head.num_or("n_latents", n_out);
-    const int head_in = (int)head.num_or("n_input", 16 + m.n_latents);
+    m.n_latents = m.view_dependent ? (int)fh.num_or("n_output", 8) : (int)head.num_or("n_latents", n_out);
+    const int head_in = (int)head.num_or("n_input", (m.view_dependent ? 32 : 16) + m.n_latents);
     const int head_in_pad = (head_in + 15) / 16 * 16;
     m.head_hidden = (int)head["network"].num_or("n_hidden_layers", 2);
     if ((int)head["network"].num_or("n_neurons", 64) != 64) return fail(FVC_ERR_CONFIG, "head width must be 64");
     if (m.head_hidden < 1 || m.head_hidden > 2) return fail(FVC_ERR_CONFIG, "head must have 1 or 2 hidden layers");
-    if (m.latent_offset + m.n_latents > 16 || head_in != m.n_latents + 16 || head_in_pad != 32)
+    if (head.num_or("freq_encoding_degree", 0) != 0) return fail(FVC_ERR_CONFIG, "the head's frequency encoding is not built");
+    if (m.view_dependent) {
+        if ((int)fh["network"].num_or("n_neurons", 64) != 64 || (int)fh["network"].num_or("n_hidden_layers", 1) != 1)
+            return fail(FVC_ERR_CONFIG, "mlp_first_head must be 32 -> 64 -> n_output (1 hidden layer of 64)");
+        if (m.n_latents != 8 || m.latent_offset + m.n_latents > 16 || (n_out + 15) / 16 != 1 || (int)fh.num_or("n_input", 32) != 32)
+            return fail(FVC_ERR_CONFIG, "mlp_first_head must map the 16 density outputs and 16 SH values to 8 latents");
+        if (head_in != m.n_latents + 32 || head_in_pad != 48)
+            return fail(FVC_ERR_CONFIG, "a view-dependent head input must be n_latents + 16 SH + 16 SH differences padded to 48");
+        const JVal &fn = fh["encoding"]["nested"];
+        if (fn.kind == JVal::ARR && fn.arr.size() && (int)fn.arr[0].num_or("degree", 4) != 4)
+            return fail(FVC_ERR_CONFIG, "only SH degree 4 direction encoding is built");
+        if (!wf) return fail(FVC_ERR_IO, "missing mlp_first_head.dat");
+        if (wf->size() != (size_t)(64 * 32 + 16 * 64) * 2) return fail(FVC_ERR_IO, "mlp_first_head.dat has the wrong size");
+    } else if (m.latent_offset + m.n_latents > 16 || head_in != m.n_latents + 16 || head_in_pad != 32) {
         return fail(FVC_ERR_CONFIG, "head input must be n_latents + 16 SH values padded to 32");
+    }
     const JVal &nested = head["encoding"]["nested"];
     if (nested.kind == JVal::ARR && nested.arr.size() && (int)nested.arr[0].num_or("degree", 4) != 4)
         return fail(FVC_ERR_CONFIG, "only SH degree 4 direction encoding is built");
@@ -542,7 +569,7 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         return fail(FVC_ERR_IO, "pos_enc.dat: " + std::to_string(tab.size()) + " bytes, hash grid needs " + std::to_string((size_t)off * F * 2));
     const int base_out_pad = (n_out + 15) / 16 * 16;
     if (wb.size() != (size_t)(64 * 32 + base_out_pad * 64) * 2) return fail(FVC_ERR_IO, "mlp_base.dat has the wrong size");
-    if (wh.size() != (size_t)(64 * 32 + (m.head_hidden - 1) * 64 * 64 + 16 * 64) * 2) return fail(FVC_ERR_IO, "mlp_head.dat has the wrong size");
+    if (wh.size() != (size_t)(64 * head_in_pad + (m.head_hidden - 1) * 64 * 64 + 16 * 64) * 2) return fail(FVC_ERR_IO, "mlp_head.dat has the wrong size");
     const size_t vals = (size_t)128 * 128 * 128;
     if (occ.size() != vals * s.grid_nlvl) return fail(FVC_ERR_IO, "occupancy_grid.dat has the wrong size");
 
@@ -578,7 +605,8 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
     std::vector<uint16_t> h0 = u16(wh, 0, 64 * 32);
     std::vector<uint16_t> l3(64 * 32, 0);
     std::vector<float> bias3(64, 0.f);
-    for (int n = 0; n < 64; ++n) {
+    /* the 32-wide head input layout; a view-dependent model uses its own tiles (below) instead */
+    for (int n = 0; n < 64 && !m.view_dependent; ++n) {
         for (int k = 0; k < 16; ++k) {
             const int src = k - m.latent_offset;
             if (src >= 0 && src < m.n_latents) l3[n * 32 + k] = h0[n * 32 + src];
@@ -646,6 +674,39 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         CU(cudaMemcpy(m.d_fp8_iw, iw, sizeof(iw), cudaMemcpyHostToDevice));
     }
 
+    /* the view-dependent network: the first head as fragment packs (the cache build's density kernel)
+     * and every layer as K-major tiles (the tcgen05 network kernel); its color head keeps the model's
+     * input order and reads the 1-padding through its weights */
+    if (m.view_dependent) {
+        m.h_first = u16(*wf, 0, wf->size() / 2);
+        std::vector<uint2> Wf(W_L3, make_uint2(0, 0));
+        frag_pack(u16(*wf, 0, 64 * 32), 64, 32, &Wf[W_L1]);
+        frag_pack(u16(*wf, 64 * 32, 16 * 64), 16, 64, &Wf[W_L2]);
+        std::vector<uint8_t> Wv(VD_WBYTES, 0);
+        auto vd_pack = [&](const std::vector<uint16_t> &M, int N, int K, int off) {
+            for (int n = 0; n < N; ++n)
+                for (int k = 0; k < K; ++k) memcpy(&Wv[off + kmajor_offset(n, k, K)], &M[(size_t)n * K + k], 2);
+        };
+        vd_pack(u16(wb, 0, 64 * 32), 64, 32, VD_B1);
+        std::vector<uint16_t> w2 = u16(wb, 64 * 32, (size_t)base_out_pad * 64);
+        w2.resize(16 * 64, 0);
+        vd_pack(w2, 16, 64, VD_B2);
+        vd_pack(u16(*wf, 0, 64 * 32), 64, 32, VD_F1);
+        vd_pack(u16(*wf, 64 * 32, 16 * 64), 16, 64, VD_F2);
+        vd_pack(u16(wh, 0, 64 * 48), 64, 48, VD_B3);
+        size_t vo = 64 * 48;
+        if (m.head_hidden == 2) {
+            vd_pack(u16(wh, vo, 64 * 64), 64, 64, VD_B4);
+            vo += 64 * 64;
+        }
+        vd_pack(u16(wh, vo, 16 * 64), 16, 64, VD_B5);
+        int rc;
+        if ((rc = dalloc(&m.d_weights_fh, Wf.size(), "first-head weights"))) return rc;
+        if ((rc = dalloc(&m.d_weights_vd, (size_t)VD_WBYTES, "view-dependent weights"))) return rc;
+        CU(cudaMemcpy(m.d_weights_fh, Wf.data(), Wf.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.d_weights_vd, Wv.data(), VD_WBYTES, cudaMemcpyHostToDevice));
+    }
+
     /* device scene block */
     DevScene &d = m.dscene;
     d.aabb_from = make_float3(s.aabb_from.x, s.aabb_from.y, s.aabb_from.z);
@@ -688,7 +749,10 @@ static int load_nerfacc(const std::string &dir, fvc_model &m)
     if (!read_file(dir + "/mlp_base.dat", wb)) return fail(FVC_ERR_IO, "missing mlp_base.dat");
     if (!read_file(dir + "/mlp_head.dat", wh)) return fail(FVC_ERR_IO, "missing mlp_head.dat");
     if (!read_file(dir + "/occupancy_grid.dat", occ)) return fail(FVC_ERR_IO, "missing occupancy_grid.dat");
-    return build_model(cfg, tab, wb, wh, occ, m);
+    std::vector<char> wf;
+    const bool vd = cfg["mlp_first_head"].kind == JVal::OBJ;
+    if (vd && !read_file(dir + "/mlp_first_head.dat", wf)) return fail(FVC_ERR_IO, "missing mlp_first_head.dat");
+    return build_model(cfg, tab, wb, wh, occ, m, vd ? &wf : nullptr);
 }
 
 /* load_ingp_snapshot (src/loader.cu:146-230): the scene, step grid and
@@ -956,7 +1020,8 @@ extern "C" int fvc_model_density(fvc_model *m, const float *pos, int n, float *l
 
 extern "C" int fvc_model_inference(fvc_model *m, const float *pos, const float *dir01, int n, float *out)
 {
-    CHECK_ARG(dir01 && out, "fvc_model_inference: null argument");
+    CHECK_ARG(m && dir01 && out, "fvc_model_inference: null argument");
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     return run_inference(m, pos, dir01, n, out, nullptr, nullptr);
 }
 
@@ -1117,6 +1182,10 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.tc_fp8_iw = m->d_fp8_iw;
     if (r->precision != FVC_PRECISION_FP16 && (cached || !r->use_tc))
         return fail(FVC_ERR_CONFIG, "BF16 and FP8 MLPs are built for the plain renderers on the tcgen05 network path");
+    if (m->view_dependent && (!r->use_tc || r->precision != FVC_PRECISION_FP16 || r->kind == FVC_RENDERER_CACHE_BASIC || per_view_caches))
+        return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    p.view_dependent = m->view_dependent;
+    p.weights_vd = m->d_weights_vd;
     p.latent_offset = m->latent_offset;
     p.basic_cache = r->kind == FVC_RENDERER_CACHE_BASIC;
     p.ray_counter = r->d_ctl; p.guard = r->d_ctl + 1; p.stats = r->d_stats;
@@ -1430,6 +1499,12 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     p.scene = m->dscene; p.steps = dev_steps(info->stepsize_info); p.cam = dev_cam(info->cam_info); p.grid = m->grid;
     p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.latent_offset = m->latent_offset;
     p.variant = r->settings.interpol_variant;
+    p.view_dependent = m->view_dependent;
+    p.weights_fh = m->d_weights_fh;
+    if (m->view_dependent) {
+        if (!b.dirs && (rc = dalloc(&b.dirs, (size_t)n_tiles * 512, "build ray directions"))) return rc;
+        p.build_dirs = b.dirs;
+    }
     p.bX = c->bX; p.bY = c->bY; p.bZ = c->bZ; p.fW = c->fW; p.fH = c->fH; p.fD = c->fD;
     p.dX = c->dX; p.dY = c->dY; p.dZ = c->dZ; p.capacity = c->capacity();
     p.rays = b.rays; p.block_step = b.block_step; p.tile_alive = b.tile_alive;
@@ -1506,6 +1581,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
 {
     CHECK_ARG(r && info, "fvc_cache_build_per_ray: null argument");
     CHECK_ARG(r->next, "fvc_cache_build_per_ray: caches not attached (fvc_renderer_set_caches)");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     int rc;
     if ((rc = check_info(info))) return rc;
     fvc_model *m = r->m;
@@ -1636,6 +1712,7 @@ extern "C" int fvc_cache_read(fvc_cache *c, int32_t *packed, size_t *packed_n, f
 namespace fvc_internal {
 int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms)
 {
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     p->scene = m->dscene;
     p->grid = m->grid;
     p->bits = m->d_bits;
@@ -1689,6 +1766,7 @@ extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
 {
     CHECK_ARG(m && out, "fvc_grad_create: null argument");
     *out = nullptr;
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "the adjoint is built for networks without the view-dependent split head");
     if (m->n_latents != 8 || m->grid.n_levels != 16)
         return fail(FVC_ERR_CONFIG, "the backward kernels are built for 16 hash levels and 8 latents");
     auto g = std::make_unique<fvc_grad>();
@@ -1993,6 +2071,7 @@ static int batch_launch(fvc_renderer *r, const RenderParams &p, int n_rays)
 extern "C" int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out)
 {
     CHECK_ARG(r, "fvc_render_batch: null renderer");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     RenderParams p;
     int n_rays = 0, rc;
@@ -2004,6 +2083,7 @@ extern "C" int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info 
                                        const fvc_render_outputs *out)
 {
     CHECK_ARG(r && caches, "fvc_render_batch_cached: null argument");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     RenderParams p;
     int n_rays = 0, rc;
@@ -2015,6 +2095,7 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
                                      fvc_autotune_result *res)
 {
     CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the plain, basic and cached performance renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     const int tiles[2] = {128, 32};        /* tcgen05 CTA tile, mma.sync warp tile */
     const int steps[4] = {16, 32, 64, 128}; /* marching steps per ray and sub-iteration */

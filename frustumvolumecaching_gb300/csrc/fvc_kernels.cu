@@ -210,6 +210,8 @@ __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
             if ((mask >> s) & 1u) {
                 const float3 cp = contract(p.scene, at(cr.o, cr.d, tm));
                 p.build_rows[row] = make_float4(cp.x, cp.y, cp.z, 0.f);
+                if (p.view_dependent) /* the build's network input direction (src/cache_renderer.cu:1026) */
+                    p.build_dirs[row] = make_float4((cr.d.x + 1.0f) / 2.0f, (cr.d.y + 1.0f) / 2.0f, (cr.d.z + 1.0f) / 2.0f, 0.f);
                 rof[s * 64 + k] = row++;
             } else {
                 rof[s * 64 + k] = -1;
@@ -222,9 +224,11 @@ __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
  * latents (fp16, as NerfNetwork::inferenceLatents stores them) */
 __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
 {
-    __shared__ uint2 Wsm[W_L3];
+    __shared__ uint2 Wsm[W_L3], Wfh[W_L3];
     __shared__ __align__(16) __half tiles[4][32 * TILE_STRIDE];
     for (int i = threadIdx.x; i < W_L3; i += blockDim.x) Wsm[i] = p.weights[i];
+    if (p.view_dependent)
+        for (int i = threadIdx.x; i < W_L3; i += blockDim.x) Wfh[i] = p.weights_fh[i];
     __syncthreads();
     const int n = *p.build_row_counter;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -241,6 +245,31 @@ __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
         }
         __syncwarp();
         density_mlp(tile, Wsm, lane);
+        __half logd = trow[16];
+        if (p.view_dependent) {
+            /* the first head (NerfNetwork::inferenceLatents, include/nerf_network.h:183-197) on
+             * [density outputs | SH of the build ray's direction]; its outputs take rows 1.. of the
+             * head input (row 0 keeps the log-density) */
+            uint4 o0 = reinterpret_cast<const uint4 *>(trow + 16)[0], o1 = reinterpret_cast<const uint4 *>(trow + 16)[1];
+            __half2 sh[8];
+            if (r < n) {
+                const float4 d = p.build_dirs[r];
+                sh16(make_float3(d.x, d.y, d.z), sh);
+            } else {
+                for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+            }
+            __syncwarp();
+            reinterpret_cast<uint4 *>(trow)[0] = o0;
+            reinterpret_cast<uint4 *>(trow)[1] = o1;
+            reinterpret_cast<uint4 *>(trow)[2] = *reinterpret_cast<const uint4 *>(sh);
+            reinterpret_cast<uint4 *>(trow)[3] = *reinterpret_cast<const uint4 *>(sh + 4);
+            __syncwarp();
+            density_mlp(tile, Wfh, lane); /* the same 32 -> 64 -> 16 shape */
+            /* rows 1..16 <- first-head outputs 0..15 */
+            __syncwarp();
+            for (int j = 15; j >= 1; --j) trow[16 + j] = trow[16 + j - 1];
+            trow[16] = logd;
+        }
         if (r < n) {
             p.build_den[r] = trow[16];
             uint32_t lw[4];

@@ -49,6 +49,19 @@ constexpr int TC_B3 = 6144;     /* 64 x 32 */
 constexpr int TC_B4 = 10240;    /* 64 x 64 */
 constexpr int TC_B5 = 18432;    /* 16 x 64 */
 constexpr int TC_WBYTES = 20480;
+/* the view-dependent split network (NerfNetwork::init_viewdep,
+ * include/nerf_network.h:120-158) as K-major tiles: density MLP, first head
+ * ([density outputs | SH of the initial direction] 32 -> 64 -> 16 latent
+ * rows), color head whose input is [latents 8 | SH 16 | SH difference 16 |
+ * 1-padding 8] (K = 48) */
+constexpr int VD_B1 = 0;        /* 64 x 32 */
+constexpr int VD_B2 = 4096;     /* 16 x 64 */
+constexpr int VD_F1 = 6144;     /* 64 x 32 */
+constexpr int VD_F2 = 10240;    /* 16 x 64 */
+constexpr int VD_B3 = 12288;    /* 64 x 48 */
+constexpr int VD_B4 = 18432;    /* 64 x 64 */
+constexpr int VD_B5 = 26624;    /* 16 x 64 */
+constexpr int VD_WBYTES = 28672;
 /* the same in e4m3 (8-bit K-major tiles) for the FP8 network */
 constexpr int TC8_B1 = 0, TC8_B2 = 2048, TC8_B3 = 3072, TC8_B4 = 5120, TC8_B5 = 9216, TC8_WBYTES = 10240;
 
@@ -168,6 +181,8 @@ struct RenderParams {
     int row_capacity;           /* rows per sub-iteration */
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
     int basic_cache;            /* 1: CacheBasicRenderer semantics for the cached rows (classify_basic) */
+    int view_dependent;         /* split head (mlp_first_head): first head + SH-difference head input */
+    const uint8_t *weights_vd;  /* VD_WBYTES of K-major tiles of the view-dependent network */
     /* batched views: rays of n_views cameras (device array), view v's pixel
      * (x, y) at ray id view_off[v] + y * W_v + x; view_off[n_views] = rays;
      * a ray's view is in its state's cnt2.w.  With view_caches, each view
@@ -260,6 +275,9 @@ struct CacheBuildParams {
     const uint2 *weights;
     int latent_offset;
     int variant;                /* CacheSettings::interpol_variant: what the voxels' density and latent 0 hold */
+    int view_dependent;         /* latents from the first head on the build ray's direction */
+    const uint2 *weights_fh;    /* the first head's W_L1 / W_L2 fragment packs */
+    float4 *build_dirs;         /* per build row: unit_to_01 of its ray direction (view-dependent models) */
     int bX, bY, bZ, fW, fH, fD, dX, dY, dZ, capacity;
     CacheRay *rays;             /* [tiles][64] */
     int *block_step;            /* [tiles] */

@@ -567,6 +567,14 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                     const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
                     p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
                     cache_lookup(C, fr, logd, lat);
+                    if (p.view_dependent) {
+                        /* the initial view direction of a cache row: from the cache camera to the sample,
+                         * unit_to_01 (src/cache_performance_renderer.cu:290-312); the head reads it */
+                        const float3 wp = at(o, d, tmh);
+                        const float vx = wp.x - ccam.c2w[3], vy = wp.y - ccam.c2w[7], vz = wp.z - ccam.c2w[11];
+                        const float inv = rsqrtf(vx * vx + vy * vy + vz * vz);
+                        p.row_pay[r] = make_float4((vx * inv + 1.0f) / 2.0f, (vy * inv + 1.0f) / 2.0f, (vz * inv + 1.0f) / 2.0f, 0.f);
+                    }
                 }
             }
             p.row_kind[r] = (uint8_t)kind;
@@ -1304,6 +1312,171 @@ __global__ void wf_reset_rows_kernel(RenderParams p, int cached)
 /* ------------------------------------------------------------------------- */
 /* host side                                                                 */
 /* ------------------------------------------------------------------------- */
+/* ------------------------------------------------------------------------- */
+/* the view-dependent split network on tcgen05                               */
+/* ------------------------------------------------------------------------- */
+/* NerfNetwork::init_viewdep / inferenceLatents / inferenceHead
+ * (include/nerf_network.h:120-158,173-266) for models with mlp_first_head.
+ * The layer structure, TMEM use (64 columns), waits and guard are those of
+ * wf_net_tc_kernel, with:
+ *   - resample rows (MODE 0): after the density network, the first head on
+ *     [density outputs 16 | SH of the initial direction 16] (32 -> 64 -> 16);
+ *     its outputs take the head-input rows 1..16, row 0 keeps the
+ *     log-density.  The initial direction of a resample row is its own, so
+ *     the SH difference is zero (the reference clears that buffer when both
+ *     inputs are the same matrix);
+ *   - cache rows (MODE 1): the looked-up latents, and the SH difference
+ *     between the ray direction and the cache camera's direction to the
+ *     sample (written by the classification into the row payload), rounded
+ *     to fp16 and subtracted in fp16 as the reference's sub kernel;
+ *   - the color head's input [latents 8 | SH 16 | SH difference 16 |
+ *     1-padding 8] as one K = 48 tile; the padding columns of its weights
+ *     give the bias.
+ * 45 KB of shared memory: four CTAs per SM. */
+struct __align__(128) VdSmem {
+    uint8_t W[VD_WBYTES];
+    uint8_t X[128 * 64 * 2];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ bool vd_run(VdSmem &S, uint32_t tmem, const uint8_t *b, int K, int N, uint32_t &phase)
+{
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        tc_layer(tmem, S.X, b, K, N);
+        tc_commit(&S.mbar);
+    }
+    const bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+template <int MODE, int HH, bool LIST>
+__global__ void __launch_bounds__(128, 4) wf_net_vd_kernel(RenderParams p, int it)
+{
+    extern __shared__ __align__(128) unsigned char vd_smem_raw[];
+    VdSmem &S = *reinterpret_cast<VdSmem *>(vd_smem_raw);
+    const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : p.counters[4];
+    if (n_rows == 0) return;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&S.mbar, 1);
+        mbar_arrive_expect_tx(&S.mbar, VD_WBYTES);
+        bulk_copy_g2s(S.W, p.weights_vd, VD_WBYTES, &S.mbar);
+    }
+    if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const RayState *states = p.states[it & 1];
+    const int lo = p.latent_offset;
+    uint32_t phase = 0;
+    bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    const int n_tiles = (n_rows + 127) / 128;
+    const uint32_t one2 = pack_h2(1.0f, 1.0f);
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int k = tile * 128 + tid;
+        const int r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : p.cache_list[k]) : -1;
+        __half2 sh[8];
+        if (r >= 0) sh16(dir01_of(states, p.row_slot[r]), sh);
+        else for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+        uint16_t log_density = 0;
+        uint4 lat = make_uint4(0u, 0u, 0u, 0u), diff0 = make_uint4(0u, 0u, 0u, 0u), diff1 = make_uint4(0u, 0u, 0u, 0u);
+        if (MODE == 0) {
+            /* ---- hash features -> tile (K = 32) ---- */
+            __half2 feat[16];
+            if (r >= 0) {
+                const float4 pw = p.row_pay[r];
+                hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
+            } else {
+                for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
+            if (!(ok = tc_publish(ok))) break;
+            ok = vd_run(S, tmem, S.W + VD_B1, 32, 64, phase);
+            epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+            if (!(ok = tc_publish(ok))) break;
+            /* ---- density outputs (16, fp16) ---- */
+            ok = vd_run(S, tmem, S.W + VD_B2, 64, 16, phase);
+            float v[16];
+            tmem_ld16(tmem + lane_base, v);
+            tmem_wait_ld();
+            const uint4 b0 = pack8(v), b1 = pack8(v + 8);
+            log_density = (uint16_t)(b0.x & 0xffffu);
+            /* ---- first head on [density outputs | SH of the initial direction] ---- */
+            st_chunk(S.X, tid, 0, 32, b0);
+            st_chunk(S.X, tid, 1, 32, b1);
+            st_chunk(S.X, tid, 2, 32, *reinterpret_cast<const uint4 *>(sh));
+            st_chunk(S.X, tid, 3, 32, *reinterpret_cast<const uint4 *>(sh + 4));
+            if (!(ok = tc_publish(ok))) break;
+            ok = vd_run(S, tmem, S.W + VD_F1, 32, 64, phase);
+            epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+            if (!(ok = tc_publish(ok))) break;
+            ok = vd_run(S, tmem, S.W + VD_F2, 64, 16, phase);
+            float f[16];
+            tmem_ld16(tmem + lane_base, f);
+            tmem_wait_ld();
+            /* head-input rows lo .. lo + 7: row 0 the log-density, rows 1.. the first head's outputs */
+            float lv[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) lv[j] = lo ? f[j] : (j == 0 ? __half2float(__ushort_as_half(log_density)) : f[j - 1]);
+            lat = pack8(lv);
+        } else {
+            /* ---- looked-up latents and the SH difference to the cache camera's direction ---- */
+            if (r >= 0) {
+                lat = p.row_lat[k];
+                const uint32_t ld = p.row_out[r].y >> 16;
+                log_density = (uint16_t)(lo == 0 ? (lat.x & 0xffffu) : ld);
+                const float4 iv = p.row_pay[r];
+                __half2 shi[8], df[8];
+                sh16(make_float3(iv.x, iv.y, iv.z), shi);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) df[q] = __hsub2(sh[q], shi[q]);
+                diff0 = *reinterpret_cast<const uint4 *>(df);
+                diff1 = *reinterpret_cast<const uint4 *>(df + 4);
+            }
+        }
+        /* ---- color head input [latents | SH | SH difference | 1-padding] (K = 48) ---- */
+        st_chunk(S.X, tid, 0, 48, lat);
+        st_chunk(S.X, tid, 1, 48, *reinterpret_cast<const uint4 *>(sh));
+        st_chunk(S.X, tid, 2, 48, *reinterpret_cast<const uint4 *>(sh + 4));
+        st_chunk(S.X, tid, 3, 48, diff0);
+        st_chunk(S.X, tid, 4, 48, diff1);
+        st_chunk(S.X, tid, 5, 48, make_uint4(one2, one2, one2, one2));
+        if (!(ok = tc_publish(ok))) break;
+        ok = vd_run(S, tmem, S.W + VD_B3, 48, 64, phase);
+        epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+        if (!(ok = tc_publish(ok))) break;
+        if (HH == 2) {
+            ok = vd_run(S, tmem, S.W + VD_B4, 64, 64, phase);
+            epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+            if (!(ok = tc_publish(ok))) break;
+        }
+        ok = vd_run(S, tmem, S.W + VD_B5, 64, 16, phase);
+        float o[16];
+        tmem_ld16(tmem + lane_base, o);
+        tmem_wait_ld();
+        if (r >= 0)
+            p.row_out[r] = make_uint2(pack_h2(o[0], o[1]),
+                                      (uint32_t)__half_as_ushort(__float2half_rn(o[2])) | ((uint32_t)log_density << 16));
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+    }
+    if (!ok && tid == 0) atomicOr(p.guard, 16);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TC_COLS);
+    }
+}
+
 template <int HH>
 static cudaError_t set_net_attrs()
 {
@@ -1317,6 +1490,10 @@ static cudaError_t set_net_attrs()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<1, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<2, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    const int vsmem = (int)sizeof(VdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_vd_kernel<0, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, vsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_vd_kernel<0, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, vsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_vd_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, vsmem);
     return e;
 }
 
@@ -1326,7 +1503,8 @@ static void launch_plain_net(const RenderParams &p, int it, int n_sms, cudaStrea
 {
     const size_t tc_smem = sizeof(TcSmem);
     const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
-    if (!p.use_tc) wf_net_resample_kernel<HH, false><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
+    if (p.view_dependent) wf_net_vd_kernel<0, HH, false><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
+    else if (!p.use_tc) wf_net_resample_kernel<HH, false><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
     else if (p.precision == 1) wf_net_tc_prec_kernel<1, HH><<<n_sms * TC_PREC_CTAS_PER_SM, 128, tc_smem, s>>>(p, it);
     else if (p.precision == 2) wf_net_tc_prec_kernel<2, HH><<<n_sms * TC_PREC_CTAS_PER_SM, 128, tc_smem, s>>>(p, it);
     else wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
@@ -1369,10 +1547,12 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
         if (CACHED) {
             wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
             timed_begin();
-            if (p.use_tc) wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            if (p.view_dependent) wf_net_vd_kernel<0, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
+            else if (p.use_tc) wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
             else wf_net_resample_kernel<HH, true><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
             timed_end();
-            if (p.use_tc) wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            if (p.view_dependent) wf_net_vd_kernel<1, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
+            else if (p.use_tc) wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
             else wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
             L.launches += 3;
         } else {

@@ -182,6 +182,7 @@ class ModelSpec:
     table_range: float = 1e-2
     occupancy_fraction: float = 0.12
     occupancy_cascades: str = "all"     # "all": threshold every cascade; "inner": outer cascades empty
+    view_dependent: bool = False        # split head (mlp_first_head): latents from a first head on an initial direction
 
 
 def spec_config1() -> ModelSpec:
@@ -240,7 +241,9 @@ class SyntheticModel:
         self.n_base_out = n_out
         self.base = [_xavier(rng, spec.width, enc_w, spec.width, _pad16(enc_w)),
                      _xavier(rng, n_out, spec.width, _pad16(n_out), spec.width)]
-        head_in = spec.n_latents + 16
+        # the head reads [latents | SH of the direction (16)], and a view-dependent head also the SH
+        # difference to the initial direction (16) (include/nerf_network.h:204-257)
+        head_in = spec.n_latents + (32 if spec.view_dependent else 16)
         self.head_in = head_in
         head_in_pad = _pad16(head_in)
         hl = [_xavier(rng, spec.width, head_in, spec.width, head_in_pad)]
@@ -248,6 +251,9 @@ class SyntheticModel:
             hl.append(_xavier(rng, spec.width, spec.width, spec.width, spec.width))
         hl.append(_xavier(rng, 3, spec.width, 16, spec.width))
         self.head = hl
+        # the first head: [density outputs (16) | SH of the initial direction (16)] -> 64 -> n_latents
+        self.first = ([_xavier(rng, spec.width, 32, spec.width, 32), _xavier(rng, spec.n_latents, spec.width, 16, spec.width)]
+                      if spec.view_dependent else None)
         self.occupancy = None
 
     # -- evaluation (float64 with fp16 rounding of layer outputs like tcnn) --
@@ -314,17 +320,21 @@ class SyntheticModel:
         net = {"otype": "FullyFusedMLP", "activation": "ReLU", "output_activation": "None",
                "n_neurons": s.width, "n_hidden_layers": 1}
         head_net = dict(net, n_hidden_layers=s.head_hidden_layers)
-        return {
+        sh_enc = {"otype": "Composite", "nested": [{"otype": "SphericalHarmonics", "degree": 4, "n_dims_to_encode": 3}]}
+        out = {
             "scene": scene,
             "mlp_base": {"encoding": enc, "network": net, "n_output": self.n_base_out},
-            "mlp_head": {"encoding": {"otype": "Composite", "nested": [
-                {"otype": "SphericalHarmonics", "degree": 4, "n_dims_to_encode": 3}]},
+            "mlp_head": {"encoding": sh_enc,
                 "network": head_net, "n_input": self.head_in, "n_latents": s.n_latents,
                 "first_latent_is_density": s.first_latent_is_density},
             "synthetic": {"seed": s.seed, "name": s.name, "occupancy_fraction": s.occupancy_fraction,
                           "table_range": s.table_range,
                           "hashmap_sizes": [lv.size for lv in self.levels]},
         }
+        if s.view_dependent:  # loaded by NerfNetwork::init_viewdep (src/loader.cu:251-262)
+            out["mlp_first_head"] = {"encoding": sh_enc, "network": dict(net), "n_input": 32, "n_output": s.n_latents,
+                                     "first_latent_is_density": s.first_latent_is_density}
+        return out
 
     def write(self, out_dir: str) -> str:
         os.makedirs(out_dir, exist_ok=True)
@@ -335,6 +345,8 @@ class SyntheticModel:
         self.table.tofile(os.path.join(out_dir, "pos_enc.dat"))
         np.concatenate([w.ravel() for w in self.base]).tofile(os.path.join(out_dir, "mlp_base.dat"))
         np.concatenate([w.ravel() for w in self.head]).tofile(os.path.join(out_dir, "mlp_head.dat"))
+        if self.first is not None:
+            np.concatenate([w.ravel() for w in self.first]).tofile(os.path.join(out_dir, "mlp_first_head.dat"))
         self.occupancy.tofile(os.path.join(out_dir, "occupancy_grid.dat"))
         return out_dir
 
@@ -344,7 +356,8 @@ def default_model_root() -> str:
 
 
 def model_dir_name(spec: ModelSpec) -> str:
-    return f"{spec.name}_s{spec.seed}_T{spec.log2_T}_n{spec.grid_nlvl}_o{int(round(spec.occupancy_fraction * 1000))}{spec.occupancy_cascades}"
+    vd = "_vd" if spec.view_dependent else ""
+    return f"{spec.name}_s{spec.seed}_T{spec.log2_T}_n{spec.grid_nlvl}_o{int(round(spec.occupancy_fraction * 1000))}{spec.occupancy_cascades}{vd}"
 
 
 def ensure_model(spec: ModelSpec, root: str | None = None) -> str:

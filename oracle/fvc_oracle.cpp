@@ -60,6 +60,8 @@ struct OrcNet {
     int head_in, head_in_pad, n_latents, latent_offset;
     const uint16_t *head_w;  /* [width x head_in_pad], [width x width]*, [16 x width] */
     int mimic_fp16;          /* round layer outputs to fp16 like the reference */
+    int view_dependent;      /* split head (mlp_first_head, include/nerf_network.h:120-158) */
+    const uint16_t *first_w; /* the first head: [width x 32], [16 x width] */
 };
 }
 
@@ -237,7 +239,7 @@ inline V3 cam2froxel(V3 c, const OrcCam &cam, const OrcSteps &st, float &t)
 /* ---------------- network (float64) ---------------- */
 struct NetD {
     const OrcNet *n;
-    std::vector<double> table, bw0, bw1, hw[4];
+    std::vector<double> table, bw0, bw1, hw[4], fw0, fw1;
 };
 
 void prepare_net(const OrcNet *n, NetD &d)
@@ -257,6 +259,12 @@ void prepare_net(const OrcNet *n, NetD &d)
         d.hw[l].resize((size_t)in * out);
         for (size_t i = 0; i < d.hw[l].size(); ++i) d.hw[l][i] = h2d(n->head_w[off + i]);
         off += (size_t)in * out;
+    }
+    if (n->view_dependent) {
+        d.fw0.resize((size_t)n->width * 32);
+        d.fw1.resize((size_t)16 * n->width);
+        for (size_t i = 0; i < d.fw0.size(); ++i) d.fw0[i] = h2d(n->first_w[i]);
+        for (size_t i = 0; i < d.fw1.size(); ++i) d.fw1[i] = h2d(n->first_w[d.fw0.size() + i]);
     }
 }
 
@@ -310,14 +318,28 @@ inline void dense_layer(const double *W, int out, int in, const double *x, doubl
     }
 }
 
-/* density network: NerfNetwork::inferenceLatents, include/nerf_network.h:173-202 */
-void base_forward(const NetD &d, V3 pos, double *out /* base_out_pad */)
+void sh16(const float *d01, double *o);
+
+/* density network: NerfNetwork::inferenceLatents, include/nerf_network.h:173-202.
+ * A view-dependent network then runs its first head on [density outputs |
+ * SH of the initial direction init01] (:183-197); the first head's outputs
+ * take rows 1.. of out, row 0 keeps the log-density. */
+void base_forward(const NetD &d, V3 pos, double *out /* base_out_pad */, const float *init01 = nullptr)
 {
     const OrcNet &n = *d.n;
     double feat[64], h[128];
     hash_encode(d, pos, feat);
     dense_layer(d.bw0.data(), n.width, n.enc_w_pad, feat, h, true, n.mimic_fp16);
     dense_layer(d.bw1.data(), n.base_out_pad, n.width, h, out, false, n.mimic_fp16);
+    if (n.view_dependent && init01) {
+        double in[32], hf[128], o[16];
+        for (int i = 0; i < 16; ++i) in[i] = out[i];
+        sh16(init01, in + 16);
+        if (n.mimic_fp16) for (int i = 16; i < 32; ++i) in[i] = round_h(in[i]);
+        dense_layer(d.fw0.data(), n.width, 32, in, hf, true, n.mimic_fp16);
+        dense_layer(d.fw1.data(), 16, n.width, hf, o, false, n.mimic_fp16);
+        for (int i = 1; i < 16; ++i) out[i] = o[i - 1];
+    }
 }
 
 /* SH degree 4 of unit_to_01 directions: x = 2*d01 - 1 (the constants of
@@ -340,14 +362,25 @@ void sh16(const float *d01, double *o)
 }
 
 /* color head: NerfNetwork::inferenceHead, include/nerf_network.h:204-257
- * (latents, SH4 of the direction, padding with 1.0 to the padded width) */
-void head_forward(const NetD &d, const double *latents, const float *dir01, double *rgb_logits)
+ * (latents, SH4 of the direction, padding with 1.0 to the padded width).  A
+ * view-dependent head also reads SH(dir) - SH(init01), fp16 operands
+ * subtracted in fp16 (nerf_network.h:47-52,226-240); without init01 (the
+ * row's own direction) that input is zero. */
+void head_forward(const NetD &d, const double *latents, const float *dir01, double *rgb_logits, const float *init01 = nullptr)
 {
     const OrcNet &n = *d.n;
     double in[128], a[128], b[128];
     for (int i = 0; i < n.n_latents; ++i) in[i] = latents[i];
     sh16(dir01, in + n.n_latents);
     if (n.mimic_fp16) for (int i = n.n_latents; i < n.n_latents + 16; ++i) in[i] = round_h(in[i]);
+    if (n.view_dependent) {
+        double shi[16];
+        if (init01) sh16(init01, shi);
+        for (int i = 0; i < 16; ++i) {
+            const double s0 = in[n.n_latents + i];
+            in[n.n_latents + 16 + i] = !init01 ? 0.0 : n.mimic_fp16 ? round_h(s0 - round_h(shi[i])) : s0 - shi[i];
+        }
+    }
     for (int i = n.head_in; i < n.head_in_pad; ++i) in[i] = 1.0;
     dense_layer(d.hw[0].data(), n.width, n.head_in_pad, in, a, true, n.mimic_fp16);
     double *x = a, *y = b;
@@ -471,7 +504,7 @@ void orc_inference(const OrcNet *net, const float *pos, const float *dir01, int 
     NetD d; prepare_net(net, d);
     parallel_rows(n, n_threads, [&](int i) {
         double bo[64];
-        base_forward(d, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), bo);
+        base_forward(d, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), bo, dir01 + 3 * i);
         double lg[3];
         head_forward(d, bo + net->latent_offset, dir01 + 3 * i, lg);
         out[4 * i + 0] = lg[0]; out[4 * i + 1] = lg[1]; out[4 * i + 2] = lg[2]; out[4 * i + 3] = bo[0];
@@ -514,7 +547,7 @@ int orc_render_plain(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, 
                     const V3 wp = at(r, tm);
                     if (!occupied(*sc, bits, wp)) continue;
                     double bo[64], lg[3];
-                    base_forward(d, contract(*sc, wp), bo);
+                    base_forward(d, contract(*sc, wp), bo, d01);
                     head_forward(d, bo + net->latent_offset, d01, lg);
                     ++ns;
                     if (composite(std::exp(bo[0]), lg, dt, sc->alpha_thre, rgb, T)) break;
@@ -679,7 +712,8 @@ int orc_cache_build(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, c
                     if (tm > rs[k].far_) { rs[k].alive = false; continue; }
                     if (!(w.mask[k] >> s & 1)) continue;
                     double bo[64];
-                    base_forward(d, contract(*sc, at(rs[k].r, tm)), bo);
+                    const float bd01[3] = {(rs[k].r.d.x + 1.0f) / 2.0f, (rs[k].r.d.y + 1.0f) / 2.0f, (rs[k].r.d.z + 1.0f) / 2.0f};
+                    base_forward(d, contract(*sc, at(rs[k].r, tm)), bo, bd01); /* the build ray's direction (src/cache_renderer.cu:1026) */
                     const double sigma = std::exp(bo[0]);
                     double alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-sigma * (double)dt)));
                     if (alpha > (double)sc->alpha_thre) { T *= 1.0 - alpha; ++visible; }
@@ -813,7 +847,10 @@ int orc_cache_build_per_ray(const OrcNet *net, const OrcScene *sc, const OrcStep
                 q.t1 = t1;
                 if (!occupied(*sc, bits, at(q.r, tm))) continue;
                 double bo[64];
-                base_forward(d, contract(*sc, at(q.r, tm)), bo);
+                {
+                    const float qd01[3] = {(q.r.d.x + 1.0f) / 2.0f, (q.r.d.y + 1.0f) / 2.0f, (q.r.d.z + 1.0f) / 2.0f};
+                    base_forward(d, contract(*sc, at(q.r, tm)), bo, qd01);
+                }
                 S e;
                 e.t0 = t0;
                 e.logd = bo[0];
@@ -1066,7 +1103,7 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         ++n_cache;
                     } else if (kind == 0) {
                         double bo[64];
-                        base_forward(d, contract(*sc, at(r, tmh)), bo);
+                        base_forward(d, contract(*sc, at(r, tmh)), bo, d01);
                         head_forward(d, bo + net->latent_offset, d01, lg);
                         sigma = std::exp(bo[0]);
                         ++n_res;
@@ -1098,14 +1135,25 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         }
                         double lat[8];
                         for (int j = 0; j < 8; ++j) lat[j] = lsum[j] / wsum;
+                        /* a view-dependent head's initial direction: from the cache camera to the sample
+                         * (generateNetworkInput_preparation_perf_kernel, :290-312) */
+                        float init01[3];
+                        {
+                            const V3 wp = at(r, tmh);
+                            const double vx = (double)wp.x - ccam->c2w[3], vy = (double)wp.y - ccam->c2w[7], vz = (double)wp.z - ccam->c2w[11];
+                            const double nv = std::sqrt(vx * vx + vy * vy + vz * vz);
+                            init01[0] = (float)((vx / nv + 1.0) / 2.0);
+                            init01[1] = (float)((vy / nv + 1.0) / 2.0);
+                            init01[2] = (float)((vz / nv + 1.0) / 2.0);
+                        }
                         if (cc->variant == 3) {
                             /* DensityIntermediates (:776-781): latent 0 is the density,
                              * log(sum w density) enters the head and gives sigma */
                             lat[0] = net->mimic_fp16 ? round_h(std::log(lsum[0])) : std::log(lsum[0]);
-                            head_forward(d, lat, d01, lg);
+                            head_forward(d, lat, d01, lg, init01);
                             sigma = std::exp(lat[0]);
                         } else {
-                            head_forward(d, lat, d01, lg);
+                            head_forward(d, lat, d01, lg, init01);
                             sigma = std::max(dsum, 1e-6);
                         }
                         ++n_cache;

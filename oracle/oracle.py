@@ -41,7 +41,7 @@ class OrcNet(C.Structure):
                 ("table", C.c_void_p), ("width", C.c_int), ("enc_w", C.c_int), ("enc_w_pad", C.c_int),
                 ("base_out_pad", C.c_int), ("base_w", C.c_void_p), ("head_layers", C.c_int), ("head_in", C.c_int),
                 ("head_in_pad", C.c_int), ("n_latents", C.c_int), ("latent_offset", C.c_int), ("head_w", C.c_void_p),
-                ("mimic_fp16", C.c_int)]
+                ("mimic_fp16", C.c_int), ("view_dependent", C.c_int), ("first_w", C.c_void_p)]
 
 
 class OrcCacheDims(C.Structure):
@@ -183,9 +183,20 @@ class OracleModel:
         assert self.base_w.size == width * enc_w_pad + base_out_pad * width
         head = cfg["mlp_head"]
         n_hidden = head["network"]["n_hidden_layers"]
-        first_lat_dens = bool(head.get("first_latent_is_density", True))
-        n_lat = int(head.get("n_latents", n_out))
-        head_in = int(head.get("n_input", 16 + n_lat))
+        # the view-dependent split network (NerfNetwork::init_viewdep, include/nerf_network.h:120-158)
+        first = cfg.get("mlp_first_head")
+        self.view_dependent = first is not None
+        if first is not None:
+            first_lat_dens = bool(first.get("first_latent_is_density", True))
+            n_lat = int(first["n_output"])
+            head_in = int(head.get("n_input", 32 + n_lat))
+            self.first_w = np.fromfile(os.path.join(model_dir, "mlp_first_head.dat"), np.uint16)
+            assert self.first_w.size == width * 32 + 16 * width
+        else:
+            first_lat_dens = bool(head.get("first_latent_is_density", True))
+            n_lat = int(head.get("n_latents", n_out))
+            head_in = int(head.get("n_input", 16 + n_lat))
+            self.first_w = np.zeros(1, np.uint16)
         head_in_pad = (head_in + 15) // 16 * 16
         self.head_w = np.fromfile(os.path.join(model_dir, "mlp_head.dat"), np.uint16)
         assert self.head_w.size == width * head_in_pad + (n_hidden - 1) * width * width + 16 * width
@@ -205,6 +216,8 @@ class OracleModel:
         n.latent_offset = 0 if first_lat_dens else 1
         n.head_w = ptr(self.head_w)
         n.mimic_fp16 = int(mimic_fp16)
+        n.view_dependent = int(self.view_dependent)
+        n.first_w = ptr(self.first_w)
         self.net = n
 
     # -- evaluation --------------------------------------------------------
