@@ -523,6 +523,16 @@ __device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, float
  * row's place in the cache list, its log-density to the high half of
  * row_out.y; the froxel point stays in row_pay for the adjoint); appends
  * the row id to the resample or cache list. */
+/* the initial view direction of a cache row for a view-dependent head: from
+ * the cache camera to the sample, unit_to_01; the head reads it from the row
+ * payload */
+__device__ __forceinline__ float3 cache_viewdir01(float3 wp, const DevCam &ccam)
+{
+    const float vx = wp.x - ccam.c2w[3], vy = wp.y - ccam.c2w[7], vz = wp.z - ccam.c2w[11];
+    const float inv = rsqrtf(vx * vx + vy * vy + vz * vz);
+    return make_float3((vx * inv + 1.0f) / 2.0f, (vy * inv + 1.0f) / 2.0f, (vz * inv + 1.0f) / 2.0f);
+}
+
 __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it)
 {
     const int n_rows = p.counters[2];
@@ -553,7 +563,9 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                     const float3 pc = contract(p.scene, at(o, d, tm));
                     p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
                 } else if (kind == KIND_CACHE) {
-                    p.row_pay[r] = make_float4(0.f, 0.f, 0.f, density);
+                    float3 iv = make_float3(0.f, 0.f, 0.f);
+                    if (p.view_dependent) iv = cache_viewdir01(at(o, d, tm), ccam); /* src/cache_basic_renderer.cu:86-87,198 */
+                    p.row_pay[r] = make_float4(iv.x, iv.y, iv.z, density);
                     logd = logf(density);
                 }
             } else {
@@ -567,13 +579,9 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                     const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
                     p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
                     cache_lookup(C, fr, logd, lat);
-                    if (p.view_dependent) {
-                        /* the initial view direction of a cache row: from the cache camera to the sample,
-                         * unit_to_01 (src/cache_performance_renderer.cu:290-312); the head reads it */
-                        const float3 wp = at(o, d, tmh);
-                        const float vx = wp.x - ccam.c2w[3], vy = wp.y - ccam.c2w[7], vz = wp.z - ccam.c2w[11];
-                        const float inv = rsqrtf(vx * vx + vy * vy + vz * vz);
-                        p.row_pay[r] = make_float4((vx * inv + 1.0f) / 2.0f, (vy * inv + 1.0f) / 2.0f, (vz * inv + 1.0f) / 2.0f, 0.f);
+                    if (p.view_dependent) { /* src/cache_performance_renderer.cu:290-312 */
+                        const float3 iv = cache_viewdir01(at(o, d, tmh), ccam);
+                        p.row_pay[r] = make_float4(iv.x, iv.y, iv.z, 0.f);
                     }
                 }
             }

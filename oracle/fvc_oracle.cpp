@@ -1096,9 +1096,20 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         if (kind == 2) { ++n_drop; continue; }
                     }
                     const float tmh = cc->basic ? tm : t0 + dt * 0.5f;  /* generateNetworkInput_* :234, :287 */
+                    /* a view-dependent head's initial direction for a cache sample: from the cache camera to
+                     * the sample (src/cache_performance_renderer.cu:290-312, src/cache_basic_renderer.cu:86-87) */
+                    float init01[3];
+                    {
+                        const V3 wp = at(r, tmh);
+                        const double vx = (double)wp.x - ccam->c2w[3], vy = (double)wp.y - ccam->c2w[7], vz = (double)wp.z - ccam->c2w[11];
+                        const double nv = std::sqrt(vx * vx + vy * vy + vz * vz);
+                        init01[0] = (float)((vx / nv + 1.0) / 2.0);
+                        init01[1] = (float)((vy / nv + 1.0) / 2.0);
+                        init01[2] = (float)((vz / nv + 1.0) / 2.0);
+                    }
                     double sigma, lg[3];
                     if (kind == 1 && cc->basic) {
-                        head_forward(d, blat, d01, lg);
+                        head_forward(d, blat, d01, lg, init01);
                         sigma = bsigma;
                         ++n_cache;
                     } else if (kind == 0) {
@@ -1135,17 +1146,6 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         }
                         double lat[8];
                         for (int j = 0; j < 8; ++j) lat[j] = lsum[j] / wsum;
-                        /* a view-dependent head's initial direction: from the cache camera to the sample
-                         * (generateNetworkInput_preparation_perf_kernel, :290-312) */
-                        float init01[3];
-                        {
-                            const V3 wp = at(r, tmh);
-                            const double vx = (double)wp.x - ccam->c2w[3], vy = (double)wp.y - ccam->c2w[7], vz = (double)wp.z - ccam->c2w[11];
-                            const double nv = std::sqrt(vx * vx + vy * vy + vz * vz);
-                            init01[0] = (float)((vx / nv + 1.0) / 2.0);
-                            init01[1] = (float)((vy / nv + 1.0) / 2.0);
-                            init01[2] = (float)((vz / nv + 1.0) / 2.0);
-                        }
                         if (cc->variant == 3) {
                             /* DensityIntermediates (:776-781): latent 0 is the density,
                              * log(sum w density) enters the head and gives sigma */

@@ -9,7 +9,8 @@ directions. A cache sample's initial direction points from the cache camera to
 the sample (src/cache_performance_renderer.cu:290-312).
 Bit-exact: sample counts, classification, brick slots and known ranges.
 Within tolerance: pixel colours (max-abs 2e-3 against the float64 oracle).
-The paths not built for these models refuse them with FVC_ERR_CONFIG."""
+The paths not built for these models (mma.sync, BF16/FP8, adjoint, batch,
+per-ray fill) refuse them with FVC_ERR_CONFIG."""
 import numpy as np
 import pytest
 
@@ -117,12 +118,43 @@ def test_paths_not_built_refuse_the_model():
     with pytest.raises(fvc._lib.FvcError) as e:
         fvc.Gradients(loader.nerf_network)
     assert e.value.code == FVC_ERR_CONFIG
-    c0, c1 = fvc.Cache(), fvc.Cache()
-    rb = fvc.CacheBasicRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
-    rb.resizeCache((16, 16), loader.stepsize_info)
-    rb.resizeRenderbuffers((16, 16))
-    rb.initCacheBlockwise(info)
-    rb.swapCache()
     with pytest.raises(fvc._lib.FvcError) as e:
-        rb.render(info, fvc.RenderBuffer((16, 16)))
+        r.render_batch([info, info])
     assert e.value.code == FVC_ERR_CONFIG
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    rc = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    rc.resizeCache((16, 16), loader.stepsize_info)
+    rc.resizeRenderbuffers((16, 16))
+    with pytest.raises(fvc._lib.FvcError) as e:
+        rc.initCache(info)  # the per-ray fill
+    assert e.value.code == FVC_ERR_CONFIG
+
+
+def test_basic_cache_renderer(vd_model):
+    """CacheBasicRenderer (src/cache_basic_renderer.cu): the cache rows' initial
+    direction is taken at the step midpoint (:86-87,198)."""
+    loader, om = vd_model
+    W, H = 48, 40
+    cam0 = small_camera(1001, W, H)
+    variant = fvc.DENSITY_INTERMEDIATES if om.net.latent_offset == 0 else fvc.DENSITY
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    r = fvc.CacheBasicRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    r.resizeCache((W, H), loader.stepsize_info)
+    r.resizeRenderbuffers((W, H))
+    r.setCacheSettings(fvc.default_cache_settings(variant, fvc.LINEAR))
+    r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
+    r.swapCache()
+    oc = om.cache_build(cam0, variant=variant).render_as_basic(variant, fvc.LINEAR, 1, 1, 1)
+    cam1 = _rotated(cam0, W, H)
+    buf = fvc.RenderBuffer((W, H))
+    r.render(fvc.raymarch_info(cam1, loader.stepsize_info), buf)
+    ref, counts = om.render_cached(cam1, oc)
+    live = ref[..., 3] >= 1e-4
+    np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])
+    np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])
+    np.testing.assert_array_equal(buf.ray_counts[..., 2][live], counts[..., 2][live])
+    err = np.abs(buf.results - ref).max()
+    hit = counts[..., 1].sum() / max(1, counts[..., :2].sum())
+    p = psnr(buf.results[..., :3] + buf.results[..., 3:], ref[..., :3] + ref[..., 3:])
+    print(f"\nview-dependent basic cached: hit {hit:.3f}, max-abs {err:.2e}, PSNR vs fp64 oracle {p:.1f} dB")
+    assert hit > 0.3 and err <= COLOR_ATOL
