@@ -1021,7 +1021,7 @@ extern "C" int fvc_model_density(fvc_model *m, const float *pos, int n, float *l
 extern "C" int fvc_model_inference(fvc_model *m, const float *pos, const float *dir01, int n, float *out)
 {
     CHECK_ARG(m && dir01 && out, "fvc_model_inference: null argument");
-    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     return run_inference(m, pos, dir01, n, out, nullptr, nullptr);
 }
 
@@ -1182,8 +1182,8 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.tc_fp8_iw = m->d_fp8_iw;
     if (r->precision != FVC_PRECISION_FP16 && (cached || !r->use_tc))
         return fail(FVC_ERR_CONFIG, "BF16 and FP8 MLPs are built for the plain renderers on the tcgen05 network path");
-    if (m->view_dependent && (!r->use_tc || r->precision != FVC_PRECISION_FP16 || per_view_caches))
-        return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    if (m->view_dependent && (!r->use_tc || r->precision != FVC_PRECISION_FP16))
+        return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     p.view_dependent = m->view_dependent;
     p.weights_vd = m->d_weights_vd;
     p.latent_offset = m->latent_offset;
@@ -1581,7 +1581,6 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
 {
     CHECK_ARG(r && info, "fvc_cache_build_per_ray: null argument");
     CHECK_ARG(r->next, "fvc_cache_build_per_ray: caches not attached (fvc_renderer_set_caches)");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
     int rc;
     if ((rc = check_info(info))) return rc;
     fvc_model *m = r->m;
@@ -1621,6 +1620,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
     memset(&q, 0, sizeof(q));
     q.grid = m->grid; q.table = m->d_table; q.weights = m->d_weights; q.latent_offset = m->latent_offset;
     q.build_rows = p.row_pay; q.build_den = x.den; q.build_lat = x.lat; q.build_row_counter = p.counters + 2;
+    q.view_dependent = m->view_dependent; q.weights_fh = m->d_weights_fh; q.dir_slot = p.row_slot;
     cudaStream_t s = r->stream;
     CU(cudaMemsetAsync(x.flag, 0, n_bricks, s));
     CU(cudaMemsetAsync(x.set, 0, n_bricks, s));
@@ -1644,6 +1644,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
         n_samples += ((long long)n_alive * n_steps + 255) / 256 * 256;     /* next_multiple(batch, 256) */
         CU(cudaMemsetAsync(p.counters + 2, 0, sizeof(int), s));
         CU(launch_fill_march(p, it, n_sms, s));
+        q.dir_states = p.states[it & 1];
         cache_density_kernel<<<n_sms * 8, 128, 0, s>>>(q);
         pr_mark_kernel<<<n_sms * 16, 128, 0, s>>>(f, it);
         pr_count_kernel<<<(int)((n_cols + 255) / 256), 256, 0, s>>>(f);
@@ -1712,7 +1713,7 @@ extern "C" int fvc_cache_read(fvc_cache *c, int32_t *packed, size_t *packed_n, f
 namespace fvc_internal {
 int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms)
 {
-    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     p->scene = m->dscene;
     p->grid = m->grid;
     p->bits = m->d_bits;
@@ -2071,7 +2072,7 @@ static int batch_launch(fvc_renderer *r, const RenderParams &p, int n_rays)
 extern "C" int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out)
 {
     CHECK_ARG(r, "fvc_render_batch: null renderer");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     RenderParams p;
     int n_rays = 0, rc;
@@ -2083,7 +2084,7 @@ extern "C" int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info 
                                        const fvc_render_outputs *out)
 {
     CHECK_ARG(r && caches, "fvc_render_batch_cached: null argument");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     RenderParams p;
     int n_rays = 0, rc;
@@ -2095,7 +2096,7 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
                                      fvc_autotune_result *res)
 {
     CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the blockwise cache build, on the tcgen05 network path in FP16");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     const int tiles[2] = {128, 32};        /* tcgen05 CTA tile, mma.sync warp tile */
     const int steps[4] = {16, 32, 64, 128}; /* marching steps per ray and sub-iteration */

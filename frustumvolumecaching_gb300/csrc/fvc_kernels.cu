@@ -253,8 +253,15 @@ __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
             uint4 o0 = reinterpret_cast<const uint4 *>(trow + 16)[0], o1 = reinterpret_cast<const uint4 *>(trow + 16)[1];
             __half2 sh[8];
             if (r < n) {
-                const float4 d = p.build_dirs[r];
-                sh16(make_float3(d.x, d.y, d.z), sh);
+                float3 d01;
+                if (p.build_dirs) {
+                    const float4 d = p.build_dirs[r];
+                    d01 = make_float3(d.x, d.y, d.z);
+                } else { /* the per-ray fill: the row's ray (src/cache_renderer.cu:899) */
+                    const float4 d = p.dir_states[p.dir_slot[r]].dt;
+                    d01 = make_float3((d.x + 1.0f) / 2.0f, (d.y + 1.0f) / 2.0f, (d.z + 1.0f) / 2.0f);
+                }
+                sh16(d01, sh);
             } else {
                 for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
             }

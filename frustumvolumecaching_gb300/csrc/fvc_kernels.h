@@ -278,6 +278,8 @@ struct CacheBuildParams {
     int view_dependent;         /* latents from the first head on the build ray's direction */
     const uint2 *weights_fh;    /* the first head's W_L1 / W_L2 fragment packs */
     float4 *build_dirs;         /* per build row: unit_to_01 of its ray direction (view-dependent models) */
+    const int *dir_slot;        /* or, when build_dirs is null: per row the alive slot of its ray ... */
+    const RayState *dir_states; /* ... in these ray states (the per-ray fill) */
     int bX, bY, bZ, fW, fH, fD, dX, dY, dZ, capacity;
     CacheRay *rays;             /* [tiles][64] */
     int *block_step;            /* [tiles] */

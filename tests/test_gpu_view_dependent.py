@@ -9,8 +9,8 @@ directions. A cache sample's initial direction points from the cache camera to
 the sample (src/cache_performance_renderer.cu:290-312).
 Bit-exact: sample counts, classification, brick slots and known ranges.
 Within tolerance: pixel colours (max-abs 2e-3 against the float64 oracle).
-The paths not built for these models (mma.sync, BF16/FP8, adjoint, batch,
-per-ray fill) refuse them with FVC_ERR_CONFIG."""
+The paths not built for these models (mma.sync, BF16/FP8, adjoint, batch)
+refuse them with FVC_ERR_CONFIG."""
 import numpy as np
 import pytest
 
@@ -49,6 +49,15 @@ def _rotated(cam0, W, H, deg=1.0):
     return fcam.camera_dict(np.concatenate([R @ c2w[:, :3], (R @ c2w[:, 3])[:, None]], axis=1), W, H)
 
 
+def _check_latents(vox, oc):
+    """the voxels' 8 latents (the first head's outputs on the build rays'
+    directions) against the oracle's, within fp16 rounding"""
+    n = oc.n_bricks_set
+    lat = vox[:n, :, 4:8].copy().view(np.float16).astype(np.float32).reshape(n, 512, 8)
+    olat = oc.vox_latents[:n * 512 * 8].view(np.float16).astype(np.float32).reshape(n, 512, 8)
+    assert n > 0 and np.abs(lat - olat).max() < 2e-3
+
+
 def test_plain_render(vd_model):
     loader, om = vd_model
     W, H = 48, 40
@@ -77,11 +86,12 @@ def test_cache_build_and_cached_render(vd_model):
     r.resizeRenderbuffers((W, H))
     r.setCacheSettings(fvc.default_cache_settings(fvc.DENSITY_INTERMEDIATES if om.net.latent_offset == 0 else fvc.DENSITY))
     r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
-    packed, known, _ = c1.read()
+    packed, known, vox = c1.read()
     variant = fvc.DENSITY_INTERMEDIATES if om.net.latent_offset == 0 else fvc.DENSITY
     oc = om.cache_build(cam0, variant=variant)
     np.testing.assert_array_equal(packed.ravel(), oc.packed_index)
     np.testing.assert_array_equal(known.ravel().view(np.uint32), oc.known_ranges.view(np.uint32))
+    _check_latents(vox, oc)
     r.swapCache()
     cam1 = _rotated(cam0, W, H)
     buf = fvc.RenderBuffer((W, H))
@@ -121,13 +131,38 @@ def test_paths_not_built_refuse_the_model():
     with pytest.raises(fvc._lib.FvcError) as e:
         r.render_batch([info, info])
     assert e.value.code == FVC_ERR_CONFIG
+
+
+def test_per_ray_fill(vd_model):
+    """CacheRenderer::initCache (src/cache_renderer.cu:848-928): the first head
+    runs on each row's own ray direction (:899)."""
+    loader, om = vd_model
+    W, H = 48, 40
+    cam0 = small_camera(1001, W, H)
+    variant = fvc.DENSITY_INTERMEDIATES if om.net.latent_offset == 0 else fvc.DENSITY
     c0, c1 = fvc.Cache(), fvc.Cache()
-    rc = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
-    rc.resizeCache((16, 16), loader.stepsize_info)
-    rc.resizeRenderbuffers((16, 16))
-    with pytest.raises(fvc._lib.FvcError) as e:
-        rc.initCache(info)  # the per-ray fill
-    assert e.value.code == FVC_ERR_CONFIG
+    r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    r.resizeCache((W, H), loader.stepsize_info)
+    r.resizeRenderbuffers((W, H))
+    r.setCacheSettings(fvc.default_cache_settings(variant))
+    r.initCache(fvc.raymarch_info(cam0, loader.stepsize_info))
+    packed, known, vox = c1.read()
+    oc = om.cache_build_per_ray(cam0, variant=variant)
+    np.testing.assert_array_equal(packed.ravel(), oc.packed_index)
+    np.testing.assert_array_equal(known.ravel().view(np.uint32), oc.known_ranges.view(np.uint32))
+    _check_latents(vox, oc)
+    r.swapCache()
+    cam1 = _rotated(cam0, W, H)
+    buf = fvc.RenderBuffer((W, H))
+    r.render(fvc.raymarch_info(cam1, loader.stepsize_info), buf)
+    ref, counts = om.render_cached(cam1, oc)
+    live = ref[..., 3] >= 1e-4
+    np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])
+    np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])
+    err = np.abs(buf.results - ref).max()
+    hit = counts[..., 1].sum() / max(1, counts[..., :2].sum())
+    print(f"\nview-dependent per-ray fill: hit {hit:.3f}, max-abs {err:.2e}")
+    assert hit > 0.1 and err <= COLOR_ATOL
 
 
 def test_basic_cache_renderer(vd_model):
