@@ -1021,7 +1021,7 @@ extern "C" int fvc_model_density(fvc_model *m, const float *pos, int n, float *l
 extern "C" int fvc_model_inference(fvc_model *m, const float *pos, const float *dir01, int n, float *out)
 {
     CHECK_ARG(m && dir01 && out, "fvc_model_inference: null argument");
-    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     return run_inference(m, pos, dir01, n, out, nullptr, nullptr);
 }
 
@@ -1183,7 +1183,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     if (r->precision != FVC_PRECISION_FP16 && (cached || !r->use_tc))
         return fail(FVC_ERR_CONFIG, "BF16 and FP8 MLPs are built for the plain renderers on the tcgen05 network path");
     if (m->view_dependent && (!r->use_tc || r->precision != FVC_PRECISION_FP16))
-        return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
+        return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     p.view_dependent = m->view_dependent;
     p.weights_vd = m->d_weights_vd;
     p.latent_offset = m->latent_offset;
@@ -1713,7 +1713,7 @@ extern "C" int fvc_cache_read(fvc_cache *c, int32_t *packed, size_t *packed_n, f
 namespace fvc_internal {
 int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms)
 {
-    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
+    if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     p->scene = m->dscene;
     p->grid = m->grid;
     p->bits = m->d_bits;
@@ -2072,7 +2072,6 @@ static int batch_launch(fvc_renderer *r, const RenderParams &p, int n_rays)
 extern "C" int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out)
 {
     CHECK_ARG(r, "fvc_render_batch: null renderer");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     RenderParams p;
     int n_rays = 0, rc;
@@ -2084,7 +2083,6 @@ extern "C" int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info 
                                        const fvc_render_outputs *out)
 {
     CHECK_ARG(r && caches, "fvc_render_batch_cached: null argument");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     RenderParams p;
     int n_rays = 0, rc;
@@ -2096,7 +2094,7 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
                                      fvc_autotune_result *res)
 {
     CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
-    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the single-view renderers and the cache builds, on the tcgen05 network path in FP16");
+    if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     const int tiles[2] = {128, 32};        /* tcgen05 CTA tile, mma.sync warp tile */
     const int steps[4] = {16, 32, 64, 128}; /* marching steps per ray and sub-iteration */

@@ -1744,7 +1744,10 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
                 const size_t tc_smem = sizeof(TcSmem);
                 const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
                 wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
-                    if (p.use_tc) {
+                if (p.view_dependent) {
+                    wf_net_vd_kernel<0, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
+                    wf_net_vd_kernel<1, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
+                } else if (p.use_tc) {
                     wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
                     wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
                 } else {

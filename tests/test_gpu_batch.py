@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import frustumvolumecaching_gb300 as fvc
+from frustumvolumecaching_gb300 import model as fmodel
 from tests.helpers import small_camera, tiny_model
 
 pytestmark = pytest.mark.gpu
@@ -56,9 +57,18 @@ def _check(single, res, cnt, img):
         off += n
 
 
-def test_batch_matches_single_views_and_reuses_graph():
+def _model(kind):
+    if kind == "view_dependent":  # the split head (mlp_first_head)
+        spec = fmodel.spec_tiny(seed=31)
+        spec.view_dependent, spec.name = True, f"{spec.name}_h2"
+        return fvc.load_data(fmodel.ensure_model(spec))
+    return fvc.load_data(tiny_model(7, 1))
+
+
+@pytest.mark.parametrize("kind", ["density_head", "view_dependent"])
+def test_batch_matches_single_views_and_reuses_graph(kind):
     torch = pytest.importorskip("torch")
-    loader = fvc.load_data(tiny_model(7, 1))
+    loader = _model(kind)
     r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
     for seed0 in (1200, 1300):  # the second batch changes only the cameras: same graph
         cams = _views(seed0)
@@ -82,14 +92,15 @@ def test_autotune_picks_a_valid_configuration():
     _check(_single(loader, cams, tcgen05=tuned.m_tile == 128), res, cnt, img)
 
 
-def test_batch_with_per_view_caches_matches_single_cached_renders():
+@pytest.mark.parametrize("kind", ["density_head", "view_dependent"])
+def test_batch_with_per_view_caches_matches_single_cached_renders(kind):
     """Each view of a batch renders against its own frustum cache (built at
     the view's pose; rendered from a pose rotated by 1 degree): the batch must
     reproduce the per-view cached renders bit for bit."""
     torch = pytest.importorskip("torch")
     from frustumvolumecaching_gb300 import camera as fcam
 
-    loader = fvc.load_data(tiny_model(7, 1))
+    loader = _model(kind)
     cams0 = _views(1500)
     a = np.radians(1.0)
     R = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])

@@ -9,8 +9,9 @@ directions. A cache sample's initial direction points from the cache camera to
 the sample (src/cache_performance_renderer.cu:290-312).
 Bit-exact: sample counts, classification, brick slots and known ranges.
 Within tolerance: pixel colours (max-abs 2e-3 against the float64 oracle).
-The paths not built for these models (mma.sync, BF16/FP8, adjoint, batch)
-refuse them with FVC_ERR_CONFIG."""
+The paths not built for these models (mma.sync, BF16/FP8, adjoint, the
+autotuner) refuse them with FVC_ERR_CONFIG; batches are checked in
+test_gpu_batch.py."""
 import numpy as np
 import pytest
 
@@ -129,7 +130,7 @@ def test_paths_not_built_refuse_the_model():
         fvc.Gradients(loader.nerf_network)
     assert e.value.code == FVC_ERR_CONFIG
     with pytest.raises(fvc._lib.FvcError) as e:
-        r.render_batch([info, info])
+        r.autotune([info, info])  # its candidates include the mma.sync path
     assert e.value.code == FVC_ERR_CONFIG
 
 
