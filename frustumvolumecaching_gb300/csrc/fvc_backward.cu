@@ -697,11 +697,16 @@ __device__ __forceinline__ void encode_levels(const DevGrid &g, const __half2 *_
             if ((g.dense_mask >> l) & 1u) {
                 const uint32_t rr = g.res[l], r2 = g.res2[l];
                 const uint32_t b0 = gx + gy * rr + gz * r2;
+                if (b0 + 1u + rr + r2 < size) { /* no corner reaches past the table */
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    uint32_t i = b0 + ((c & 1) ? 1u : 0u) + ((c & 2) ? rr : 0u) + ((c & 4) ? r2 : 0u);
-                    if (i >= size) i -= size;
-                    v[j][c] = __ldg(tl + i);
+                    for (int c = 0; c < 8; ++c) v[j][c] = __ldg(tl + (b0 + ((c & 1) ? 1u : 0u) + ((c & 2) ? rr : 0u) + ((c & 4) ? r2 : 0u)));
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        uint32_t i = b0 + ((c & 1) ? 1u : 0u) + ((c & 2) ? rr : 0u) + ((c & 4) ? r2 : 0u);
+                        if (i >= size) i -= size;
+                        v[j][c] = __ldg(tl + i);
+                    }
                 }
             } else {
                 const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;

@@ -1534,9 +1534,9 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     std::vector<int> dummy;
     for (; iter < max_iter && n_alive > 0; ++iter) {
         CU(cudaMemsetAsync(p.build_row_counter, 0, sizeof(int), s));
-        cache_search_kernel<<<std::min(n_alive, 1 << 16), 64, 0, s>>>(p);
+        CU(launch_cache_search(p, std::min(n_alive, 1 << 16), s));
         CU(cudaGetLastError());
-        cache_density_kernel<<<m->n_sms * 8, 128, 0, s>>>(p);
+        CU(launch_cache_density(p, m->n_sms * 8, s));
         CU(cudaGetLastError());
         cache_composite_kernel<<<std::min((n_alive + 3) / 4, 1 << 16), 128, 0, s>>>(p);
         CU(cudaGetLastError());
@@ -1645,7 +1645,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
         CU(cudaMemsetAsync(p.counters + 2, 0, sizeof(int), s));
         CU(launch_fill_march(p, it, n_sms, s));
         q.dir_states = p.states[it & 1];
-        cache_density_kernel<<<n_sms * 8, 128, 0, s>>>(q);
+        CU(launch_cache_density(q, n_sms * 8, s));
         pr_mark_kernel<<<n_sms * 16, 128, 0, s>>>(f, it);
         pr_count_kernel<<<(int)((n_cols + 255) / 256), 256, 0, s>>>(f);
         pr_scan_kernel<<<1, 1024, 0, s>>>(f);

@@ -271,11 +271,16 @@ __device__ __forceinline__ void hash_encode(const DevGrid &g, const __half2 *__r
             if ((g.dense_mask >> l) & 1u) {
                 const uint32_t r = g.res[l], r2 = g.res2[l];
                 const uint32_t b = gx + gy * r + gz * r2;
+                if (b + 1u + r + r2 < size) { /* no corner reaches past the table (all but the grid's far faces) */
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    uint32_t i = b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u);
-                    if (i >= size) i -= size; /* == i % size: dense indices stay below 2*size */
-                    v[j][c] = __ldg(tl + i);
+                    for (int c = 0; c < 8; ++c) v[j][c] = __ldg(tl + (b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u)));
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        uint32_t i = b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u);
+                        if (i >= size) i -= size; /* == i % size: dense indices stay below 2*size */
+                        v[j][c] = __ldg(tl + i);
+                    }
                 }
             } else {
                 const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;

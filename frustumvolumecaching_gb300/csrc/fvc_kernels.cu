@@ -145,6 +145,7 @@ __device__ __forceinline__ int tile_block_sum(int v, int *red)
     return red[0] + red[1];
 }
 
+template <bool VD>
 __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
 {
     __shared__ int red[4];
@@ -210,7 +211,7 @@ __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
             if ((mask >> s) & 1u) {
                 const float3 cp = contract(p.scene, at(cr.o, cr.d, tm));
                 p.build_rows[row] = make_float4(cp.x, cp.y, cp.z, 0.f);
-                if (p.view_dependent) /* the build's network input direction (src/cache_renderer.cu:1026) */
+                if (VD) /* the build's network input direction (src/cache_renderer.cu:1026) */
                     p.build_dirs[row] = make_float4((cr.d.x + 1.0f) / 2.0f, (cr.d.y + 1.0f) / 2.0f, (cr.d.z + 1.0f) / 2.0f, 0.f);
                 rof[s * 64 + k] = row++;
             } else {
@@ -221,13 +222,15 @@ __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
 }
 
 /* density network on every row of the iteration: log-density and the 8
- * latents (fp16, as NerfNetwork::inferenceLatents stores them) */
+ * latents (fp16, as NerfNetwork::inferenceLatents stores them); VD: the view-dependent network's first head on the rows' ray
+ * directions */
+template <bool VD>
 __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
 {
-    __shared__ uint2 Wsm[W_L3], Wfh[W_L3];
+    __shared__ uint2 Wsm[W_L3], Wfh[VD ? W_L3 : 1];
     __shared__ __align__(16) __half tiles[4][32 * TILE_STRIDE];
     for (int i = threadIdx.x; i < W_L3; i += blockDim.x) Wsm[i] = p.weights[i];
-    if (p.view_dependent)
+    if (VD)
         for (int i = threadIdx.x; i < W_L3; i += blockDim.x) Wfh[i] = p.weights_fh[i];
     __syncthreads();
     const int n = *p.build_row_counter;
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
         __syncwarp();
         density_mlp(tile, Wsm, lane);
         __half logd = trow[16];
-        if (p.view_dependent) {
+        if (VD) {
             /* the first head (NerfNetwork::inferenceLatents, include/nerf_network.h:183-197) on
              * [density outputs | SH of the build ray's direction]; its outputs take rows 1.. of the
              * head input (row 0 keeps the log-density) */
@@ -287,6 +290,20 @@ __global__ void __launch_bounds__(128) cache_density_kernel(CacheBuildParams p)
         }
         __syncwarp();
     }
+}
+
+cudaError_t launch_cache_search(const CacheBuildParams &p, int grid, cudaStream_t s)
+{
+    if (p.view_dependent) cache_search_kernel<true><<<grid, 64, 0, s>>>(p);
+    else cache_search_kernel<false><<<grid, 64, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cache_density(const CacheBuildParams &p, int grid, cudaStream_t s)
+{
+    if (p.view_dependent) cache_density_kernel<true><<<grid, 128, 0, s>>>(p);
+    else cache_density_kernel<false><<<grid, 128, 0, s>>>(p);
+    return cudaGetLastError();
 }
 
 /* One warp per processed tile, rays lane and lane + 32 per lane:

@@ -379,8 +379,8 @@ cudaError_t launch_grad_finalize(float *scratch, float *out, size_t n, float inv
 cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sms, cudaStream_t s);
 
 __global__ void cache_init_kernel(CacheBuildParams p);
-__global__ void cache_search_kernel(CacheBuildParams p);
-__global__ void cache_density_kernel(CacheBuildParams p);
+cudaError_t launch_cache_search(const CacheBuildParams &p, int grid, cudaStream_t s);
+cudaError_t launch_cache_density(const CacheBuildParams &p, int grid, cudaStream_t s);
 __global__ void cache_composite_kernel(CacheBuildParams p);
 __global__ void cache_assign_kernel(CacheBuildParams p);
 __global__ void cache_fill_kernel(CacheBuildParams p);

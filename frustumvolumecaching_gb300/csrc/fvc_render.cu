@@ -533,6 +533,7 @@ __device__ __forceinline__ float3 cache_viewdir01(float3 wp, const DevCam &ccam)
     return make_float3((vx * inv + 1.0f) / 2.0f, (vy * inv + 1.0f) / 2.0f, (vz * inv + 1.0f) / 2.0f);
 }
 
+template <bool VD>
 __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it)
 {
     const int n_rows = p.counters[2];
@@ -564,7 +565,7 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                     p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
                 } else if (kind == KIND_CACHE) {
                     float3 iv = make_float3(0.f, 0.f, 0.f);
-                    if (p.view_dependent) iv = cache_viewdir01(at(o, d, tm), ccam); /* src/cache_basic_renderer.cu:86-87,198 */
+                    if (VD) iv = cache_viewdir01(at(o, d, tm), ccam); /* src/cache_basic_renderer.cu:86-87,198 */
                     p.row_pay[r] = make_float4(iv.x, iv.y, iv.z, density);
                     logd = logf(density);
                 }
@@ -579,7 +580,7 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                     const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
                     p.row_pay[r] = make_float4(fr.x, fr.y, fr.z, 0.f);
                     cache_lookup(C, fr, logd, lat);
-                    if (p.view_dependent) { /* src/cache_performance_renderer.cu:290-312 */
+                    if (VD) { /* src/cache_performance_renderer.cu:290-312 */
                         const float3 iv = cache_viewdir01(at(o, d, tmh), ccam);
                         p.row_pay[r] = make_float4(iv.x, iv.y, iv.z, 0.f);
                     }
@@ -603,6 +604,14 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
             p.row_out[r] = make_uint2(0u, (uint32_t)__half_as_ushort(__float2half_rn(logd)) << 16);
         }
     }
+}
+
+/* the view-dependent form only for those models: the default one keeps its
+ * register count (and so its occupancy) */
+static inline void launch_classify(const RenderParams &p, int it, int n_sms, cudaStream_t s)
+{
+    if (p.view_dependent) wf_classify_kernel<true><<<n_sms * 8, 256, 0, s>>>(p, it);
+    else wf_classify_kernel<false><<<n_sms * 8, 256, 0, s>>>(p, it);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1553,7 +1562,7 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
         wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
         ++L.launches;
         if (CACHED) {
-            wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
+            launch_classify(p, it, n_sms, s);
             timed_begin();
             if (p.view_dependent) wf_net_vd_kernel<0, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
             else if (p.use_tc) wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
@@ -1646,7 +1655,7 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
         if (CACHED) {
             const size_t tc_smem = sizeof(TcSmem);
             const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
-            wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
+            launch_classify(p, it, n_sms, s);
             if (p.use_tc) {
                 wf_net_tc_kernel<0, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
                 wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
@@ -1743,7 +1752,7 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
             if (CACHED) {
                 const size_t tc_smem = sizeof(TcSmem);
                 const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
-                wf_classify_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
+                launch_classify(p, it, n_sms, s);
                 if (p.view_dependent) {
                     wf_net_vd_kernel<0, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
                     wf_net_vd_kernel<1, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
