@@ -8,15 +8,17 @@
  * white-background pixel (C + T, writeImageBuffer_performance_kernel,
  * src/performance_renderer.cu:127-149).
  *
- * Two forms of the network backward.  wf_net_bwd_tc_kernel (the default) runs
- * it on the tcgen05 tensor cores, 128 rows per CTA, with the weight gradients
- * accumulated in TMEM (its comment block below has the layout).
- * wf_net_bwd_kernel (the mma.sync network path) takes one warp per 32 rows
- * (mma.sync m16n8k16, fp16 or bf16
- * operands like the forward MLP, fp32 accumulation): the forward activations of the rows (hash features,
- * density hidden layer, head input [latents | SH | 1-padding], head hidden
- * layers) are recomputed into shared memory; the gradient tile then walks
- * back through the layers.  Input gradients are tile x weight-pack products;
+ * Two forms of the network backward:
+ *   - wf_net_bwd_tc_kernel (the default) runs on the tcgen05 tensor cores,
+ *     warp-specialised, 128 rows per tile, with the weight gradients
+ *     accumulated in TMEM (its comment block below has the layout);
+ *   - wf_net_bwd_kernel (the mma.sync network path) takes one warp per 32
+ *     rows (mma.sync m16n8k16, fp16 or bf16 operands like the forward MLP,
+ *     fp32 accumulation).
+ * Both recompute the forward activations of the rows (hash features, density
+ * hidden layer, head input [latents | SH | 1-padding], head hidden layers)
+ * into shared memory; the gradient tile then walks back through the layers.
+ * In the mma.sync form:  Input gradients are tile x weight-pack products;
  * weight gradients dW = G^T X take both operands from the shared tiles with
  * ldmatrix.trans and accumulate in a per-CTA fp32 copy of the parameter
  * blobs, added to the global gradients once per launch.  Feature gradients
@@ -405,14 +407,16 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_net_bwd_kernel(RenderPara
 /* ------------------------------------------------------------------------- */
 /* network adjoint on the 5th-generation tensor cores                        */
 /* ------------------------------------------------------------------------- */
-/* Warp-specialised: two CTAs of 256 threads per SM, each CTA persistent
- * over 128-row tiles.
+/* Warp-specialised: two CTAs per SM, each CTA persistent over 128-row
+ * tiles, 128 + 128 * FVC_BT_HASH_SPLIT threads.
  *   - MMA warps 0..3: thread t owns row t of a tile and TMEM lane t; thread 0
  *     issues the tcgen05 MMAs, the warps wait (bounded) and run the
  *     epilogues.  They synchronise among themselves with named barrier 1.
- *   - hash warps 4..7: thread 128 + t fetches row t of the next tile, runs
- *     its hash encode into a double-buffered feature / head-input tile, and
- *     scatters the feature gradients of the tile before, read from TMEM.
+ *   - hash warps 4..: thread 128 + h fetches row h & 127 of the next tile,
+ *     runs the hash encode of its share of the 16 levels into a
+ *     double-buffered feature / head-input tile, and scatters that share of
+ *     the feature gradients of the tile before, read from TMEM.  With the
+ *     default split of 1 there are 4 hash warps, one thread per row.
  * The hash gathers and the table-gradient atomics (L2-bound) thus overlap the
  * MMA stage chain of another tile.  Handoffs use mbarriers:
  *   in_full[b]  hash -> MMA: F[b], IN[b] (SH, 1-padding) and dout[b] written;
