@@ -172,7 +172,11 @@ const char *fvc_version(void);
 /* model (reference: bool load_data(fs::path, LoaderData&), include/loader.h:49,   */
 /* src/loader.cu:146-300): a path ending in ".ingp" is an instant-ngp snapshot */
 /* (load_ingp_snapshot), any other path a nerfacc export directory            */
-/* (load_nerfacc_export: config.json + *.dat)                                 */
+/* (load_nerfacc_export: config.json + *.dat).  An export whose config has    */
+/* mlp_first_head loads as the view-dependent split network                  */
+/* (NerfNetwork::init_viewdep, src/loader.cu:251-262); the renderers and     */
+/* cache builds take it on the tcgen05 FP16 network path, the other paths    */
+/* return FVC_ERR_CONFIG.                                                    */
 /* ------------------------------------------------------------------------ */
 int fvc_model_load(const char *data_dir, fvc_model **out);
 /* Host only (no device work): the .ingp snapshot rewritten as the equivalent
