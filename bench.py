@@ -17,6 +17,7 @@ bounded sample of frame 0.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -506,6 +507,7 @@ def run_fvc(args) -> dict | None:
     from frustumvolumecaching_gb300 import build as fbuild
     from frustumvolumecaching_gb300 import camera as fcam
     from frustumvolumecaching_gb300 import model as fmodel
+    from frustumvolumecaching_gb300 import _lib as fvc_lib
 
     fbuild.build()
     spec = fmodel.spec_config2()
@@ -726,7 +728,9 @@ def run_fvc(args) -> dict | None:
                      "plain_path_achieved_gbs": plain_net_gbs,
                      "note": "hash tables (32 MiB) are L2-resident: the gathers are served by L2, so DRAM traffic "
                              "(ncu dram bytes, scaled per row) is far below the algorithmic bytes"},
-        "e2e": {"value": fps_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
+        # per frame the host passes its RaymarchInfo (camera, steps) by value into the call, which the library
+        # hands to the device as kernel arguments; the image, results and per-ray counts come back to host memory
+        "e2e": {"value": fps_e2e, "unit": UNIT, "h2d_bytes_per_step": n_frames * ctypes.sizeof(fvc_lib.RaymarchInfo),
                 "d2h_bytes_per_step": n_frames * W * H * (4 + 16 + 16)},
         "backward": backward,
         "precision": precision,

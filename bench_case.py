@@ -1,7 +1,7 @@
 """A small, fixed rendering case for kernel profiles.
 
-    python -m frustumvolumecaching_gb300.profile_case --res 960x540 --frames 2 --path plain --network tc
-    python -m frustumvolumecaching_gb300.profile_case --res 400x400 --frames 2 --path backward --rays 65536
+    python bench_case.py --res 960x540 --frames 2 --path plain --network tc
+    python bench_case.py --res 400x400 --frames 2 --path backward --rays 65536
 
 Renders `frames` frames of the benchmark's camera path (the synthetic
 3-cascade, 2^19-entry scene) at the given resolution through the C ABI and
@@ -17,9 +17,9 @@ from __future__ import annotations
 import argparse
 import json
 
-from . import camera as fcam
-from . import model as fmodel
-from .renderer import (Cache, CachePerformanceRenderer, PerformanceRenderer, default_cache_settings, load_data,
+from frustumvolumecaching_gb300 import camera as fcam
+from frustumvolumecaching_gb300 import model as fmodel
+from frustumvolumecaching_gb300.renderer import (Cache, CachePerformanceRenderer, PerformanceRenderer, default_cache_settings, load_data,
                        raymarch_info)
 
 
@@ -79,7 +79,7 @@ def backward_case(args, W: int, H: int) -> None:
     import numpy as np
     import torch
 
-    from .renderer import Gradients
+    from frustumvolumecaching_gb300.renderer import Gradients
 
     spec = fmodel.spec_config5()
     train = load_data(fmodel.ensure_model(spec))

@@ -1163,28 +1163,28 @@ cudaError_t launch_loss(const RenderParams &p, const BwdParams &b, cudaStream_t 
 
 cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int head_hidden, int it, int n_sms, cudaStream_t s)
 {
-    static bool attrs = false;
+    static PerDeviceOnce attrs;
     const int smem = (int)sizeof(BwdSmem);
-    if (!attrs) {
+    cudaError_t ea = attrs.run([smem] {
         cudaError_t e = cudaFuncSetAttribute(wf_net_bwd_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attrs = true;
-    }
+        return e;
+    });
+    if (ea != cudaSuccess) return ea;
     const bool bf16 = p.precision == 1;
     if (p.use_tc) {
-        static bool tc_attrs = false;
+        static PerDeviceOnce tc_attrs;
         const int tsmem = (int)sizeof(BtSmem);
-        if (!tc_attrs) {
+        ea = tc_attrs.run([tsmem] {
             cudaError_t e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
             if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
             if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
             if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_bwd_tc_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
-            if (e != cudaSuccess) return e;
-            tc_attrs = true;
-        }
+            return e;
+        });
+        if (ea != cudaSuccess) return ea;
         const int grid = 2 * n_sms;
         if (head_hidden == 2) {
             if (bf16) wf_net_bwd_tc_kernel<1, 2><<<grid, BT_THREADS, tsmem, s>>>(p, b, it);
@@ -1207,14 +1207,14 @@ cudaError_t launch_net_backward(const RenderParams &p, const BwdParams &b, int h
 
 cudaError_t launch_cache_backward(const RenderParams &p, const BwdParams &b, int head_hidden, int it, int n_sms, cudaStream_t s)
 {
-    static bool attrs = false;
+    static PerDeviceOnce attrs;
     const int smem = (int)sizeof(BwdSmem);
-    if (!attrs) {
+    const cudaError_t ea = attrs.run([smem] {
         cudaError_t e = cudaFuncSetAttribute(wf_cache_bwd_kernel<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_cache_bwd_kernel<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attrs = true;
-    }
+        return e;
+    });
+    if (ea != cudaSuccess) return ea;
     if (head_hidden == 2) wf_cache_bwd_kernel<0, 2><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
     else wf_cache_bwd_kernel<0, 1><<<n_sms, BW_WARPS * 32, smem, s>>>(p, b, it);
     return cudaGetLastError();

@@ -1728,6 +1728,10 @@ int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sm
     return FVC_OK;
 }
 void set_error(const char *msg) { g_err = msg; }
+/* the device forms of the step and camera structs, built exactly as the
+ * allocating renderers build them */
+DevSteps steps_view(const fvc_stepsize_info &s) { return dev_steps(s); }
+DevCam cam_view(const fvc_camera_info &c) { return dev_cam(c); }
 }  // namespace fvc_internal
 
 extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)

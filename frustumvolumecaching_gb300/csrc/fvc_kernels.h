@@ -6,10 +6,36 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "fvc_device.cuh"
 #include "fvc_tc.cuh"
 
 namespace fvc {
+
+/* Runs a set-up step (kernel attributes: cudaFuncSetAttribute applies to the
+ * current device only) once per device ordinal, with that device current. */
+class PerDeviceOnce {
+public:
+    template <class F>
+    cudaError_t run(F &&setup)
+    {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lk(mu_);
+        if (done_[dev]) return cudaSuccess;
+        e = setup();
+        if (e == cudaSuccess) done_[dev] = true;
+        return e;
+    }
+
+private:
+    static constexpr int kMaxDevices = 256;
+    std::mutex mu_;
+    bool done_[kMaxDevices] = {};
+};
 
 /* read-only view of a built frustum cache (Cache, include/cache.h:12-74):
  * packed brick index [bZ][bY][bX] (x fastest; pack3D(slot) or -1),

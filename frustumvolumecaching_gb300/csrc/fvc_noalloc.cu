@@ -17,13 +17,17 @@
  * streams, two host threads) race on it: serialise them.  The counters that
  * must start at zero are cleared at the start of every call.
  *
+ * The call blocks the host like the allocating render: every few
+ * sub-iterations it reads the alive-ray count back into a host word and
+ * synchronises the stream, and it returns once the frame has finished
+ * marching.
+ *
  * The first call on a device looks up the array's device address with
  * cudaGetSymbolAddress while that device is current; make that first call
  * before any stream capture on the device.
  */
 #include <cuda_runtime.h>
 
-#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -94,6 +98,8 @@ T *carve(unsigned char *&cursor, size_t n)
 namespace fvc_internal {
 int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms);
 void set_error(const char *msg);
+DevSteps steps_view(const fvc_stepsize_info &s);
+DevCam cam_view(const fvc_camera_info &c);
 }  // namespace fvc_internal
 
 extern "C" int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, const fvc_render_outputs *out, void *cuda_stream)
@@ -123,28 +129,8 @@ extern "C" int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, c
     memset(&p, 0, sizeof(p));
     int head_hidden = 2, n_sms = 1;
     if ((rc = fvc_internal::model_views(m, &p, &head_hidden, &n_sms))) return rc;
-    p.steps = fvc::DevSteps{};
-    {
-        const fvc_stepsize_info &s = info->stepsize_info;
-        DevSteps d;
-        d.cone = s.cone_angle; d.log1p_c = s.log1p_c;
-        d.log1p_c_lo = (float)(std::log(1.0 + (double)s.cone_angle) - (double)s.log1p_c);
-        d.near_ = s.near_; d.near_i = s.near_i; d.far_ = s.far_;
-        d.dt_min = s.dt_min; d.dt_max = s.dt_max; d.t_min = s.t_min; d.t_max = s.t_max; d.i_min = s.i_min; d.i_max = s.i_max;
-        p.steps = d;
-    }
-    {
-        const fvc_camera_info &c = info->cam_info;
-        DevCam d;
-        d.W = c.resolution.x; d.H = c.resolution.y; d.gl = c.is_open_gl ? 1 : 0;
-        d.fx = c.focal.x; d.fy = c.focal.y; d.px = c.principal.x; d.py = c.principal.y;
-        const fvc_float4 *mc = &c.cam2world.m0, *mw = &c.world2cam.m0;
-        for (int r = 0; r < 3; ++r) {
-            d.c2w[4 * r] = mc[r].x; d.c2w[4 * r + 1] = mc[r].y; d.c2w[4 * r + 2] = mc[r].z; d.c2w[4 * r + 3] = mc[r].w;
-            d.w2c[4 * r] = mw[r].x; d.w2c[4 * r + 1] = mw[r].y; d.w2c[4 * r + 2] = mw[r].z; d.w2c[4 * r + 3] = mw[r].w;
-        }
-        p.cam = d;
-    }
+    p.steps = fvc_internal::steps_view(info->stepsize_info);
+    p.cam = fvc_internal::cam_view(info->cam_info);
     /* carve the scratch: header (counters, statistics) then per-ray arrays */
     unsigned char *cursor = static_cast<unsigned char *>(base);
     int *ctl = carve<int>(cursor, 16);              /* [0] ray counter, [1] guard, [8..15] sub-iteration counters */

@@ -1520,6 +1520,13 @@ static cudaError_t set_net_attrs()
     return e;
 }
 
+template <int HH>
+static cudaError_t ensure_net_attrs()
+{
+    static PerDeviceOnce once;
+    return once.run([] { return set_net_attrs<HH>(); });
+}
+
 /* the network kernel of the plain path's rows in the renderer's network path and precision */
 template <int HH>
 static void launch_plain_net(const RenderParams &p, int it, int n_sms, cudaStream_t s)
@@ -1537,11 +1544,9 @@ template <bool CACHED, int HH>
 static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, int *h_pinned, int check_every, int *n_iter,
                              LaunchLog *log)
 {
-    static bool attrs_set = false;
-    if (!attrs_set) {
-        cudaError_t e = set_net_attrs<HH>();
+    {
+        cudaError_t e = ensure_net_attrs<HH>();
         if (e != cudaSuccess) return e;
-        attrs_set = true;
     }
     LaunchLog local;
     LaunchLog &L = log ? *log : local;
@@ -1644,11 +1649,9 @@ template <bool CACHED, int HH>
 static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n_sms, cudaStream_t s, int *h_pinned,
                                 int check_every, LaunchLog *log)
 {
-    static bool attrs_set = false;
-    if (!attrs_set) {
-        cudaError_t e = set_net_attrs<HH>();
+    {
+        cudaError_t e = ensure_net_attrs<HH>();
         if (e != cudaSuccess) return e;
-        attrs_set = true;
     }
     LaunchLog local;
     LaunchLog &L = log ? *log : local;
@@ -1705,11 +1708,9 @@ template <bool CACHED, int HH>
 static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStream_t s, int n_rays, cudaGraphExec_t *exec,
                                        int *n_kernels)
 {
-    static bool attrs_set = false;
-    if (!attrs_set) {
-        cudaError_t e = set_net_attrs<HH>();
+    {
+        cudaError_t e = ensure_net_attrs<HH>();
         if (e != cudaSuccess) return e;
-        attrs_set = true;
     }
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaGraphCreate(&graph, 0);

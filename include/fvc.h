@@ -311,8 +311,10 @@ int fvc_renderer_set_kernel_timing(fvc_renderer *r, int enable);
  * device array of FVC_NOALLOC_SCRATCH_BYTES that every GPU loading the
  * library holds until exit.  Images up to FVC_NOALLOC_MAX_RAYS pixels;
  * larger ones fail with FVC_ERR_ARG.  `out` holds DEVICE pointers; the work
- * runs on `cuda_stream` (NULL = legacy default stream) and the call returns
- * once the last sub-iteration is enqueued.  All calls share the scratch:
+ * runs on `cuda_stream` (NULL = legacy default stream).  Like fvc_render the
+ * call blocks the host: every few sub-iterations it copies the alive-ray
+ * count to the host and synchronises the stream, and it returns once the
+ * frame has finished marching.  All calls share the scratch:
  * calls whose GPU work overlaps race, so serialise them.  The first call on
  * a device looks the scratch address up (cudaGetSymbolAddress); make it
  * before any stream capture on that device. */

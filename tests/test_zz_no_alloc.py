@@ -5,7 +5,10 @@ scratch is a file-scope device array inside libfvc.so.  This file is
 collected last so a failure here leaves the rest of the suite already run.
 The test calls the entry point through the C ABI twice in a row and checks
 both results against the allocating render path (fvc_render), and that an
-image beyond the array's stated maximum is refused.
+image beyond the array's stated maximum is refused.  During the two calls the
+library's allocation hook is armed to fail the very next device allocation
+(fvc_debug_fail_allocation(0)), so a call that allocated anything through the
+library would fail instead of returning FVC_OK.
 """
 import ctypes as C
 
@@ -40,10 +43,17 @@ def test_noalloc_render_matches_allocating_render_twice():
     r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
     r.render(info, ref)
     lib = L.load()
-    for call in range(2):
-        out, img, res, cnt = _device_outputs(torch, W, H)
-        L.check(lib.fvc_render_noalloc(loader.nerf_network.handle, C.byref(info), C.byref(out), None))
-        torch.cuda.synchronize()
+    outs = [_device_outputs(torch, W, H) for _ in range(2)]  # torch allocates these before the hook is armed
+    torch.cuda.synchronize()
+    try:
+        assert lib.fvc_debug_fail_allocation(0) == 0  # the library's next device allocation fails
+        for out, *_ in outs:
+            rc = lib.fvc_render_noalloc(loader.nerf_network.handle, C.byref(info), C.byref(out), None)
+            assert rc == 0, lib.fvc_last_error().decode()
+    finally:
+        lib.fvc_debug_fail_allocation(-1)
+    torch.cuda.synchronize()
+    for call, (out, img, res, cnt) in enumerate(outs):
         got = res.cpu().numpy()
         assert np.abs(got - ref.results).max() <= COLOR_ATOL, call
         np.testing.assert_array_equal(cnt.cpu().numpy(), ref.ray_counts)
