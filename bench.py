@@ -490,6 +490,58 @@ def run_double_buffered(torch, dev, cached, infos, image, results, rebuild) -> d
                     "synchronously between frames"}
 
 
+def run_quality(torch, dev, plain, cached, infos, cams, model_dir, n_rows: int = 8) -> dict:
+    """The metric's quality clause, outside the timed region: the camera path
+    replayed with the benchmark's rebuild rule, and at frame 0 (rendered from
+    a cache built at its own pose), frame 1 (the first frame rendered from a
+    cache built one path step earlier) and the last frame, a band of n_rows
+    image rows through the image centre compared with the float64 oracle
+    (plain render, and the cached render from the device's own cache read
+    back).  The definitions are oracle/quality.py's."""
+    from oracle import oracle as orc
+    from oracle import quality as oq
+
+    W, H = RES
+    r0 = H // 2 - n_rows // 2
+    rows = (r0, r0 + n_rows)
+    om = orc.OracleModel(model_dir)
+    res_p = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    res_c = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    img = torch.zeros((H, W, 4), dtype=torch.uint8, device=dev)
+    picks = sorted({0, 1, len(infos) - 1})
+    cached.initCacheBlockwise(infos[0])
+    cached.swapCache()
+    cache_frame = 0
+    frames = []
+    t0 = time.perf_counter()
+    for i, info in enumerate(infos):
+        cached.render_device(info, image=img, results=res_c)
+        st = cached._render_stats
+        cov = st.n_cache_hits / max(1, st.n_cache_hits + st.n_resamples)
+        if i in picks:
+            plain.render_device(info, image=img, results=res_p)
+            torch.cuda.synchronize(dev)
+            q = oq.cached_quality(om, cams[i], rows, res_p.cpu().numpy(), res_c.cpu().numpy(), cached._cache.read(),
+                                  cams[cache_frame])
+            q.update({"frame": i, "cache_built_at_frame": cache_frame, "frame_coverage": cov})
+            frames.append(q)
+        if cov < COVERAGE_REBUILD and i + 1 < len(infos):
+            cached.initCacheBlockwise(info)
+            cached.swapCache()
+            cache_frame = i
+    worst = max(frames, key=lambda q: q["delta_db"])
+    return {"frames": frames, "delta_db_max": worst["delta_db"],
+            "psnr_plain_db_min": min(q["psnr_plain_db"] for q in frames),
+            "psnr_cached_db_min": min(q["psnr_cached_db"] for q in frames),
+            "cache_vs_plain_db_min": min(q["cache_vs_plain_db"] for q in frames),
+            "max_abs_plain": max(q["max_abs_plain"] for q in frames),
+            "clause_met": bool(worst["delta_db"] <= 0.1),
+            "definition": "final pixel colour (rgb + T, white background) on rows [r0, r1) of 1920; psnr_plain/cached: "
+                          "GPU render vs the FP64 plain oracle; delta_db = PSNR(FP64 cached oracle on the device's cache) "
+                          "- PSNR(GPU cached), both vs the FP64 plain oracle; cache_vs_plain: GPU cached vs GPU plain",
+            "seconds": time.perf_counter() - t0}
+
+
 # --------------------------------------------------------------------------
 # GB300 arm
 # --------------------------------------------------------------------------
@@ -671,6 +723,7 @@ def run_fvc(args) -> dict | None:
     # thread rebuilds the next cache (on the renderer's low-priority stream) whenever a frame's coverage is
     # below the threshold and no build is running, while the frames keep rendering from the current cache
     double_buffered = run_double_buffered(torch, dev, cached, infos, image, results, rebuild)
+    quality = None if args.no_quality else run_quality(torch, dev, plain, cached, infos, cams, d)
 
     def mean_ms(pairs):
         return sum(a.elapsed_time(b) for a, b in pairs) / max(1, len(pairs))
@@ -715,6 +768,7 @@ def run_fvc(args) -> dict | None:
                    "resample_per_frame": res_per_frame, "cache_samples_per_frame": hit_per_frame,
                    "bricks_demanded": log["bricks_demanded"], "bricks_set": log["bricks_set"], "overflow": bool(log["overflow"]),
                    "speedup_vs_plain": fps_cached / fps_plain, "double_buffered": double_buffered},
+        "quality": quality,
         "roofline": {"kernel": NET_KERNEL, "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"] if achieved_gbs else None,
                      "traffic": (NET_TRAFFIC_PER_ROW * log["net_rows"] / max(1, log["net_launches"])
@@ -757,6 +811,7 @@ def main():
     ap.add_argument("--frames", type=int, default=PATH_FRAMES, help="frames of the camera path per step (60 for the metric)")
     ap.add_argument("--res", default=None, help="WxH override for small profiling cases (the metric is 1920x1080)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-quality", action="store_true", help="skip the untimed dPSNR rows against the float64 oracle")
     args = ap.parse_args()
     global RES
     if args.res:
