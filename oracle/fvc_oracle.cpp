@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <thread>
+#include <mutex>
 #include <vector>
 
 #include "../frustumvolumecaching_gb300/csrc/fvc_detmath.h"
@@ -955,9 +956,11 @@ inline int brick_lookup(const OrcCache &cc, int bx, int by, int bz)
 
 /* CacheBasicRenderer's cache decision and lookup at froxel point fp
  * (sample_cache_kernel, src/cache_basic_renderer.cu:95-210; froxel2data and
- * fetchBrickTex3DInterpol, include/raymarch_common.h:331-444): 0 resample,
- * 1 cache (lat = head inputs, sigma = density), 2 dropped.  Texture weights
- * in full precision (the texture unit's 8-bit weights are not emulated). */
+ * fetchBrickTex3DInterpol, include/raymarch_common.h:331-444): 1 cache
+ * (lat = head inputs, sigma = density), or 2 dropped with the reason in the
+ * upper bits (5 brick without a slot, 6 voxel not set, 7 alpha not above the
+ * threshold).  Texture weights in full precision (the texture unit's 8-bit
+ * weights are not emulated). */
 int basic_sample(const OrcCache &cc, const OrcScene *sc, V3 fp, float dt, double *lat, double &sigma)
 {
     const OrcCacheDims &cd = cc.dims;
@@ -972,11 +975,11 @@ int basic_sample(const OrcCache &cc, const OrcScene *sc, V3 fp, float dt, double
         iz = std::min(std::max(iz, 0.5f), 7.5f);
     }
     const int packed = brick_lookup(cc, bx, by, bz);
-    if (packed < 0) return 2;
+    if (packed < 0) return 2 | (5 << 2);
     const float dx = (float)(((packed >> 20) & 1023) * 8) + ix, dy = (float)(((packed >> 10) & 1023) * 8) + iy,
                 dz = (float)((packed & 1023) * 8) + iz;
     Vox v0;
-    if (!fetch_texel(cc, (int)floorf(dx), (int)floorf(dy), (int)floorf(dz), v0) || !(v0.isset > 0.0)) return 2;
+    if (!fetch_texel(cc, (int)floorf(dx), (int)floorf(dy), (int)floorf(dz), v0) || !(v0.isset > 0.0)) return 2 | (6 << 2);
     double weight = 0, dac = 0, ls[8] = {0};
     auto add = [&](const Vox &v, double w) {
         weight += w * v.isset; dac += w * v.density;
@@ -1021,25 +1024,57 @@ int basic_sample(const OrcCache &cc, const OrcScene *sc, V3 fp, float dt, double
     default: density = dac; alpha = std::min(1.0, std::max(0.0, 1.0 - std::exp(-density * dt))); break;
     }
     if (cc.reweight && cc.keep_first) ls[0] *= weight;
-    if (!(alpha > (double)sc->alpha_thre)) return 2;
+    if (!(alpha > (double)sc->alpha_thre)) return 2 | (7 << 2);
     const double div = cc.reweight ? weight : 1.0;
     for (int j = 0; j < 8; ++j) lat[j] = ls[j] / div;
     sigma = density;
     return 1;
 }
 
+/* Front-to-back compositing of given network outputs over one batch, as
+ * accumulate_performance_kernel (src/performance_renderer.cu:71-125): ray i
+ * owns samples s = 0 .. n_steps[i]-1 at row s * n_alive + i (sample-major),
+ * out4 holds 4 rows of `batch` values (r, g, b logits and log-density, the
+ * fp16 outputs as floats), t0 the samples' t0; results (rgb, T) and alive
+ * are updated in place (alive cleared when T < 1e-4), with the oracle's
+ * float64 compositing step. */
+void orc_composite_rows(int n_alive, int batch, const OrcSteps *st, float alpha_thre, const int32_t *n_steps, uint8_t *alive,
+                        float *results, const float *out4, const float *t0)
+{
+    for (int i = 0; i < n_alive; ++i) {
+        double rgb[3] = {results[4 * i], results[4 * i + 1], results[4 * i + 2]}, T = results[4 * i + 3];
+        for (int s = 0; s < n_steps[i]; ++s) {
+            const size_t row = (size_t)s * n_alive + i;
+            const double lg[3] = {out4[row], out4[row + (size_t)batch], out4[row + 2 * (size_t)batch]};
+            const double sigma = std::exp((double)out4[row + 3 * (size_t)batch]);
+            if (composite(sigma, lg, calc_step(*st, t0[row]), alpha_thre, rgb, T)) {
+                alive[i] = 0;
+                break;
+            }
+        }
+        for (int k = 0; k < 3; ++k) results[4 * i + k] = (float)rgb[k];
+        results[4 * i + 3] = (float)T;
+    }
+}
+
 /* Cached render: CachePerformanceRenderer::render and its kernels
  * (src/cache_performance_renderer.cu:22-313, 678-908, 1059-1263) as one pass
- * per ray.  counts[4*W*H]: resample, cache, dropped, steps. */
+ * per ray.  counts[4*W*H]: resample, cache, dropped, steps.  reasons[8]
+ * (optional): over the samples composited or dropped, why they were not
+ * cache hits: 1 outside the cache image, 2 outside the froxel depth, 3 before
+ * the near plane, 4 beyond the known range (resampled); 5 brick without a
+ * slot, 6 empty voxel (not set: basic), 7 alpha (basic) (dropped). */
 int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
                       const OrcCache *cc, const OrcCam *ccam, const OrcSteps *cst, int mode,
-                      int row0, int row1, float *results, int32_t *counts, int n_threads)
+                      int row0, int row1, float *results, int32_t *counts, int n_threads, long long *reasons)
 {
     NetD d; prepare_net(net, d);
     const OrcCacheDims &cd = cc->dims;
     const int W = cam->W;
+    std::mutex reason_mutex;
     parallel_rows(row1 - row0, n_threads, [&](int rr) {
         const int y = row0 + rr;
+        long long why_row[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int x = 0; x < W; ++x) {
             const size_t id = (size_t)y * W + x;
             const Ray r = generate_ray(*cam, x, y);
@@ -1067,25 +1102,33 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                     const bool in_fov = fp.x >= 0 && fp.x < (float)cd.fW && fp.y >= 0 && fp.y < (float)cd.fH;
                     const bool inside = in_fov && fp.z >= 0 && fp.z < (float)cd.fD;
                     bool unsampled = true;
+                    float kr = 0.0f;
                     if (in_fov) {
-                        const float kr = cc->known_ranges[(size_t)(int)floorf(fp.y) * cd.fW + (int)floorf(fp.x)];
+                        kr = cc->known_ranges[(size_t)(int)floorf(fp.y) * cd.fW + (int)floorf(fp.x)];
                         unsampled = tfr < cst->near_ || tfr > kr;
                     }
+                    /* why the sample is outside the cache's sampled region (0: inside) */
+                    const int why_out = !in_fov ? 1 : !inside ? 2 : tfr < cst->near_ ? 3 : tfr > kr ? 4 : 0;
                     int kind = 0; /* 0 resample, 1 cache, 2 drop */
                     double blat[8], bsigma = 0.0;
                     if (cc->basic) {
                         /* CacheBasicRenderer: decided and looked up at the midpoint */
-                        kind = (!inside || unsampled) ? 0 : basic_sample(*cc, sc, fp, dt, blat, bsigma);
-                        if (kind == 2) { ++n_drop; continue; }
+                        const int code = (!inside || unsampled) ? 0 : basic_sample(*cc, sc, fp, dt, blat, bsigma);
+                        kind = code & 3;
+                        if (kind == 0) ++why_row[why_out];
+                        if (kind == 2) { ++why_row[code >> 2]; ++n_drop; continue; }
                     } else if (!inside || unsampled) {
                         if (mode == 1) continue;
                         kind = 0;
+                        ++why_row[why_out];
                     } else {
                         if (mode == 2) continue;
                         const int bx = (int)(fp.x / 8.0f), by = (int)(fp.y / 8.0f), bz = (int)(fp.z / 8.0f);
                         const int packed = brick_lookup(*cc, bx, by, bz);
                         kind = 2;
+                        int why_drop = 5;
                         if (packed >= 0) {
+                            why_drop = 6;
                             const float ix = fp.x - (float)(bx * 8), iy = fp.y - (float)(by * 8), iz = fp.z - (float)(bz * 8);
                             const float ax = (float)(((packed >> 20) & 1023) * 8) + ix;
                             const float ay = (float)(((packed >> 10) & 1023) * 8) + iy;
@@ -1093,7 +1136,7 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                             Vox v;
                             if (fetch_texel(*cc, (int)floorf(ax), (int)floorf(ay), (int)floorf(az), v) && v.density > 0.0) kind = 1;
                         }
-                        if (kind == 2) { ++n_drop; continue; }
+                        if (kind == 2) { ++why_row[why_drop]; ++n_drop; continue; }
                     }
                     const float tmh = cc->basic ? tm : t0 + dt * 0.5f;  /* generateNetworkInput_* :234, :287 */
                     /* a view-dependent head's initial direction for a cache sample: from the cache camera to
@@ -1164,6 +1207,10 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
             results[4 * id + 0] = (float)rgb[0]; results[4 * id + 1] = (float)rgb[1];
             results[4 * id + 2] = (float)rgb[2]; results[4 * id + 3] = (float)T;
             if (counts) { counts[4 * id] = n_res; counts[4 * id + 1] = n_cache; counts[4 * id + 2] = n_drop; counts[4 * id + 3] = nst; }
+        }
+        if (reasons) {
+            std::lock_guard<std::mutex> lk(reason_mutex);
+            for (int q = 0; q < 8; ++q) reasons[q] += why_row[q];
         }
     });
     return 0;

@@ -99,13 +99,15 @@ def lib():
                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                               C.c_void_p]
         _lib.orc_loss_grad_cached.restype = C.c_double
+        _lib.orc_composite_rows.argtypes = [C.c_int, C.c_int, P(OrcSteps), C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]
         _lib.orc_cache_dims.argtypes = [P(OrcScene), P(OrcSteps), C.c_int, C.c_int, P(OrcCacheDims)]
         _lib.orc_cache_build.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache), C.c_int]
         _lib.orc_cache_build_per_ray.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
                                                  C.c_int]
         _lib.orc_render_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
                                            P(OrcCam), P(OrcSteps), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
-                                           C.c_int]
+                                           C.c_int, C.c_void_p]
     return _lib
 
 
@@ -271,9 +273,14 @@ class OracleModel:
                                    ptr(gh) if grads else None, pgp, pip, pdp, npert, threads or default_threads(), ptr(pred))
         return loss, gt, gb, gh, pred
 
-    def cache_dims(self, W: int, H: int, steps: OrcSteps | None = None) -> OrcCacheDims:
+    def cache_dims(self, W: int, H: int, steps: OrcSteps | None = None, sizing: tuple[int, float] = (32, 0.5)) -> OrcCacheDims:
+        """Cache dimensions of resizeCache (src/cache_renderer.cu:832-846); `sizing` = (estimated samples
+        per ray, brick sparsity), the reference's compile-time (32, 0.5) by default."""
         d = OrcCacheDims()
         lib().orc_cache_dims(C.byref(self.scene), C.byref(steps or self.steps), W, H, C.byref(d))
+        if tuple(sizing) != (32, 0.5):
+            est_bricks = (W * H * int(sizing[0])) // max(1, int(np.float32(sizing[1]) * np.float32(512.0)))
+            d.dZ = max(1, (est_bricks + d.dX * d.dY - 1) // (d.dX * d.dY))
         return d
 
     def cache_build(self, cam: dict, threads: int | None = None, variant: int = 0, interp: int = 0,
@@ -324,16 +331,24 @@ class OracleModel:
                                           threads or default_threads(), ptr(pred))
         return (loss, *outs, pred)
 
-    def render_cached(self, cam: dict, cache: "OracleCache", mode: int = 0, rows=None, threads: int | None = None):
+    # why samples were not cache hits (orc_render_cached's reasons[1..7])
+    REASONS = ("outside_fov", "outside_depth", "before_near", "beyond_known", "brick_unset", "voxel_empty", "alpha")
+
+    def render_cached(self, cam: dict, cache: "OracleCache", mode: int = 0, rows=None, threads: int | None = None,
+                      reasons: bool = False):
+        """(results, counts) or, with reasons=True, (results, counts, {reason: samples})."""
         c = make_cam(cam)
         cc = make_cam(cache.cam)
         W, H = c.W, c.H
         r0, r1 = rows or (0, H)
         res = np.zeros((H, W, 4), np.float32)
         counts = np.zeros((H, W, 4), np.int32)
+        why = np.zeros(8, np.int64)
         lib().orc_render_cached(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
                                 C.byref(cache.s), C.byref(cc), C.byref(cache.steps or self.steps), mode, r0, r1, ptr(res),
-                                ptr(counts), threads or default_threads())
+                                ptr(counts), threads or default_threads(), ptr(why))
+        if reasons:
+            return res, counts, {k: int(why[i + 1]) for i, k in enumerate(self.REASONS)}
         return res, counts
 
 
