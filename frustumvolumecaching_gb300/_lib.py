@@ -81,7 +81,11 @@ class RenderStats(C.Structure):
     _fields_ = [("samples_ppx", C.c_double), ("n_samples", C.c_longlong), ("n_resamples", C.c_longlong),
                 ("n_cache_hits", C.c_longlong), ("n_dropped", C.c_longlong), ("n_steps", C.c_longlong),
                 ("n_rounds", c_int), ("guard_flags", c_int), ("n_launches", C.c_longlong),
-                ("n_timed_launches", c_int), ("timed_kernel_ms", C.c_float)]
+                ("n_timed_launches", c_int), ("timed_kernel_ms", C.c_float),
+                ("n_miss_outside_fov", C.c_longlong), ("n_miss_outside_depth", C.c_longlong),
+                ("n_miss_before_near", C.c_longlong), ("n_miss_beyond_known", C.c_longlong),
+                ("n_drop_brick_unset", C.c_longlong), ("n_drop_voxel_empty", C.c_longlong),
+                ("n_drop_alpha", C.c_longlong)]
 
 
 class ModelProps(C.Structure):
@@ -101,7 +105,7 @@ class CacheStats(C.Structure):
 
 assert C.sizeof(SceneInfo) == 76 and C.sizeof(StepsizeInfo) == 48
 assert C.sizeof(CameraInfo) == 144 and CameraInfo.cam2world.offset == 32 and CameraInfo.world2cam.offset == 80
-assert C.sizeof(RenderStats) == 72 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 24
+assert C.sizeof(RenderStats) == 128 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 24
 assert C.sizeof(RaymarchInfo) == 352 and RaymarchInfo.stepsize_info.offset == 288 and RaymarchInfo.sample_index.offset == 336
 
 FVC_OK = 0

@@ -47,7 +47,7 @@ static_assert(sizeof(fvc_camera_info) == 144 && offsetof(fvc_camera_info, is_ope
 static_assert(sizeof(fvc_raymarch_info) == 352 && offsetof(fvc_raymarch_info, next_cam_info) == 144 &&
               offsetof(fvc_raymarch_info, stepsize_info) == 288 && offsetof(fvc_raymarch_info, sample_index) == 336 &&
               offsetof(fvc_raymarch_info, motion_blur) == 340 && offsetof(fvc_raymarch_info, deterministic) == 341, "RaymarchInfo layout");
-static_assert(sizeof(fvc_render_stats_t) == 72 && sizeof(fvc_cache_stats_t) == 32, "statistics layout");
+static_assert(sizeof(fvc_render_stats_t) == 128 && sizeof(fvc_cache_stats_t) == 32, "statistics layout");
 static_assert(sizeof(fvc_ray_result) == 16 && sizeof(fvc_camera_matrix) == 48, "BaseRayResult / CameraMatrix layout");
 
 /* ------------------------------------------------------------------------ */
@@ -1297,6 +1297,13 @@ extern "C" int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *o)
         o->n_rounds = iters;
         o->n_launches = 1 + (long long)(r->graph_kernels - 1) * (iters / 2);
     }
+    o->n_miss_outside_fov = (long long)s.n_reason[REASON_OUTSIDE_FOV];
+    o->n_miss_outside_depth = (long long)s.n_reason[REASON_OUTSIDE_DEPTH];
+    o->n_miss_before_near = (long long)s.n_reason[REASON_BEFORE_NEAR];
+    o->n_miss_beyond_known = (long long)s.n_reason[REASON_BEYOND_KNOWN];
+    o->n_drop_brick_unset = (long long)s.n_reason[REASON_BRICK_UNSET];
+    o->n_drop_voxel_empty = (long long)s.n_reason[REASON_VOXEL_EMPTY];
+    o->n_drop_alpha = (long long)s.n_reason[REASON_ALPHA];
     o->n_timed_launches = r->log.ev ? r->log.n_timed : 0;
     o->timed_kernel_ms = 0.0f;
     for (int i = 0; i < o->n_timed_launches; ++i) {

@@ -98,6 +98,24 @@ struct __align__(16) Voxel {
 };
 
 enum : int { KIND_RESAMPLE = 0, KIND_CACHE = 1, KIND_DROP = 2, KIND_SKIP = 3 };
+/* Why a cached render's sample is not a cache hit, kept in the upper bits of
+ * its row kind (row_kind = kind | reason << 2) and counted by the compositing
+ * kernel over the rows it composites or drops
+ * (sample_cache_performance_kernel, src/cache_performance_renderer.cu:91-163;
+ * sample_cache_kernel, src/cache_basic_renderer.cu:20-210). */
+enum : int {
+    REASON_NONE = 0,
+    REASON_OUTSIDE_FOV = 1,   /* resampled: outside the cache camera's image */
+    REASON_OUTSIDE_DEPTH = 2, /* resampled: inside the image, outside the froxel depth */
+    REASON_BEFORE_NEAR = 3,   /* resampled: before the cache's near plane */
+    REASON_BEYOND_KNOWN = 4,  /* resampled: beyond the pixel's known range (where its tile's build stopped) */
+    REASON_BRICK_UNSET = 5,   /* dropped: the froxel's brick holds no slot */
+    REASON_VOXEL_EMPTY = 6,   /* dropped: the voxel under the point holds no density (basic: not set) */
+    REASON_ALPHA = 7,         /* dropped (basic renderer): interpolated alpha not above the threshold */
+    N_REASONS = 8
+};
+__host__ __device__ constexpr int row_kind_of(int k) { return k & 3; }
+__host__ __device__ constexpr int row_reason_of(int k) { return k >> 2; }
 
 /* voxel (X, Y, Z) of the data array, or null outside it or in a slot the
  * last build did not write (the reference clears its arrays per build) */
@@ -154,6 +172,7 @@ struct __align__(16) RayState {
 struct RenderStatsDev {
     unsigned long long n_samples, n_resamples, n_cache_hits, n_dropped, n_steps;
     int n_rounds, pad;
+    unsigned long long n_reason[N_REASONS]; /* composited or dropped rows per REASON_* (cached renderers) */
 };
 
 /* one view's frustum cache with the camera and step grid it was built for */

@@ -40,6 +40,7 @@ namespace fvc {
 
 constexpr unsigned FULLMASK = 0xffffffffu;
 constexpr int S_ROWS = 16;        /* rows per ray and sub-iteration (the reference keeps up to 8) */
+static_assert(S_ROWS < 256, "the compositing kernel counts a ray's rows per miss reason in 8-bit fields");
 constexpr int NET_WARPS = 8;
 /* tcgen05 network kernel: CTAs resident per SM (launch bound and grid) and
  * hash levels whose gathers are in flight together.  Measured at 1080p on the
@@ -233,30 +234,42 @@ __global__ void wf_loop_cond_kernel(RenderParams p, cudaGraphConditionalHandle h
 /* march                                                                     */
 /* ------------------------------------------------------------------------- */
 
+/* Why a sample lies outside the cache's sampled region (REASON_*), or 0
+ * when it lies inside: the frustum and known-range tests of
+ * sample_cache_performance_kernel (src/cache_performance_renderer.cu:91-122),
+ * which both cache renderers share.  The sample is outside when any test
+ * fails; the reason named is the first failing one in the order image, near
+ * plane, known range, froxel depth. */
+__device__ __forceinline__ int unsampled_reason(const CacheView &C, const DevSteps &cst, float3 fr, float tfr)
+{
+    const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
+    if (!in_fov) return REASON_OUTSIDE_FOV;
+    const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
+    if (tfr < cst.near_) return REASON_BEFORE_NEAR;
+    if (tfr > kr) return REASON_BEYOND_KNOWN;
+    if (!(fr.z >= 0.f && fr.z < (float)C.fD)) return REASON_OUTSIDE_DEPTH;
+    return REASON_NONE;
+}
+
 /* Classification of one occupied sample, sample_cache_performance_kernel
- * (src/cache_performance_renderer.cu:91-163). */
+ * (src/cache_performance_renderer.cu:91-163): the row kind with its
+ * REASON_* in the upper bits. */
 __device__ __forceinline__ int classify(const RenderParams &p, const CacheView &C, const DevCam &ccam, const DevSteps &cst,
                                         float3 oc, float3 dc, float tm)
 {
     float tfr;
     const float3 fr = cam2froxel(at(oc, dc, tm), ccam, cst, tfr);
-    const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
-    const bool inside = in_fov && fr.z >= 0.f && fr.z < (float)C.fD;
-    bool unsampled = true;
-    if (in_fov) {
-        const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
-        unsampled = tfr < cst.near_ || tfr > kr;
-    }
-    if (!inside || unsampled) return p.render_mode == 1 ? KIND_SKIP : KIND_RESAMPLE;
+    const int why = unsampled_reason(C, cst, fr, tfr);
+    if (why) return (p.render_mode == 1 ? KIND_SKIP : KIND_RESAMPLE) | (why << 2);
     if (p.render_mode == 2) return KIND_SKIP;
     const int bx = (int)F_MUL(fr.x, 0.125f), by = (int)F_MUL(fr.y, 0.125f), bz = (int)F_MUL(fr.z, 0.125f);
     const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
-    if (packed < 0) return KIND_DROP;
+    if (packed < 0) return KIND_DROP | (REASON_BRICK_UNSET << 2);
     const float ax = F_ADD((float)(((packed >> 20) & 1023) * 8), F_SUB(fr.x, (float)(bx * 8)));
     const float ay = F_ADD((float)(((packed >> 10) & 1023) * 8), F_SUB(fr.y, (float)(by * 8)));
     const float az = F_ADD((float)((packed & 1023) * 8), F_SUB(fr.z, (float)(bz * 8)));
     const Voxel *v = texel(C, (int)floorf(ax), (int)floorf(ay), (int)floorf(az));
-    if (!v || !(__ldg(&v->density) > 0.0f)) return KIND_DROP;
+    if (!v || !(__ldg(&v->density) > 0.0f)) return KIND_DROP | (REASON_VOXEL_EMPTY << 2);
     return KIND_CACHE;
 }
 
@@ -299,14 +312,8 @@ __device__ __forceinline__ int classify_basic(const RenderParams &p, const Cache
 {
     float tfr;
     const float3 fr = cam2froxel(at(oc, dc, tm), ccam, cst, tfr);
-    const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
-    const bool inside = in_fov && fr.z >= 0.f && fr.z < (float)C.fD;
-    bool unsampled = true;
-    if (in_fov) {
-        const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
-        unsampled = tfr < cst.near_ || tfr > kr;
-    }
-    if (!inside || unsampled) return KIND_RESAMPLE;
+    const int why = unsampled_reason(C, cst, fr, tfr);
+    if (why) return KIND_RESAMPLE | (why << 2);
     /* froxel2data */
     const int bx = (int)F_MUL(fr.x, 0.125f), by = (int)F_MUL(fr.y, 0.125f), bz = (int)F_MUL(fr.z, 0.125f);
     float ix = F_SUB(fr.x, (float)(bx * 8)), iy = F_SUB(fr.y, (float)(by * 8)), iz = F_SUB(fr.z, (float)(bz * 8));
@@ -319,11 +326,11 @@ __device__ __forceinline__ int classify_basic(const RenderParams &p, const Cache
         iz = fminf(fmaxf(iz, 0.5f), 7.5f);
     }
     const int packed = __ldg(C.packed_index + ((size_t)bz * C.bY + by) * C.bX + bx);
-    if (packed < 0) return KIND_DROP;
+    if (packed < 0) return KIND_DROP | (REASON_BRICK_UNSET << 2);
     const float3 dp = make_float3(F_ADD((float)(((packed >> 20) & 1023) * 8), ix), F_ADD((float)(((packed >> 10) & 1023) * 8), iy),
                                   F_ADD((float)((packed & 1023) * 8), iz));
     const Voxel *vc = texel(C, (int)floorf(dp.x), (int)floorf(dp.y), (int)floorf(dp.z));
-    if (!vc || !(__ldg(&vc->isset) > 0.0f)) return KIND_DROP;
+    if (!vc || !(__ldg(&vc->isset) > 0.0f)) return KIND_DROP | (REASON_VOXEL_EMPTY << 2);
     /* fetchBrickTex3DInterpol for isset, the density slot and the latents */
     const Voxel *vp[8];
     float wc[8];
@@ -378,7 +385,7 @@ __device__ __forceinline__ int classify_basic(const RenderParams &p, const Cache
         break;
     }
     if (C.reweight && C.keep_first) ls[0] *= weight;
-    if (!(alpha > p.scene.alpha_thre)) return KIND_DROP;
+    if (!(alpha > p.scene.alpha_thre)) return KIND_DROP | (REASON_ALPHA << 2);
     const float div = C.reweight ? weight : 1.0f;
 #pragma unroll
     for (int j = 0; j < 8; ++j) lat[j] = ls[j] / div;
@@ -546,7 +553,7 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
     const RayState *states = p.states[it & 1];
     for (int base = blockIdx.x * blockDim.x; base < n_rows; base += gridDim.x * blockDim.x) {
         const int r = base + threadIdx.x;
-        int kind = KIND_SKIP;
+        int kind = KIND_SKIP, code = KIND_SKIP;
         float logd = 0.f, lat[8];
         if (r < n_rows) {
             const int slot = p.row_slot[r];
@@ -565,7 +572,8 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                 /* CacheBasicRenderer: lookup and resample position at the midpoint;
                  * a cache row keeps its looked-up density for compositing */
                 float density = 0.f;
-                kind = classify_basic(p, C, ccam, cst, oc, dc, tm, dt, lat, density);
+                code = classify_basic(p, C, ccam, cst, oc, dc, tm, dt, lat, density);
+                kind = row_kind_of(code);
                 if (kind == KIND_RESAMPLE) {
                     const float3 pc = contract(p.scene, at(o, d, tm));
                     p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
@@ -577,7 +585,8 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                 }
             } else {
                 const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));
-                kind = classify(p, C, ccam, cst, oc, dc, tm);
+                code = classify(p, C, ccam, cst, oc, dc, tm);
+                kind = row_kind_of(code);
                 if (kind == KIND_RESAMPLE) {
                     const float3 pc = contract(p.scene, at(o, d, tmh));
                     p.row_pay[r] = make_float4(pc.x, pc.y, pc.z, 0.f);
@@ -592,7 +601,7 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
                     }
                 }
             }
-            p.row_kind[r] = (uint8_t)kind;
+            p.row_kind[r] = (uint8_t)code;
         }
         const unsigned m0 = __ballot_sync(FULLMASK, kind == KIND_RESAMPLE), m1 = __ballot_sync(FULLMASK, kind == KIND_CACHE);
         int b0 = 0, b1 = 0;
@@ -1172,6 +1181,7 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
         bool keep = false;
         RayState st;
         int n_comp = 0;
+        unsigned long long why = 0; /* rows per REASON_* 1..7, 8 bits each (at most S_ROWS rows a ray and sub-iteration) */
         if (valid) {
             st = cur[i];
             const int2 rr = p.ray_rows[i];
@@ -1182,7 +1192,9 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
              * streams of accumulate_cache_perf_kernel (:270-304) */
             for (int j = 0; j < rr.y; ++j) {
                 const int r = rr.x + j;
-                const int kind = CACHED ? (int)p.row_kind[r] : KIND_RESAMPLE;
+                const int code = CACHED ? (int)p.row_kind[r] : KIND_RESAMPLE;
+                const int kind = row_kind_of(code);
+                if (CACHED && kind != KIND_SKIP && row_reason_of(code)) why += 1ull << (8 * (row_reason_of(code) - 1));
                 if (kind >= KIND_DROP) {
                     c_drop += kind == KIND_DROP;
                     continue;
@@ -1221,6 +1233,13 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
         }
         const int ws = __reduce_add_sync(FULLMASK, n_comp);
         if (lane_id() == 0 && ws) atomicAdd(&p.stats->n_samples, (unsigned long long)ws);
+        if (CACHED && __any_sync(FULLMASK, why != 0)) {
+#pragma unroll
+            for (int q = 1; q < N_REASONS; ++q) {
+                const unsigned c = __reduce_add_sync(FULLMASK, (unsigned)(why >> (8 * (q - 1))) & 255u);
+                if (lane_id() == 0 && c) atomicAdd(&p.stats->n_reason[q], (unsigned long long)c);
+            }
+        }
         const unsigned m = __ballot_sync(FULLMASK, keep);
         int nb = 0;
         if (lane_id() == 0 && m) nb = atomicAdd(p.counters + ((it + 1) & 1), __popc(m));
@@ -1261,7 +1280,7 @@ __global__ void __launch_bounds__(128) wf_composite_bwd_kernel(RenderParams p, i
             for (int j = 0; j < rr.y; ++j) {
                 const int r = rr.x + j;
                 float4 dout = make_float4(0.f, 0.f, 0.f, 0.f);
-                const int kind = CACHED ? (int)p.row_kind[r] : KIND_RESAMPLE;
+                const int kind = CACHED ? row_kind_of(p.row_kind[r]) : KIND_RESAMPLE;
                 if (!term && kind < KIND_DROP) {
                     const uint2 ov = p.row_out[r];
                     const float t0 = p.row_t0[r];

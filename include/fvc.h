@@ -146,6 +146,23 @@ typedef struct {
     long long n_launches;            /* kernels launched by the last render  */
     int n_timed_launches;            /* resample network launches timed      */
     float timed_kernel_ms;           /* their summed event time (0 = off)    */
+    /* Cached renderers: why samples were not served by the cache, over the
+     * samples composited or dropped (no counterpart in the reference, whose
+     * _render_stats keep only the totals).  A sample outside several tests
+     * counts under the first in the order image, near plane, known range,
+     * froxel depth.  Resampled: */
+    long long n_miss_outside_fov;    /* outside the cache camera's image         */
+    long long n_miss_outside_depth;  /* in the image, outside the froxel depth   */
+    long long n_miss_before_near;    /* before the cache's near plane            */
+    long long n_miss_beyond_known;   /* beyond the pixel's known range: where its
+                                      * tile's build stopped (opacity, the frustum
+                                      * depth, or no slot left)                  */
+    /* dropped: */
+    long long n_drop_brick_unset;    /* the froxel's brick holds no slot         */
+    long long n_drop_voxel_empty;    /* the voxel under the point holds no density
+                                      * (basic renderer: is not set)             */
+    long long n_drop_alpha;          /* basic renderer: interpolated alpha not
+                                      * above the threshold                      */
 } fvc_render_stats_t;
 
 typedef struct {

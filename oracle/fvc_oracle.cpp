@@ -1107,8 +1107,9 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         kr = cc->known_ranges[(size_t)(int)floorf(fp.y) * cd.fW + (int)floorf(fp.x)];
                         unsampled = tfr < cst->near_ || tfr > kr;
                     }
-                    /* why the sample is outside the cache's sampled region (0: inside) */
-                    const int why_out = !in_fov ? 1 : !inside ? 2 : tfr < cst->near_ ? 3 : tfr > kr ? 4 : 0;
+                    /* why the sample is outside the cache's sampled region (0: inside): the first failing
+                     * test in the order image, near plane, known range, froxel depth */
+                    const int why_out = !in_fov ? 1 : tfr < cst->near_ ? 3 : tfr > kr ? 4 : !inside ? 2 : 0;
                     int kind = 0; /* 0 resample, 1 cache, 2 drop */
                     double blat[8], bsigma = 0.0;
                     if (cc->basic) {

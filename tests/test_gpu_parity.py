@@ -183,6 +183,14 @@ def test_cache_build_parity(request, fixture, W, H):
     assert np.abs(lat - olat).max() < 2e-3
 
 
+MISS_FIELDS = {
+    "outside_fov": "n_miss_outside_fov", "outside_depth": "n_miss_outside_depth",
+    "before_near": "n_miss_before_near", "beyond_known": "n_miss_beyond_known",
+    "brick_unset": "n_drop_brick_unset", "voxel_empty": "n_drop_voxel_empty", "alpha": "n_drop_alpha",
+}
+RESAMPLE_REASONS = ("outside_fov", "outside_depth", "before_near", "beyond_known")
+
+
 @pytest.mark.parametrize("tcgen05", [False, True], ids=["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
 def test_cached_render_parity(request, fixture, W, H, tcgen05):
@@ -201,8 +209,19 @@ def test_cached_render_parity(request, fixture, W, H, tcgen05):
     cam1 = fcam.camera_dict(c2w_new, W, H)
     buf = fvc.RenderBuffer((W, H))
     r.render(fvc.raymarch_info(cam1, loader.stepsize_info), buf)
-    ref, counts = om.render_cached(cam1, oc)
+    ref, counts, why = om.render_cached(cam1, oc, reasons=True)
     live = ref[..., 3] >= 1e-4
+    # miss breakdown: every resampled sample under its first failing test, every drop under its cause
+    # (drops are compared on live rays below: a ray whose T crosses 1e-4 within rounding of the
+    # float64 oracle may stop one dropped sample apart, so drop causes may differ by that much)
+    st = r._render_stats
+    got = {k: int(getattr(st, f)) for k, f in MISS_FIELDS.items()}
+    for k in RESAMPLE_REASONS:
+        assert got[k] == why[k], (k, got, why)
+    slack = int(np.abs(buf.ray_counts[..., 2][~live] - counts[..., 2][~live]).sum())
+    for k in set(MISS_FIELDS) - set(RESAMPLE_REASONS):
+        assert abs(got[k] - why[k]) <= slack, (k, got, why, slack)
+    assert sum(got[k] for k in RESAMPLE_REASONS) == int(counts[..., 0].sum())
     np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])  # resample
     np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])  # cache
     np.testing.assert_array_equal(buf.ray_counts[..., 2][live], counts[..., 2][live])  # dropped
