@@ -95,7 +95,7 @@ class ModelProps(C.Structure):
 
 class AutotuneResult(C.Structure):
     _fields_ = [("m_tile", c_int), ("steps_per_iter", c_int), ("rows_per_iteration", C.c_longlong), ("ms", C.c_float),
-                ("n_candidates", c_int)]
+                ("n_candidates", c_int), ("batch_rows", c_int), ("reserved", c_int)]
 
 
 class CacheStats(C.Structure):
@@ -105,7 +105,7 @@ class CacheStats(C.Structure):
 
 assert C.sizeof(SceneInfo) == 76 and C.sizeof(StepsizeInfo) == 48
 assert C.sizeof(CameraInfo) == 144 and CameraInfo.cam2world.offset == 32 and CameraInfo.world2cam.offset == 80
-assert C.sizeof(RenderStats) == 128 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 24
+assert C.sizeof(RenderStats) == 128 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 32
 assert C.sizeof(RaymarchInfo) == 352 and RaymarchInfo.stepsize_info.offset == 288 and RaymarchInfo.sample_index.offset == 336
 
 FVC_OK = 0
@@ -149,6 +149,7 @@ SIGNATURES = {
     "fvc_cache_dims": (c_int, [P, C.POINTER(Int3), C.POINTER(Int3), C.POINTER(Int3)]),
     "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
+    "fvc_renderer_set_tiling": (c_int, [P, c_int, c_int]),
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_renderer_set_precision": (c_int, [P, c_int]),
     "fvc_render_batch": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs)]),

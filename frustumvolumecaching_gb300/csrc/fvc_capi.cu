@@ -413,7 +413,9 @@ struct fvc_renderer {
     int graph_head_hidden = 0;
     int graph_kernels = 0;            /* kernels of one loop body + prologue */
     bool last_was_graph = false;
-    int steps_per_iter = 64;          /* marching steps per sub-iteration (autotuned) */
+    int steps_per_iter = 64;          /* marching steps per sub-iteration */
+    int m_tile = 128;                 /* tcgen05 network tile of the plain path (autotuned) */
+    int row_target = 0;               /* compaction batch, rows per sub-iteration (0: the row capacity; autotuned) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
     int *d_grad_rows = nullptr;       /* resample rows with a gradient */
     int *d_grad_cache_rows = nullptr; /* cache rows with a gradient */
@@ -1218,6 +1220,8 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.counters = r->d_wf_counters;
     p.row_capacity = r->row_capacity;
     p.steps_per_iter = r->steps_per_iter;
+    p.m_tile = r->m_tile;
+    p.row_target = std::min(r->row_target, r->row_capacity);
     return FVC_OK;
 }
 
@@ -1748,6 +1752,15 @@ extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
     return FVC_OK;
 }
 
+extern "C" int fvc_renderer_set_tiling(fvc_renderer *r, int m_tile, int batch_rows)
+{
+    CHECK_ARG(r && (m_tile == 64 || m_tile == 128 || m_tile == 256) && (batch_rows == 0 || (batch_rows >= 1024 && batch_rows <= (1 << 26))),
+              "fvc_renderer_set_tiling: m_tile must be 64, 128 or 256 and batch_rows 0 or in [2^10, 2^26]");
+    r->m_tile = m_tile;
+    r->row_target = batch_rows;
+    return FVC_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* differentiable render                                                     */
 /* ------------------------------------------------------------------------ */
@@ -2107,18 +2120,22 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
     CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
     if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     std::lock_guard<std::mutex> lk(r->read_mutex);
-    const int tiles[2] = {128, 32};        /* tcgen05 CTA tile, mma.sync warp tile */
-    const int steps[4] = {16, 32, 64, 128}; /* marching steps per ray and sub-iteration */
+    /* candidates: the tcgen05 tile heights and the 32-row mma.sync warp tile, each with compaction
+     * batches of 2^16..2^20 rows per sub-iteration */
+    const int tiles[4] = {64, 128, 256, 32};
+    const int batches[5] = {1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20};
+    const int saved_tc = r->use_tc, saved_tile = r->m_tile, saved_target = r->row_target;
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
     float best = 1e30f;
-    int best_tile = 128, best_steps = 64, n_cand = 0, rc = FVC_OK;
+    int best_tile = 0, best_batch = 0, n_cand = 0, rc = FVC_OK;
     long long best_rows = 0;
-    for (int ti = 0; ti < 2 && rc == FVC_OK; ++ti)
-        for (int si = 0; si < 4 && rc == FVC_OK; ++si) {
-            r->use_tc = tiles[ti] == 128;
-            r->steps_per_iter = steps[si];
+    for (int ti = 0; ti < 4 && rc == FVC_OK; ++ti)
+        for (int bi = 0; bi < 5 && rc == FVC_OK; ++bi) {
+            r->use_tc = tiles[ti] != 32;
+            r->m_tile = tiles[ti] == 32 ? 128 : tiles[ti];
+            r->row_target = batches[bi];
             RenderParams p;
             int n_rays = 0;
             if ((rc = batch_setup(r, infos, n_views, out, p, n_rays))) break;
@@ -2138,19 +2155,25 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
             if (ms < best) {
                 best = ms;
                 best_tile = tiles[ti];
-                best_steps = steps[si];
+                best_batch = batches[bi];
                 best_rows = (long long)st.n_samples / std::max(1, iters);
             }
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    r->use_tc = best_tile == 128;
-    r->steps_per_iter = best_steps;
-    if (rc) return rc;
+    if (rc) {
+        r->use_tc = saved_tc; r->m_tile = saved_tile; r->row_target = saved_target;
+        return rc;
+    }
+    r->use_tc = best_tile != 32;
+    r->m_tile = best_tile == 32 ? 128 : best_tile;
+    r->row_target = best_batch;
     res->m_tile = best_tile;
-    res->steps_per_iter = best_steps;
+    res->steps_per_iter = r->steps_per_iter;
     res->rows_per_iteration = best_rows;
     res->ms = best;
     res->n_candidates = n_cand;
+    res->batch_rows = best_batch;
+    res->reserved = 0;
     return FVC_OK;
 }

@@ -253,9 +253,10 @@ __device__ __forceinline__ float2 f2_lerp(float2 a, float2 b, float t)
  * all issued before any of them is consumed, so a thread keeps 8*LG gathers
  * in flight instead of 8. */
 template <int LG = 4>
-__device__ __forceinline__ void hash_encode(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out)
+__device__ __forceinline__ void hash_encode_levels(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out,
+                                                   int l_begin, int l_end)
 {
-    for (int l0 = 0; l0 < g.n_levels; l0 += LG) {
+    for (int l0 = l_begin; l0 < l_end; l0 += LG) {
         __half2 v[LG][8];
         float wx[LG], wy[LG], wz[LG];
 #pragma unroll
@@ -301,6 +302,13 @@ __device__ __forceinline__ void hash_encode(const DevGrid &g, const __half2 *__r
             out[l0 + j] = __float22half2_rn(f2_lerp(g0, g1, wz[j]));
         }
     }
+}
+
+/* all levels of the grid (features of level l in out[l]) */
+template <int LG = 4>
+__device__ __forceinline__ void hash_encode(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out)
+{
+    hash_encode_levels<LG>(g, table, pos, out, 0, g.n_levels);
 }
 
 /* SH degree 4 (16 values) of a unit_to_01 direction, written as 8 half2.

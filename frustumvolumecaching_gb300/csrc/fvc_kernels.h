@@ -225,6 +225,9 @@ struct RenderParams {
     int *counters;              /* [0], [1] alive rays (ping-pong), [2] rows, [3] resample, [4] cache */
     int row_capacity;           /* rows per sub-iteration */
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
+    int m_tile;                 /* rows per tcgen05 network tile on the plain path: 64, 128 (0 = 128) or 256 */
+    int row_target;             /* compaction batch: rows per sub-iteration the march aims at, samples per ray
+                                 * = clamp(row_target / alive rays, 1, S_ROWS) (0 = row_capacity) */
     int basic_cache;            /* 1: CacheBasicRenderer semantics for the cached rows (classify_basic) */
     int view_dependent;         /* split head (mlp_first_head): first head + SH-difference head input */
     const uint8_t *weights_vd;  /* VD_WBYTES of K-major tiles of the view-dependent network */

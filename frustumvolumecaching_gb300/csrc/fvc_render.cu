@@ -408,7 +408,11 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
 {
     const int n_alive = p.counters[it & 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) p.counters[(it + 1) & 1] = 0; /* next alive count */
-    const int S = max(1, min(S_ROWS, p.row_capacity / max(1, n_alive)));
+    /* samples per ray this sub-iteration: the compaction batch (row_target, else the row capacity)
+     * over the alive rays, clamped to [1, S_ROWS] as n_steps_curr_subiter of
+     * src/performance_renderer.cu:249 (the host keeps row_target <= row_capacity) */
+    const int batch = p.row_target > 0 ? p.row_target : p.row_capacity;
+    const int S = max(1, min(S_ROWS, batch / max(1, n_alive)));
     RayState *states = p.states[it & 1];
     for (int base = blockIdx.x * blockDim.x; base < n_alive; base += gridDim.x * blockDim.x) {
         const int i = base + threadIdx.x;
@@ -961,6 +965,193 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
 }
 
 /* ------------------------------------------------------------------------- */
+/* the network on tile heights M = 64 and M = 256 (resample rows)            */
+/* ------------------------------------------------------------------------- */
+/* The layers, weights, epilogue arithmetic and bounded waits of
+ * wf_net_tc_kernel, on other tile heights for the batch autotuner.
+ * M = 256: 256 threads, thread t owns row t.  The operand is one 256-row
+ * K-major tile and each layer issues two M = 128 MMAs: rows 0..127 into TMEM
+ * columns 0..63, rows 128..255 into columns 64..127.  Warp w reads TMEM lanes
+ * 32 (w mod 4)..+31 of its half's columns.
+ * M = 64: one M = 64 MMA per layer, whose accumulator rows 16q..16q+15 sit in
+ * TMEM lanes 32q..32q+15.  128 threads: lanes 0..15 of warp q own rows
+ * 16q..16q+15 and run the epilogues; for the hash features both half-warps
+ * work on the same 16 rows, lanes 16..31 taking the upper levels, so each
+ * thread's chain of dependent gathers is half as long. */
+template <int MT>
+struct __align__(128) TcmSmem {
+    uint8_t W[TC_WBYTES];
+    uint8_t X[MT * 64 * 2];
+    float bias3[64];
+    uint64_t mbar;
+    uint32_t tmem_base;
+};
+template <int MT> __host__ __device__ constexpr int tcm_threads() { return MT == 64 ? 128 : MT; }
+template <int MT> __host__ __device__ constexpr int tcm_cols() { return MT == 256 ? 128 : 64; }
+template <int MT> __host__ __device__ constexpr int tcm_ctas_per_sm() { return MT == 256 ? 3 : FVC_TC_CTAS_PER_SM; }
+static_assert(tcm_ctas_per_sm<256>() * tcm_cols<256>() <= 512 && tcm_ctas_per_sm<64>() * tcm_cols<64>() <= 512,
+              "resident CTAs must fit in the SM's 512 TMEM columns");
+
+template <int MT>
+__device__ __forceinline__ void tcm_layer(uint32_t tmem, const uint8_t *a, const uint8_t *b, int K, int N)
+{
+    const uint32_t sbo = (uint32_t)(K / 8) * 128u;
+    const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
+    const uint32_t id = idesc_f16(MT == 64 ? 64 : 128, N, false);
+#pragma unroll
+    for (int h = 0; h < (MT == 256 ? 2 : 1); ++h)
+        for (int kc = 0; kc < K / 16; ++kc)
+            tc_mma_f16(tmem + 64u * h, umma_desc(a0 + (uint32_t)h * 16u * sbo + 256u * kc, 128u, sbo),
+                       umma_desc(b0 + 256u * kc, 128u, sbo), id, kc > 0 ? 1u : 0u);
+}
+
+template <int MT>
+__device__ __forceinline__ bool tcm_run(TcmSmem<MT> &S, uint32_t tmem, const uint8_t *b, int K, int N, uint32_t &phase)
+{
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        tcm_layer<MT>(tmem, S.X, b, K, N);
+        tc_commit(&S.mbar);
+    }
+    const bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    tc_fence_after();
+    return ok;
+}
+
+/* epi_hidden with the row's writes limited to the threads that own a row
+ * (the TMEM loads are warp-collective and run on every lane) */
+__device__ __forceinline__ void epi_hidden_own(uint32_t taddr, const float *bias, uint8_t *dst, int row, bool own)
+{
+    const __half2 zero = __float2half2_rn(0.0f);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float v[32];
+        tmem_ld32(taddr + 32 * h, v);
+        tmem_wait_ld();
+        uint32_t w[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            float2 x = make_float2(v[2 * i], v[2 * i + 1]);
+            if (bias) x = __fadd2_rn(x, make_float2(bias[32 * h + 2 * i], bias[32 * h + 2 * i + 1]));
+            const __half2 r = __hmax2(__float22half2_rn(x), zero);
+            w[i] = *reinterpret_cast<const uint32_t *>(&r);
+        }
+        if (own) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) st_chunk(dst, row, 4 * h + q, 64, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
+        }
+    }
+}
+
+template <int MT, int HH, bool LIST>
+__global__ void __launch_bounds__(tcm_threads<MT>(), tcm_ctas_per_sm<MT>()) wf_net_tcm_kernel(RenderParams p, int it)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TcmSmem<MT> &S = *reinterpret_cast<TcmSmem<MT> *>(smem_raw);
+    const int n_rows = LIST ? p.counters[3] : p.counters[2];
+    if (n_rows == 0) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int trow = MT == 64 ? 16 * warp + (lane & 15) : tid; /* the tile row this thread works on */
+    const bool own = MT == 64 ? lane < 16 : true;                /* ... and whose epilogues it runs */
+    const int upper = MT == 64 ? lane >> 4 : 0;
+    if (tid == 0) {
+        mbar_init(&S.mbar, 1);
+        mbar_arrive_expect_tx(&S.mbar, TC_WBYTES);
+        bulk_copy_g2s(S.W, p.weights_tc, TC_WBYTES, &S.mbar);
+    }
+    if (tid < 64) S.bias3[tid] = p.bias3[tid];
+    if (warp == 0) tmem_alloc(&S.tmem_base, tcm_cols<MT>());
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (MT == 256 && tid >= 128 ? 64u : 0u);
+    const RayState *states = p.states[it & 1];
+    /* levels of the lower half-warp (M = 64): a multiple of 4, so each half writes whole 8-value chunks */
+    const int l_split = 4 * ((p.grid.n_levels + 7) / 8);
+    uint32_t phase = 0;
+    bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    const int n_tiles = (n_rows + MT - 1) / MT;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int k = tile * MT + trow;
+        const int r = k < n_rows ? (LIST ? p.res_list[k] : k) : -1;
+        /* ---- hash features -> tile (K = 32) ---- */
+        __half2 feat[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+        const int lb = upper ? l_split : 0, le = upper ? p.grid.n_levels : min(l_split, p.grid.n_levels);
+        if (r >= 0) {
+            const float4 pw = p.row_pay[r];
+            if (MT == 64) hash_encode_levels<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat, lb, le);
+            else hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
+        }
+        if (MT == 64) {
+            const int c0 = upper ? l_split / 4 : 0, c1 = upper ? 4 : l_split / 4;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c >= c0 && c < c1) st_chunk(S.X, trow, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) st_chunk(S.X, trow, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
+        }
+        if (!(ok = tc_publish(ok))) break;
+        /* ---- layer 1: 32 -> 64, ReLU ---- */
+        ok = tcm_run<MT>(S, tmem, S.W + TC_B1, 32, 64, phase);
+        epi_hidden_own(taddr, nullptr, S.X, trow, own);
+        if (!(ok = tc_publish(ok))) break;
+        /* ---- layer 2: 64 -> 16 (log-density, latents) ---- */
+        ok = tcm_run<MT>(S, tmem, S.W + TC_B2, 64, 16, phase);
+        uint16_t log_density = 0;
+        {
+            float v[16];
+            tmem_ld16(taddr, v);
+            tmem_wait_ld();
+            const uint4 b0 = pack8(v), b1 = pack8(v + 8);
+            log_density = (uint16_t)(b0.x & 0xffffu);
+            __half2 sh[8];
+            if (r >= 0 && own) sh16(dir01_of(states, p.row_slot[r]), sh);
+            else for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
+            if (own) {
+                st_chunk(S.X, trow, 0, 32, b0);
+                st_chunk(S.X, trow, 1, 32, b1);
+                st_chunk(S.X, trow, 2, 32, *reinterpret_cast<const uint4 *>(sh));
+                st_chunk(S.X, trow, 3, 32, *reinterpret_cast<const uint4 *>(sh + 4));
+            }
+        }
+        if (!(ok = tc_publish(ok))) break;
+        /* ---- head layer 1: (latents | SH) 32 -> 64, bias from the 1-padding, ReLU ---- */
+        ok = tcm_run<MT>(S, tmem, S.W + TC_B3, 32, 64, phase);
+        epi_hidden_own(taddr, S.bias3, S.X, trow, own);
+        if (!(ok = tc_publish(ok))) break;
+        if (HH == 2) {
+            /* ---- head layer 2: 64 -> 64, ReLU ---- */
+            ok = tcm_run<MT>(S, tmem, S.W + TC_B4, 64, 64, phase);
+            epi_hidden_own(taddr, nullptr, S.X, trow, own);
+            if (!(ok = tc_publish(ok))) break;
+        }
+        /* ---- output layer: 64 -> 16 (rgb logits in cols 0..2) ---- */
+        ok = tcm_run<MT>(S, tmem, S.W + TC_B5, 64, 16, phase);
+        float o[16];
+        tmem_ld16(taddr, o);
+        tmem_wait_ld();
+        if (r >= 0 && own)
+            p.row_out[r] = make_uint2(pack_h2(o[0], o[1]),
+                                      (uint32_t)__half_as_ushort(__float2half_rn(o[2])) | ((uint32_t)log_density << 16));
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+    }
+    if (!ok && tid == 0) atomicOr(p.guard, 16);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, tcm_cols<MT>());
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* tcgen05 network kernel at reduced precision (plain path, resample rows)   */
 /* ------------------------------------------------------------------------- */
 /* PREC 1, BF16: kind::f16 with bf16 operands; hash features, SH and every
@@ -1194,7 +1385,7 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
                 const int r = rr.x + j;
                 const int code = CACHED ? (int)p.row_kind[r] : KIND_RESAMPLE;
                 const int kind = row_kind_of(code);
-                if (CACHED && kind != KIND_SKIP && row_reason_of(code)) why += 1ull << (8 * (row_reason_of(code) - 1));
+                if (CACHED && kind != KIND_SKIP && row_reason_of(code)) why += 1ull << ((8 * (row_reason_of(code) - 1)) & 63);
                 if (kind >= KIND_DROP) {
                     c_drop += kind == KIND_DROP;
                     continue;
@@ -1530,6 +1721,8 @@ static cudaError_t set_net_attrs()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tcm_kernel<64, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcmSmem<64>));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tcm_kernel<256, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcmSmem<256>));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<1, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<2, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     const int vsmem = (int)sizeof(VdSmem);
@@ -1556,6 +1749,10 @@ static void launch_plain_net(const RenderParams &p, int it, int n_sms, cudaStrea
     else if (!p.use_tc) wf_net_resample_kernel<HH, false><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
     else if (p.precision == 1) wf_net_tc_prec_kernel<1, HH><<<n_sms * TC_PREC_CTAS_PER_SM, 128, tc_smem, s>>>(p, it);
     else if (p.precision == 2) wf_net_tc_prec_kernel<2, HH><<<n_sms * TC_PREC_CTAS_PER_SM, 128, tc_smem, s>>>(p, it);
+    else if (p.m_tile == 64)
+        wf_net_tcm_kernel<64, HH, false><<<n_sms * tcm_ctas_per_sm<64>(), tcm_threads<64>(), sizeof(TcmSmem<64>), s>>>(p, it);
+    else if (p.m_tile == 256)
+        wf_net_tcm_kernel<256, HH, false><<<n_sms * tcm_ctas_per_sm<256>(), tcm_threads<256>(), sizeof(TcmSmem<256>), s>>>(p, it);
     else wf_net_tc_kernel<0, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
 }
 

@@ -305,6 +305,13 @@ int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
  * counterpart (the reference runs tiny-cuda-nn's FullyFusedMLP). */
 int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05);
 
+/* Rows per tcgen05 network tile of the plain path (64, 128 or 256; FP16, not
+ * view-dependent; default 128) and the compaction batch, the rows per
+ * sub-iteration the march aims at (0: the renderer's row capacity, the
+ * default; else in [2^10, 2^26], capped at the capacity).  Results do not
+ * depend on either: every row's arithmetic is the same. */
+int fvc_renderer_set_tiling(fvc_renderer *r, int m_tile, int batch_rows);
+
 /* MLP precision of the plain renderers on the tcgen05 path (no counterpart
  * in the reference, whose MLPs are fp16): FP16 (default), BF16, or
  * FP8-E4M3 with per-layer weight scaling and per-row activation scaling;
@@ -418,15 +425,20 @@ int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_view
 int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, fvc_cache *const *caches,
                             const fvc_render_outputs *out);
 
-/* Times each candidate network tile (128-row tcgen05 CTA tiles or 32-row
- * mma.sync warp tiles) and marching batch (16, 32, 64 or 128 steps per ray
- * and sub-iteration) on this batch, keeps the fastest for the renderer. */
+/* Times each candidate network tile (tcgen05 tiles of 64, 128 or 256 rows,
+ * or 32-row mma.sync warp tiles) with each compaction batch (2^16..2^20
+ * rows per sub-iteration: a ray takes clamp(batch / alive rays, 1, 16)
+ * samples a sub-iteration, n_steps_curr_subiter of
+ * src/performance_renderer.cu:249) on this batch of views, 20 candidates in
+ * all, and keeps the fastest for the renderer. */
 typedef struct {
-    int m_tile;                  /* rows per network tile of the winner */
+    int m_tile;                  /* rows per network tile of the winner (32: the mma.sync path) */
     int steps_per_iter;          /* marching steps per ray and sub-iteration */
-    long long rows_per_iteration;/* samples per sub-iteration it produced (compaction batch) */
+    long long rows_per_iteration;/* mean rows per sub-iteration the winner produced */
     float ms;                    /* its time per batch */
     int n_candidates;
+    int batch_rows;              /* the winner's compaction batch */
+    int reserved;
 } fvc_autotune_result;
 int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
                           fvc_autotune_result *res);

@@ -21,7 +21,10 @@
  *   int32 n_pix; int32 pix[2*n_pix]; int32 max_steps;
  *   int32 n_pts; float pts[3*n_pts];
  *   uint8 grid[nlvl*128^3]
- * Output: see write_out below.
+ * Output: see write_out below.  With a third argument it also writes the
+ * input of the device march (ref_golden_dev.cu): sizeof(RaymarchInfo),
+ * sizeof(SceneInfo), both structs' bytes, the pixel list, max_steps, nlvl and
+ * the Morton bitfield.
  */
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -39,7 +42,7 @@ template <class T> static void wr(FILE *f, const T *p, size_t n = 1) { fwrite(p,
 
 int main(int argc, char **argv)
 {
-    if (argc != 3) { fprintf(stderr, "usage: ref_golden in.bin out.bin\n"); return 1; }
+    if (argc != 3 && argc != 4) { fprintf(stderr, "usage: ref_golden in.bin out.bin [device_input.bin]\n"); return 1; }
     FILE *fi = fopen(argv[1], "rb");
     if (!fi) return 1;
     int nlvl, contraction;
@@ -83,6 +86,18 @@ int main(int argc, char **argv)
         const int lvl = i / vals, j = i % vals;
         const uint32_t x = morton3D_invert(j >> 0), y = morton3D_invert(j >> 1), z = morton3D_invert(j >> 2);
         if (grid[(size_t)lvl * vals + x * R * R + y * R + z]) bits[i / 8] |= (uint8_t)(1u << (i % 8));
+    }
+
+    if (argc == 4) {
+        /* input of ref_golden_dev.cu's device march: the structs as the reference's host hands them
+         * to its kernels, the Morton bitfield and the pixel list */
+        FILE *fd = fopen(argv[3], "wb");
+        if (!fd) return 1;
+        const int srm = (int)sizeof(RaymarchInfo), ssi = (int)sizeof(SceneInfo), nb = (int)bits.size();
+        wr(fd, &srm); wr(fd, &ssi); wr(fd, &rm); wr(fd, &si);
+        wr(fd, &n_pix); wr(fd, pix.data(), pix.size()); wr(fd, &max_steps);
+        wr(fd, &nlvl); wr(fd, &nb); wr(fd, bits.data(), bits.size());
+        fclose(fd);
     }
 
     FILE *fo = fopen(argv[2], "wb");

@@ -171,3 +171,121 @@ def test_backward_one_hidden_layer_head(tcgen05):
         cos, rel = _compare(a.astype(np.float64), b)
         print(f"one-hidden-layer head {name}: cos {cos:.6f} rel {rel:.3e}")
         assert cos > 0.9999 and rel < 2e-3, (name, cos, rel)
+
+
+H_FD = 1e-4      # central-difference step of the float64 oracle loss
+SMOOTH = 1e-4    # an entry is smooth when its differences at h and h/2 agree to this (relative)
+FD_REL = 1e-3    # the gradient bound
+
+
+def _fd(om, cam, pix, tgt, group, k):
+    def d(h):
+        lp = om.loss_grad(cam, pix, tgt, grads=False, perturb=([group], [k], [h]))[0]
+        lm = om.loss_grad(cam, pix, tgt, grads=False, perturb=([group], [k], [-h]))[0]
+        return (lp - lm) / (2 * h)
+    return d(H_FD), d(0.5 * H_FD)
+
+
+@pytest.mark.parametrize("group", [0, 1, 2], ids=["hash_table", "density_mlp", "color_head"])
+def test_device_gradients_against_central_differences(group):
+    """Device gradients (fp16 MLPs on tcgen05, fp32 adjoint) against float64
+    central differences of the oracle's loss on 86 sampled parameters per
+    group (258 in all).
+
+    Kink rule: a perturbation of +-h can cross a ReLU kink or move a ray's
+    early termination, where the loss is not differentiable; an entry whose
+    differences at h and h/2 disagree by more than 1e-4 (relative) is such a
+    crossing and is left out.  On the smooth entries the bound is 1e-3
+    relative to max(|fd|, 1e-2 * max|fd| of the group): entries two orders
+    below the group's largest are held to 1e-5 of it absolutely, the scale
+    at which the fp16 rounding of the forward activations (the device's
+    arithmetic) sets the floor."""
+    torch, d, loader, cam, pix, tgt = _case(W=24, H=24, n=64)
+    _, g, _ = _gpu(torch, loader, cam, pix, tgt)
+    dev = g.read()[group].astype(np.float64)
+    om = orc.OracleModel(d, mimic_fp16=False)
+    _, *exact, _ = om.loss_grad(cam, pix, tgt)
+    nz = np.flatnonzero(exact[group])
+    assert nz.size > 100
+    pick = np.random.default_rng(17 + group).choice(nz, 86, replace=False)
+    fd = np.array([_fd(om, cam, pix, tgt, group, int(k)) for k in pick])
+    smooth = np.abs(fd[:, 0] - fd[:, 1]) <= SMOOTH * np.maximum(np.abs(fd[:, 0]), 1e-12)
+    f = fd[smooth, 0]
+    a = dev[pick][smooth]
+    scale = np.maximum(np.abs(f), 1e-2 * np.abs(f).max())
+    rel = np.abs(a - f) / scale
+    cos = float(a @ f / (np.linalg.norm(a) * np.linalg.norm(f)))
+    print(f"\nFD {['table', 'base', 'head'][group]}: smooth {int(smooth.sum())}/86, rel median {np.median(rel):.2e} "
+          f"p95 {np.quantile(rel, 0.95):.2e} max {rel.max():.2e}, within 1e-3 {np.mean(rel <= FD_REL):.3f}, cos {cos:.7f}")
+    assert smooth.sum() >= 30
+    assert np.median(rel) <= FD_REL and np.quantile(rel, 0.95) <= 10 * FD_REL, rel
+    assert cos > 0.99999
+
+
+class RenderLoss:
+    """Test-harness torch.autograd.Function over fvc_render_backward: the mean
+    squared error of the plain render at `pixels` against `target`, with the
+    model's parameters as differentiable inputs (table, density-MLP blob,
+    color-head blob, each fp32 in the model file layout).  The renderer reads
+    its parameters from the loaded model, so the tensors stand for them and
+    must not be modified in place between forward and backward; target is
+    differentiable too (dL/dtarget = -2/n (C + T - target))."""
+
+    @staticmethod
+    def make():
+        torch = pytest.importorskip("torch")
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, table, base, head, target, renderer, network, info, pixels):
+                g = fvc.Gradients(network)
+                pred = torch.zeros((pixels.numel(), 4), dtype=torch.float32, device="cuda")
+                loss = renderer.render_backward(info, pixels, target.detach().contiguous(), g, pred=pred)
+                gt, gb, gh = (torch.from_numpy(x).to(table.device, torch.float64) for x in g.read())
+                ctx.save_for_backward(gt.view_as(table), gb.view_as(base), gh.view_as(head), pred, target)
+                ctx.params = (table, base, head)
+                ctx.versions = tuple(t._version for t in ctx.params)
+                return torch.tensor(loss, dtype=torch.float64, device=table.device)
+
+            @staticmethod
+            def backward(ctx, gout):
+                gt, gb, gh, pred, target = ctx.saved_tensors
+                if tuple(t._version for t in ctx.params) != ctx.versions:
+                    raise RuntimeError("RenderLoss: a parameter tensor was modified in place after the forward")
+                n = pred.shape[0]
+                dtgt = -2.0 / n * (pred[:, :3] + pred[:, 3:4] - target)
+                return gout * gt, gout * gb, gout * gh, (gout * dtgt).to(target.dtype), None, None, None, None
+
+        return _Fn
+
+
+def test_autograd_function_wrapper():
+    """torch.autograd through RenderLoss: parameter gradients equal the
+    library's own, agree with the float64 adjoint, and the target's gradient
+    equals autograd of the loss written in torch over the returned colours."""
+    torch, d, loader, cam, pix, tgt = _case(n=256)
+    Fn = RenderLoss.make()
+    om = orc.OracleModel(d, mimic_fp16=True)
+    dev = torch.device("cuda")
+    table = torch.zeros(om.table.size, dtype=torch.float64, device=dev, requires_grad=True)
+    base = torch.zeros(om.base_w.size, dtype=torch.float64, device=dev, requires_grad=True)
+    head = torch.zeros(om.head_w.size, dtype=torch.float64, device=dev, requires_grad=True)
+    target = torch.from_numpy(tgt).to(dev).requires_grad_(True)
+    r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    info = fvc.raymarch_info(cam, loader.stepsize_info)
+    pixels = torch.from_numpy(pix).to(dev)
+    loss = Fn.apply(table, base, head, target, r, loader.nerf_network, info, pixels)
+    (3.0 * loss).backward()
+    lref, g, pred = _gpu(torch, loader, cam, pix, tgt)
+    assert abs(float(loss) - lref) <= 1e-6 * lref
+    for name, t, a in zip(("table", "base", "head"), (table, base, head), g.read()):
+        np.testing.assert_allclose(t.grad.cpu().numpy(), 3.0 * a.astype(np.float64), rtol=1e-6, atol=0, err_msg=name)
+    oloss, ot, ob, oh, _ = om.loss_grad(cam, pix, tgt)
+    for name, t, b in zip(("table", "base", "head"), (table, base, head), (ot, ob, oh)):
+        cos, rel = _compare(t.grad.cpu().numpy() / 3.0, b)
+        assert cos > 0.9999 and rel < 2e-3, (name, cos, rel)
+    # d loss / d target through autograd of the same loss written in torch
+    p = torch.from_numpy(pred).to(dev)
+    tt = torch.from_numpy(tgt).to(dev).requires_grad_(True)
+    (3.0 * ((p[:, :3] + p[:, 3:4] - tt) ** 2).sum(1).mean()).backward()
+    torch.testing.assert_close(target.grad, tt.grad, rtol=1e-5, atol=1e-7)
