@@ -54,13 +54,72 @@ def test_traces_c1_deterministic_math_identical():
     _check_traces(sc, g, scene, steps, cam, bits, exact=True)
 
 
-def test_traces_c2_deterministic_math_close():
+def test_traces_c2_deterministic_math_identical_counts():
     """cone_angle > 0: the kernels use fvc_detmath log/exp (host==device)
-    instead of libm; the step grid may move by a few ulp, which changes at
-    most a tiny fraction of occupancy decisions."""
+    instead of libm; on every golden ray the steps and the occupied steps
+    still equal the reference header's."""
     sc, g, scene, steps, cam, bits = _setup("c2", False)
     stats = _check_traces(sc, g, scene, steps, cam, bits, exact=False)
-    assert stats["ray_mismatch"] <= 0.02 * stats["rays"], stats
+    assert stats["ray_mismatch"] == 0, stats
+
+
+def _fnv_t0(t0b, occ, n):
+    h = 2166136261
+    for j in np.nonzero(occ[:n])[0]:
+        b = int(t0b[j])
+        for _ in range(4):
+            h = ((h ^ (b & 255)) * 16777619) & 0xFFFFFFFF
+            b >>= 8
+    return h
+
+
+# the reference's marcher compiled for the GPU with its own flags (-use_fast_math: approximate division and
+# reciprocal square root, contracted multiply-adds; oracle/ref_golden_dev.cu), against the oracle's
+# deterministic-math march: rays whose steps, occupied-step count or occupied t0 sequence differ
+DEV_GOLDEN_MISMATCH = {"c1": 1, "c2": 0}        # of the 256 golden rays
+DEV_DENSE_OCC_FRAC = {"c1": 4e-3, "c2": 3e-3}   # occupied-count differences, dense-grid subsample
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_traces_against_reference_device_path(name):
+    """The oracle's march against the reference's CUDA path (device golden
+    vectors, tests/golden/make_golden_dev.py): on the 256 golden rays the
+    steps, the occupied count and an FNV-1a hash of the occupied steps' t0
+    agree on all but DEV_GOLDEN_MISMATCH rays; on a subsample of the dense
+    grid, steps agree on all rays of c2, and occupied counts differ on a
+    fraction of rays below DEV_DENSE_OCC_FRAC, by one sample at most."""
+    sc, _, scene, steps, cam, bits = _setup(name, False)
+    d = np.load(os.path.join(HERE, "golden", f"march_{name}_dev.npz"))
+    max_steps = sc["max_steps"]
+    t0b = np.zeros(max_steps, np.uint32)
+    occ = np.zeros(max_steps, np.uint8)
+    init = np.zeros(3, np.float32)
+    bad = 0
+    for i, (x, y) in enumerate(pixels(sc)):
+        n = orc.lib().orc_trace_ray(C.byref(scene), C.byref(steps), C.byref(cam), orc.ptr(bits), int(x), int(y),
+                                    max_steps, orc.ptr(t0b), orc.ptr(occ), orc.ptr(init))
+        assert int(init[2]) == d["g_hits"][i]
+        if init[2] and (n != d["g_steps"][i] or int(occ[:n].sum()) != d["g_occupied"][i]
+                        or _fnv_t0(t0b, occ, n) != int(d["g_t0_hash"][i])):
+            bad += 1
+    assert bad <= DEV_GOLDEN_MISMATCH[name], bad
+    s = int(d["stride"])
+    sub = 4  # every 4th pixel of the dense grid in each direction
+    n_rays = ds = do = 0
+    for yy in range(0, d["steps"].shape[0], sub):
+        for xx in range(0, d["steps"].shape[1], sub):
+            n = orc.lib().orc_trace_ray(C.byref(scene), C.byref(steps), C.byref(cam), orc.ptr(bits), xx * s, yy * s,
+                                        max_steps, orc.ptr(t0b), orc.ptr(occ), orc.ptr(init))
+            assert int(init[2]) == d["hits"][yy, xx]
+            if not init[2]:
+                continue
+            n_rays += 1
+            ds += n != d["steps"][yy, xx]
+            dd = abs(int(occ[:n].sum()) - int(d["occupied"][yy, xx]))
+            assert dd <= 1
+            do += dd != 0
+    print(f"\n{name}: {n_rays} dense rays, steps differ {ds}, occupied differ {do}")
+    assert (ds == 0 if name == "c2" else ds <= 1e-3 * n_rays) and do <= DEV_DENSE_OCC_FRAC[name] * n_rays
 
 
 def _check_traces(sc, g, scene, steps, cam, bits, exact):

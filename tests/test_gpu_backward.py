@@ -278,8 +278,11 @@ def test_autograd_function_wrapper():
     (3.0 * loss).backward()
     lref, g, pred = _gpu(torch, loader, cam, pix, tgt)
     assert abs(float(loss) - lref) <= 1e-6 * lref
+    # a second call of the library: the table gradient is an atomic scatter, so its float sums may differ
+    # in the last bits between calls
     for name, t, a in zip(("table", "base", "head"), (table, base, head), g.read()):
-        np.testing.assert_allclose(t.grad.cpu().numpy(), 3.0 * a.astype(np.float64), rtol=1e-6, atol=0, err_msg=name)
+        a = 3.0 * a.astype(np.float64)
+        np.testing.assert_allclose(t.grad.cpu().numpy(), a, rtol=1e-5, atol=1e-6 * np.abs(a).max(), err_msg=name)
     oloss, ot, ob, oh, _ = om.loss_grad(cam, pix, tgt)
     for name, t, b in zip(("table", "base", "head"), (table, base, head), (ot, ob, oh)):
         cos, rel = _compare(t.grad.cpu().numpy() / 3.0, b)

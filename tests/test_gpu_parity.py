@@ -119,8 +119,8 @@ def test_march_matches_reference_golden_c1(tmp_path, model1):
 
 def test_march_c2_cone_matches_oracle_and_reference(tmp_path, model3):
     """cone_angle > 0 with 3 cascades and the L-inf contraction: the GPU equals
-    the oracle's deterministic-math march exactly; against the reference's
-    libm march at most a tiny fraction of rays differs."""
+    the oracle's deterministic-math march exactly, and both equal the
+    reference header's own march on the host on every golden ray."""
     _, _, base = model3
     sc = SCENES["c2"]
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", "march_c2.npz"))
@@ -148,7 +148,7 @@ def test_march_c2_cone_matches_oracle_and_reference(tmp_path, model3):
         assert c[3] == n + 1 and c[0] == int(occ[:n].sum()), (i, c, n, int(occ[:n].sum()))
         if c[3] != g["n_steps"][i] + 1 or c[0] != occ_counts[i]:
             mism_ref += 1
-    assert mism_ref <= 0.02 * len(pixels(sc)), mism_ref
+    assert mism_ref == 0, mism_ref
 
 
 def _cache_setup(loader, cam):
@@ -250,3 +250,43 @@ def test_progressive_average_image(model1):
     first = buf.image.copy()
     r.render(fvc.raymarch_info(cam, loader.stepsize_info, 3), buf)
     np.testing.assert_array_equal(buf.image, orc.composite_image(buf.results, 3, first))
+
+
+# the reference's CUDA path (oracle/ref_golden_dev.cu: the reference's marcher compiled for the GPU with its
+# own -use_fast_math flags) against this renderer, over a dense pixel grid.  Measured on a GB300 (fractions of
+# the rays that hit the scene's box): c1 steps 7 / 59,843 rays, occupied samples 148 / 59,843 (0.25 %);
+# c2 steps 0 / 129,600, occupied samples 226 / 129,600 (0.17 %); every difference is one sample.  The
+# renderer evaluates the marcher in IEEE float32 (as the reference's host code does); the reference's
+# device build divides approximately (div.full), takes approximate reciprocal square roots and contracts
+# multiply-adds, which moves a sample point across an occupancy-cell face on those rays.
+DEV_STEP_FRAC = {"c1": 2e-4, "c2": 0.0}
+DEV_OCC_FRAC = {"c1": 3e-3, "c2": 2e-3}
+
+
+@pytest.mark.parametrize("name,fixture", [("c1", "model1"), ("c2", "model3")])
+def test_march_against_reference_device_path(tmp_path, request, name, fixture):
+    """Per-ray steps and occupied samples of a full-frame render against the
+    reference's own marcher run on the GPU (tests/golden/march_<scene>_dev.npz)."""
+    _, _, base = request.getfixturevalue(fixture)
+    sc = SCENES[name]
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"march_{name}_dev.npz"))
+    loader = fvc.load_data(_golden_model(tmp_path, name, base))
+    cam = _golden_cam(sc)
+    r, buf = _render(fvc.PerformanceRenderer, loader, cam)
+    r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
+    s = int(g["stride"])
+    cnt = buf.ray_counts[::s, ::s]
+    live = buf.results[::s, ::s, 3] >= 1e-4
+    hits = g["hits"].astype(bool)
+    np.testing.assert_array_equal(cnt[..., 3] > 0, hits)
+    m = hits & live
+    steps = cnt[..., 3][m] - 1
+    occ = cnt[..., 0][m]
+    ds = steps != g["steps"][m]
+    do = occ != g["occupied"][m]
+    n = int(m.sum())
+    print(f"\n{name}: {n} rays, steps differ {int(ds.sum())}, occupied differ {int(do.sum())}, "
+          f"max |d occupied| {int(np.abs(occ.astype(np.int64) - g['occupied'][m]).max())}")
+    assert n > 0.8 * hits.sum()
+    assert ds.sum() <= DEV_STEP_FRAC[name] * n and do.sum() <= DEV_OCC_FRAC[name] * n
+    assert np.abs(occ.astype(np.int64) - g["occupied"][m]).max() <= 1
