@@ -150,6 +150,7 @@ SIGNATURES = {
     "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
     "fvc_renderer_set_tiling": (c_int, [P, c_int, c_int]),
+    "fvc_renderer_set_fused_classify": (c_int, [P, c_int]),
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_renderer_set_precision": (c_int, [P, c_int]),
     "fvc_render_batch": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs)]),

@@ -416,6 +416,7 @@ struct fvc_renderer {
     int steps_per_iter = 64;          /* marching steps per sub-iteration */
     int m_tile = 128;                 /* tcgen05 network tile of the plain path (autotuned) */
     int row_target = 0;               /* compaction batch, rows per sub-iteration (0: the row capacity; autotuned) */
+    int fused_classify = 1;           /* cached renders: classification inside the march (see fvc_renderer_set_fused_classify) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
     int *d_grad_rows = nullptr;       /* resample rows with a gradient */
     int *d_grad_cache_rows = nullptr; /* cache rows with a gradient */
@@ -1221,6 +1222,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.row_capacity = r->row_capacity;
     p.steps_per_iter = r->steps_per_iter;
     p.m_tile = r->m_tile;
+    p.fused_classify = r->fused_classify;
     p.row_target = std::min(r->row_target, r->row_capacity);
     return FVC_OK;
 }
@@ -1749,6 +1751,13 @@ extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
 {
     CHECK_ARG(r && (use_tcgen05 == 0 || use_tcgen05 == 1), "fvc_renderer_set_network_path: bad arguments");
     r->use_tc = use_tcgen05;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_fused_classify(fvc_renderer *r, int on)
+{
+    CHECK_ARG(r && (on == 0 || on == 1), "fvc_renderer_set_fused_classify: bad arguments");
+    r->fused_classify = on;
     return FVC_OK;
 }
 

@@ -403,7 +403,7 @@ __device__ __forceinline__ int classify_basic(const RenderParams &p, const Cache
                                   * 32 -> 12.0, 64 -> 11.5, 128 -> 11.6) */
 #endif
 
-template <bool CACHED>
+template <bool CACHED, bool FUSED = false>
 __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
 {
     const int n_alive = p.counters[it & 1];
@@ -457,8 +457,50 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
             dt4.w = t1;
         }
         const int rbase = warp_alloc(p.counters + 2, n);
-        if (valid) {
+        int n_res = 0, n_hit = 0;
+        if (FUSED && valid) {
+            /* the cached renderer's classification of this ray's rows (wf_classify_kernel's
+             * non-basic form), with the ray moved into the cache camera once per ray */
+            const ViewCache *vc = p.view_caches ? p.view_caches + states[i].cnt2.w : nullptr;
+            const CacheView &C = vc ? vc->cache : p.cache;
+            const DevCam &ccam = vc ? vc->ccam : p.ccam;
+            const DevSteps &cst = vc ? vc->csteps : p.csteps;
+            const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
+            float3 oc, dc;
+            transform_ray(ccam.w2c, o, d, oc, dc);
             for (int s = 0; s < n; ++s) {
+                const float t0 = t0s[s];
+                const float dt = calc_step(p.steps, t0);
+                const float tm = F_MUL(F_ADD(t0, F_ADD(t0, dt)), 0.5f);
+                const float tmh = F_ADD(t0, F_MUL(dt, 0.5f));
+                const int code = classify(p, C, ccam, cst, oc, dc, tm);
+                const int kind = row_kind_of(code);
+                float4 pay = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kind == KIND_RESAMPLE) {
+                    const float3 pc = contract(p.scene, at(o, d, tmh));
+                    pay = make_float4(pc.x, pc.y, pc.z, 0.f);
+                    ++n_res;
+                } else if (kind == KIND_CACHE) {
+                    float tf2;
+                    const float3 fr = cam2froxel(at(oc, dc, tmh), ccam, cst, tf2);
+                    pay = make_float4(fr.x, fr.y, fr.z, 0.f);
+                    ++n_hit;
+                }
+                p.row_t0[rbase + s] = t0;
+                p.row_slot[rbase + s] = i;
+                p.row_pay[rbase + s] = pay;
+                p.row_kind[rbase + s] = (uint8_t)code;
+            }
+        }
+        if (FUSED) {
+            const int wr = __reduce_add_sync(FULLMASK, n_res), wh = __reduce_add_sync(FULLMASK, n_hit);
+            if (lane_id() == 0) {
+                if (wr) atomicAdd(p.counters + 3, wr);
+                if (wh) atomicAdd(p.counters + 4, wh);
+            }
+        }
+        if (valid) {
+            for (int s = 0; s < n && !FUSED; ++s) {
                 p.row_t0[rbase + s] = t0s[s];
                 p.row_slot[rbase + s] = i;
                 if (!CACHED) {
@@ -707,12 +749,12 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_resample_kernel(Rend
  * classification looked it up: halves 16..31
  * of trow (log-density at 16 when latent_offset is 1, the latents from
  * 16 + latent_offset, zeros after) */
-__device__ __forceinline__ void cache_row_input(const RenderParams &p, int k, int r, __half *trow)
+/* the head input (16 fp16 after the density layer's place: log-density at
+ * K = 0 when latent_offset is 1, the 8 latents from K = latent_offset) of a
+ * cache row from its lookup */
+__device__ __forceinline__ void cache_head_input(uint4 lt, uint32_t ld, int latent_offset, uint32_t (&h)[8])
 {
-    const uint4 lt = p.row_lat[k];
-    const uint32_t ld = p.row_out[r].y >> 16;
-    uint32_t *h = reinterpret_cast<uint32_t *>(trow + 16);
-    if (p.latent_offset == 0) {
+    if (latent_offset == 0) {
         h[0] = lt.x; h[1] = lt.y; h[2] = lt.z; h[3] = lt.w;
         h[4] = h[5] = h[6] = h[7] = 0u;
     } else {
@@ -723,6 +765,15 @@ __device__ __forceinline__ void cache_row_input(const RenderParams &p, int k, in
         h[4] = lt.w >> 16;
         h[5] = h[6] = h[7] = 0u;
     }
+}
+
+__device__ __forceinline__ void cache_row_input(const RenderParams &p, int k, int r, __half *trow)
+{
+    uint32_t h[8];
+    cache_head_input(p.row_lat[k], p.row_out[r].y >> 16, p.latent_offset, h);
+    uint32_t *o = reinterpret_cast<uint32_t *>(trow + 16);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) o[q] = h[q];
 }
 
 template <int HEAD_HIDDEN>
@@ -860,12 +911,19 @@ __device__ __forceinline__ bool tc_publish(bool ok)
     return __syncthreads_or(!ok) == 0;
 }
 
+/* MODE 0: resample rows (the list, or all rows of the plain path); MODE 1: the
+ * cache list (head only); MODE 2: every row of a cached sub-iteration in row
+ * order, classified by the march: a resample row gathers its hash features, a
+ * cache row its trilinear cache lookup (cache_lookup, at the froxel point in
+ * its payload) in the same stage, and after the density layers a cache row
+ * replaces their output with its looked-up head input; dropped and skipped
+ * rows ride along as zero rows.  One launch for both streams, no lists. */
 template <int MODE, int HH, bool LIST>
 __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(RenderParams p, int it)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
-    const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : p.counters[4];
+    const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : MODE == 1 ? p.counters[4] : p.counters[2];
     if (n_rows == 0) return;
     const int tid = threadIdx.x, warp = tid >> 5;
     /* the weights arrive by one bulk copy on the TMA engine, completing the
@@ -889,19 +947,33 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
     const int n_tiles = (n_rows + 127) / 128;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const int k = tile * 128 + tid;
-        const int r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : p.cache_list[k]) : -1;
+        int r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : MODE == 1 ? p.cache_list[k] : k) : -1;
+        int kind = KIND_RESAMPLE;
+        if (MODE == 2 && r >= 0) {
+            kind = row_kind_of(p.row_kind[r]);
+            if (kind >= KIND_DROP) r = -1;
+        }
         __half2 sh[8];
         uint16_t log_density = 0;
         if (r >= 0) sh16(dir01_of(states, p.row_slot[r]), sh);
         else for (int q = 0; q < 8; ++q) sh[q] = __floats2half2_rn(0.f, 0.f);
-        if (MODE == 0) {
-            /* ---- hash features -> tile (K = 32) ---- */
+        if (MODE != 1) {
+            /* ---- hash features -> tile (K = 32); MODE 2 cache rows: the cache lookup ---- */
             __half2 feat[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+            uint32_t hin[8];
             if (r >= 0) {
                 const float4 pw = p.row_pay[r];
-                hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
-            } else {
-                for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+                if (MODE == 2 && kind == KIND_CACHE) {
+                    float logd, lat[8];
+                    cache_lookup(row_cache(p, states, r), make_float3(pw.x, pw.y, pw.z), logd, lat);
+                    const uint4 lt = make_uint4(pack_h2(lat[0], lat[1]), pack_h2(lat[2], lat[3]), pack_h2(lat[4], lat[5]),
+                                                pack_h2(lat[6], lat[7]));
+                    cache_head_input(lt, (uint32_t)__half_as_ushort(__float2half_rn(logd)), p.latent_offset, hin);
+                } else {
+                    hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
+                }
             }
 #pragma unroll
             for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
@@ -915,7 +987,11 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
             float v[16];
             tmem_ld16(tmem + lane_base, v);
             tmem_wait_ld();
-            const uint4 b0 = pack8(v), b1 = pack8(v + 8);
+            uint4 b0 = pack8(v), b1 = pack8(v + 8);
+            if (MODE == 2 && kind == KIND_CACHE) {
+                b0 = make_uint4(hin[0], hin[1], hin[2], hin[3]);
+                b1 = make_uint4(hin[4], hin[5], hin[6], hin[7]);
+            }
             log_density = (uint16_t)(b0.x & 0xffffu);
             st_chunk(S.X, tid, 0, 32, b0);
             st_chunk(S.X, tid, 1, 32, b1);
@@ -1721,6 +1797,7 @@ static cudaError_t set_net_attrs()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<2, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tcm_kernel<64, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcmSmem<64>));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tcm_kernel<256, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcmSmem<256>));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_prec_kernel<1, HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
@@ -1737,6 +1814,15 @@ static cudaError_t ensure_net_attrs()
 {
     static PerDeviceOnce once;
     return once.run([] { return set_net_attrs<HH>(); });
+}
+
+/* The cached render's sub-iteration as march-with-classification + one network launch over all rows
+ * (wf_net_tc_kernel MODE 2): the performance cache renderer on the tcgen05 path with the density head.
+ * The basic cache renderer, view-dependent heads and the mma.sync path keep the classification kernel
+ * and the two row lists. */
+static inline bool fused_cached_path(const RenderParams &p)
+{
+    return p.fused_classify && !p.basic_cache && !p.view_dependent && p.use_tc;
 }
 
 /* the network kernel of the plain path's rows in the renderer's network path and precision */
@@ -1783,12 +1869,21 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     const size_t net_smem = sizeof(NetSmem);
     const size_t tc_smem = sizeof(TcSmem);
     const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM; /* <= 8 CTAs x 64 TMEM columns per SM */
+    const bool fused = CACHED && fused_cached_path(p);
     int it = 0;
     const int max_it = 1 << 20;
     for (; it < max_it; ++it) {
-        wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
-        ++L.launches;
-        if (CACHED) {
+        if (fused) {
+            wf_march_kernel<true, true><<<grid_ray, 128, 0, s>>>(p, it);
+            timed_begin();
+            wf_net_tc_kernel<2, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
+            timed_end();
+            L.launches += 2;
+        } else {
+            wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+            ++L.launches;
+        }
+        if (CACHED && !fused) {
             launch_classify(p, it, n_sms, s);
             timed_begin();
             if (p.view_dependent) wf_net_vd_kernel<0, HH, true><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
@@ -1799,7 +1894,7 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
             else if (p.use_tc) wf_net_tc_kernel<1, HH, true><<<grid_tc, 128, tc_smem, s>>>(p, it);
             else wf_net_cache_kernel<HH><<<grid_net, NET_WARPS * 32, net_smem, s>>>(p, it);
             L.launches += 3;
-        } else {
+        } else if (!CACHED) {
             timed_begin();
             launch_plain_net<HH>(p, it, n_sms, s);
             timed_end();
@@ -1970,9 +2065,16 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
     if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         const int grid_ray = n_sms * FVC_RAY_BLOCKS_PER_SM;
+        const bool fused = CACHED && fused_cached_path(p);
         for (int it = 0; it < 2; ++it) {
-            wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
-            if (CACHED) {
+            if (fused) {
+                wf_march_kernel<true, true><<<grid_ray, 128, 0, s>>>(p, it);
+                wf_net_tc_kernel<2, HH, false><<<n_sms * FVC_TC_CTAS_PER_SM, 128, sizeof(TcSmem), s>>>(p, it);
+                kernels += 1;
+            } else {
+                wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+            }
+            if (CACHED && !fused) {
                 const size_t tc_smem = sizeof(TcSmem);
                 const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
                 launch_classify(p, it, n_sms, s);
@@ -1987,7 +2089,7 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
                     wf_net_cache_kernel<HH><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
                 }
                 kernels += 3;
-            } else {
+            } else if (!CACHED) {
                 launch_plain_net<HH>(p, it, n_sms, s);
                 kernels += 1;
             }

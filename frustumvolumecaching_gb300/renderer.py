@@ -172,6 +172,10 @@ class Renderer:
         """tcgen05 (default) or mma.sync network kernels."""
         L.check(L.load().fvc_renderer_set_network_path(self.handle, int(bool(use_tcgen05))))
 
+    def set_fused_classify(self, on: bool) -> None:
+        """Cache renderers: classification inside the march + one network launch (default) or the separate pass."""
+        L.check(L.load().fvc_renderer_set_fused_classify(self.handle, int(bool(on))))
+
     def set_tiling(self, m_tile: int = 128, batch_rows: int = 0) -> None:
         """tcgen05 network tile height (64, 128, 256) and compaction batch (rows per sub-iteration, 0 = capacity)."""
         L.check(L.load().fvc_renderer_set_tiling(self.handle, int(m_tile), int(batch_rows)))

@@ -312,6 +312,14 @@ int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05);
  * depend on either: every row's arithmetic is the same. */
 int fvc_renderer_set_tiling(fvc_renderer *r, int m_tile, int batch_rows);
 
+/* Cache renderers (CACHE_PERFORMANCE, tcgen05 path, density head): 1 (the
+ * default) classifies each sample inside the march and runs one network
+ * launch over all rows of a sub-iteration, a resample row gathering its hash
+ * features and a cache row its trilinear lookup; 0 keeps the separate
+ * classification pass with a resample list and a cache list.  The results
+ * are the same bit for bit; the switch is for measurement. */
+int fvc_renderer_set_fused_classify(fvc_renderer *r, int on);
+
 /* MLP precision of the plain renderers on the tcgen05 path (no counterpart
  * in the reference, whose MLPs are fp16): FP16 (default), BF16, or
  * FP8-E4M3 with per-layer weight scaling and per-row activation scaling;
