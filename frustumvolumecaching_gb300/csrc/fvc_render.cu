@@ -667,6 +667,26 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
     }
 }
 
+/* The cache rows' trilinear lookups of a sub-iteration classified in the
+ * march (cache_lookup at the froxel point in the row payload), one thread
+ * per row, at full occupancy so that many rows' eight corner gathers are in
+ * flight at once.  The head input goes to row_lat at the row's own index and
+ * its fp16 log-density to the high half of row_out.y, which the network
+ * kernel's MODE 2 reads for a cache row. */
+__global__ void __launch_bounds__(256) wf_cache_lookup_kernel(RenderParams p, int it)
+{
+    const int n_rows = p.counters[2];
+    const RayState *states = p.states[it & 1];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+        if (row_kind_of(p.row_kind[r]) != KIND_CACHE) continue;
+        const float4 fr = p.row_pay[r];
+        float logd, lat[8];
+        cache_lookup(row_cache(p, states, r), make_float3(fr.x, fr.y, fr.z), logd, lat);
+        p.row_lat[r] = make_uint4(pack_h2(lat[0], lat[1]), pack_h2(lat[2], lat[3]), pack_h2(lat[4], lat[5]), pack_h2(lat[6], lat[7]));
+        p.row_out[r] = make_uint2(0u, (uint32_t)__half_as_ushort(__float2half_rn(logd)) << 16);
+    }
+}
+
 /* the view-dependent form only for those models: the default one keeps its
  * register count (and so its occupancy) */
 static inline void launch_classify(const RenderParams &p, int it, int n_sms, cudaStream_t s)
@@ -913,11 +933,10 @@ __device__ __forceinline__ bool tc_publish(bool ok)
 
 /* MODE 0: resample rows (the list, or all rows of the plain path); MODE 1: the
  * cache list (head only); MODE 2: every row of a cached sub-iteration in row
- * order, classified by the march: a resample row gathers its hash features, a
- * cache row its trilinear cache lookup (cache_lookup, at the froxel point in
- * its payload) in the same stage, and after the density layers a cache row
- * replaces their output with its looked-up head input; dropped and skipped
- * rows ride along as zero rows.  One launch for both streams, no lists. */
+ * order, classified by the march: a resample row gathers its hash features,
+ * and after the density layers a cache row replaces their output with the
+ * head input of its lookup (wf_cache_lookup_kernel); dropped and skipped rows
+ * ride along as zero rows.  One launch for both streams, no lists. */
 template <int MODE, int HH, bool LIST>
 __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(RenderParams p, int it)
 {
@@ -964,13 +983,9 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
             for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
             uint32_t hin[8];
             if (r >= 0) {
-                const float4 pw = p.row_pay[r];
+                const float4 pw = MODE == 2 && kind == KIND_CACHE ? make_float4(0.f, 0.f, 0.f, 0.f) : p.row_pay[r];
                 if (MODE == 2 && kind == KIND_CACHE) {
-                    float logd, lat[8];
-                    cache_lookup(row_cache(p, states, r), make_float3(pw.x, pw.y, pw.z), logd, lat);
-                    const uint4 lt = make_uint4(pack_h2(lat[0], lat[1]), pack_h2(lat[2], lat[3]), pack_h2(lat[4], lat[5]),
-                                                pack_h2(lat[6], lat[7]));
-                    cache_head_input(lt, (uint32_t)__half_as_ushort(__float2half_rn(logd)), p.latent_offset, hin);
+                    cache_head_input(p.row_lat[r], p.row_out[r].y >> 16, p.latent_offset, hin);
                 } else {
                     hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
                 }
@@ -1875,10 +1890,11 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     for (; it < max_it; ++it) {
         if (fused) {
             wf_march_kernel<true, true><<<grid_ray, 128, 0, s>>>(p, it);
+            wf_cache_lookup_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
             timed_begin();
             wf_net_tc_kernel<2, HH, false><<<grid_tc, 128, tc_smem, s>>>(p, it);
             timed_end();
-            L.launches += 2;
+            L.launches += 3;
         } else {
             wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
             ++L.launches;
@@ -2069,8 +2085,9 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
         for (int it = 0; it < 2; ++it) {
             if (fused) {
                 wf_march_kernel<true, true><<<grid_ray, 128, 0, s>>>(p, it);
+                wf_cache_lookup_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
                 wf_net_tc_kernel<2, HH, false><<<n_sms * FVC_TC_CTAS_PER_SM, 128, sizeof(TcSmem), s>>>(p, it);
-                kernels += 1;
+                kernels += 2;
             } else {
                 wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
             }
