@@ -42,7 +42,13 @@ FLOP_CACHE = 11648     # per cache sample: color head only
 BYTES_HASH = 512       # per resampled sample: 16 levels x 8 corners x 2 fp16
 BYTES_CACHE = 8 * 24   # per cache sample: 8 corners x (density, isset, 8 fp16 latents)
 BYTES_ROW_IO = 28 + 8  # per resampled sample: the 28 B sample record read + 4 fp16 outputs written
-NET_KERNEL = "wf_net_tc_kernel<0> (resample rows: hash-grid encode + density MLP + color head on tcgen05)"
+NET_KERNEL = ("wf_net_tc_kernel<2> (all rows of a cached sub-iteration on tcgen05: a resample row's hash-grid "
+              "encode + density MLP, a cache row's looked-up head input; color head for both)")
+FLOP_HEAD = 11648        # per cache row: the color head only
+BYTES_CACHE_ROW = 16 + 4 + 8 + 28  # per cache row: head input + log-density read, 4 fp16 out, 28 B row record
+SCENE_SIZING = (64, 0.25)  # cache sizing of the scene-sized run: 64 samples per ray, brick sparsity 0.25
+MISS_FIELDS = ("n_miss_outside_fov", "n_miss_outside_depth", "n_miss_before_near", "n_miss_beyond_known",
+               "n_drop_brick_unset", "n_drop_voxel_empty")
 # DRAM bytes (read + write) per resample row of that kernel: dram__bytes_read.sum + dram__bytes_write.sum over all
 # its launches of 2 frames of the same scene at 960x540 / the rows they processed (4.616 GB / 116,864,373 rows)
 NET_TRAFFIC_PER_ROW = 39.5
@@ -341,6 +347,62 @@ BWD_RAYS = 1 << 18
 BWD_RES = (800, 800)
 
 
+# network adjoint per resampled row: the forward re-run's 512 B of hash gathers, the fp32 feature-gradient
+# scatter into the table (16 levels x 8 corners x 2 x 4 B = 1,024 B of reductions), 28 B of row input and
+# 16 B of per-row gradient; FLOPs: the forward (16,896) and twice it for the input and weight gradients
+BWD_BYTES_PER_ROW = 512 + 1024 + 28 + 16
+BWD_FLOP_PER_ROW = 3 * FLOP_RESAMPLE
+BWD_KERNEL = "wf_net_bwd_tc_kernel (network adjoint: forward re-run, input and weight gradients on tcgen05, table scatter)"
+
+
+def backward_roofline(adj_ms: float, adj_launches: int, adj_rows: int, step_ms_total: float) -> dict | None:
+    """Roofline of the adjoint pass's dominant kernel from its CUDA-event times (the renderer's kernel
+    timing around each launch) and its rows: algorithmic bytes against the measured L2 copy bandwidth
+    (the tables and their gradients are L2-resident) and the HBM copy bandwidth, FLOPs against bf16."""
+    if adj_ms <= 0 or adj_launches == 0:
+        return None
+    peaks = measured_peaks()
+    l2 = l2_copy_gbs()
+    gbs = adj_rows * BWD_BYTES_PER_ROW / (adj_ms / 1e3) / 1e9
+    tfl = adj_rows * BWD_FLOP_PER_ROW / (adj_ms / 1e3) / 1e12
+    return {"kernel": BWD_KERNEL, "bound": "l2", "achieved": gbs, "peak": l2, "unit": "GB/s",
+            "frac": gbs / l2 if l2 else None, "frac_of_hbm": gbs / peaks["hbm_gbs"],
+            "peak_source": "L2 copy bandwidth measured in this run (64 MiB resident copy); HBM " + peaks["source"],
+            "traffic": None, "algorithmic_bytes_per_row": BWD_BYTES_PER_ROW, "rows_per_launch": adj_rows / adj_launches,
+            "launch_ms": adj_ms / adj_launches, "share_of_step": adj_ms / step_ms_total,
+            "tensor_tflops": tfl, "tensor_peak": peaks["bf16_tflops"],
+            "ncu": "profiles/wf_net_bwd_tc_kernel_backward_400x400.md: L2 44.9 %, L1 44.8 %, tensor pipe 3.8 %"}
+
+
+_L2_GBS = None
+
+
+def l2_copy_gbs() -> float | None:
+    """Copy bandwidth of a 32 MiB -> 32 MiB device copy (both buffers resident in the 129 MB L2):
+    bytes read + written per second, best of 50 after warm-up (CUDA events)."""
+    global _L2_GBS
+    if _L2_GBS is None:
+        import torch
+        a = torch.empty(8 << 20, dtype=torch.float32, device="cuda")
+        b = torch.empty_like(a)
+        a.fill_(1.0)
+        for _ in range(10):
+            b.copy_(a)
+        best = None
+        for _ in range(50):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                b.copy_(a)
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 10
+            best = t if best is None else min(best, t)
+        _L2_GBS = 2 * a.numel() * 4 / (best / 1e3) / 1e9
+        del a, b
+    return _L2_GBS
+
+
 def run_backward_bench(args, torch, dev, stream) -> dict:
     """Forward + adjoint of the plain render on 2^18 random rays of an 800x800
     view against the image of a second seeded network (same architecture,
@@ -375,6 +437,8 @@ def run_backward_bench(args, torch, dev, stream) -> dict:
         r.render_backward(info, pixels, target, grads)
     torch.cuda.synchronize(dev)
     times, loss, launches = [], None, 0
+    adj_ms, adj_launches, adj_rows = 0.0, 0, 0
+    r.set_kernel_timing(True)
     for _ in range(args.steps):
         a, b = ev(), ev()
         a.record(stream)
@@ -382,7 +446,12 @@ def run_backward_bench(args, torch, dev, stream) -> dict:
         b.record(stream)
         torch.cuda.synchronize(dev)
         times.append(a.elapsed_time(b))
-        launches += r._render_stats.n_launches
+        bst = r._render_stats
+        launches += bst.n_launches
+        adj_ms += bst.timed_adjoint_ms
+        adj_launches += bst.n_timed_adjoint_launches
+        adj_rows += bst.n_resamples
+    r.set_kernel_timing(False)
     ms = sum(times) / len(times)
     # the same step with BF16 MLPs
     r.set_precision(fvc.PerformanceRenderer.BF16)
@@ -429,6 +498,7 @@ def run_backward_bench(args, torch, dev, stream) -> dict:
            "cached": {"value": BWD_RAYS / (ms_c / 1e3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms_c, "loss": loss_cached,
                       "cache_rows": cst.n_cache_hits, "resample_rows": cst.n_resamples,
                       "note": "gradients of the hash table, MLPs and cache brick latents"},
+           "roofline": backward_roofline(adj_ms, adj_launches, adj_rows, ms * args.steps),
            "resolution": list(BWD_RES), "loss": loss, "gpu_launches": launches // max(1, args.steps),
            "workload": "c5 differentiable plain render: forward + adjoint (hash table, both MLPs), fp16 MLP",
            "dtype": "f16 MLP (fp32 accumulate, loss-scaled fp16 gradient tiles), f32 compositing and gradients"}
@@ -492,6 +562,66 @@ def run_double_buffered(torch, dev, cached, infos, image, results, rebuild) -> d
             "mean_coverage": float(np.mean(covs)), "error": state["error"],
             "note": "auxiliary: builds overlap renders (low-priority stream); the headline value rebuilds "
                     "synchronously between frames"}
+
+
+def run_scene_sized(torch, dev, loader, infos, stream, image, results, plain_ms_per_frame: float) -> dict:
+    """The cached camera path with a cache sized for the scene instead of the reference's compile-time
+    estimate (fvc_cache_set_sizing(64, 0.25): 4x the slots), same rebuild rule, one untimed warm-up
+    pass and one pass timed by CUDA events.  Shows what coverage buys on this GPU."""
+    import frustumvolumecaching_gb300 as fvc
+    caches = (fvc.Cache(), fvc.Cache())
+    rc = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network,
+                                      caches[0], caches[1])
+    rc.set_cache_sizing(*SCENE_SIZING)
+    rc.resizeCache(RES, loader.stepsize_info)
+    rc.resizeRenderbuffers(RES)
+    rc.setCacheSettings(fvc.default_cache_settings())
+    rc.set_stream(stream.cuda_stream)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    out = {}
+    for rec in (False, True):
+        renders, builds, covs = [], [], []
+        a, b = ev(), ev()
+        a.record(stream)
+        rc.initCacheBlockwise(infos[0])
+        rc.swapCache()
+        b.record(stream)
+        builds.append((a, b))
+        st0 = rc._init_stats
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for i, info in enumerate(infos):
+            a, b = ev(), ev()
+            a.record(stream)
+            rc.render_device(info, image=image, results=results)
+            b.record(stream)
+            renders.append((a, b))
+            st = rc._render_stats
+            cov = st.n_cache_hits / max(1, st.n_cache_hits + st.n_resamples)
+            covs.append(cov)
+            if cov < COVERAGE_REBUILD and i + 1 < len(infos):
+                a, b = ev(), ev()
+                a.record(stream)
+                rc.initCacheBlockwise(info)
+                rc.swapCache()
+                b.record(stream)
+                builds.append((a, b))
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        if rec:
+            total = t0.elapsed_time(t1) + builds[0][0].elapsed_time(builds[0][1])
+            render_ms = sum(x.elapsed_time(y) for x, y in renders) / len(renders)
+            out = {"ms_per_frame": total / len(infos), "value": len(infos) / (total / 1e3), "unit": UNIT,
+                   "render_ms": render_ms, "build_ms": sum(x.elapsed_time(y) for x, y in builds) / len(builds),
+                   "rebuilds_per_path": len(builds), "mean_coverage": float(np.mean(covs)),
+                   "bricks_demanded": st0.n_bricks_demanded, "bricks_reserved": st0.n_bricks_reserved,
+                   "overflow": bool(st0.overflow),
+                   "render_speedup_vs_plain": plain_ms_per_frame / render_ms,
+                   "speedup_vs_plain": plain_ms_per_frame / (total / len(infos)),
+                   "sizing": {"est_samples_per_ray": SCENE_SIZING[0], "brick_sparsity": SCENE_SIZING[1]},
+                   "note": "auxiliary (not the headline): the reference's sizing is 32 samples per ray, sparsity 0.5"}
+    del rc, caches
+    return out
 
 
 def run_quality(torch, dev, plain, cached, infos, cams, model_dir, n_rows: int = 8) -> dict:
@@ -595,7 +725,8 @@ def run_fvc(args) -> dict | None:
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     log = {"render_plain_ms": [], "render_cached_ms": [], "build_ms": [], "rebuilds": 0, "coverage": [],
            "plain_res": 0, "cache_res": 0, "cache_hits": 0, "launches": 0, "build_iters": 0, "overflow": 0,
-           "bricks_demanded": 0, "bricks_set": 0, "net_ms": 0.0, "net_launches": 0, "net_rows": 0,
+           "bricks_demanded": 0, "bricks_set": 0, "net_ms": 0.0, "net_launches": 0, "net_rows": 0, "net_hits": 0,
+           "miss": {k: 0 for k in MISS_FIELDS},
            "plain_net_ms": 0.0, "plain_net_launches": 0, "plain_net_rows": 0, "plain_launches": 0}
 
     def plain_path(record: bool):
@@ -649,6 +780,9 @@ def run_fvc(args) -> dict | None:
                 log["net_ms"] += st.timed_kernel_ms
                 log["net_launches"] += st.n_timed_launches
                 log["net_rows"] += st.n_resamples
+                log["net_hits"] += st.n_cache_hits
+                for k in MISS_FIELDS:
+                    log["miss"][k] += getattr(st, k)
             if cov < COVERAGE_REBUILD and i + 1 < len(infos):
                 rebuild(info, record)
 
@@ -727,6 +861,8 @@ def run_fvc(args) -> dict | None:
     # thread rebuilds the next cache (on the renderer's low-priority stream) whenever a frame's coverage is
     # below the threshold and no build is running, while the frames keep rendering from the current cache
     double_buffered = run_double_buffered(torch, dev, cached, infos, image, results, rebuild)
+    scene_sized = run_scene_sized(torch, dev, loader, infos, stream, image, results,
+                                  (sum(t_plain) / len(t_plain)) / n_frames)
     quality = None if args.no_quality else run_quality(torch, dev, plain, cached, infos, cams, d)
 
     def mean_ms(pairs):
@@ -747,9 +883,11 @@ def run_fvc(args) -> dict | None:
     peaks = measured_peaks()
     plain_samples_per_frame = st.n_resamples
     net_ms = log["net_ms"]
-    net_bytes = log["net_rows"] * (BYTES_HASH + BYTES_ROW_IO)
+    net_bytes = log["net_rows"] * (BYTES_HASH + BYTES_ROW_IO) + log["net_hits"] * BYTES_CACHE_ROW
     achieved_gbs = net_bytes / (net_ms / 1e3) / 1e9 if net_ms > 0 else None
-    net_tflops = log["net_rows"] * FLOP_RESAMPLE / (net_ms / 1e3) / 1e12 if net_ms > 0 else None
+    net_tflops = ((log["net_rows"] * FLOP_RESAMPLE + log["net_hits"] * FLOP_HEAD) / (net_ms / 1e3) / 1e12
+                  if net_ms > 0 else None)
+    l2_gbs = l2_copy_gbs()
     plain_net_gbs = (log["plain_net_rows"] * (BYTES_HASH + BYTES_ROW_IO) / (log["plain_net_ms"] / 1e3) / 1e9
                      if log["plain_net_ms"] > 0 else None)
     n_frames_cached = len(log["_pending_cached"])
@@ -771,15 +909,22 @@ def run_fvc(args) -> dict | None:
                    "rebuilds_per_path": log["rebuilds"] / args.steps, "mean_coverage": float(np.mean(log["coverage"])) if log["coverage"] else None,
                    "resample_per_frame": res_per_frame, "cache_samples_per_frame": hit_per_frame,
                    "bricks_demanded": log["bricks_demanded"], "bricks_set": log["bricks_set"], "overflow": bool(log["overflow"]),
-                   "speedup_vs_plain": fps_cached / fps_plain, "double_buffered": double_buffered},
+                   "speedup_vs_plain": fps_cached / fps_plain,
+                   "render_speedup_vs_plain": (steps_ms_plain / n_frames) / cached_launch_ms if cached_launch_ms else None,
+                   "miss_breakdown_per_frame": {k[2:]: v / max(1, n_frames_cached) for k, v in log["miss"].items()},
+                   "pipeline": "march with classification -> cache lookups -> one tcgen05 network launch over all rows",
+                   "double_buffered": double_buffered, "scene_sized_cache": scene_sized},
         "quality": quality,
-        "roofline": {"kernel": NET_KERNEL, "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"] if achieved_gbs else None,
-                     "traffic": (NET_TRAFFIC_PER_ROW * log["net_rows"] / max(1, log["net_launches"])
+        "roofline": {"kernel": NET_KERNEL, "bound": "l2", "achieved": achieved_gbs, "peak": l2_gbs,
+                     "unit": "GB/s", "frac": achieved_gbs / l2_gbs if achieved_gbs and l2_gbs else None,
+                     "frac_of_hbm": achieved_gbs / peaks["hbm_gbs"] if achieved_gbs else None,
+                     "hbm_peak": peaks["hbm_gbs"],
+                     "traffic": (NET_TRAFFIC_PER_ROW * (log["net_rows"] + log["net_hits"]) / max(1, log["net_launches"])
                                  if NET_TRAFFIC_PER_ROW else None),
-                     "peak_source": peaks["source"] + " HBM copy bandwidth",
-                     "algorithmic_bytes_per_row": BYTES_HASH + BYTES_ROW_IO,
-                     "rows_per_launch": log["net_rows"] / max(1, log["net_launches"]),
+                     "peak_source": "L2 copy bandwidth measured in this run (32 MiB -> 32 MiB, L2-resident); HBM: "
+                                    + peaks["source"] + " copy bandwidth",
+                     "algorithmic_bytes_per_row": {"resample": BYTES_HASH + BYTES_ROW_IO, "cache": BYTES_CACHE_ROW},
+                     "rows_per_launch": (log["net_rows"] + log["net_hits"]) / max(1, log["net_launches"]),
                      "launch_ms": net_ms / max(1, log["net_launches"]), "launches_timed": log["net_launches"],
                      "share_of_step": net_ms / (sum(t_cached)),
                      "tensor_tflops": net_tflops, "tensor_peak": peaks["bf16_tflops"],

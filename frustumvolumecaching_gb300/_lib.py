@@ -85,7 +85,7 @@ class RenderStats(C.Structure):
                 ("n_miss_outside_fov", C.c_longlong), ("n_miss_outside_depth", C.c_longlong),
                 ("n_miss_before_near", C.c_longlong), ("n_miss_beyond_known", C.c_longlong),
                 ("n_drop_brick_unset", C.c_longlong), ("n_drop_voxel_empty", C.c_longlong),
-                ("n_drop_alpha", C.c_longlong)]
+                ("n_drop_alpha", C.c_longlong), ("n_timed_adjoint_launches", c_int), ("timed_adjoint_ms", C.c_float)]
 
 
 class ModelProps(C.Structure):
@@ -105,7 +105,7 @@ class CacheStats(C.Structure):
 
 assert C.sizeof(SceneInfo) == 76 and C.sizeof(StepsizeInfo) == 48
 assert C.sizeof(CameraInfo) == 144 and CameraInfo.cam2world.offset == 32 and CameraInfo.world2cam.offset == 80
-assert C.sizeof(RenderStats) == 128 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 32
+assert C.sizeof(RenderStats) == 136 and C.sizeof(CacheStats) == 32 and C.sizeof(AutotuneResult) == 32
 assert C.sizeof(RaymarchInfo) == 352 and RaymarchInfo.stepsize_info.offset == 288 and RaymarchInfo.sample_index.offset == 336
 
 FVC_OK = 0
@@ -151,6 +151,7 @@ SIGNATURES = {
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
     "fvc_renderer_set_tiling": (c_int, [P, c_int, c_int]),
     "fvc_renderer_set_fused_classify": (c_int, [P, c_int]),
+    "fvc_cache_set_sizing": (c_int, [P, c_int, C.c_float]),
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_renderer_set_precision": (c_int, [P, c_int]),
     "fvc_render_batch": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs)]),

@@ -47,7 +47,7 @@ static_assert(sizeof(fvc_camera_info) == 144 && offsetof(fvc_camera_info, is_ope
 static_assert(sizeof(fvc_raymarch_info) == 352 && offsetof(fvc_raymarch_info, next_cam_info) == 144 &&
               offsetof(fvc_raymarch_info, stepsize_info) == 288 && offsetof(fvc_raymarch_info, sample_index) == 336 &&
               offsetof(fvc_raymarch_info, motion_blur) == 340 && offsetof(fvc_raymarch_info, deterministic) == 341, "RaymarchInfo layout");
-static_assert(sizeof(fvc_render_stats_t) == 128 && sizeof(fvc_cache_stats_t) == 32, "statistics layout");
+static_assert(sizeof(fvc_render_stats_t) == 136 && sizeof(fvc_cache_stats_t) == 32, "statistics layout");
 static_assert(sizeof(fvc_ray_result) == 16 && sizeof(fvc_camera_matrix) == 48, "BaseRayResult / CameraMatrix layout");
 
 /* ------------------------------------------------------------------------ */
@@ -417,6 +417,8 @@ struct fvc_renderer {
     int m_tile = 128;                 /* tcgen05 network tile of the plain path (autotuned) */
     int row_target = 0;               /* compaction batch, rows per sub-iteration (0: the row capacity; autotuned) */
     int fused_classify = 1;           /* cached renders: classification inside the march (see fvc_renderer_set_fused_classify) */
+    int cache_est_samples = 32;       /* cache sizing: estimated samples per ray ... */
+    float cache_sparsity = 0.5f;      /* ... and brick sparsity (fvc_cache_set_sizing) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
     int *d_grad_rows = nullptr;       /* resample rows with a gradient */
     int *d_grad_cache_rows = nullptr; /* cache rows with a gradient */
@@ -1231,6 +1233,7 @@ static void reset_launch_log(fvc_renderer *r)
 {
     r->log.launches = 0;
     r->log.n_timed = r->log.n_untimed = 0;
+    r->log.split = -1;
     r->log.ev = r->events.empty() ? nullptr : r->events.data();
     r->log.cap = (int)r->events.size() / 2;
 }
@@ -1310,12 +1313,16 @@ extern "C" int fvc_render_stats(fvc_renderer *r, fvc_render_stats_t *o)
     o->n_drop_brick_unset = (long long)s.n_reason[REASON_BRICK_UNSET];
     o->n_drop_voxel_empty = (long long)s.n_reason[REASON_VOXEL_EMPTY];
     o->n_drop_alpha = (long long)s.n_reason[REASON_ALPHA];
-    o->n_timed_launches = r->log.ev ? r->log.n_timed : 0;
+    const int n_timed = r->log.ev ? r->log.n_timed : 0;
+    const int split = r->log.split >= 0 ? std::min(r->log.split, n_timed) : n_timed;
+    o->n_timed_launches = split;
+    o->n_timed_adjoint_launches = n_timed - split;
     o->timed_kernel_ms = 0.0f;
-    for (int i = 0; i < o->n_timed_launches; ++i) {
+    o->timed_adjoint_ms = 0.0f;
+    for (int i = 0; i < n_timed; ++i) {
         float ms = 0.0f;
         CU(cudaEventElapsedTime(&ms, r->log.ev[2 * i], r->log.ev[2 * i + 1]));
-        o->timed_kernel_ms += ms;
+        (i < split ? o->timed_kernel_ms : o->timed_adjoint_ms) += ms;
     }
     return FVC_OK;
 }
@@ -1407,10 +1414,12 @@ extern "C" int fvc_renderer_set_cache_settings(fvc_renderer *r, const fvc_cache_
  * CacheRenderer::resizeCache (src/cache_renderer.cu:832-846). */
 static int cache_resize(fvc_renderer *r, fvc_cache *c, int W, int H, const fvc_stepsize_info &st)
 {
-    const int n_rays = W * H;
-    const int est_samples = n_rays * 32;                         /* INIT_ESTIMATED_N_SAMPLES_PER_RAY */
-    const int est_per_brick = (int)(0.5f * std::pow(8.0f, 3.0f)); /* INIT_ESTIMATED_BRICK_SPARSITY * 8^3 */
-    const int est_bricks = est_samples / est_per_brick;
+    const long long n_rays = (long long)W * H;
+    /* INIT_ESTIMATED_N_SAMPLES_PER_RAY (32) and INIT_ESTIMATED_BRICK_SPARSITY (0.5), include/cache.h:14-15,
+     * unless fvc_cache_set_sizing changed them */
+    const long long est_samples = n_rays * r->cache_est_samples;
+    const int est_per_brick = (int)(r->cache_sparsity * std::pow(8.0f, 3.0f));
+    const long long est_bricks = est_samples / std::max(1, est_per_brick);
     const fvc_scene_info &s = r->m->scene;
     const float dx = s.aabb_to.x - s.aabb_from.x, dy = s.aabb_to.y - s.aabb_from.y, dz = s.aabb_to.z - s.aabb_from.z;
     const float diag = sqrtf(dx * dx + dy * dy + dz * dz);       /* max_step_in_scene */
@@ -1423,7 +1432,8 @@ static int cache_resize(fvc_renderer *r, fvc_cache *c, int W, int H, const fvc_s
     const int max_n_steps = (int)std::ceil(msteps);
     const int depth = (max_n_steps + 3) / 4 * 4;
     const int bX = (W + 7) / 8, bY = (H + 7) / 8, bZ = (depth + 7) / 8;
-    const int dX = 128, dY = 128, dZ = (est_bricks + dX * dY - 1) / (dX * dY);
+    const int dX = 128, dY = 128, dZ = (int)((est_bricks + dX * dY - 1) / (dX * dY));
+    if (dZ > 1024) return fail(FVC_ERR_ARG, "fvc_cache_resize: the sizing asks for more than 128 x 128 x 1024 bricks");
     if (c->initialized && c->fW == W && c->fH == H && c->fD == depth && c->dZ == dZ) return FVC_OK;
     dfree(c->d_packed); dfree(c->d_known);
     if (c->d_voxels) cudaFree(c->d_voxels);
@@ -1437,6 +1447,15 @@ static int cache_resize(fvc_renderer *r, fvc_cache *c, int W, int H, const fvc_s
     if (e != cudaSuccess) { cudaGetLastError(); c->d_voxels = nullptr; return fail(FVC_ERR_OOM, "cudaMalloc cache data array"); }
     c->fW = W; c->fH = H; c->fD = depth; c->bX = bX; c->bY = bY; c->bZ = bZ; c->dX = dX; c->dY = dY; c->dZ = dZ;
     c->initialized = true;
+    return FVC_OK;
+}
+
+extern "C" int fvc_cache_set_sizing(fvc_renderer *r, int est_samples_per_ray, float brick_sparsity)
+{
+    CHECK_ARG(r && est_samples_per_ray >= 1 && est_samples_per_ray <= 4096 && brick_sparsity > 0.0f && brick_sparsity <= 1.0f,
+              "fvc_cache_set_sizing: est_samples_per_ray in [1, 4096], brick_sparsity in (0, 1]");
+    r->cache_est_samples = est_samples_per_ray;
+    r->cache_sparsity = brick_sparsity;
     return FVC_OK;
 }
 
@@ -1990,6 +2009,7 @@ extern "C" int fvc_render_backward(fvc_renderer *r, fvc_grad *g, const fvc_rayma
     CU(cudaMemsetAsync(g->d_loss, 0, sizeof(double), s));
     CU(launch_loss(p, b, s));
     /* pass 2: re-march, compositing adjoint, network adjoint */
+    r->log.split = r->log.n_timed;
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), s));
     CU(backward_frame(p, b, cached, m->head_hidden, m->n_sms, s, r->h_pinned + 8, 4, &r->log));
     const float inv = 1.0f / (FVC_LOSS_SCALE * (float)n_rays);

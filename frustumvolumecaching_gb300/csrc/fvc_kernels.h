@@ -367,6 +367,7 @@ struct LaunchLog {
     int cap = 0;
     int n_timed = 0;
     int n_untimed = 0;
+    int split = -1;  /* fvc_render_backward: timed launches before this index are the forward pass's */
 };
 
 /* The per-ray cache fill (CacheRenderer::initCache, src/cache_renderer.cu:

@@ -1984,6 +1984,14 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
     LaunchLog &L = log ? *log : local;
     wf_raygen_list_kernel<<<(p.n_list + 255) / 256, 256, 0, s>>>(p);
     ++L.launches;
+    /* the network adjoint's launches are timed (when the renderer's kernel timing is on) */
+    auto timed_begin = [&]() {
+        if (L.ev && L.n_timed < L.cap) cudaEventRecord(L.ev[2 * L.n_timed], s);
+    };
+    auto timed_end = [&]() {
+        if (L.ev && L.n_timed < L.cap) cudaEventRecord(L.ev[2 * L.n_timed++ + 1], s);
+        else if (L.ev) ++L.n_untimed;
+    };
     const int grid_ray = n_sms * FVC_RAY_BLOCKS_PER_SM;
     for (int it = 0; it < (1 << 20); ++it) {
         wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
@@ -2005,7 +2013,9 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
             L.launches += 1;
         }
         wf_composite_bwd_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
+        timed_begin();
         cudaError_t e = launch_net_backward(p, b, HH, it, n_sms, s);
+        timed_end();
         if (e == cudaSuccess && CACHED) e = launch_cache_backward(p, b, HH, it, n_sms, s);
         if (e != cudaSuccess) return e;
         wf_reset_rows_kernel<<<1, 32, 0, s>>>(p, CACHED ? 1 : 0);

@@ -350,6 +350,10 @@ class CachePerformanceRenderer(Renderer):
         L.check(L.load().fvc_renderer_set_caches(self.handle, cache.handle, next_cache.handle))
         self._cache, self._cache_next = cache, next_cache
 
+    def set_cache_sizing(self, est_samples_per_ray: int = 32, brick_sparsity: float = 0.5) -> None:
+        """resizeCache's two estimates (the reference's compile-time 32 and 0.5); takes effect at the next resizeCache."""
+        L.check(L.load().fvc_cache_set_sizing(self.handle, int(est_samples_per_ray), float(brick_sparsity)))
+
     def resizeCache(self, resolution, stepsize_info) -> None:
         L.check(L.load().fvc_cache_resize(self.handle, int(resolution[0]), int(resolution[1]), C.byref(stepsize_info)))
 

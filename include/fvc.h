@@ -163,6 +163,11 @@ typedef struct {
                                       * (basic renderer: is not set)             */
     long long n_drop_alpha;          /* basic renderer: interpolated alpha not
                                       * above the threshold                      */
+    /* fvc_render_backward with kernel timing on: the network adjoint's
+     * launches and their summed event time (the forward pass's network
+     * launches stay in n_timed_launches / timed_kernel_ms) */
+    int n_timed_adjoint_launches;
+    float timed_adjoint_ms;
 } fvc_render_stats_t;
 
 typedef struct {
@@ -366,6 +371,16 @@ void fvc_cache_destroy(fvc_cache *c);
 int fvc_renderer_set_caches(fvc_renderer *r, fvc_cache *cache, fvc_cache *next_cache);
 /* resizeCache(int2 resolution, StepsizeInfo), src/cache_renderer.cu:832-846. */
 int fvc_cache_resize(fvc_renderer *r, int width, int height, const fvc_stepsize_info *steps);
+
+/* The two estimates resizeCache sizes the data array with: samples per ray
+ * (INIT_ESTIMATED_N_SAMPLES_PER_RAY, 32) and brick sparsity
+ * (INIT_ESTIMATED_BRICK_SPARSITY, 0.5), compile-time constants in the
+ * reference (include/cache.h:14-15).  The slots are 128 x 128 x
+ * ceil(W H samples / (sparsity 512) / 16384); the next fvc_cache_resize uses
+ * them.  A scene whose occupied froxels outnumber the slots overflows (bricks
+ * beyond the capacity stay unset and their samples are resampled or dropped,
+ * as in the reference). */
+int fvc_cache_set_sizing(fvc_renderer *r, int est_samples_per_ray, float brick_sparsity);
 /* setCacheSettings, include/cache_renderer.h:75. The settings the cached
  * performance renderer reads (src/cache_performance_renderer.cu:1094,
  * 491, 617, 714): interpol_function for the trilinear weights, and

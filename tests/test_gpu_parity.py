@@ -320,3 +320,34 @@ def test_fused_classification_equals_separate_pass(request, fixture, W, H):
     np.testing.assert_array_equal(a_.ray_counts, b_.ray_counts)
     assert sa == sb, (sa, sb)
     assert sa["n_cache_hits"] > 0 and sa["n_resamples"] > 0
+
+
+def test_cache_sizing_changes_capacity_and_matches_oracle(model3):
+    """A larger cache (fvc_cache_set_sizing: 128 samples per ray, sparsity
+    0.25, 16x the slots) holds every demanded brick; the cached render from
+    it matches the oracle's lookup of the same (device-built) cache."""
+    loader, om, _ = model3
+    W, H = 48, 40
+    cam0 = small_camera(1001, W, H)
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    r.set_cache_sizing(128, 0.25)
+    r.resizeCache((W, H), loader.stepsize_info)
+    r.resizeRenderbuffers((W, H))
+    r.setCacheSettings(fvc.default_cache_settings())
+    r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
+    r.swapCache()
+    st = r._init_stats
+    dims = om.cache_dims(W, H, sizing=(128, 0.25))
+    assert c1.dims()[2][2] == dims.dZ and dims.dZ >= 8 * om.cache_dims(W, H).dZ
+    assert st.n_bricks_demanded <= dims.dX * dims.dY * dims.dZ and not st.overflow
+    with pytest.raises(fvc._lib.FvcError):
+        r.set_cache_sizing(0, 0.5)
+    buf = fvc.RenderBuffer((W, H))
+    r.render(fvc.raymarch_info(cam0, loader.stepsize_info), buf)
+    occ = orc.OracleCache(dims, cam0)
+    occ.load_device_cache(*c1.read())
+    ref, counts = om.render_cached(cam0, occ)
+    np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])
+    np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])
+    assert float(np.abs(buf.results - ref).max()) <= COLOR_ATOL
