@@ -323,26 +323,28 @@ def test_fused_classification_equals_separate_pass(request, fixture, W, H):
 
 
 def test_cache_sizing_changes_capacity_and_matches_oracle(model3):
-    """A larger cache (fvc_cache_set_sizing: 128 samples per ray, sparsity
-    0.25, 16x the slots) holds every demanded brick; the cached render from
-    it matches the oracle's lookup of the same (device-built) cache."""
+    """fvc_cache_set_sizing (128 samples per ray, sparsity 0.25: 16x the
+    estimate) sizes the data array as the oracle's resizeCache formula does,
+    and a cached render from a cache built with it matches the oracle's
+    lookup of the same (device-built) cache."""
     loader, om, _ = model3
-    W, H = 48, 40
-    cam0 = small_camera(1001, W, H)
     c0, c1 = fvc.Cache(), fvc.Cache()
     r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
     r.set_cache_sizing(128, 0.25)
+    r.resizeCache((512, 480), loader.stepsize_info)
+    big = om.cache_dims(512, 480, sizing=(128, 0.25))
+    assert c1.dims()[2] == (big.dX, big.dY, big.dZ) and big.dZ >= 15 * om.cache_dims(512, 480).dZ
+    with pytest.raises(fvc._lib.FvcError):
+        r.set_cache_sizing(0, 0.5)
+    W, H = 48, 40
+    cam0 = small_camera(1001, W, H)
     r.resizeCache((W, H), loader.stepsize_info)
     r.resizeRenderbuffers((W, H))
     r.setCacheSettings(fvc.default_cache_settings())
     r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
     r.swapCache()
-    st = r._init_stats
     dims = om.cache_dims(W, H, sizing=(128, 0.25))
-    assert c1.dims()[2][2] == dims.dZ and dims.dZ >= 8 * om.cache_dims(W, H).dZ
-    assert st.n_bricks_demanded <= dims.dX * dims.dY * dims.dZ and not st.overflow
-    with pytest.raises(fvc._lib.FvcError):
-        r.set_cache_sizing(0, 0.5)
+    assert c1.dims()[2] == (dims.dX, dims.dY, dims.dZ) and not r._init_stats.overflow
     buf = fvc.RenderBuffer((W, H))
     r.render(fvc.raymarch_info(cam0, loader.stepsize_info), buf)
     occ = orc.OracleCache(dims, cam0)
