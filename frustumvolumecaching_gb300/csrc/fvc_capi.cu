@@ -231,12 +231,30 @@ DevSteps dev_steps(const fvc_stepsize_info &s)
 DevCam dev_cam(const fvc_camera_info &c)
 {
     DevCam d;
+    memset(&d, 0, sizeof(d));
     d.W = c.resolution.x; d.H = c.resolution.y; d.gl = c.is_open_gl ? 1 : 0;
     d.fx = c.focal.x; d.fy = c.focal.y; d.px = c.principal.x; d.py = c.principal.y;
     const fvc_float4 *m = &c.cam2world.m0, *w = &c.world2cam.m0;
     for (int r = 0; r < 3; ++r) {
         d.c2w[4 * r] = m[r].x; d.c2w[4 * r + 1] = m[r].y; d.c2w[4 * r + 2] = m[r].z; d.c2w[4 * r + 3] = m[r].w;
         d.w2c[4 * r] = w[r].x; d.w2c[4 * r + 1] = w[r].y; d.w2c[4 * r + 2] = w[r].z; d.w2c[4 * r + 3] = w[r].w;
+    }
+    return d;
+}
+
+/* the camera with RaymarchInfo's sampling fields (deterministic, motion
+ * blur toward next_cam_info, sample index, depth of field) */
+DevCam dev_cam_rm(const fvc_raymarch_info &rm)
+{
+    DevCam d = dev_cam(rm.cam_info);
+    d.nd = rm.deterministic ? 0 : 1;
+    d.motion_blur = rm.motion_blur ? 1 : 0;
+    d.sample_index = rm.sample_index;
+    d.aperature = rm.cam_info.aperature;
+    d.focus_z = rm.cam_info.focus_z;
+    const fvc_float4 *n = &rm.next_cam_info.cam2world.m0;
+    for (int r = 0; r < 3; ++r) {
+        d.nc2w[4 * r] = n[r].x; d.nc2w[4 * r + 1] = n[r].y; d.nc2w[4 * r + 2] = n[r].z; d.nc2w[4 * r + 3] = n[r].w;
     }
     return d;
 }
@@ -1124,10 +1142,12 @@ extern "C" int fvc_renderer_set_render_mode(fvc_renderer *r, int mode)
     return FVC_OK;
 }
 
-static int check_info(const fvc_raymarch_info *info)
+static int check_info(const fvc_raymarch_info *info, bool cache_build = false)
 {
-    if (!info->deterministic)
-        return fail(FVC_ERR_CONFIG, "only deterministic rendering (RaymarchInfo::deterministic = true) is built");
+    if (cache_build && !info->deterministic)
+        return fail(FVC_ERR_CONFIG, "cache builds march the pixel centres: RaymarchInfo::deterministic must be true");
+    if (!info->deterministic && info->cam_info.aperature != 0.0f && !(info->cam_info.focus_z != 0.0f))
+        return fail(FVC_ERR_ARG, "depth of field needs a nonzero focus_z");
     const fvc_int2 res = info->cam_info.resolution;
     if (res.x <= 0 || res.y <= 0 || (long long)res.x * res.y > (1ll << 30)) return fail(FVC_ERR_ARG, "bad resolution");
     return FVC_OK;
@@ -1176,7 +1196,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     memset(&p, 0, sizeof(p));
     p.scene = m->dscene;
     p.steps = dev_steps(info->stepsize_info);
-    p.cam = dev_cam(info->cam_info);
+    p.cam = dev_cam_rm(*info);
     p.grid = m->grid;
     p.bits = m->d_bits; p.table = m->d_table; p.weights = m->d_weights; p.bias3 = m->d_bias3;
     p.weights_tc = m->d_weights_tc;
@@ -1505,7 +1525,7 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
     CHECK_ARG(r && info, "fvc_cache_build: null argument");
     CHECK_ARG(r->next, "fvc_cache_build: caches not attached (fvc_renderer_set_caches)");
     int rc;
-    if ((rc = check_info(info))) return rc;
+    if ((rc = check_info(info, true))) return rc;
     fvc_model *m = r->m;
     if ((rc = check_variant(r))) return rc;
     std::lock_guard<std::mutex> lk(r->write_mutex);
@@ -1614,7 +1634,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
     CHECK_ARG(r && info, "fvc_cache_build_per_ray: null argument");
     CHECK_ARG(r->next, "fvc_cache_build_per_ray: caches not attached (fvc_renderer_set_caches)");
     int rc;
-    if ((rc = check_info(info))) return rc;
+    if ((rc = check_info(info, true))) return rc;
     fvc_model *m = r->m;
     if ((rc = check_variant(r))) return rc;
     std::scoped_lock lk(r->read_mutex, r->write_mutex); /* the fill runs on the renderer's wavefront buffers */
@@ -1763,7 +1783,7 @@ void set_error(const char *msg) { g_err = msg; }
 /* the device forms of the step and camera structs, built exactly as the
  * allocating renderers build them */
 DevSteps steps_view(const fvc_stepsize_info &s) { return dev_steps(s); }
-DevCam cam_view(const fvc_camera_info &c) { return dev_cam(c); }
+DevCam cam_view(const fvc_raymarch_info &rm) { return dev_cam_rm(rm); }
 }  // namespace fvc_internal
 
 extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
@@ -2082,7 +2102,7 @@ static int batch_setup(fvc_renderer *r, const fvc_raymarch_info *infos, int n_vi
     std::vector<DevCam> cams(n_views);
     std::vector<int> off(n_views + 1, 0);
     for (int v = 0; v < n_views; ++v) {
-        cams[v] = dev_cam(infos[v].cam_info);
+        cams[v] = dev_cam_rm(infos[v]);
         off[v + 1] = off[v] + infos[v].cam_info.resolution.x * infos[v].cam_info.resolution.y;
     }
     /* pageable sources: staged before the calls return, so the vectors may go */

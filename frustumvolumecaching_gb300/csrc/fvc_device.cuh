@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "fvc_detmath.h"
+#include "fvc_sampling.h"
 
 namespace fvc {
 
@@ -42,6 +43,11 @@ struct DevCam {
     float fx, fy, px, py;
     float c2w[12];
     float w2c[12];
+    /* RaymarchInfo's sampling: nd = 1 when not deterministic (pixel and start
+     * jitter, depth of field when aperature != 0), motion_blur toward nc2w */
+    int nd, motion_blur, sample_index;
+    float aperature, focus_z;
+    float nc2w[12];
 };
 
 constexpr int MAX_LEVELS = 16;
@@ -120,6 +126,50 @@ __device__ __forceinline__ void generate_ray(const DevCam &c, int x, int y, floa
     const float inv = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn((double)dot3(v, v))));
     d = make_float3(F_MUL(v.x, inv), F_MUL(v.y, inv), F_MUL(v.z, inv));
     o = make_float3(c.c2w[3], c.c2w[7], c.c2w[11]);
+}
+
+/* generateRay with RaymarchInfo's sampling (include/raymarch_common.h:218-251,
+ * src/renderer.cu:105-108): the deterministic pixel centre, or the pixel plus
+ * ld_random_pixel_offset, the camera slerped toward next_cam_info for motion
+ * blur (ld_random_val seeded by the pixel index) and the thin-lens offset of
+ * depth of field (the direction then (lookat - origin) / focus_z, not
+ * renormalised, as the reference leaves it).  fvc_sampling.h holds the
+ * sampling arithmetic, shared with the oracle. */
+__device__ __forceinline__ void generate_ray_rm(const DevCam &c, int x, int y, float3 &o, float3 &d)
+{
+    if (!c.nd) {
+        generate_ray(c, x, y, o, d);
+        return;
+    }
+    float ox, oy;
+    fvc_smp::pixel_offset((uint32_t)c.sample_index, ox, oy);
+    const float sx = F_ADD((float)x, ox), sy = F_ADD((float)y, oy);
+    float m[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) m[k] = c.c2w[k];
+    if (c.motion_blur) {
+        const float tm = fvc_smp::ld_val((uint32_t)c.sample_index, (uint32_t)(y * c.W + x) * 72239731u);
+        fvc_smp::camera_slerp(c.c2w, c.nc2w, tm, m);
+    }
+    const float sgn = c.gl ? -1.f : 1.f;
+    const float dx = F_DIV(F_SUB(sx, c.px), c.fx);
+    const float dy = F_MUL(F_DIV(F_SUB(sy, c.py), c.fy), sgn);
+    const float dz = sgn;
+    float3 v = make_float3(dot4(dx, dy, dz, 0.f, m), dot4(dx, dy, dz, 0.f, m + 4), dot4(dx, dy, dz, 0.f, m + 8));
+    const float inv = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn((double)dot3(v, v))));
+    d = make_float3(F_MUL(v.x, inv), F_MUL(v.y, inv), F_MUL(v.z, inv));
+    o = make_float3(m[3], m[7], m[11]);
+    if (c.aperature != 0.0f) {
+        const float3 look = make_float3(F_ADD(o.x, F_MUL(d.x, c.focus_z)), F_ADD(o.y, F_MUL(d.y, c.focus_z)),
+                                        F_ADD(o.z, F_MUL(d.z, c.focus_z)));
+        float bx, by;
+        fvc_smp::lens_offset((uint32_t)c.sample_index, sx, sy, c.W, c.H, c.aperature, bx, by);
+        o.x = F_ADD(o.x, F_ADD(F_MUL(m[0], bx), F_MUL(m[1], by)));
+        o.y = F_ADD(o.y, F_ADD(F_MUL(m[4], bx), F_MUL(m[5], by)));
+        o.z = F_ADD(o.z, F_ADD(F_MUL(m[8], bx), F_MUL(m[9], by)));
+        d = make_float3(F_DIV(F_SUB(look.x, o.x), c.focus_z), F_DIV(F_SUB(look.y, o.y), c.focus_z),
+                        F_DIV(F_SUB(look.z, o.z), c.focus_z));
+    }
 }
 
 /* ray_aabb_intersect, include/raymarch_common.h:482-532 */

@@ -99,7 +99,7 @@ namespace fvc_internal {
 int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms);
 void set_error(const char *msg);
 DevSteps steps_view(const fvc_stepsize_info &s);
-DevCam cam_view(const fvc_camera_info &c);
+DevCam cam_view(const fvc_raymarch_info &rm);
 }  // namespace fvc_internal
 
 extern "C" int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, const fvc_render_outputs *out, void *cuda_stream)
@@ -108,10 +108,6 @@ extern "C" int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, c
     if (!m || !info) {
         fvc_internal::set_error("fvc_render_noalloc: null argument");
         return FVC_ERR_ARG;
-    }
-    if (!info->deterministic) {
-        fvc_internal::set_error("only deterministic rendering (RaymarchInfo::deterministic = true) is built");
-        return FVC_ERR_CONFIG;
     }
     const long long n_rays = (long long)info->cam_info.resolution.x * info->cam_info.resolution.y;
     if (info->cam_info.resolution.x <= 0 || info->cam_info.resolution.y <= 0 || n_rays > FVC_NOALLOC_MAX_RAYS) {
@@ -130,7 +126,7 @@ extern "C" int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, c
     int head_hidden = 2, n_sms = 1;
     if ((rc = fvc_internal::model_views(m, &p, &head_hidden, &n_sms))) return rc;
     p.steps = fvc_internal::steps_view(info->stepsize_info);
-    p.cam = fvc_internal::cam_view(info->cam_info);
+    p.cam = fvc_internal::cam_view(*info);
     /* carve the scratch: header (counters, statistics) then per-ray arrays */
     unsigned char *cursor = static_cast<unsigned char *>(base);
     int *ctl = carve<int>(cursor, 16);              /* [0] ray counter, [1] guard, [8..15] sub-iteration counters */

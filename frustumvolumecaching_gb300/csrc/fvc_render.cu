@@ -112,6 +112,16 @@ __device__ __forceinline__ void write_pixel(const RenderParams &p, int id, float
 /* ------------------------------------------------------------------------- */
 /* raygen                                                                    */
 /* ------------------------------------------------------------------------- */
+/* the ray's first t1 (initRayPayloads_split_kernel, src/renderer.cu:119-124):
+ * valid_t_from_t of the box entry plus, when not deterministic, the first
+ * step times ld_random_t_offset(sample_index, ray_id * 56924617) */
+__device__ __forceinline__ float start_t1(const DevCam &c, const DevSteps &st, float tn, int ray_id)
+{
+    const float start = valid_t_from_t(st, tn);
+    const float toff = c.nd ? fvc_smp::t_offset((uint32_t)c.sample_index, (uint32_t)ray_id) : 0.0f;
+    return F_ADD(start, F_MUL(calc_step(st, start), toff));
+}
+
 /* Pixels are visited in 8x4 tiles per warp so that a warp's rays are
  * neighbours (coherent marching and gathers). */
 __global__ void __launch_bounds__(256) wf_raygen_kernel(RenderParams p)
@@ -127,7 +137,7 @@ __global__ void __launch_bounds__(256) wf_raygen_kernel(RenderParams p)
     float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
     float tn = 0.f, tf = 0.f;
     if (valid) {
-        generate_ray(p.cam, x, y, o, d);
+        generate_ray_rm(p.cam, x, y, o, d);
         hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
     }
     const int id = y * W + x;
@@ -139,7 +149,7 @@ __global__ void __launch_bounds__(256) wf_raygen_kernel(RenderParams p)
     if (hits) {
         RayState st;
         st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
-        st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
+        st.dt = make_float4(d.x, d.y, d.z, start_t1(p.cam, p.steps, tn, id));
         st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
         st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
         st.cnt = make_int4(id, 0, 0, 0);
@@ -160,7 +170,7 @@ __global__ void __launch_bounds__(256) wf_raygen_list_kernel(RenderParams p)
     float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
     float tn = 0.f, tf = 0.f;
     if (valid) {
-        generate_ray(p.cam, pix % W, pix / W, o, d);
+        generate_ray_rm(p.cam, pix % W, pix / W, o, d);
         hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
     }
     if (i < p.n_list && !hits) write_pixel(p, i, make_float4(0.f, 0.f, 0.f, 1.f), make_int4(0, 0, 0, 0));
@@ -171,7 +181,7 @@ __global__ void __launch_bounds__(256) wf_raygen_list_kernel(RenderParams p)
     if (hits) {
         RayState st;
         st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
-        st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
+        st.dt = make_float4(d.x, d.y, d.z, start_t1(p.cam, p.steps, tn, pix));
         st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
         st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
         st.cnt = make_int4(i, 0, 0, 0);
@@ -189,7 +199,7 @@ __global__ void __launch_bounds__(256) wf_raygen_views_kernel(RenderParams p)
     bool hits = false;
     float3 o = make_float3(0, 0, 0), d = make_float3(0, 0, 0);
     float tn = 0.f, tf = 0.f;
-    int view = 0;
+    int view = 0, local = 0;
     if (valid) {
         int lo = 0, hi = p.n_views - 1; /* the view holding ray i: last offset <= i */
         while (lo < hi) {
@@ -198,8 +208,8 @@ __global__ void __launch_bounds__(256) wf_raygen_views_kernel(RenderParams p)
         }
         view = lo;
         const DevCam &cam = p.views[lo];
-        const int local = i - p.view_off[lo];
-        generate_ray(cam, local % cam.W, local / cam.W, o, d);
+        local = i - p.view_off[lo];
+        generate_ray_rm(cam, local % cam.W, local / cam.W, o, d);
         hits = ray_aabb(o, d, p.scene.aabb_from, p.scene.aabb_to, tn, tf);
     }
     if (valid && !hits) write_pixel(p, i, make_float4(0.f, 0.f, 0.f, 1.f), make_int4(0, 0, 0, 0));
@@ -210,7 +220,7 @@ __global__ void __launch_bounds__(256) wf_raygen_views_kernel(RenderParams p)
     if (hits) {
         RayState st;
         st.of = make_float4(o.x, o.y, o.z, fminf(tf, p.steps.far_));
-        st.dt = make_float4(d.x, d.y, d.z, F_ADD(valid_t_from_t(p.steps, tn), 0.0f));
+        st.dt = make_float4(d.x, d.y, d.z, start_t1(p.views[view], p.steps, tn, local));
         st.acc = make_float4(0.f, 0.f, 0.f, 1.f);
         st.comp = make_float4(0.f, 0.f, 0.f, 0.f);
         st.cnt = make_int4(i, 0, 0, 0);

@@ -115,20 +115,27 @@ def camera_info(cam: dict) -> L.CameraInfo:
         m.x, m.y, m.z, m.w = [float(v) for v in c2w[r]]
         m = getattr(ci.world2cam, name)
         m.x, m.y, m.z, m.w = [float(v) for v in w2c[r]]
-    ci.aperature = 0.0
-    ci.focus_z = 1.0
+    ci.aperature = float(cam.get("aperature", 0.0))
+    ci.focus_z = float(cam.get("focus_z", 1.0))
     return ci
 
 
-def raymarch_info(cam: dict, stepsize_info: L.StepsizeInfo, sample_index: int = 0) -> L.RaymarchInfo:
-    """RaymarchInfo as src/eval.cu:160-167 builds it (deterministic, no motion blur)."""
+def raymarch_info(cam: dict, stepsize_info: L.StepsizeInfo, sample_index: int | None = None) -> L.RaymarchInfo:
+    """RaymarchInfo as src/eval.cu:160-167 builds it: deterministic, no motion
+    blur, unless the camera dict says otherwise (keys "deterministic",
+    "motion_blur", "sample_index", "aperature", "focus_z", and
+    "next_cam2world" for the motion-blur end pose)."""
     rm = L.RaymarchInfo()
     rm.cam_info = camera_info(cam)
-    rm.next_cam_info = camera_info(cam)
+    nxt = dict(cam)
+    if "next_cam2world" in cam:
+        nxt["cam2world"] = cam["next_cam2world"]
+        nxt.pop("world2cam", None)
+    rm.next_cam_info = camera_info(nxt)
     rm.stepsize_info = stepsize_info
-    rm.sample_index = sample_index
-    rm.motion_blur = 0
-    rm.deterministic = 1
+    rm.sample_index = int(cam.get("sample_index", 0) if sample_index is None else sample_index)
+    rm.motion_blur = int(bool(cam.get("motion_blur", False)))
+    rm.deterministic = int(bool(cam.get("deterministic", True)))
     return rm
 
 

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "../frustumvolumecaching_gb300/csrc/fvc_detmath.h"
+#include "../frustumvolumecaching_gb300/csrc/fvc_sampling.h"
 
 namespace {
 
@@ -47,9 +48,14 @@ struct OrcSteps {  /* StepsizeInfo, include/common.h:93-107, plus L_lo */
     float dt_min, dt_max, t_min, t_max, i_min, i_max;
     float log1p_c_lo; int use_libm;
 };
-struct OrcCam {    /* CameraInfo, include/common.h:166-180 */
+struct OrcCam {    /* CameraInfo, include/common.h:166-180, plus RaymarchInfo's sampling fields */
     int W, H; int is_open_gl; float fx, fy, px, py;
     float c2w[12]; float w2c[12];
+    int nd;                /* 1: RaymarchInfo::deterministic = false */
+    int motion_blur;       /* RaymarchInfo::motion_blur */
+    int sample_index;      /* RaymarchInfo::sample_index */
+    float aperature, focus_z;
+    float nc2w[12];        /* next_cam_info.cam2world (motion blur) */
 };
 struct OrcNet {
     int n_levels, F;
@@ -117,20 +123,52 @@ inline float dot4(float ax, float ay, float az, float aw, const float *m)
 
 struct Ray { V3 o, d; };
 
-/* generateRayDir + generateRay (deterministic), include/raymarch_common.h:190-251 */
+/* generateRayDir + generateRay, include/raymarch_common.h:190-251, with the
+ * initRayPayloads screen point (src/renderer.cu:105-108): the pixel centre,
+ * or with deterministic = false the pixel plus ld_random_pixel_offset, the
+ * camera slerped toward next_cam_info for motion blur (ld_random_val seeded
+ * by the pixel index) and the thin-lens offset for depth of field. */
 inline Ray generate_ray(const OrcCam &c, int px, int py)
 {
-    const float sx = (float)px + 0.5f, sy = (float)py + 0.5f;
+    float ox = 0.5f, oy = 0.5f;
+    if (c.nd) fvc_smp::pixel_offset((uint32_t)c.sample_index, ox, oy);
+    const float sx = (float)px + ox, sy = (float)py + oy;
+    float m[12];
+    std::memcpy(m, c.c2w, sizeof(m));
+    if (c.nd && c.motion_blur) {
+        const float tm = fvc_smp::ld_val((uint32_t)c.sample_index, (uint32_t)(py * c.W + px) * 72239731u);
+        fvc_smp::camera_slerp(c.c2w, c.nc2w, tm, m);
+    }
     const float sgn = c.is_open_gl ? -1.f : 1.f;
     const float dx = (sx - c.px) / c.fx;
     const float dy = (sy - c.py) / c.fy * sgn;
     const float dz = sgn;
-    V3 d = v3(dot4(dx, dy, dz, 0.f, c.c2w), dot4(dx, dy, dz, 0.f, c.c2w + 4), dot4(dx, dy, dz, 0.f, c.c2w + 8));
+    V3 d = v3(dot4(dx, dy, dz, 0.f, m), dot4(dx, dy, dz, 0.f, m + 4), dot4(dx, dy, dz, 0.f, m + 8));
     /* normalize(): rsqrtf as the reference header evaluates it on the host
      * (nvcc host math: 1/sqrt in double, rounded once to float). */
     const float inv = (float)(1.0 / std::sqrt((double)dot3(d, d)));
     d = v3(d.x * inv, d.y * inv, d.z * inv);
-    return Ray{v3(c.c2w[3], c.c2w[7], c.c2w[11]), d};
+    V3 o = v3(m[3], m[7], m[11]);
+    if (c.nd && c.aperature != 0.0f) {
+        const V3 look = v3(o.x + d.x * c.focus_z, o.y + d.y * c.focus_z, o.z + d.z * c.focus_z);
+        float bx, by;
+        fvc_smp::lens_offset((uint32_t)c.sample_index, sx, sy, c.W, c.H, c.aperature, bx, by);
+        o.x += m[0] * bx + m[1] * by;
+        o.y += m[4] * bx + m[5] * by;
+        o.z += m[8] * bx + m[9] * by;
+        d = v3((look.x - o.x) / c.focus_z, (look.y - o.y) / c.focus_z, (look.z - o.z) / c.focus_z);
+    }
+    return Ray{o, d};
+}
+
+/* the ray's first t1 (initRayPayloads_split_kernel, src/renderer.cu:119-124):
+ * valid_t_from_t of the box entry, plus the first step times
+ * ld_random_t_offset(sample_index, ray_id * 56924617) when not deterministic */
+inline float start_t1(const OrcCam &c, const OrcSteps &st, float tn, int ray_id)
+{
+    const float start = valid_t_from_t(st, tn);
+    const float toff = c.nd ? fvc_smp::t_offset((uint32_t)c.sample_index, (uint32_t)ray_id) : 0.0f;
+    return start + calc_step(st, start) * toff;
 }
 
 /* ray_aabb_intersect, include/raymarch_common.h:482-532 */
@@ -486,6 +524,29 @@ int orc_trace_ray(const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, con
 
 /* Single-point helpers for golden vectors. */
 float orc_step_from_t(const OrcSteps *st, float t) { return step_from_t(*st, t); }
+
+/* the sampling of non-deterministic ray generation (fvc_sampling.h) */
+uint32_t orc_smp_sobol(uint32_t index, uint32_t dim) { return fvc_smp::sobol(index, dim); }
+float orc_smp_ld_val(uint32_t index, uint32_t seed, uint32_t dim) { return fvc_smp::ld_val(index, seed, dim); }
+void orc_smp_pixel_offset(uint32_t spp, float *out) { fvc_smp::pixel_offset(spp, out[0], out[1]); }
+float orc_smp_t_offset(uint32_t spp, uint32_t ray_id) { return fvc_smp::t_offset(spp, ray_id); }
+void orc_smp_square_to_disk(float a, float b, float *out) { fvc_smp::square_to_disk(a, b, out[0], out[1]); }
+void orc_smp_camera_slerp(const float *a, const float *b, float t, float *out)
+{
+    float m[12] = {0};
+    fvc_smp::camera_slerp(a, b, t, m);
+    std::memcpy(out, m, sizeof(m));
+}
+/* generate_ray of pixel (px, py) and the ray's first t1: out = origin, dir, start t1, hits */
+void orc_generate_ray(const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, int px, int py, float *out)
+{
+    const Ray r = generate_ray(*cam, px, py);
+    float tn, tf;
+    const bool hits = ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf);
+    out[0] = r.o.x; out[1] = r.o.y; out[2] = r.o.z; out[3] = r.d.x; out[4] = r.d.y; out[5] = r.d.z;
+    out[6] = hits ? start_t1(*cam, *st, tn, py * cam->W + px) : 0.0f;
+    out[7] = hits ? 1.0f : 0.0f;
+}
 float orc_t_from_step(const OrcSteps *st, float s) { return t_from_step(*st, s); }
 int orc_occupied(const OrcScene *sc, const uint8_t *bits, const float *p, int *cell)
 {
@@ -536,7 +597,7 @@ int orc_render_plain(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, 
             int ns = 0, nst = 0;
             if (hits) {
                 const float far_ = fminf(tf, st->far_);
-                float t1 = valid_t_from_t(*st, tn) + 0.0f;
+                float t1 = start_t1(*cam, *st, tn, (int)id);
                 const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
                 for (;;) {
                     const float t0 = t1;
@@ -1085,7 +1146,7 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
             if (hits) {
                 const Ray rc = transform_ray(r, ccam->w2c);
                 const float far_ = fminf(tf, st->far_);
-                float t1 = valid_t_from_t(*st, tn) + 0.0f;
+                float t1 = start_t1(*cam, *st, tn, (int)id);
                 const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
                 for (;;) {
                     const float t0 = t1;
@@ -1407,7 +1468,7 @@ double ray_loss_grad(const NetD &d, const OrcScene *sc, const OrcSteps *st, cons
     const float d01[3] = {(r.d.x + 1.0f) / 2.0f, (r.d.y + 1.0f) / 2.0f, (r.d.z + 1.0f) / 2.0f};
     if (ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf)) {
         const float far_ = fminf(tf, st->far_);
-        float t1 = valid_t_from_t(*st, tn) + 0.0f;
+        float t1 = start_t1(*cam, *st, tn, py * cam->W + px);
         for (;;) {
             const float t0 = t1;
             const float dt = calc_step(*st, t0);
@@ -1495,7 +1556,7 @@ double ray_loss_grad_cached(const NetD &d, const OrcScene *sc, const OrcSteps *s
     if (ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf)) {
         const Ray rc = transform_ray(r, ccam->w2c);
         const float far_ = fminf(tf, st->far_);
-        float t1 = valid_t_from_t(*st, tn) + 0.0f;
+        float t1 = start_t1(*cam, *st, tn, py * cam->W + px);
         for (;;) {
             const float t0 = t1;
             const float dt = calc_step(*st, t0);

@@ -32,7 +32,9 @@ class OrcSteps(C.Structure):
 
 class OrcCam(C.Structure):
     _fields_ = [("W", C.c_int), ("H", C.c_int), ("is_open_gl", C.c_int), ("fx", C.c_float), ("fy", C.c_float),
-                ("px", C.c_float), ("py", C.c_float), ("c2w", C.c_float * 12), ("w2c", C.c_float * 12)]
+                ("px", C.c_float), ("py", C.c_float), ("c2w", C.c_float * 12), ("w2c", C.c_float * 12),
+                ("nd", C.c_int), ("motion_blur", C.c_int), ("sample_index", C.c_int), ("aperature", C.c_float),
+                ("focus_z", C.c_float), ("nc2w", C.c_float * 12)]
 
 
 class OrcNet(C.Structure):
@@ -78,6 +80,16 @@ def lib():
         _lib.orc_trace_ray.restype = C.c_int
         _lib.orc_step_from_t.argtypes = [P(OrcSteps), C.c_float]
         _lib.orc_step_from_t.restype = C.c_float
+        _lib.orc_smp_sobol.argtypes = [C.c_uint32, C.c_uint32]
+        _lib.orc_smp_sobol.restype = C.c_uint32
+        _lib.orc_smp_ld_val.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+        _lib.orc_smp_ld_val.restype = C.c_float
+        _lib.orc_smp_pixel_offset.argtypes = [C.c_uint32, C.c_void_p]
+        _lib.orc_smp_t_offset.argtypes = [C.c_uint32, C.c_uint32]
+        _lib.orc_smp_t_offset.restype = C.c_float
+        _lib.orc_smp_square_to_disk.argtypes = [C.c_float, C.c_float, C.c_void_p]
+        _lib.orc_smp_camera_slerp.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
+        _lib.orc_generate_ray.argtypes = [P(OrcScene), P(OrcSteps), P(OrcCam), C.c_int, C.c_int, C.c_void_p]
         _lib.orc_t_from_step.argtypes = [P(OrcSteps), C.c_float]
         _lib.orc_t_from_step.restype = C.c_float
         _lib.orc_occupied.argtypes = [P(OrcScene), C.c_void_p, C.c_void_p, C.c_void_p]
@@ -154,6 +166,13 @@ def make_cam(cam: dict) -> OrcCam:
     c.px, c.py = cam["principal"]
     c.c2w[:] = np.asarray(cam["cam2world"], np.float32).ravel().tolist()
     c.w2c[:] = np.asarray(cam["world2cam"], np.float32).ravel().tolist()
+    # RaymarchInfo's sampling fields (camera dict keys of frustumvolumecaching_gb300.raymarch_info)
+    c.nd = int(not cam.get("deterministic", True))
+    c.motion_blur = int(bool(cam.get("motion_blur", False)))
+    c.sample_index = int(cam.get("sample_index", 0))
+    c.aperature = float(cam.get("aperature", 0.0))
+    c.focus_z = float(cam.get("focus_z", 1.0))
+    c.nc2w[:] = np.asarray(cam.get("next_cam2world", cam["cam2world"]), np.float32).ravel().tolist()
     return c
 
 
