@@ -23,6 +23,8 @@ HEADERS = ["fvc_kernels.h", "fvc_device.cuh", "fvc_detmath.h", "fvc_tc.cuh", "fv
 INCLUDE = os.path.join(PKG, "..", "include")
 EVAL_SRC = os.path.join(PKG, "cpp", "eval.cpp")
 EVAL = os.path.join(OUT_DIR, "eval")
+PATH_SRC = os.path.join(PKG, "cpp", "render_path.cpp")
+PATH_EXE = os.path.join(OUT_DIR, "render_path")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -64,27 +66,39 @@ def cuda_root() -> str:
     return os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
 
 
-def build_eval(force: bool = False) -> str:
-    """g++ build of the eval program; needs libfvc.so first."""
+def _build_program(src: str, exe: str, extra_deps: list, force: bool) -> str:
+    """g++ build of a program on the C++ renderer API; needs libfvc.so first."""
     lib = build()
-    deps = [EVAL_SRC, os.path.join(INCLUDE, "fvc.hpp"), os.path.join(INCLUDE, "fvc.h"), lib]
-    if not force and os.path.exists(EVAL) and all(os.path.getmtime(d) < os.path.getmtime(EVAL) for d in deps):
-        return EVAL
+    deps = [src, os.path.join(INCLUDE, "fvc.hpp"), os.path.join(INCLUDE, "fvc.h"), lib, *extra_deps]
+    if not force and os.path.exists(exe) and all(os.path.getmtime(d) < os.path.getmtime(exe) for d in deps):
+        return exe
     cuda = cuda_root()
     cudalib = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib")) if os.path.isdir(d)), None)
     if cudalib is None:
         raise RuntimeError("CUDA runtime library directory not found under " + cuda)
-    tmp = EVAL + ".tmp"
+    tmp = exe + ".tmp"
     cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", INCLUDE, "-I", os.path.join(cuda, "include"),
-           EVAL_SRC, "-o", tmp, "-L", OUT_DIR, "-lfvc", "-L", cudalib, "-lcudart",
+           src, "-o", tmp, "-L", OUT_DIR, "-lfvc", "-L", cudalib, "-lcudart",
            "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cudalib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("g++ failed:\n" + r.stdout + r.stderr)
-    os.replace(tmp, EVAL)
-    return EVAL
+    os.replace(tmp, exe)
+    return exe
+
+
+def build_eval(force: bool = False) -> str:
+    """The eval program (src/eval.cu's command line)."""
+    return _build_program(EVAL_SRC, EVAL, [], force)
+
+
+def build_render_path(force: bool = False) -> str:
+    """The headless camera-path renderer (the real-time viewer's path rendering)."""
+    return _build_program(PATH_SRC, PATH_EXE, [os.path.join(INCLUDE, "fvc_camera_path.hpp"),
+                                               os.path.join(PKG, "csrc", "fvc_sampling.h")], force)
 
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
     print(build_eval(force="--force" in sys.argv))
+    print(build_render_path(force="--force" in sys.argv))
