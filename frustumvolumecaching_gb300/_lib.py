@@ -74,7 +74,8 @@ class CacheSettings(C.Structure):
 
 
 class RenderOutputs(C.Structure):
-    _fields_ = [("image_rgba8", C.c_void_p), ("results", C.c_void_p), ("ray_counts", C.c_void_p)]
+    _fields_ = [("image_rgba8", C.c_void_p), ("results", C.c_void_p), ("ray_counts", C.c_void_p),
+                ("contrib_resample", C.c_void_p), ("contrib_cache", C.c_void_p)]
 
 
 class RenderStats(C.Structure):

@@ -17,7 +17,10 @@
  * -sc compares the plain render with the frame's PNG (when it can be read: the
  * dataset images are not part of this project) and the cached render with the
  * plain one (>= 35 dB, src/eval.cu:321), stopping at the first failure.
- * -wc writes no contribution images: the renderers here do not produce them.
+ * -wc (with -w) writes, for every rotation and translation offset, the
+ * per-pixel compositing weight of the resampled and of the cached samples as
+ * <name>_contr_new.png / <name>_contr_cache.png (gray, [0, 1] -> [0, 255];
+ * src/eval.cu:381-410, 466-484).
  */
 #include "fvc.hpp"
 
@@ -311,6 +314,10 @@ int main(int argc, char **argv)
         std::vector<Timing> timings_rot, timings_trans;
         const Timing no_cache{out_dir + "/no_cache", 0.0f, render_time_new_ms / a.n_iter, renderer._timer.getTimings(a.n_iter)};
         if (a.write_images) render_image.writeToFile(out_dir + "/no_cache.png");
+        if (a.write_contrib) {
+            contrib_resample.set(0.0f);
+            contrib_cache.set(0.0f);
+        }
 
         /* render with cache */
         cache_renderer.initCacheBlockwise(cache_rm, render_debug);
@@ -354,12 +361,20 @@ int main(int argc, char **argv)
                 t0 = now_ms();
                 cache_renderer.initCacheBlockwise(sub_rm, render_debug);
                 const float init_ms = (float)(now_ms() - t0);
+                if (a.write_contrib) {
+                    contrib_resample.set(0.0f);
+                    contrib_cache.set(0.0f);
+                }
                 cache_renderer._timer.reset();
                 t0 = now_ms();
                 for (unsigned it = 0; it < a.n_iter; ++it)
                     cache_renderer.render(render_rm, render_image, a.write_contrib ? &debug_data : nullptr);
                 const float rt = (float)(now_ms() - t0);
                 if (a.write_images) render_image.writeToFile(sub + "/" + name + ".png");
+                if (a.write_contrib) {
+                    contrib_resample.writeToFile(sub + "/" + name + "_contr_new.png", createMinMaxConverter<float>(0.0f, 1.0f));
+                    contrib_cache.writeToFile(sub + "/" + name + "_contr_cache.png", createMinMaxConverter<float>(0.0f, 1.0f));
+                }
                 const auto &is = cache_renderer._init_stats;
                 const auto &rs = cache_renderer._render_stats;
                 metrics_rot.push_back({std::to_string(deg) + "/" + name, is.n_bricks_set, is.n_bricks_reserved,
@@ -385,12 +400,20 @@ int main(int argc, char **argv)
             t0 = now_ms();
             cache_renderer.initCacheBlockwise(sub_rm, render_debug);
             const float init_ms = (float)(now_ms() - t0);
+            if (a.write_contrib) {
+                contrib_resample.set(0.0f);
+                contrib_cache.set(0.0f);
+            }
             cache_renderer._timer.reset();
             t0 = now_ms();
             for (unsigned it = 0; it < a.n_iter; ++it)
                 cache_renderer.render(render_rm, render_image, a.write_contrib ? &debug_data : nullptr);
             const float rt = (float)(now_ms() - t0);
             if (a.write_images) render_image.writeToFile(sub + "/" + name + ".png");
+            if (a.write_contrib) {
+                contrib_resample.writeToFile(sub + "/" + name + "_contr_new.png", createMinMaxConverter<float>(0.0f, 1.0f));
+                contrib_cache.writeToFile(sub + "/" + name + "_contr_cache.png", createMinMaxConverter<float>(0.0f, 1.0f));
+            }
             const auto &is = cache_renderer._init_stats;
             const auto &rs = cache_renderer._render_stats;
             metrics_trans.push_back({name, is.n_bricks_set, is.n_bricks_reserved, is.n_bricks_set >= is.n_bricks_reserved,

@@ -1258,13 +1258,16 @@ static void reset_launch_log(fvc_renderer *r)
     r->log.cap = (int)r->events.size() / 2;
 }
 
-static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts)
+static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4 *results, uchar4 *image, int4 *counts,
+                          float *contrib_res = nullptr, float *contrib_cache = nullptr)
 {
     fvc_model *m = r->m;
     const bool cached = is_cache_kind(r->kind);
     RenderParams p;
     int rc;
     if ((rc = setup_render_params(r, info, results, image, counts, p))) return rc;
+    p.contrib_res = contrib_res;
+    p.contrib_cache = contrib_cache;
     CU(cudaMemsetAsync(r->d_ctl, 0, 4 * sizeof(int), r->stream));
     CU(cudaMemsetAsync(r->d_stats, 0, sizeof(RenderStatsDev), r->stream));
     CU(cudaMemsetAsync(r->d_wf_counters, 0, 8 * sizeof(int), r->stream));
@@ -1277,16 +1280,21 @@ static int enqueue_render(fvc_renderer *r, const fvc_raymarch_info *info, float4
 extern "C" int fvc_render_device(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out)
 {
     CHECK_ARG(r && info, "fvc_render_device: null argument");
+    CHECK_ARG(!out || (!out->contrib_resample && !out->contrib_cache) || is_cache_kind(r->kind),
+              "fvc_render_device: contribution buffers are written by the cache renderers");
     int rc;
     if ((rc = check_info(info))) return rc;
     std::lock_guard<std::mutex> lk(r->read_mutex);
     return enqueue_render(r, info, out ? (float4 *)out->results : nullptr, out ? (uchar4 *)out->image_rgba8 : nullptr,
-                          out ? (int4 *)out->ray_counts : nullptr);
+                          out ? (int4 *)out->ray_counts : nullptr, out ? out->contrib_resample : nullptr,
+                          out ? out->contrib_cache : nullptr);
 }
 
 extern "C" int fvc_render(fvc_renderer *r, const fvc_raymarch_info *info, const fvc_render_outputs *out)
 {
     CHECK_ARG(r && info, "fvc_render: null argument");
+    CHECK_ARG(!out || (!out->contrib_resample && !out->contrib_cache),
+              "fvc_render: contribution buffers are device buffers (fvc_render_device)");
     int rc;
     if ((rc = check_info(info))) return rc;
     if ((rc = fvc_renderer_resize(r, info->cam_info.resolution.x, info->cam_info.resolution.y))) return rc;

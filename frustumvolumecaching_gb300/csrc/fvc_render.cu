@@ -1479,6 +1479,7 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
             const int2 rr = p.ray_rows[i];
             float4 acc = st.acc, comp = st.comp;
             int c_res = st.cnt.y, c_cache = st.cnt.z, c_drop = st.cnt2.x;
+            float w_res = 0.f, w_cache = 0.f; /* this sub-iteration's contribution weights (DEBUG form, :867-871) */
             bool term = false;
             /* rows are in t order: the merge of the resample and cache
              * streams of accumulate_cache_perf_kernel (:270-304) */
@@ -1509,8 +1510,16 @@ __global__ void __launch_bounds__(128) wf_composite_kernel(RenderParams p, int i
                     kahan_add(acc.y, comp.y, wgt / (1.0f + expf(-rg.y)));
                     kahan_add(acc.z, comp.z, wgt / (1.0f + expf(-lb)));
                     acc.w *= 1.0f - alpha;
+                    if (CACHED) {
+                        if (kind == KIND_CACHE) w_cache += wgt;
+                        else w_res += wgt;
+                    }
                 }
                 if (acc.w < 1e-4f) { term = true; break; }
+            }
+            if (CACHED) { /* one ray a pixel: no other thread adds to it in this launch */
+                if (p.contrib_res) p.contrib_res[st.cnt.x] += w_res;
+                if (p.contrib_cache) p.contrib_cache[st.cnt.x] += w_cache;
             }
             st.acc = acc;
             st.comp = comp;

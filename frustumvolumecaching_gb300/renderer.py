@@ -205,10 +205,13 @@ class Renderer:
         out = render_buffer.outputs()
         L.check(L.load().fvc_render(self.handle, C.byref(rm_info), C.byref(out)))
 
-    def render_device(self, rm_info: L.RaymarchInfo, image=None, results=None, ray_counts=None) -> None:
-        """Enqueue a render into device buffers (pointers or torch tensors)."""
+    def render_device(self, rm_info: L.RaymarchInfo, image=None, results=None, ray_counts=None, contrib_resample=None,
+                      contrib_cache=None) -> None:
+        """Enqueue a render into device buffers (pointers or torch tensors); cache renderers add the
+        per-pixel contribution weights of resampled and cache samples to contrib_* (float, W x H)."""
         out = L.RenderOutputs()
         out.image_rgba8, out.results, out.ray_counts = L.ptr(image), L.ptr(results), L.ptr(ray_counts)
+        out.contrib_resample, out.contrib_cache = L.ptr(contrib_resample), L.ptr(contrib_cache)
         L.check(L.load().fvc_render_device(self.handle, C.byref(rm_info), C.byref(out)))
 
     def render_backward(self, rm_info: L.RaymarchInfo, pixels, target, grads: "Gradients", pred=None, n_rays=None) -> float:

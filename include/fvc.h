@@ -283,6 +283,14 @@ typedef struct {
     uint8_t *image_rgba8;
     fvc_ray_result *results;
     int32_t *ray_counts;
+    /* cache renderers, fvc_render_device only: per pixel, the compositing
+     * weight (alpha T) the frame's resampled samples and its cache samples
+     * contributed, ADDED to the device float buffers' contents (W x H each;
+     * the caller clears them) - accumulate_cache_perf_kernel<DEBUG>'s
+     * contribution surfaces (src/cache_performance_renderer.cu:789-908),
+     * eval's -wc images.  NULL: not written. */
+    float *contrib_resample;
+    float *contrib_cache;
 } fvc_render_outputs;
 
 /* render(RaymarchInfo, RenderBuffer&, DebugData*) of the renderer's kind:

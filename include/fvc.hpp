@@ -31,6 +31,7 @@
 #include <vector_types.h>
 
 #include <algorithm>
+#include <functional>
 #include <chrono>
 #include <cmath>
 #include <cstddef>
@@ -264,14 +265,15 @@ inline uint32_t crc32(const uint8_t *p, size_t n, uint32_t c = 0)
     return ~c;
 }
 
-/* RGBA8 PNG with uncompressed (stored) deflate blocks */
-inline bool write_png(const fs::path &path, const uint8_t *rgba, int w, int h)
+/* 8-bit PNG (channels 4: RGBA, 1: gray) with uncompressed (stored) deflate blocks */
+inline bool write_png(const fs::path &path, const uint8_t *rgba, int w, int h, int channels = 4)
 {
     std::vector<uint8_t> raw;
-    raw.reserve((size_t)h * (1 + 4 * (size_t)w));
+    const size_t row = (size_t)w * channels;
+    raw.reserve((size_t)h * (1 + row));
     for (int y = 0; y < h; ++y) {
         raw.push_back(0);
-        raw.insert(raw.end(), rgba + (size_t)y * w * 4, rgba + (size_t)(y + 1) * w * 4);
+        raw.insert(raw.end(), rgba + (size_t)y * row, rgba + (size_t)(y + 1) * row);
     }
     std::vector<uint8_t> z = {0x78, 0x01};
     uint32_t a = 1, b = 0;
@@ -300,7 +302,7 @@ inline bool write_png(const fs::path &path, const uint8_t *rgba, int w, int h)
     f.write((const char *)sig, 8);
     std::vector<uint8_t> ihdr(13);
     for (int i = 0; i < 4; ++i) { ihdr[i] = uint8_t(w >> (24 - 8 * i)); ihdr[4 + i] = uint8_t(h >> (24 - 8 * i)); }
-    ihdr[8] = 8; ihdr[9] = 6; ihdr[10] = ihdr[11] = ihdr[12] = 0;
+    ihdr[8] = 8; ihdr[9] = channels == 1 ? 0 : 6; ihdr[10] = ihdr[11] = ihdr[12] = 0;
     chunk("IHDR", ihdr);
     chunk("IDAT", z);
     chunk("IEND", {});
@@ -610,16 +612,43 @@ public:
     }
     int2 resolution() const { return _res; }
     T *data() { return _buf.data(); }
+    /* one-channel PNG through a value -> byte converter (src/util/debug_buffer.cu:69-89, PNG only) */
+    void writeToFile(fs::path filename, std::function<unsigned char(T)> converter) const
+    {
+        std::vector<T> h;
+        _buf.download(h);
+        std::vector<uint8_t> g(h.size());
+        std::transform(h.begin(), h.end(), g.begin(), converter);
+        if (filename.extension() != ".png") throw std::runtime_error("Image file extension not supported!");
+        if (!fvc_cpp::write_png(filename, g.data(), _res.x, _res.y, 1)) throw std::runtime_error("cannot write " + filename.string());
+    }
+    std::vector<T> download() const
+    {
+        std::vector<T> h;
+        _buf.download(h);
+        return h;
+    }
 
 private:
     int2 _res;
     CudaBuffer<T> _buf;
 };
 
-/* DebugData, include/renderer.h:72-75. */
+/* DebugData, include/renderer.h:72-75: the cache renderers add the
+ * contribution weights of resampled samples to buffers[0] and of cache
+ * samples to buffers[1] (src/cache_performance_renderer.cu:889-898). */
 struct DebugData {
     std::vector<DebugBuffer<float> *> buffers;
 };
+
+/* createMinMaxConverter (include/util/bmpwriter.h:22-27) */
+template <typename T>
+std::function<unsigned char(T)> createMinMaxConverter(T min_val, T max_val)
+{
+    return [min_val, max_val](T x) -> unsigned char {
+        return (unsigned char)((float)(std::min(std::max(x, min_val), max_val) - min_val) / (max_val - min_val) * 255.0f);
+    };
+}
 
 /* CudaTimer (include/util/cuda_timer.h), reduced to what the renderers here
  * measure: wall time of each synchronous render and the summed CUDA-event
@@ -669,7 +698,7 @@ struct Renderer {
 
 protected:
     /* one synchronous render into the buffer; returns the frame statistics */
-    fvc_render_stats_t render_into(const RaymarchInfo &rm_info, RenderBuffer &buf)
+    fvc_render_stats_t render_into(const RaymarchInfo &rm_info, RenderBuffer &buf, DebugData *debug = nullptr)
     {
         const int2 r = buf.resolution();
         if (r.x != rm_info.cam_info.resolution.x || r.y != rm_info.cam_info.resolution.y)
@@ -677,6 +706,10 @@ protected:
         fvc_render_outputs out{};
         out.image_rgba8 = reinterpret_cast<uint8_t *>(buf.image_device());
         out.results = reinterpret_cast<fvc_ray_result *>(buf.results_device());
+        if (debug && debug->buffers.size() >= 2) {
+            out.contrib_resample = debug->buffers[0]->data();
+            out.contrib_cache = debug->buffers[1]->data();
+        }
         const auto t0 = std::chrono::steady_clock::now();
         fvc_cpp::check(fvc_render_device(_handle, fvc_cpp::abi(rm_info), &out));
         fvc_cpp::check(fvc_renderer_synchronize(_handle));
@@ -813,10 +846,10 @@ struct CachePerformanceRenderer : public CacheRenderer {
     CachePerformanceRenderer(SceneInfo s, CudaBuffer<uint8_t> &g, NerfNetwork<half> &n, Cache *cache, Cache *next_cache)
         : CacheRenderer(s, g, n, cache, next_cache) {}
 
-    void render(RaymarchInfo rm_info, RenderBuffer &b, DebugData * = nullptr) override
+    void render(RaymarchInfo rm_info, RenderBuffer &b, DebugData *debug_data = nullptr) override
     {
         fvc_cpp::check(fvc_renderer_set_render_mode(_handle, (int)_render_mode));
-        const fvc_render_stats_t st = render_into(rm_info, b);
+        const fvc_render_stats_t st = render_into(rm_info, b, debug_data);
         const float n_rays = (float)std::max(1, rm_info.cam_info.resolution.x * rm_info.cam_info.resolution.y);
         _render_stats.samples_ppx = (float)st.samples_ppx;
         _render_stats.resample_samples_evaluated = (float)st.n_resamples / n_rays;

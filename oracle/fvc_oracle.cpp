@@ -1127,7 +1127,8 @@ void orc_composite_rows(int n_alive, int batch, const OrcSteps *st, float alpha_
  * slot, 6 empty voxel (not set: basic), 7 alpha (basic) (dropped). */
 int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, const OrcCam *cam, const uint8_t *bits,
                       const OrcCache *cc, const OrcCam *ccam, const OrcSteps *cst, int mode,
-                      int row0, int row1, float *results, int32_t *counts, int n_threads, long long *reasons)
+                      int row0, int row1, float *results, int32_t *counts, int n_threads, long long *reasons,
+                      double *contrib)
 {
     NetD d; prepare_net(net, d);
     const OrcCacheDims &cd = cc->dims;
@@ -1141,7 +1142,7 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
             const Ray r = generate_ray(*cam, x, y);
             float tn, tf;
             const bool hits = ray_aabb(r, sc->aabb_from, sc->aabb_to, tn, tf);
-            double rgb[3] = {0, 0, 0}, T = 1.0;
+            double rgb[3] = {0, 0, 0}, T = 1.0, w_contrib[2] = {0.0, 0.0};
             int n_res = 0, n_cache = 0, n_drop = 0, nst = 0;
             if (hits) {
                 const Ray rc = transform_ray(r, ccam->w2c);
@@ -1263,11 +1264,16 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         }
                         ++n_cache;
                     }
-                    if (composite(sigma, lg, dt, sc->alpha_thre, rgb, T)) break;
+                    const double T_before = T;
+                    const bool stop = composite(sigma, lg, dt, sc->alpha_thre, rgb, T);
+                    /* contribution weight alpha T of the sample (accumulate_cache_perf_kernel<DEBUG>, :867-871) */
+                    if (T != T_before) w_contrib[kind == 1 ? 1 : 0] += T_before - T;
+                    if (stop) break;
                 }
             }
             results[4 * id + 0] = (float)rgb[0]; results[4 * id + 1] = (float)rgb[1];
             results[4 * id + 2] = (float)rgb[2]; results[4 * id + 3] = (float)T;
+            if (contrib) { contrib[2 * id] = w_contrib[0]; contrib[2 * id + 1] = w_contrib[1]; }
             if (counts) { counts[4 * id] = n_res; counts[4 * id + 1] = n_cache; counts[4 * id + 2] = n_drop; counts[4 * id + 3] = nst; }
         }
         if (reasons) {

@@ -119,7 +119,7 @@ def lib():
                                                  C.c_int]
         _lib.orc_render_cached.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, P(OrcCache),
                                            P(OrcCam), P(OrcSteps), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
-                                           C.c_int, C.c_void_p]
+                                           C.c_int, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -354,8 +354,9 @@ class OracleModel:
     REASONS = ("outside_fov", "outside_depth", "before_near", "beyond_known", "brick_unset", "voxel_empty", "alpha")
 
     def render_cached(self, cam: dict, cache: "OracleCache", mode: int = 0, rows=None, threads: int | None = None,
-                      reasons: bool = False):
-        """(results, counts) or, with reasons=True, (results, counts, {reason: samples})."""
+                      reasons: bool = False, contrib: bool = False):
+        """(results, counts), plus {reason: samples} with reasons=True, plus the per-pixel contribution
+        weights [H, W, 2] (resampled, cache; alpha T summed) with contrib=True."""
         c = make_cam(cam)
         cc = make_cam(cache.cam)
         W, H = c.W, c.H
@@ -363,12 +364,16 @@ class OracleModel:
         res = np.zeros((H, W, 4), np.float32)
         counts = np.zeros((H, W, 4), np.int32)
         why = np.zeros(8, np.int64)
+        con = np.zeros((H, W, 2), np.float64) if contrib else None
         lib().orc_render_cached(C.byref(self.net), C.byref(self.scene), C.byref(self.steps), C.byref(c), ptr(self.bits),
                                 C.byref(cache.s), C.byref(cc), C.byref(cache.steps or self.steps), mode, r0, r1, ptr(res),
-                                ptr(counts), threads or default_threads(), ptr(why))
+                                ptr(counts), threads or default_threads(), ptr(why), ptr(con) if contrib else None)
+        out = (res, counts)
         if reasons:
-            return res, counts, {k: int(why[i + 1]) for i, k in enumerate(self.REASONS)}
-        return res, counts
+            out += ({k: int(why[i + 1]) for i, k in enumerate(self.REASONS)},)
+        if contrib:
+            out += (con,)
+        return out
 
 
 class OracleCache:

@@ -353,3 +353,41 @@ def test_cache_sizing_changes_capacity_and_matches_oracle(model3):
     np.testing.assert_array_equal(buf.ray_counts[..., 0], counts[..., 0])
     np.testing.assert_array_equal(buf.ray_counts[..., 1], counts[..., 1])
     assert float(np.abs(buf.results - ref).max()) <= COLOR_ATOL
+
+
+def test_contribution_weights_match_oracle(model3):
+    """The cached render's per-pixel contribution weights (alpha T summed
+    over resampled and over cache samples, accumulate_cache_perf_kernel<DEBUG>)
+    against the oracle's; they add up to the pixel's opacity 1 - T, and they
+    accumulate into the caller's buffers across renders."""
+    torch = pytest.importorskip("torch")
+    loader, om, _ = model3
+    W, H = 48, 40
+    cam0 = small_camera(1001, W, H)
+    r, c0, c1 = _cache_setup(loader, cam0)
+    r.initCacheBlockwise(fvc.raymarch_info(cam0, loader.stepsize_info))
+    r.swapCache()
+    c2w = np.asarray(cam0["cam2world"], np.float64)
+    a = np.radians(1.5)
+    R = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+    cam1 = fcam.camera_dict(np.concatenate([R @ c2w[:, :3], (R @ c2w[:, 3])[:, None]], axis=1), W, H)
+    res = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    cr = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    cc = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    info = fvc.raymarch_info(cam1, loader.stepsize_info)
+    r.render_device(info, results=res, contrib_resample=cr, contrib_cache=cc)
+    r.synchronize()
+    oc = orc.OracleCache(om.cache_dims(W, H), cam0)
+    oc.load_device_cache(*c1.read())
+    ref, counts, con = om.render_cached(cam1, oc, contrib=True)
+    g_r, g_c = cr.cpu().numpy(), cc.cpu().numpy()
+    assert con[..., 1].sum() > 1.0 and con[..., 0].sum() > 1.0
+    assert np.abs(g_r - con[..., 0]).max() <= COLOR_ATOL and np.abs(g_c - con[..., 1]).max() <= COLOR_ATOL
+    T = res.cpu().numpy()[..., 3]
+    np.testing.assert_allclose(g_r + g_c, 1.0 - T, atol=1e-4)
+    r.render_device(info, results=res, contrib_resample=cr, contrib_cache=cc)
+    r.synchronize()
+    np.testing.assert_allclose(cr.cpu().numpy(), 2 * g_r, rtol=1e-6, atol=1e-7)
+    plain = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+    with pytest.raises(fvc._lib.FvcError):
+        plain.render_device(info, results=res, contrib_resample=cr, contrib_cache=cc)
