@@ -43,13 +43,14 @@ def _read_png(path):
         assert zlib.crc32(t + body) & 0xFFFFFFFF == crc
         if t == b"IHDR":
             w, h = struct.unpack(">II", body[:8])
+            ch = {6: 4, 0: 1}[body[9]]
         elif t == b"IDAT":
             idat += body
         off += 12 + n
     raw = zlib.decompress(idat)
-    rows = np.frombuffer(raw, np.uint8).reshape(h, 1 + 4 * w)
+    rows = np.frombuffer(raw, np.uint8).reshape(h, 1 + ch * w)
     assert (rows[:, 0] == 0).all()
-    return rows[:, 1:].reshape(h, w, 4)
+    return rows[:, 1:].reshape(h, w, ch) if ch > 1 else rows[:, 1:].reshape(h, w)
 
 
 def test_cpp_header_host_checks(tmp_path):
@@ -98,3 +99,23 @@ def test_eval_writes_reference_output_tree(tmp_path):
         assert set(m["rot"][0]) == {"image", "n_bricks_set", "n_bricks_reserved", "overflow", "n_cache_samples", "n_resamples"}
         t = json.load(open(d / "timings.json"))
         assert t["no_cache"]["render_time_ms"] > 0 and len(t["rot"]) == 18
+
+
+def test_eval_writes_contribution_images(tmp_path):
+    """-w -wc: every rotation / translation offset gets <name>_contr_new.png and
+    <name>_contr_cache.png, one-channel images of the resampled and cached
+    samples' compositing weight; where both are written their sum is the
+    pixel's opacity, at most 255 (plus rounding)."""
+    exe = fbuild.build_eval()
+    cam_file, cams = _camera_file(tmp_path, W=64, H=48)
+    out = tmp_path / "out"
+    r = subprocess.run([exe, tiny_model(7, 1), str(cam_file), str(out), "-w", "-wc"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    d = out / "frame_000"
+    for stem in ["rot/5/0", "rot/10/60", "trans/0.100000"]:
+        new = _read_png(d / f"{stem}_contr_new.png")
+        cache = _read_png(d / f"{stem}_contr_cache.png")
+        assert new.shape == (48, 64) and cache.shape == (48, 64)
+        assert (new.astype(int) + cache.astype(int)).max() <= 256
+        assert new.any() or cache.any()
