@@ -2,6 +2,7 @@
 
     python bench_case.py --res 960x540 --frames 2 --path plain --network tc
     python bench_case.py --res 400x400 --frames 2 --path backward --rays 65536
+    python bench_case.py --res 960x540 --frames 1 --path plain --tile 256
 
 Renders `frames` frames of the benchmark's camera path (the synthetic
 3-cascade, 2^19-entry scene) at the given resolution through the C ABI and
@@ -30,6 +31,11 @@ def main(argv=None) -> None:
     ap.add_argument("--path", choices=["plain", "cached", "backward"], default="plain")
     ap.add_argument("--network", choices=["tc", "mma"], default="tc")
     ap.add_argument("--rays", type=int, default=1 << 16, help="rays per backward step")
+    ap.add_argument("--tile", type=int, choices=[64, 128, 256], default=128, help="tcgen05 network tile height (plain path)")
+    ap.add_argument("--batch-rows", type=int, default=0, help="compaction batch, rows per sub-iteration (0: capacity)")
+    ap.add_argument("--no-skip", action="store_true", help="occupancy lookup at every step (no empty-space skipping)")
+    ap.add_argument("--separate-classify", action="store_true",
+                    help="cached path: the classification pass and two row lists instead of the classifying march")
     args = ap.parse_args(argv)
     W, H = (int(v) for v in args.res.lower().split("x"))
     if args.path == "backward":
@@ -48,6 +54,10 @@ def main(argv=None) -> None:
         r.setCacheSettings(default_cache_settings())
     r.resizeRenderbuffers((W, H))
     r.set_network_path(args.network == "tc")
+    r.set_tiling(args.tile, args.batch_rows)
+    r.set_empty_space_skipping(not args.no_skip)
+    if args.path == "cached":
+        r.set_fused_classify(not args.separate_classify)
     r.set_kernel_timing(True)
     for i, info in enumerate(infos):
         build = None

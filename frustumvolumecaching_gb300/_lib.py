@@ -152,6 +152,7 @@ SIGNATURES = {
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
     "fvc_renderer_set_tiling": (c_int, [P, c_int, c_int]),
     "fvc_renderer_set_fused_classify": (c_int, [P, c_int]),
+    "fvc_renderer_set_empty_space_skipping": (c_int, [P, c_int]),
     "fvc_cache_set_sizing": (c_int, [P, c_int, C.c_float]),
     "fvc_renderer_set_kernel_timing": (c_int, [P, c_int]),
     "fvc_renderer_set_precision": (c_int, [P, c_int]),

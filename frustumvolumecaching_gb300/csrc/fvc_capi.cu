@@ -435,6 +435,7 @@ struct fvc_renderer {
     int m_tile = 128;                 /* tcgen05 network tile of the plain path (autotuned) */
     int row_target = 0;               /* compaction batch, rows per sub-iteration (0: the row capacity; autotuned) */
     int fused_classify = 1;           /* cached renders: classification inside the march (see fvc_renderer_set_fused_classify) */
+    int skip_empty = 1;               /* empty-space skipping in the march (fvc_renderer_set_empty_space_skipping) */
     int cache_est_samples = 32;       /* cache sizing: estimated samples per ray ... */
     float cache_sparsity = 0.5f;      /* ... and brick sparsity (fvc_cache_set_sizing) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
@@ -1245,6 +1246,7 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.steps_per_iter = r->steps_per_iter;
     p.m_tile = r->m_tile;
     p.fused_classify = r->fused_classify;
+    p.skip_empty = r->skip_empty;
     p.row_target = std::min(r->row_target, r->row_capacity);
     return FVC_OK;
 }
@@ -1798,6 +1800,13 @@ extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
 {
     CHECK_ARG(r && (use_tcgen05 == 0 || use_tcgen05 == 1), "fvc_renderer_set_network_path: bad arguments");
     r->use_tc = use_tcgen05;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_empty_space_skipping(fvc_renderer *r, int on)
+{
+    CHECK_ARG(r && (on == 0 || on == 1), "fvc_renderer_set_empty_space_skipping: bad arguments");
+    r->skip_empty = on;
     return FVC_OK;
 }
 

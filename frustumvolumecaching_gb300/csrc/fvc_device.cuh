@@ -240,6 +240,61 @@ __device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__re
     return (__ldg(bits + bidx) >> (idx & 7u)) & 1u;
 }
 
+/* occupied() plus, for an empty cell, the extent of empty space along the
+ * ray: the DDA of grid_occupied_at's t_dist_to_next_voxel form
+ * (include/raymarch_common.h:712-744), made conservative so that skipping
+ * never changes a result.  t_free receives a t below which every point
+ * o + t d (t >= the query's) lies in the same empty cell by the same
+ * arithmetic occupied() uses: the cell's exit face along each axis less a
+ * margin of 1/1024 of the cell (in world units, far above the float rounding
+ * of the point, of its unit coordinates and of the cell index), and no skip
+ * at all (t_free = -inf) when the point itself is within that margin of a
+ * face, the cell is outside the grid or the ray is axis-parallel in a way
+ * that leaves a face within the margin.  Cells of one mip level never
+ * straddle a cascade boundary (the inner cascade covers cells 32..95 of the
+ * outer one), so a mip-m cell's points all index mip m. */
+__device__ __forceinline__ bool occupied_skip(const DevScene &sc, const uint8_t *__restrict__ bits, float3 o, float3 d,
+                                              float3 inv_d, float t, float &t_free)
+{
+    const float3 p = at(o, d, t);
+    float3 u = p;
+    if (!sc.normalized)
+        u = make_float3(F_DIV(F_SUB(p.x, sc.unit_off.x), sc.unit_den.x), F_DIV(F_SUB(p.y, sc.unit_off.y), sc.unit_den.y),
+                        F_DIV(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z));
+    const float ax = F_SUB(u.x, 0.5f), ay = F_SUB(u.y, 0.5f), az = F_SUB(u.z, 0.5f);
+    const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
+    t_free = -1e30f;
+    if (!(mx <= 3.0e38f)) return false;
+    const int mip = max(0, frexp_exponent(mx) + 1);
+    if (mip >= sc.nlvl) return false;
+    const float sm = __int_as_float((127 - mip) << 23);
+    const int ix = (int)F_MUL(F_ADD(F_MUL(ax, sm), 0.5f), 128.0f);
+    const int iy = (int)F_MUL(F_ADD(F_MUL(ay, sm), 0.5f), 128.0f);
+    const int iz = (int)F_MUL(F_ADD(F_MUL(az, sm), 0.5f), 128.0f);
+    const uint32_t idx = expand_bits3((uint32_t)ix) | (expand_bits3((uint32_t)iy) << 1) | (expand_bits3((uint32_t)iz) << 2);
+    const uint32_t bidx = idx / 8u + (uint32_t)((128 * 128 * 128 / 8) * mip);
+    if ((__ldg(bits + bidx) >> (idx & 7u)) & 1u) return true;
+    /* the empty cell's faces in world units: unit a = (i / 128 - 1/2) 2^mip + 1/2 */
+    const float cell = __int_as_float((127 + mip - 7) << 23); /* 2^mip / 128, in unit coordinates */
+    const float den[3] = {sc.normalized ? 1.f : sc.unit_den.x, sc.normalized ? 1.f : sc.unit_den.y, sc.normalized ? 1.f : sc.unit_den.z};
+    const float off[3] = {sc.normalized ? 0.f : sc.unit_off.x, sc.normalized ? 0.f : sc.unit_off.y, sc.normalized ? 0.f : sc.unit_off.z};
+    const int ic[3] = {ix, iy, iz};
+    const float pc[3] = {p.x, p.y, p.z}, oc[3] = {o.x, o.y, o.z}, dc[3] = {d.x, d.y, d.z}, ic_inv[3] = {inv_d.x, inv_d.y, inv_d.z};
+    const float half = __int_as_float((127 + mip - 1) << 23); /* 2^mip / 2 */
+    float tf = 1e30f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float lo_u = (float)ic[k] * cell - half + 0.5f, hi_u = lo_u + cell;
+        const float lo = off[k] + lo_u * den[k], hi = off[k] + hi_u * den[k];
+        const float margin = cell * den[k] * (1.0f / 1024.0f);
+        if (!(pc[k] - lo > margin && hi - pc[k] > margin)) return false; /* too close to a face: no skip */
+        if (dc[k] > 0.f) tf = fminf(tf, (hi - margin - oc[k]) * ic_inv[k]);
+        else if (dc[k] < 0.f) tf = fminf(tf, (lo + margin - oc[k]) * ic_inv[k]);
+    }
+    t_free = tf;
+    return false;
+}
+
 /* apply_contraction, include/raymarch_common.h:610-653 */
 __device__ __forceinline__ float3 contract(const DevScene &sc, float3 p)
 {

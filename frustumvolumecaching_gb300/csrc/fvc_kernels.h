@@ -227,6 +227,7 @@ struct RenderParams {
     int steps_per_iter;         /* marching steps per ray and sub-iteration */
     int m_tile;                 /* rows per tcgen05 network tile on the plain path: 64, 128 (0 = 128) or 256 */
     int fused_classify;         /* cached renders: classification in the march, one network launch for all rows */
+    int skip_empty;             /* the march skips occupancy lookups inside empty cells (exact: occupied_skip) */
     float *contrib_res, *contrib_cache; /* cached renders: per-pixel compositing weight of resample / cache samples (added) */
     int row_target;             /* compaction batch: rows per sub-iteration the march aims at, samples per ray
                                  * = clamp(row_target / alive rays, 1, S_ROWS) (0 = row_capacity) */

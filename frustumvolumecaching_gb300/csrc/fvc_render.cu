@@ -436,6 +436,11 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
             dt4 = states[i].dt;
             const float3 o = make_float3(of.x, of.y, of.z), d = make_float3(dt4.x, dt4.y, dt4.z);
             float t1 = dt4.w;
+            /* empty-space skipping: steps whose midpoint lies before t_free are in an empty cell
+             * (occupied_skip's conservative DDA bound) and skip the occupancy lookup; the step
+             * sequence and every occupancy outcome stay those of the plain march */
+            const float3 inv_d = make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+            float t_free = -1e30f;
             for (int c0 = 0; c0 < p.steps_per_iter; c0 += 4) {
                 float t0c[4], t1c[4];
                 bool past[4], occ[4];
@@ -447,7 +452,12 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
                     t1c[c] = F_ADD(tt, dtc);
                     const float tm = F_MUL(F_ADD(tt, t1c[c]), 0.5f);
                     past[c] = tm > of.w;
-                    occ[c] = !past[c] && occupied(p.scene, p.bits, at(o, d, tm));
+                    bool oc = false;
+                    if (!past[c] && !(tm < t_free)) {
+                        if (p.skip_empty) oc = occupied_skip(p.scene, p.bits, o, d, inv_d, tm, t_free);
+                        else oc = occupied(p.scene, p.bits, at(o, d, tm));
+                    }
+                    occ[c] = oc;
                     tt = t1c[c];
                 }
 #pragma unroll

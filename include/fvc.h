@@ -333,6 +333,14 @@ int fvc_renderer_set_tiling(fvc_renderer *r, int m_tile, int batch_rows);
  * are the same bit for bit; the switch is for measurement. */
 int fvc_renderer_set_fused_classify(fvc_renderer *r, int on);
 
+/* Empty-space skipping in the renderers' march: 1 (the default) looks the
+ * occupancy grid up once per empty cell and steps through the rest of the
+ * cell without lookups (a DDA bound on the cell's extent along the ray, as
+ * grid_occupied_at's t_dist_to_next_voxel, include/raymarch_common.h:712-744,
+ * kept a margin inside the cell so every step and occupancy decision is the
+ * plain march's); 0 looks up every step.  Results are identical. */
+int fvc_renderer_set_empty_space_skipping(fvc_renderer *r, int on);
+
 /* MLP precision of the plain renderers on the tcgen05 path (no counterpart
  * in the reference, whose MLPs are fp16): FP16 (default), BF16, or
  * FP8-E4M3 with per-layer weight scaling and per-row activation scaling;

@@ -391,3 +391,34 @@ def test_contribution_weights_match_oracle(model3):
     plain = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
     with pytest.raises(fvc._lib.FvcError):
         plain.render_device(info, results=res, contrib_resample=cr, contrib_cache=cc)
+
+
+@pytest.mark.parametrize("scene", ["c1_golden", "c2_golden", "config1"])
+def test_empty_space_skipping_is_exact(tmp_path, request, scene):
+    """The march with empty-space skipping (one occupancy lookup per empty
+    cell, a conservative DDA bound for the rest of the cell) gives the plain
+    march's render bit for bit: results, per-ray samples and steps, on the
+    hash-defined golden grids (1 and 3 cascades, full frame) and on the 256x256
+    workload's scene; and it performs fewer lookups, which shows as time only."""
+    if scene == "config1":
+        loader = fvc.load_data(fmodel.ensure_model(fmodel.spec_config1()))
+        cam = small_camera(1701, 256, 256)
+    else:
+        name = scene.split("_")[0]
+        _, _, base = request.getfixturevalue("model1" if name == "c1" else "model3")
+        loader = fvc.load_data(_golden_model(tmp_path, name, base))
+        sc = SCENES[name]
+        cam = _golden_cam(sc)
+        if name == "c2":
+            cam = fcam.camera_dict(np.asarray(cam["cam2world"], np.float64), 640, 360)
+    out = []
+    for skip in (True, False):
+        r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
+        r.set_empty_space_skipping(skip)
+        buf = fvc.RenderBuffer(cam["resolution"])
+        r.render(fvc.raymarch_info(cam, loader.stepsize_info), buf)
+        out.append((buf, r._render_stats.n_steps))
+    (a, sa), (b, sb) = out
+    np.testing.assert_array_equal(a.ray_counts, b.ray_counts)
+    np.testing.assert_array_equal(a.results, b.results)
+    assert sa == sb and a.ray_counts[..., 0].sum() > 0
