@@ -101,6 +101,7 @@ def test_eval_writes_reference_output_tree(tmp_path):
         assert t["no_cache"]["render_time_ms"] > 0 and len(t["rot"]) == 18
 
 
+@pytest.mark.gpu
 def test_eval_writes_contribution_images(tmp_path):
     """-w -wc: every rotation / translation offset gets <name>_contr_new.png and
     <name>_contr_cache.png, one-channel images of the resampled and cached
