@@ -249,12 +249,13 @@ __device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__re
  * margin of 1/1024 of the cell (in world units, far above the float rounding
  * of the point, of its unit coordinates and of the cell index), and no skip
  * at all (t_free = -inf) when the point itself is within that margin of a
- * face, the cell is outside the grid or the ray is axis-parallel in a way
- * that leaves a face within the margin.  Cells of one mip level never
+ * face or the cell is outside the grid.  A cell narrower than 4 steps (dt,
+ * the query's step) is not skipped: computing its bound costs about what
+ * the lookups it saves do.  Cells of one mip level never
  * straddle a cascade boundary (the inner cascade covers cells 32..95 of the
  * outer one), so a mip-m cell's points all index mip m. */
 __device__ __forceinline__ bool occupied_skip(const DevScene &sc, const uint8_t *__restrict__ bits, float3 o, float3 d,
-                                              float3 inv_d, float t, float &t_free)
+                                              float3 inv_d, float t, float dt, float &t_free)
 {
     const float3 p = at(o, d, t);
     float3 u = p;
@@ -277,6 +278,8 @@ __device__ __forceinline__ bool occupied_skip(const DevScene &sc, const uint8_t 
     /* the empty cell's faces in world units: unit a = (i / 128 - 1/2) 2^mip + 1/2 */
     const float cell = __int_as_float((127 + mip - 7) << 23); /* 2^mip / 128, in unit coordinates */
     const float den[3] = {sc.normalized ? 1.f : sc.unit_den.x, sc.normalized ? 1.f : sc.unit_den.y, sc.normalized ? 1.f : sc.unit_den.z};
+    /* cells that span fewer than 4 steps along the ray are cheaper to look up step by step */
+    if (cell * fminf(fminf(den[0], den[1]), den[2]) < 4.0f * dt * fmaxf(fmaxf(fabsf(d.x), fabsf(d.y)), fabsf(d.z))) return false;
     const float off[3] = {sc.normalized ? 0.f : sc.unit_off.x, sc.normalized ? 0.f : sc.unit_off.y, sc.normalized ? 0.f : sc.unit_off.z};
     const int ic[3] = {ix, iy, iz};
     const float pc[3] = {p.x, p.y, p.z}, oc[3] = {o.x, o.y, o.z}, dc[3] = {d.x, d.y, d.z}, ic_inv[3] = {inv_d.x, inv_d.y, inv_d.z};

@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
                     past[c] = tm > of.w;
                     bool oc = false;
                     if (!past[c] && !(tm < t_free)) {
-                        if (p.skip_empty) oc = occupied_skip(p.scene, p.bits, o, d, inv_d, tm, t_free);
+                        if (p.skip_empty) oc = occupied_skip(p.scene, p.bits, o, d, inv_d, tm, dtc, t_free);
                         else oc = occupied(p.scene, p.bits, at(o, d, tm));
                     }
                     occ[c] = oc;
