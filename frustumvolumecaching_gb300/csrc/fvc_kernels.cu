@@ -157,11 +157,12 @@ __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
         const int tile = p.alive_list[ai];
         CacheRay cr = p.rays[(size_t)tile * 64 + k];
         int bstep = p.block_step[tile];
-        int total = 0;
         uint32_t mask = 0;
+        bool found = false;
+        /* one block-wide vote per depth brick (__syncthreads_or): any ray alive, any sample occupied */
         for (int guard = 0; guard < p.max_search; ++guard) {
-            if (tile_block_sum(cr.alive, red) <= 0) break;
-            if (bstep >= p.bZ) { cr.alive = 0; total = 0; break; } /* beyond the frustum depth: stop the tile */
+            if (!__syncthreads_or(cr.alive)) break;
+            if (bstep >= p.bZ) { cr.alive = 0; break; } /* beyond the frustum depth: stop the tile */
             float t1 = t_from_step(p.steps, F_ADD((float)(bstep * 8), p.steps.near_i));
             mask = 0;
 #pragma unroll
@@ -173,11 +174,11 @@ __global__ void __launch_bounds__(64) cache_search_kernel(CacheBuildParams p)
                 if (tm > cr.far_) cr.alive = 0;
                 else if (occupied(p.scene, p.bits, at(cr.o, cr.d, tm))) mask |= 1u << s;
             }
-            total = tile_block_sum(__popc(mask), red);
-            if (total > 0) break;
+            if (__syncthreads_or(mask != 0u)) { found = true; break; }
             ++bstep;
             if (guard == p.max_search - 1) atomicOr(p.guard, 4);
         }
+        const int total = found ? tile_block_sum(__popc(mask), red) : 0; /* found is block-uniform */
         const int n_alive = tile_block_sum(cr.alive, red);
         const bool processed = total > 0 && n_alive > 0;
         if (k == 0) {
