@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import time
 
 from frustumvolumecaching_gb300 import camera as fcam
 from frustumvolumecaching_gb300 import model as fmodel
@@ -34,15 +35,22 @@ def main(argv=None) -> None:
     ap.add_argument("--tile", type=int, choices=[64, 128, 256], default=128, help="tcgen05 network tile height (plain path)")
     ap.add_argument("--batch-rows", type=int, default=0, help="compaction batch, rows per sub-iteration (0: capacity)")
     ap.add_argument("--no-skip", action="store_true", help="occupancy lookup at every step (no empty-space skipping)")
+    ap.add_argument("--scene", choices=["c2", "c1"], default="c2",
+                    help="c2: the cached workload's scene and camera path; c1: the 256x256 workload's scene, seeded camera")
     ap.add_argument("--separate-classify", action="store_true",
                     help="cached path: the classification pass and two row lists instead of the classifying march")
     args = ap.parse_args(argv)
     W, H = (int(v) for v in args.res.lower().split("x"))
     if args.path == "backward":
         return backward_case(args, W, H)
-    spec = fmodel.spec_config2()
-    loader = load_data(fmodel.ensure_model(spec))
-    cams = fcam.rotation_path(spec.seed, n_frames=args.frames, width=W, height=H)
+    if args.scene == "c1":
+        spec = fmodel.spec_config1()
+        loader = load_data(fmodel.ensure_model(spec))
+        cams = [fcam.seeded_camera(spec.seed, width=W, height=H)] * args.frames
+    else:
+        spec = fmodel.spec_config2()
+        loader = load_data(fmodel.ensure_model(spec))
+        cams = fcam.rotation_path(spec.seed, n_frames=args.frames, width=W, height=H)
     infos = [raymarch_info(c, loader.stepsize_info) for c in cams]
     if args.path == "plain":
         r = PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
@@ -65,11 +73,13 @@ def main(argv=None) -> None:
             r.initCacheBlockwise(info)
             r.swapCache()
             build = r._init_stats
+        t0 = time.perf_counter()
         r.render_device(info)
-        st = r._render_stats
+        st = r._render_stats  # waits for the frame
+        frame_ms = (time.perf_counter() - t0) * 1e3
         line = {"frame": i, "resample_rows": st.n_resamples, "cache_rows": st.n_cache_hits, "steps": st.n_steps,
                 "launches": st.n_launches, "resample_kernel_launches": st.n_timed_launches,
-                "resample_kernel_ms": round(st.timed_kernel_ms, 3), "guard": st.guard_flags}
+                "resample_kernel_ms": round(st.timed_kernel_ms, 3), "frame_ms": round(frame_ms, 3), "guard": st.guard_flags}
         if args.path == "cached":
             cov = st.n_cache_hits / max(1, st.n_cache_hits + st.n_resamples)
             line["coverage"] = round(cov, 4)
