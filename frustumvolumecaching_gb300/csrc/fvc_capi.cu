@@ -2187,9 +2187,11 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
     if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     /* candidates: the tcgen05 tile heights and the 32-row mma.sync warp tile, each with compaction
-     * batches of 2^16..2^20 rows per sub-iteration */
+     * batches of 2^16..2^20 rows per sub-iteration and two larger ones (2^22, 2^24: on batches of tens of
+     * millions of rays a small batch leaves one sample per ray and sub-iteration, and the sub-iterations'
+     * fixed cost - every alive ray's state moved once - dominates) */
     const int tiles[4] = {64, 128, 256, 32};
-    const int batches[5] = {1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20};
+    const int batches[7] = {1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20, 1 << 22, 1 << 24};
     const int saved_tc = r->use_tc, saved_tile = r->m_tile, saved_target = r->row_target;
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
@@ -2198,7 +2200,7 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
     int best_tile = 0, best_batch = 0, n_cand = 0, rc = FVC_OK;
     long long best_rows = 0;
     for (int ti = 0; ti < 4 && rc == FVC_OK; ++ti)
-        for (int bi = 0; bi < 5 && rc == FVC_OK; ++bi) {
+        for (int bi = 0; bi < 7 && rc == FVC_OK; ++bi) {
             r->use_tc = tiles[ti] != 32;
             r->m_tile = tiles[ti] == 32 ? 128 : tiles[ti];
             r->row_target = batches[bi];
