@@ -124,6 +124,7 @@ SIGNATURES = {
     "fvc_model_info": (c_int, [P, C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
     "fvc_debug_fail_allocation": (c_int, [C.c_longlong]),
     "fvc_selftest_wait_timeout": (c_int, [C.c_double, C.POINTER(C.c_double)]),
+    "fvc_selftest_division": (c_int, [P, P, c_int, P, P]),
     "fvc_stepsize_setup": (c_int, [C.POINTER(SceneInfo), C.POINTER(StepsizeInfo)]),
     "fvc_model_density": (c_int, [P, P, c_int, P]),
     "fvc_model_inference": (c_int, [P, P, P, c_int, P]),

@@ -435,7 +435,8 @@ struct fvc_renderer {
     int m_tile = 128;                 /* tcgen05 network tile of the plain path (autotuned) */
     int row_target = 0;               /* compaction batch, rows per sub-iteration (0: the row capacity; autotuned) */
     int fused_classify = 1;           /* cached renders: classification inside the march (see fvc_renderer_set_fused_classify) */
-    int skip_empty = 1;               /* empty-space skipping in the march (fvc_renderer_set_empty_space_skipping) */
+    int skip_empty = 0;               /* empty-space skipping in the march (fvc_renderer_set_empty_space_skipping); off by
+                                       * default: measured slower (the lanes of a warp rarely skip the same steps) */
     int cache_est_samples = 32;       /* cache sizing: estimated samples per ray ... */
     float cache_sparsity = 0.5f;      /* ... and brick sparsity (fvc_cache_set_sizing) */
     float4 *d_row_dout = nullptr;     /* per-row gradients of the differentiable render */
@@ -527,7 +528,8 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
     const int n_levels = (int)enc.num_or("n_levels", 16), F = (int)enc.num_or("n_features_per_level", 2);
     const int log2T = (int)enc.num_or("log2_hashmap_size", 19), N0 = (int)enc.num_or("base_resolution", 16);
     const float b = (float)enc.num_or("per_level_scale", 2.0);
-    if (n_levels != 16 || F != 2) return fail(FVC_ERR_CONFIG, "only the 16-level, 2-feature hash grid is built");
+    if (!((n_levels == 16 && F == 2) || (n_levels == 8 && F == 4)))
+        return fail(FVC_ERR_CONFIG, "the hash grid must have 16 levels of 2 features or 8 levels of 4 features");
     if (log2T < 4 || log2T > 24) return fail(FVC_ERR_CONFIG, "log2_hashmap_size out of range");
     const int width = (int)base["network"].num_or("n_neurons", 64);
     if (width != 64 || (int)base["network"].num_or("n_hidden_layers", 1) != 1)
@@ -573,6 +575,7 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
      * size = min(round_up(res^3, 8), 2^log2T); explicit fvc_level_scales wins */
     DevGrid &g = m.grid;
     g.n_levels = n_levels;
+    g.F = F;
     g.dense_mask = 0;
     const JVal &ls = enc["fvc_level_scales"];
     const float log2b = std::log2(b);
@@ -584,7 +587,7 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         uint64_t n = (uint64_t)res * res * res;
         n = (n + 7) / 8 * 8;
         const uint32_t size = (uint32_t)std::min<uint64_t>(n, 1ull << log2T);
-        g.scale[l] = scale; g.res[l] = res; g.res2[l] = res * res; g.size[l] = size; g.offset[l] = off;
+        g.scale[l] = scale; g.res[l] = res; g.res2[l] = res * res; g.size[l] = size; g.offset[l] = off * (uint32_t)(F / 2);
         if ((uint64_t)res * res * res <= size) g.dense_mask |= 1u << l;
         off += size;
     }
@@ -739,9 +742,13 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
     d.unit_off = make_float3(s.aabb_from.x / sc2, s.aabb_from.y / sc2, s.aabb_from.z / sc2);
     d.unit_den = make_float3((s.aabb_to.x - s.aabb_from.x) / sc2, (s.aabb_to.y - s.aabb_from.y) / sc2, (s.aabb_to.z - s.aabb_from.z) / sc2);
     d.aabb_den = make_float3(s.aabb_to.x - s.aabb_from.x, s.aabb_to.y - s.aabb_from.y, s.aabb_to.z - s.aabb_from.z);
+    /* correctly rounded reciprocals for the kernels' exact divisions (div_rn_by) */
+    d.unit_rcp = make_float3(1.0f / d.unit_den.x, 1.0f / d.unit_den.y, 1.0f / d.unit_den.z);
+    d.aabb_rcp = make_float3(1.0f / d.aabb_den.x, 1.0f / d.aabb_den.y, 1.0f / d.aabb_den.z);
     d.c_from = make_float3(s.contraction_aabb_from.x, s.contraction_aabb_from.y, s.contraction_aabb_from.z);
     d.c_den = make_float3(s.contraction_aabb_to.x - s.contraction_aabb_from.x, s.contraction_aabb_to.y - s.contraction_aabb_from.y,
                           s.contraction_aabb_to.z - s.contraction_aabb_from.z);
+    d.c_rcp = make_float3(1.0f / d.c_den.x, 1.0f / d.c_den.y, 1.0f / d.c_den.z);
     d.nlvl = s.grid_nlvl; d.normalized = s.normalized; d.contraction = s.contraction_type; d.is_open_gl = s.is_open_gl;
     d.alpha_thre = s.alpha_thre;
 
@@ -749,7 +756,7 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
     CU(cudaDeviceGetAttribute(&m.n_sms, cudaDevAttrMultiProcessorCount, m.device));
     int rc;
     if ((rc = dalloc(&m.d_bits, bits.size(), "occupancy bits"))) return rc;
-    if ((rc = dalloc(&m.d_table, (size_t)off, "hash tables"))) return rc;
+    if ((rc = dalloc(&m.d_table, (size_t)off * (F / 2), "hash tables"))) return rc;
     if ((rc = dalloc(&m.d_weights, (size_t)W_TOTAL, "weights"))) return rc;
     if ((rc = dalloc(&m.d_bias3, (size_t)64, "bias"))) return rc;
     if ((rc = dalloc(&m.d_weights_tc, (size_t)TC_WBYTES, "tcgen05 weights"))) return rc;
@@ -994,6 +1001,22 @@ extern "C" int fvc_selftest_wait_timeout(double limit_ms, double *waited_ms)
     if (e != cudaSuccess) return fail(FVC_ERR_CUDA, std::string("wait self-test: ") + cudaGetErrorString(e));
     if (waited_ms) *waited_ms = (double)h[1] / (double)khz;
     if (h[0]) return fail(FVC_ERR_TIMEOUT, "bounded device wait gave up after " + std::to_string((double)h[1] / khz) + " ms");
+    return FVC_OK;
+}
+
+extern "C" int fvc_selftest_division(const float *x, const float *d, int n, float *q, float *q_ieee)
+{
+    CHECK_ARG(x && d && q && q_ieee && n > 0 && n <= (1 << 24), "fvc_selftest_division: bad arguments");
+    float *b = nullptr;
+    int rc;
+    if ((rc = dalloc(&b, (size_t)4 * n, "division self-test"))) return rc;
+    cudaError_t e = cudaMemcpy(b, x, (size_t)n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b + n, d, (size_t)n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_div_selftest(b, b + n, n, b + 2 * (size_t)n, b + 3 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(q, b + 2 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(q_ieee, b + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    dfree(b);
+    if (e != cudaSuccess) return fail(FVC_ERR_CUDA, std::string("division self-test: ") + cudaGetErrorString(e));
     return FVC_OK;
 }
 
@@ -1858,7 +1881,7 @@ extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
     *out = nullptr;
     if (m->view_dependent) return fail(FVC_ERR_CONFIG, "the adjoint is built for networks without the view-dependent split head");
     if (m->n_latents != 8 || m->grid.n_levels != 16)
-        return fail(FVC_ERR_CONFIG, "the backward kernels are built for 16 hash levels and 8 latents");
+        return fail(FVC_ERR_CONFIG, "the backward kernels are built for 16 hash levels of 2 features and 8 latents");
     auto g = std::make_unique<fvc_grad>();
     g->m = m;
     g->n_table = m->table_entries * 2;

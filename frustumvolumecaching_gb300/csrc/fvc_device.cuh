@@ -29,6 +29,7 @@ struct DevScene {
     float3 unit_den;  /* (aabb_to - aabb_from) / 2^(nlvl-1) */
     float3 aabb_den;  /* aabb_to - aabb_from                 (contract_aabb)      */
     float3 c_from, c_den; /* contraction aabb and its extent */
+    float3 unit_rcp, aabb_rcp, c_rcp; /* correctly rounded 1 / unit_den, 1 / aabb_den, 1 / c_den (div_rn_by) */
     int nlvl, normalized, contraction, is_open_gl;
     float alpha_thre;
 };
@@ -53,6 +54,7 @@ struct DevCam {
 constexpr int MAX_LEVELS = 16;
 struct DevGrid {
     int n_levels;
+    int F;                /* features per level: 2 (16 levels) or 4 (8 levels); offset[] counts half2 */
     uint32_t dense_mask;
     float scale[MAX_LEVELS];
     uint32_t res[MAX_LEVELS], res2[MAX_LEVELS], size[MAX_LEVELS], offset[MAX_LEVELS];
@@ -111,6 +113,22 @@ __device__ __forceinline__ float dot3(float3 a, float3 b)
 __device__ __forceinline__ float3 at(float3 o, float3 d, float t)
 {
     return make_float3(F_ADD(o.x, F_MUL(t, d.x)), F_ADD(o.y, F_MUL(t, d.y)), F_ADD(o.z, F_MUL(t, d.z)));
+}
+
+/* x / d rounded to nearest, from r = RN(1 / d): q0 = RN(x r), the exact
+ * residual e = x - q0 d by one fused multiply-add, q = RN(q0 + e r).  With a
+ * correctly rounded reciprocal this is the correctly rounded quotient
+ * (Markstein, "Computation of elementary functions on the IBM RISC
+ * System/6000 processor", IBM J. Res. Dev. 1990) for operands away from
+ * overflow and underflow: the same bits as the IEEE division, in three
+ * instructions when d is fixed and r computed once.  The scene's
+ * denominators come with their reciprocals; a per-ray denominator takes one
+ * __frcp_rn. */
+__device__ __forceinline__ float div_rn_by(float x, float d, float r)
+{
+    const float q0 = __fmul_rn(x, r);
+    const float e = __fmaf_rn(-q0, d, x);
+    return __fmaf_rn(e, r, q0);
 }
 
 /* generateRay for the pixel centre (deterministic), include/raymarch_common.h:190-251;
@@ -224,8 +242,9 @@ __device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__re
 {
     float3 u = p;
     if (!sc.normalized)
-        u = make_float3(F_DIV(F_SUB(p.x, sc.unit_off.x), sc.unit_den.x), F_DIV(F_SUB(p.y, sc.unit_off.y), sc.unit_den.y),
-                        F_DIV(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z));
+        u = make_float3(div_rn_by(F_SUB(p.x, sc.unit_off.x), sc.unit_den.x, sc.unit_rcp.x),
+                        div_rn_by(F_SUB(p.y, sc.unit_off.y), sc.unit_den.y, sc.unit_rcp.y),
+                        div_rn_by(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z, sc.unit_rcp.z));
     const float ax = F_SUB(u.x, 0.5f), ay = F_SUB(u.y, 0.5f), az = F_SUB(u.z, 0.5f);
     const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
     if (!(mx <= 3.0e38f)) return false; /* NaN / inf positions never index the grid */
@@ -260,8 +279,9 @@ __device__ __forceinline__ bool occupied_skip(const DevScene &sc, const uint8_t 
     const float3 p = at(o, d, t);
     float3 u = p;
     if (!sc.normalized)
-        u = make_float3(F_DIV(F_SUB(p.x, sc.unit_off.x), sc.unit_den.x), F_DIV(F_SUB(p.y, sc.unit_off.y), sc.unit_den.y),
-                        F_DIV(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z));
+        u = make_float3(div_rn_by(F_SUB(p.x, sc.unit_off.x), sc.unit_den.x, sc.unit_rcp.x),
+                        div_rn_by(F_SUB(p.y, sc.unit_off.y), sc.unit_den.y, sc.unit_rcp.y),
+                        div_rn_by(F_SUB(p.z, sc.unit_off.z), sc.unit_den.z, sc.unit_rcp.z));
     const float ax = F_SUB(u.x, 0.5f), ay = F_SUB(u.y, 0.5f), az = F_SUB(u.z, 0.5f);
     const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
     t_free = -1e30f;
@@ -302,18 +322,22 @@ __device__ __forceinline__ bool occupied_skip(const DevScene &sc, const uint8_t 
 __device__ __forceinline__ float3 contract(const DevScene &sc, float3 p)
 {
     if (sc.contraction == 1)
-        return make_float3(F_DIV(F_SUB(p.x, sc.aabb_from.x), sc.aabb_den.x), F_DIV(F_SUB(p.y, sc.aabb_from.y), sc.aabb_den.y),
-                           F_DIV(F_SUB(p.z, sc.aabb_from.z), sc.aabb_den.z));
+        return make_float3(div_rn_by(F_SUB(p.x, sc.aabb_from.x), sc.aabb_den.x, sc.aabb_rcp.x),
+                           div_rn_by(F_SUB(p.y, sc.aabb_from.y), sc.aabb_den.y, sc.aabb_rcp.y),
+                           div_rn_by(F_SUB(p.z, sc.aabb_from.z), sc.aabb_den.z, sc.aabb_rcp.z));
     if (sc.contraction == 2 || sc.contraction == 3) {
-        const float ux = F_SUB(F_MUL(F_DIV(F_SUB(p.x, sc.c_from.x), sc.c_den.x), 2.0f), 1.0f);
-        const float uy = F_SUB(F_MUL(F_DIV(F_SUB(p.y, sc.c_from.y), sc.c_den.y), 2.0f), 1.0f);
-        const float uz = F_SUB(F_MUL(F_DIV(F_SUB(p.z, sc.c_from.z), sc.c_den.z), 2.0f), 1.0f);
+        const float ux = F_SUB(F_MUL(div_rn_by(F_SUB(p.x, sc.c_from.x), sc.c_den.x, sc.c_rcp.x), 2.0f), 1.0f);
+        const float uy = F_SUB(F_MUL(div_rn_by(F_SUB(p.y, sc.c_from.y), sc.c_den.y, sc.c_rcp.y), 2.0f), 1.0f);
+        const float uz = F_SUB(F_MUL(div_rn_by(F_SUB(p.z, sc.c_from.z), sc.c_den.z, sc.c_rcp.z), 2.0f), 1.0f);
         const float n = sc.contraction == 3 ? fmaxf(fmaxf(fabsf(ux), fabsf(uy)), fabsf(uz))
                                             : F_SQRT(F_ADD(F_ADD(F_MUL(ux, ux), F_MUL(uy, uy)), F_MUL(uz, uz)));
         const float f = fmaxf(n, 1.0f);
-        const float k = F_SUB(2.0f, F_DIV(1.0f, f));
-        return make_float3(F_ADD(F_DIV(F_MUL(k, F_DIV(ux, f)), 4.0f), 0.5f), F_ADD(F_DIV(F_MUL(k, F_DIV(uy, f)), 4.0f), 0.5f),
-                           F_ADD(F_DIV(F_MUL(k, F_DIV(uz, f)), 4.0f), 0.5f));
+        /* 1 / f is the correctly rounded reciprocal (the IEEE 1.0f / f); / 4 is an exact * 0.25 */
+        const float rf = __frcp_rn(f);
+        const float k = F_SUB(2.0f, rf);
+        return make_float3(F_ADD(F_MUL(F_MUL(k, div_rn_by(ux, f, rf)), 0.25f), 0.5f),
+                           F_ADD(F_MUL(F_MUL(k, div_rn_by(uy, f, rf)), 0.25f), 0.5f),
+                           F_ADD(F_MUL(F_MUL(k, div_rn_by(uz, f, rf)), 0.25f), 0.5f));
     }
     return p;
 }
@@ -322,9 +346,9 @@ __device__ __forceinline__ float3 contract(const DevScene &sc, float3 p)
 __device__ __forceinline__ float3 cam2froxel(float3 c, const DevCam &cam, const DevSteps &st, float &t)
 {
     const float sgn = cam.gl ? -1.f : 1.f;
-    const float z = F_MUL(c.z, sgn);
+    const float z = F_MUL(c.z, sgn), rz = __frcp_rn(z);
     t = F_SQRT(dot3(c, c));
-    return make_float3(F_ADD(F_MUL(F_DIV(c.x, z), cam.fx), cam.px), F_ADD(F_MUL(F_DIV(F_MUL(c.y, sgn), z), cam.fy), cam.py),
+    return make_float3(F_ADD(F_MUL(div_rn_by(c.x, z, rz), cam.fx), cam.px), F_ADD(F_MUL(div_rn_by(F_MUL(c.y, sgn), z, rz), cam.fy), cam.py),
                        F_MUL(F_SUB(step_from_t(st, t), st.near_i), c.z < 0.0f ? -1.0f : 1.0f));
 }
 
@@ -360,10 +384,71 @@ __device__ __forceinline__ float2 f2_lerp(float2 a, float2 b, float t)
  * Levels are processed in groups of LG: the 8*LG corner loads of a group are
  * all issued before any of them is consumed, so a thread keeps 8*LG gathers
  * in flight instead of 8. */
+/* the 4-feature grid (instant-ngp's 8 levels x 4 features): an entry is two
+ * half2 (one 8-byte gather per corner), the level's features go to
+ * out[2l], out[2l + 1]; levels in groups of LG / 2 */
+template <int LG>
+__device__ __forceinline__ void hash_encode_levels_f4(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out,
+                                                      int l_begin, int l_end)
+{
+    constexpr int G = LG / 2 > 0 ? LG / 2 : 1;
+    for (int l0 = l_begin; l0 < l_end; l0 += G) {
+        uint2 v[G][8];
+        float wx[G], wy[G], wz[G];
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            const int l = l0 + j;
+            const float sc = g.scale[l];
+            const float px = __fmaf_rn(sc, pos.x, 0.5f), py = __fmaf_rn(sc, pos.y, 0.5f), pz = __fmaf_rn(sc, pos.z, 0.5f);
+            const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+            const uint32_t gx = (uint32_t)(int)fx, gy = (uint32_t)(int)fy, gz = (uint32_t)(int)fz;
+            wx[j] = __fsub_rn(px, fx); wy[j] = __fsub_rn(py, fy); wz[j] = __fsub_rn(pz, fz);
+            const uint32_t size = g.size[l];
+            const uint2 *tl = reinterpret_cast<const uint2 *>(table + g.offset[l]);
+            if ((g.dense_mask >> l) & 1u) {
+                const uint32_t r = g.res[l], r2 = g.res2[l];
+                const uint32_t b = gx + gy * r + gz * r2;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t i = b + ((c & 1) ? 1u : 0u) + ((c & 2) ? r : 0u) + ((c & 4) ? r2 : 0u);
+                    if (i >= size) i -= size;
+                    v[j][c] = __ldg(tl + i);
+                }
+            } else {
+                const uint32_t hy0 = gy * 2654435761u, hy1 = (gy + 1u) * 2654435761u;
+                const uint32_t hz0 = gz * 805459861u, hz1 = (gz + 1u) * 805459861u;
+                const uint32_t m = size - 1u;
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    v[j][c] = __ldg(tl + (((gx + ((c & 1) ? 1u : 0u)) ^ ((c & 2) ? hy1 : hy0) ^ ((c & 4) ? hz1 : hz0)) & m));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) { /* features 0-1, then 2-3 */
+                float2 e[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t a = h ? v[j][2 * k].y : v[j][2 * k].x, b = h ? v[j][2 * k + 1].y : v[j][2 * k + 1].x;
+                    e[k] = f2_lerp(__half22float2(*reinterpret_cast<const __half2 *>(&a)),
+                                   __half22float2(*reinterpret_cast<const __half2 *>(&b)), wx[j]);
+                }
+                const float2 g0 = f2_lerp(e[0], e[1], wy[j]), g1 = f2_lerp(e[2], e[3], wy[j]);
+                out[2 * (l0 + j) + h] = __float22half2_rn(f2_lerp(g0, g1, wz[j]));
+            }
+        }
+    }
+}
+
 template <int LG = 4>
 __device__ __forceinline__ void hash_encode_levels(const DevGrid &g, const __half2 *__restrict__ table, float3 pos, __half2 *out,
                                                    int l_begin, int l_end)
 {
+    if (g.F == 4) {
+        hash_encode_levels_f4<LG>(g, table, pos, out, l_begin, l_end);
+        return;
+    }
     for (int l0 = l_begin; l0 < l_end; l0 += LG) {
         __half2 v[LG][8];
         float wx[LG], wy[LG], wz[LG];

@@ -424,6 +424,7 @@ __global__ void pr_reserve_kernel(PerRayFillParams p);
 __global__ void pr_zero_kernel(PerRayFillParams p);
 __global__ void pr_write_kernel(PerRayFillParams p, int it);
 cudaError_t launch_fill_march(const RenderParams &p, int it, int n_sms, cudaStream_t s);
+cudaError_t launch_div_selftest(const float *x, const float *d, int n, float *q, float *ieee);
 cudaError_t launch_wait_selftest(long long limit_cycles, long long *d_out, cudaStream_t s);
 cudaError_t launch_fill_raygen(const RenderParams &p, cudaStream_t s);
 

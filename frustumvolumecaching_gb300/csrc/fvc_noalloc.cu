@@ -146,7 +146,7 @@ extern "C" int fvc_render_noalloc(fvc_model *m, const fvc_raymarch_info *info, c
     p.stats = stats;
     p.row_capacity = (int)cap;
     p.steps_per_iter = 64;
-    p.skip_empty = 1;
+    p.skip_empty = 0;
     p.results = out ? (float4 *)out->results : nullptr;
     p.image = out ? (uchar4 *)out->image_rgba8 : nullptr;
     p.ray_counts = out ? (int4 *)out->ray_counts : nullptr;

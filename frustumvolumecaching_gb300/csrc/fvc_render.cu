@@ -740,7 +740,7 @@ __device__ __forceinline__ void store_logits(__half *tile, const float (&lo)[2][
 __device__ __forceinline__ float3 dir01_of(const RayState *states, int slot)
 {
     const float4 d = states[slot].dt;
-    return make_float3(F_DIV(F_ADD(d.x, 1.0f), 2.0f), F_DIV(F_ADD(d.y, 1.0f), 2.0f), F_DIV(F_ADD(d.z, 1.0f), 2.0f));
+    return make_float3(F_MUL(F_ADD(d.x, 1.0f), 0.5f), F_MUL(F_ADD(d.y, 1.0f), 0.5f), F_MUL(F_ADD(d.z, 1.0f), 0.5f)); /* / 2, exact */
 }
 
 /* Network over the resample rows (all rows of the plain renderer). */
@@ -1179,8 +1179,10 @@ __global__ void __launch_bounds__(tcm_threads<MT>(), tcm_ctas_per_sm<MT>()) wf_n
     const uint32_t tmem = S.tmem_base;
     const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (MT == 256 && tid >= 128 ? 64u : 0u);
     const RayState *states = p.states[it & 1];
-    /* levels of the lower half-warp (M = 64): a multiple of 4, so each half writes whole 8-value chunks */
+    /* levels of the lower half-warp (M = 64): a multiple of 4, so each half writes whole 8-value chunks
+     * (chunk c holds features 8c..8c+7: levels 4c..4c+3 of 2 features, 2c..2c+1 of 4) */
     const int l_split = 4 * ((p.grid.n_levels + 7) / 8);
+    const int c_split = l_split * p.grid.F / 8;
     uint32_t phase = 0;
     bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
     phase ^= 1u;
@@ -1199,7 +1201,7 @@ __global__ void __launch_bounds__(tcm_threads<MT>(), tcm_ctas_per_sm<MT>()) wf_n
             else hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
         }
         if (MT == 64) {
-            const int c0 = upper ? l_split / 4 : 0, c1 = upper ? 4 : l_split / 4;
+            const int c0 = upper ? c_split : 0, c1 = upper ? 4 : c_split;
 #pragma unroll
             for (int c = 0; c < 4; ++c)
                 if (c >= c0 && c < c1) st_chunk(S.X, trow, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
@@ -1958,6 +1960,22 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     }
     if (n_iter) *n_iter = it;
     return cudaGetLastError();
+}
+
+/* Self-test of the exact division (div_rn_by with the correctly rounded
+ * reciprocal) against the hardware IEEE division, element by element. */
+__global__ void div_selftest_kernel(const float *x, const float *d, int n, float *q, float *ieee)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    q[i] = div_rn_by(x[i], d[i], __frcp_rn(d[i]));
+    ieee[i] = __fdiv_rn(x[i], d[i]);
+}
+
+cudaError_t launch_div_selftest(const float *x, const float *d, int n, float *q, float *ieee)
+{
+    div_selftest_kernel<<<(n + 255) / 256, 256>>>(x, d, n, q, ieee);
+    return cudaDeviceSynchronize();
 }
 
 /* Self-test of the bounded device wait: one warp waits on an mbarrier that

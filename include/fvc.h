@@ -224,6 +224,10 @@ int fvc_model_info(const fvc_model *m, fvc_scene_info *scene, fvc_stepsize_info 
  * same wait (about 1 s) and report a run-out through the render guard. */
 int fvc_debug_fail_allocation(long long n);
 int fvc_selftest_wait_timeout(double limit_ms, double *waited_ms);
+/* The kernels' exact division by a known denominator (Markstein's
+ * correction of x * RN(1/d)) and the hardware IEEE division on n host pairs:
+ * q[i] and q_ieee[i], for the tests that check they agree bit for bit. */
+int fvc_selftest_division(const float *x, const float *d, int n, float *q, float *q_ieee);
 /* StepsizeInfo::setAdditionalInfo (include/common.h:109-131): fills the
  * derived fields (dt_min/max, t_min/max, i_min/max, log1p_c, near_i) from
  * cone_angle, stepsize, near and far for the scene's grid.  Used by
@@ -333,12 +337,15 @@ int fvc_renderer_set_tiling(fvc_renderer *r, int m_tile, int batch_rows);
  * are the same bit for bit; the switch is for measurement. */
 int fvc_renderer_set_fused_classify(fvc_renderer *r, int on);
 
-/* Empty-space skipping in the renderers' march: 1 (the default) looks the
- * occupancy grid up once per empty cell and steps through the rest of the
- * cell without lookups (a DDA bound on the cell's extent along the ray, as
- * grid_occupied_at's t_dist_to_next_voxel, include/raymarch_common.h:712-744,
- * kept a margin inside the cell so every step and occupancy decision is the
- * plain march's); 0 looks up every step.  Results are identical. */
+/* Empty-space skipping in the renderers' march: 1 looks the occupancy grid
+ * up once per empty cell at least four steps long and steps through the rest
+ * of the cell without lookups (a DDA bound on the cell's extent along the
+ * ray, as grid_occupied_at's t_dist_to_next_voxel,
+ * include/raymarch_common.h:712-744, kept a margin inside the cell so every
+ * step and occupancy decision is the plain march's); 0 (the default) looks up
+ * every step.  Results are identical; on GB300 the skip measured slower
+ * (the 32 rays of a warp seldom skip the same steps, so the lookups still
+ * issue while the bound costs extra). */
 int fvc_renderer_set_empty_space_skipping(fvc_renderer *r, int on);
 
 /* MLP precision of the plain renderers on the tcgen05 path (no counterpart

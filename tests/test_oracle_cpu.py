@@ -87,3 +87,18 @@ def test_view_dependent_network_matches_numpy_fp16_path():
     got = o.inference(pos, d01)
     np.testing.assert_allclose(got[:, :3], ref, atol=1e-3)
     np.testing.assert_allclose(got[:, 3], bo[:, 0], atol=1e-12)
+
+
+def test_four_feature_hash_encoding_matches_numpy():
+    """The 8-level x 4-feature grid (instant-ngp's default): the oracle's
+    encoding against the numpy restatement, features level-major."""
+    import dataclasses
+    spec = dataclasses.replace(fmodel.spec_tiny(seed=41), name="tiny41_f4", n_levels=8, F=4, per_level_scale=2.0)
+    o = orc.OracleModel(fmodel.ensure_model(spec))
+    sm = fmodel.SyntheticModel(spec)
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0, 1, size=(2000, 3)).astype(np.float32)
+    ref = fmodel.hash_encode(pos, sm.table.astype(np.float64), o.levels, F=4)
+    got = o.hash_encode(pos)[:, :32]
+    assert ref.shape == (2000, 32)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9)
