@@ -34,7 +34,7 @@ def main(argv=None) -> None:
     ap.add_argument("--rays", type=int, default=1 << 16, help="rays per backward step")
     ap.add_argument("--tile", type=int, choices=[64, 128, 256], default=128, help="tcgen05 network tile height (plain path)")
     ap.add_argument("--batch-rows", type=int, default=0, help="compaction batch, rows per sub-iteration (0: capacity)")
-    ap.add_argument("--no-skip", action="store_true", help="occupancy lookup at every step (no empty-space skipping)")
+    ap.add_argument("--skip", action="store_true", help="empty-space skipping in the march (off by default, as in the library)")
     ap.add_argument("--scene", choices=["c2", "c1"], default="c2",
                     help="c2: the cached workload's scene and camera path; c1: the 256x256 workload's scene, seeded camera")
     ap.add_argument("--separate-classify", action="store_true",
@@ -63,7 +63,7 @@ def main(argv=None) -> None:
     r.resizeRenderbuffers((W, H))
     r.set_network_path(args.network == "tc")
     r.set_tiling(args.tile, args.batch_rows)
-    r.set_empty_space_skipping(not args.no_skip)
+    r.set_empty_space_skipping(args.skip)
     if args.path == "cached":
         r.set_fused_classify(not args.separate_classify)
     r.set_kernel_timing(True)

@@ -21,6 +21,7 @@ import pytest
 import frustumvolumecaching_gb300 as fvc
 from frustumvolumecaching_gb300 import _lib as L
 from frustumvolumecaching_gb300 import camera as fcam
+from frustumvolumecaching_gb300 import model as fmodel
 from oracle import ingp as oingp
 from tests.ingp_fixture import density_grid, ingp_model, make_snapshot, pack, write_snapshot
 
@@ -164,3 +165,21 @@ def test_snapshot_renders_like_its_export_and_the_oracle(tmp_path):
     with pytest.raises(fvc._lib.FvcError) as e:
         rc.initCacheBlockwise(fvc.raymarch_info(cam_c, a.stepsize_info))
     assert e.value.code == 2 and "8 latents" in str(e.value)
+
+
+def test_eight_level_four_feature_grid_exports_like_the_oracle(tmp_path):
+    """instant-ngp's default grid (8 levels x 4 features): the snapshot's
+    parameter split and export match the oracle's restatement."""
+    import dataclasses
+    spec, wb, wh, _, occ = ingp_model(51, 2)
+    spec = dataclasses.replace(spec, name="ingp_like51_f4", n_levels=8, F=4,
+                               per_level_scale=float((2048.0 * 2 / 16.0) ** (1.0 / 7.0)))
+    tab = fmodel.SyntheticModel(spec).table.ravel().view(np.uint16)
+    dens = density_grid(occ, 2, 52)
+    snap = write_snapshot(tmp_path / "f4.ingp", 2, np.concatenate([wb, wh, tab]), dens, n_levels=8, n_features=4)
+    fvc.ingp_export(snap, tmp_path / "lib")
+    cfg = oingp.snapshot_to_export(snap, str(tmp_path / "orc"))
+    _same_export(tmp_path / "lib", tmp_path / "orc")
+    enc = cfg["mlp_base"]["encoding"]
+    assert enc["n_levels"] == 8 and enc["n_features_per_level"] == 4
+    assert os.path.getsize(tmp_path / "lib" / "pos_enc.dat") == tab.size * 2
