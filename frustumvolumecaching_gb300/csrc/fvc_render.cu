@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
             __half2 feat[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
-            uint32_t hin[8];
+            uint32_t hin[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
             if (r >= 0) {
                 const float4 pw = MODE == 2 && kind == KIND_CACHE ? make_float4(0.f, 0.f, 0.f, 0.f) : p.row_pay[r];
                 if (MODE == 2 && kind == KIND_CACHE) {
@@ -1010,22 +1010,26 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
                     hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
                 }
             }
+            /* MODE 2: a tile without resample rows skips the density layers (block-uniform vote) */
+            const bool dense = MODE != 2 || __syncthreads_or(r >= 0 && kind == KIND_RESAMPLE);
+            uint4 b0 = make_uint4(hin[0], hin[1], hin[2], hin[3]), b1 = make_uint4(hin[4], hin[5], hin[6], hin[7]);
+            if (dense) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
-            if (!(ok = tc_publish(ok))) break;
-            /* ---- layer 1: 32 -> 64, ReLU ---- */
-            ok = tc_run(S, tmem, S.W + TC_B1, 32, 64, phase);
-            epi_hidden(tmem + lane_base, nullptr, S.X, tid);
-            if (!(ok = tc_publish(ok))) break;
-            /* ---- layer 2: 64 -> 16 (log-density, latents) ---- */
-            ok = tc_run(S, tmem, S.W + TC_B2, 64, 16, phase);
-            float v[16];
-            tmem_ld16(tmem + lane_base, v);
-            tmem_wait_ld();
-            uint4 b0 = pack8(v), b1 = pack8(v + 8);
-            if (MODE == 2 && kind == KIND_CACHE) {
-                b0 = make_uint4(hin[0], hin[1], hin[2], hin[3]);
-                b1 = make_uint4(hin[4], hin[5], hin[6], hin[7]);
+                for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
+                if (!(ok = tc_publish(ok))) break;
+                /* ---- layer 1: 32 -> 64, ReLU ---- */
+                ok = tc_run(S, tmem, S.W + TC_B1, 32, 64, phase);
+                epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+                if (!(ok = tc_publish(ok))) break;
+                /* ---- layer 2: 64 -> 16 (log-density, latents) ---- */
+                ok = tc_run(S, tmem, S.W + TC_B2, 64, 16, phase);
+                float v[16];
+                tmem_ld16(tmem + lane_base, v);
+                tmem_wait_ld();
+                if (!(MODE == 2 && kind == KIND_CACHE)) {
+                    b0 = pack8(v);
+                    b1 = pack8(v + 8);
+                }
             }
             log_density = (uint16_t)(b0.x & 0xffffu);
             st_chunk(S.X, tid, 0, 32, b0);
