@@ -335,7 +335,7 @@ def run_batch_bench(args, torch, dev, stream) -> dict:
             "gpu_launches": st.n_launches, "host_launches_per_batch": 1,
             "autotune": {"m_tile": tuned.m_tile, "compaction_batch": tuned.batch_rows, "steps_per_iter": tuned.steps_per_iter,
                          "rows_per_iteration": tuned.rows_per_iteration, "ms": tuned.ms, "candidates": tuned.n_candidates,
-                         "space": "M-tile {64, 128, 256} tcgen05 + 32 mma.sync x compaction batch {2^16..2^20, 2^22, 2^24}",
+                         "space": "M-tile {64, 128, 256} tcgen05 + 32 mma.sync x compaction batch {2^16..2^20, 2^22, 2^24} x march steps {16, 64}",
                          "tuned_on_views": BATCH_TUNE_VIEWS},
             "workload": "c4: 64 views of the config-1 scene, resolutions uniform over 320x240..1920x1080, plain render"}
 

@@ -2215,18 +2215,21 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
      * fixed cost - every alive ray's state moved once - dominates) */
     const int tiles[4] = {64, 128, 256, 32};
     const int batches[7] = {1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20, 1 << 22, 1 << 24};
-    const int saved_tc = r->use_tc, saved_tile = r->m_tile, saved_target = r->row_target;
+    const int march_steps[2] = {16, 64}; /* marching steps per ray and sub-iteration */
+    const int saved_tc = r->use_tc, saved_tile = r->m_tile, saved_target = r->row_target, saved_steps = r->steps_per_iter;
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
     float best = 1e30f;
-    int best_tile = 0, best_batch = 0, n_cand = 0, rc = FVC_OK;
+    int best_tile = 0, best_batch = 0, best_steps = 0, n_cand = 0, rc = FVC_OK;
     long long best_rows = 0;
     for (int ti = 0; ti < 4 && rc == FVC_OK; ++ti)
-        for (int bi = 0; bi < 7 && rc == FVC_OK; ++bi) {
+        for (int bi = 0; bi < 7 && rc == FVC_OK; ++bi)
+        for (int si = 0; si < 2 && rc == FVC_OK; ++si) {
             r->use_tc = tiles[ti] != 32;
             r->m_tile = tiles[ti] == 32 ? 128 : tiles[ti];
             r->row_target = batches[bi];
+            r->steps_per_iter = march_steps[si];
             RenderParams p;
             int n_rays = 0;
             if ((rc = batch_setup(r, infos, n_views, out, p, n_rays))) break;
@@ -2247,20 +2250,22 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
                 best = ms;
                 best_tile = tiles[ti];
                 best_batch = batches[bi];
+                best_steps = march_steps[si];
                 best_rows = (long long)st.n_samples / std::max(1, iters);
             }
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) {
-        r->use_tc = saved_tc; r->m_tile = saved_tile; r->row_target = saved_target;
+        r->use_tc = saved_tc; r->m_tile = saved_tile; r->row_target = saved_target; r->steps_per_iter = saved_steps;
         return rc;
     }
     r->use_tc = best_tile != 32;
     r->m_tile = best_tile == 32 ? 128 : best_tile;
     r->row_target = best_batch;
+    r->steps_per_iter = best_steps;
     res->m_tile = best_tile;
-    res->steps_per_iter = r->steps_per_iter;
+    res->steps_per_iter = best_steps;
     res->rows_per_iteration = best_rows;
     res->ms = best;
     res->n_candidates = n_cand;

@@ -475,8 +475,9 @@ int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info *infos, int
  * or 32-row mma.sync warp tiles) with each compaction batch (2^16..2^20,
  * 2^22 and 2^24 rows per sub-iteration: a ray takes
  * clamp(batch / alive rays, 1, 16) samples a sub-iteration,
- * n_steps_curr_subiter of src/performance_renderer.cu:249) on this batch of
- * views, 28 candidates in all, and keeps the fastest for the renderer. */
+ * n_steps_curr_subiter of src/performance_renderer.cu:249) and each march
+ * length (16 or 64 steps per ray and sub-iteration) on this batch of views,
+ * 56 candidates in all, and keeps the fastest for the renderer. */
 typedef struct {
     int m_tile;                  /* rows per network tile of the winner (32: the mma.sync path) */
     int steps_per_iter;          /* marching steps per ray and sub-iteration */

@@ -85,7 +85,8 @@ def test_autotune_picks_a_valid_configuration():
     r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
     cams = _views(1400)
     res, cnt, img, tuned = _batch(torch, r, loader, cams, tune=True)
-    assert tuned.n_candidates == 28  # tiles {64, 128, 256, mma.sync 32} x batches 2^16..2^20, 2^22, 2^24
+    assert tuned.n_candidates == 56  # tiles {64, 128, 256, mma.sync 32} x batches 2^16..2^20, 2^22, 2^24 x steps {16, 64}
+    assert tuned.steps_per_iter in (16, 64)
     assert tuned.m_tile in (32, 64, 128, 256) and tuned.batch_rows in [1 << k for k in (16, 17, 18, 19, 20, 22, 24)]
     assert tuned.ms > 0 and tuned.rows_per_iteration > 0
     # the batch ran with the winner's network path: compare with single views on the same path
