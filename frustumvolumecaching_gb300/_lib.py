@@ -160,6 +160,7 @@ SIGNATURES = {
     "fvc_render_batch": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs)]),
     "fvc_render_batch_cached": (c_int, [P, C.POINTER(RaymarchInfo), c_int, PP, C.POINTER(RenderOutputs)]),
     "fvc_renderer_autotune": (c_int, [P, C.POINTER(RaymarchInfo), c_int, C.POINTER(RenderOutputs), C.POINTER(AutotuneResult)]),
+    "fvc_renderer_set_autotune_space": (c_int, [P, C.POINTER(c_int), c_int, C.POINTER(c_int), c_int, C.POINTER(c_int), c_int]),
     "fvc_model_properties": (c_int, [P, C.POINTER(ModelProps)]),
     "fvc_renderer_synchronize": (c_int, [P]),
     "fvc_grad_create": (c_int, [P, PP]),

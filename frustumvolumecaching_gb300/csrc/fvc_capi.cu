@@ -433,6 +433,11 @@ struct fvc_renderer {
     bool last_was_graph = false;
     int steps_per_iter = 64;          /* marching steps per sub-iteration */
     int m_tile = 128;                 /* tcgen05 network tile of the plain path (autotuned) */
+    /* the autotuner's candidates (fvc_renderer_set_autotune_space); the default is the batched workload's
+     * stated space: tcgen05 tiles {64, 128, 256} x compaction batches 2^16..2^20, march lengths 16 and 64 */
+    std::vector<int> tune_tiles{64, 128, 256};
+    std::vector<int> tune_batches{1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20};
+    std::vector<int> tune_steps{16, 64};
     int row_target = 0;               /* compaction batch, rows per sub-iteration (0: the row capacity; autotuned) */
     int fused_classify = 1;           /* cached renders: classification inside the march (see fvc_renderer_set_fused_classify) */
     int skip_empty = 0;               /* empty-space skipping in the march (fvc_renderer_set_empty_space_skipping); off by
@@ -2203,19 +2208,37 @@ extern "C" int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info 
     return batch_launch(r, p, n_rays);
 }
 
+extern "C" int fvc_renderer_set_autotune_space(fvc_renderer *r, const int *m_tiles, int n_tiles, const int *batch_rows, int n_batches,
+                                               const int *march_steps, int n_steps)
+{
+    CHECK_ARG(r && m_tiles && batch_rows && march_steps && n_tiles > 0 && n_tiles <= 16 && n_batches > 0 && n_batches <= 16 &&
+                  n_steps > 0 && n_steps <= 16,
+              "fvc_renderer_set_autotune_space: null argument or a list of 0 or more than 16 candidates");
+    for (int i = 0; i < n_tiles; ++i)
+        CHECK_ARG(m_tiles[i] == 32 || m_tiles[i] == 64 || m_tiles[i] == 128 || m_tiles[i] == 256,
+                  "fvc_renderer_set_autotune_space: tiles must be 32 (mma.sync), 64, 128 or 256");
+    for (int i = 0; i < n_batches; ++i)
+        CHECK_ARG(batch_rows[i] >= 1024 && batch_rows[i] <= (1 << 26), "fvc_renderer_set_autotune_space: batches must lie in [2^10, 2^26]");
+    for (int i = 0; i < n_steps; ++i)
+        CHECK_ARG(march_steps[i] >= 4 && march_steps[i] <= 1024 && march_steps[i] % 4 == 0,
+                  "fvc_renderer_set_autotune_space: march lengths must be multiples of 4 in [4, 1024]");
+    std::lock_guard<std::mutex> lk(r->read_mutex);
+    r->tune_tiles.assign(m_tiles, m_tiles + n_tiles);
+    r->tune_batches.assign(batch_rows, batch_rows + n_batches);
+    r->tune_steps.assign(march_steps, march_steps + n_steps);
+    return FVC_OK;
+}
+
 extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
                                      fvc_autotune_result *res)
 {
     CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
     if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
     std::lock_guard<std::mutex> lk(r->read_mutex);
-    /* candidates: the tcgen05 tile heights and the 32-row mma.sync warp tile, each with compaction
-     * batches of 2^16..2^20 rows per sub-iteration and two larger ones (2^22, 2^24: on batches of tens of
-     * millions of rays a small batch leaves one sample per ray and sub-iteration, and the sub-iterations'
-     * fixed cost - every alive ray's state moved once - dominates) */
-    const int tiles[4] = {64, 128, 256, 32};
-    const int batches[7] = {1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20, 1 << 22, 1 << 24};
-    const int march_steps[2] = {16, 64}; /* marching steps per ray and sub-iteration */
+    /* candidates: the space set by fvc_renderer_set_autotune_space (tile heights, 32 = the mma.sync warp
+     * tile; compaction batches; march lengths), every combination */
+    const std::vector<int> tiles = r->tune_tiles, batches = r->tune_batches, march_steps = r->tune_steps;
+    const int n_ti = (int)tiles.size(), n_bi = (int)batches.size(), n_si = (int)march_steps.size();
     const int saved_tc = r->use_tc, saved_tile = r->m_tile, saved_target = r->row_target, saved_steps = r->steps_per_iter;
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
@@ -2223,9 +2246,9 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
     float best = 1e30f;
     int best_tile = 0, best_batch = 0, best_steps = 0, n_cand = 0, rc = FVC_OK;
     long long best_rows = 0;
-    for (int ti = 0; ti < 4 && rc == FVC_OK; ++ti)
-        for (int bi = 0; bi < 7 && rc == FVC_OK; ++bi)
-        for (int si = 0; si < 2 && rc == FVC_OK; ++si) {
+    for (int ti = 0; ti < n_ti && rc == FVC_OK; ++ti)
+        for (int bi = 0; bi < n_bi && rc == FVC_OK; ++bi)
+        for (int si = 0; si < n_si && rc == FVC_OK; ++si) {
             r->use_tc = tiles[ti] != 32;
             r->m_tile = tiles[ti] == 32 ? 128 : tiles[ti];
             r->row_target = batches[bi];

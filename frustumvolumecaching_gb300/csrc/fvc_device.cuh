@@ -219,23 +219,36 @@ __device__ __forceinline__ void transform_ray(const float *m, float3 o, float3 d
 /* --------------------------------------------------------------------- */
 /* occupancy grid (grid_occupied_at<128, true>, include/raymarch_common.h:660-710) */
 /* --------------------------------------------------------------------- */
+/* morton3D's bit spreading (include/raymarch_common.h:98-110) for the cell
+ * indices this grid produces, 0..128: for inputs below 256 the 10-bit
+ * spreading's first step (v * 0x00010001 & 0xFF0000FF) is the identity, so
+ * the three remaining steps give the same bits. */
 __device__ __forceinline__ uint32_t expand_bits3(uint32_t v)
 {
-    v = (v * 0x00010001u) & 0xFF0000FFu;
     v = (v * 0x00000101u) & 0x0F00F00Fu;
     v = (v * 0x00000011u) & 0xC30C30C3u;
     v = (v * 0x00000005u) & 0x49249249u;
     return v;
 }
 
-__device__ __forceinline__ int frexp_exponent(float m)
+/* mip_from_unit's cascade of a point whose largest offset from the grid
+ * centre is mx (finite, >= 0): max(0, frexp exponent of mx + 1), read from
+ * the exponent field.  A zero or subnormal mx reads -126 (its frexp exponent
+ * is at most -126) and gives mip 0 like frexpf. */
+__device__ __forceinline__ int mip_of(float mx)
 {
-    const uint32_t b = __float_as_uint(m);
-    const int be = (int)((b >> 23) & 0xffu);
-    if (be != 0 && be != 0xff) return be - 126;  /* normal: m = f*2^e, f in [0.5,1) */
-    int e;
-    frexpf(m, &e);
-    return e;
+    return max(0, (int)(__float_as_uint(mx) >> 23) - 125);
+}
+
+/* Cell index along one axis at cascade mip, for a = unit coordinate - 1/2
+ * with |a| < 2^(mip-1): (int)((a * 2^-mip + 1/2) * 128) as the reference
+ * evaluates it, rounded once.  a * 2^-mip and the final * 128 are exact
+ * (powers of two), and rounding commutes with a power-of-two scale away from
+ * overflow and underflow, so RN(a 2^-mip + 1/2) * 128 = RN(a 2^(7-mip) + 64),
+ * one fused multiply-add with the same bits.  The result lies in [0, 128]. */
+__device__ __forceinline__ int cell_of(float a, int mip)
+{
+    return (int)__fmaf_rn(a, __int_as_float((134 - mip) << 23), 64.0f);
 }
 
 __device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__restrict__ bits, float3 p)
@@ -248,12 +261,9 @@ __device__ __forceinline__ bool occupied(const DevScene &sc, const uint8_t *__re
     const float ax = F_SUB(u.x, 0.5f), ay = F_SUB(u.y, 0.5f), az = F_SUB(u.z, 0.5f);
     const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
     if (!(mx <= 3.0e38f)) return false; /* NaN / inf positions never index the grid */
-    const int mip = max(0, frexp_exponent(mx) + 1);
+    const int mip = mip_of(mx);
     if (mip >= sc.nlvl) return false;
-    const float sm = __int_as_float((127 - mip) << 23); /* scalbnf(1, -mip) */
-    const int ix = (int)F_MUL(F_ADD(F_MUL(ax, sm), 0.5f), 128.0f);
-    const int iy = (int)F_MUL(F_ADD(F_MUL(ay, sm), 0.5f), 128.0f);
-    const int iz = (int)F_MUL(F_ADD(F_MUL(az, sm), 0.5f), 128.0f);
+    const int ix = cell_of(ax, mip), iy = cell_of(ay, mip), iz = cell_of(az, mip);
     const uint32_t idx = expand_bits3((uint32_t)ix) | (expand_bits3((uint32_t)iy) << 1) | (expand_bits3((uint32_t)iz) << 2);
     const uint32_t bidx = idx / 8u + (uint32_t)((128 * 128 * 128 / 8) * mip);
     return (__ldg(bits + bidx) >> (idx & 7u)) & 1u;
@@ -286,12 +296,9 @@ __device__ __forceinline__ bool occupied_skip(const DevScene &sc, const uint8_t 
     const float mx = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fabsf(az));
     t_free = -1e30f;
     if (!(mx <= 3.0e38f)) return false;
-    const int mip = max(0, frexp_exponent(mx) + 1);
+    const int mip = mip_of(mx);
     if (mip >= sc.nlvl) return false;
-    const float sm = __int_as_float((127 - mip) << 23);
-    const int ix = (int)F_MUL(F_ADD(F_MUL(ax, sm), 0.5f), 128.0f);
-    const int iy = (int)F_MUL(F_ADD(F_MUL(ay, sm), 0.5f), 128.0f);
-    const int iz = (int)F_MUL(F_ADD(F_MUL(az, sm), 0.5f), 128.0f);
+    const int ix = cell_of(ax, mip), iy = cell_of(ay, mip), iz = cell_of(az, mip);
     const uint32_t idx = expand_bits3((uint32_t)ix) | (expand_bits3((uint32_t)iy) << 1) | (expand_bits3((uint32_t)iz) << 2);
     const uint32_t bidx = idx / 8u + (uint32_t)((128 * 128 * 128 / 8) * mip);
     if ((__ldg(bits + bidx) >> (idx & 7u)) & 1u) return true;

@@ -478,6 +478,7 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
         }
         const int rbase = warp_alloc(p.counters + 2, n);
         int n_res = 0, n_hit = 0;
+        uint32_t kinds = 0; /* FUSED: 2 bits per row, its kind */
         if (FUSED && valid) {
             /* the cached renderer's classification of this ray's rows (wf_classify_kernel's
              * non-basic form), with the ray moved into the cache camera once per ray */
@@ -510,13 +511,17 @@ __global__ void __launch_bounds__(128) wf_march_kernel(RenderParams p, int it)
                 p.row_slot[rbase + s] = i;
                 p.row_pay[rbase + s] = pay;
                 p.row_kind[rbase + s] = (uint8_t)code;
+                kinds |= (uint32_t)kind << (2 * s);
             }
         }
         if (FUSED) {
-            const int wr = __reduce_add_sync(FULLMASK, n_res), wh = __reduce_add_sync(FULLMASK, n_hit);
-            if (lane_id() == 0) {
-                if (wr) atomicAdd(p.counters + 3, wr);
-                if (wh) atomicAdd(p.counters + 4, wh);
+            /* the resample rows and the cache rows each go to a list, so that the network's tiles hold one
+             * kind of row: a cache row never waits on its tile's hash gathers */
+            int rb = warp_alloc(p.counters + 3, n_res), hb = warp_alloc(p.counters + 4, n_hit);
+            for (int s = 0; s < n && (n_res | n_hit); ++s) {
+                const uint32_t kind = (kinds >> (2 * s)) & 3u;
+                if (kind == KIND_RESAMPLE) p.res_list[rb++] = rbase + s;
+                else if (kind == KIND_CACHE) p.cache_list[hb++] = rbase + s;
             }
         }
         if (valid) {
@@ -689,16 +694,16 @@ __global__ void __launch_bounds__(256) wf_classify_kernel(RenderParams p, int it
 
 /* The cache rows' trilinear lookups of a sub-iteration classified in the
  * march (cache_lookup at the froxel point in the row payload), one thread
- * per row, at full occupancy so that many rows' eight corner gathers are in
- * flight at once.  The head input goes to row_lat at the row's own index and
- * its fp16 log-density to the high half of row_out.y, which the network
- * kernel's MODE 2 reads for a cache row. */
+ * per row of the cache list, at full occupancy so that many rows' eight
+ * corner gathers are in flight at once.  The head input goes to row_lat at
+ * the row's own index and its fp16 log-density to the high half of
+ * row_out.y, which the network kernel's MODE 2 reads for a cache row. */
 __global__ void __launch_bounds__(256) wf_cache_lookup_kernel(RenderParams p, int it)
 {
-    const int n_rows = p.counters[2];
+    const int n_rows = p.counters[4];
     const RayState *states = p.states[it & 1];
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
-        if (row_kind_of(p.row_kind[r]) != KIND_CACHE) continue;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_rows; k += gridDim.x * blockDim.x) {
+        const int r = p.cache_list[k];
         const float4 fr = p.row_pay[r];
         float logd, lat[8];
         cache_lookup(row_cache(p, states, r), make_float3(fr.x, fr.y, fr.z), logd, lat);
@@ -952,18 +957,19 @@ __device__ __forceinline__ bool tc_publish(bool ok)
 }
 
 /* MODE 0: resample rows (the list, or all rows of the plain path); MODE 1: the
- * cache list (head only); MODE 2: every row of a cached sub-iteration in row
- * order, classified by the march: a resample row gathers its hash features,
- * and after the density layers a cache row replaces their output with the
- * head input of its lookup (wf_cache_lookup_kernel); dropped and skipped rows
- * ride along as zero rows.  One launch for both streams, no lists. */
+ * cache list (head only); MODE 2: both lists of a cached sub-iteration
+ * classified by the march in one launch, the resample list's tiles first
+ * (hash features, density layers, head), then the cache list's tiles (the
+ * head input of each row's lookup, wf_cache_lookup_kernel; head only), so
+ * that no tile mixes the two kinds of row. */
 template <int MODE, int HH, bool LIST>
 __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(RenderParams p, int it)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
-    const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : MODE == 1 ? p.counters[4] : p.counters[2];
-    if (n_rows == 0) return;
+    const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : MODE == 1 ? p.counters[4] : p.counters[3];
+    const int n_hit = MODE == 2 ? p.counters[4] : 0;
+    if (n_rows == 0 && n_hit == 0) return;
     const int tid = threadIdx.x, warp = tid >> 5;
     /* the weights arrive by one bulk copy on the TMA engine, completing the
      * mbarrier's phase 0; the layers' MMA commits complete the later phases */
@@ -983,14 +989,16 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
     uint32_t phase = 0;
     bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
     phase ^= 1u;
-    const int n_tiles = (n_rows + 127) / 128;
+    const int res_tiles = (n_rows + 127) / 128;
+    const int n_tiles = res_tiles + (n_hit + 127) / 128;
     for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        const int k = tile * 128 + tid;
-        int r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : MODE == 1 ? p.cache_list[k] : k) : -1;
-        int kind = KIND_RESAMPLE;
-        if (MODE == 2 && r >= 0) {
-            kind = row_kind_of(p.row_kind[r]);
-            if (kind >= KIND_DROP) r = -1;
+        int k = tile * 128 + tid, r = -1, kind = KIND_RESAMPLE;
+        if (MODE == 2 && tile >= res_tiles) {
+            k = (tile - res_tiles) * 128 + tid;
+            kind = KIND_CACHE;
+            r = k < n_hit ? p.cache_list[k] : -1;
+        } else {
+            r = k < n_rows ? (MODE == 0 ? (LIST ? p.res_list[k] : k) : MODE == 1 ? p.cache_list[k] : p.res_list[k]) : -1;
         }
         __half2 sh[8];
         uint16_t log_density = 0;
@@ -1010,8 +1018,8 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
                     hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(pw.x, pw.y, pw.z), feat);
                 }
             }
-            /* MODE 2: a tile without resample rows skips the density layers (block-uniform vote) */
-            const bool dense = MODE != 2 || __syncthreads_or(r >= 0 && kind == KIND_RESAMPLE);
+            /* MODE 2: the cache list's tiles skip the density layers (tile is block-uniform) */
+            const bool dense = MODE != 2 || tile < res_tiles;
             uint4 b0 = make_uint4(hin[0], hin[1], hin[2], hin[3]), b1 = make_uint4(hin[4], hin[5], hin[6], hin[7]);
             if (dense) {
 #pragma unroll

@@ -247,6 +247,12 @@ class Renderer:
         handles = (C.c_void_p * len(caches))(*[c.handle.value for c in caches])
         L.check(L.load().fvc_render_batch_cached(self.handle, arr, len(infos), handles, C.byref(out)))
 
+    def set_autotune_space(self, m_tiles, batch_rows, march_steps) -> None:
+        """Candidate network tiles (32 = mma.sync), compaction batches and march lengths of autotune()."""
+        arr = lambda v: (C.c_int * len(v))(*[int(x) for x in v])  # noqa: E731
+        L.check(L.load().fvc_renderer_set_autotune_space(self.handle, arr(m_tiles), len(m_tiles), arr(batch_rows), len(batch_rows),
+                                                         arr(march_steps), len(march_steps)))
+
     def autotune(self, infos, image=None, results=None, ray_counts=None) -> L.AutotuneResult:
         """Pick the network tile and marching batch that render this batch fastest."""
         arr, out = self._batch_args(infos, image, results, ray_counts)

@@ -471,13 +471,15 @@ int fvc_render_batch(fvc_renderer *r, const fvc_raymarch_info *infos, int n_view
 int fvc_render_batch_cached(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, fvc_cache *const *caches,
                             const fvc_render_outputs *out);
 
-/* Times each candidate network tile (tcgen05 tiles of 64, 128 or 256 rows,
- * or 32-row mma.sync warp tiles) with each compaction batch (2^16..2^20,
- * 2^22 and 2^24 rows per sub-iteration: a ray takes
- * clamp(batch / alive rays, 1, 16) samples a sub-iteration,
- * n_steps_curr_subiter of src/performance_renderer.cu:249) and each march
- * length (16 or 64 steps per ray and sub-iteration) on this batch of views,
- * 56 candidates in all, and keeps the fastest for the renderer. */
+/* Times each candidate network tile with each compaction batch (rows per
+ * sub-iteration: a ray takes clamp(batch / alive rays, 1, 16) samples a
+ * sub-iteration, n_steps_curr_subiter of src/performance_renderer.cu:249)
+ * and each march length (steps per ray and sub-iteration) on this batch of
+ * views, and keeps the fastest for the renderer.  The candidates are those
+ * of fvc_renderer_set_autotune_space; by default tcgen05 tiles of 64, 128
+ * and 256 rows x batches of 2^16..2^20 rows x march lengths 16 and 64
+ * (30 candidates).  No counterpart in the reference (TARGET_BATCH_SIZE is a
+ * compile-time constant there). */
 typedef struct {
     int m_tile;                  /* rows per network tile of the winner (32: the mma.sync path) */
     int steps_per_iter;          /* marching steps per ray and sub-iteration */
@@ -489,6 +491,11 @@ typedef struct {
 } fvc_autotune_result;
 int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *infos, int n_views, const fvc_render_outputs *out,
                           fvc_autotune_result *res);
+/* The autotuner's candidate lists (each 1..16 entries): tile heights 64, 128,
+ * 256 (tcgen05) or 32 (the mma.sync warp tile); compaction batches in
+ * [2^10, 2^26] rows; march lengths, multiples of 4 in [4, 1024]. */
+int fvc_renderer_set_autotune_space(fvc_renderer *r, const int *m_tiles, int n_tiles, const int *batch_rows, int n_batches,
+                                    const int *march_steps, int n_steps);
 
 /* ------------------------------------------------------------------------ */
 /* differentiable render (no counterpart in the reference)                   */

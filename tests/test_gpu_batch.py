@@ -85,12 +85,21 @@ def test_autotune_picks_a_valid_configuration():
     r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
     cams = _views(1400)
     res, cnt, img, tuned = _batch(torch, r, loader, cams, tune=True)
-    assert tuned.n_candidates == 56  # tiles {64, 128, 256, mma.sync 32} x batches 2^16..2^20, 2^22, 2^24 x steps {16, 64}
+    # the default space is the batched workload's: tcgen05 tiles {64, 128, 256} x batches 2^16..2^20 x steps {16, 64}
+    assert tuned.n_candidates == 30
     assert tuned.steps_per_iter in (16, 64)
-    assert tuned.m_tile in (32, 64, 128, 256) and tuned.batch_rows in [1 << k for k in (16, 17, 18, 19, 20, 22, 24)]
+    assert tuned.m_tile in (64, 128, 256) and tuned.batch_rows in [1 << k for k in (16, 17, 18, 19, 20)]
     assert tuned.ms > 0 and tuned.rows_per_iteration > 0
+    _check(_single(loader, cams), res, cnt, img)
+    # a space of the caller's: the mma.sync tile and a batch beyond 2^20 are candidates too
+    r.set_autotune_space([32, 128], [1 << 22], [16])
+    res, cnt, img, tuned = _batch(torch, r, loader, cams, tune=True)
+    assert tuned.n_candidates == 2 and tuned.m_tile in (32, 128) and tuned.batch_rows == 1 << 22 and tuned.steps_per_iter == 16
     # the batch ran with the winner's network path: compare with single views on the same path
     _check(_single(loader, cams, tcgen05=tuned.m_tile != 32), res, cnt, img)
+    for bad in (([96], [1 << 16], [16]), ([128], [100], [16]), ([128], [1 << 16], [6]), ([], [1 << 16], [16])):
+        with pytest.raises(RuntimeError):
+            r.set_autotune_space(*bad)
 
 
 TILINGS = [(64, 0), (256, 0), (128, 1 << 16), (64, 1 << 17), (256, 1 << 20), (128, 1024)]
