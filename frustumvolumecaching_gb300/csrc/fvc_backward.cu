@@ -1020,8 +1020,9 @@ __global__ void __launch_bounds__(BW_WARPS * 32, 1) wf_cache_bwd_kernel(RenderPa
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 if (!vp[c]) continue;
-                const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
-                const uint4 lt = __ldg(&vp[c]->lat);
+                float2 di;
+                uint4 lt;
+                ld_voxel(vp[c], di, lt);
                 wsum = fmaf(wc[c], di.y, wsum);
                 const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
 #pragma unroll

@@ -1626,7 +1626,10 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
         CU(cudaMemsetAsync(p.build_row_counter, 0, sizeof(int), s));
         CU(launch_cache_search(p, std::min(n_alive, 1 << 16), s));
         CU(cudaGetLastError());
-        CU(launch_cache_density(p, m->n_sms * 8, s));
+        /* the density network on tcgen05 in the renderer's default network path; the first head of
+         * view-dependent models and the mma.sync path keep the warp-level kernel */
+        if (r->use_tc && !m->view_dependent) CU(launch_cache_density_tc(p, m->d_weights_tc, m->n_sms, s));
+        else CU(launch_cache_density(p, m->n_sms * 8, s));
         CU(cudaGetLastError());
         cache_composite_kernel<<<std::min((n_alive + 3) / 4, 1 << 16), 128, 0, s>>>(p);
         CU(cudaGetLastError());
@@ -1710,7 +1713,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
     memset(&q, 0, sizeof(q));
     q.grid = m->grid; q.table = m->d_table; q.weights = m->d_weights; q.latent_offset = m->latent_offset;
     q.build_rows = p.row_pay; q.build_den = x.den; q.build_lat = x.lat; q.build_row_counter = p.counters + 2;
-    q.view_dependent = m->view_dependent; q.weights_fh = m->d_weights_fh; q.dir_slot = p.row_slot;
+    q.view_dependent = m->view_dependent; q.weights_fh = m->d_weights_fh; q.dir_slot = p.row_slot; q.guard = p.guard;
     cudaStream_t s = r->stream;
     CU(cudaMemsetAsync(x.flag, 0, n_bricks, s));
     CU(cudaMemsetAsync(x.set, 0, n_bricks, s));
@@ -1735,7 +1738,8 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
         CU(cudaMemsetAsync(p.counters + 2, 0, sizeof(int), s));
         CU(launch_fill_march(p, it, n_sms, s));
         q.dir_states = p.states[it & 1];
-        CU(launch_cache_density(q, n_sms * 8, s));
+        if (r->use_tc && !m->view_dependent) CU(launch_cache_density_tc(q, m->d_weights_tc, n_sms, s));
+        else CU(launch_cache_density(q, n_sms * 8, s));
         pr_mark_kernel<<<n_sms * 16, 128, 0, s>>>(f, it);
         pr_count_kernel<<<(int)((n_cols + 255) / 256), 256, 0, s>>>(f);
         pr_scan_kernel<<<1, 1024, 0, s>>>(f);

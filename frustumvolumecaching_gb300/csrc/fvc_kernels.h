@@ -97,6 +97,20 @@ struct __align__(16) Voxel {
     uint4 lat;
 };
 
+/* One voxel's density, isset and latents by a single 32-byte load (one
+ * sector, one load instruction instead of two; voxels sit at 32-byte
+ * multiples of the 256-byte aligned data array).  Read-only path: the data
+ * array does not change while a render reads it. */
+__device__ __forceinline__ void ld_voxel(const Voxel *v, float2 &di, uint4 &lt)
+{
+    uint32_t a, b, c, d, e, f, g, h;
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(a), "=r"(b), "=r"(c), "=r"(d), "=r"(e), "=r"(f), "=r"(g), "=r"(h)
+        : "l"(v));
+    di = make_float2(__uint_as_float(a), __uint_as_float(b));
+    lt = make_uint4(e, f, g, h);
+}
+
 enum : int { KIND_RESAMPLE = 0, KIND_CACHE = 1, KIND_DROP = 2, KIND_SKIP = 3 };
 /* Why a cached render's sample is not a cache hit, kept in the upper bits of
  * its row kind (row_kind = kind | reason << 2) and counted by the compositing
@@ -451,6 +465,8 @@ cudaError_t launch_inference(const InferenceParams &p, int head_hidden, int n_sm
 __global__ void cache_init_kernel(CacheBuildParams p);
 cudaError_t launch_cache_search(const CacheBuildParams &p, int grid, cudaStream_t s);
 cudaError_t launch_cache_density(const CacheBuildParams &p, int grid, cudaStream_t s);
+/* the density network of a build iteration on tcgen05 (models without a first head) */
+cudaError_t launch_cache_density_tc(const CacheBuildParams &p, const uint8_t *weights_tc, int n_sms, cudaStream_t s);
 __global__ void cache_composite_kernel(CacheBuildParams p);
 __global__ void cache_assign_kernel(CacheBuildParams p);
 __global__ void cache_fill_kernel(CacheBuildParams p);

@@ -357,8 +357,9 @@ __device__ __forceinline__ int classify_basic(const RenderParams &p, const Cache
     for (int c = 0; c < 8; ++c) {
         if (!vp[c]) continue;
         const float w = wc[c];
-        const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
-        const uint4 lt = __ldg(&vp[c]->lat);
+        float2 di;
+        uint4 lt;
+        ld_voxel(vp[c], di, lt);
         weight = fmaf(w, di.y, weight);
         dac = fmaf(w, di.x, dac);
         const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
@@ -572,8 +573,9 @@ __device__ __forceinline__ void cache_lookup(const CacheView &C, float3 f, float
     for (int c = 0; c < 8; ++c) {
         if (!vp[c]) continue;
         const float w = wc[c];
-        const float2 di = __ldg(reinterpret_cast<const float2 *>(vp[c]));
-        const uint4 lt = __ldg(&vp[c]->lat);
+        float2 di;
+        uint4 lt;
+        ld_voxel(vp[c], di, lt);
         wsum = fmaf(w, di.y, wsum);
         dsum = fmaf(w, di.x, dsum);
         const uint32_t lw[4] = {lt.x, lt.y, lt.z, lt.w};
@@ -1085,6 +1087,90 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
         tc_fence_after();
         tmem_dealloc(tmem, TC_COLS);
     }
+}
+
+/* The cache build's density network (NerfNetwork::inferenceLatents on the
+ * build rows, src/cache_renderer.cu:1020-1030) on tcgen05: the hash features
+ * and the two density layers of wf_net_tc_kernel (same tiles, weights,
+ * epilogues and bounded waits), on every row of a build iteration; writes
+ * the row's fp16 log-density and its 8 latents from output latent_offset. */
+__global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) cache_density_tc_kernel(CacheBuildParams p, const uint8_t *weights_tc,
+                                                                                     const int *n_rows_ptr)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
+    const int n_rows = *n_rows_ptr;
+    if (n_rows == 0) return;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) {
+        mbar_init(&S.mbar, 1);
+        mbar_arrive_expect_tx(&S.mbar, TC_WBYTES);
+        bulk_copy_g2s(S.W, weights_tc, TC_WBYTES, &S.mbar);
+    }
+    if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    uint32_t phase = 0;
+    bool ok = mbar_wait(&S.mbar, phase, TC_WAIT_LIMIT);
+    phase ^= 1u;
+    const int lo = p.latent_offset;
+    const int n_tiles = (n_rows + 127) / 128;
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int r = tile * 128 + tid;
+        __half2 feat[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) feat[q] = __floats2half2_rn(0.f, 0.f);
+        if (r < n_rows) {
+            const float4 rw = p.build_rows[r];
+            hash_encode<FVC_TC_HASH_GROUP>(p.grid, p.table, make_float3(rw.x, rw.y, rw.z), feat);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) st_chunk(S.X, tid, c, 32, *reinterpret_cast<const uint4 *>(feat + 4 * c));
+        if (!(ok = tc_publish(ok))) break;
+        /* ---- layer 1: 32 -> 64, ReLU ---- */
+        ok = tc_run(S, tmem, S.W + TC_B1, 32, 64, phase);
+        epi_hidden(tmem + lane_base, nullptr, S.X, tid);
+        if (!(ok = tc_publish(ok))) break;
+        /* ---- layer 2: 64 -> 16 (log-density, latents) ---- */
+        ok = tc_run(S, tmem, S.W + TC_B2, 64, 16, phase);
+        float v[16];
+        tmem_ld16(tmem + lane_base, v);
+        tmem_wait_ld();
+        if (r < n_rows) {
+            __half h[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) h[j] = __float2half_rn(v[j]);
+            p.build_den[r] = h[0];
+            uint32_t lw[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                lw[q] = (uint32_t)__half_as_ushort(h[lo + 2 * q]) | ((uint32_t)__half_as_ushort(h[lo + 2 * q + 1]) << 16);
+            p.build_lat[r] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        tc_fence_before();
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+    }
+    if (!ok && tid == 0 && p.guard) atomicOr(p.guard, 16);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TC_COLS);
+    }
+}
+
+cudaError_t launch_cache_density_tc(const CacheBuildParams &p, const uint8_t *weights_tc, int n_sms, cudaStream_t s)
+{
+    static PerDeviceOnce once;
+    cudaError_t e = once.run([] {
+        return cudaFuncSetAttribute(cache_density_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcSmem));
+    });
+    if (e != cudaSuccess) return e;
+    cache_density_tc_kernel<<<n_sms * FVC_TC_CTAS_PER_SM, 128, sizeof(TcSmem), s>>>(p, weights_tc, p.build_row_counter);
+    return cudaGetLastError();
 }
 
 /* ------------------------------------------------------------------------- */

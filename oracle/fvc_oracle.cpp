@@ -572,6 +572,18 @@ void orc_inference(const OrcNet *net, const float *pos, const float *dir01, int 
         out[4 * i + 0] = lg[0]; out[4 * i + 1] = lg[1]; out[4 * i + 2] = lg[2]; out[4 * i + 3] = bo[0];
     });
 }
+/* The density network's outputs at given inputs (float64, base_out_pad per
+ * row; row 0 the log-density): what NerfNetwork::inferenceLatents writes for
+ * a model without a first head (include/nerf_network.h:173-202). */
+void orc_base_outputs(const OrcNet *net, const float *pos, const float *dir01, int n, double *out, int n_threads)
+{
+    NetD d; prepare_net(net, d);
+    parallel_rows(n, n_threads, [&](int i) {
+        double bo[64];
+        base_forward(d, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), bo, dir01 + 3 * i);
+        for (int j = 0; j < net->base_out_pad; ++j) out[(size_t)i * net->base_out_pad + j] = bo[j];
+    });
+}
 void orc_hash_encode(const OrcNet *net, const float *pos, int n, double *feat_out)
 {
     NetD d; prepare_net(net, d);

@@ -100,6 +100,7 @@ def lib():
         _lib.orc_expf.restype = C.c_float
         _lib.orc_inference.argtypes = [P(OrcNet), C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         _lib.orc_hash_encode.argtypes = [P(OrcNet), C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_base_outputs.argtypes = [P(OrcNet), C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         _lib.orc_render_plain.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, C.c_int, C.c_int,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         _lib.orc_loss_grad.argtypes = [P(OrcNet), P(OrcScene), P(OrcSteps), P(OrcCam), C.c_void_p, C.c_void_p, C.c_int,
@@ -247,6 +248,14 @@ class OracleModel:
         dir01 = np.ascontiguousarray(dir01, np.float32)
         out = np.zeros((pos.shape[0], 4), np.float64)
         lib().orc_inference(C.byref(self.net), ptr(pos), ptr(dir01), pos.shape[0], ptr(out), threads or default_threads())
+        return out
+
+    def base_outputs(self, pos: np.ndarray, dir01: np.ndarray, threads: int | None = None) -> np.ndarray:
+        """The density network's padded outputs (float64, row 0 the log-density) at contracted positions."""
+        pos = np.ascontiguousarray(pos, np.float32)
+        dir01 = np.ascontiguousarray(dir01, np.float32)
+        out = np.zeros((pos.shape[0], self.net.base_out_pad), np.float64)
+        lib().orc_base_outputs(C.byref(self.net), ptr(pos), ptr(dir01), pos.shape[0], ptr(out), threads or default_threads())
         return out
 
     def hash_encode(self, pos: np.ndarray) -> np.ndarray:
