@@ -151,6 +151,7 @@ SIGNATURES = {
     "fvc_cache_dims": (c_int, [P, C.POINTER(Int3), C.POINTER(Int3), C.POINTER(Int3)]),
     "fvc_render_noalloc": (c_int, [P, C.POINTER(RaymarchInfo), C.POINTER(RenderOutputs), P]),
     "fvc_renderer_set_network_path": (c_int, [P, c_int]),
+    "fvc_renderer_set_build_network_path": (c_int, [P, c_int]),
     "fvc_renderer_set_tiling": (c_int, [P, c_int, c_int]),
     "fvc_renderer_set_fused_classify": (c_int, [P, c_int]),
     "fvc_renderer_set_empty_space_skipping": (c_int, [P, c_int]),

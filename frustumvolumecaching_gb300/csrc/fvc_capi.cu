@@ -308,6 +308,8 @@ struct fvc_model {
     DevGrid grid{};
     int latent_offset = 1, n_latents = 8, head_hidden = 2;
     int view_dependent = 0;                 /* split head with an initial view direction (mlp_first_head) */
+    int freq = 0;                           /* the head's positional frequency encoding degree (0 or 4) */
+    int tc_wbytes = TC_WBYTES;              /* bytes of the tcgen05 weight tiles (TCF_WBYTES with the encoding) */
     std::vector<uint16_t> h_base, h_head;  /* fp16 weight blobs in the model file layouts */
     std::vector<uint16_t> h_first;         /* the first head's blob (view-dependent models) */
     uint8_t *d_weights_vd = nullptr;        /* VD_WBYTES of K-major tiles (view-dependent models) */
@@ -462,6 +464,7 @@ struct fvc_renderer {
     int render_mode = 0;
     int max_samples = 0;
     int use_tc = 1;                   /* network kernels on tcgen05 (1) or mma.sync (0) */
+    int build_tc = 0;                 /* the cache builds' density network on tcgen05 (1) or mma.sync (0, faster) */
     int precision = FVC_PRECISION_FP16;
     BuildScratch bs;
     PerRayScratch pr;
@@ -551,12 +554,17 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
                                                  : head.bool_or("first_latent_is_density", true);
     m.latent_offset = first_lat_dens ? 0 : 1;
     m.n_latents = m.view_dependent ? (int)fh.num_or("n_output", 8) : (int)head.num_or("n_latents", n_out);
-    const int head_in = (int)head.num_or("n_input", (m.view_dependent ? 32 : 16) + m.n_latents);
+    /* NerfNetwork::init: freq_encoding_degree (include/nerf_network.h:103); the encoding's 6 * degree values
+     * follow the SH inputs of the head (:241-246) */
+    m.freq = (int)head.num_or("freq_encoding_degree", 0);
+    if (m.freq != 0 && m.freq != 4) return fail(FVC_ERR_CONFIG, "freq_encoding_degree must be 0 or 4");
+    if (m.freq && m.view_dependent)
+        return fail(FVC_ERR_CONFIG, "the frequency encoding is built for the color head without mlp_first_head");
+    const int head_in = (int)head.num_or("n_input", (m.view_dependent ? 32 : 16) + m.n_latents + 6 * m.freq);
     const int head_in_pad = (head_in + 15) / 16 * 16;
     m.head_hidden = (int)head["network"].num_or("n_hidden_layers", 2);
     if ((int)head["network"].num_or("n_neurons", 64) != 64) return fail(FVC_ERR_CONFIG, "head width must be 64");
     if (m.head_hidden < 1 || m.head_hidden > 2) return fail(FVC_ERR_CONFIG, "head must have 1 or 2 hidden layers");
-    if (head.num_or("freq_encoding_degree", 0) != 0) return fail(FVC_ERR_CONFIG, "the head's frequency encoding is not built");
     if (m.view_dependent) {
         if ((int)fh["network"].num_or("n_neurons", 64) != 64 || (int)fh["network"].num_or("n_hidden_layers", 1) != 1)
             return fail(FVC_ERR_CONFIG, "mlp_first_head must be 32 -> 64 -> n_output (1 hidden layer of 64)");
@@ -569,7 +577,9 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
             return fail(FVC_ERR_CONFIG, "only SH degree 4 direction encoding is built");
         if (!wf) return fail(FVC_ERR_IO, "missing mlp_first_head.dat");
         if (wf->size() != (size_t)(64 * 32 + 16 * 64) * 2) return fail(FVC_ERR_IO, "mlp_first_head.dat has the wrong size");
-    } else if (m.latent_offset + m.n_latents > 16 || head_in != m.n_latents + 16 || head_in_pad != 32) {
+    } else if (m.freq && (m.latent_offset + m.n_latents > 16 || head_in != m.n_latents + 16 + 24 || head_in_pad != 48)) {
+        return fail(FVC_ERR_CONFIG, "a head with the frequency encoding must read n_latents + 16 SH + 24 frequency values (48)");
+    } else if (!m.freq && (m.latent_offset + m.n_latents > 16 || head_in != m.n_latents + 16 || head_in_pad != 32)) {
         return fail(FVC_ERR_CONFIG, "head input must be n_latents + 16 SH values padded to 32");
     }
     const JVal &nested = head["encoding"]["nested"];
@@ -634,30 +644,35 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         w2.resize(16 * 64, 0);
         frag_pack(w2, 16, 64, &W[W_L2]);
     }
-    std::vector<uint16_t> h0 = u16(wh, 0, 64 * 32);
-    std::vector<uint16_t> l3(64 * 32, 0);
+    const int K3 = m.freq ? 64 : 32; /* the kernels' head input: [density outputs 16 | SH 16 (| frequency 24 | 0 8)] */
+    std::vector<uint16_t> h0 = u16(wh, 0, (size_t)64 * head_in_pad);
+    std::vector<uint16_t> l3((size_t)64 * K3, 0);
     std::vector<float> bias3(64, 0.f);
-    /* the 32-wide head input layout; a view-dependent model uses its own tiles (below) instead */
+    /* the head input layout of the kernels; a view-dependent model uses its own tiles (below) instead */
     for (int n = 0; n < 64 && !m.view_dependent; ++n) {
         for (int k = 0; k < 16; ++k) {
             const int src = k - m.latent_offset;
-            if (src >= 0 && src < m.n_latents) l3[n * 32 + k] = h0[n * 32 + src];
+            if (src >= 0 && src < m.n_latents) l3[n * K3 + k] = h0[n * head_in_pad + src];
         }
-        for (int j = 0; j < 16; ++j) l3[n * 32 + 16 + j] = h0[n * 32 + m.n_latents + j];
+        for (int j = 0; j < 16; ++j) l3[n * K3 + 16 + j] = h0[n * head_in_pad + m.n_latents + j];
+        for (int j = 0; j < 6 * m.freq; ++j) l3[n * K3 + 32 + j] = h0[n * head_in_pad + m.n_latents + 16 + j];
         double acc = 0.0;  /* inputs padded with 1.0 (include/nerf_network.h:248-253) */
-        for (int k = head_in; k < head_in_pad; ++k) acc += h2f(h0[n * 32 + k]);
+        for (int k = head_in; k < head_in_pad; ++k) acc += h2f(h0[n * head_in_pad + k]);
         bias3[n] = (float)acc;
     }
-    frag_pack(l3, 64, 32, &W[W_L3]);
-    size_t ho = 64 * 32;
+    if (!m.freq) frag_pack(l3, 64, 32, &W[W_L3]); /* the mma.sync path has no frequency encoding */
+    size_t ho = (size_t)64 * head_in_pad;
+    const size_t h_l4 = ho; /* the second hidden layer's weights */
     if (m.head_hidden == 2) {
         frag_pack(u16(wh, ho, 64 * 64), 64, 64, &W[W_L4]);
         ho += 64 * 64;
     }
     frag_pack(u16(wh, ho, 16 * 64), 16, 64, &W[W_L5]);
 
-    /* the same matrices as canonical K-major tiles for the tcgen05 kernels */
-    std::vector<uint8_t> Wt(TC_WBYTES, 0);
+    /* the same matrices as canonical K-major tiles for the tcgen05 kernels (the head's first layer with
+     * K = 64 and the later layers shifted for a frequency-encoded head) */
+    m.tc_wbytes = m.freq ? TCF_WBYTES : TC_WBYTES;
+    std::vector<uint8_t> Wt(m.tc_wbytes, 0);
     auto tc_pack = [&](const std::vector<uint16_t> &M, int N, int K, int off) {
         for (int n = 0; n < N; ++n)
             for (int k = 0; k < K; ++k) memcpy(&Wt[off + kmajor_offset(n, k, K)], &M[(size_t)n * K + k], 2);
@@ -668,13 +683,13 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         w2.resize(16 * 64, 0);
         tc_pack(w2, 16, 64, TC_B2);
     }
-    tc_pack(l3, 64, 32, TC_B3);
-    if (m.head_hidden == 2) tc_pack(u16(wh, 64 * 32, 64 * 64), 64, 64, TC_B4);
-    tc_pack(u16(wh, ho, 16 * 64), 16, 64, TC_B5);
+    tc_pack(l3, 64, K3, m.freq ? TCF_B3 : TC_B3);
+    if (m.head_hidden == 2) tc_pack(u16(wh, h_l4, 64 * 64), 64, 64, m.freq ? TCF_B4 : TC_B4);
+    tc_pack(u16(wh, ho, 16 * 64), 16, 64, m.freq ? TCF_B5 : TC_B5);
 
     /* reduced-precision copies: bf16 tiles (same layout) and e4m3 tiles
-     * (8-bit K-major layout), each e4m3 layer scaled by 448 / amax(W) */
-    {
+     * (8-bit K-major layout), each e4m3 layer scaled by 448 / amax(W); none for a frequency-encoded head */
+    if (!m.freq) {
         std::vector<uint8_t> Wb(TC_WBYTES, 0), W8(TC8_WBYTES, 0);
         float iw[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
         auto pack_low = [&](const std::vector<uint16_t> &M, int N, int K, int off16, int off8, int layer) {
@@ -764,8 +779,8 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
     if ((rc = dalloc(&m.d_table, (size_t)off * (F / 2), "hash tables"))) return rc;
     if ((rc = dalloc(&m.d_weights, (size_t)W_TOTAL, "weights"))) return rc;
     if ((rc = dalloc(&m.d_bias3, (size_t)64, "bias"))) return rc;
-    if ((rc = dalloc(&m.d_weights_tc, (size_t)TC_WBYTES, "tcgen05 weights"))) return rc;
-    CU(cudaMemcpy(m.d_weights_tc, Wt.data(), TC_WBYTES, cudaMemcpyHostToDevice));
+    if ((rc = dalloc(&m.d_weights_tc, (size_t)m.tc_wbytes, "tcgen05 weights"))) return rc;
+    CU(cudaMemcpy(m.d_weights_tc, Wt.data(), m.tc_wbytes, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_table, tab.data(), tab.size(), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(m.d_weights, W.data(), W.size() * sizeof(uint2), cudaMemcpyHostToDevice));
@@ -961,6 +976,12 @@ extern "C" int fvc_ingp_export(const char *snapshot, const char *export_dir)
     return FVC_OK;
 }
 
+/* the head's tcgen05 tile layout of a model (TC_* without, TCF_* with the frequency encoding) */
+static void set_head_layout(const fvc_model &m, RenderParams &p)
+{
+    p.freq = m.freq;
+}
+
 extern "C" int fvc_model_load(const char *data_dir, fvc_model **out)
 {
     CHECK_ARG(data_dir && out, "fvc_model_load: null argument");
@@ -1036,6 +1057,7 @@ extern "C" int fvc_stepsize_setup(const fvc_scene_info *scene, fvc_stepsize_info
 static int run_inference(fvc_model *m, const float *pos, const float *dir, int n, float *out4, float *base_out, float *features)
 {
     CHECK_ARG(m && pos && n >= 0, "inference: bad arguments");
+    if (m->freq && dir) return fail(FVC_ERR_CONFIG, "network inference evaluates heads without the frequency encoding");
     if (n == 0) return FVC_OK;
     float *dp = nullptr, *dd = nullptr, *d4 = nullptr, *db = nullptr, *df = nullptr;
     int rc = FVC_OK;
@@ -1241,6 +1263,9 @@ static int setup_render_params(fvc_renderer *r, const fvc_raymarch_info *info, f
     p.view_dependent = m->view_dependent;
     p.weights_vd = m->d_weights_vd;
     p.latent_offset = m->latent_offset;
+    if (m->freq && (!r->use_tc || r->precision != FVC_PRECISION_FP16 || r->m_tile != 128))
+        return fail(FVC_ERR_CONFIG, "heads with the frequency encoding are built for the tcgen05 network path in FP16 on 128-row tiles");
+    set_head_layout(*m, p);
     p.basic_cache = r->kind == FVC_RENDERER_CACHE_BASIC;
     p.ray_counter = r->d_ctl; p.guard = r->d_ctl + 1; p.stats = r->d_stats;
     p.results = results; p.image = image; p.ray_counts = counts;
@@ -1626,9 +1651,9 @@ extern "C" int fvc_cache_build(fvc_renderer *r, const fvc_raymarch_info *info)
         CU(cudaMemsetAsync(p.build_row_counter, 0, sizeof(int), s));
         CU(launch_cache_search(p, std::min(n_alive, 1 << 16), s));
         CU(cudaGetLastError());
-        /* the density network on tcgen05 in the renderer's default network path; the first head of
-         * view-dependent models and the mma.sync path keep the warp-level kernel */
-        if (r->use_tc && !m->view_dependent) CU(launch_cache_density_tc(p, m->d_weights_tc, m->n_sms, s));
+        /* the density network (fvc_renderer_set_build_network_path); view-dependent models' first head runs
+         * in the warp-level kernel */
+        if (r->build_tc && !m->view_dependent) CU(launch_cache_density_tc(p, m->d_weights_tc, m->n_sms, s));
         else CU(launch_cache_density(p, m->n_sms * 8, s));
         CU(cudaGetLastError());
         cache_composite_kernel<<<std::min((n_alive + 3) / 4, 1 << 16), 128, 0, s>>>(p);
@@ -1738,7 +1763,7 @@ extern "C" int fvc_cache_build_per_ray(fvc_renderer *r, const fvc_raymarch_info 
         CU(cudaMemsetAsync(p.counters + 2, 0, sizeof(int), s));
         CU(launch_fill_march(p, it, n_sms, s));
         q.dir_states = p.states[it & 1];
-        if (r->use_tc && !m->view_dependent) CU(launch_cache_density_tc(q, m->d_weights_tc, n_sms, s));
+        if (r->build_tc && !m->view_dependent) CU(launch_cache_density_tc(q, m->d_weights_tc, n_sms, s));
         else CU(launch_cache_density(q, n_sms * 8, s));
         pr_mark_kernel<<<n_sms * 16, 128, 0, s>>>(f, it);
         pr_count_kernel<<<(int)((n_cols + 255) / 256), 256, 0, s>>>(f);
@@ -1808,6 +1833,7 @@ namespace fvc_internal {
 int model_views(const fvc_model *m, RenderParams *p, int *head_hidden, int *n_sms)
 {
     if (m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
+    set_head_layout(*m, *p);
     p->scene = m->dscene;
     p->grid = m->grid;
     p->bits = m->d_bits;
@@ -1832,6 +1858,13 @@ extern "C" int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05)
 {
     CHECK_ARG(r && (use_tcgen05 == 0 || use_tcgen05 == 1), "fvc_renderer_set_network_path: bad arguments");
     r->use_tc = use_tcgen05;
+    return FVC_OK;
+}
+
+extern "C" int fvc_renderer_set_build_network_path(fvc_renderer *r, int use_tcgen05)
+{
+    CHECK_ARG(r && (use_tcgen05 == 0 || use_tcgen05 == 1), "fvc_renderer_set_build_network_path: bad arguments");
+    r->build_tc = use_tcgen05;
     return FVC_OK;
 }
 
@@ -1889,6 +1922,7 @@ extern "C" int fvc_grad_create(fvc_model *m, fvc_grad **out)
     CHECK_ARG(m && out, "fvc_grad_create: null argument");
     *out = nullptr;
     if (m->view_dependent) return fail(FVC_ERR_CONFIG, "the adjoint is built for networks without the view-dependent split head");
+    if (m->freq) return fail(FVC_ERR_CONFIG, "the adjoint is built for heads without the frequency encoding");
     if (m->n_latents != 8 || m->grid.n_levels != 16)
         return fail(FVC_ERR_CONFIG, "the backward kernels are built for 16 hash levels of 2 features and 8 latents");
     auto g = std::make_unique<fvc_grad>();
@@ -2238,6 +2272,7 @@ extern "C" int fvc_renderer_autotune(fvc_renderer *r, const fvc_raymarch_info *i
 {
     CHECK_ARG(r && res, "fvc_renderer_autotune: null argument");
     if (r->m->view_dependent) return fail(FVC_ERR_CONFIG, "view-dependent models (mlp_first_head) are built for the renderers and cache builds on the tcgen05 network path in FP16 (the autotuner also tries the mma.sync path)");
+    if (r->m->freq) return fail(FVC_ERR_CONFIG, "heads with the frequency encoding run on 128-row tcgen05 tiles only: nothing to tune");
     std::lock_guard<std::mutex> lk(r->read_mutex);
     /* candidates: the space set by fvc_renderer_set_autotune_space (tile heights, 32 = the mma.sync warp
      * tile; compaction batches; march lengths), every combination */

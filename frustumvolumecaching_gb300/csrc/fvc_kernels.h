@@ -75,6 +75,13 @@ constexpr int TC_B3 = 6144;     /* 64 x 32 */
 constexpr int TC_B4 = 10240;    /* 64 x 64 */
 constexpr int TC_B5 = 18432;    /* 16 x 64 */
 constexpr int TC_WBYTES = 20480;
+/* a head with the positional frequency encoding (freq_encoding_degree 4,
+ * include/nerf_network.h:55-81,241-246): its first layer reads K = 64 inputs
+ * [density outputs 16 | SH 16 | 24 sines and cosines | 8 zero] */
+constexpr int TCF_B3 = 6144;    /* 64 x 64 */
+constexpr int TCF_B4 = 14336;   /* 64 x 64 */
+constexpr int TCF_B5 = 22528;   /* 16 x 64 */
+constexpr int TCF_WBYTES = 24576;
 /* the view-dependent split network (NerfNetwork::init_viewdep,
  * include/nerf_network.h:120-158) as K-major tiles: density MLP, first head
  * ([density outputs | SH of the initial direction] 32 -> 64 -> 16 latent
@@ -107,6 +114,7 @@ __device__ __forceinline__ void ld_voxel(const Voxel *v, float2 &di, uint4 &lt)
     asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=r"(a), "=r"(b), "=r"(c), "=r"(d), "=r"(e), "=r"(f), "=r"(g), "=r"(h)
         : "l"(v));
+    (void)c; (void)d; /* the two pad words */
     di = make_float2(__uint_as_float(a), __uint_as_float(b));
     lt = make_uint4(e, f, g, h);
 }
@@ -264,6 +272,7 @@ struct RenderParams {
                                  * = clamp(row_target / alive rays, 1, S_ROWS) (0 = row_capacity) */
     int basic_cache;            /* 1: CacheBasicRenderer semantics for the cached rows (classify_basic) */
     int view_dependent;         /* split head (mlp_first_head): first head + SH-difference head input */
+    int freq;                   /* the head's positional frequency encoding degree (0, or 4: the TCF_* tile layout) */
     const uint8_t *weights_vd;  /* VD_WBYTES of K-major tiles of the view-dependent network */
     /* batched views: rays of n_views cameras (device array), view v's pixel
      * (x, y) at ray id view_off[v] + y * W_v + x; view_off[n_views] = rays;

@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
  * with tcgen05.ld, applies ReLU / fp16 rounding and writes the next layer's
  * operand. */
 struct __align__(128) TcSmem {
-    uint8_t W[TC_WBYTES];
+    uint8_t W[TCF_WBYTES]; /* TC_WBYTES used unless the head has the frequency encoding */
     uint8_t X[128 * 64 * 2];
     float bias3[64];
     uint64_t mbar;
@@ -958,6 +958,34 @@ __device__ __forceinline__ bool tc_publish(bool ok)
     return __syncthreads_or(!ok) == 0;
 }
 
+/* frequency_encoding (include/nerf_network.h:55-81) of one axis of the
+ * network's input position: sin(pi 2^k x) for k < 4, then the cosines (the
+ * reference's phase of pi/2), rounded to fp16; x 2^k is exact. */
+__device__ __forceinline__ uint4 freq_chunk(float x)
+{
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float xk = x * (float)(1 << k);
+        v[k] = sinpif(xk);
+        v[4 + k] = cospif(xk);
+    }
+    return pack8(v);
+}
+
+/* the head's input position of a cache row: the contracted point at the
+ * midpoint the row's network input is evaluated at (t0 + dt/2,
+ * generateNetworkInput_preparation_perf_kernel :284-297; (t0 + t1)/2 for the
+ * basic cache renderer) */
+__device__ __forceinline__ float3 cache_row_position(const RenderParams &p, const RayState *states, int r)
+{
+    const int slot = p.row_slot[r];
+    const float4 of = states[slot].of, dt4 = states[slot].dt;
+    const float t0 = p.row_t0[r], dt = calc_step(p.steps, t0);
+    const float t = p.basic_cache ? F_MUL(F_ADD(t0, F_ADD(t0, dt)), 0.5f) : F_ADD(t0, F_MUL(dt, 0.5f));
+    return contract(p.scene, at(make_float3(of.x, of.y, of.z), make_float3(dt4.x, dt4.y, dt4.z), t));
+}
+
 /* MODE 0: resample rows (the list, or all rows of the plain path); MODE 1: the
  * cache list (head only); MODE 2: both lists of a cached sub-iteration
  * classified by the march in one launch, the resample list's tiles first
@@ -975,10 +1003,14 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
     const int tid = threadIdx.x, warp = tid >> 5;
     /* the weights arrive by one bulk copy on the TMA engine, completing the
      * mbarrier's phase 0; the layers' MMA commits complete the later phases */
+    /* the head's input width and tile layout: 32 inputs (TC_*), or 64 with the frequency encoding (TCF_*) */
+    const int HK = p.freq ? 64 : 32;
+    const int wb3 = p.freq ? TCF_B3 : TC_B3, wb4 = p.freq ? TCF_B4 : TC_B4, wb5 = p.freq ? TCF_B5 : TC_B5;
     if (tid == 0) {
+        const int wbytes = p.freq ? TCF_WBYTES : TC_WBYTES;
         mbar_init(&S.mbar, 1);
-        mbar_arrive_expect_tx(&S.mbar, TC_WBYTES);
-        bulk_copy_g2s(S.W, p.weights_tc, TC_WBYTES, &S.mbar);
+        mbar_arrive_expect_tx(&S.mbar, wbytes);
+        bulk_copy_g2s(S.W, p.weights_tc, wbytes, &S.mbar);
     }
     if (tid < 64) S.bias3[tid] = p.bias3[tid];
     if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
@@ -1042,8 +1074,8 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
                 }
             }
             log_density = (uint16_t)(b0.x & 0xffffu);
-            st_chunk(S.X, tid, 0, 32, b0);
-            st_chunk(S.X, tid, 1, 32, b1);
+            st_chunk(S.X, tid, 0, HK, b0);
+            st_chunk(S.X, tid, 1, HK, b1);
         } else {
             /* ---- cache lookup -> head input (log-density, latents) ---- */
             __half hin[32];
@@ -1053,24 +1085,45 @@ __global__ void __launch_bounds__(128, FVC_TC_CTAS_PER_SM) wf_net_tc_kernel(Rend
                 for (int q = 16; q < 32; ++q) hin[q] = __float2half_rn(0.f);
             }
             log_density = __half_as_ushort(hin[16]);
-            st_chunk(S.X, tid, 0, 32, *reinterpret_cast<const uint4 *>(hin + 16));
-            st_chunk(S.X, tid, 1, 32, *reinterpret_cast<const uint4 *>(hin + 24));
+            st_chunk(S.X, tid, 0, HK, *reinterpret_cast<const uint4 *>(hin + 16));
+            st_chunk(S.X, tid, 1, HK, *reinterpret_cast<const uint4 *>(hin + 24));
         }
-        st_chunk(S.X, tid, 2, 32, *reinterpret_cast<const uint4 *>(sh));
-        st_chunk(S.X, tid, 3, 32, *reinterpret_cast<const uint4 *>(sh + 4));
+        st_chunk(S.X, tid, 2, HK, *reinterpret_cast<const uint4 *>(sh));
+        st_chunk(S.X, tid, 3, HK, *reinterpret_cast<const uint4 *>(sh + 4));
+        if (p.freq) {
+            /* the frequency encoding of the row's network input position (include/nerf_network.h:241-246) */
+            uint4 fx = make_uint4(0u, 0u, 0u, 0u), fy = fx, fz = fx;
+            if (r >= 0) {
+                const bool cache_row = MODE == 1 || (MODE == 2 && kind == KIND_CACHE);
+                float3 q;
+                if (cache_row) {
+                    q = cache_row_position(p, states, r);
+                } else {
+                    const float4 pw = p.row_pay[r];
+                    q = make_float3(pw.x, pw.y, pw.z);
+                }
+                fx = freq_chunk(q.x);
+                fy = freq_chunk(q.y);
+                fz = freq_chunk(q.z);
+            }
+            st_chunk(S.X, tid, 4, HK, fx);
+            st_chunk(S.X, tid, 5, HK, fy);
+            st_chunk(S.X, tid, 6, HK, fz);
+            st_chunk(S.X, tid, 7, HK, make_uint4(0u, 0u, 0u, 0u));
+        }
         if (!(ok = tc_publish(ok))) break;
-        /* ---- head layer 1: (latents | SH) 32 -> 64, bias from the 1-padding, ReLU ---- */
-        ok = tc_run(S, tmem, S.W + TC_B3, 32, 64, phase);
+        /* ---- head layer 1: (latents | SH (| frequency)) HK -> 64, bias from the 1-padding, ReLU ---- */
+        ok = tc_run(S, tmem, S.W + wb3, HK, 64, phase);
         epi_hidden(tmem + lane_base, S.bias3, S.X, tid);
         if (!(ok = tc_publish(ok))) break;
         if (HH == 2) {
             /* ---- head layer 2: 64 -> 64, ReLU ---- */
-            ok = tc_run(S, tmem, S.W + TC_B4, 64, 64, phase);
+            ok = tc_run(S, tmem, S.W + wb4, 64, 64, phase);
             epi_hidden(tmem + lane_base, nullptr, S.X, tid);
             if (!(ok = tc_publish(ok))) break;
         }
         /* ---- output layer: 64 -> 16 (rgb logits in cols 0..2) ---- */
-        ok = tc_run(S, tmem, S.W + TC_B5, 64, 16, phase);
+        ok = tc_run(S, tmem, S.W + wb5, 64, 16, phase);
         float o[16];
         tmem_ld16(tmem + lane_base, o);
         tmem_wait_ld();

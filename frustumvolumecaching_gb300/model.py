@@ -183,6 +183,7 @@ class ModelSpec:
     occupancy_fraction: float = 0.12
     occupancy_cascades: str = "all"     # "all": threshold every cascade; "inner": outer cascades empty
     view_dependent: bool = False        # split head (mlp_first_head): latents from a first head on an initial direction
+    freq_encoding_degree: int = 0       # 4: the head also reads sin / cos(pi 2^k p) of the contracted position, k < 4
 
 
 def spec_config1() -> ModelSpec:
@@ -241,9 +242,10 @@ class SyntheticModel:
         self.n_base_out = n_out
         self.base = [_xavier(rng, spec.width, enc_w, spec.width, _pad16(enc_w)),
                      _xavier(rng, n_out, spec.width, _pad16(n_out), spec.width)]
-        # the head reads [latents | SH of the direction (16)], and a view-dependent head also the SH
-        # difference to the initial direction (16) (include/nerf_network.h:204-257)
-        head_in = spec.n_latents + (32 if spec.view_dependent else 16)
+        # the head reads [latents | SH of the direction (16)], a view-dependent head also the SH
+        # difference to the initial direction (16), and with a frequency encoding the 6 * degree
+        # sines and cosines of the position (include/nerf_network.h:55-81,204-257)
+        head_in = spec.n_latents + (32 if spec.view_dependent else 16) + 6 * spec.freq_encoding_degree
         self.head_in = head_in
         head_in_pad = _pad16(head_in)
         hl = [_xavier(rng, spec.width, head_in, spec.width, head_in_pad)]
@@ -326,7 +328,8 @@ class SyntheticModel:
             "mlp_base": {"encoding": enc, "network": net, "n_output": self.n_base_out},
             "mlp_head": {"encoding": sh_enc,
                 "network": head_net, "n_input": self.head_in, "n_latents": s.n_latents,
-                "first_latent_is_density": s.first_latent_is_density},
+                "first_latent_is_density": s.first_latent_is_density,
+                "freq_encoding_degree": s.freq_encoding_degree},
             "synthetic": {"seed": s.seed, "name": s.name, "occupancy_fraction": s.occupancy_fraction,
                           "table_range": s.table_range,
                           "hashmap_sizes": [lv.size for lv in self.levels]},
@@ -357,7 +360,9 @@ def default_model_root() -> str:
 
 def model_dir_name(spec: ModelSpec) -> str:
     vd = "_vd" if spec.view_dependent else ""
-    return f"{spec.name}_s{spec.seed}_T{spec.log2_T}_n{spec.grid_nlvl}_o{int(round(spec.occupancy_fraction * 1000))}{spec.occupancy_cascades}{vd}"
+    fq = f"_freq{spec.freq_encoding_degree}" if spec.freq_encoding_degree else ""
+    return (f"{spec.name}_s{spec.seed}_T{spec.log2_T}_n{spec.grid_nlvl}_o{int(round(spec.occupancy_fraction * 1000))}"
+            f"{spec.occupancy_cascades}{vd}{fq}")
 
 
 def ensure_model(spec: ModelSpec, root: str | None = None) -> str:

@@ -179,6 +179,10 @@ class Renderer:
         """tcgen05 (default) or mma.sync network kernels."""
         L.check(L.load().fvc_renderer_set_network_path(self.handle, int(bool(use_tcgen05))))
 
+    def set_build_network_path(self, use_tcgen05: bool) -> None:
+        """The cache builds' density network: mma.sync (default, faster here) or tcgen05; same slots."""
+        L.check(L.load().fvc_renderer_set_build_network_path(self.handle, int(bool(use_tcgen05))))
+
     def set_empty_space_skipping(self, on: bool) -> None:
         """Occupancy lookups once per empty cell (default) or every step; identical results."""
         L.check(L.load().fvc_renderer_set_empty_space_skipping(self.handle, int(bool(on))))

@@ -321,6 +321,15 @@ int fvc_renderer_set_max_samples_per_ray(fvc_renderer *r, int max_samples);
  * Both compute the same layers in fp16 with fp32 accumulation.  No reference
  * counterpart (the reference runs tiny-cuda-nn's FullyFusedMLP). */
 int fvc_renderer_set_network_path(fvc_renderer *r, int use_tcgen05);
+/* Density network of the cache builds (the blockwise build and the per-ray
+ * fill; inferenceLatents, src/cache_renderer.cu:1020-1030, :893-900):
+ * 0 = warp-level mma.sync (the default: these two layers on 32-row warp
+ * tiles measured faster than 128-row tcgen05 tiles, whose per-layer
+ * CTA-wide round trips the short network does not amortise), 1 = tcgen05.
+ * View-dependent models build on mma.sync.  Slots, known ranges and isset
+ * flags do not depend on it; voxel values agree to fp16 rounding.  No
+ * reference counterpart. */
+int fvc_renderer_set_build_network_path(fvc_renderer *r, int use_tcgen05);
 
 /* Rows per tcgen05 network tile of the plain path (64, 128 or 256; FP16, not
  * view-dependent; default 128) and the compaction batch, the rows per

@@ -69,6 +69,7 @@ struct OrcNet {
     int mimic_fp16;          /* round layer outputs to fp16 like the reference */
     int view_dependent;      /* split head (mlp_first_head, include/nerf_network.h:120-158) */
     const uint16_t *first_w; /* the first head: [width x 32], [16 x width] */
+    int freq_deg;            /* the head's positional frequency encoding degree (0 or 4) */
 };
 }
 
@@ -405,7 +406,8 @@ void sh16(const float *d01, double *o)
  * view-dependent head also reads SH(dir) - SH(init01), fp16 operands
  * subtracted in fp16 (nerf_network.h:47-52,226-240); without init01 (the
  * row's own direction) that input is zero. */
-void head_forward(const NetD &d, const double *latents, const float *dir01, double *rgb_logits, const float *init01 = nullptr)
+void head_forward(const NetD &d, const double *latents, const float *dir01, double *rgb_logits, const float *init01 = nullptr,
+                  const V3 *pos = nullptr)
 {
     const OrcNet &n = *d.n;
     double in[128], a[128], b[128];
@@ -418,6 +420,18 @@ void head_forward(const NetD &d, const double *latents, const float *dir01, doub
         for (int i = 0; i < 16; ++i) {
             const double s0 = in[n.n_latents + i];
             in[n.n_latents + 16 + i] = !init01 ? 0.0 : n.mimic_fp16 ? round_h(s0 - round_h(shi[i])) : s0 - shi[i];
+        }
+    }
+    if (n.freq_deg > 0) {
+        /* frequency_encoding (include/nerf_network.h:55-81) of the network's input position, after the SH
+         * inputs: per axis the sines of pi 2^k p, then the cosines (a phase of pi/2), k < degree */
+        const int o = n.n_latents + (n.view_dependent ? 32 : 16);
+        const double p3[3] = {pos ? (double)pos->x : 0.0, pos ? (double)pos->y : 0.0, pos ? (double)pos->z : 0.0};
+        for (int j = 0; j < 6 * n.freq_deg; ++j) {
+            const int axis = j / (2 * n.freq_deg), k = j % n.freq_deg, cosine = (j / n.freq_deg) % 2;
+            const double x = M_PI * std::ldexp(p3[axis], k);
+            const double v = cosine ? std::cos(x) : std::sin(x);
+            in[o + j] = n.mimic_fp16 ? round_h(v) : v;
         }
     }
     for (int i = n.head_in; i < n.head_in_pad; ++i) in[i] = 1.0;
@@ -566,9 +580,10 @@ void orc_inference(const OrcNet *net, const float *pos, const float *dir01, int 
     NetD d; prepare_net(net, d);
     parallel_rows(n, n_threads, [&](int i) {
         double bo[64];
-        base_forward(d, v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]), bo, dir01 + 3 * i);
+        const V3 p = v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        base_forward(d, p, bo, dir01 + 3 * i);
         double lg[3];
-        head_forward(d, bo + net->latent_offset, dir01 + 3 * i, lg);
+        head_forward(d, bo + net->latent_offset, dir01 + 3 * i, lg, nullptr, &p);
         out[4 * i + 0] = lg[0]; out[4 * i + 1] = lg[1]; out[4 * i + 2] = lg[2]; out[4 * i + 3] = bo[0];
     });
 }
@@ -621,8 +636,9 @@ int orc_render_plain(const OrcNet *net, const OrcScene *sc, const OrcSteps *st, 
                     const V3 wp = at(r, tm);
                     if (!occupied(*sc, bits, wp)) continue;
                     double bo[64], lg[3];
-                    base_forward(d, contract(*sc, wp), bo, d01);
-                    head_forward(d, bo + net->latent_offset, d01, lg);
+                    const V3 cp = contract(*sc, wp);
+                    base_forward(d, cp, bo, d01);
+                    head_forward(d, bo + net->latent_offset, d01, lg, nullptr, &cp);
                     ++ns;
                     if (composite(std::exp(bo[0]), lg, dt, sc->alpha_thre, rgb, T)) break;
                 }
@@ -1226,14 +1242,15 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                         init01[2] = (float)((vz / nv + 1.0) / 2.0);
                     }
                     double sigma, lg[3];
+                    const V3 cp = contract(*sc, at(r, tmh)); /* the head's network input position */
                     if (kind == 1 && cc->basic) {
-                        head_forward(d, blat, d01, lg, init01);
+                        head_forward(d, blat, d01, lg, init01, &cp);
                         sigma = bsigma;
                         ++n_cache;
                     } else if (kind == 0) {
                         double bo[64];
-                        base_forward(d, contract(*sc, at(r, tmh)), bo, d01);
-                        head_forward(d, bo + net->latent_offset, d01, lg);
+                        base_forward(d, cp, bo, d01);
+                        head_forward(d, bo + net->latent_offset, d01, lg, nullptr, &cp);
                         sigma = std::exp(bo[0]);
                         ++n_res;
                     } else {
@@ -1268,10 +1285,10 @@ int orc_render_cached(const OrcNet *net, const OrcScene *sc, const OrcSteps *st,
                             /* DensityIntermediates (:776-781): latent 0 is the density,
                              * log(sum w density) enters the head and gives sigma */
                             lat[0] = net->mimic_fp16 ? round_h(std::log(lsum[0])) : std::log(lsum[0]);
-                            head_forward(d, lat, d01, lg, init01);
+                            head_forward(d, lat, d01, lg, init01, &cp);
                             sigma = std::exp(lat[0]);
                         } else {
-                            head_forward(d, lat, d01, lg, init01);
+                            head_forward(d, lat, d01, lg, init01, &cp);
                             sigma = std::max(dsum, 1e-6);
                         }
                         ++n_cache;

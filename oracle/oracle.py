@@ -43,7 +43,7 @@ class OrcNet(C.Structure):
                 ("table", C.c_void_p), ("width", C.c_int), ("enc_w", C.c_int), ("enc_w_pad", C.c_int),
                 ("base_out_pad", C.c_int), ("base_w", C.c_void_p), ("head_layers", C.c_int), ("head_in", C.c_int),
                 ("head_in_pad", C.c_int), ("n_latents", C.c_int), ("latent_offset", C.c_int), ("head_w", C.c_void_p),
-                ("mimic_fp16", C.c_int), ("view_dependent", C.c_int), ("first_w", C.c_void_p)]
+                ("mimic_fp16", C.c_int), ("view_dependent", C.c_int), ("first_w", C.c_void_p), ("freq_deg", C.c_int)]
 
 
 class OrcCacheDims(C.Structure):
@@ -240,6 +240,7 @@ class OracleModel:
         n.mimic_fp16 = int(mimic_fp16)
         n.view_dependent = int(self.view_dependent)
         n.first_w = ptr(self.first_w)
+        n.freq_deg = int(head.get("freq_encoding_degree", 0))
         self.net = n
 
     # -- evaluation --------------------------------------------------------

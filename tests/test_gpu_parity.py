@@ -161,10 +161,12 @@ def _cache_setup(loader, cam):
 
 
 @pytest.mark.parametrize("fixture,W,H", [("model1", 64, 48), ("model3", 48, 40)])
-def test_cache_build_parity(request, fixture, W, H):
+@pytest.mark.parametrize("build_tc", [False, True], ids=["build_mma_sync", "build_tcgen05"])
+def test_cache_build_parity(request, fixture, W, H, build_tc):
     loader, om, _ = request.getfixturevalue(fixture)
     cam = small_camera(1001, W, H)
     r, c0, c1 = _cache_setup(loader, cam)
+    r.set_build_network_path(build_tc)
     r.initCacheBlockwise(fvc.raymarch_info(cam, loader.stepsize_info))
     packed, known, vox = c1.read()
     oc = om.cache_build(cam)
