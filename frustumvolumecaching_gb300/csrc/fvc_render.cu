@@ -877,12 +877,17 @@ __global__ void __launch_bounds__(NET_WARPS * 32, 2) wf_net_cache_kernel(RenderP
  * with tcgen05.ld, applies ReLU / fp16 rounding and writes the next layer's
  * operand. */
 struct __align__(128) TcSmem {
-    uint8_t W[TCF_WBYTES]; /* TC_WBYTES used unless the head has the frequency encoding */
     uint8_t X[128 * 64 * 2];
     float bias3[64];
     uint64_t mbar;
     uint32_t tmem_base;
+    /* the weight tiles, last: a head with the frequency encoding (TCF_WBYTES) launches with the extra
+     * bytes past the struct (tc_smem_bytes), the others keep the smaller footprint, so that 5 CTAs
+     * leave the SM its larger L1 share for the hash gathers */
+    __align__(128) uint8_t W[TC_WBYTES];
 };
+/* dynamic shared memory of a TcSmem launch */
+static inline size_t tc_smem_bytes(int freq) { return sizeof(TcSmem) + (freq ? (size_t)(TCF_WBYTES - TC_WBYTES) : 0); }
 
 constexpr long long TC_WAIT_LIMIT = 2000000000ll; /* ~1 s of SM clocks */
 constexpr int TC_COLS = 64;
@@ -1990,7 +1995,7 @@ static cudaError_t set_net_attrs()
     cudaError_t e = cudaFuncSetAttribute(wf_net_resample_kernel<HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_resample_kernel<HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_cache_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    const int tsmem = (int)sizeof(TcSmem);
+    const int tsmem = (int)tc_smem_bytes(1); /* the largest launch (a head with the frequency encoding) */
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<0, HH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(wf_net_tc_kernel<1, HH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tsmem);
@@ -2026,7 +2031,7 @@ static inline bool fused_cached_path(const RenderParams &p)
 template <int HH>
 static void launch_plain_net(const RenderParams &p, int it, int n_sms, cudaStream_t s)
 {
-    const size_t tc_smem = sizeof(TcSmem);
+    const size_t tc_smem = tc_smem_bytes(p.freq);
     const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
     if (p.view_dependent) wf_net_vd_kernel<0, HH, false><<<n_sms * 4, 128, sizeof(VdSmem), s>>>(p, it);
     else if (!p.use_tc) wf_net_resample_kernel<HH, false><<<n_sms * 2, NET_WARPS * 32, sizeof(NetSmem), s>>>(p, it);
@@ -2064,7 +2069,7 @@ static cudaError_t run_frame(const RenderParams &p, int n_sms, cudaStream_t s, i
     const int grid_ray = n_sms * FVC_RAY_BLOCKS_PER_SM;
     const int grid_net = n_sms * 2;
     const size_t net_smem = sizeof(NetSmem);
-    const size_t tc_smem = sizeof(TcSmem);
+    const size_t tc_smem = tc_smem_bytes(p.freq);
     const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM; /* <= 8 CTAs x 64 TMEM columns per SM */
     const bool fused = CACHED && fused_cached_path(p);
     int it = 0;
@@ -2195,7 +2200,7 @@ static cudaError_t run_backward(const RenderParams &p, const BwdParams &b, int n
         wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
         /* the forward kernels of pass 1, so both passes composite the same values */
         if (CACHED) {
-            const size_t tc_smem = sizeof(TcSmem);
+            const size_t tc_smem = tc_smem_bytes(p.freq);
             const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
             launch_classify(p, it, n_sms, s);
             if (p.use_tc) {
@@ -2294,13 +2299,13 @@ static cudaError_t build_batch_graph_t(const RenderParams &p, int n_sms, cudaStr
             if (fused) {
                 wf_march_kernel<true, true><<<grid_ray, 128, 0, s>>>(p, it);
                 wf_cache_lookup_kernel<<<n_sms * 8, 256, 0, s>>>(p, it);
-                wf_net_tc_kernel<2, HH, false><<<n_sms * FVC_TC_CTAS_PER_SM, 128, sizeof(TcSmem), s>>>(p, it);
+                wf_net_tc_kernel<2, HH, false><<<n_sms * FVC_TC_CTAS_PER_SM, 128, tc_smem_bytes(p.freq), s>>>(p, it);
                 kernels += 2;
             } else {
                 wf_march_kernel<CACHED><<<grid_ray, 128, 0, s>>>(p, it);
             }
             if (CACHED && !fused) {
-                const size_t tc_smem = sizeof(TcSmem);
+                const size_t tc_smem = tc_smem_bytes(p.freq);
                 const int grid_tc = n_sms * FVC_TC_CTAS_PER_SM;
                 launch_classify(p, it, n_sms, s);
                 if (p.view_dependent) {
