@@ -37,6 +37,7 @@ def main(argv=None) -> None:
     ap.add_argument("--skip", action="store_true", help="empty-space skipping in the march (off by default, as in the library)")
     ap.add_argument("--scene", choices=["c2", "c1"], default="c2",
                     help="c2: the cached workload's scene and camera path; c1: the 256x256 workload's scene, seeded camera")
+    ap.add_argument("--build-tc", action="store_true", help="cache builds' density network on tcgen05 (default mma.sync)")
     ap.add_argument("--separate-classify", action="store_true",
                     help="cached path: the classification pass and two row lists instead of the classifying march")
     args = ap.parse_args(argv)
@@ -66,6 +67,7 @@ def main(argv=None) -> None:
     r.set_empty_space_skipping(args.skip)
     if args.path == "cached":
         r.set_fused_classify(not args.separate_classify)
+        r.set_build_network_path(args.build_tc)
     r.set_kernel_timing(True)
     for i, info in enumerate(infos):
         build = None
