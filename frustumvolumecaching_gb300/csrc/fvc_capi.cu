@@ -558,8 +558,6 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
      * follow the SH inputs of the head (:241-246) */
     m.freq = (int)head.num_or("freq_encoding_degree", 0);
     if (m.freq != 0 && m.freq != 4) return fail(FVC_ERR_CONFIG, "freq_encoding_degree must be 0 or 4");
-    if (m.freq && m.view_dependent)
-        return fail(FVC_ERR_CONFIG, "the frequency encoding is built for the color head without mlp_first_head");
     const int head_in = (int)head.num_or("n_input", (m.view_dependent ? 32 : 16) + m.n_latents + 6 * m.freq);
     const int head_in_pad = (head_in + 15) / 16 * 16;
     m.head_hidden = (int)head["network"].num_or("n_hidden_layers", 2);
@@ -570,8 +568,10 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
             return fail(FVC_ERR_CONFIG, "mlp_first_head must be 32 -> 64 -> n_output (1 hidden layer of 64)");
         if (m.n_latents != 8 || m.latent_offset + m.n_latents > 16 || (n_out + 15) / 16 != 1 || (int)fh.num_or("n_input", 32) != 32)
             return fail(FVC_ERR_CONFIG, "mlp_first_head must map the 16 density outputs and 16 SH values to 8 latents");
-        if (head_in != m.n_latents + 32 || head_in_pad != 48)
+        if (!m.freq && (head_in != m.n_latents + 32 || head_in_pad != 48))
             return fail(FVC_ERR_CONFIG, "a view-dependent head input must be n_latents + 16 SH + 16 SH differences padded to 48");
+        if (m.freq && (head_in != m.n_latents + 32 + 24 || head_in_pad != 64))
+            return fail(FVC_ERR_CONFIG, "a view-dependent head with the frequency encoding must read n_latents + 16 SH + 16 SH differences + 24 frequency values (64)");
         const JVal &fn = fh["encoding"]["nested"];
         if (fn.kind == JVal::ARR && fn.arr.size() && (int)fn.arr[0].num_or("degree", 4) != 4)
             return fail(FVC_ERR_CONFIG, "only SH degree 4 direction encoding is built");
@@ -729,7 +729,8 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         std::vector<uint2> Wf(W_L3, make_uint2(0, 0));
         frag_pack(u16(*wf, 0, 64 * 32), 64, 32, &Wf[W_L1]);
         frag_pack(u16(*wf, 64 * 32, 16 * 64), 16, 64, &Wf[W_L2]);
-        std::vector<uint8_t> Wv(VD_WBYTES, 0);
+        const int vd_bytes = m.freq ? VDF_WBYTES : VD_WBYTES;
+        std::vector<uint8_t> Wv(vd_bytes, 0);
         auto vd_pack = [&](const std::vector<uint16_t> &M, int N, int K, int off) {
             for (int n = 0; n < N; ++n)
                 for (int k = 0; k < K; ++k) memcpy(&Wv[off + kmajor_offset(n, k, K)], &M[(size_t)n * K + k], 2);
@@ -740,18 +741,18 @@ static int build_model(const JVal &cfg, std::vector<char> &tab, std::vector<char
         vd_pack(w2, 16, 64, VD_B2);
         vd_pack(u16(*wf, 0, 64 * 32), 64, 32, VD_F1);
         vd_pack(u16(*wf, 64 * 32, 16 * 64), 16, 64, VD_F2);
-        vd_pack(u16(wh, 0, 64 * 48), 64, 48, VD_B3);
-        size_t vo = 64 * 48;
+        vd_pack(u16(wh, 0, (size_t)64 * head_in_pad), 64, head_in_pad, VD_B3);
+        size_t vo = (size_t)64 * head_in_pad;
         if (m.head_hidden == 2) {
-            vd_pack(u16(wh, vo, 64 * 64), 64, 64, VD_B4);
+            vd_pack(u16(wh, vo, 64 * 64), 64, 64, m.freq ? VDF_B4 : VD_B4);
             vo += 64 * 64;
         }
-        vd_pack(u16(wh, vo, 16 * 64), 16, 64, VD_B5);
+        vd_pack(u16(wh, vo, 16 * 64), 16, 64, m.freq ? VDF_B5 : VD_B5);
         int rc;
         if ((rc = dalloc(&m.d_weights_fh, Wf.size(), "first-head weights"))) return rc;
-        if ((rc = dalloc(&m.d_weights_vd, (size_t)VD_WBYTES, "view-dependent weights"))) return rc;
+        if ((rc = dalloc(&m.d_weights_vd, (size_t)vd_bytes, "view-dependent weights"))) return rc;
         CU(cudaMemcpy(m.d_weights_fh, Wf.data(), Wf.size() * sizeof(uint2), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(m.d_weights_vd, Wv.data(), VD_WBYTES, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.d_weights_vd, Wv.data(), vd_bytes, cudaMemcpyHostToDevice));
     }
 
     /* device scene block */

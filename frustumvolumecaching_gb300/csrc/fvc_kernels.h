@@ -95,6 +95,11 @@ constexpr int VD_B3 = 12288;    /* 64 x 48 */
 constexpr int VD_B4 = 18432;    /* 64 x 64 */
 constexpr int VD_B5 = 26624;    /* 16 x 64 */
 constexpr int VD_WBYTES = 28672;
+/* with the positional frequency encoding the color head reads [latents 8 | SH 16 | SH difference 16 |
+ * frequency 24] (K = 64, no padding): its tiles shift */
+constexpr int VDF_B4 = 20480;   /* 64 x 64 (VD_B3 holds 64 x 64) */
+constexpr int VDF_B5 = 28672;   /* 16 x 64 */
+constexpr int VDF_WBYTES = 30720;
 /* the same in e4m3 (8-bit K-major tiles) for the FP8 network */
 constexpr int TC8_B1 = 0, TC8_B2 = 2048, TC8_B3 = 3072, TC8_B4 = 5120, TC8_B5 = 9216, TC8_WBYTES = 10240;
 

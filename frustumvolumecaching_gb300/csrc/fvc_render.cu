@@ -1845,7 +1845,7 @@ __global__ void wf_reset_rows_kernel(RenderParams p, int cached)
  *     give the bias.
  * 45 KB of shared memory: four CTAs per SM. */
 struct __align__(128) VdSmem {
-    uint8_t W[VD_WBYTES];
+    uint8_t W[VDF_WBYTES]; /* VD_WBYTES unless the head has the frequency encoding */
     uint8_t X[128 * 64 * 2];
     uint64_t mbar;
     uint32_t tmem_base;
@@ -1872,10 +1872,14 @@ __global__ void __launch_bounds__(128, 4) wf_net_vd_kernel(RenderParams p, int i
     const int n_rows = MODE == 0 ? (LIST ? p.counters[3] : p.counters[2]) : p.counters[4];
     if (n_rows == 0) return;
     const int tid = threadIdx.x, warp = tid >> 5;
+    /* the color head's input: K = 48 with the 1-padding, or K = 64 with the frequency encoding */
+    const int HK = p.freq ? 64 : 48;
+    const int wb4 = p.freq ? VDF_B4 : VD_B4, wb5 = p.freq ? VDF_B5 : VD_B5;
     if (tid == 0) {
+        const int wbytes = p.freq ? VDF_WBYTES : VD_WBYTES;
         mbar_init(&S.mbar, 1);
-        mbar_arrive_expect_tx(&S.mbar, VD_WBYTES);
-        bulk_copy_g2s(S.W, p.weights_vd, VD_WBYTES, &S.mbar);
+        mbar_arrive_expect_tx(&S.mbar, wbytes);
+        bulk_copy_g2s(S.W, p.weights_vd, wbytes, &S.mbar);
     }
     if (warp == 0) tmem_alloc(&S.tmem_base, TC_COLS);
     tc_fence_before();
@@ -1953,23 +1957,44 @@ __global__ void __launch_bounds__(128, 4) wf_net_vd_kernel(RenderParams p, int i
                 diff1 = *reinterpret_cast<const uint4 *>(df + 4);
             }
         }
-        /* ---- color head input [latents | SH | SH difference | 1-padding] (K = 48) ---- */
-        st_chunk(S.X, tid, 0, 48, lat);
-        st_chunk(S.X, tid, 1, 48, *reinterpret_cast<const uint4 *>(sh));
-        st_chunk(S.X, tid, 2, 48, *reinterpret_cast<const uint4 *>(sh + 4));
-        st_chunk(S.X, tid, 3, 48, diff0);
-        st_chunk(S.X, tid, 4, 48, diff1);
-        st_chunk(S.X, tid, 5, 48, make_uint4(one2, one2, one2, one2));
+        /* ---- color head input [latents | SH | SH difference | 1-padding or frequency encoding] ---- */
+        st_chunk(S.X, tid, 0, HK, lat);
+        st_chunk(S.X, tid, 1, HK, *reinterpret_cast<const uint4 *>(sh));
+        st_chunk(S.X, tid, 2, HK, *reinterpret_cast<const uint4 *>(sh + 4));
+        st_chunk(S.X, tid, 3, HK, diff0);
+        st_chunk(S.X, tid, 4, HK, diff1);
+        if (p.freq) {
+            /* the frequency encoding of the row's network input position (include/nerf_network.h:55-81,
+             * src/my_fully_fused_mlp.cu:20-100) */
+            uint4 fx = make_uint4(0u, 0u, 0u, 0u), fy = fx, fz = fx;
+            if (r >= 0) {
+                float3 q;
+                if (MODE == 1) {
+                    q = cache_row_position(p, states, r);
+                } else {
+                    const float4 pw = p.row_pay[r];
+                    q = make_float3(pw.x, pw.y, pw.z);
+                }
+                fx = freq_chunk(q.x);
+                fy = freq_chunk(q.y);
+                fz = freq_chunk(q.z);
+            }
+            st_chunk(S.X, tid, 5, HK, fx);
+            st_chunk(S.X, tid, 6, HK, fy);
+            st_chunk(S.X, tid, 7, HK, fz);
+        } else {
+            st_chunk(S.X, tid, 5, HK, make_uint4(one2, one2, one2, one2));
+        }
         if (!(ok = tc_publish(ok))) break;
-        ok = vd_run(S, tmem, S.W + VD_B3, 48, 64, phase);
+        ok = vd_run(S, tmem, S.W + VD_B3, HK, 64, phase);
         epi_hidden(tmem + lane_base, nullptr, S.X, tid);
         if (!(ok = tc_publish(ok))) break;
         if (HH == 2) {
-            ok = vd_run(S, tmem, S.W + VD_B4, 64, 64, phase);
+            ok = vd_run(S, tmem, S.W + wb4, 64, 64, phase);
             epi_hidden(tmem + lane_base, nullptr, S.X, tid);
             if (!(ok = tc_publish(ok))) break;
         }
-        ok = vd_run(S, tmem, S.W + VD_B5, 64, 16, phase);
+        ok = vd_run(S, tmem, S.W + wb5, 64, 16, phase);
         float o[16];
         tmem_ld16(tmem + lane_base, o);
         tmem_wait_ld();

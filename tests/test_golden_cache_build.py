@@ -68,3 +68,42 @@ def test_oracle_cache_build_matches_reference_kernels(case):
     np.testing.assert_array_equal(own.packed_index >= 0, ref_set)
     ulp = np.abs(own.known_ranges.view(np.int32).astype(np.int64) - g[f"{name}/known"].reshape(-1).view(np.int32).astype(np.int64))
     assert int(ulp.max()) <= 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_device_cache_build_matches_reference_kernels(case):
+    """The device's blockwise build against the same golden vectors: which
+    bricks hold a slot, the bricks demanded and each brick's set voxels
+    exactly; known ranges within 2 ulp (the device's step grid uses
+    fvc_detmath.h, the golden run libm); latents and densities within fp16
+    rounding (the device's network accumulates in float32, the golden's
+    outputs are the float64 network rounded)."""
+    import frustumvolumecaching_gb300 as fvc
+
+    name, seed, nlvl, cam_seed, radius, W, H, variant = case
+    g = np.load(GOLDEN)
+    loader = fvc.load_data(fmodel.ensure_model(fmodel.spec_tiny(seed=seed, nlvl=nlvl)))
+    cam = fcam.seeded_camera(cam_seed, radius=radius, width=W, height=H)
+    c0, c1 = fvc.Cache(), fvc.Cache()
+    r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
+    r.resizeCache((W, H), loader.stepsize_info)
+    r.setCacheSettings(fvc.default_cache_settings(variant))
+    r.initCacheBlockwise(fvc.raymarch_info(cam, loader.stepsize_info))
+    packed, known, vox = c1.read()
+    ref_set = g[f"{name}/brick_set"].astype(bool)
+    np.testing.assert_array_equal(packed.ravel() >= 0, ref_set)
+    assert r._init_stats.n_bricks_demanded == int(g[f"{name}/demanded"])
+    ulp = np.abs(known.ravel().view(np.int32).astype(np.int64) - g[f"{name}/known"].reshape(-1).view(np.int32).astype(np.int64))
+    assert int(ulp.max()) <= 2
+    p = packed.ravel()[ref_set]
+    _, _, (dX, dY, dZ) = c1.dims()
+    slots = (((p >> 20) & 1023) * dY + ((p >> 10) & 1023)) * dZ + (p & 1023)
+    v = vox.reshape(-1, 512, 8)[slots]  # [bricks, 512, 8] u32 words: density, isset, 2 pad, 8 fp16 latents
+    isset = v[..., 1].view(np.float32) > 0
+    np.testing.assert_array_equal(isset, np.unpackbits(g[f"{name}/isset"], axis=1, count=512).astype(bool))
+    lat = np.ascontiguousarray(v[..., 4:8][isset]).view(np.uint16).reshape(-1, 8).view(np.float16).astype(np.float32)
+    ref_lat = g[f"{name}/latents"].view(np.float16).astype(np.float32)
+    assert float(np.abs(lat - ref_lat).max()) < 2e-3
+    dens = v[..., 0].view(np.float32)[isset]
+    np.testing.assert_allclose(dens, g[f"{name}/density"], rtol=2e-3, atol=1e-6)

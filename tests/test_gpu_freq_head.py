@@ -4,7 +4,8 @@ encoding of the network's input position appended after the SH inputs,
 :55-81,241-246) against the float64 oracle.
 
 The head reads [latents | SH of the direction | sin, cos(pi 2^k p) per axis,
-k < 4] (48 inputs).  A resampled row's position is its contracted sample
+k < 4] (48 inputs); a view-dependent split head also the SH difference to
+the initial direction before them (64 inputs).  A resampled row's position is its contracted sample
 point; a cache row's is the contracted point at its network-input midpoint
 (src/cache_performance_renderer.cu:284-297).  Bit-exact: sample counts,
 classification, brick slots and known ranges.  Within tolerance: pixel
@@ -26,15 +27,19 @@ COLOR_ATOL = 2e-3
 FVC_ERR_CONFIG = 2
 
 
-def _spec(nlvl: int, head_hidden: int = 2):
+def _spec(nlvl: int, head_hidden: int = 2, view_dependent: bool = False):
     spec = fmodel.spec_tiny(seed=41, nlvl=nlvl)
     spec.freq_encoding_degree = 4
     spec.head_hidden_layers = head_hidden
+    spec.view_dependent = view_dependent
     spec.name = f"{spec.name}_h{head_hidden}"
     return spec
 
 
-@pytest.fixture(scope="module", params=[(1, 2), (3, 2), (1, 1)], ids=["c1", "c3", "c1_head1"])
+# the view-dependent case is the reference's custom split head with FREQ_ENC_DEGREE 4
+# (src/my_fully_fused_mlp.cu:1358-1421): [latents | SH | SH difference | frequency], 64 inputs
+@pytest.fixture(scope="module", params=[(1, 2, False), (3, 2, False), (1, 1, False), (1, 1, True), (3, 2, True)],
+                ids=["c1", "c3", "c1_head1", "c1_viewdep_head1", "c3_viewdep"])
 def freq_model(request):
     d = fmodel.ensure_model(_spec(*request.param))
     return fvc.load_data(d), orc.OracleModel(d, mimic_fp16=True)
@@ -49,7 +54,7 @@ def _rotated(cam0, W, H, deg=1.0):
 
 def test_plain_render(freq_model):
     loader, om = freq_model
-    assert om.net.freq_deg == 4 and om.net.head_in == 48
+    assert om.net.freq_deg == 4 and om.net.head_in == (64 if om.view_dependent else 48)
     W, H = 48, 40
     cam = small_camera(1001, W, H)
     r = fvc.PerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network)
@@ -74,6 +79,8 @@ def test_plain_render(freq_model):
 @pytest.mark.parametrize("fused", [True, False], ids=["march_classifies", "classify_pass"])
 def test_cache_build_and_cached_render(freq_model, fused):
     loader, om = freq_model
+    if om.view_dependent and not fused:
+        pytest.skip("view-dependent models always take the classification pass")
     W, H = 48, 40
     cam0 = small_camera(1001, W, H)
     c0, c1 = fvc.Cache(), fvc.Cache()
