@@ -349,14 +349,24 @@ __device__ __forceinline__ float3 contract(const DevScene &sc, float3 p)
     return p;
 }
 
-/* cam2froxel, include/raymarch_common.h:316-329 */
-__device__ __forceinline__ float3 cam2froxel(float3 c, const DevCam &cam, const DevSteps &st, float &t)
+/* cam2froxel, include/raymarch_common.h:316-329, in two parts: the image
+ * coordinates and the distance t, and the depth coordinate (the step index
+ * of t, the costly part), which a caller can leave until it needs it */
+__device__ __forceinline__ float2 cam2froxel_xy(float3 c, const DevCam &cam, float &t)
 {
     const float sgn = cam.gl ? -1.f : 1.f;
     const float z = F_MUL(c.z, sgn), rz = __frcp_rn(z);
     t = F_SQRT(dot3(c, c));
-    return make_float3(F_ADD(F_MUL(div_rn_by(c.x, z, rz), cam.fx), cam.px), F_ADD(F_MUL(div_rn_by(F_MUL(c.y, sgn), z, rz), cam.fy), cam.py),
-                       F_MUL(F_SUB(step_from_t(st, t), st.near_i), c.z < 0.0f ? -1.0f : 1.0f));
+    return make_float2(F_ADD(F_MUL(div_rn_by(c.x, z, rz), cam.fx), cam.px), F_ADD(F_MUL(div_rn_by(F_MUL(c.y, sgn), z, rz), cam.fy), cam.py));
+}
+__device__ __forceinline__ float froxel_z(const DevSteps &st, float t, float cz)
+{
+    return F_MUL(F_SUB(step_from_t(st, t), st.near_i), cz < 0.0f ? -1.0f : 1.0f);
+}
+__device__ __forceinline__ float3 cam2froxel(float3 c, const DevCam &cam, const DevSteps &st, float &t)
+{
+    const float2 xy = cam2froxel_xy(c, cam, t);
+    return make_float3(xy.x, xy.y, froxel_z(st, t, c.z));
 }
 
 /* --------------------------------------------------------------------- */

@@ -247,16 +247,23 @@ __global__ void wf_loop_cond_kernel(RenderParams p, cudaGraphConditionalHandle h
 /* Why a sample lies outside the cache's sampled region (REASON_*), or 0
  * when it lies inside: the frustum and known-range tests of
  * sample_cache_performance_kernel (src/cache_performance_renderer.cu:91-122),
- * which both cache renderers share.  The sample is outside when any test
- * fails; the reason named is the first failing one in the order image, near
- * plane, known range, froxel depth. */
-__device__ __forceinline__ int unsampled_reason(const CacheView &C, const DevSteps &cst, float3 fr, float tfr)
+ * which both cache renderers share, for the point c in the cache camera's
+ * frame.  The sample is outside when any test fails; the reason named is the
+ * first failing one in the order image, near plane, known range, froxel
+ * depth.  The froxel depth (the step index of t, a logarithm) is computed
+ * only for a sample that passes the first three.  fr receives the froxel
+ * point (its z only past those tests), tfr the distance. */
+__device__ __forceinline__ int unsampled_reason_at(const CacheView &C, const DevCam &ccam, const DevSteps &cst, float3 c, float3 &fr,
+                                                   float &tfr)
 {
-    const bool in_fov = fr.x >= 0.f && fr.x < (float)C.fW && fr.y >= 0.f && fr.y < (float)C.fH;
+    const float2 xy = cam2froxel_xy(c, ccam, tfr);
+    fr = make_float3(xy.x, xy.y, 0.f);
+    const bool in_fov = xy.x >= 0.f && xy.x < (float)C.fW && xy.y >= 0.f && xy.y < (float)C.fH;
     if (!in_fov) return REASON_OUTSIDE_FOV;
-    const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(fr.y) * C.fW + (int)floorf(fr.x));
+    const float kr = __ldg(C.known_ranges + (size_t)(int)floorf(xy.y) * C.fW + (int)floorf(xy.x));
     if (tfr < cst.near_) return REASON_BEFORE_NEAR;
     if (tfr > kr) return REASON_BEYOND_KNOWN;
+    fr.z = froxel_z(cst, tfr, c.z);
     if (!(fr.z >= 0.f && fr.z < (float)C.fD)) return REASON_OUTSIDE_DEPTH;
     return REASON_NONE;
 }
@@ -268,8 +275,8 @@ __device__ __forceinline__ int classify(const RenderParams &p, const CacheView &
                                         float3 oc, float3 dc, float tm)
 {
     float tfr;
-    const float3 fr = cam2froxel(at(oc, dc, tm), ccam, cst, tfr);
-    const int why = unsampled_reason(C, cst, fr, tfr);
+    float3 fr;
+    const int why = unsampled_reason_at(C, ccam, cst, at(oc, dc, tm), fr, tfr);
     if (why) return (p.render_mode == 1 ? KIND_SKIP : KIND_RESAMPLE) | (why << 2);
     if (p.render_mode == 2) return KIND_SKIP;
     const int bx = (int)F_MUL(fr.x, 0.125f), by = (int)F_MUL(fr.y, 0.125f), bz = (int)F_MUL(fr.z, 0.125f);
@@ -321,8 +328,8 @@ __device__ __forceinline__ int classify_basic(const RenderParams &p, const Cache
                                               float3 oc, float3 dc, float tm, float dt, float (&lat)[8], float &density)
 {
     float tfr;
-    const float3 fr = cam2froxel(at(oc, dc, tm), ccam, cst, tfr);
-    const int why = unsampled_reason(C, cst, fr, tfr);
+    float3 fr;
+    const int why = unsampled_reason_at(C, ccam, cst, at(oc, dc, tm), fr, tfr);
     if (why) return KIND_RESAMPLE | (why << 2);
     /* froxel2data */
     const int bx = (int)F_MUL(fr.x, 0.125f), by = (int)F_MUL(fr.y, 0.125f), bz = (int)F_MUL(fr.z, 0.125f);
