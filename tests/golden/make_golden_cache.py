@@ -1,9 +1,12 @@
-"""Regenerates tests/golden/cache_build.npz from the reference's own blockwise
-cache-build kernels (initPayloads_cache_init_kernel through
-writeImageBuffer_cache_init_kernel2, src/cache_renderer.cu:18-569), run on
-the host by oracle/_ref/libref_cache_build.so (oracle/Makefile, target
-``ref``) under the host loop of CacheRenderer::initCacheBlockwise
-(src/cache_renderer.cu:931-1041).
+"""Regenerates tests/golden/cache_build.npz from the reference's own cache-build
+kernels run on the host: the blockwise build (initPayloads_cache_init_kernel
+through writeImageBuffer_cache_init_kernel2, src/cache_renderer.cu:18-569,
+under the host loop of CacheRenderer::initCacheBlockwise, :931-1041) by
+oracle/_ref/libref_cache_build.so, and the per-ray fill (the payload,
+compaction and sampling kernels of src/renderer.cu and
+accumulate_cache_init_first_kernel .. writeImageBuffer_cache_init_kernel,
+src/cache_renderer.cu:571-830, under CacheRenderer::initCache, :848-928) by
+oracle/_ref/libref_cache_fill.so (oracle/Makefile, target ``ref``).
 
 Run from the repository root where the reference tree is available:
     make -C oracle ref REF=<reference checkout>
@@ -30,6 +33,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 LIB = os.path.join(ROOT, "oracle", "_ref", "libref_cache_build.so")
+FILL_LIB = os.path.join(ROOT, "oracle", "_ref", "libref_cache_fill.so")
 
 # (name, model seed, cascades, camera seed, camera radius, W, H, interpol_variant); the cameras lie inside the
 # scene box: the reference sizes the frustum depth for that (resizeCache) and writes past its brick arrays otherwise
@@ -110,6 +114,48 @@ def run_case(lib, om, cam, W, H, variant):
     }
 
 
+def run_fill_case(lib, om, cam, W, H, variant):
+    """The per-ray fill (CacheRenderer::initCache, src/cache_renderer.cu:848-928) through the reference's
+    kernels in oracle/_ref/libref_cache_fill.so; the same outputs as run_case."""
+    sci, f = scene_params(om, cam)
+    dims = om.cache_dims(W, H)
+    data_bricks = np.asarray([dims.dX, dims.dY, dims.dZ], np.int32)
+    assert lib.rcf_init(sci.ctypes.data, f.ctypes.data, W, H, om.bits.ctypes.data, data_bricks.ctypes.data,
+                        int(om.net.latent_offset), variant) == W * H
+    fr = np.zeros(6, np.int32)
+    lib.rcf_dims(fr.ctypes.data)
+    iters = 0
+    while True:
+        pp = C.POINTER(C.c_float)()
+        batch = C.c_int(0)
+        rows = lib.rcf_search(C.byref(pp), C.byref(batch))
+        if rows <= 0:
+            break
+        pos = np.ctypeslib.as_array(pp, shape=(rows * 3,)).reshape(rows, 3).copy()
+        bo = om.base_outputs(pos, np.full((rows, 3), 0.5, np.float32))
+        out = np.zeros((bo.shape[1], batch.value), np.float16)
+        out[:, :rows] = bo.T.astype(np.float32).astype(np.float16)
+        assert lib.rcf_accumulate(out.view(np.uint16).ctypes.data) == 0
+        iters += 1
+    bX, bY, bZ = int(fr[3]), int(fr[4]), int(fr[5])
+    packed = np.zeros(bX * bY * bZ, np.int32)
+    known = np.zeros(int(fr[0]) * int(fr[1]), np.float32)
+    oob = C.c_longlong(0)
+    demanded = lib.rcf_finish(packed.ctypes.data, known.ctypes.data, C.byref(oob))
+    n_set = int((packed >= 0).sum())
+    isset = np.zeros((n_set, 512), np.float32)
+    dens = np.zeros((n_set, 512), np.float32)
+    lat = np.zeros((n_set, 512, 8), np.uint16)
+    assert lib.rcf_bricks(isset.ctypes.data, dens.ctypes.data, lat.ctypes.data) == n_set
+    vox = isset > 0
+    return {
+        "frustum": fr[:3].copy(), "bricks": fr[3:].copy(), "brick_set": (packed >= 0).astype(np.uint8),
+        "known": known.reshape(int(fr[1]), int(fr[0])), "demanded": np.int32(demanded), "iterations": np.int32(iters),
+        "out_of_range_writes": np.int64(oob.value), "isset": np.packbits(vox, axis=1),
+        "density": dens[vox], "latents": lat[vox], "variant": np.int32(variant),
+    }
+
+
 def main():
     lib = C.CDLL(LIB)
     V, I = C.c_void_p, C.c_int
@@ -129,6 +175,22 @@ def main():
             arrays[f"{name}/{k}"] = v
         print(f"{name}: {int(r['brick_set'].sum())} bricks, {int(r['demanded'])} demanded, {int(r['iterations'])} iterations, "
               f"{r['density'].size} voxels set, {int(r['out_of_range_writes'])} out-of-range writes")
+    fill = C.CDLL(FILL_LIB)
+    fill.rcf_init.argtypes = [V, V, I, I, V, V, I, I]
+    fill.rcf_dims.argtypes = [V]
+    fill.rcf_search.argtypes = [C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.c_int)]
+    fill.rcf_accumulate.argtypes = [V]
+    fill.rcf_finish.argtypes = [V, V, C.POINTER(C.c_longlong)]
+    fill.rcf_bricks.argtypes = [V, V, V]
+    for fn in (fill.rcf_init, fill.rcf_search, fill.rcf_accumulate, fill.rcf_finish, fill.rcf_bricks):
+        fn.restype = I
+    for name, seed, nlvl, cam_seed, radius, W, H, variant in CASES:
+        om, cam = case_inputs(seed, nlvl, cam_seed, radius, W, H)
+        r = run_fill_case(fill, om, cam, W, H, variant)
+        for k, v in r.items():
+            arrays[f"fill_{name}/{k}"] = v
+        print(f"per-ray fill {name}: {int(r['brick_set'].sum())} bricks, {int(r['demanded'])} demanded, "
+              f"{int(r['iterations'])} iterations, {r['density'].size} voxels set, {int(r['out_of_range_writes'])} out-of-range writes")
     np.savez_compressed(os.path.join(HERE, "cache_build.npz"), **arrays)
 
 

@@ -1,8 +1,10 @@
-"""The oracle's blockwise cache build against golden vectors from the
-reference's own build kernels (tests/golden/cache_build.npz, made by
-tests/golden/make_golden_cache.py from initPayloads_cache_init_kernel ..
-writeImageBuffer_cache_init_kernel2, src/cache_renderer.cu:18-569, with the
-oracle's density network rounded to fp16 between them).
+"""The oracle's cache builds against golden vectors from the reference's own
+build kernels (tests/golden/cache_build.npz, made by
+tests/golden/make_golden_cache.py: the blockwise build from
+initPayloads_cache_init_kernel .. writeImageBuffer_cache_init_kernel2,
+src/cache_renderer.cu:18-569; the per-ray fill from the payload, compaction
+and sampling kernels of src/renderer.cu and src/cache_renderer.cu:571-830;
+with the oracle's density network rounded to fp16 between them).
 
 Compared per case (no overflow, so the reference's set of bricks is
 deterministic; its slots come from atomicAdd and are not compared):
@@ -34,15 +36,28 @@ CASES = [
 ]
 
 
+BUILDS = ["blockwise", "per_ray"]
+
+
+def _build(om, cam, variant, builder):
+    return om.cache_build(cam, variant=variant) if builder == "blockwise" else om.cache_build_per_ray(cam, variant=variant)
+
+
+@pytest.mark.parametrize("builder", BUILDS)
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_oracle_cache_build_matches_reference_kernels(case):
+def test_oracle_cache_build_matches_reference_kernels(case, builder):
+    """the blockwise build against initPayloads_cache_init_kernel ..
+    writeImageBuffer_cache_init_kernel2, the per-ray fill against the
+    payload, compaction and sampling kernels and accumulate_cache_init_*,
+    reserveNewBricks_kernel and writeImageBuffer_cache_init_kernel"""
     from oracle import oracle as orc
 
-    name, seed, nlvl, cam_seed, radius, W, H, variant = case
+    case_name, seed, nlvl, cam_seed, radius, W, H, variant = case
+    name = case_name if builder == "blockwise" else "fill_" + case_name
     g = np.load(GOLDEN)
     om = orc.OracleModel(fmodel.ensure_model(fmodel.spec_tiny(seed=seed, nlvl=nlvl)), use_libm=True)
     cam = fcam.seeded_camera(cam_seed, radius=radius, width=W, height=H)
-    cc = om.cache_build(cam, variant=variant)
+    cc = _build(om, cam, variant, builder)
     d = cc.dims
     assert [d.fW, d.fH, d.fD] == g[f"{name}/frustum"].tolist()
     assert [d.bX, d.bY, d.bZ] == g[f"{name}/bricks"].tolist()
@@ -64,15 +79,16 @@ def test_oracle_cache_build_matches_reference_kernels(case):
     dens = cc.vox_density[vox[isset.reshape(-1)]]
     np.testing.assert_allclose(dens, g[f"{name}/density"], rtol=2e-3, atol=1e-6)
     # the same build on the oracle's own step-grid arithmetic: the same bricks and voxels, known ranges within 2 ulp
-    own = orc.OracleModel(fmodel.ensure_model(fmodel.spec_tiny(seed=seed, nlvl=nlvl))).cache_build(cam, variant=variant)
+    own = _build(orc.OracleModel(fmodel.ensure_model(fmodel.spec_tiny(seed=seed, nlvl=nlvl))), cam, variant, builder)
     np.testing.assert_array_equal(own.packed_index >= 0, ref_set)
     ulp = np.abs(own.known_ranges.view(np.int32).astype(np.int64) - g[f"{name}/known"].reshape(-1).view(np.int32).astype(np.int64))
     assert int(ulp.max()) <= 2
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("builder", BUILDS)
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_device_cache_build_matches_reference_kernels(case):
+def test_device_cache_build_matches_reference_kernels(case, builder):
     """The device's blockwise build against the same golden vectors: which
     bricks hold a slot, the bricks demanded and each brick's set voxels
     exactly; known ranges within 2 ulp (the device's step grid uses
@@ -81,7 +97,8 @@ def test_device_cache_build_matches_reference_kernels(case):
     outputs are the float64 network rounded)."""
     import frustumvolumecaching_gb300 as fvc
 
-    name, seed, nlvl, cam_seed, radius, W, H, variant = case
+    case_name, seed, nlvl, cam_seed, radius, W, H, variant = case
+    name = case_name if builder == "blockwise" else "fill_" + case_name
     g = np.load(GOLDEN)
     loader = fvc.load_data(fmodel.ensure_model(fmodel.spec_tiny(seed=seed, nlvl=nlvl)))
     cam = fcam.seeded_camera(cam_seed, radius=radius, width=W, height=H)
@@ -89,7 +106,12 @@ def test_device_cache_build_matches_reference_kernels(case):
     r = fvc.CachePerformanceRenderer(loader.scene_info, loader.occupancy_grid_morton_bitfield, loader.nerf_network, c0, c1)
     r.resizeCache((W, H), loader.stepsize_info)
     r.setCacheSettings(fvc.default_cache_settings(variant))
-    r.initCacheBlockwise(fvc.raymarch_info(cam, loader.stepsize_info))
+    r.resizeRenderbuffers((W, H))
+    info = fvc.raymarch_info(cam, loader.stepsize_info)
+    if builder == "blockwise":
+        r.initCacheBlockwise(info)
+    else:
+        r.initCache(info)
     packed, known, vox = c1.read()
     ref_set = g[f"{name}/brick_set"].astype(bool)
     np.testing.assert_array_equal(packed.ravel() >= 0, ref_set)
