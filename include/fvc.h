@@ -383,7 +383,8 @@ int fvc_renderer_set_kernel_timing(fvc_renderer *r, int enable);
  * runs on `cuda_stream` (NULL = legacy default stream).  Like fvc_render the
  * call blocks the host: every few sub-iterations it copies the alive-ray
  * count to the host and synchronises the stream, and it returns once the
- * frame has finished marching.  All calls share the scratch:
+ * frame has finished marching, so it cannot be called inside a stream
+ * capture.  All calls share the scratch:
  * calls whose GPU work overlaps race, so serialise them.  The first call on
  * a device looks the scratch address up (cudaGetSymbolAddress); make it
  * before any stream capture on that device. */

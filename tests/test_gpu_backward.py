@@ -277,7 +277,7 @@ def test_autograd_function_wrapper():
     loss = Fn.apply(table, base, head, target, r, loader.nerf_network, info, pixels)
     (3.0 * loss).backward()
     lref, g, pred = _gpu(torch, loader, cam, pix, tgt)
-    assert abs(float(loss) - lref) <= 1e-6 * lref
+    assert abs(float(loss.detach()) - lref) <= 1e-6 * lref
     # a second call of the library: the table gradient is an atomic scatter, so its float sums may differ
     # in the last bits between calls
     for name, t, a in zip(("table", "base", "head"), (table, base, head), g.read()):
